@@ -1,0 +1,207 @@
+/*
+ * lfdm.h — C ABI of the GB300-native batched half-implicit vehicle stepper.
+ *
+ * This is the drop-in boundary for the reference's GPU solver classes
+ *   d18SolverHalfImplicitGPU  (18dof-gpu/dof18_halfImplicit_gpu.cuh:15-343)
+ *   d11SolverHalfImplicitGPU  (11dof-gpu/dof11_halfImplicit_gpu.cuh:16)
+ *   d24SolverHalfImplicitGPU  (24dof-gpu/dof24_halfImplicit_gpu.cuh:15)
+ * The reference has no C ABI: its callers compile against those C++ classes. The header-only
+ * C++ classes in include/lfdm/ keep the reference's class names, overloads and struct field
+ * names and forward every method to the functions below, so an FFI binding (ctypes, cgo, JNI)
+ * binds exactly this file.
+ *
+ * Conventions: every function returns an lfdm_status; on failure lfdm_last_error() returns a
+ * message. All pointers are host pointers unless a name ends in _dev. Sizes are in elements.
+ * One solver handle per host thread; calls on a handle are serialised by the caller. Every
+ * solve call returns after its work (including requested device-to-host copies) has completed.
+ */
+#ifndef LFDM_H
+#define LFDM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------------------------ */
+/* Status codes. The reference prints and continues (utils/utils_gpu.cuh:18-25) or exits       */
+/* (18dof-gpu/dof18_halfImplicit_gpu.cu:502-507); here every failure is a returned code.        */
+typedef enum {
+    LFDM_OK = 0,
+    LFDM_ERR_ARG = 1,      /* bad argument (null pointer, out-of-range index, size mismatch) */
+    LFDM_ERR_IO = 2,       /* file cannot be opened */
+    LFDM_ERR_PARSE = 3,    /* malformed JSON or driver table, missing required key */
+    LFDM_ERR_CUDA = 4,     /* CUDA runtime error (message carries cudaGetErrorString) */
+    LFDM_ERR_STATE = 5,    /* call order violated (e.g. Solve before Construct/Initialize) */
+    LFDM_ERR_CAPACITY = 6, /* more vehicles/classes/map points than the solver was sized for */
+    LFDM_ERR_NUMERIC = 7,  /* a vehicle produced a non-finite state (see lfdm_get_status_words) */
+    LFDM_ERR_NODEVICE = 8  /* no CUDA device / extension not usable */
+} lfdm_status;
+
+typedef enum { LFDM_MODEL_11 = 11, LFDM_MODEL_18 = 18, LFDM_MODEL_24 = 24 } lfdm_model;
+
+/* TireType (18dof-gpu/dof18_gpu.cuh:12) */
+typedef enum { LFDM_TIRE_TMEASY = 0, LFDM_TIRE_TMEASY_NR = 1 } lfdm_tire_type;
+
+/* Arithmetic of the stepper. FP64 reproduces the reference; MIXED runs the RHS and tire math in  */
+/* FP32 and keeps FP64 in the X/Y/yaw accumulation and the low-speed slip normalisation.          */
+typedef enum { LFDM_PREC_FP64 = 0, LFDM_PREC_MIXED = 1 } lfdm_precision;
+
+/* ------------------------------------------------------------------------------------------ */
+/* Flat per-vehicle parameter vector (doubles). Vehicle part follows VehicleParam               */
+/* (18dof-gpu/dof18_gpu.cuh:502-709); tire part is a superset of TMeasyParam (:25-153) and        */
+/* TMeasyNrParam (:263-400). Index names drop the leading underscore of the reference fields.    */
+enum {
+    LFDM_P_A = 0, LFDM_P_B, LFDM_P_H, LFDM_P_M, LFDM_P_JZ, LFDM_P_JX, LFDM_P_JXZ, LFDM_P_CF, LFDM_P_CR,
+    LFDM_P_MUF, LFDM_P_MUR, LFDM_P_HRCF, LFDM_P_HRCR, LFDM_P_KROF, LFDM_P_KROR, LFDM_P_BROF, LFDM_P_BROR,
+    LFDM_P_MAXSTEER, LFDM_P_CRANKINERTIA, LFDM_P_MAXBRAKETORQUE,
+    /* tire block */
+    LFDM_P_JW = 20, LFDM_P_RR, LFDM_P_MU, LFDM_P_R0, LFDM_P_PN, LFDM_P_PNMAX, LFDM_P_CX, LFDM_P_CY, LFDM_P_KT,
+    LFDM_P_DX, LFDM_P_DY, LFDM_P_RDYNCOPN, LFDM_P_RDYNCOP2N, LFDM_P_FZRDYNCO, LFDM_P_RDYNCOCRIT,
+    LFDM_P_DFX0PN, LFDM_P_DFX0P2N, LFDM_P_FXMPN, LFDM_P_FXMP2N, LFDM_P_FXSPN, LFDM_P_FXSP2N, LFDM_P_SXMPN,
+    LFDM_P_SXMP2N, LFDM_P_SXSPN, LFDM_P_SXSP2N, LFDM_P_DFY0PN, LFDM_P_DFY0P2N, LFDM_P_FYMPN, LFDM_P_FYMP2N,
+    LFDM_P_FYSPN, LFDM_P_FYSP2N, LFDM_P_SYMPN, LFDM_P_SYMP2N, LFDM_P_SYSPN, LFDM_P_SYSP2N,
+    /* TMeasyNr-only fields */
+    LFDM_P_WIDTH, LFDM_P_RIM_RADIUS, LFDM_P_VCOULOMB, LFDM_P_FRBLEND_BEGIN, LFDM_P_FRBLEND_END,
+    LFDM_P_BEARINGCAPACITY, LFDM_P_LI, LFDM_P_P_LI, LFDM_P_P_USE,
+    LFDM_P_COUNT /* = 64 */
+};
+
+/* Per-class data shared by all vehicles built from one vehicle JSON: flags, gears and maps.     */
+/* Map x units are those the reference stores after loading (rad/s for engine/shift maps,        */
+/* dof18_gpu.cu:1132-1174). Maps hold at most LFDM_MAX_MAP points, gears LFDM_MAX_GEARS.          */
+#define LFDM_MAX_MAP 32
+#define LFDM_MAX_GEARS 16
+typedef struct {
+    int32_t nonLinearSteer, tcbool, throttleMod, driveType, whichWheels;
+    int32_t noGears, steerMapSize, powertrainMapSize, lossesMapSize, CFmapSize, TRmapSize, pad_;
+    double gearRatios[LFDM_MAX_GEARS];
+    double shiftMap[LFDM_MAX_GEARS][2];       /* [gear] = {downshift, upshift} rad/s */
+    double steerMap[LFDM_MAX_MAP][2];         /* {normalised input, wheel angle} */
+    double powertrainMap[LFDM_MAX_MAP][2];    /* {crank rad/s, torque N m} */
+    double lossesMap[LFDM_MAX_MAP][2];        /* {crank rad/s, loss torque N m} */
+    double CFmap[LFDM_MAX_MAP][2];            /* {speed ratio, capacity factor} */
+    double TRmap[LFDM_MAX_MAP][2];            /* {speed ratio, torque ratio} */
+} lfdm_class18;
+
+/* Flat per-vehicle state vector (doubles), 18-DOF. Field order follows VehicleState            */
+/* (dof18_gpu.cuh:719-810) then 4 x TMeasyState (:164-253) in LF, RF, LR, RR order. current_gr is */
+/* stored as a double holding an integer. TMeasyNr vehicles leave xe, ye, xedot, yedot at 0.      */
+enum {
+    LFDM_S_X = 0, LFDM_S_Y, LFDM_S_U, LFDM_S_V, LFDM_S_PSI, LFDM_S_WZ, LFDM_S_PHI, LFDM_S_WX,
+    LFDM_S_UDOT, LFDM_S_VDOT, LFDM_S_WXDOT, LFDM_S_WZDOT, LFDM_S_CRANKOMEGA, LFDM_S_DOMEGA_CRANK,
+    LFDM_S_CURRENT_GR,
+    LFDM_S_TIRE0 = 15, /* tire k starts at LFDM_S_TIRE0 + k*LFDM_S_TIRE_STRIDE */
+    LFDM_S_TIRE_STRIDE = 15,
+    LFDM_S_COUNT = 75
+};
+enum { /* offsets inside one tire block */
+    LFDM_T_XE = 0, LFDM_T_YE, LFDM_T_XEDOT, LFDM_T_YEDOT, LFDM_T_OMEGA, LFDM_T_DOMEGA, LFDM_T_XT, LFDM_T_RSTAT,
+    LFDM_T_FX, LFDM_T_FY, LFDM_T_FZ, LFDM_T_VSX, LFDM_T_VSY, LFDM_T_MY, LFDM_T_ENGTOR
+};
+
+/* Response channels written every output sample, in this order (dof18_halfImplicit_gpu.cu:954-974): */
+/* time, x, y, u(vx), v(vy), phi(roll), psi(yaw), wx(roll rate), wz(yaw rate), wlf, wrf, wlr, wrr.  */
+#define LFDM18_RESP_CHANNELS 13
+
+/* Driver table row = DriverInput (utils/utils_gpu.cuh:28-41): {time, steering, throttle, braking}. */
+#define LFDM_DRIVER_COLS 4
+
+/* ------------------------------------------------------------------------------------------ */
+typedef struct lfdm_solver lfdm_solver;
+
+/* ctor d18SolverHalfImplicitGPU(unsigned total_num_vehicles) (dof18_halfImplicit_gpu.cu:14-37). */
+/* Device 0 is used, as in the reference (:35-36); lfdm_create_on_device picks another.         */
+int lfdm_create(int model, unsigned total_num_vehicles, lfdm_solver** out);
+int lfdm_create_on_device(int model, unsigned total_num_vehicles, int device, lfdm_solver** out);
+/* ~d18SolverHalfImplicitGPU (:38-50) */
+int lfdm_destroy(lfdm_solver* h);
+/* Message of the last failing call on h (or of the last failing lfdm_create when h is NULL). */
+const char* lfdm_last_error(const lfdm_solver* h);
+
+/* Construct(veh, tire, n, driver[, TireType]) and Construct(veh, tire, n[, TireType])          */
+/* (dof18_halfImplicit_gpu.cu:53-285). sus_json is the 24-DOF suspension file                  */
+/* (24dof-gpu/dof24_halfImplicit_gpu.cu:53-57), NULL otherwise. driver_file may be NULL (vehicles */
+/* then need SolveStep controls). Each call appends n vehicles of one new parameter class.        */
+int lfdm_construct(lfdm_solver* h, const char* veh_json, const char* tire_json, const char* sus_json,
+                   unsigned num_vehicles, const char* driver_file, int tire_type);
+
+/* Extension (replaces writing the reference's public m_sim_data[i] members directly):          */
+/* append n vehicles of a class given as data. params is [n][LFDM_P_COUNT]; the tire block must   */
+/* already hold fzRdynco/rdyncoCrit (tireInit, dof18_gpu.cu:227-241) or lfdm_tire_init fills it.  */
+int lfdm_construct_class(lfdm_solver* h, const lfdm_class18* cls, unsigned num_vehicles, const double* params,
+                         int tire_type);
+/* Overwrite parameters of vehicles [first, first+count), [count][LFDM_P_COUNT]. */
+int lfdm_set_params(lfdm_solver* h, unsigned first, unsigned count, const double* params);
+int lfdm_get_params(lfdm_solver* h, unsigned first, unsigned count, double* params);
+/* tireInit (dof18_gpu.cu:227-241) applied to one flat parameter vector in place. */
+int lfdm_tire_init(double* params);
+
+/* Driver tables. One table shared by vehicles [first, first+count) (rows: [nrows][4]), or one    */
+/* table per vehicle with equal row counts (rows: [count][nrows][4]). Times must be              */
+/* non-decreasing. Replaces the per-vehicle managed copies of dof18_halfImplicit_gpu.cu:84-94.    */
+int lfdm_set_driver_table(lfdm_solver* h, unsigned first, unsigned count, const double* rows, unsigned nrows);
+int lfdm_set_driver_tables(lfdm_solver* h, unsigned first, unsigned count, const double* rows, unsigned nrows);
+
+/* Initialize(VehicleState&, TMeasyState& x4, n) (dof18_halfImplicit_gpu.cu:290-313): copy one    */
+/* flat state [LFDM_S_COUNT] to the next n vehicles.                                              */
+int lfdm_initialize(lfdm_solver* h, const double* state, unsigned num_vehicles);
+/* Per-vehicle states [count][LFDM_S_COUNT] (extension; GetSimState reads one, :667-682). */
+int lfdm_set_states(lfdm_solver* h, unsigned first, unsigned count, const double* states);
+int lfdm_get_states(lfdm_solver* h, unsigned first, unsigned count, double* states);
+
+/* Setters of dof18_halfImplicit_gpu.cuh:93-110. */
+int lfdm_set_time_step(lfdm_solver* h, double step);
+int lfdm_set_end_time(lfdm_solver* h, double tend);
+int lfdm_set_kernel_sim_time(lfdm_solver* h, double time);
+int lfdm_set_host_dump_time(lfdm_solver* h, double time);
+int lfdm_set_threads_per_block(lfdm_solver* h, unsigned threads);
+int lfdm_get_step(lfdm_solver* h, double* step);
+int lfdm_get_end_time(lfdm_solver* h, double* tend);
+int lfdm_get_tire_type(lfdm_solver* h, int* tire_type);
+int lfdm_get_num_vehicles(lfdm_solver* h, unsigned* total, unsigned* constructed, unsigned* initialized);
+/* Extension: arithmetic of the stepper (default LFDM_PREC_FP64). */
+int lfdm_set_precision(lfdm_solver* h, int precision);
+
+/* SetOutput(file, freq, store_all=false, no_outs=50) (dof18_halfImplicit_gpu.cu:342-399):       */
+/* per-vehicle CSV files <file>_<idx>.csv written by Solve, byte-compatible with the reference.   */
+int lfdm_set_output(lfdm_solver* h, const char* output_file, double output_freq, int store_all,
+                    unsigned no_outs);
+/* Extension: stream the SoA response [sample][channels][N] of Solve into caller memory instead  */
+/* of (or as well as) CSV files. dst holds capacity doubles; Solve fails with LFDM_ERR_CAPACITY   */
+/* when the run needs more. Page-locked dst (cudaHostRegister'ed by lfdm_register_host) lets the  */
+/* copies overlap the next window's compute. Sample k (k >= 1) is the state at t = k/output_freq.  */
+int lfdm_set_response_buffer(lfdm_solver* h, double* dst, size_t capacity, double output_freq);
+int lfdm_response_samples(lfdm_solver* h, size_t* samples_written);
+int lfdm_register_host(void* ptr, size_t bytes);
+int lfdm_unregister_host(void* ptr);
+
+/* Solve() (dof18_halfImplicit_gpu.cu:404-494): integrate all vehicles from t = 0 to end time in */
+/* windows of kernel_sim_time.                                                                     */
+int lfdm_solve(lfdm_solver* h);
+/* SolveStep(t, steering, throttle, braking) (:497-550): one window with constant controls;       */
+/* *t_out receives t + kernel_sim_time.                                                            */
+int lfdm_solve_step(lfdm_solver* h, double t, double steering, double throttle, double braking, double* t_out);
+/* Extension: one window with per-vehicle constant controls, arrays of total_num_vehicles.        */
+int lfdm_solve_step_controls(lfdm_solver* h, double t, const double* steering, const double* throttle,
+                             const double* braking, double* t_out);
+
+/* GetSimState(i) (dof18_halfImplicit_gpu.cu:667-682) as a flat state vector. */
+int lfdm_get_sim_state(lfdm_solver* h, unsigned vehicle_index, double* state);
+
+/* Per-vehicle status words after the last solve: bit 0 = non-finite state seen. */
+int lfdm_get_status_words(lfdm_solver* h, unsigned first, unsigned count, uint32_t* words);
+
+/* Device time in milliseconds of the last lfdm_solve / lfdm_solve_step* call's stepping kernels  */
+/* (CUDA events on the solver's stream), and how many stepping kernels it launched.               */
+int lfdm_last_kernel_ms(lfdm_solver* h, double* ms, unsigned* launches);
+
+/* Library build information (arch, version). */
+const char* lfdm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LFDM_H */

@@ -1,0 +1,136 @@
+"""Seeded synthetic fleets (parameter jitter, driver-input families, initial states).
+
+These stand in for the reference's JSON/driver-file fixtures at fleet scale. The vehicle is a
+mid-size SUV: mass 2,100 kg, Jz 3,500 kg m^2, CG 1.6 m behind the front axle and 1.7 m ahead of
+the rear axle, track 1.8 m, CG height 0.7 m, wheel radius 0.47 m, wheel inertia 1.5 kg m^2, a
+6-point engine torque map peaking at 500 N m near 300 rad/s, a torque converter with 10-point
+capacity-factor and torque-ratio tables, and TMeasy tires with vertical stiffness 2e5 N/m whose
+force curves peak at 1.0*Fz at slip 0.1 and slide at 0.8*Fz from slip 0.5. Fields the
+description leaves open are chosen here and listed in SUV18_VEHICLE / SUV_TIRE.
+
+Driver families (per vehicle, seeded): steering wheel angle A*sin(2*pi*f*t) with
+A ~ U[0, 0.5] rad and f ~ U[0.2, 1] Hz, given to the model as the normalised input
+A/maxSteer*sin(...); throttle ramping linearly from 0 to U[0.3, 1] over 2 s; optionally a brake
+pulse of 0.6 for 1 s starting at U[4, 8] s, during which the throttle is released. Tables are
+sampled every `table_dt` seconds (rows {t, steering, throttle, braking}).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from ._abi import Class18, P, P_COUNT, S, S_COUNT, S_TIRE0, S_TIRE_STRIDE, T, TIRE_TMEASY
+from .params import vehicle_from_json
+
+SUV18_VEHICLE = {
+    "a": 1.6, "b": 1.7, "m": 2100.0, "h": 0.7, "jz": 3500.0, "jx": 900.0, "jxz": 3.0,
+    "cf": 1.8, "cr": 1.8, "muf": 100.0, "mur": 100.0, "hrcf": 0.35, "hrcr": 0.32,
+    "krof": 40000.0, "kror": 40000.0, "brof": 3500.0, "bror": 3500.0,
+    "nonLinearSteer": False, "maxSteer": 0.6, "crankInertia": 0.8,
+    "upshiftRPM": 4000.0, "downshiftRPM": 1800.0,
+    "gearRatios": [0.05, 0.09, 0.14, 0.2],
+    # 6 points (RPM, N m): peak 500 N m at 2865 RPM = 300 rad/s
+    "torqueMap": [[-100.0, 300.0], [1000.0, 420.0], [2000.0, 480.0], [2865.0, 500.0], [4000.0, 430.0],
+                  [5000.0, -300.0]],
+    "lossesMap": [[-50.0, 20.0], [0.0, 0.0], [50.0, -20.0], [1000.0, -35.0], [2000.0, -50.0], [3000.0, -65.0]],
+    "tcBool": True,
+    "capacityFactorMap": [[0.0, 15.0], [0.1, 15.0], [0.2, 15.0], [0.3, 15.2], [0.4, 15.5], [0.5, 16.0],
+                          [0.6, 16.5], [0.7, 17.5], [0.85, 20.0], [1.0, 35.0]],
+    "torqueRatioMap": [[0.0, 2.2], [0.1, 2.05], [0.2, 1.9], [0.3, 1.75], [0.4, 1.6], [0.5, 1.45],
+                       [0.6, 1.3], [0.7, 1.15], [0.85, 1.05], [1.0, 1.0]],
+    "maxBrakeTorque": 4000.0, "throttleMod": False, "4wd": True, "rearWheels": True,
+}
+_PN = 5150.0  # nominal tire load ~ m*g/4
+SUV_TIRE = {
+    "jw": 1.5, "rr": 0.015, "r0": 0.47, "pn": _PN, "pnmax": 3.0 * _PN, "cx": 185000.0, "cy": 165000.0,
+    "kt": 2.0e5, "dx": 3700.0, "dy": 3500.0, "rdyncoPn": 0.375, "rdyncoP2n": 0.75, "fzRdynco": 0.0,
+    "rdyncoCrit": 0.0,
+    "dfx0Pn": 25.0 * _PN, "dfx0P2n": 45.0 * _PN, "fxmPn": 1.0 * _PN, "fxmP2n": 2.0 * _PN,
+    "fxsPn": 0.8 * _PN, "fxsP2n": 1.6 * _PN, "sxmPn": 0.1, "sxmP2n": 0.1, "sxsPn": 0.5, "sxsP2n": 0.5,
+    "dfy0Pn": 22.0 * _PN, "dfy0P2n": 40.0 * _PN, "fymPn": 1.0 * _PN, "fymP2n": 2.0 * _PN,
+    "fysPn": 0.8 * _PN, "fysP2n": 1.6 * _PN, "symPn": 0.1, "symP2n": 0.1, "sysPn": 0.5, "sysP2n": 0.5,
+}
+FRICTION_FIELDS = ("fxmpn", "fxmp2n", "fxspn", "fxsp2n", "fympn", "fymp2n", "fyspn", "fysp2n")
+WHEELBASE = SUV18_VEHICLE["a"] + SUV18_VEHICLE["b"]
+
+
+def suv18() -> tuple[Class18, np.ndarray]:
+    return vehicle_from_json(SUV18_VEHICLE, SUV_TIRE, TIRE_TMEASY)
+
+
+def jitter_params(base: np.ndarray, n: int, rng: np.random.Generator, frac: float = 0.1) -> np.ndarray:
+    """Per-vehicle copies of `base` with mass, Jz, CG position (a; b = wheelbase - a), tire vertical
+    stiffness and peak-friction scale drawn uniformly within +/-frac of the base values. The
+    friction scale multiplies the TMeasy peak and sliding forces (fxm*, fym*, fxs*, fys*)."""
+    p = np.repeat(base[None, :], n, axis=0)
+    u = lambda: rng.uniform(1.0 - frac, 1.0 + frac, size=n)  # noqa: E731
+    p[:, P["m"]] *= u()
+    p[:, P["jz"]] *= u()
+    wb = base[P["a"]] + base[P["b"]]
+    p[:, P["a"]] *= u()
+    p[:, P["b"]] = wb - p[:, P["a"]]
+    p[:, P["kt"]] *= u()
+    mu = u()
+    for f in FRICTION_FIELDS:
+        p[:, P[f]] *= mu
+    return p
+
+
+def driver_tables(n: int, rng: np.random.Generator, horizon: float, table_dt: float = 0.01,
+                  max_steer: np.ndarray | float = 0.6, brake_pulse: bool = True,
+                  dtype=np.float64) -> np.ndarray:
+    """[n][rows][4] tables {t, steering, throttle, braking}, rows = horizon/table_dt + 1."""
+    rows = int(round(horizon / table_dt)) + 1
+    t = (np.arange(rows, dtype=np.float64) / round(1.0 / table_dt)) if abs(1.0 / table_dt - round(1.0 / table_dt)) < 1e-9 \
+        else np.arange(rows, dtype=np.float64) * table_dt
+    A = rng.uniform(0.0, 0.5, size=n)
+    f = rng.uniform(0.2, 1.0, size=n)
+    thr = rng.uniform(0.3, 1.0, size=n)
+    out = np.empty((n, rows, 4), dtype=dtype)
+    out[:, :, 0] = t[None, :]
+    ms = np.broadcast_to(np.asarray(max_steer, dtype=np.float64), (n,))
+    out[:, :, 1] = (A / ms)[:, None] * np.sin(2.0 * math.pi * f[:, None] * t[None, :])
+    out[:, :, 2] = thr[:, None] * np.minimum(t[None, :] / 2.0, 1.0)
+    out[:, :, 3] = 0.0
+    if brake_pulse:
+        tb = rng.uniform(4.0, 8.0, size=n)
+        on = (t[None, :] >= tb[:, None]) & (t[None, :] < tb[:, None] + 1.0)
+        out[:, :, 3] = np.where(on, 0.6, 0.0)
+        out[:, :, 2] = np.where(on, 0.0, out[:, :, 2])
+    return out
+
+
+def initial_states(cls: Class18, params: np.ndarray, rng: np.random.Generator,
+                   u0_range=(0.0, 20.0)) -> np.ndarray:
+    """[n][S_COUNT] states at rest pose moving straight at u0 ~ U[u0_range]. Every wheel spins at
+    omega = u0 / r0; the gear is the lowest one whose crank speed omega/ratio is below the upshift
+    speed, and the crank spins at that speed (converter locked)."""
+    n = params.shape[0]
+    u0 = rng.uniform(u0_range[0], u0_range[1], size=n)
+    s = np.zeros((n, S_COUNT), dtype=np.float64)
+    s[:, S["u"]] = u0
+    w = u0 / params[:, P["r0"]]
+    for k in range(4):
+        s[:, S_TIRE0 + k * S_TIRE_STRIDE + T["omega"]] = w
+    gears = np.array([cls.gearRatios[i] for i in range(cls.noGears)])
+    ups = np.array([cls.shiftMap[i][1] for i in range(cls.noGears)])
+    crank = w[:, None] / gears[None, :]
+    ok = crank < ups[None, :]
+    gear = np.where(ok.any(axis=1), ok.argmax(axis=1), cls.noGears - 1)
+    s[:, S["current_gr"]] = gear
+    s[:, S["crankomega"]] = w / gears[gear]
+    return s
+
+
+def fleet18(n: int, seed: int = 20261203, horizon: float = 10.0, table_dt: float = 0.01,
+            brake_pulse: bool = True, jitter: bool = True, u0_range=(0.0, 20.0)) -> dict:
+    """The seeded 18-DOF SUV fleet: one class, jittered parameters, per-vehicle driver tables and
+    initial states. Returns dict(cls=[Class18], class_of, params, tables, states)."""
+    rng = np.random.default_rng(seed)
+    cls, base = suv18()
+    params = jitter_params(base, n, rng) if jitter else np.repeat(base[None, :], n, axis=0)
+    tables = driver_tables(n, rng, horizon, table_dt, params[:, P["maxsteer"]], brake_pulse)
+    states = initial_states(cls, params, rng, u0_range)
+    return {"cls": [cls], "class_of": np.zeros(n, dtype=np.int32), "params": params, "tables": tables,
+            "states": states, "seed": seed, "horizon": horizon}

@@ -1,0 +1,696 @@
+/*
+ * ORACLE — test infrastructure only (see lfdm_oracle.h). Never linked into the product.
+ *
+ * Plain-C FP64 restatement of the reference's 18-DOF half-implicit stepper. Each function keeps
+ * the reference's expression order and parenthesisation so that, compiled without FMA
+ * contraction, it reproduces the reference CPU solver bit for bit (checked against
+ * tests/golden/). Reference files cited by path inside wheeled_vehicle_models/.
+ */
+#define _GNU_SOURCE
+#include "lfdm_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+static const double C_PI = 3.141592653589793238462643383279;
+static const double C_2PI = 6.283185307179586476925286766559;
+static const double G = 9.81;
+
+/* ---------------------------------------------------------------------------------------------- */
+/* utils (utils/utils_gpu.cuh, utils/utils_gpu.cu)                                                */
+
+/* InterpL, InterpQ: utils_gpu.cuh:86-93 */
+static double InterpL(double fz, double w1, double w2, double pn) { return w1 + (w2 - w1) * (fz / pn - 1.); }
+static double InterpQ(double fz, double w1, double w2, double pn) {
+    return (fz / pn) * (2. * w1 - 0.5 * w2 - (w1 - 0.5 * w2) * (fz / pn));
+}
+/* sgn: utils_gpu.cuh:96-99 */
+static int sgn(double v) { return (0. < v) - (v < 0.); }
+/* clamp: utils_gpu.cuh:104-111 */
+static double clampd(double v, double lo, double hi) {
+    if (v < lo) return lo;
+    if (v > hi) return hi;
+    return v;
+}
+/* sineStep: utils_gpu.cu:78-88 */
+static double sineStep(double x, double x1, double y1, double x2, double y2) {
+    if (x <= x1) return y1;
+    if (x >= x2) return y2;
+    double dx = x2 - x1;
+    double dy = y2 - y1;
+    double y = y1 + dy * (x - x1) / dx - (dy / C_2PI) * sin(C_2PI * (x - x1) / dx);
+    return y;
+}
+/* lower_bound over {x, y} pairs keyed on x: utils_gpu.cu:109-121 (std::lower_bound on CPU) */
+static int lower_bound_key(const double* a, int n, int stride, double x) {
+    int l = 0, h = n;
+    while (l < h) {
+        int mid = l + (h - l) / 2;
+        if (x <= a[(size_t)mid * stride]) h = mid;
+        else l = mid + 1;
+    }
+    return l;
+}
+/* getMapY: utils_gpu.cu:60-75 */
+double oracle_map_y(const double* map, int n, double x) {
+    if (x <= map[0]) return map[1];
+    else if (x >= map[2 * (n - 1)]) return map[2 * (n - 1) + 1];
+    int right = lower_bound_key(map, n, 2, x);
+    int left = right - 1;
+    double mbar = (x - map[2 * left]) / (map[2 * right] - map[2 * left]);
+    return (map[2 * left + 1] + mbar * (map[2 * right + 1] - map[2 * left + 1]));
+}
+/* GetDriverInput: utils_gpu.cu:34-56; out = {time, steering, throttle, braking} */
+void oracle_driver_input(double t, const double* d, int len, double* out) {
+    if (t <= d[0]) {
+        memcpy(out, d, 4 * sizeof(double));
+    } else if (t >= d[4 * (len - 1)]) {
+        memcpy(out, d + 4 * (len - 1), 4 * sizeof(double));
+    } else {
+        int right = lower_bound_key(d, len, 4, t);
+        int left = right - 1;
+        const double* L = d + 4 * left;
+        const double* R = d + 4 * right;
+        double tbar = (t - L[0]) / (R[0] - L[0]);
+        out[0] = t;
+        out[1] = L[1] + tbar * (R[1] - L[1]);
+        out[2] = L[2] + tbar * (R[2] - L[2]);
+        out[3] = L[3] + tbar * (R[3] - L[3]);
+    }
+}
+
+/* ---------------------------------------------------------------------------------------------- */
+/* state views                                                                                     */
+typedef struct {
+    double xe, ye, xedot, yedot, omega, dOmega, xt, rStat, fx, fy, fz, vsx, vsy, My, engTor;
+} Tire;
+typedef struct {
+    double x, y, u, v, psi, wz, phi, wx, udot, vdot, wxdot, wzdot, crankOmega, dOmega_crank;
+    int current_gr;
+} Veh;
+typedef struct {
+    const double* p;        /* flat params */
+    const lfdm_class18* c;  /* class */
+} Par;
+
+#define P(i) (pp->p[(i)])
+
+static void tire_init(double* p) {
+    /* tireInit: 18dof-gpu/dof18_gpu.cu:227-233 */
+    p[LFDM_P_FZRDYNCO] = (p[LFDM_P_PN] * (p[LFDM_P_RDYNCOP2N] - 2.0 * p[LFDM_P_RDYNCOPN] + 1.)) /
+                         (2. * (p[LFDM_P_RDYNCOP2N] - p[LFDM_P_RDYNCOPN]));
+    p[LFDM_P_RDYNCOCRIT] = InterpL(p[LFDM_P_FZRDYNCO], p[LFDM_P_RDYNCOPN], p[LFDM_P_RDYNCOP2N], p[LFDM_P_PN]);
+}
+void oracle_tire_init(double* params) { tire_init(params); }
+
+/* steering input -> wheel angle: the head of vehToTireTransform etc. (dof18_gpu.cu:79-87) */
+static double wheel_angle(const Par* pp, double steering) {
+    if (pp->c->nonLinearSteer) return oracle_map_y(&pp->c->steerMap[0][0], pp->c->steerMapSize, steering);
+    return steering * P(LFDM_P_MAXSTEER);
+}
+
+/* driveTorque: dof18_gpu.cu:15-38. throttleMod scales a private copy of the map, as the CPU     */
+/* solver does (18dof/dof18.cpp:23-29); the GPU solver scales the shared map in place.           */
+static double driveTorque(const Par* pp, double throttle, double motor_speed) {
+    double motor_torque = 0.;
+    const lfdm_class18* c = pp->c;
+    if (c->throttleMod) {
+        double m[LFDM_MAX_MAP][2];
+        int len = c->powertrainMapSize;
+        for (int i = 0; i < len; i++) {
+            m[i][0] = c->powertrainMap[i][0] * throttle;
+            m[i][1] = c->powertrainMap[i][1] * throttle;
+        }
+        motor_torque = oracle_map_y(&m[0][0], len, motor_speed);
+        double motor_losses = oracle_map_y(&c->lossesMap[0][0], c->lossesMapSize, motor_speed);
+        motor_torque = motor_torque + motor_losses;
+    } else {
+        motor_torque = oracle_map_y(&c->powertrainMap[0][0], c->powertrainMapSize, motor_speed);
+        double motor_losses = oracle_map_y(&c->lossesMap[0][0], c->lossesMapSize, motor_speed);
+        motor_torque = motor_torque * throttle + motor_losses;
+    }
+    return motor_torque;
+}
+
+/* differentialSplit: dof18_gpu.cu:42-69 */
+static void differentialSplit(double torque, double max_bias, double speed_left, double speed_right,
+                              double* torque_left, double* torque_right) {
+    double diff = fabs(speed_left - speed_right);
+    double bias = 1;
+    if (diff > 0.5) bias = max_bias;
+    else if (diff > 0.25) bias = 4 * (max_bias - 1) * diff + (2 - max_bias);
+    double alpha = bias / (1 + bias);
+    double slow = alpha * torque;
+    double fast = torque - slow;
+    if (fabs(speed_left) < fabs(speed_right)) {
+        *torque_left = slow;
+        *torque_right = fast;
+    } else {
+        *torque_left = fast;
+        *torque_right = slow;
+    }
+}
+
+/* vehToTireTransform: dof18_gpu.cu:71-109 */
+static void vehToTireTransform(Tire* t, const Veh* v, const double* loads, const Par* pp, double steering) {
+    double delta = wheel_angle(pp, steering);
+    t[0].fz = loads[0];
+    t[0].vsy = v->v + v->wz * P(LFDM_P_A);
+    t[0].vsx = (v->u - (v->wz * P(LFDM_P_CF)) / 2.) * cos(delta) + t[0].vsy * sin(delta);
+    t[1].fz = loads[1];
+    t[1].vsy = v->v + v->wz * P(LFDM_P_A);
+    t[1].vsx = (v->u + (v->wz * P(LFDM_P_CF)) / 2.) * cos(delta) + t[1].vsy * sin(delta);
+    t[2].fz = loads[2];
+    t[2].vsy = v->v - v->wz * P(LFDM_P_B);
+    t[2].vsx = v->u - (v->wz * P(LFDM_P_CR)) / 2.;
+    t[3].fz = loads[3];
+    t[3].vsy = v->v - v->wz * P(LFDM_P_B);
+    t[3].vsx = v->u + (v->wz * P(LFDM_P_CR)) / 2.;
+}
+
+/* tireToVehTransform: dof18_gpu.cu:152-185 (front tires rotated by the wheel angle) */
+static void tireToVehTransform(Tire* t, const Par* pp, double steering) {
+    double delta = wheel_angle(pp, steering);
+    for (int k = 0; k < 2; ++k) {
+        double fx = t[k].fx * cos(delta) - t[k].fy * sin(delta);
+        double fy = t[k].fx * sin(delta) + t[k].fy * cos(delta);
+        t[k].fx = fx;
+        t[k].fy = fy;
+    }
+}
+
+/* tmxy_combined: dof18_gpu.cu:243-285 */
+static void tmxy_combined(double* f, double* fos, double s, double df0, double sm, double fm, double ss, double fs) {
+    double df0loc = 0.0;
+    if (sm > 0.0) df0loc = fmax(2.0 * fm / sm, df0);
+    if (s > 0.0 && df0loc > 0.0) {
+        if (s > ss) {
+            *f = fs;
+            *fos = *f / s;
+        } else {
+            if (s < sm) {
+                double p = df0loc * sm / fm - 2.0;
+                double sn = s / sm;
+                double dn = 1.0 + (sn + p) * sn;
+                *f = df0loc * sm * sn / dn;
+                *fos = df0loc / dn;
+            } else {
+                double a = pow(fm / sm, 2.0) / (df0loc * sm);
+                double sstar = sm + (fm - fs) / (a * (ss - sm));
+                if (sstar <= ss) {
+                    if (s <= sstar) {
+                        *f = fm - a * (s - sm) * (s - sm);
+                    } else {
+                        double b = a * (sstar - sm) / (ss - sstar);
+                        *f = fs + b * (ss - s) * (ss - s);
+                    }
+                } else {
+                    double sn = (s - sm) / (ss - sm);
+                    *f = fm - (fm - fs) * sn * sn * (3.0 - 2.0 * sn);
+                }
+                *fos = *f / s;
+            }
+        }
+    } else {
+        *f = 0.0;
+        *fos = 0.0;
+    }
+}
+
+/* computeCombinedCoulombForce: dof18_gpu.cu:287-303 */
+static void coulomb(double* fx, double* fy, double mu, double vsx, double vsy, double fz, double vcoulomb) {
+    *fx = tanh(-2.0 * vsx / vcoulomb) * fz * mu;
+    *fy = tanh(-2.0 * vsy / vcoulomb) * fz * mu;
+    if (hypot(*fx, *fy) > fz * mu) {
+        double f = fz * mu / hypot(*fx, *fy);
+        *fx *= f;
+        *fy *= f;
+    }
+}
+
+/* computeTireLoads: dof18_gpu.cu:305-340 (identical for both tire types) */
+static void computeTireLoads(double* loads, const Veh* v, const Par* pp) {
+    double huf = P(LFDM_P_R0);
+    double hur = P(LFDM_P_R0);
+    const double a = P(LFDM_P_A), b = P(LFDM_P_B), m = P(LFDM_P_M), h = P(LFDM_P_H);
+    const double muf = P(LFDM_P_MUF), mur = P(LFDM_P_MUR), cf = P(LFDM_P_CF), cr = P(LFDM_P_CR);
+    double Z1 = (m * G * b) / (2. * (a + b)) + (muf * G) / 2.;
+    double Z2 = ((muf * huf) / cf + m * b * (h - P(LFDM_P_HRCF)) / (cf * (a + b))) * (v->vdot + v->wz * v->u);
+    double Z3 = (P(LFDM_P_KROF) * v->phi + P(LFDM_P_BROF) * v->wx) / cf;
+    double Z4 = ((m * h + muf * huf + mur * hur) * (v->udot - v->wz * v->v)) / (2. * (a + b));
+    loads[0] = (Z1 - Z2 - Z3 - Z4) > 0. ? (Z1 - Z2 - Z3 - Z4) : 0.;
+    loads[1] = (Z1 + Z2 + Z3 - Z4) > 0. ? (Z1 + Z2 + Z3 - Z4) : 0.;
+    Z1 = (m * G * a) / (2. * (a + b)) + (mur * G) / 2.;
+    Z2 = ((mur * hur) / cr + m * a * (h - P(LFDM_P_HRCR)) / (cr * (a + b))) * (v->vdot + v->wz * v->u);
+    Z3 = (P(LFDM_P_KROR) * v->phi + P(LFDM_P_BROR) * v->wx) / cr;
+    loads[2] = (Z1 - Z2 - Z3 + Z4) > 0. ? (Z1 - Z2 - Z3 + Z4) : 0.;
+    loads[3] = (Z1 + Z2 + Z3 + Z4) > 0. ? (Z1 + Z2 + Z3 + Z4) : 0.;
+}
+
+/* computeTireRHS, TMeasy: dof18_gpu.cu:379-530 */
+static void tireRHS_TM(Tire* ts, const Par* pp, double steering) {
+    double delta = wheel_angle(pp, steering);
+    double fz = ts->fz;
+    double vsy = ts->vsy;
+    double vsx = ts->vsx;
+    if (fz <= 0) {
+        ts->xe = 0;
+        ts->ye = 0;
+        ts->omega = 0;
+        ts->xt = 0;
+        ts->rStat = P(LFDM_P_R0);
+        ts->fx = 0;
+        ts->fy = 0;
+        ts->My = 0;
+        return;
+    }
+    const double pn = P(LFDM_P_PN), r0 = P(LFDM_P_R0);
+    ts->xt = fz / P(LFDM_P_KT);
+    ts->rStat = r0 - ts->xt;
+    double r_eff, rdynco;
+    if (fz <= P(LFDM_P_FZRDYNCO)) {
+        rdynco = InterpL(fz, P(LFDM_P_RDYNCOPN), P(LFDM_P_RDYNCOP2N), pn);
+        r_eff = rdynco * r0 + (1. - rdynco) * ts->rStat;
+    } else {
+        rdynco = P(LFDM_P_RDYNCOCRIT);
+        r_eff = rdynco * r0 + (1. - rdynco) * ts->rStat;
+    }
+    vsx = vsx - (ts->omega * r_eff);
+    double vta = r_eff * fabs(ts->omega) + 0.01;
+    double sx = -vsx / vta;
+    double alpha = atan2(vsy, vta) - delta;
+    double sy = -tan(alpha);
+    if (fz > P(LFDM_P_PNMAX)) fz = P(LFDM_P_PNMAX);
+    double dfx0 = InterpQ(fz, P(LFDM_P_DFX0PN), P(LFDM_P_DFX0P2N), pn);
+    double dfy0 = InterpQ(fz, P(LFDM_P_DFY0PN), P(LFDM_P_DFY0P2N), pn);
+    double fxm = InterpQ(fz, P(LFDM_P_FXMPN), P(LFDM_P_FXMP2N), pn);
+    double fym = InterpQ(fz, P(LFDM_P_FYMPN), P(LFDM_P_FYMP2N), pn);
+    double fxs = InterpQ(fz, P(LFDM_P_FXSPN), P(LFDM_P_FXSP2N), pn);
+    double fys = InterpQ(fz, P(LFDM_P_FYSPN), P(LFDM_P_FYSP2N), pn);
+    double sxm = InterpL(fz, P(LFDM_P_SXMPN), P(LFDM_P_SXMP2N), pn);
+    double sym = InterpL(fz, P(LFDM_P_SYMPN), P(LFDM_P_SYMP2N), pn);
+    double sxs = InterpL(fz, P(LFDM_P_SXSPN), P(LFDM_P_SXSP2N), pn);
+    double sys = InterpL(fz, P(LFDM_P_SYSPN), P(LFDM_P_SYSP2N), pn);
+    double hsxn = sxm / (sxm + sym) + (fxm / dfx0) / (fxm / dfx0 + fym / dfy0);
+    double hsyn = sym / (sxm + sym) + (fym / dfy0) / (fxm / dfx0 + fym / dfy0);
+    double sxn = sx / hsxn;
+    double syn = sy / hsyn;
+    double sc = hypot(sxn, syn);
+    double calpha, salpha;
+    if (sc > 0) {
+        calpha = sxn / sc;
+        salpha = syn / sc;
+    } else {
+        calpha = sqrt(2.) / 2.;
+        salpha = sqrt(2.) / 2.;
+    }
+    double df0 = hypot(dfx0 * calpha * hsxn, dfy0 * salpha * hsyn);
+    double fm = hypot(fxm * calpha, fym * salpha);
+    double sm = hypot(sxm * calpha / hsxn, sym * salpha / hsyn);
+    double fs = hypot(fxs * calpha, fys * salpha);
+    double ss = hypot(sxs * calpha / hsxn, sys * salpha / hsyn);
+    double f, fos;
+    tmxy_combined(&f, &fos, sc, df0, sm, fm, ss, fs);
+    /* rolling resistance; sineStep(vta, 0, 0, 0, 1) with vx_min = vx_max = 0 */
+    double vx_min = 0., vx_max = 0.;
+    ts->My = -sineStep(vta, vx_min, 0., vx_max, 1.) * P(LFDM_P_RR) * fz * ts->rStat * sgn(ts->omega);
+    double vtxs = r_eff * fabs(ts->omega) * hsxn + 0.01;
+    double vtys = r_eff * fabs(ts->omega) * hsyn + 0.01;
+    const double cx = P(LFDM_P_CX), cy = P(LFDM_P_CY), dx = P(LFDM_P_DX), dy = P(LFDM_P_DY);
+    ts->xedot = (-vtxs * cx * ts->xe - fos * vsx) / (vtxs * dx + fos);
+    ts->yedot = (-vtys * cy * ts->ye - fos * (-sy * vta)) / (vtys * dy + fos);
+    double fxdyn = dx * (-vtxs * cx * ts->xe - fos * vsx) / (vtxs * dx + fos) + cx * ts->xe;
+    double fydyn = dy * ((-vtys * cy * ts->ye - fos * (-sy * vta)) / (vtys * dy + fos)) + (cy * ts->ye);
+    double fxstr = clampd(ts->xe * cx + ts->xedot * dx, -P(LFDM_P_FXMP2N), P(LFDM_P_FXMP2N));
+    double fystr = clampd(ts->ye * cy + ts->yedot * dy, -P(LFDM_P_FYMP2N), P(LFDM_P_FYMP2N));
+    double weightx = sineStep(fabs(vsx), 1., 1., 1.5, 0.);
+    double weighty = sineStep(fabs(-sy * vta), 1., 1., 1.5, 0.);
+    ts->fx = weightx * fxstr + (1. - weightx) * fxdyn;
+    ts->fy = weighty * fystr + (1. - weighty) * fydyn;
+}
+
+/* computeTireRHS, TMeasyNr: dof18_gpu.cu:532-662 */
+static void tireRHS_Nr(Tire* ts, const Par* pp, double steering) {
+    double delta = wheel_angle(pp, steering);
+    double fz = ts->fz;
+    double vsy = ts->vsy;
+    double vsx = ts->vsx;
+    if (fz <= 0) {
+        ts->omega = 0;
+        ts->xt = 0;
+        ts->rStat = P(LFDM_P_R0);
+        ts->fx = 0;
+        ts->fy = 0;
+        ts->My = 0;
+        return;
+    }
+    const double pn = P(LFDM_P_PN), r0 = P(LFDM_P_R0), mu = P(LFDM_P_MU);
+    ts->xt = fz / P(LFDM_P_KT);
+    ts->rStat = r0 - ts->xt;
+    double r_eff, rdynco;
+    if (fz <= P(LFDM_P_FZRDYNCO)) {
+        rdynco = InterpL(fz, P(LFDM_P_RDYNCOPN), P(LFDM_P_RDYNCOP2N), pn);
+        r_eff = rdynco * r0 + (1. - rdynco) * ts->rStat;
+    } else {
+        rdynco = P(LFDM_P_RDYNCOCRIT);
+        r_eff = rdynco * r0 + (1. - rdynco) * ts->rStat;
+    }
+    vsx = vsx - (ts->omega * r_eff);
+    double vta = r_eff * fabs(ts->omega) + 0.01;
+    double Fx0 = 0, Fy0 = 0;
+    coulomb(&Fx0, &Fy0, mu, vsx, vsy, fz, P(LFDM_P_VCOULOMB));
+    double sx = -vsx / vta;
+    double alpha = atan2(vsy, vta) - delta;
+    double sy = -tan(alpha);
+    if (fz > P(LFDM_P_PNMAX)) fz = P(LFDM_P_PNMAX);
+    double dfx0 = InterpQ(fz, P(LFDM_P_DFX0PN), P(LFDM_P_DFX0P2N), pn);
+    double dfy0 = InterpQ(fz, P(LFDM_P_DFY0PN), P(LFDM_P_DFY0P2N), pn);
+    double fxm = InterpQ(fz, P(LFDM_P_FXMPN), P(LFDM_P_FXMP2N), pn);
+    double fym = InterpQ(fz, P(LFDM_P_FYMPN), P(LFDM_P_FYMP2N), pn);
+    double fxs = InterpQ(fz, P(LFDM_P_FXSPN), P(LFDM_P_FXSP2N), pn);
+    double fys = InterpQ(fz, P(LFDM_P_FYSPN), P(LFDM_P_FYSP2N), pn);
+    double sxm = InterpL(fz, P(LFDM_P_SXMPN), P(LFDM_P_SXMP2N), pn);
+    double sym = InterpL(fz, P(LFDM_P_SYMPN), P(LFDM_P_SYMP2N), pn);
+    double sxs = InterpL(fz, P(LFDM_P_SXSPN), P(LFDM_P_SXSP2N), pn);
+    double sys = InterpL(fz, P(LFDM_P_SYSPN), P(LFDM_P_SYSP2N), pn);
+    double frblend = sineStep(fabs(ts->vsx), P(LFDM_P_FRBLEND_BEGIN), 0., P(LFDM_P_FRBLEND_END), 1.);
+    double sc = hypot(sx, sy);
+    double salpha = 0, calpha = 0;
+    if (sc > 0) {
+        calpha = sx / sc;
+        salpha = sy / sc;
+    } else {
+        calpha = sqrt(2.) / 2.;
+        salpha = sqrt(2.) / 2.;
+    }
+    double df0 = hypot(dfx0 * calpha, dfy0 * salpha);
+    double fm = mu * hypot(fxm * calpha, fym * salpha);
+    double sm = mu * hypot(sxm * calpha, sym * salpha);
+    double fs = mu * hypot(fxs * calpha, fys * salpha);
+    double ss = mu * hypot(sxs * calpha, sys * salpha);
+    double f, fos;
+    tmxy_combined(&f, &fos, sc, df0, sm, fm, ss, fs);
+    double Fx, Fy;
+    if (sc > 0.) {
+        Fx = f * sx / sc;
+        Fy = f * sy / sc;
+    } else {
+        Fx = 0.;
+        Fy = 0.;
+    }
+    Fx = (1.0 - frblend) * Fx0 + frblend * Fx;
+    Fy = (1.0 - frblend) * Fy0 + frblend * Fy;
+    ts->My = -P(LFDM_P_RR) * fz * ts->rStat * tanh(ts->omega);
+    ts->fx = Fx;
+    ts->fy = Fy;
+}
+
+/* computePowertrainRHS: dof18_gpu.cu:664-839 (same body for both tire types) */
+static void powertrainRHS(Veh* v, Tire* t, const Par* pp, const double* controls) {
+    const lfdm_class18* c = pp->c;
+    double torque_t = 0;
+    double max_bias = 2;
+    const double throttle = controls[2], braking = controls[3];
+    if (c->tcbool) {
+        int tc_reverse_flow = 0;
+        double omega_t = 0.25 * (t[0].omega + t[1].omega + t[2].omega + t[3].omega);
+        double omega_out = omega_t / (c->gearRatios[v->current_gr]);
+        double omega_in = v->crankOmega;
+        double sr, cf, tr;
+        if ((omega_out < 1e-9) || (omega_in < 1e-9)) {
+            sr = 0;
+            cf = oracle_map_y(&c->CFmap[0][0], c->CFmapSize, sr);
+            tr = oracle_map_y(&c->TRmap[0][0], c->TRmapSize, sr);
+        } else {
+            sr = omega_out / omega_in;
+            if (sr > 1.) {
+                sr = 1. - (sr - 1.);
+                tc_reverse_flow = 1;
+            }
+            if (sr < 0) sr = 0;
+            cf = oracle_map_y(&c->CFmap[0][0], c->CFmapSize, sr);
+            tr = oracle_map_y(&c->TRmap[0][0], c->TRmapSize, sr);
+        }
+        double torque_in = -pow((omega_in / cf), 2);
+        if (tc_reverse_flow) torque_in = -torque_in;
+        double torque_out;
+        if (tc_reverse_flow) torque_out = -torque_in;
+        else torque_out = -tr * torque_in;
+        torque_t = torque_out / c->gearRatios[v->current_gr];
+        /* reference: abs((u - 0) < 1e-9) && (torque_t < 0) — abs() of the comparison's result */
+        if ((v->u - 0) < 1e-9 && (torque_t < 0)) torque_t = 0;
+        v->dOmega_crank = (1. / P(LFDM_P_CRANKINERTIA)) * (driveTorque(pp, throttle, v->crankOmega) + torque_in);
+        if (omega_out > c->shiftMap[v->current_gr][1]) {
+            if (v->current_gr < c->noGears - 1) v->current_gr++;
+        } else if (omega_out < c->shiftMap[v->current_gr][0]) {
+            if (v->current_gr > 0) v->current_gr--;
+        }
+    } else {
+        v->crankOmega =
+            0.25 * (t[0].omega + t[1].omega + t[2].omega + t[3].omega) / c->gearRatios[v->current_gr];
+        torque_t = driveTorque(pp, throttle, v->crankOmega) / c->gearRatios[v->current_gr];
+        if ((v->u - 0) < 1e-9 && (torque_t < 0)) torque_t = 0;
+        if (v->crankOmega > c->shiftMap[v->current_gr][1]) {
+            if (v->current_gr < c->noGears - 1) v->current_gr++;
+        } else if (v->crankOmega < c->shiftMap[v->current_gr][0]) {
+            if (v->current_gr > 0) v->current_gr--;
+        }
+    }
+    double torque_front = 0, torque_rear = 0;
+    if (c->driveType) {
+        torque_front = torque_t * 0.5;
+        torque_rear = torque_t * 0.5;
+    } else {
+        if (c->whichWheels) {
+            torque_front = 0;
+            torque_rear = torque_t;
+        } else {
+            torque_front = torque_t;
+            torque_rear = 0;
+        }
+    }
+    differentialSplit(torque_front, max_bias, t[0].omega, t[1].omega, &t[0].engTor, &t[1].engTor);
+    differentialSplit(torque_rear, max_bias, t[2].omega, t[3].omega, &t[2].engTor, &t[3].engTor);
+    const double jw = P(LFDM_P_JW);
+    const double brake = P(LFDM_P_MAXBRAKETORQUE) * braking; /* brakeTorque: dof18_gpu.cuh:1069-1071 */
+    for (int k = 0; k < 4; ++k)
+        t[k].dOmega = (1 / jw) * (t[k].engTor + t[k].My - sgn(t[k].omega) * brake - t[k].fx * t[k].rStat);
+}
+
+/* computeVehRHS: dof18_gpu.cu:1017-1068 */
+static void vehRHS(Veh* v, const Par* pp, const double* fx, const double* fy) {
+    const double a = P(LFDM_P_A), b = P(LFDM_P_B), m = P(LFDM_P_M), muf = P(LFDM_P_MUF), mur = P(LFDM_P_MUR);
+    const double jx = P(LFDM_P_JX), jz = P(LFDM_P_JZ), jxz = P(LFDM_P_JXZ);
+    double mt = m + 2 * (muf + mur);
+    double hrc = (P(LFDM_P_HRCF) * b + P(LFDM_P_HRCR) * a) / (a + b);
+    double E1 = -mt * v->wz * v->u + (fy[0] + fy[1] + fy[2] + fy[3]);
+    double E2 = (fy[0] + fy[1]) * a - (fy[2] + fy[3]) * b + (fx[1] - fx[0]) * P(LFDM_P_CF) / 2 +
+                (fx[3] - fx[2]) * P(LFDM_P_CR) / 2 + (-muf * a + mur * b) * v->wz * v->u;
+    double E3 = m * G * hrc * v->phi - (P(LFDM_P_KROF) + P(LFDM_P_KROR)) * v->phi -
+                (P(LFDM_P_BROF) + P(LFDM_P_BROR)) * v->wx + hrc * m * v->wz * v->u;
+    double A1 = mur * b - muf * a;
+    double A2 = jx + m * pow(hrc, 2);
+    double A3 = hrc * m;
+    v->udot = v->wz * v->v +
+              (1 / mt) * ((fx[0] + fx[1] + fx[2] + fx[3]) + (-mur * b + muf * a) * pow(v->wz, 2) -
+                          2. * hrc * m * v->wz * v->wx);
+    double denom = (A2 * pow(A1, 2) - 2. * A1 * A3 * jxz + jz * pow(A3, 2) + mt * pow(jxz, 2) - A2 * jz * mt);
+    v->vdot = (E1 * pow(jxz, 2) - A1 * A2 * E2 + A1 * E3 * jxz + A3 * E2 * jxz - A2 * E1 * jz - A3 * E3 * jz) / denom;
+    v->wxdot = (pow(A1, 2) * E3 - A1 * A3 * E2 + A1 * E1 * jxz - A3 * E1 * jz + E2 * jxz * mt - E3 * jz * mt) / denom;
+    v->wzdot = (pow(A3, 2) * E2 - A1 * A2 * E1 - A1 * A3 * E3 + A3 * E1 * jxz - A2 * E2 * mt + E3 * jxz * mt) / denom;
+}
+
+/* ---------------------------------------------------------------------------------------------- */
+/* one vehicle                                                                                     */
+
+static void load_state(const double* s, Veh* v, Tire* t) {
+    v->x = s[LFDM_S_X];
+    v->y = s[LFDM_S_Y];
+    v->u = s[LFDM_S_U];
+    v->v = s[LFDM_S_V];
+    v->psi = s[LFDM_S_PSI];
+    v->wz = s[LFDM_S_WZ];
+    v->phi = s[LFDM_S_PHI];
+    v->wx = s[LFDM_S_WX];
+    v->udot = s[LFDM_S_UDOT];
+    v->vdot = s[LFDM_S_VDOT];
+    v->wxdot = s[LFDM_S_WXDOT];
+    v->wzdot = s[LFDM_S_WZDOT];
+    v->crankOmega = s[LFDM_S_CRANKOMEGA];
+    v->dOmega_crank = s[LFDM_S_DOMEGA_CRANK];
+    v->current_gr = (int)s[LFDM_S_CURRENT_GR];
+    for (int k = 0; k < 4; ++k) memcpy(&t[k], s + LFDM_S_TIRE0 + k * LFDM_S_TIRE_STRIDE, sizeof(Tire));
+}
+static void store_state(double* s, const Veh* v, const Tire* t) {
+    s[LFDM_S_X] = v->x;
+    s[LFDM_S_Y] = v->y;
+    s[LFDM_S_U] = v->u;
+    s[LFDM_S_V] = v->v;
+    s[LFDM_S_PSI] = v->psi;
+    s[LFDM_S_WZ] = v->wz;
+    s[LFDM_S_PHI] = v->phi;
+    s[LFDM_S_WX] = v->wx;
+    s[LFDM_S_UDOT] = v->udot;
+    s[LFDM_S_VDOT] = v->vdot;
+    s[LFDM_S_WXDOT] = v->wxdot;
+    s[LFDM_S_WZDOT] = v->wzdot;
+    s[LFDM_S_CRANKOMEGA] = v->crankOmega;
+    s[LFDM_S_DOMEGA_CRANK] = v->dOmega_crank;
+    s[LFDM_S_CURRENT_GR] = (double)v->current_gr;
+    for (int k = 0; k < 4; ++k) memcpy(s + LFDM_S_TIRE0 + k * LFDM_S_TIRE_STRIDE, &t[k], sizeof(Tire));
+}
+
+/* rhsFun: 18dof-gpu/dof18_halfImplicit_gpu.cu:685-729 */
+static void rhs(Veh* v, Tire* t, const Par* pp, const double* controls, int nr) {
+    double loads[4] = {0., 0., 0., 0.};
+    computeTireLoads(loads, v, pp);
+    vehToTireTransform(t, v, loads, pp, controls[1]);
+    if (nr) {
+        tireRHS_Nr(&t[0], pp, controls[1]);
+        tireRHS_Nr(&t[1], pp, controls[1]);
+        tireRHS_Nr(&t[2], pp, 0);
+        tireRHS_Nr(&t[3], pp, 0);
+    } else {
+        tireRHS_TM(&t[0], pp, controls[1]);
+        tireRHS_TM(&t[1], pp, controls[1]);
+        tireRHS_TM(&t[2], pp, 0);
+        tireRHS_TM(&t[3], pp, 0);
+    }
+    powertrainRHS(v, t, pp, controls);
+    tireToVehTransform(t, pp, controls[1]);
+    double fx[4] = {t[0].fx, t[1].fx, t[2].fx, t[3].fx};
+    double fy[4] = {t[0].fy, t[1].fy, t[2].fy, t[3].fy};
+    vehRHS(v, pp, fx, fy);
+}
+
+/* half-implicit update: dof18_halfImplicit_gpu.cu:913-946 */
+static void update(Veh* v, Tire* t, const Par* pp, double step, int nr) {
+    for (int k = 0; k < 4; ++k) {
+        if (!nr) {
+            t[k].xe += t[k].xedot * step;
+            t[k].ye += t[k].yedot * step;
+        }
+        t[k].omega += t[k].dOmega * step;
+    }
+    if (pp->c->tcbool) v->crankOmega += v->dOmega_crank * step;
+    v->u += v->udot * step;
+    v->v += v->vdot * step;
+    v->wx += v->wxdot * step;
+    v->wz += v->wzdot * step;
+    v->x += (v->u * cos(v->psi) - v->v * sin(v->psi)) * step;
+    v->y += (v->u * sin(v->psi) + v->v * cos(v->psi)) * step;
+    v->psi += v->wz * step;
+    v->phi += v->wx * step;
+}
+
+static void controls_at(const oracle18_args* a, int i, double t, double* c) {
+    if (a->drv_rows) {
+        oracle_driver_input(t, a->drv_rows + 4 * a->drv_off[i], a->drv_len[i], c);
+    } else {
+        c[0] = t;
+        c[1] = a->ctl[3 * i + 0];
+        c[2] = a->ctl[3 * i + 1];
+        c[3] = a->ctl[3 * i + 2];
+    }
+}
+
+/* one GPU launch window for vehicle i: Integrate, dof18_halfImplicit_gpu.cu:882-977 */
+static void window(const oracle18_args* a, int i, Veh* v, Tire* t, const Par* pp, double current_time,
+                   int64_t sample_base) {
+    const int nr = a->tire_type == LFDM_TIRE_TMEASY_NR;
+    const double step = a->dt;
+    double tt = current_time;
+    double kernel_time = 0;
+    int64_t stored = 0;
+    const double end_time = (tt + a->ksim) - step / 10.;
+    while (tt < end_time) {
+        double c[4];
+        controls_at(a, i, tt, c);
+        rhs(v, t, pp, c, nr);
+        update(v, t, pp, step, nr);
+        tt += step;
+        kernel_time += step;
+        if (a->resp && a->dtout > 0) {
+            if (fabs(kernel_time - (stored + 1) * a->dtout) < 1e-7) {
+                int64_t smp = sample_base + stored;
+                if (stored < a->samples_per_window && smp < a->resp_samples) {
+                    double* r = a->resp + (size_t)smp * LFDM18_RESP_CHANNELS * a->n;
+                    const double ch[LFDM18_RESP_CHANNELS] = {tt,     v->x,  v->y,  v->u,       v->v,
+                                                             v->phi, v->psi, v->wx, v->wz,      t[0].omega,
+                                                             t[1].omega, t[2].omega, t[3].omega};
+                    for (int k = 0; k < LFDM18_RESP_CHANNELS; ++k) r[(size_t)k * a->n + i] = ch[k];
+                }
+                stored++;
+            }
+        }
+    }
+}
+
+static void run_vehicle(const oracle18_args* a, int i) {
+    Veh v;
+    Tire t[4];
+    Par pp = {a->params + (size_t)i * LFDM_P_COUNT, &a->classes[a->class_of[i]]};
+    const int nr = a->tire_type == LFDM_TIRE_TMEASY_NR;
+    load_state(a->states + (size_t)i * LFDM_S_COUNT, &v, t);
+    if (a->schedule == 0) {
+        /* d18SolverHalfImplicit::Integrate, 18dof/dof18_halfImplicit.cpp:163-242 */
+        double tt = a->t0;
+        while (tt < (a->tend - a->dt / 10.)) {
+            double c[4];
+            controls_at(a, i, tt, c);
+            rhs(&v, t, &pp, c, nr);
+            update(&v, t, &pp, a->dt, nr);
+            tt += a->dt;
+        }
+    } else if (a->schedule == 1) {
+        /* d18SolverHalfImplicitGPU::Solve, dof18_halfImplicit_gpu.cu:438-463 */
+        double current_time = a->t0;
+        int64_t w = 0;
+        while (current_time < a->tend) {
+            window(a, i, &v, t, &pp, current_time, w * a->samples_per_window);
+            current_time = current_time + a->ksim;
+            ++w;
+        }
+    } else {
+        window(a, i, &v, t, &pp, a->t0, 0);
+    }
+    store_state(a->states + (size_t)i * LFDM_S_COUNT, &v, t);
+}
+
+typedef struct {
+    const oracle18_args* a;
+    int lo, hi;
+} Chunk;
+
+static void* worker(void* p) {
+    Chunk* c = (Chunk*)p;
+    for (int i = c->lo; i < c->hi; ++i) run_vehicle(c->a, i);
+    return NULL;
+}
+
+int oracle18_run(const oracle18_args* a) {
+    if (!a || a->n < 0 || !a->classes || !a->class_of || !a->params || !a->states) return 1;
+    if (!a->drv_rows && !a->ctl) return 1;
+    if (a->drv_rows && (!a->drv_off || !a->drv_len)) return 1;
+    if (a->schedule != 0 && !(a->ksim > 0)) return 1;
+    int nt = a->nthreads < 1 ? 1 : a->nthreads;
+    if (nt > a->n) nt = a->n > 0 ? a->n : 1;
+    if (nt == 1) {
+        for (int i = 0; i < a->n; ++i) run_vehicle(a, i);
+        return 0;
+    }
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nt);
+    Chunk* ch = (Chunk*)malloc(sizeof(Chunk) * nt);
+    for (int k = 0; k < nt; ++k) {
+        ch[k].a = a;
+        ch[k].lo = (int)((long)a->n * k / nt);
+        ch[k].hi = (int)((long)a->n * (k + 1) / nt);
+        pthread_create(&th[k], NULL, worker, &ch[k]);
+    }
+    for (int k = 0; k < nt; ++k) pthread_join(th[k], NULL);
+    free(th);
+    free(ch);
+    return 0;
+}

@@ -1,0 +1,62 @@
+/*
+ * ORACLE — test infrastructure only. Nothing in the product links, loads or calls this.
+ *
+ * CPU restatement (plain C, FP64, no FMA contraction) of the reference's batched half-implicit
+ * stepper for the 18-DOF model (TMeasy and TMeasyNr tires). It is the checker the CUDA path is
+ * compared against in tests/, smoke() and bench.py's CPU-baseline leg. It is pinned against the
+ * reference's own CPU solver (oracle/refrun18.cpp, built by `make ref`) through the golden
+ * fixtures in tests/golden/.
+ */
+#ifndef LFDM_ORACLE_H
+#define LFDM_ORACLE_H
+
+#include <stdint.h>
+#include "../include/lfdm.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    int n;                        /* vehicles */
+    int tire_type;                /* LFDM_TIRE_TMEASY / LFDM_TIRE_TMEASY_NR */
+    const lfdm_class18* classes;  /* class table */
+    const int32_t* class_of;      /* [n] class index of each vehicle */
+    const double* params;         /* [n][LFDM_P_COUNT] */
+    double* states;               /* [n][LFDM_S_COUNT], advanced in place */
+    /* controls: driver tables (rows of {t, steering, throttle, braking}) ... */
+    const double* drv_rows;       /* concatenated rows, or NULL */
+    const int64_t* drv_off;       /* [n] first row of each vehicle's table */
+    const int32_t* drv_len;       /* [n] rows of each vehicle's table */
+    /* ... or constant per-vehicle controls for the whole window (SolveStep) */
+    const double* ctl;            /* [n][3] {steering, throttle, braking}, used when drv_rows == NULL */
+    double dt;                    /* integration step */
+    double t0;                    /* start time */
+    double tend;                  /* end time (schedule 0 and 1) */
+    double ksim;                  /* window length (schedule 1 and 2) */
+    int schedule;                 /* 0: CPU solver (t from t0 while t < tend - dt/10)
+                                     1: GPU Solve (windows from t0 while window start < tend)
+                                     2: GPU SolveStep (exactly one window from t0) */
+    double dtout;                 /* output interval, <= 0 for none (schedules 1 and 2) */
+    double* resp;                 /* [samples][13][n], window w writes samples w*spw ... */
+    int64_t resp_samples;         /* capacity in samples */
+    int64_t samples_per_window;   /* spw = ceil(ksim / dtout) */
+    int nthreads;                 /* host threads (>= 1) */
+} oracle18_args;
+
+/* Returns 0 on success, nonzero on bad arguments. */
+int oracle18_run(const oracle18_args* a);
+
+/* tireInit (18dof-gpu/dof18_gpu.cu:227-241) on one flat parameter vector. */
+void oracle_tire_init(double* params);
+
+/* Driver-table interpolation of one vehicle at time t (utils/utils_gpu.cu:34-56); out[4]. */
+void oracle_driver_input(double t, const double* rows, int len, double* out);
+
+/* Map lookup (utils/utils_gpu.cu:60-75) on [n][2] points. */
+double oracle_map_y(const double* map, int n, double x);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

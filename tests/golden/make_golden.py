@@ -1,0 +1,148 @@
+"""Generate tests/golden/golden18.json from the reference's own CPU 18-DOF solver.
+
+Run where the reference checkout exists (it reads vehicle/tire JSON and driver tables from it):
+    make -C oracle ref REF=<reference>/wheeled_vehicle_models
+    python tests/golden/make_golden.py [<reference>/wheeled_vehicle_models]
+
+Each case stores its complete inputs (vehicle and tire parameters re-serialised from the
+reference's data files or from the seeded synthetic SUV fleet, the driver table rows, the
+schedule and initial state) and the reference's outputs: sampled trajectories and the full final
+state, printed with 17 significant digits. The oracle and the CUDA path are checked against these
+values on machines that have no reference checkout.
+"""
+from __future__ import annotations
+
+import importlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+lfdm = importlib.import_module("low-fidelity-dynamic-models_gb300")
+from importlib import import_module  # noqa: E402
+
+fleet = import_module("low-fidelity-dynamic-models_gb300.fleet")
+abi = import_module("low-fidelity-dynamic-models_gb300._abi")
+
+REFRUN = os.path.join(ROOT, "oracle", "_ref", "refrun18")
+SEED = 20261203
+
+
+def _fmt(x: float) -> str:
+    return repr(float(x))
+
+
+def run_ref(job_lines: list[str]) -> list[dict]:
+    out = subprocess.run([REFRUN], input="\n".join(job_lines) + "\n", capture_output=True, text=True, check=True)
+    results, cur = [], {"samples": []}
+    for line in out.stdout.splitlines():
+        tok = line.split()
+        if not tok:
+            continue
+        if tok[0] == "S":
+            cur["samples"].append([int(tok[1])] + [float(v) for v in tok[2:]])
+        elif tok[0] == "F":
+            vals = [float(v) for v in tok[1:]]
+            cur["final"] = vals
+        elif tok[0] == "E":
+            results.append(cur)
+            cur = {"samples": []}
+    return results
+
+
+def final_to_state(final: list[float]) -> list[float]:
+    """refrun18 'F' row -> flat state vector (include/lfdm.h order)."""
+    s = [0.0] * abi.S_COUNT
+    s[:15] = final[:15]
+    s[15:75] = final[15:75]
+    return s
+
+
+def main(ref: str) -> None:
+    d18 = os.path.join(ref, "18dof-gpu", "data")
+    veh_hmmwv = json.load(open(os.path.join(d18, "json", "HMMWV", "vehicle.json")))
+    tire_hmmwv = json.load(open(os.path.join(d18, "json", "HMMWV", "tmeasy.json")))
+    cases = []
+    with tempfile.TemporaryDirectory() as tmp:
+        def write_json(name, obj):
+            p = os.path.join(tmp, name)
+            with open(p, "w") as f:
+                json.dump(obj, f)
+            return p
+
+        def write_table(name, rows):
+            p = os.path.join(tmp, name)
+            with open(p, "w") as f:
+                for r in rows:
+                    f.write(" ".join(_fmt(v) for v in r) + "\n")
+            return p
+
+        vj, tj = write_json("hmmwv_vehicle.json", veh_hmmwv), write_json("hmmwv_tmeasy.json", tire_hmmwv)
+        named = [
+            ("hmmwv_acc3_cpu", "acc3", 0.0, None, 100),
+            ("hmmwv_acc3_gpu", "acc3", 2.0, 10.0, 100),
+            ("hmmwv_dl4_gpu", "double_lane4", 2.0, 22.0, 100),
+            ("hmmwv_st3_gpu", "st3_right", 2.0, None, 100),
+        ]
+        jobs, meta = [], []
+        for name, drv, ksim, tend, sample in named:
+            rows = lfdm.params.load_driver_table(os.path.join(d18, "input", drv + ".txt")).tolist()
+            tp = write_table(f"{name}.txt", rows)
+            tend_v = tend if tend is not None else rows[-1][0]
+            jobs += [f"veh {vj}", f"tire {tj}", "tiretype 0", f"driver {tp}", "dt 0.001", f"tend {_fmt(tend_v)}",
+                     f"ksim {_fmt(ksim)}", f"sample {sample}", "run"]
+            meta.append({"name": name, "vehicle": veh_hmmwv, "tire": tire_hmmwv, "tire_type": 0, "driver": rows,
+                         "dt": 0.001, "tend": tend_v, "ksim": ksim, "sample": sample, "vp": {}, "tp": {},
+                         "state": [0.0] * abi.S_COUNT, "source": f"HMMWV vehicle.json + tmeasy.json, {drv}.txt"})
+        # seeded synthetic SUV fleet (GPU schedule, 1 s windows)
+        n_syn = 12
+        fl = fleet.fleet18(n_syn, seed=SEED, horizon=10.0)
+        sj, stj = write_json("suv_vehicle.json", fleet.SUV18_VEHICLE), write_json("suv_tire.json", fleet.SUV_TIRE)
+        _, base = fleet.suv18()
+        P = abi.P
+        vfields = ["m", "jz", "a", "b"]
+        tfields = ["kt"] + list(fleet.FRICTION_FIELDS)
+        key = {"fxmpn": "fxmPn", "fxmp2n": "fxmP2n", "fxspn": "fxsPn", "fxsp2n": "fxsP2n", "fympn": "fymPn",
+               "fymp2n": "fymP2n", "fyspn": "fysPn", "fysp2n": "fysP2n", "kt": "kt"}
+        for i in range(n_syn):
+            rows = fl["tables"][i].tolist()
+            tp = write_table(f"suv_{i}.txt", rows)
+            vp = {k: float(fl["params"][i, P[k]]) for k in vfields}
+            tpv = {key[k]: float(fl["params"][i, P[k]]) for k in tfields}
+            st = fl["states"][i]
+            u0 = float(st[abi.S["u"]])
+            w0 = float(st[abi.S_TIRE0 + abi.T["omega"]])
+            crank = float(st[abi.S["crankomega"]])
+            gear = int(st[abi.S["current_gr"]])
+            lines = [f"veh {sj}", f"tire {stj}", "tiretype 0", f"driver {tp}", "dt 0.001", "tend 10",
+                     "ksim 1", "sample 250"]
+            lines += [f"vp {k} {_fmt(v)}" for k, v in vp.items()] + [f"tp {k} {_fmt(v)}" for k, v in tpv.items()]
+            lines += [f"vs u {_fmt(u0)}", f"vs crankOmega {_fmt(crank)}", f"gear {gear}"]
+            lines += [f"ts {k} omega {_fmt(w0)}" for k in range(4)] + ["run"]
+            jobs += lines
+            meta.append({"name": f"suv_fleet_{i}", "vehicle": fleet.SUV18_VEHICLE, "tire": fleet.SUV_TIRE,
+                         "tire_type": 0, "driver": rows, "dt": 0.001, "tend": 10.0, "ksim": 1.0, "sample": 250,
+                         "vp": vp, "tp": tpv, "state": st.tolist(),
+                         "source": f"synthetic SUV fleet seed {SEED} vehicle {i}"})
+        results = run_ref(jobs)
+    assert len(results) == len(meta)
+    for m, r in zip(meta, results):
+        m["expected_samples"] = r["samples"]
+        m["expected_final"] = final_to_state(r["final"])
+        cases.append(m)
+    out = {"generator": "tests/golden/make_golden.py", "reference_solver": "d18SolverHalfImplicit (CPU), "
+           "replayed step by step through IntegrateStep; ksim>0 uses the GPU solver's window schedule",
+           "cases": cases}
+    with open(os.path.join(HERE, "golden18.json"), "w") as f:
+        json.dump(out, f, separators=(",", ":"))
+    print(f"wrote {len(cases)} cases; e.g. {cases[0]['name']} x={cases[0]['expected_final'][0]!r}")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/wheeled_vehicle_models")

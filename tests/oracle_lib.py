@@ -1,0 +1,116 @@
+"""ctypes access to the oracle (oracle/_build/liboracle.so) — test infrastructure only.
+
+The oracle is the CPU restatement of the reference stepper (oracle/lfdm_oracle.c); tests and
+bench.py's CPU-baseline leg use it as the checker. It is built with `make -C oracle oracle`.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+LIB = os.path.join(ORACLE_DIR, "_build", "liboracle.so")
+REFRUN18 = os.path.join(ORACLE_DIR, "_ref", "refrun18")
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR, "oracle"], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        _lib = ctypes.CDLL(LIB)
+        _lib.oracle18_run.argtypes = [ctypes.c_void_p]
+        _lib.oracle18_run.restype = ctypes.c_int
+        _lib.oracle_map_y.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
+        _lib.oracle_map_y.restype = ctypes.c_double
+        _lib.oracle_driver_input.argtypes = [ctypes.c_double, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        _lib.oracle_tire_init.argtypes = [ctypes.c_void_p]
+    return _lib
+
+
+class _Args(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_int), ("tire_type", ctypes.c_int),
+        ("classes", ctypes.c_void_p), ("class_of", ctypes.c_void_p),
+        ("params", ctypes.c_void_p), ("states", ctypes.c_void_p),
+        ("drv_rows", ctypes.c_void_p), ("drv_off", ctypes.c_void_p), ("drv_len", ctypes.c_void_p),
+        ("ctl", ctypes.c_void_p),
+        ("dt", ctypes.c_double), ("t0", ctypes.c_double), ("tend", ctypes.c_double), ("ksim", ctypes.c_double),
+        ("schedule", ctypes.c_int),
+        ("dtout", ctypes.c_double), ("resp", ctypes.c_void_p),
+        ("resp_samples", ctypes.c_int64), ("samples_per_window", ctypes.c_int64),
+        ("nthreads", ctypes.c_int),
+    ]
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None else None
+
+
+def run18(classes, class_of, params, states, tables=None, ctl=None, *, tire_type=0, dt=1e-3, t0=0.0,
+          tend=10.0, ksim=2.0, schedule=1, dtout=0.0, nthreads=1):
+    """Advance `states` ([n][75], copied) with the oracle. `tables` is a list of per-vehicle
+    [rows][4] arrays or one [n][rows][4] array. schedule 0 = CPU solver, 1 = GPU Solve,
+    2 = one SolveStep window. Returns (states, resp or None)."""
+    n = params.shape[0]
+    cls_arr = (type(classes[0]) * len(classes))(*classes)
+    class_of = np.ascontiguousarray(class_of, dtype=np.int32)
+    params = np.ascontiguousarray(params, dtype=np.float64)
+    st = np.array(states, dtype=np.float64, order="C", copy=True)
+    rows = off = ln = None
+    if tables is not None:
+        if isinstance(tables, np.ndarray) and tables.ndim == 3:
+            rows = np.ascontiguousarray(tables.reshape(-1, 4), dtype=np.float64)
+            ln = np.full(n, tables.shape[1], dtype=np.int32)
+        else:
+            rows = np.ascontiguousarray(np.concatenate([np.asarray(t, np.float64).reshape(-1, 4) for t in tables]))
+            ln = np.array([len(t) for t in tables], dtype=np.int32)
+        off = np.zeros(n, dtype=np.int64)
+        off[1:] = np.cumsum(ln[:-1].astype(np.int64))
+    ctl_arr = np.ascontiguousarray(ctl, dtype=np.float64) if ctl is not None else None
+    resp = None
+    spw = 0
+    nsamp = 0
+    if dtout > 0:
+        spw = int(np.ceil(ksim / dtout))
+        windows = 1 if schedule == 2 else int(np.ceil((tend - t0) / ksim - 1e-12))
+        # count the windows exactly as the solver loop does
+        if schedule == 1:
+            windows, ct = 0, t0
+            while ct < tend:
+                windows += 1
+                ct = ct + ksim
+        nsamp = windows * spw
+        resp = np.full((nsamp, 13, n), np.nan, dtype=np.float64)
+    a = _Args(n=n, tire_type=tire_type, classes=ctypes.addressof(cls_arr), class_of=_ptr(class_of),
+              params=_ptr(params), states=_ptr(st), drv_rows=_ptr(rows), drv_off=_ptr(off), drv_len=_ptr(ln),
+              ctl=_ptr(ctl_arr), dt=dt, t0=t0, tend=tend, ksim=ksim, schedule=schedule, dtout=dtout,
+              resp=_ptr(resp), resp_samples=nsamp, samples_per_window=spw, nthreads=nthreads)
+    rc = lib().oracle18_run(ctypes.byref(a))
+    if rc != 0:
+        raise RuntimeError(f"oracle18_run failed rc={rc}")
+    return st, resp
+
+
+def map_y(points, x) -> float:
+    m = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 2))
+    return lib().oracle_map_y(m.ctypes.data, m.shape[0], float(x))
+
+
+def driver_input(t, rows) -> np.ndarray:
+    r = np.ascontiguousarray(np.asarray(rows, dtype=np.float64).reshape(-1, 4))
+    out = np.zeros(4)
+    lib().oracle_driver_input(float(t), r.ctypes.data, r.shape[0], out.ctypes.data)
+    return out
