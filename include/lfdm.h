@@ -201,6 +201,24 @@ int lfdm_last_kernel_ms(lfdm_solver* h, double* ms, unsigned* launches);
 /* Library build information (arch, version). */
 const char* lfdm_version(void);
 
+/* Host-only utilities (no device needed). setVehParamsJSON + setTireParamsJSON + tireInit        */
+/* (dof18_gpu.cu:1075-1330, :227-241) into a class record and a flat parameter vector, and        */
+/* LoadDriverData (utils/utils_gpu.cu:7-31) into rows [capacity_rows][4].                          */
+int lfdm_parse_vehicle18(const char* veh_json, const char* tire_json, int tire_type, lfdm_class18* cls,
+                         double* params, char* err, size_t err_len);
+int lfdm_load_driver_file(const char* path, double* rows, unsigned capacity_rows, unsigned* nrows, char* err,
+                          size_t err_len);
+
+/* Extension: one window whose controls follow a per-step schedule shared by all vehicles          */
+/* (ctl: [nsteps][3] {steering, throttle, braking}), the C-ABI form of the reference's functor      */
+/* SolveStep (dof18_halfImplicit_gpu.cuh:234-287): the C++ header evaluates the functor at the      */
+/* window's step times and passes the schedule. ctl_on_device says whether ctl is a device pointer. */
+/* Fails with LFDM_ERR_ARG when nsteps differs from the window's step count (lfdm_window_steps).    */
+int lfdm_solve_step_schedule(lfdm_solver* h, double t, const double* ctl, unsigned nsteps, int ctl_on_device,
+                             double* t_out);
+/* Step count and step start times of the window starting at t (times: [capacity] or NULL). */
+int lfdm_window_steps(lfdm_solver* h, double t, unsigned* nsteps, double* times, unsigned capacity);
+
 #ifdef __cplusplus
 }
 #endif

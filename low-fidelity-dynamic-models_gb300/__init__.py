@@ -1,0 +1,332 @@
+"""GB300-native batched half-implicit stepper for the 11/18/24-DOF wheeled-vehicle models.
+
+Python binding of the C ABI in include/lfdm.h (library: _build/liblfdm.so, built by build.py).
+`d18SolverHalfImplicitGPU` mirrors the reference class of the same name
+(18dof-gpu/dof18_halfImplicit_gpu.cuh:15-343): Construct, Initialize, SetTimeStep, SetEndTime,
+SetKernelSimTime, SetHostDumpTime, SetThreadsPerBlock, SetOutput, Solve, SolveStep, GetSimState.
+The extensions take numpy arrays: per-vehicle parameters, driver tables and states, per-vehicle
+SolveStep controls, and a streamed SoA response buffer.
+
+There is no CPU fallback: loading the library or creating a solver without a CUDA device raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import Class18, P, P_COUNT, S, S_COUNT, T, S_TIRE0, S_TIRE_STRIDE, RESP18
+
+__all__ = ["lib", "LfdmError", "d18SolverHalfImplicitGPU", "TireType", "Class18", "P", "S", "T", "S_COUNT",
+           "P_COUNT", "RESP18", "S_TIRE0", "S_TIRE_STRIDE"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "liblfdm.so")
+
+
+class LfdmError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_abi.STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class TireType:
+    TMeasy = _abi.TIRE_TMEASY
+    TMeasyNr = _abi.TIRE_TMEASY_NR
+
+
+_lib = None
+_c_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def _sig(lib):
+    vp, u, i, d, dp, sz = ctypes.c_void_p, ctypes.c_uint, ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_size_t
+    cp = ctypes.c_char_p
+    table = {
+        "lfdm_create": ([i, u, ctypes.POINTER(vp)], i),
+        "lfdm_create_on_device": ([i, u, i, ctypes.POINTER(vp)], i),
+        "lfdm_destroy": ([vp], i),
+        "lfdm_last_error": ([vp], cp),
+        "lfdm_construct": ([vp, cp, cp, cp, u, cp, i], i),
+        "lfdm_construct_class": ([vp, vp, u, dp, i], i),
+        "lfdm_set_params": ([vp, u, u, dp], i),
+        "lfdm_get_params": ([vp, u, u, dp], i),
+        "lfdm_tire_init": ([dp], i),
+        "lfdm_set_driver_table": ([vp, u, u, dp, u], i),
+        "lfdm_set_driver_tables": ([vp, u, u, dp, u], i),
+        "lfdm_initialize": ([vp, dp, u], i),
+        "lfdm_set_states": ([vp, u, u, dp], i),
+        "lfdm_get_states": ([vp, u, u, dp], i),
+        "lfdm_set_time_step": ([vp, d], i),
+        "lfdm_set_end_time": ([vp, d], i),
+        "lfdm_set_kernel_sim_time": ([vp, d], i),
+        "lfdm_set_host_dump_time": ([vp, d], i),
+        "lfdm_set_threads_per_block": ([vp, u], i),
+        "lfdm_get_step": ([vp, _c_dp], i),
+        "lfdm_get_end_time": ([vp, _c_dp], i),
+        "lfdm_get_tire_type": ([vp, ctypes.POINTER(i)], i),
+        "lfdm_get_num_vehicles": ([vp, ctypes.POINTER(u), ctypes.POINTER(u), ctypes.POINTER(u)], i),
+        "lfdm_set_precision": ([vp, i], i),
+        "lfdm_set_output": ([vp, cp, d, i, u], i),
+        "lfdm_set_response_buffer": ([vp, dp, sz, d], i),
+        "lfdm_response_samples": ([vp, ctypes.POINTER(sz)], i),
+        "lfdm_register_host": ([vp, sz], i),
+        "lfdm_unregister_host": ([vp], i),
+        "lfdm_solve": ([vp], i),
+        "lfdm_solve_step": ([vp, d, d, d, d, _c_dp], i),
+        "lfdm_solve_step_controls": ([vp, d, dp, dp, dp, _c_dp], i),
+        "lfdm_solve_step_schedule": ([vp, d, dp, u, i, _c_dp], i),
+        "lfdm_window_steps": ([vp, d, ctypes.POINTER(u), dp, u], i),
+        "lfdm_get_sim_state": ([vp, u, dp], i),
+        "lfdm_get_status_words": ([vp, u, u, dp], i),
+        "lfdm_last_kernel_ms": ([vp, _c_dp, ctypes.POINTER(u)], i),
+        "lfdm_version": ([], cp),
+        "lfdm_parse_vehicle18": ([cp, cp, i, vp, dp, ctypes.c_char_p, sz], i),
+        "lfdm_load_driver_file": ([cp, dp, u, ctypes.POINTER(u), ctypes.c_char_p, sz], i),
+    }
+    for name, (args, res) in table.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    return lib
+
+
+def lib():
+    """The loaded C-ABI library. Raises when it has not been built (no silent fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; "
+                               "g.build()'` (needs nvcc)")
+        _lib = _sig(ctypes.CDLL(LIB_PATH))
+    return _lib
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+def parse_vehicle18(veh_json: str, tire_json: str, tire_type: int = TireType.TMeasy):
+    """The library's own JSON loader (host only): returns (Class18, params[P_COUNT])."""
+    c = Class18()
+    p = np.zeros(P_COUNT)
+    err = ctypes.create_string_buffer(512)
+    rc = lib().lfdm_parse_vehicle18(veh_json.encode(), tire_json.encode(), tire_type, ctypes.byref(c), _ptr(p),
+                                    err, 512)
+    if rc:
+        raise LfdmError(rc, err.value.decode())
+    return c, p
+
+
+def load_driver_file(path: str) -> np.ndarray:
+    n = ctypes.c_uint()
+    err = ctypes.create_string_buffer(512)
+    rc = lib().lfdm_load_driver_file(path.encode(), None, 0, ctypes.byref(n), err, 512)
+    if rc:
+        raise LfdmError(rc, err.value.decode())
+    rows = np.zeros((n.value, 4))
+    rc = lib().lfdm_load_driver_file(path.encode(), _ptr(rows), n.value, ctypes.byref(n), err, 512)
+    if rc:
+        raise LfdmError(rc, err.value.decode())
+    return rows
+
+
+class d18SolverHalfImplicitGPU:
+    """18-DOF batched half-implicit stepper on one GPU (reference: d18SolverHalfImplicitGPU)."""
+
+    def __init__(self, total_num_vehicles: int, device: int = 0):
+        self._L = lib()
+        h = ctypes.c_void_p()
+        rc = self._L.lfdm_create_on_device(18, int(total_num_vehicles), int(device), ctypes.byref(h))
+        if rc:
+            raise LfdmError(rc, self._L.lfdm_last_error(None).decode())
+        self._h = h
+        self.n = int(total_num_vehicles)
+
+    # -- plumbing -----------------------------------------------------------------------------
+    def _ck(self, rc: int):
+        if rc:
+            raise LfdmError(rc, self._L.lfdm_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.lfdm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- reference API --------------------------------------------------------------------------
+    def Construct(self, vehicle_params_file: str, tire_params_file: str, num_vehicles: int,
+                  driver_inputs_file: str | None = None, type: int = TireType.TMeasy):  # noqa: A002
+        self._ck(self._L.lfdm_construct(self._h, vehicle_params_file.encode(), tire_params_file.encode(), None,
+                                        int(num_vehicles),
+                                        driver_inputs_file.encode() if driver_inputs_file else None, int(type)))
+
+    def Initialize(self, state: np.ndarray, num_vehicles: int):
+        """Copy one flat state (S_COUNT doubles, include/lfdm.h order) into the next num_vehicles."""
+        s = _f64(state, (S_COUNT,))
+        self._ck(self._L.lfdm_initialize(self._h, _ptr(s), int(num_vehicles)))
+
+    def SetTimeStep(self, step: float):
+        self._ck(self._L.lfdm_set_time_step(self._h, float(step)))
+
+    def SetEndTime(self, tend: float):
+        self._ck(self._L.lfdm_set_end_time(self._h, float(tend)))
+
+    def SetKernelSimTime(self, t: float):
+        self._ck(self._L.lfdm_set_kernel_sim_time(self._h, float(t)))
+
+    def SetHostDumpTime(self, t: float):
+        self._ck(self._L.lfdm_set_host_dump_time(self._h, float(t)))
+
+    def SetThreadsPerBlock(self, threads: int):
+        self._ck(self._L.lfdm_set_threads_per_block(self._h, int(threads)))
+
+    def GetStep(self) -> float:
+        v = ctypes.c_double()
+        self._ck(self._L.lfdm_get_step(self._h, ctypes.byref(v)))
+        return v.value
+
+    def GetEndTime(self) -> float:
+        v = ctypes.c_double()
+        self._ck(self._L.lfdm_get_end_time(self._h, ctypes.byref(v)))
+        return v.value
+
+    def GetTireType(self) -> int:
+        v = ctypes.c_int()
+        self._ck(self._L.lfdm_get_tire_type(self._h, ctypes.byref(v)))
+        return v.value
+
+    def SetOutput(self, output_file: str, output_freq: float, store_all: bool = False, no_outs: int = 50):
+        self._ck(self._L.lfdm_set_output(self._h, output_file.encode(), float(output_freq), int(bool(store_all)),
+                                         int(no_outs)))
+
+    def Solve(self):
+        self._ck(self._L.lfdm_solve(self._h))
+
+    def SolveStep(self, t: float, steering=None, throttle=None, braking=None, schedule=None) -> float:
+        """SolveStep(t, steering, throttle, braking) with scalars (reference :497-550), per-vehicle
+        arrays (extension), or schedule=callable(t)->(steering, throttle, braking) evaluated at every
+        step time of the window (the reference's functor SolveStep, .cuh:234-287)."""
+        out = ctypes.c_double()
+        if schedule is not None:
+            times = self.window_times(t)
+            sched = _f64([schedule(x) for x in times], (len(times), 3))
+            self._ck(self._L.lfdm_solve_step_schedule(self._h, float(t), _ptr(sched), len(times), 0,
+                                                      ctypes.byref(out)))
+        elif np.ndim(steering) == 0 and np.ndim(throttle) == 0 and np.ndim(braking) == 0:
+            self._ck(self._L.lfdm_solve_step(self._h, float(t), float(steering), float(throttle), float(braking),
+                                             ctypes.byref(out)))
+        else:
+            st = _f64(np.broadcast_to(steering, (self.n,)))
+            th = _f64(np.broadcast_to(throttle, (self.n,)))
+            br = _f64(np.broadcast_to(braking, (self.n,)))
+            self._ck(self._L.lfdm_solve_step_controls(self._h, float(t), _ptr(st), _ptr(th), _ptr(br),
+                                                      ctypes.byref(out)))
+        return out.value
+
+    def GetSimState(self, vehicle_index: int) -> np.ndarray:
+        s = np.zeros(S_COUNT)
+        self._ck(self._L.lfdm_get_sim_state(self._h, int(vehicle_index), _ptr(s)))
+        return s
+
+    # -- extensions ---------------------------------------------------------------------------
+    def construct_class(self, cls: Class18, params: np.ndarray, tire_type: int = TireType.TMeasy):
+        p = _f64(params).reshape(-1, P_COUNT)
+        self._ck(self._L.lfdm_construct_class(self._h, ctypes.byref(cls), p.shape[0], _ptr(p), int(tire_type)))
+
+    def set_params(self, params: np.ndarray, first: int = 0):
+        p = _f64(params).reshape(-1, P_COUNT)
+        self._ck(self._L.lfdm_set_params(self._h, int(first), p.shape[0], _ptr(p)))
+
+    def get_params(self, first: int = 0, count: int | None = None) -> np.ndarray:
+        count = self.n - first if count is None else count
+        p = np.zeros((count, P_COUNT))
+        self._ck(self._L.lfdm_get_params(self._h, int(first), int(count), _ptr(p)))
+        return p
+
+    def set_driver_tables(self, tables: np.ndarray, first: int = 0):
+        """tables: [rows][4] shared by all vehicles from `first`, or [count][rows][4] per vehicle."""
+        t = _f64(tables)
+        if t.ndim == 2:
+            self._ck(self._L.lfdm_set_driver_table(self._h, int(first), self.n - first, _ptr(t), t.shape[0]))
+        else:
+            self._ck(self._L.lfdm_set_driver_tables(self._h, int(first), t.shape[0], _ptr(t), t.shape[1]))
+
+    def set_states(self, states: np.ndarray, first: int = 0):
+        s = _f64(states).reshape(-1, S_COUNT)
+        self._ck(self._L.lfdm_set_states(self._h, int(first), s.shape[0], _ptr(s)))
+
+    def get_states(self, first: int = 0, count: int | None = None) -> np.ndarray:
+        count = self.n - first if count is None else count
+        s = np.zeros((count, S_COUNT))
+        self._ck(self._L.lfdm_get_states(self._h, int(first), int(count), _ptr(s)))
+        return s
+
+    def set_precision(self, precision: int):
+        self._ck(self._L.lfdm_set_precision(self._h, int(precision)))
+
+    def set_response_buffer(self, buf: np.ndarray | None, output_freq: float = 100.0):
+        """Stream Solve's SoA response [sample][13][N] into `buf` (float64, C-contiguous); samples
+        beyond its capacity wrap around."""
+        if buf is None:
+            self._ck(self._L.lfdm_set_response_buffer(self._h, None, 0, 1.0))
+            self._resp = None
+            return
+        if buf.dtype != np.float64 or not buf.flags.c_contiguous:
+            raise ValueError("response buffer must be C-contiguous float64")
+        self._resp = buf
+        self._ck(self._L.lfdm_set_response_buffer(self._h, _ptr(buf), buf.size, float(output_freq)))
+
+    def response_samples(self) -> int:
+        n = ctypes.c_size_t()
+        self._ck(self._L.lfdm_response_samples(self._h, ctypes.byref(n)))
+        return n.value
+
+    def window_times(self, t: float) -> np.ndarray:
+        n = ctypes.c_uint()
+        self._ck(self._L.lfdm_window_steps(self._h, float(t), ctypes.byref(n), None, 0))
+        times = np.zeros(n.value)
+        self._ck(self._L.lfdm_window_steps(self._h, float(t), ctypes.byref(n), _ptr(times), n.value))
+        return times
+
+    def last_kernel_ms(self):
+        ms = ctypes.c_double()
+        n = ctypes.c_uint()
+        self._ck(self._L.lfdm_last_kernel_ms(self._h, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
+    def status_words(self) -> np.ndarray:
+        w = np.zeros(self.n, dtype=np.uint32)
+        self._ck(self._L.lfdm_get_status_words(self._h, 0, self.n, _ptr(w)))
+        return w
+
+
+def register_host(a: np.ndarray) -> None:
+    """Page-lock a numpy array (for overlapped copies)."""
+    rc = lib().lfdm_register_host(ctypes.c_void_p(a.ctypes.data), a.nbytes)
+    if rc:
+        raise LfdmError(rc, "cudaHostRegister failed")
+
+
+def unregister_host(a: np.ndarray) -> None:
+    lib().lfdm_unregister_host(ctypes.c_void_p(a.ctypes.data))

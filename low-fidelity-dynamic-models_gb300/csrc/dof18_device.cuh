@@ -1,0 +1,578 @@
+// 18-DOF vehicle model: device-side data layouts and the right-hand side + half-implicit update.
+//
+// Algorithm: the reference's rhsFun (18dof-gpu/dof18_halfImplicit_gpu.cu:685-729) and Integrate
+// update (:913-946) with the physics of 18dof-gpu/dof18_gpu.cu. The arithmetic is rearranged for
+// a GPU whose FP64 issue rate is the bottleneck (every rearrangement is exact in real arithmetic
+// and changes results only at the rounding level):
+//   * parameter-only subexpressions are evaluated once per vehicle (prepare_constants18);
+//   * pow(x, 2) -> x*x; hypot(x, y) -> sqrt(x*x + y*y);
+//   * -tan(atan2(vsy, vta) - delta) -> -(vsy*cos d - vta*sin d) / (vta*cos d + vsy*sin d)
+//     (tangent difference identity; vta > 0);
+//   * sin/cos of the wheel angle once per step instead of once per use;
+//   * divisions sharing a step are merged into one reciprocal where the operands allow.
+// Branch structure (wheel lift-off, tmxy_combined regimes, gear shifts, torque-converter flow
+// direction, sineStep bands) is kept exactly, so the branch taken matches the reference whenever
+// the compared quantities agree.
+#pragma once
+
+#include <cstdint>
+
+#include "../../include/lfdm.h"
+
+namespace lfdm {
+
+constexpr double kG = 9.81;                                       // utils/utils_gpu.cuh:12
+constexpr double k2Pi = 6.283185307179586476925286766559;         // utils/utils_gpu.cuh:11
+constexpr double kSqrt2Over2 = 0.70710678118654757;               // sqrt(2.)/2. rounded to double
+
+// ---------------------------------------------------------------------------------------------
+// Per-vehicle derived constants (FP64), SoA [K18_COUNT][n_pad] in HBM, staged per block.
+enum K18 : int {
+    K_A = 0, K_B, K_CF2, K_CR2, K_MAXSTEER,
+    // computeTireLoads (dof18_gpu.cu:305-340)
+    K_Z1F, K_Z2F, K_Z3FK, K_Z3FB, K_Z4, K_Z1R, K_Z2R, K_Z3RK, K_Z3RB,
+    // computeVehRHS (dof18_gpu.cu:1017-1068)
+    K_MT, K_INVMT, K_E2WU, K_E3PHI, K_E3WX, K_E3WU, K_UWZ2, K_UWZWX,
+    K_CV1, K_CV2, K_CV3, K_CX2, K_CX3, K_CZ2,
+    // powertrain
+    K_INVCI, K_MAXBRAKE, K_INVJW,
+    // computeTireRHS (dof18_gpu.cu:379-530)
+    K_R0, K_INVKT, K_INVPN, K_PNMAX, K_FZRD, K_RDPN, K_DRD, K_RDCRIT,
+    K_Q1DFX0, K_Q2DFX0, K_Q1DFY0, K_Q2DFY0, K_Q1FXM, K_Q2FXM, K_Q1FYM, K_Q2FYM, K_Q1FXS, K_Q2FXS, K_Q1FYS,
+    K_Q2FYS,
+    K_LSXM, K_DSXM, K_LSYM, K_DSYM, K_LSXS, K_DSXS, K_LSYS, K_DSYS,
+    K_CX, K_CY, K_DX, K_DY, K_FXMP2N, K_FYMP2N, K_RR,
+    // TMeasyNr extras (dof18_gpu.cu:532-662)
+    K_MU, K_VCOUL, K_FRB0, K_FRB1,
+    K18_COUNT
+};
+
+// ---------------------------------------------------------------------------------------------
+// Per-class tables (flags, gears, maps) with precomputed segment reciprocals, staged in smem.
+struct MapDev {
+    int n;
+    int pad_;
+    double x[LFDM_MAX_MAP];
+    double y[LFDM_MAX_MAP];
+    double invdx[LFDM_MAX_MAP];  // 1 / (x[k+1] - x[k])
+    double dy[LFDM_MAX_MAP];     // y[k+1] - y[k]
+};
+struct ClassDev18 {
+    int nonLinearSteer, tcbool, throttleMod, driveType, whichWheels, noGears;
+    double gear[LFDM_MAX_GEARS];
+    double invgear[LFDM_MAX_GEARS];
+    double down[LFDM_MAX_GEARS];
+    double up[LFDM_MAX_GEARS];
+    MapDev steer, pt, loss, cf, tr;
+};
+
+// lower_bound over a sorted key array: first k with x <= a[k] (utils/utils_gpu.cu:109-121).
+__device__ __forceinline__ int lower_bound_x(const double* a, int n, double x) {
+    int l = 0, h = n;
+    while (l < h) {
+        int mid = (l + h) >> 1;
+        if (x <= a[mid]) h = mid;
+        else l = mid + 1;
+    }
+    return l;
+}
+
+// getMapY (utils/utils_gpu.cu:60-75): clamp outside, linear interpolation inside.
+__device__ __forceinline__ double map_y(const MapDev& m, double x) {
+    if (x <= m.x[0]) return m.y[0];
+    if (x >= m.x[m.n - 1]) return m.y[m.n - 1];
+    int r = lower_bound_x(m.x, m.n, x);
+    int l = r - 1;
+    double mbar = (x - m.x[l]) * m.invdx[l];
+    return fma(mbar, m.dy[l], m.y[l]);
+}
+
+// getMapY on the map with both coordinates scaled by s (driveTorque with throttleMod,
+// dof18_gpu.cu:18-31; the scaled copy is private to the call as in 18dof/dof18.cpp:23-29).
+__device__ __forceinline__ double map_y_scaled(const MapDev& m, double x, double s) {
+    const int n = m.n;
+    if (x <= m.x[0] * s) return m.y[0] * s;
+    if (x >= m.x[n - 1] * s) return m.y[n - 1] * s;
+    int l = 0, h = n;
+    while (l < h) {
+        int mid = (l + h) >> 1;
+        if (x <= m.x[mid] * s) h = mid;
+        else l = mid + 1;
+    }
+    const int r = l, lf = r - 1;
+    const double xl = m.x[lf] * s, xr = m.x[r] * s, yl = m.y[lf] * s, yr = m.y[r] * s;
+    double mbar = (x - xl) / (xr - xl);
+    return yl + mbar * (yr - yl);
+}
+
+// sineStep (utils/utils_gpu.cu:78-88)
+__device__ __forceinline__ double sine_step(double x, double x1, double y1, double x2, double y2) {
+    if (x <= x1) return y1;
+    if (x >= x2) return y2;
+    double dx = x2 - x1;
+    double dy = y2 - y1;
+    double u = (x - x1) / dx;
+    return y1 + dy * u - (dy / k2Pi) * sin(k2Pi * u);
+}
+
+__device__ __forceinline__ double sgnd(double v) { return (double)((0. < v) - (v < 0.)); }
+
+// ---------------------------------------------------------------------------------------------
+// Carried state of one vehicle (registers).
+struct TireC {
+    double xe, ye, xedot, yedot, omega;
+};
+struct VehC {
+    double x, y, u, v, psi, wz, phi, wx, udot, vdot, crank;
+    int gear;
+};
+// Values of the last RHS evaluation (written back with the state at the end of a window so that
+// GetSimState returns the reference's full SimState).
+struct TireAux {
+    double dOmega, xt, rStat, fx, fy, fz, vsx, vsy, My, engTor;
+};
+struct VehAux {
+    double wxdot, wzdot, dOmega_crank;
+};
+
+// Constant accessor: K(i) reads derived constant i of this thread's vehicle.
+struct KView {
+    const double* base;  // base + i*stride
+    int stride;
+    __device__ __forceinline__ double operator()(int i) const { return base[i * stride]; }
+};
+
+// tmxy_combined (dof18_gpu.cu:243-285)
+__device__ __forceinline__ void tmxy(double& f, double& fos, double s, double df0, double sm, double fm,
+                                     double ss, double fs) {
+    double df0loc = 0.0;
+    double ism = 0.0;
+    if (sm > 0.0) {
+        ism = 1.0 / sm;
+        df0loc = fmax(2.0 * fm * ism, df0);
+    }
+    if (s > 0.0 && df0loc > 0.0) {
+        if (s > ss) {
+            f = fs;
+            fos = fs / s;
+        } else if (s < sm) {  // adhesion
+            double p = df0loc * sm / fm - 2.0;
+            double sn = s * ism;
+            double dn = fma(sn + p, sn, 1.0);
+            double idn = 1.0 / dn;
+            f = df0loc * sm * sn * idn;
+            fos = df0loc * idn;
+        } else {
+            double q = fm * ism;
+            double a = q * q / (df0loc * sm);
+            double sstar = sm + (fm - fs) / (a * (ss - sm));
+            if (sstar <= ss) {
+                if (s <= sstar) {
+                    f = fm - a * (s - sm) * (s - sm);
+                } else {
+                    double b = a * (sstar - sm) / (ss - sstar);
+                    f = fs + b * (ss - s) * (ss - s);
+                }
+            } else {
+                double sn = (s - sm) / (ss - sm);
+                f = fm - (fm - fs) * sn * sn * (3.0 - 2.0 * sn);
+            }
+            fos = f / s;
+        }
+    } else {
+        f = 0.0;
+        fos = 0.0;
+    }
+}
+
+// computeTireRHS, TMeasy (dof18_gpu.cu:379-530). (c, s) = (cos, sin) of this tire's wheel angle;
+// steered says whether the angle may be nonzero. Writes xedot/yedot (left stale when the wheel is
+// off the ground, as in the reference) and the aux values.
+template <bool kSteered>
+__device__ __forceinline__ void tire_rhs_tm(TireC& ts, TireAux& ta, const KView& K, double c, double s) {
+    double fz = ta.fz;
+    const double vsy = ta.vsy;
+    if (fz <= 0) {
+        ts.xe = 0;
+        ts.ye = 0;
+        ts.omega = 0;
+        ta.xt = 0;
+        ta.rStat = K(K_R0);
+        ta.fx = 0;
+        ta.fy = 0;
+        ta.My = 0;
+        return;
+    }
+    const double omega = ts.omega;
+    ta.xt = fz * K(K_INVKT);
+    ta.rStat = K(K_R0) - ta.xt;
+    double r_eff;
+    if (fz <= K(K_FZRD)) {
+        double rdynco = fma(K(K_DRD), fma(fz, K(K_INVPN), -1.0), K(K_RDPN));
+        r_eff = fma(rdynco, ta.xt, ta.rStat);
+    } else {
+        r_eff = fma(K(K_RDCRIT), ta.xt, ta.rStat);
+    }
+    const double vsx = fma(-omega, r_eff, ta.vsx);
+    const double rw = r_eff * fabs(omega);
+    const double vta = rw + 0.01;
+    const double ivta = 1.0 / vta;
+    const double sx = -vsx * ivta;
+    double sy;
+    if (kSteered) {
+        sy = -(vsy * c - vta * s) / (vta * c + vsy * s);
+    } else {
+        sy = -vsy * ivta;
+    }
+    fz = fmin(fz, K(K_PNMAX));
+    const double fzn = fz * K(K_INVPN);
+    const double dfx0 = fzn * fma(-K(K_Q2DFX0), fzn, K(K_Q1DFX0));
+    const double dfy0 = fzn * fma(-K(K_Q2DFY0), fzn, K(K_Q1DFY0));
+    const double fxm = fzn * fma(-K(K_Q2FXM), fzn, K(K_Q1FXM));
+    const double fym = fzn * fma(-K(K_Q2FYM), fzn, K(K_Q1FYM));
+    const double fxs = fzn * fma(-K(K_Q2FXS), fzn, K(K_Q1FXS));
+    const double fys = fzn * fma(-K(K_Q2FYS), fzn, K(K_Q1FYS));
+    const double fzn1 = fzn - 1.0;
+    const double sxm = fma(K(K_DSXM), fzn1, K(K_LSXM));
+    const double sym = fma(K(K_DSYM), fzn1, K(K_LSYM));
+    const double sxs = fma(K(K_DSXS), fzn1, K(K_LSXS));
+    const double sys = fma(K(K_DSYS), fzn1, K(K_LSYS));
+    // hsxn = sxm/(sxm+sym) + (fxm/dfx0)/(fxm/dfx0 + fym/dfy0): one reciprocal for both quotients
+    const double ssum = sxm + sym;
+    const double fxd = fxm * dfy0, fyd = fym * dfx0;
+    const double fsum = fxd + fyd;
+    const double r12 = 1.0 / (ssum * fsum);
+    const double issum = fsum * r12, ifsum = ssum * r12;
+    const double hsxn = fma(sxm, issum, fxd * ifsum);
+    const double hsyn = fma(sym, issum, fyd * ifsum);
+    const double rh = 1.0 / (hsxn * hsyn);
+    const double ihx = hsyn * rh, ihy = hsxn * rh;
+    const double sxn = sx * ihx;
+    const double syn = sy * ihy;
+    const double q = fma(sxn, sxn, syn * syn);
+    double sc, calpha, salpha;
+    if (q > 0) {
+        const double isc = rsqrt(q);
+        sc = q * isc;
+        calpha = sxn * isc;
+        salpha = syn * isc;
+    } else {
+        sc = 0;
+        calpha = kSqrt2Over2;
+        salpha = kSqrt2Over2;
+    }
+    auto hyp = [](double a, double b) { return sqrt(fma(a, a, b * b)); };
+    const double df0 = hyp(dfx0 * calpha * hsxn, dfy0 * salpha * hsyn);
+    const double fm = hyp(fxm * calpha, fym * salpha);
+    const double cax = calpha * ihx, say = salpha * ihy;
+    const double sm = hyp(sxm * cax, sym * say);
+    const double fs = hyp(fxs * calpha, fys * salpha);
+    const double ss = hyp(sxs * cax, sys * say);
+    double f, fos;
+    tmxy(f, fos, sc, df0, sm, fm, ss, fs);
+    (void)f;
+    // rolling resistance: sineStep(vta, 0, 0, 0, 1) == 1 for vta >= 0.01
+    ta.My = -K(K_RR) * fz * ta.rStat * sgnd(omega);
+    const double vtxs = fma(rw, hsxn, 0.01);
+    const double vtys = fma(rw, hsyn, 0.01);
+    const double cx = K(K_CX), cy = K(K_CY), dx = K(K_DX), dy = K(K_DY);
+    const double numx = fma(-vtxs * cx, ts.xe, -fos * vsx);
+    const double numy = fma(-vtys * cy, ts.ye, fos * (sy * vta));
+    const double denx = fma(vtxs, dx, fos), deny = fma(vtys, dy, fos);
+    const double rd = 1.0 / (denx * deny);
+    ts.xedot = numx * (deny * rd);
+    ts.yedot = numy * (denx * rd);
+    const double fxdyn = fma(dx, ts.xedot, cx * ts.xe);
+    const double fydyn = fma(dy, ts.yedot, cy * ts.ye);
+    const double fxstr = fmin(fmax(fma(ts.xe, cx, ts.xedot * dx), -K(K_FXMP2N)), K(K_FXMP2N));
+    const double fystr = fmin(fmax(fma(ts.ye, cy, ts.yedot * dy), -K(K_FYMP2N)), K(K_FYMP2N));
+    const double wx = sine_step(fabs(vsx), 1., 1., 1.5, 0.);
+    const double wy = sine_step(fabs(sy * vta), 1., 1., 1.5, 0.);
+    ta.fx = (wx == 0.0) ? fxdyn : fma(wx, fxstr, (1. - wx) * fxdyn);
+    ta.fy = (wy == 0.0) ? fydyn : fma(wy, fystr, (1. - wy) * fydyn);
+}
+
+// computeCombinedCoulombForce (dof18_gpu.cu:287-303)
+__device__ __forceinline__ void coulomb(double& fx, double& fy, double mu, double vsx, double vsy, double fz,
+                                        double vcoul) {
+    fx = tanh(-2.0 * vsx / vcoul) * fz * mu;
+    fy = tanh(-2.0 * vsy / vcoul) * fz * mu;
+    const double h = sqrt(fma(fx, fx, fy * fy));
+    if (h > fz * mu) {
+        double f = fz * mu / h;
+        fx *= f;
+        fy *= f;
+    }
+}
+
+// computeTireRHS, TMeasyNr (dof18_gpu.cu:532-662)
+template <bool kSteered>
+__device__ __forceinline__ void tire_rhs_nr(TireC& ts, TireAux& ta, const KView& K, double c, double s) {
+    double fz = ta.fz;
+    const double vsy = ta.vsy;
+    if (fz <= 0) {
+        ts.omega = 0;
+        ta.xt = 0;
+        ta.rStat = K(K_R0);
+        ta.fx = 0;
+        ta.fy = 0;
+        ta.My = 0;
+        return;
+    }
+    const double omega = ts.omega;
+    const double mu = K(K_MU);
+    ta.xt = fz * K(K_INVKT);
+    ta.rStat = K(K_R0) - ta.xt;
+    double r_eff;
+    if (fz <= K(K_FZRD)) {
+        double rdynco = fma(K(K_DRD), fma(fz, K(K_INVPN), -1.0), K(K_RDPN));
+        r_eff = fma(rdynco, ta.xt, ta.rStat);
+    } else {
+        r_eff = fma(K(K_RDCRIT), ta.xt, ta.rStat);
+    }
+    const double vsx = fma(-omega, r_eff, ta.vsx);
+    const double vta = r_eff * fabs(omega) + 0.01;
+    double Fx0, Fy0;
+    coulomb(Fx0, Fy0, mu, vsx, vsy, fz, K(K_VCOUL));
+    const double sx = -vsx / vta;
+    double sy;
+    if (kSteered) sy = -(vsy * c - vta * s) / (vta * c + vsy * s);
+    else sy = -vsy / vta;
+    fz = fmin(fz, K(K_PNMAX));
+    const double fzn = fz * K(K_INVPN);
+    const double dfx0 = fzn * fma(-K(K_Q2DFX0), fzn, K(K_Q1DFX0));
+    const double dfy0 = fzn * fma(-K(K_Q2DFY0), fzn, K(K_Q1DFY0));
+    const double fxm = fzn * fma(-K(K_Q2FXM), fzn, K(K_Q1FXM));
+    const double fym = fzn * fma(-K(K_Q2FYM), fzn, K(K_Q1FYM));
+    const double fxs = fzn * fma(-K(K_Q2FXS), fzn, K(K_Q1FXS));
+    const double fys = fzn * fma(-K(K_Q2FYS), fzn, K(K_Q1FYS));
+    const double fzn1 = fzn - 1.0;
+    const double sxm = fma(K(K_DSXM), fzn1, K(K_LSXM));
+    const double sym = fma(K(K_DSYM), fzn1, K(K_LSYM));
+    const double sxs = fma(K(K_DSXS), fzn1, K(K_LSXS));
+    const double sys = fma(K(K_DSYS), fzn1, K(K_LSYS));
+    const double frblend = sine_step(fabs(ta.vsx), K(K_FRB0), 0., K(K_FRB1), 1.);
+    const double q = fma(sx, sx, sy * sy);
+    double sc, calpha, salpha, isc = 0;
+    if (q > 0) {
+        isc = rsqrt(q);
+        sc = q * isc;
+        calpha = sx * isc;
+        salpha = sy * isc;
+    } else {
+        sc = 0;
+        calpha = kSqrt2Over2;
+        salpha = kSqrt2Over2;
+    }
+    auto hyp = [](double a, double b) { return sqrt(fma(a, a, b * b)); };
+    const double df0 = hyp(dfx0 * calpha, dfy0 * salpha);
+    const double fm = mu * hyp(fxm * calpha, fym * salpha);
+    const double sm = mu * hyp(sxm * calpha, sym * salpha);
+    const double fs = mu * hyp(fxs * calpha, fys * salpha);
+    const double ss = mu * hyp(sxs * calpha, sys * salpha);
+    double f, fos;
+    tmxy(f, fos, sc, df0, sm, fm, ss, fs);
+    double Fx = 0., Fy = 0.;
+    if (sc > 0.) {
+        Fx = f * sx * isc;
+        Fy = f * sy * isc;
+    }
+    ta.fx = fma(1.0 - frblend, Fx0, frblend * Fx);
+    ta.fy = fma(1.0 - frblend, Fy0, frblend * Fy);
+    ta.My = -K(K_RR) * fz * ta.rStat * tanh(omega);
+}
+
+// differentialSplit (dof18_gpu.cu:42-69) with max_bias = 2.
+__device__ __forceinline__ void diff_split(double torque, double wl, double wr, double& tl, double& tr) {
+    double diff = fabs(wl - wr);
+    double alpha;
+    if (diff > 0.5) alpha = 2.0 / 3.0;          // bias = max_bias = 2
+    else if (diff > 0.25) {
+        double bias = 4 * (2.0 - 1) * diff + (2 - 2.0);
+        alpha = bias / (1 + bias);
+    } else alpha = 0.5;                          // bias = 1
+    double slow = alpha * torque;
+    double fast = torque - slow;
+    if (fabs(wl) < fabs(wr)) {
+        tl = slow;
+        tr = fast;
+    } else {
+        tl = fast;
+        tr = slow;
+    }
+}
+
+// driveTorque (dof18_gpu.cu:15-38)
+__device__ __forceinline__ double drive_torque(const ClassDev18& C, double throttle, double w) {
+    if (C.throttleMod) {
+        double t = map_y_scaled(C.pt, w, throttle);
+        return t + map_y(C.loss, w);
+    }
+    return fma(map_y(C.pt, w), throttle, map_y(C.loss, w));
+}
+
+// computePowertrainRHS (dof18_gpu.cu:664-839). Mutates crank (no converter) and gear.
+template <bool kNr>
+__device__ __forceinline__ void powertrain_rhs(VehC& v, VehAux& va, TireC* ts, TireAux* ta, const KView& K,
+                                               const ClassDev18& C, double throttle, double braking) {
+    double torque_t;
+    const int g = v.gear;
+    if (C.tcbool) {
+        bool reverse = false;
+        const double omega_t = 0.25 * (((ts[0].omega + ts[1].omega) + ts[2].omega) + ts[3].omega);
+        const double omega_out = omega_t * C.invgear[g];
+        const double omega_in = v.crank;
+        double sr, cf, tr;
+        if ((omega_out < 1e-9) || (omega_in < 1e-9)) {
+            sr = 0;
+        } else {
+            sr = omega_out / omega_in;
+            if (sr > 1.) {
+                sr = 1. - (sr - 1.);
+                reverse = true;
+            }
+            if (sr < 0) sr = 0;
+        }
+        cf = map_y(C.cf, sr);
+        tr = map_y(C.tr, sr);
+        const double r = omega_in / cf;
+        double torque_in = -(r * r);
+        if (reverse) torque_in = -torque_in;
+        const double torque_out = reverse ? -torque_in : -tr * torque_in;
+        torque_t = torque_out * C.invgear[g];
+        if (v.u < 1e-9 && torque_t < 0) torque_t = 0;
+        va.dOmega_crank = K(K_INVCI) * (drive_torque(C, throttle, v.crank) + torque_in);
+        if (omega_out > C.up[g]) {
+            if (g < C.noGears - 1) v.gear = g + 1;
+        } else if (omega_out < C.down[g]) {
+            if (g > 0) v.gear = g - 1;
+        }
+    } else {
+        v.crank = 0.25 * (((ts[0].omega + ts[1].omega) + ts[2].omega) + ts[3].omega) * C.invgear[g];
+        torque_t = drive_torque(C, throttle, v.crank) * C.invgear[g];
+        if (v.u < 1e-9 && torque_t < 0) torque_t = 0;
+        if (v.crank > C.up[g]) {
+            if (g < C.noGears - 1) v.gear = g + 1;
+        } else if (v.crank < C.down[g]) {
+            if (g > 0) v.gear = g - 1;
+        }
+    }
+    double tf, trr;
+    if (C.driveType) {
+        tf = torque_t * 0.5;
+        trr = torque_t * 0.5;
+    } else if (C.whichWheels) {
+        tf = 0;
+        trr = torque_t;
+    } else {
+        tf = torque_t;
+        trr = 0;
+    }
+    diff_split(tf, ts[0].omega, ts[1].omega, ta[0].engTor, ta[1].engTor);
+    diff_split(trr, ts[2].omega, ts[3].omega, ta[2].engTor, ta[3].engTor);
+    const double brake = K(K_MAXBRAKE) * braking;
+    const double ijw = K(K_INVJW);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        ta[k].dOmega = ijw * (fma(-sgnd(ts[k].omega), brake, ta[k].engTor + ta[k].My) - ta[k].fx * ta[k].rStat);
+}
+
+// One right-hand-side evaluation (rhsFun, dof18_halfImplicit_gpu.cu:685-729) followed by the
+// half-implicit update (:913-946). steering/throttle/braking are this step's driver inputs.
+template <bool kNr>
+__device__ __forceinline__ void step18(VehC& v, VehAux& va, TireC* ts, TireAux* ta, const KView& K,
+                                       const ClassDev18& C, double steering, double throttle, double braking,
+                                       double dt) {
+    // computeTireLoads (dof18_gpu.cu:305-340); udot/vdot are the previous step's accelerations.
+    {
+        const double lat = fma(v.wz, v.u, v.vdot);
+        const double lon = fma(-v.wz, v.v, v.udot);
+        const double Z4 = K(K_Z4) * lon;
+        const double Z2f = K(K_Z2F) * lat;
+        const double Z3f = fma(K(K_Z3FK), v.phi, K(K_Z3FB) * v.wx);
+        const double Z2r = K(K_Z2R) * lat;
+        const double Z3r = fma(K(K_Z3RK), v.phi, K(K_Z3RB) * v.wx);
+        const double Af = K(K_Z1F) - Z4, Bf = Z2f + Z3f;
+        const double Ar = K(K_Z1R) + Z4, Br = Z2r + Z3r;
+        ta[0].fz = fmax(Af - Bf, 0.0);
+        ta[1].fz = fmax(Af + Bf, 0.0);
+        ta[2].fz = fmax(Ar - Br, 0.0);
+        ta[3].fz = fmax(Ar + Br, 0.0);
+    }
+    // vehToTireTransform (dof18_gpu.cu:71-109)
+    double delta;
+    if (C.nonLinearSteer) delta = map_y(C.steer, steering);
+    else delta = steering * K(K_MAXSTEER);
+    double cd = 1.0, sd = 0.0;
+    if (delta != 0.0) sincos(delta, &sd, &cd);
+    {
+        const double vsyf = fma(v.wz, K(K_A), v.v);
+        const double vsyr = fma(-v.wz, K(K_B), v.v);
+        const double wcf = v.wz * K(K_CF2), wcr = v.wz * K(K_CR2);
+        ta[0].vsy = vsyf;
+        ta[1].vsy = vsyf;
+        ta[0].vsx = fma(v.u - wcf, cd, vsyf * sd);
+        ta[1].vsx = fma(v.u + wcf, cd, vsyf * sd);
+        ta[2].vsy = vsyr;
+        ta[3].vsy = vsyr;
+        ta[2].vsx = v.u - wcr;
+        ta[3].vsx = v.u + wcr;
+    }
+    if (kNr) {
+        tire_rhs_nr<true>(ts[0], ta[0], K, cd, sd);
+        tire_rhs_nr<true>(ts[1], ta[1], K, cd, sd);
+        tire_rhs_nr<false>(ts[2], ta[2], K, 1.0, 0.0);
+        tire_rhs_nr<false>(ts[3], ta[3], K, 1.0, 0.0);
+    } else {
+        tire_rhs_tm<true>(ts[0], ta[0], K, cd, sd);
+        tire_rhs_tm<true>(ts[1], ta[1], K, cd, sd);
+        tire_rhs_tm<false>(ts[2], ta[2], K, 1.0, 0.0);
+        tire_rhs_tm<false>(ts[3], ta[3], K, 1.0, 0.0);
+    }
+    powertrain_rhs<kNr>(v, va, ts, ta, K, C, throttle, braking);
+    // tireToVehTransform (dof18_gpu.cu:152-185): front forces into the vehicle frame
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const double fx = ta[k].fx, fy = ta[k].fy;
+        ta[k].fx = fma(fx, cd, -fy * sd);
+        ta[k].fy = fma(fx, sd, fy * cd);
+    }
+    // computeVehRHS (dof18_gpu.cu:1017-1068)
+    {
+        const double fx0 = ta[0].fx, fx1 = ta[1].fx, fx2 = ta[2].fx, fx3 = ta[3].fx;
+        const double fy0 = ta[0].fy, fy1 = ta[1].fy, fy2 = ta[2].fy, fy3 = ta[3].fy;
+        const double wu = v.wz * v.u;
+        const double fyf = fy0 + fy1, fyr = fy2 + fy3;
+        const double E1 = fma(-K(K_MT), wu, fyf + fyr);
+        const double E2 = fma(K(K_E2WU), wu,
+                              fma(fx3 - fx2, K(K_CR2), fma(fx1 - fx0, K(K_CF2), fma(fyf, K(K_A), -fyr * K(K_B)))));
+        const double E3 = fma(K(K_E3WU), wu, fma(K(K_E3PHI), v.phi, K(K_E3WX) * v.wx));
+        const double sfx = ((fx0 + fx1) + fx2) + fx3;
+        v.udot = fma(K(K_INVMT), fma(K(K_UWZ2), v.wz * v.wz, fma(-K(K_UWZWX), v.wz * v.wx, sfx)), v.wz * v.v);
+        v.vdot = fma(K(K_CV1), E1, fma(K(K_CV2), E2, K(K_CV3) * E3));
+        va.wxdot = fma(K(K_CV3), E1, fma(K(K_CX2), E2, K(K_CX3) * E3));
+        va.wzdot = fma(K(K_CV2), E1, fma(K(K_CZ2), E2, K(K_CX2) * E3));
+    }
+    // half-implicit update (dof18_halfImplicit_gpu.cu:913-946)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (!kNr) {
+            ts[k].xe = fma(ts[k].xedot, dt, ts[k].xe);
+            ts[k].ye = fma(ts[k].yedot, dt, ts[k].ye);
+        }
+        ts[k].omega = fma(ta[k].dOmega, dt, ts[k].omega);
+    }
+    if (C.tcbool) v.crank = fma(va.dOmega_crank, dt, v.crank);
+    v.u = fma(v.udot, dt, v.u);
+    v.v = fma(v.vdot, dt, v.v);
+    v.wx = fma(va.wxdot, dt, v.wx);
+    v.wz = fma(va.wzdot, dt, v.wz);
+    double sp, cp;
+    sincos(v.psi, &sp, &cp);
+    v.x = fma(fma(v.u, cp, -v.v * sp), dt, v.x);
+    v.y = fma(fma(v.u, sp, v.v * cp), dt, v.y);
+    v.psi = fma(v.wz, dt, v.psi);
+    v.phi = fma(v.wx, dt, v.phi);
+}
+
+}  // namespace lfdm

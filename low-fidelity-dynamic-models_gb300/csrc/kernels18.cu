@@ -1,0 +1,441 @@
+// CUDA kernels of the 18-DOF stepper: derived constants, state layout transposes and the window
+// stepping kernel (the GB300 counterpart of the reference's Integrate kernels,
+// 18dof-gpu/dof18_halfImplicit_gpu.cu:882-1250 and .cuh:454-640).
+//
+// Layout in HBM (n vehicles, npad = row stride):
+//   K  [K18_COUNT][npad] FP64 derived per-vehicle constants (prepare18_kernel)
+//   S  [LFDM_S_COUNT][npad] FP64 state, one coalesced row per field
+//   rows  per-vehicle driver tables, {t, steering, throttle, braking} rows, 32-byte aligned
+//   resp  [sample][13][n] FP64 response of one window (the reference's device response layout)
+// Each thread integrates one vehicle over a whole window with the carried state in registers;
+// per-block copies of the class tables and of the block's derived constants live in shared
+// memory.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "dof18_device.cuh"
+#include "kernels.h"
+
+namespace lfdm {
+
+static_assert(sizeof(ClassDev18) % 16 == 0, "ClassDev18 must be a multiple of 16 bytes");
+
+int k18_count() { return K18_COUNT; }
+size_t class_dev18_size() { return sizeof(ClassDev18); }
+
+// ---------------------------------------------------------------------------------------------
+// derived constants
+
+__global__ void prepare18_kernel(const double* __restrict__ P, int n, int npad, double* __restrict__ K) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* p = P + (size_t)i * LFDM_P_COUNT;
+    auto put = [&](int k, double v) { K[(size_t)k * npad + i] = v; };
+    const double a = p[LFDM_P_A], b = p[LFDM_P_B], h = p[LFDM_P_H], m = p[LFDM_P_M];
+    const double jz = p[LFDM_P_JZ], jx = p[LFDM_P_JX], jxz = p[LFDM_P_JXZ];
+    const double cf = p[LFDM_P_CF], cr = p[LFDM_P_CR], muf = p[LFDM_P_MUF], mur = p[LFDM_P_MUR];
+    const double hrcf = p[LFDM_P_HRCF], hrcr = p[LFDM_P_HRCR];
+    const double krof = p[LFDM_P_KROF], kror = p[LFDM_P_KROR], brof = p[LFDM_P_BROF], bror = p[LFDM_P_BROR];
+    const double r0 = p[LFDM_P_R0], pn = p[LFDM_P_PN];
+    put(K_A, a);
+    put(K_B, b);
+    put(K_CF2, cf / 2.);
+    put(K_CR2, cr / 2.);
+    put(K_MAXSTEER, p[LFDM_P_MAXSTEER]);
+    // computeTireLoads (dof18_gpu.cu:305-340), huf = hur = r0
+    const double huf = r0, hur = r0;
+    put(K_Z1F, (m * kG * b) / (2. * (a + b)) + (muf * kG) / 2.);
+    put(K_Z2F, (muf * huf) / cf + m * b * (h - hrcf) / (cf * (a + b)));
+    put(K_Z3FK, krof / cf);
+    put(K_Z3FB, brof / cf);
+    put(K_Z4, (m * h + muf * huf + mur * hur) / (2. * (a + b)));
+    put(K_Z1R, (m * kG * a) / (2. * (a + b)) + (mur * kG) / 2.);
+    put(K_Z2R, (mur * hur) / cr + m * a * (h - hrcr) / (cr * (a + b)));
+    put(K_Z3RK, kror / cr);
+    put(K_Z3RB, bror / cr);
+    // computeVehRHS (dof18_gpu.cu:1017-1068): the 3x3 solve as coefficients of E1, E2, E3
+    const double mt = m + 2 * (muf + mur);
+    const double hrc = (hrcf * b + hrcr * a) / (a + b);
+    const double A1 = mur * b - muf * a;
+    const double A2 = jx + m * hrc * hrc;
+    const double A3 = hrc * m;
+    const double denom = A2 * A1 * A1 - 2. * A1 * A3 * jxz + jz * A3 * A3 + mt * jxz * jxz - A2 * jz * mt;
+    put(K_MT, mt);
+    put(K_INVMT, 1 / mt);
+    put(K_E2WU, -muf * a + mur * b);
+    put(K_E3PHI, m * kG * hrc - (krof + kror));
+    put(K_E3WX, -(brof + bror));
+    put(K_E3WU, hrc * m);
+    put(K_UWZ2, -mur * b + muf * a);
+    put(K_UWZWX, 2. * hrc * m);
+    put(K_CV1, (jxz * jxz - A2 * jz) / denom);
+    put(K_CV2, (A3 * jxz - A1 * A2) / denom);
+    put(K_CV3, (A1 * jxz - A3 * jz) / denom);
+    put(K_CX2, (jxz * mt - A1 * A3) / denom);
+    put(K_CX3, (A1 * A1 - jz * mt) / denom);
+    put(K_CZ2, (A3 * A3 - A2 * mt) / denom);
+    put(K_INVCI, 1. / p[LFDM_P_CRANKINERTIA]);
+    put(K_MAXBRAKE, p[LFDM_P_MAXBRAKETORQUE]);
+    put(K_INVJW, 1 / p[LFDM_P_JW]);
+    // computeTireRHS (dof18_gpu.cu:379-530); InterpQ(fz,w1,w2,pn) = fzn*(Q1 - Q2*fzn),
+    // InterpL(fz,w1,w2,pn) = w1 + (w2-w1)*(fzn-1) with fzn = fz/pn (utils_gpu.cuh:86-93)
+    put(K_R0, r0);
+    put(K_INVKT, 1. / p[LFDM_P_KT]);
+    put(K_INVPN, 1. / pn);
+    put(K_PNMAX, p[LFDM_P_PNMAX]);
+    put(K_FZRD, p[LFDM_P_FZRDYNCO]);
+    put(K_RDPN, p[LFDM_P_RDYNCOPN]);
+    put(K_DRD, p[LFDM_P_RDYNCOP2N] - p[LFDM_P_RDYNCOPN]);
+    put(K_RDCRIT, p[LFDM_P_RDYNCOCRIT]);
+    auto q = [&](int k1, int k2, double w1, double w2) {
+        put(k1, 2. * w1 - 0.5 * w2);
+        put(k2, w1 - 0.5 * w2);
+    };
+    q(K_Q1DFX0, K_Q2DFX0, p[LFDM_P_DFX0PN], p[LFDM_P_DFX0P2N]);
+    q(K_Q1DFY0, K_Q2DFY0, p[LFDM_P_DFY0PN], p[LFDM_P_DFY0P2N]);
+    q(K_Q1FXM, K_Q2FXM, p[LFDM_P_FXMPN], p[LFDM_P_FXMP2N]);
+    q(K_Q1FYM, K_Q2FYM, p[LFDM_P_FYMPN], p[LFDM_P_FYMP2N]);
+    q(K_Q1FXS, K_Q2FXS, p[LFDM_P_FXSPN], p[LFDM_P_FXSP2N]);
+    q(K_Q1FYS, K_Q2FYS, p[LFDM_P_FYSPN], p[LFDM_P_FYSP2N]);
+    auto l = [&](int k1, int k2, double w1, double w2) {
+        put(k1, w1);
+        put(k2, w2 - w1);
+    };
+    l(K_LSXM, K_DSXM, p[LFDM_P_SXMPN], p[LFDM_P_SXMP2N]);
+    l(K_LSYM, K_DSYM, p[LFDM_P_SYMPN], p[LFDM_P_SYMP2N]);
+    l(K_LSXS, K_DSXS, p[LFDM_P_SXSPN], p[LFDM_P_SXSP2N]);
+    l(K_LSYS, K_DSYS, p[LFDM_P_SYSPN], p[LFDM_P_SYSP2N]);
+    put(K_CX, p[LFDM_P_CX]);
+    put(K_CY, p[LFDM_P_CY]);
+    put(K_DX, p[LFDM_P_DX]);
+    put(K_DY, p[LFDM_P_DY]);
+    put(K_FXMP2N, p[LFDM_P_FXMP2N]);
+    put(K_FYMP2N, p[LFDM_P_FYMP2N]);
+    put(K_RR, p[LFDM_P_RR]);
+    put(K_MU, p[LFDM_P_MU]);
+    put(K_VCOUL, p[LFDM_P_VCOULOMB]);
+    put(K_FRB0, p[LFDM_P_FRBLEND_BEGIN]);
+    put(K_FRB1, p[LFDM_P_FRBLEND_END]);
+}
+
+cudaError_t launch_prepare18(const double* params_dev, int n, int npad, double* K_dev, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    prepare18_kernel<<<(n + 127) / 128, 128, 0, stream>>>(params_dev, n, npad, K_dev);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// state transposes
+
+__global__ void aos_to_soa_kernel(const double* __restrict__ aos, int n, int npad, double* __restrict__ soa) {
+    const size_t total = (size_t)n * LFDM_S_COUNT;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t v = i / LFDM_S_COUNT, f = i % LFDM_S_COUNT;
+        soa[f * npad + v] = aos[i];
+    }
+}
+__global__ void soa_to_aos_kernel(const double* __restrict__ soa, int n, int npad, double* __restrict__ aos) {
+    const size_t total = (size_t)n * LFDM_S_COUNT;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t v = i / LFDM_S_COUNT, f = i % LFDM_S_COUNT;
+        aos[i] = soa[f * npad + v];
+    }
+}
+static int grid_for(size_t total) {
+    size_t g = (total + 255) / 256;
+    return (int)(g > 152 * 32 ? 152 * 32 : (g == 0 ? 1 : g));
+}
+cudaError_t launch_states_to_soa(const double* aos, int n, int npad, double* soa, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    aos_to_soa_kernel<<<grid_for((size_t)n * LFDM_S_COUNT), 256, 0, stream>>>(aos, n, npad, soa);
+    return cudaGetLastError();
+}
+cudaError_t launch_states_to_aos(const double* soa, int n, int npad, double* aos, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    soa_to_aos_kernel<<<grid_for((size_t)n * LFDM_S_COUNT), 256, 0, stream>>>(soa, n, npad, aos);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------
+// class tables
+
+static void build_map(const double (*pts)[2], int n, MapDev& m) {
+    std::memset(&m, 0, sizeof(m));
+    m.n = n;
+    for (int k = 0; k < n; ++k) {
+        m.x[k] = pts[k][0];
+        m.y[k] = pts[k][1];
+    }
+    for (int k = 0; k + 1 < n; ++k) {
+        m.invdx[k] = 1.0 / (m.x[k + 1] - m.x[k]);
+        m.dy[k] = m.y[k + 1] - m.y[k];
+    }
+}
+
+void build_class_dev18(const lfdm_class18& c, ClassDev18* out) {
+    std::memset(out, 0, sizeof(*out));
+    out->nonLinearSteer = c.nonLinearSteer;
+    out->tcbool = c.tcbool;
+    out->throttleMod = c.throttleMod;
+    out->driveType = c.driveType;
+    out->whichWheels = c.whichWheels;
+    out->noGears = c.noGears;
+    for (int g = 0; g < c.noGears && g < LFDM_MAX_GEARS; ++g) {
+        out->gear[g] = c.gearRatios[g];
+        out->invgear[g] = 1.0 / c.gearRatios[g];
+        out->down[g] = c.shiftMap[g][0];
+        out->up[g] = c.shiftMap[g][1];
+    }
+    build_map(c.steerMap, c.steerMapSize, out->steer);
+    build_map(c.powertrainMap, c.powertrainMapSize, out->pt);
+    build_map(c.lossesMap, c.lossesMapSize, out->loss);
+    build_map(c.CFmap, c.CFmapSize, out->cf);
+    build_map(c.TRmap, c.TRmapSize, out->tr);
+}
+
+// ---------------------------------------------------------------------------------------------
+// window kernel
+
+constexpr int kMaxSmemClasses = 8;
+
+size_t window18_smem(int threads, int nclasses) {
+    const size_t cls = nclasses <= kMaxSmemClasses ? (size_t)nclasses * sizeof(ClassDev18) : 0;
+    return cls + (size_t)K18_COUNT * threads * sizeof(double);
+}
+
+struct DriverCursor {
+    const double* rows;
+    int len;
+    int r;         // first row with time >= t (valid while rows[0].t < t < rows[len-1].t)
+    double tfirst, tlast;
+};
+
+__device__ __forceinline__ void driver_begin(DriverCursor& c, const double* rows, int len, double t) {
+    c.rows = rows;
+    c.len = len;
+    c.tfirst = __ldg(rows);
+    c.tlast = __ldg(rows + 4 * (len - 1));
+    int l = 0, h = len;
+    while (l < h) {
+        int mid = (l + h) >> 1;
+        if (t <= __ldg(rows + 4 * mid)) h = mid;
+        else l = mid + 1;
+    }
+    c.r = l;
+}
+
+// GetDriverInput (utils/utils_gpu.cu:34-56) with a monotone cursor in place of the per-step
+// binary search; the segment found is the same lower_bound segment for non-decreasing tables.
+__device__ __forceinline__ void driver_at(DriverCursor& c, double t, double& st, double& th, double& br) {
+    if (t <= c.tfirst) {
+        st = __ldg(c.rows + 1);
+        th = __ldg(c.rows + 2);
+        br = __ldg(c.rows + 3);
+        return;
+    }
+    if (t >= c.tlast) {
+        const double* L = c.rows + 4 * (c.len - 1);
+        st = __ldg(L + 1);
+        th = __ldg(L + 2);
+        br = __ldg(L + 3);
+        return;
+    }
+    while (__ldg(c.rows + 4 * c.r) < t) ++c.r;
+    while (c.r > 1 && __ldg(c.rows + 4 * (c.r - 1)) >= t) --c.r;  // t moved backwards (new window)
+    const double2* L = reinterpret_cast<const double2*>(c.rows + 4 * (c.r - 1));
+    const double2 L01 = __ldg(L), L23 = __ldg(L + 1), R01 = __ldg(L + 2), R23 = __ldg(L + 3);
+    const double tbar = (t - L01.x) / (R01.x - L01.x);
+    st = L01.y + tbar * (R01.y - L01.y);
+    th = L23.x + tbar * (R23.x - L23.x);
+    br = L23.y + tbar * (R23.y - L23.y);
+}
+
+template <bool kNr, int kCtl, bool kOut>
+__global__ void __launch_bounds__(128) window18_kernel(const Window18 w) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int tid = threadIdx.x;
+    const bool cls_smem = w.nclasses <= kMaxSmemClasses;
+    ClassDev18* cls = reinterpret_cast<ClassDev18*>(smem);
+    double* ks = reinterpret_cast<double*>(smem + (cls_smem ? (size_t)w.nclasses * sizeof(ClassDev18) : 0));
+    if (cls_smem) {
+        const int4* src = reinterpret_cast<const int4*>(w.classes);
+        int4* dst = reinterpret_cast<int4*>(smem);
+        const int words = (int)(w.nclasses * sizeof(ClassDev18) / 16);
+        for (int i = tid; i < words; i += blockDim.x) dst[i] = __ldg(src + i);
+    }
+    const int vid = blockIdx.x * blockDim.x + tid;
+    const bool active = vid < w.n;
+    if (active) {
+#pragma unroll 4
+        for (int k = 0; k < K18_COUNT; ++k) ks[k * blockDim.x + tid] = __ldg(w.K + (size_t)k * w.npad + vid);
+    }
+    __syncthreads();
+    if (!active) return;
+
+    const KView K{ks + tid, (int)blockDim.x};
+    const int ci = __ldg(w.class_of + vid);
+    const ClassDev18& C = cls_smem ? cls[ci] : w.classes[ci];
+    const size_t np = (size_t)w.npad;
+    double* S = w.S + vid;
+
+    VehC v;
+    VehAux va;
+    TireC ts[4];
+    TireAux ta[4];
+    v.x = S[LFDM_S_X * np];
+    v.y = S[LFDM_S_Y * np];
+    v.u = S[LFDM_S_U * np];
+    v.v = S[LFDM_S_V * np];
+    v.psi = S[LFDM_S_PSI * np];
+    v.wz = S[LFDM_S_WZ * np];
+    v.phi = S[LFDM_S_PHI * np];
+    v.wx = S[LFDM_S_WX * np];
+    v.udot = S[LFDM_S_UDOT * np];
+    v.vdot = S[LFDM_S_VDOT * np];
+    v.crank = S[LFDM_S_CRANKOMEGA * np];
+    v.gear = (int)S[LFDM_S_CURRENT_GR * np];
+    va.wxdot = S[LFDM_S_WXDOT * np];
+    va.wzdot = S[LFDM_S_WZDOT * np];
+    va.dOmega_crank = S[LFDM_S_DOMEGA_CRANK * np];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const size_t b = (size_t)(LFDM_S_TIRE0 + k * LFDM_S_TIRE_STRIDE) * np;
+        ts[k].xe = S[b + LFDM_T_XE * np];
+        ts[k].ye = S[b + LFDM_T_YE * np];
+        ts[k].xedot = S[b + LFDM_T_XEDOT * np];
+        ts[k].yedot = S[b + LFDM_T_YEDOT * np];
+        ts[k].omega = S[b + LFDM_T_OMEGA * np];
+        ta[k].dOmega = S[b + LFDM_T_DOMEGA * np];
+        ta[k].xt = S[b + LFDM_T_XT * np];
+        ta[k].rStat = S[b + LFDM_T_RSTAT * np];
+        ta[k].fx = S[b + LFDM_T_FX * np];
+        ta[k].fy = S[b + LFDM_T_FY * np];
+        ta[k].fz = S[b + LFDM_T_FZ * np];
+        ta[k].vsx = S[b + LFDM_T_VSX * np];
+        ta[k].vsy = S[b + LFDM_T_VSY * np];
+        ta[k].My = S[b + LFDM_T_MY * np];
+        ta[k].engTor = S[b + LFDM_T_ENGTOR * np];
+    }
+
+    DriverCursor cur;
+    double steer = w.steer, thr = w.thr, brk = w.brk;
+    if (kCtl == CTL_TABLE) {
+        driver_begin(cur, w.rows + 4 * __ldg(w.row_off + vid), __ldg(w.row_len + vid), w.t0);
+    } else if (kCtl == CTL_ARRAY) {
+        steer = __ldg(w.ctl + vid);
+        thr = __ldg(w.ctl + np + vid);
+        brk = __ldg(w.ctl + 2 * np + vid);
+    }
+    int next_k = 0;
+    int next_step = (kOut && w.nsamples > 0) ? __ldg(w.sample_steps) : -1;
+
+    double t = w.t0;
+    const double dt = w.dt;
+    for (int s = 0; s < w.nsteps; ++s) {
+        if (kCtl == CTL_TABLE) {
+            driver_at(cur, t, steer, thr, brk);
+        } else if (kCtl == CTL_SCHEDULE) {
+            steer = __ldg(w.sched + 3 * s);
+            thr = __ldg(w.sched + 3 * s + 1);
+            brk = __ldg(w.sched + 3 * s + 2);
+        }
+        step18<kNr>(v, va, ts, ta, K, C, steer, thr, brk, dt);
+        t += dt;
+        if (kOut && s + 1 == next_step) {
+            double* r = w.resp + (size_t)next_k * LFDM18_RESP_CHANNELS * w.n + vid;
+            const size_t n = (size_t)w.n;
+            r[0 * n] = t;
+            r[1 * n] = v.x;
+            r[2 * n] = v.y;
+            r[3 * n] = v.u;
+            r[4 * n] = v.v;
+            r[5 * n] = v.phi;
+            r[6 * n] = v.psi;
+            r[7 * n] = v.wx;
+            r[8 * n] = v.wz;
+            r[9 * n] = ts[0].omega;
+            r[10 * n] = ts[1].omega;
+            r[11 * n] = ts[2].omega;
+            r[12 * n] = ts[3].omega;
+            ++next_k;
+            next_step = next_k < w.nsamples ? __ldg(w.sample_steps + next_k) : -1;
+        }
+    }
+
+    S[LFDM_S_X * np] = v.x;
+    S[LFDM_S_Y * np] = v.y;
+    S[LFDM_S_U * np] = v.u;
+    S[LFDM_S_V * np] = v.v;
+    S[LFDM_S_PSI * np] = v.psi;
+    S[LFDM_S_WZ * np] = v.wz;
+    S[LFDM_S_PHI * np] = v.phi;
+    S[LFDM_S_WX * np] = v.wx;
+    S[LFDM_S_UDOT * np] = v.udot;
+    S[LFDM_S_VDOT * np] = v.vdot;
+    S[LFDM_S_WXDOT * np] = va.wxdot;
+    S[LFDM_S_WZDOT * np] = va.wzdot;
+    S[LFDM_S_CRANKOMEGA * np] = v.crank;
+    S[LFDM_S_DOMEGA_CRANK * np] = va.dOmega_crank;
+    S[LFDM_S_CURRENT_GR * np] = (double)v.gear;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const size_t b = (size_t)(LFDM_S_TIRE0 + k * LFDM_S_TIRE_STRIDE) * np;
+        S[b + LFDM_T_XE * np] = ts[k].xe;
+        S[b + LFDM_T_YE * np] = ts[k].ye;
+        S[b + LFDM_T_XEDOT * np] = ts[k].xedot;
+        S[b + LFDM_T_YEDOT * np] = ts[k].yedot;
+        S[b + LFDM_T_OMEGA * np] = ts[k].omega;
+        S[b + LFDM_T_DOMEGA * np] = ta[k].dOmega;
+        S[b + LFDM_T_XT * np] = ta[k].xt;
+        S[b + LFDM_T_RSTAT * np] = ta[k].rStat;
+        S[b + LFDM_T_FX * np] = ta[k].fx;
+        S[b + LFDM_T_FY * np] = ta[k].fy;
+        S[b + LFDM_T_FZ * np] = ta[k].fz;
+        S[b + LFDM_T_VSX * np] = ta[k].vsx;
+        S[b + LFDM_T_VSY * np] = ta[k].vsy;
+        S[b + LFDM_T_MY * np] = ta[k].My;
+        S[b + LFDM_T_ENGTOR * np] = ta[k].engTor;
+    }
+    if (w.status) {
+        const bool bad = !(isfinite(v.x) && isfinite(v.y) && isfinite(v.u) && isfinite(v.v) && isfinite(v.psi) &&
+                           isfinite(v.wz) && isfinite(ts[0].omega) && isfinite(ts[1].omega) &&
+                           isfinite(ts[2].omega) && isfinite(ts[3].omega));
+        if (bad) w.status[vid] |= 1u;
+    }
+}
+
+template <bool kNr, int kCtl, bool kOut>
+static cudaError_t launch_t(const Window18& w, cudaStream_t stream) {
+    const int threads = w.threads;
+    const size_t smem = window18_smem(threads, w.nclasses);
+    auto kern = window18_kernel<kNr, kCtl, kOut>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int blocks = (w.n + threads - 1) / threads;
+    kern<<<blocks, threads, smem, stream>>>(w);
+    return cudaGetLastError();
+}
+
+template <bool kNr, int kCtl>
+static cudaError_t launch_o(const Window18& w, cudaStream_t s) {
+    return (w.resp && w.nsamples > 0) ? launch_t<kNr, kCtl, true>(w, s) : launch_t<kNr, kCtl, false>(w, s);
+}
+template <bool kNr>
+static cudaError_t launch_c(const Window18& w, cudaStream_t s) {
+    switch (w.ctl_mode) {
+        case CTL_TABLE: return launch_o<kNr, CTL_TABLE>(w, s);
+        case CTL_SCALAR: return launch_o<kNr, CTL_SCALAR>(w, s);
+        case CTL_SCHEDULE: return launch_o<kNr, CTL_SCHEDULE>(w, s);
+        default: return launch_o<kNr, CTL_ARRAY>(w, s);
+    }
+}
+
+cudaError_t launch_window18(const Window18& w, cudaStream_t stream) {
+    if (w.n <= 0 || w.nsteps <= 0) return cudaSuccess;
+    if (w.threads <= 0 || w.threads > 128 || (w.threads & 31)) return cudaErrorInvalidValue;
+    return w.tire_nr ? launch_c<true>(w, stream) : launch_c<false>(w, stream);
+}
+
+}  // namespace lfdm

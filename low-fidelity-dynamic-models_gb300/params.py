@@ -125,10 +125,6 @@ def vehicle_from_json(veh, tire, tire_type: int = TIRE_TMEASY) -> tuple[Class18,
             if k in ("cx", "cy", "dx", "dy"):
                 continue
             p[P[k.lower()]] = float(t[k])
-        p[P["mu"]] = float(t.get("mu", p[P["mu"]]))
-        for jk, pk in (("vCoulomb", "vcoulomb"), ("frblendBegin", "frblend_begin"), ("frblendEnd", "frblend_end")):
-            if jk in t:
-                p[P[pk]] = float(t[jk])
     else:
         raise ValueError("unknown tire type")
     tire_init(p)

@@ -1,0 +1,100 @@
+import importlib
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+TESTS = os.path.dirname(os.path.abspath(__file__))
+for p in (ROOT, TESTS):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+PKG = "low-fidelity-dynamic-models_gb300"
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA device (runs the library's kernels)")
+
+
+def load_pkg():
+    return importlib.import_module(PKG)
+
+
+def pkg_mod(name):
+    return importlib.import_module(f"{PKG}.{name}")
+
+
+@pytest.fixture(scope="session")
+def lfdm():
+    return load_pkg()
+
+
+@pytest.fixture(scope="session")
+def golden18():
+    with open(os.path.join(TESTS, "golden", "golden18.json")) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="session")
+def built_lib():
+    """Build liblfdm.so if needed (nvcc cross-compiles without a GPU)."""
+    pkg_mod("build").build()
+    return load_pkg()
+
+
+# Parity floors s_k of the per-state check |a - b| <= rtol * max(|b|, s_k): 1 m for positions,
+# 1 m/s for velocities, 1 rad for angles, 1 rad/s for body rates, 10 rad/s for wheel and crank
+# speeds, 1e-3 m for tire deflections, 1 m/s^2 for accelerations.
+def state_floors():
+    abi = pkg_mod("_abi")
+    fl = np.full(abi.S_COUNT, np.inf)  # fields not listed are not compared
+    S, T = abi.S, abi.T
+    for k in ("x", "y"):
+        fl[S[k]] = 1.0
+    for k in ("u", "v"):
+        fl[S[k]] = 1.0
+    for k in ("psi", "phi"):
+        fl[S[k]] = 1.0
+    for k in ("wz", "wx"):
+        fl[S[k]] = 1.0
+    for k in ("udot", "vdot"):
+        fl[S[k]] = 1.0
+    fl[S["crankomega"]] = 10.0
+    fl[S["current_gr"]] = 1.0
+    for t in range(4):
+        b = abi.S_TIRE0 + t * abi.S_TIRE_STRIDE
+        fl[b + T["omega"]] = 10.0
+        fl[b + T["xe"]] = 1e-3
+        fl[b + T["ye"]] = 1e-3
+    return fl
+
+
+RESP_FLOORS = np.array([1.0, 1, 1, 1, 1, 1, 1, 1, 1, 10, 10, 10, 10], dtype=np.float64)
+
+
+def rel_err(a, b, floors):
+    """Elementwise |a-b| / max(|b|, floor); inf floors mark fields that are not compared."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    den = np.maximum(np.abs(b), floors)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        e = np.abs(a - b) / den
+    e[..., ~np.isfinite(np.broadcast_to(floors, a.shape[-1:]))] = 0.0
+    return np.where(np.isnan(e), np.inf, e)
+
+
+def case_inputs(case):
+    """(Class18, params[P], state[S], table[rows][4]) of a golden case."""
+    params = pkg_mod("params")
+    abi = pkg_mod("_abi")
+    cls, p = params.vehicle_from_json(case["vehicle"], case["tire"], case["tire_type"])
+    for k, v in case["vp"].items():
+        p[abi.P[k.lower()]] = v
+    for k, v in case["tp"].items():
+        p[abi.P[k.lower()]] = v
+    if case["tp"]:
+        params.tire_init(p)
+    return cls, p, np.array(case["state"], dtype=np.float64), np.array(case["driver"], dtype=np.float64)
