@@ -1,0 +1,325 @@
+"""Throughput of the batched half-implicit 18-DOF stepper on GB300 (vehicle-steps/s).
+
+Workload (default): the seeded synthetic SUV fleet, 18-DOF with TMeasy tires, FP64, dt = 1e-3 s,
+300,000 vehicles with mass, Jz, CG position, tire vertical stiffness and peak friction jittered
++/-10%, per-vehicle driver tables sampled every 10 ms (sine steering, throttle ramp, brake
+pulse), outputs (13 channels) sampled every 10 ms. A bench "step" is one stepping window of
+kernel_sim_time = 1 s (1,000 integration steps) over all vehicles, continuing the trajectory;
+W warm-up windows then K timed windows (defaults 3 + 7 = the 10 s horizon).
+
+value: device time (CUDA events on the solver's stream around each window kernel) with inputs
+       resident in HBM and the response written into HBM.
+e2e:   the same windows through the C ABI with host buffers: each step uploads that window's
+       driver-table rows from page-locked host memory and streams the window's response back to
+       page-locked host memory; wall-clock time.
+--impl reference: the reference's CPU algorithm (the oracle restatement, oracle/lfdm_oracle.c) on
+       all host cores over a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+PKG = "low-fidelity-dynamic-models_gb300"
+SEED = 20261203
+W_ALG_18 = 1391  # FP64 source-level operations per 18-DOF vehicle-step of the reference algorithm
+METRIC = "18-DOF vehicle-steps/s on 1 GB300: FP64 plain vs mixed at stated error; adjoint/fwd"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=7)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--vehicles", type=int, default=300_000)
+    ap.add_argument("--ksim", type=float, default=1.0)
+    ap.add_argument("--threads", type=int, default=0, help="threads per block (0: library default)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=8192, help="vehicles in the CPU-baseline sample")
+    return ap.parse_args()
+
+
+class Dist:
+    def __init__(self, n):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _oracle_rate(f, nveh: int, ksim: float, threads: int) -> tuple[float, float]:
+    """Vehicle-steps/s of the CPU restatement over nveh vehicles for one window."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    sl = slice(0, nveh)
+    tabs = f["tables"][sl]
+    t0 = time.perf_counter()
+    oracle_lib.run18(f["cls"], f["class_of"][sl], f["params"][sl], f["states"][sl], tabs, tend=ksim, ksim=ksim,
+                     schedule=1, nthreads=threads)
+    dt = time.perf_counter() - t0
+    steps = int(round(ksim / 1e-3))
+    return nveh * steps / dt, dt
+
+
+def run_reference(a, dist: Dist):
+    if dist.rank != 0:
+        return
+    fleet = importlib.import_module(PKG + ".fleet")
+    cores = os.cpu_count() or 1
+    n = a.cpu_sample
+    f = fleet.fleet18(n, seed=SEED, horizon=(a.warmup + a.steps) * a.ksim)
+    for _ in range(a.warmup):
+        _oracle_rate(f, n, a.ksim, cores)
+    times = []
+    for _ in range(a.steps):
+        _, dt = _oracle_rate(f, n, a.ksim, cores)
+        times.append(dt)
+    steps = int(round(a.ksim / 1e-3))
+    v = n * steps * a.steps / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "vehicle-steps/s", "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * sum(times) / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SUV fleet)",
+        "config": _config(a, n_override=n),
+        "cpu_baseline": {"value": v, "unit": "vehicle-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{n} vehicles x {steps} steps per step (bounded sample of the fleet), "
+                                   f"{cores} host threads; the reference's CPU algorithm as restated in "
+                                   "oracle/lfdm_oracle.c (the reference checkout is not on this host)"},
+        "e2e": {"value": v, "unit": "vehicle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _config(a, n_override=None):
+    return {"workload": "18-DOF TMeasy SUV fleet, FP64, dt 1e-3 s, 10 ms driver tables and outputs, "
+                        f"{n_override or a.vehicles} vehicles, windows of {a.ksim:g} s",
+            "vehicles": n_override or a.vehicles, "dt": 1e-3, "kernel_sim_time": a.ksim, "output_hz": 100,
+            "model": "18dof-tmeasy", "seed": SEED,
+            "l2": "inputs larger than L2 (driver tables ~32 KB/vehicle, state 600 B, constants 560 B)"}
+
+
+def run_ours(a, dist: Dist):
+    import torch
+
+    lfdm = importlib.import_module(PKG)
+    fleet = importlib.import_module(PKG + ".fleet")
+    dev = dist.local if torch.cuda.device_count() > dist.local else 0
+    torch.cuda.set_device(dev)
+    n, K, W, ksim = a.vehicles, a.steps, a.warmup, a.ksim
+    horizon = (W + K) * ksim
+    steps_per_window = int(round(ksim / 1e-3))
+    f = fleet.fleet18(n, seed=SEED + dist.rank, horizon=horizon)
+
+    sol = lfdm.d18SolverHalfImplicitGPU(n, device=dev)
+    sol.construct_class(f["cls"][0], f["params"])
+    sol.set_driver_tables(f["tables"])
+    sol.set_states(f["states"])
+    sol.SetKernelSimTime(ksim)
+    sol.SetEndTime(horizon)
+    if a.threads:
+        sol.SetThreadsPerBlock(a.threads)
+    spw = int(np.ceil(ksim * 100.0 - 1e-9))
+    per_window = spw * lfdm.RESP18 * n
+    dresp = torch.empty(2 * per_window, dtype=torch.float64, device=f"cuda:{dev}")
+    sol.set_response_device(dresp.data_ptr(), dresp.numel(), 100.0)
+
+    # warm-up windows, then K timed windows (device time of the window kernels, CUDA events)
+    sol.solve_range(0.0, W * ksim)
+    torch.cuda.synchronize()
+    dist.barrier()
+    clk = ClockSampler(dev)
+    clk.start()
+    wall0 = time.perf_counter()
+    sol.solve_range(W * ksim, (W + K) * ksim)
+    wall = time.perf_counter() - wall0
+    kms, launches = sol.last_kernel_ms()
+    clocks = clk.stop()
+    torch.cuda.synchronize()
+    dist.barrier()
+    kms_max = dist.max(kms)
+    vsteps_rank = n * steps_per_window * K
+    total_vsteps = dist.sum(vsteps_rank)
+    value = total_vsteps / (kms_max * 1e-3)
+    final = sol.get_states()
+    finite = bool(np.isfinite(final[:, :15]).all())
+
+    # e2e through the C ABI with host buffers: per step, H2D of that window's table rows from
+    # page-locked memory and D2H of the window's response into page-locked memory
+    e2e = None
+    if not a.no_e2e:
+        rows_pw = int(round(ksim / 0.01)) + 1
+        win_tabs = np.empty((W + K, n, rows_pw, 4))
+        for w in range(W + K):
+            win_tabs[w] = f["tables"][:, w * (rows_pw - 1): w * (rows_pw - 1) + rows_pw, :]
+        host_resp = np.empty(2 * per_window)
+        lfdm.register_host(win_tabs)
+        lfdm.register_host(host_resp)
+        sol.set_response_device(None)
+        sol.set_states(f["states"])
+        sol.set_response_buffer(host_resp, 100.0)
+        for w in range(W):
+            sol.set_driver_tables(win_tabs[w])
+            sol.solve_range(w * ksim, (w + 1) * ksim)
+        dist.barrier()
+        t0 = time.perf_counter()
+        for w in range(W, W + K):
+            sol.set_driver_tables(win_tabs[w])
+            sol.solve_range(w * ksim, (w + 1) * ksim)
+        e2e_wall = dist.max(time.perf_counter() - t0)
+        lfdm.unregister_host(win_tabs)
+        lfdm.unregister_host(host_resp)
+        e2e = {"value": total_vsteps / e2e_wall, "unit": "vehicle-steps/s",
+               "h2d_bytes_per_step": int(win_tabs[0].nbytes), "d2h_bytes_per_step": int(per_window * 8),
+               "ms_per_step": 1e3 * e2e_wall / K}
+
+    peak_dfma = lfdm.measure_fp64_peak(dev)
+    launch_ms = kms / launches
+    alg_flop = W_ALG_18 * n * steps_per_window
+    achieved = alg_flop / (launch_ms * 1e-3) / 1e12
+    peak = 2 * peak_dfma / 1e12
+    # HBM view of the same kernel: algorithmic bytes per window (state in/out, constants, the
+    # window's table rows, the response written)
+    alg_bytes = n * (2 * 75 * 8 + 70 * 8 + (rows_w := int(round(ksim / 0.01)) + 1) * 32 + spw * 13 * 8)
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except OSError:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+
+    cpu = None
+    if dist.rank == 0:
+        cores = os.cpu_count() or 1
+        rate, secs = _oracle_rate(f, min(a.cpu_sample, n), ksim, cores)
+        cpu = {"value": rate, "unit": "vehicle-steps/s", "cores": cores, "kind": "port",
+               "sample": f"{min(a.cpu_sample, n)} vehicles x {steps_per_window} steps ({secs:.1f} s wall), "
+                         "oracle/lfdm_oracle.c (the reference's CPU algorithm restated) on all host cores"}
+    if dist.rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "vehicle-steps/s", "n_gpus": dist.world, "steps": K,
+            "warmup": W, "ms_per_step": kms_max / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SUV fleet; see config)",
+            "config": dict(_config(a), parallelism=f"replicas x{dist.world}" if dist.world > 1 else "1 GPU"),
+            "rtf": (kms_max * 1e-3) / (K * ksim),
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "peak_source": "measured live: DFMA throughput kernel (lfdm_measure_fp64_peak), "
+                                        "x2 flop/FMA; MEASURED_PEAKS.json has no FP64 figure",
+                         "algorithmic": f"{W_ALG_18} FP64 ops per vehicle-step (reference op count) x "
+                                        f"{n * steps_per_window} vehicle-steps per launch"},
+            "roofline_hbm": {"bound": "hbm", "achieved": alg_bytes / (launch_ms * 1e-3) / 1e9, "peak": hbm_peak,
+                             "unit": "GB/s", "frac": alg_bytes / (launch_ms * 1e-3) / 1e9 / hbm_peak,
+                             "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "wall_s_timed": wall,
+            "finite_states": finite,
+        }
+        print(json.dumps(line), flush=True)
+    sol.close()
+
+
+def main():
+    a = _args()
+    dist = Dist(a.gpus)
+    if a.impl == "reference":
+        run_reference(a, dist)
+    else:
+        run_ours(a, dist)
+    if dist.pg:
+        dist.pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

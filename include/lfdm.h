@@ -178,9 +178,18 @@ int lfdm_response_samples(lfdm_solver* h, size_t* samples_written);
 int lfdm_register_host(void* ptr, size_t bytes);
 int lfdm_unregister_host(void* ptr);
 
+/* Extension: like lfdm_set_response_buffer, but dst is device memory of the solver's GPU and the   */
+/* stepping kernel writes samples straight into it (no copy). capacity (doubles) must hold a whole */
+/* number of windows (samples per window = ceil(kernel_sim_time * output_freq)); samples wrap.      */
+int lfdm_set_response_device(lfdm_solver* h, double* dst_dev, size_t capacity, double output_freq);
+
 /* Solve() (dof18_halfImplicit_gpu.cu:404-494): integrate all vehicles from t = 0 to end time in */
 /* windows of kernel_sim_time.                                                                     */
 int lfdm_solve(lfdm_solver* h);
+/* Extension: the part of Solve() whose windows start in [t_begin, t_end): window starts are      */
+/* 0, k, 2k, ... (k = kernel_sim_time) exactly as in Solve, so consecutive ranges reproduce one     */
+/* Solve() call; lfdm_solve(h) == lfdm_solve_range(h, 0, end time) plus CSV output.                */
+int lfdm_solve_range(lfdm_solver* h, double t_begin, double t_end);
 /* SolveStep(t, steering, throttle, braking) (:497-550): one window with constant controls;       */
 /* *t_out receives t + kernel_sim_time.                                                            */
 int lfdm_solve_step(lfdm_solver* h, double t, double steering, double throttle, double braking, double* t_out);
@@ -200,6 +209,10 @@ int lfdm_last_kernel_ms(lfdm_solver* h, double* ms, unsigned* launches);
 
 /* Library build information (arch, version). */
 const char* lfdm_version(void);
+
+/* Measurement helper (no counterpart in the reference): FP64 fused-multiply-add instruction rate of */
+/* a device, measured with a throughput kernel (the FP64 issue roofline of the stepping kernel).     */
+int lfdm_measure_fp64_peak(int device, double* dfma_per_s);
 
 /* Host-only utilities (no device needed). setVehParamsJSON + setTireParamsJSON + tireInit        */
 /* (dof18_gpu.cu:1075-1330, :227-241) into a class record and a flat parameter vector, and        */

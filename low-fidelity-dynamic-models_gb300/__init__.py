@@ -83,6 +83,9 @@ def _sig(lib):
         "lfdm_get_status_words": ([vp, u, u, dp], i),
         "lfdm_last_kernel_ms": ([vp, _c_dp, ctypes.POINTER(u)], i),
         "lfdm_version": ([], cp),
+        "lfdm_set_response_device": ([vp, vp, sz, d], i),
+        "lfdm_solve_range": ([vp, d, d], i),
+        "lfdm_measure_fp64_peak": ([i, _c_dp], i),
         "lfdm_parse_vehicle18": ([cp, cp, i, vp, dp, ctypes.c_char_p, sz], i),
         "lfdm_load_driver_file": ([cp, dp, u, ctypes.POINTER(u), ctypes.c_char_p, sz], i),
     }
@@ -297,6 +300,16 @@ class d18SolverHalfImplicitGPU:
         self._resp = buf
         self._ck(self._L.lfdm_set_response_buffer(self._h, _ptr(buf), buf.size, float(output_freq)))
 
+    def set_response_device(self, ptr: int | None, capacity: int = 0, output_freq: float = 100.0):
+        """Write Solve's SoA response straight into device memory at `ptr` (e.g. a torch CUDA tensor's
+        data_ptr()) holding `capacity` doubles, a whole number of windows; windows wrap around."""
+        self._ck(self._L.lfdm_set_response_device(self._h, ctypes.c_void_p(ptr) if ptr else None, int(capacity),
+                                                  float(output_freq)))
+
+    def solve_range(self, t_begin: float, t_end: float):
+        """The windows of Solve() that start in [t_begin, t_end)."""
+        self._ck(self._L.lfdm_solve_range(self._h, float(t_begin), float(t_end)))
+
     def response_samples(self) -> int:
         n = ctypes.c_size_t()
         self._ck(self._L.lfdm_response_samples(self._h, ctypes.byref(n)))
@@ -319,6 +332,15 @@ class d18SolverHalfImplicitGPU:
         w = np.zeros(self.n, dtype=np.uint32)
         self._ck(self._L.lfdm_get_status_words(self._h, 0, self.n, _ptr(w)))
         return w
+
+
+def measure_fp64_peak(device: int = 0) -> float:
+    """Measured FP64 FMA instruction rate (DFMA/s) of a device."""
+    v = ctypes.c_double()
+    rc = lib().lfdm_measure_fp64_peak(int(device), ctypes.byref(v))
+    if rc:
+        raise LfdmError(rc, "FP64 peak probe failed")
+    return v.value
 
 
 def register_host(a: np.ndarray) -> None:

@@ -54,7 +54,7 @@ struct MapDev {
     int pad_;
     double x[LFDM_MAX_MAP];
     double y[LFDM_MAX_MAP];
-    double invdx[LFDM_MAX_MAP];  // 1 / (x[k+1] - x[k])
+    double dx[LFDM_MAX_MAP];     // x[k+1] - x[k]
     double dy[LFDM_MAX_MAP];     // y[k+1] - y[k]
 };
 struct ClassDev18 {
@@ -77,13 +77,15 @@ __device__ __forceinline__ int lower_bound_x(const double* a, int n, double x) {
     return l;
 }
 
-// getMapY (utils/utils_gpu.cu:60-75): clamp outside, linear interpolation inside.
+// getMapY (utils/utils_gpu.cu:60-75): clamp outside, linear interpolation inside. The quotient is
+// kept as a division: at a grid point it is exactly 1 (or 0), so an engine at rest sees exactly the
+// tabulated loss torque (0 at 0 rad/s) and stays at rest, as in the reference.
 __device__ __forceinline__ double map_y(const MapDev& m, double x) {
     if (x <= m.x[0]) return m.y[0];
     if (x >= m.x[m.n - 1]) return m.y[m.n - 1];
     int r = lower_bound_x(m.x, m.n, x);
     int l = r - 1;
-    double mbar = (x - m.x[l]) * m.invdx[l];
+    double mbar = (x - m.x[l]) / m.dx[l];
     return fma(mbar, m.dy[l], m.y[l]);
 }
 
@@ -420,7 +422,9 @@ __device__ __forceinline__ void powertrain_rhs(VehC& v, VehAux& va, TireC* ts, T
     if (C.tcbool) {
         bool reverse = false;
         const double omega_t = 0.25 * (((ts[0].omega + ts[1].omega) + ts[2].omega) + ts[3].omega);
-        const double omega_out = omega_t * C.invgear[g];
+        // division as in the reference: a converter started locked (crank = wheel speed / ratio)
+        // must see a speed ratio of exactly 1, not 1 + ulp (which would select reverse flow)
+        const double omega_out = omega_t / C.gear[g];
         const double omega_in = v.crank;
         double sr, cf, tr;
         if ((omega_out < 1e-9) || (omega_in < 1e-9)) {
@@ -448,7 +452,7 @@ __device__ __forceinline__ void powertrain_rhs(VehC& v, VehAux& va, TireC* ts, T
             if (g > 0) v.gear = g - 1;
         }
     } else {
-        v.crank = 0.25 * (((ts[0].omega + ts[1].omega) + ts[2].omega) + ts[3].omega) * C.invgear[g];
+        v.crank = 0.25 * (((ts[0].omega + ts[1].omega) + ts[2].omega) + ts[3].omega) / C.gear[g];
         torque_t = drive_torque(C, throttle, v.crank) * C.invgear[g];
         if (v.u < 1e-9 && torque_t < 0) torque_t = 0;
         if (v.crank > C.up[g]) {

@@ -54,6 +54,15 @@ cudaError_t launch_prepare18(const double* params_dev, int n, int npad, double* 
 cudaError_t launch_states_to_soa(const double* aos, int n, int npad, double* soa, cudaStream_t stream);
 cudaError_t launch_states_to_aos(const double* soa, int n, int npad, double* aos, cudaStream_t stream);
 
+// Counts table rows whose time is smaller than the previous row's (per vehicle, equal-length tables
+// of nrows rows each; shared != 0: one table). *bad_dev must be zeroed by the caller.
+cudaError_t launch_check_tables(const double* rows, long long ntables, int nrows, unsigned* bad_dev,
+                                cudaStream_t stream);
+
+// Measured FP64 fused-multiply-add throughput of the current device, in DFMA instructions per second
+// (a dependent-chain-free kernel timed with CUDA events).
+cudaError_t measure_dfma_rate(double* dfma_per_s);
+
 // Host-side conversion of a class record into the device table (computes segment reciprocals).
 void build_class_dev18(const lfdm_class18& c, ClassDev18* out);
 size_t class_dev18_size();

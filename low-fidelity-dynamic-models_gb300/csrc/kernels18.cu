@@ -159,6 +159,74 @@ cudaError_t launch_states_to_aos(const double* soa, int n, int npad, double* aos
 }
 
 // ---------------------------------------------------------------------------------------------
+// driver-table validation and the FP64 peak probe
+
+__global__ void check_tables_kernel(const double* __restrict__ rows, long long ntables, int nrows, unsigned* bad) {
+    const long long total = ntables * (long long)nrows;
+    unsigned local = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        if (i % nrows == 0) continue;
+        if (rows[4 * i] < rows[4 * (i - 1)]) ++local;
+    }
+    if (local) atomicAdd(bad, local);
+}
+
+cudaError_t launch_check_tables(const double* rows, long long ntables, int nrows, unsigned* bad_dev,
+                                cudaStream_t stream) {
+    if (ntables <= 0 || nrows <= 1) return cudaSuccess;
+    check_tables_kernel<<<152 * 8, 256, 0, stream>>>(rows, ntables, nrows, bad_dev);
+    return cudaGetLastError();
+}
+
+constexpr int kProbeIter = 4096;
+__global__ void dfma_probe_kernel(double* out, double seed) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    double a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = seed + tid * 1e-9 + k * 0.1;
+    const double m = 0.999999, c = 1e-7;
+#pragma unroll 4
+    for (int i = 0; i < kProbeIter; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = fma(a[k], m, c);
+    }
+    double s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += a[k];
+    out[tid] = s;
+}
+
+cudaError_t measure_dfma_rate(double* rate) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int threads = 256, blocks = sms * 8;
+    double* out = nullptr;
+    if ((e = cudaMalloc(&out, sizeof(double) * threads * blocks)) != cudaSuccess) return e;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    dfma_probe_kernel<<<blocks, threads>>>(out, 0.5);
+    float best = 1e30f;
+    for (int r = 0; r < 3; ++r) {
+        cudaEventRecord(a);
+        dfma_probe_kernel<<<blocks, threads>>>(out, 0.5);
+        cudaEventRecord(b);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        best = ms < best ? ms : best;
+    }
+    e = cudaGetLastError();
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    *rate = (double)threads * blocks * kProbeIter * 8 / (best * 1e-3);
+    return e;
+}
+
+// ---------------------------------------------------------------------------------------------
 // class tables
 
 static void build_map(const double (*pts)[2], int n, MapDev& m) {
@@ -169,7 +237,7 @@ static void build_map(const double (*pts)[2], int n, MapDev& m) {
         m.y[k] = pts[k][1];
     }
     for (int k = 0; k + 1 < n; ++k) {
-        m.invdx[k] = 1.0 / (m.x[k + 1] - m.x[k]);
+        m.dx[k] = m.x[k + 1] - m.x[k];
         m.dy[k] = m.y[k + 1] - m.y[k];
     }
 }

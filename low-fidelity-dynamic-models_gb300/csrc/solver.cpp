@@ -96,6 +96,9 @@ struct lfdm_solver {
     double* resp_host = nullptr;
     size_t resp_cap = 0;
     double resp_dtout = 0;
+    double* resp_dev = nullptr;
+    size_t resp_dev_cap = 0;
+    double resp_dev_dtout = 0;
     size_t resp_written = 0;
 
     // device mirrors
@@ -104,6 +107,8 @@ struct lfdm_solver {
     DevBuf<int32_t> d_len, d_class_of, d_samples;
     DevBuf<unsigned char> d_classes;
     DevBuf<uint32_t> d_status;
+    DevBuf<unsigned> d_bad;
+    bool rows_device_only = false;  // driver rows live only in d_rows (bulk upload path)
     bool dirty_params = true, dirty_classes = true, dirty_tables = true, dirty_states = true;
     bool device_newer = false;  // device state newer than host mirror
 
@@ -186,7 +191,7 @@ int sync_device(lfdm_solver* h) {
         h->dirty_params = false;
     }
     if (h->dirty_tables) {
-        if (!h->rows.empty()) {
+        if (!h->rows.empty() && !h->rows_device_only) {
             CK(h->d_rows.ensure(h->rows.size()));
             CK(cudaMemcpyAsync(h->d_rows.p, h->rows.data(), h->rows.size() * sizeof(double), cudaMemcpyHostToDevice,
                                h->stream));
@@ -220,6 +225,20 @@ int pull_states(lfdm_solver* h) {
                        cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->device_newer = false;
+    return LFDM_OK;
+}
+
+// Bring device-only driver rows back to the host mirror (before a partial table update).
+int pull_rows(lfdm_solver* h) {
+    if (!h->rows_device_only) return LFDM_OK;
+    int rc = set_device(h);
+    if (rc) return rc;
+    size_t nd = 0;
+    for (unsigned i = 0; i < h->N; ++i)
+        nd = std::max(nd, (size_t)(h->row_off[i] + h->row_len[i]) * 4);
+    h->rows.resize(nd);
+    if (nd) CK(cudaMemcpy(h->rows.data(), h->d_rows.p, nd * sizeof(double), cudaMemcpyDeviceToHost));
+    h->rows_device_only = false;
     return LFDM_OK;
 }
 
@@ -276,20 +295,29 @@ int csv_write(lfdm_solver* h) {
     return LFDM_OK;
 }
 
-// Runs windows starting at t0 (Solve: from 0 while start < tend; step: exactly one).
-int run_windows(lfdm_solver* h, double t0, bool solve_all, int ctl_mode, double st, double th, double br,
-                const double* ctl_dev, const double* sched_dev, unsigned sched_steps) {
+// Runs windows. solve_all: the Solve() schedule (starts 0, k, 2k, ... while start < tend), of which
+// only windows starting in [t0, t_end) are run; otherwise exactly one window starting at t0.
+int run_windows(lfdm_solver* h, double t0, double t_end, bool solve_all, int ctl_mode, double st, double th,
+                double br, const double* ctl_dev, const double* sched_dev, unsigned sched_steps, bool csv_ok) {
     int rc = sync_device(h);
     if (rc) return rc;
     const size_t N = h->N;
-    // output configuration: CSV (reference semantics) or response streaming
-    const bool csv = h->output && solve_all;
-    const bool stream_resp = h->resp_host != nullptr && solve_all;
-    const double dtout = csv ? h->dtout : (stream_resp ? h->resp_dtout : 0.0);
+    // output configuration: CSV (reference semantics), response streaming to host, or device
+    const bool csv = h->output && solve_all && csv_ok;
+    const bool dev_resp = h->resp_dev != nullptr && solve_all && !csv;
+    const bool stream_resp = h->resp_host != nullptr && solve_all && !csv && !dev_resp;
+    const double dtout = csv ? h->dtout : (stream_resp ? h->resp_dtout : (dev_resp ? h->resp_dev_dtout : 0.0));
     const int spw = dtout > 0 ? (int)std::ceil(h->ksim / dtout) : 0;
     const size_t slot = (size_t)spw * LFDM18_RESP_CHANNELS * N;  // doubles per window buffer
     const int nbuf = stream_resp ? 2 : 1;
-    if (dtout > 0) CK(h->d_resp.ensure(slot * nbuf));
+    if (dtout > 0 && !dev_resp) CK(h->d_resp.ensure(slot * nbuf));
+    size_t dev_windows = 0;
+    if (dev_resp) {
+        dev_windows = spw > 0 ? h->resp_dev_cap / slot : 0;
+        if (dev_windows == 0 || dev_windows * slot != h->resp_dev_cap)
+            return h->fail(LFDM_ERR_CAPACITY, "device response buffer must hold a whole number of windows (%zu doubles)",
+                           slot);
+    }
     std::vector<double> host_window;
     if (csv) {
         host_window.resize(slot);
@@ -321,16 +349,21 @@ int run_windows(lfdm_solver* h, double t0, bool solve_all, int ctl_mode, double 
     w.threads = h->threads;
 
     std::vector<int32_t> samp;
-    double current = t0;
+    double current = solve_all ? 0.0 : t0;
     unsigned launches = 0;
     size_t widx = 0;
     float total_ms = 0;
-    h->resp_written = 0;
+    if (!solve_all || t0 <= 0) h->resp_written = 0;
     const size_t resp_cap_samples = stream_resp ? h->resp_cap / (LFDM18_RESP_CHANNELS * N) : 0;
     if (stream_resp && resp_cap_samples == 0)
         return h->fail(LFDM_ERR_CAPACITY, "response buffer holds less than one sample");
     for (;;) {
-        if (solve_all && !(current < h->tend)) break;
+        if (solve_all && !(current < h->tend && current < t_end)) break;
+        if (solve_all && current < t0) {  // window before the requested range: same start times as Solve
+            current = current + h->ksim;
+            ++widx;
+            continue;
+        }
         int nsteps = 0;
         window_schedule(current, h->ksim, h->step, dtout, spw, nsteps, samp);
         if (sched_dev && (unsigned)nsteps != sched_steps)
@@ -342,10 +375,11 @@ int run_windows(lfdm_solver* h, double t0, bool solve_all, int ctl_mode, double 
             CK(cudaMemcpyAsync(h->d_samples.p + (size_t)b * (spw + 1), samp.data(), samp.size() * sizeof(int32_t),
                                cudaMemcpyHostToDevice, h->stream));
         }
-        if (stream_resp && widx >= 2) CK(cudaStreamWaitEvent(h->stream, h->copy_done[b], 0));
+        if (stream_resp && launches >= 2) CK(cudaStreamWaitEvent(h->stream, h->copy_done[b], 0));
         w.t0 = current;
         w.nsteps = nsteps;
-        w.resp = dtout > 0 ? h->d_resp.p + (size_t)b * slot : nullptr;
+        w.resp = dtout > 0 ? (dev_resp ? h->resp_dev + (widx % dev_windows) * slot : h->d_resp.p + (size_t)b * slot)
+                           : nullptr;
         w.nsamples = dtout > 0 ? (int)samp.size() : 0;
         w.sample_steps = dtout > 0 ? h->d_samples.p + (size_t)b * (spw + 1) : nullptr;
         CK(cudaEventRecord(h->ev0, h->stream));
@@ -355,13 +389,16 @@ int run_windows(lfdm_solver* h, double t0, bool solve_all, int ctl_mode, double 
         if (stream_resp) {
             CK(cudaEventRecord(h->win_done[b], h->stream));
             CK(cudaStreamWaitEvent(h->copy_stream, h->win_done[b], 0));
-            // window samples k land at global sample widx*spw + k (ring over the caller's buffer)
-            for (int k = 0; k < w.nsamples; ++k) {
+            // window samples k land at global sample widx*spw + k (ring over the caller's buffer);
+            // one copy per contiguous run of ring slots
+            const size_t per = LFDM18_RESP_CHANNELS * N;
+            for (int k = 0; k < w.nsamples;) {
                 const size_t gs = widx * (size_t)spw + k;
-                const size_t dst = (gs % resp_cap_samples) * LFDM18_RESP_CHANNELS * N;
-                CK(cudaMemcpyAsync(h->resp_host + dst, w.resp + (size_t)k * LFDM18_RESP_CHANNELS * N,
-                                   LFDM18_RESP_CHANNELS * N * sizeof(double), cudaMemcpyDeviceToHost,
-                                   h->copy_stream));
+                const size_t slot0 = gs % resp_cap_samples;
+                const int run = (int)std::min<size_t>((size_t)(w.nsamples - k), resp_cap_samples - slot0);
+                CK(cudaMemcpyAsync(h->resp_host + slot0 * per, w.resp + (size_t)k * per, run * per * sizeof(double),
+                                   cudaMemcpyDeviceToHost, h->copy_stream));
+                k += run;
             }
             CK(cudaEventRecord(h->copy_done[b], h->copy_stream));
             h->resp_written = widx * (size_t)spw + w.nsamples;
@@ -422,6 +459,10 @@ int append_vehicles(lfdm_solver* h, const lfdm_class18& cls, const double* param
             if ((*table)[4 * r] < (*table)[4 * (r - 1)])
                 return h->fail(LFDM_ERR_PARSE, "driver table times must be non-decreasing (row %zu)", r);
     }
+    if (table) {
+        int rc = pull_rows(h);
+        if (rc) return rc;
+    }
     h->tire_type = tire_type;
     const int ci = (int)h->classes.size();
     h->classes.push_back(cls);
@@ -452,6 +493,12 @@ int append_vehicles(lfdm_solver* h, const lfdm_class18& cls, const double* param
 extern "C" {
 
 const char* lfdm_version(void) { return "lfdm-gb300 0.1 (sm_103a, FP64 + mixed)"; }
+
+int lfdm_measure_fp64_peak(int device, double* dfma_per_s) {
+    if (!dfma_per_s) return LFDM_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return LFDM_ERR_NODEVICE;
+    return measure_dfma_rate(dfma_per_s) == cudaSuccess ? LFDM_OK : LFDM_ERR_CUDA;
+}
 
 int lfdm_create_on_device(int model, unsigned total_num_vehicles, int device, lfdm_solver** out) {
     if (!out) return LFDM_ERR_ARG;
@@ -568,17 +615,50 @@ static int set_tables(lfdm_solver* h, unsigned first, unsigned count, const doub
     if (!h || !rows || nrows == 0) return h ? h->fail(LFDM_ERR_ARG, "empty driver table") : LFDM_ERR_ARG;
     if ((size_t)first + count > h->N) return h->fail(LFDM_ERR_ARG, "vehicles [%u, %u) out of range", first, first + count);
     const unsigned ntab = shared ? 1 : count;
+    const bool all = first == 0 && count == h->N;
+    if (all) {
+        // every table replaced: DMA straight from the caller's buffer (page-locked buffers copy at
+        // full link speed), validate on the device, keep no host copy
+        int rc = set_device(h);
+        if (rc) return rc;
+        const size_t nd = (size_t)ntab * nrows * 4;
+        CK(h->d_rows.ensure(nd));
+        CK(cudaMemcpyAsync(h->d_rows.p, rows, nd * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        CK(h->d_bad.ensure(1));
+        CK(cudaMemsetAsync(h->d_bad.p, 0, sizeof(unsigned), h->stream));
+        CK(launch_check_tables(h->d_rows.p, ntab, (int)nrows, h->d_bad.p, h->stream));
+        unsigned bad = 0;
+        CK(cudaMemcpyAsync(&bad, h->d_bad.p, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (bad) {
+            h->dirty_tables = true;  // restore the previous tables at the next solve
+            return h->fail(LFDM_ERR_PARSE, "driver tables: %u rows have a time smaller than the previous row", bad);
+        }
+        h->rows.clear();
+        h->rows.shrink_to_fit();
+        h->rows_device_only = true;
+        for (unsigned k = 0; k < count; ++k) {
+            h->row_off[k] = shared ? 0 : (int64_t)k * nrows;
+            h->row_len[k] = (int32_t)nrows;
+        }
+        CK(h->d_off.ensure(h->N));
+        CK(h->d_len.ensure(h->N));
+        CK(cudaMemcpyAsync(h->d_off.p, h->row_off.data(), h->N * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->d_len.p, h->row_len.data(), h->N * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        h->dirty_tables = false;
+        return LFDM_OK;
+    }
     for (unsigned k = 0; k < ntab; ++k) {
         const double* t = rows + (size_t)k * nrows * 4;
         for (unsigned r = 1; r < nrows; ++r)
             if (t[4 * r] < t[4 * (r - 1)])
                 return h->fail(LFDM_ERR_PARSE, "driver table %u: times must be non-decreasing (row %u)", k, r);
     }
+    int rc = pull_rows(h);
+    if (rc) return rc;
     const int64_t base = (int64_t)(h->rows.size() / 4);
-    // replacing every table of the solver: drop the old rows
-    bool all = first == 0 && count == h->N;
-    if (all) h->rows.clear();
-    const int64_t b2 = all ? 0 : base;
+    const int64_t b2 = base;
     h->rows.insert(h->rows.end(), rows, rows + (size_t)ntab * nrows * 4);
     for (unsigned k = 0; k < count; ++k) {
         h->row_off[first + k] = b2 + (shared ? 0 : (int64_t)k * nrows);
@@ -759,12 +839,40 @@ int lfdm_unregister_host(void* ptr) {
     return cudaHostUnregister(ptr) == cudaSuccess ? LFDM_OK : LFDM_ERR_CUDA;
 }
 
+int lfdm_set_response_device(lfdm_solver* h, double* dst_dev, size_t capacity, double output_freq) {
+    if (!h) return LFDM_ERR_ARG;
+    if (!dst_dev) {
+        h->resp_dev = nullptr;
+        h->resp_dev_cap = 0;
+        return LFDM_OK;
+    }
+    if (!(output_freq > 0)) return h->fail(LFDM_ERR_ARG, "output frequency must be positive");
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, dst_dev) != cudaSuccess || at.type != cudaMemoryTypeDevice ||
+        at.device != h->device) {
+        cudaGetLastError();
+        return h->fail(LFDM_ERR_ARG, "response buffer is not device memory of device %d", h->device);
+    }
+    h->resp_dev = dst_dev;
+    h->resp_dev_cap = capacity;
+    h->resp_dev_dtout = 1.0 / output_freq;
+    return LFDM_OK;
+}
+
+int lfdm_solve_range(lfdm_solver* h, double t_begin, double t_end) {
+    if (!h) return LFDM_ERR_ARG;
+    if (!(h->tend > 0)) return h->fail(LFDM_ERR_STATE, "Final time not set, please use SetEndTime function");
+    int rc = check_ready(h, true);
+    if (rc) return rc;
+    return run_windows(h, t_begin, t_end, true, CTL_TABLE, 0, 0, 0, nullptr, nullptr, 0, false);
+}
+
 int lfdm_solve(lfdm_solver* h) {
     if (!h) return LFDM_ERR_ARG;
     if (!(h->tend > 0)) return h->fail(LFDM_ERR_STATE, "Final time not set, please use SetEndTime function");
     int rc = check_ready(h, true);
     if (rc) return rc;
-    return run_windows(h, 0.0, true, CTL_TABLE, 0, 0, 0, nullptr, nullptr, 0);
+    return run_windows(h, 0.0, h->tend, true, CTL_TABLE, 0, 0, 0, nullptr, nullptr, 0, true);
 }
 
 static int step_guard(lfdm_solver* h) {
@@ -779,7 +887,7 @@ int lfdm_solve_step(lfdm_solver* h, double t, double steering, double throttle, 
     if (!h) return LFDM_ERR_ARG;
     int rc = step_guard(h);
     if (rc) return rc;
-    rc = run_windows(h, t, false, CTL_SCALAR, steering, throttle, braking, nullptr, nullptr, 0);
+    rc = run_windows(h, t, t, false, CTL_SCALAR, steering, throttle, braking, nullptr, nullptr, 0, false);
     if (rc) return rc;
     if (t_out) *t_out = t + h->ksim;
     return LFDM_OK;
@@ -797,7 +905,7 @@ int lfdm_solve_step_controls(lfdm_solver* h, double t, const double* steering, c
     CK(cudaMemcpyAsync(h->d_ctl.p, steering, h->N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_ctl.p + np, throttle, h->N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_ctl.p + 2 * np, braking, h->N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    rc = run_windows(h, t, false, CTL_ARRAY, 0, 0, 0, h->d_ctl.p, nullptr, 0);
+    rc = run_windows(h, t, t, false, CTL_ARRAY, 0, 0, 0, h->d_ctl.p, nullptr, 0, false);
     if (rc) return rc;
     if (t_out) *t_out = t + h->ksim;
     return LFDM_OK;
@@ -830,7 +938,7 @@ int lfdm_solve_step_schedule(lfdm_solver* h, double t, const double* ctl, unsign
         CK(cudaMemcpyAsync(h->d_sched.p, ctl, (size_t)nsteps * 3 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
         sched = h->d_sched.p;
     }
-    rc = run_windows(h, t, false, CTL_SCHEDULE, 0, 0, 0, nullptr, sched, nsteps);
+    rc = run_windows(h, t, t, false, CTL_SCHEDULE, 0, 0, 0, nullptr, sched, nsteps, false);
     if (rc) return rc;
     if (t_out) *t_out = t + h->ksim;
     return LFDM_OK;
