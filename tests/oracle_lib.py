@@ -22,22 +22,25 @@ def build() -> str:
     return LIB
 
 
-_lib = None
+LIB_FMA = os.path.join(ORACLE_DIR, "_build", "liboracle_fma.so")
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB):
+def lib(fma: bool = False):
+    """The oracle; fma=True loads the same restatement compiled with FMA contraction."""
+    path = LIB_FMA if fma else LIB
+    if path not in _libs:
+        if not os.path.exists(path):
             build()
-        _lib = ctypes.CDLL(LIB)
-        _lib.oracle18_run.argtypes = [ctypes.c_void_p]
-        _lib.oracle18_run.restype = ctypes.c_int
-        _lib.oracle_map_y.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
-        _lib.oracle_map_y.restype = ctypes.c_double
-        _lib.oracle_driver_input.argtypes = [ctypes.c_double, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
-        _lib.oracle_tire_init.argtypes = [ctypes.c_void_p]
-    return _lib
+        L = ctypes.CDLL(path)
+        L.oracle18_run.argtypes = [ctypes.c_void_p]
+        L.oracle18_run.restype = ctypes.c_int
+        L.oracle_map_y.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
+        L.oracle_map_y.restype = ctypes.c_double
+        L.oracle_driver_input.argtypes = [ctypes.c_double, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.oracle_tire_init.argtypes = [ctypes.c_void_p]
+        _libs[path] = L
+    return _libs[path]
 
 
 class _Args(ctypes.Structure):
@@ -60,7 +63,7 @@ def _ptr(a):
 
 
 def run18(classes, class_of, params, states, tables=None, ctl=None, *, tire_type=0, dt=1e-3, t0=0.0,
-          tend=10.0, ksim=2.0, schedule=1, dtout=0.0, nthreads=1):
+          tend=10.0, ksim=2.0, schedule=1, dtout=0.0, nthreads=1, fma=False):
     """Advance `states` ([n][75], copied) with the oracle. `tables` is a list of per-vehicle
     [rows][4] arrays or one [n][rows][4] array. schedule 0 = CPU solver, 1 = GPU Solve,
     2 = one SolveStep window. Returns (states, resp or None)."""
@@ -98,7 +101,7 @@ def run18(classes, class_of, params, states, tables=None, ctl=None, *, tire_type
               params=_ptr(params), states=_ptr(st), drv_rows=_ptr(rows), drv_off=_ptr(off), drv_len=_ptr(ln),
               ctl=_ptr(ctl_arr), dt=dt, t0=t0, tend=tend, ksim=ksim, schedule=schedule, dtout=dtout,
               resp=_ptr(resp), resp_samples=nsamp, samples_per_window=spw, nthreads=nthreads)
-    rc = lib().oracle18_run(ctypes.byref(a))
+    rc = lib(fma).oracle18_run(ctypes.byref(a))
     if rc != 0:
         raise RuntimeError(f"oracle18_run failed rc={rc}")
     return st, resp
