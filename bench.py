@@ -212,13 +212,13 @@ def run_ours(a, dist: Dist):
     sol.set_response_device(dresp.data_ptr(), dresp.numel(), 100.0)
 
     # warm-up windows, then K timed windows (device time of the window kernels, CUDA events)
-    sol.solve_range(0.0, W * ksim)
+    sol.solve_range(-0.5 * ksim, (W - 0.5) * ksim)
     torch.cuda.synchronize()
     dist.barrier()
     clk = ClockSampler(dev)
     clk.start()
     wall0 = time.perf_counter()
-    sol.solve_range(W * ksim, (W + K) * ksim)
+    sol.solve_range((W - 0.5) * ksim, (W + K - 0.5) * ksim)
     wall = time.perf_counter() - wall0
     kms, launches = sol.last_kernel_ms()
     clocks = clk.stop()
@@ -247,12 +247,12 @@ def run_ours(a, dist: Dist):
         sol.set_response_buffer(host_resp, 100.0)
         for w in range(W):
             sol.set_driver_tables(win_tabs[w])
-            sol.solve_range(w * ksim, (w + 1) * ksim)
+            sol.solve_range((w - 0.5) * ksim, (w + 0.5) * ksim)
         dist.barrier()
         t0 = time.perf_counter()
         for w in range(W, W + K):
             sol.set_driver_tables(win_tabs[w])
-            sol.solve_range(w * ksim, (w + 1) * ksim)
+            sol.solve_range((w - 0.5) * ksim, (w + 0.5) * ksim)
         e2e_wall = dist.max(time.perf_counter() - t0)
         lfdm.unregister_host(win_tabs)
         lfdm.unregister_host(host_resp)
