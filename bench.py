@@ -46,6 +46,9 @@ def _args():
     ap.add_argument("--ksim", type=float, default=1.0)
     ap.add_argument("--threads", type=int, default=0, help="threads per block (0: library default)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--error-vehicles", type=int, default=65536)
+    ap.add_argument("--error-horizon", type=float, default=20.0)
     ap.add_argument("--cpu-sample", type=int, default=8192, help="vehicles in the CPU-baseline sample")
     return ap.parse_args()
 
@@ -186,6 +189,35 @@ def _config(a, n_override=None):
             "l2": "inputs larger than L2 (driver tables ~32 KB/vehicle, state 600 B, constants 560 B)"}
 
 
+def _mixed_error(lfdm, fleet, dev, n, horizon):
+    """End-of-horizon error of the mixed form against the FP64 form: the seeded fleet with initial
+    speeds U[0.5, 30] m/s (near-standstill starts stress the low-speed slip path)."""
+    f = fleet.fleet18(n, seed=SEED + 7, horizon=horizon, u0_range=(0.5, 30.0))
+    out = {}
+    for prec in (0, 1):
+        s = lfdm.d18SolverHalfImplicitGPU(n, device=dev)
+        s.construct_class(f["cls"][0], f["params"])
+        s.set_driver_tables(f["tables"])
+        s.set_states(f["states"])
+        s.SetKernelSimTime(1.0)
+        s.SetEndTime(horizon)
+        s.set_precision(prec)
+        s.Solve()
+        out[prec] = s.get_states()
+        s.close()
+    S = lfdm.S
+    a, b = out[0], out[1]
+    pos = np.hypot(b[:, S["x"]] - a[:, S["x"]], b[:, S["y"]] - a[:, S["y"]])
+    yaw = np.abs(b[:, S["psi"]] - a[:, S["psi"]])
+    spd = np.abs(np.hypot(b[:, S["u"]], b[:, S["v"]]) - np.hypot(a[:, S["u"]], a[:, S["v"]]))
+
+    def st(e):
+        return {"max": float(e.max()), "p99": float(np.quantile(e, 0.99)), "p50": float(np.median(e))}
+
+    return {"vehicles": n, "horizon_s": horizon, "u0_range": [0.5, 30.0], "position_m": st(pos), "yaw_rad": st(yaw),
+            "speed_mps": st(spd), "frac_position_within_1cm": float((pos <= 0.01).mean())}
+
+
 def run_ours(a, dist: Dist):
     import torch
 
@@ -260,6 +292,28 @@ def run_ours(a, dist: Dist):
                "h2d_bytes_per_step": int(win_tabs[0].nbytes), "d2h_bytes_per_step": int(per_window * 8),
                "ms_per_step": 1e3 * e2e_wall / K}
 
+    # mixed precision: throughput on the same fleet and windows, accuracy against the FP64 path
+    mixed = None
+    if not a.no_mixed:
+        solm = lfdm.d18SolverHalfImplicitGPU(n, device=dev)
+        solm.construct_class(f["cls"][0], f["params"])
+        solm.set_driver_tables(f["tables"])
+        solm.set_states(f["states"])
+        solm.SetKernelSimTime(ksim)
+        solm.SetEndTime(horizon)
+        solm.set_precision(1)
+        if a.threads:
+            solm.SetThreadsPerBlock(a.threads)
+        solm.set_response_device(dresp.data_ptr(), dresp.numel(), 100.0)
+        solm.solve_range(-0.5 * ksim, (W - 0.5) * ksim)
+        torch.cuda.synchronize()
+        solm.solve_range((W - 0.5) * ksim, (W + K - 0.5) * ksim)
+        mms, mlaunch = solm.last_kernel_ms()
+        solm.close()
+        mvalue = dist.sum(vsteps_rank) / (dist.max(mms) * 1e-3)
+        mixed = {"value": mvalue, "unit": "vehicle-steps/s", "speedup_vs_fp64": mvalue / value,
+                 "ms_per_step": mms / K, "gpu_launches": mlaunch, "dtype": "f32 RHS + f64 states/X/Y/yaw/slip"}
+        mixed["error_vs_fp64"] = _mixed_error(lfdm, fleet, dev, a.error_vehicles, a.error_horizon)
     peak_dfma = lfdm.measure_fp64_peak(dev)
     launch_ms = kms / launches
     alg_flop = W_ALG_18 * n * steps_per_window
@@ -301,6 +355,7 @@ def run_ours(a, dist: Dist):
                              "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "mixed": mixed,
             "gpu_launches": launches,
             "clocks": clocks,
             "wall_s_timed": wall,

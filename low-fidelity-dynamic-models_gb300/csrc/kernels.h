@@ -11,6 +11,7 @@
 namespace lfdm {
 
 struct ClassDev18;
+struct ClassDev18F;
 
 // Control source of a window.
 enum CtlMode : int { CTL_TABLE = 0, CTL_SCALAR = 1, CTL_ARRAY = 2, CTL_SCHEDULE = 3 };
@@ -24,6 +25,7 @@ struct Window18 {
     int nsteps = 0;      // steps in this window (host-simulated loop of the reference)
     const double* K = nullptr;           // [K18_COUNT][npad] derived constants
     const ClassDev18* classes = nullptr; // [nclasses]
+    const ClassDev18F* classes_f = nullptr;  // FP32 copies for the mixed kernel
     int nclasses = 0;
     const int32_t* class_of = nullptr;   // [n]
     double* S = nullptr;                 // [LFDM_S_COUNT][npad] state, in/out
@@ -66,6 +68,8 @@ cudaError_t measure_dfma_rate(double* dfma_per_s);
 // Host-side conversion of a class record into the device table (computes segment reciprocals).
 void build_class_dev18(const lfdm_class18& c, ClassDev18* out);
 size_t class_dev18_size();
+void build_class_dev18f(const lfdm_class18& c, ClassDev18F* out);
+size_t class_dev18f_size();
 
 int k18_count();
 

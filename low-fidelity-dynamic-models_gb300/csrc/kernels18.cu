@@ -16,11 +16,13 @@
 #include <cstring>
 
 #include "dof18_device.cuh"
+#include "dof18_mixed.cuh"
 #include "kernels.h"
 
 namespace lfdm {
 
 static_assert(sizeof(ClassDev18) % 16 == 0, "ClassDev18 must be a multiple of 16 bytes");
+static_assert(sizeof(ClassDev18F) % 16 == 0, "ClassDev18F must be a multiple of 16 bytes");
 
 int k18_count() { return K18_COUNT; }
 size_t class_dev18_size() { return sizeof(ClassDev18); }
@@ -474,6 +476,267 @@ __global__ void __launch_bounds__(128) window18_kernel(const Window18 w) {
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// mixed-precision window kernel (TMeasy)
+
+size_t window18_mixed_smem(int threads, int nclasses) {
+    const size_t cls = nclasses <= kMaxSmemClasses ? (size_t)nclasses * sizeof(ClassDev18F) : 0;
+    return cls + (size_t)K18_COUNT * threads * sizeof(float);
+}
+
+// Driver input with the current table segment cached in FP32 (reloaded when the cursor moves):
+// the step costs one FP64 subtraction and one conversion.
+struct DriverCursorF {
+    DriverCursor c;
+    int seg;       // cursor value the cache was built for (-1: none)
+    double tL;
+    float inv, sL, dS, hL, dH, bL, dB;
+};
+
+__device__ __forceinline__ void driver_at_f(DriverCursorF& d, double t, float& st, float& th, float& br) {
+    DriverCursor& c = d.c;
+    if (t <= c.tfirst) {
+        st = (float)__ldg(c.rows + 1);
+        th = (float)__ldg(c.rows + 2);
+        br = (float)__ldg(c.rows + 3);
+        return;
+    }
+    if (t >= c.tlast) {
+        const double* L = c.rows + 4 * (c.len - 1);
+        st = (float)__ldg(L + 1);
+        th = (float)__ldg(L + 2);
+        br = (float)__ldg(L + 3);
+        return;
+    }
+    while (__ldg(c.rows + 4 * c.r) < t) ++c.r;
+    while (c.r > 1 && __ldg(c.rows + 4 * (c.r - 1)) >= t) --c.r;
+    if (d.seg != c.r) {
+        const double2* L = reinterpret_cast<const double2*>(c.rows + 4 * (c.r - 1));
+        const double2 L01 = __ldg(L), L23 = __ldg(L + 1), R01 = __ldg(L + 2), R23 = __ldg(L + 3);
+        d.tL = L01.x;
+        d.inv = (float)(1.0 / (R01.x - L01.x));
+        d.sL = (float)L01.y;
+        d.dS = (float)(R01.y - L01.y);
+        d.hL = (float)L23.x;
+        d.dH = (float)(R23.x - L23.x);
+        d.bL = (float)L23.y;
+        d.dB = (float)(R23.y - L23.y);
+        d.seg = c.r;
+    }
+    const float tbar = (float)(t - d.tL) * d.inv;
+    st = fmaf(tbar, d.dS, d.sL);
+    th = fmaf(tbar, d.dH, d.hL);
+    br = fmaf(tbar, d.dB, d.bL);
+}
+
+template <int kCtl, bool kOut>
+__global__ void __launch_bounds__(128) window18_mixed_kernel(const Window18 w) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int tid = threadIdx.x;
+    const bool cls_smem = w.nclasses <= kMaxSmemClasses;
+    const ClassDev18F* gcls = reinterpret_cast<const ClassDev18F*>(w.classes_f);
+    float* ks = reinterpret_cast<float*>(smem + (cls_smem ? (size_t)w.nclasses * sizeof(ClassDev18F) : 0));
+    if (cls_smem) {
+        const int4* src = reinterpret_cast<const int4*>(gcls);
+        int4* dst = reinterpret_cast<int4*>(smem);
+        const int words = (int)(w.nclasses * sizeof(ClassDev18F) / 16);
+        for (int i = tid; i < words; i += blockDim.x) dst[i] = __ldg(src + i);
+    }
+    const int vid = blockIdx.x * blockDim.x + tid;
+    const bool active = vid < w.n;
+    if (active) {
+#pragma unroll 4
+        for (int k = 0; k < K18_COUNT; ++k) ks[k * blockDim.x + tid] = (float)__ldg(w.K + (size_t)k * w.npad + vid);
+    }
+    __syncthreads();
+    if (!active) return;
+    const KViewF K{ks + tid, (int)blockDim.x};
+    const int ci = __ldg(w.class_of + vid);
+    const ClassDev18F& C = cls_smem ? reinterpret_cast<const ClassDev18F*>(smem)[ci] : gcls[ci];
+    const size_t np = (size_t)w.npad;
+    double* S = w.S + vid;
+
+    VehM v;
+    VehAux va;
+    TireM ts[4];
+    TireAuxF ta[4];
+    v.x = S[LFDM_S_X * np];
+    v.y = S[LFDM_S_Y * np];
+    v.u = S[LFDM_S_U * np];
+    v.v = S[LFDM_S_V * np];
+    v.psi = S[LFDM_S_PSI * np];
+    v.wz = S[LFDM_S_WZ * np];
+    v.phi = S[LFDM_S_PHI * np];
+    v.wx = S[LFDM_S_WX * np];
+    v.udot = (float)S[LFDM_S_UDOT * np];
+    v.vdot = (float)S[LFDM_S_VDOT * np];
+    v.crank = S[LFDM_S_CRANKOMEGA * np];
+    v.gear = (int)S[LFDM_S_CURRENT_GR * np];
+    va.wxdot = S[LFDM_S_WXDOT * np];
+    va.wzdot = S[LFDM_S_WZDOT * np];
+    va.dOmega_crank = S[LFDM_S_DOMEGA_CRANK * np];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const size_t b = (size_t)(LFDM_S_TIRE0 + k * LFDM_S_TIRE_STRIDE) * np;
+        ts[k].xe = (float)S[b + LFDM_T_XE * np];
+        ts[k].ye = (float)S[b + LFDM_T_YE * np];
+        ts[k].xedot = (float)S[b + LFDM_T_XEDOT * np];
+        ts[k].yedot = (float)S[b + LFDM_T_YEDOT * np];
+        ts[k].omega = S[b + LFDM_T_OMEGA * np];
+        ta[k].dOmega = (float)S[b + LFDM_T_DOMEGA * np];
+        ta[k].xt = (float)S[b + LFDM_T_XT * np];
+        ta[k].rStat = (float)S[b + LFDM_T_RSTAT * np];
+        ta[k].fx = (float)S[b + LFDM_T_FX * np];
+        ta[k].fy = (float)S[b + LFDM_T_FY * np];
+        ta[k].fz = (float)S[b + LFDM_T_FZ * np];
+        ta[k].vsx = (float)S[b + LFDM_T_VSX * np];
+        ta[k].vsy = (float)S[b + LFDM_T_VSY * np];
+        ta[k].My = (float)S[b + LFDM_T_MY * np];
+        ta[k].engTor = (float)S[b + LFDM_T_ENGTOR * np];
+    }
+    DriverCursorF cur;
+    float steer = (float)w.steer, thr = (float)w.thr, brk = (float)w.brk;
+    if (kCtl == CTL_TABLE) {
+        driver_begin(cur.c, w.rows + 4 * __ldg(w.row_off + vid), __ldg(w.row_len + vid), w.t0);
+        cur.seg = -1;
+    } else if (kCtl == CTL_ARRAY) {
+        steer = (float)__ldg(w.ctl + vid);
+        thr = (float)__ldg(w.ctl + np + vid);
+        brk = (float)__ldg(w.ctl + 2 * np + vid);
+    }
+    int next_k = 0;
+    int next_step = (kOut && w.nsamples > 0) ? __ldg(w.sample_steps) : -1;
+    double t = w.t0;
+    const double dt = w.dt;
+    for (int s = 0; s < w.nsteps; ++s) {
+        if (kCtl == CTL_TABLE) {
+            driver_at_f(cur, t, steer, thr, brk);
+        } else if (kCtl == CTL_SCHEDULE) {
+            steer = (float)__ldg(w.sched + 3 * s);
+            thr = (float)__ldg(w.sched + 3 * s + 1);
+            brk = (float)__ldg(w.sched + 3 * s + 2);
+        }
+        step18_mixed(v, va, ts, ta, K, C, steer, thr, brk, dt);
+        t += dt;
+        if (kOut && s + 1 == next_step) {
+            double* r = w.resp + (size_t)next_k * LFDM18_RESP_CHANNELS * w.n + vid;
+            const size_t n = (size_t)w.n;
+            r[0 * n] = t;
+            r[1 * n] = v.x;
+            r[2 * n] = v.y;
+            r[3 * n] = v.u;
+            r[4 * n] = v.v;
+            r[5 * n] = v.phi;
+            r[6 * n] = v.psi;
+            r[7 * n] = v.wx;
+            r[8 * n] = v.wz;
+            r[9 * n] = ts[0].omega;
+            r[10 * n] = ts[1].omega;
+            r[11 * n] = ts[2].omega;
+            r[12 * n] = ts[3].omega;
+            ++next_k;
+            next_step = next_k < w.nsamples ? __ldg(w.sample_steps + next_k) : -1;
+        }
+    }
+    S[LFDM_S_X * np] = v.x;
+    S[LFDM_S_Y * np] = v.y;
+    S[LFDM_S_U * np] = v.u;
+    S[LFDM_S_V * np] = v.v;
+    S[LFDM_S_PSI * np] = v.psi;
+    S[LFDM_S_WZ * np] = v.wz;
+    S[LFDM_S_PHI * np] = v.phi;
+    S[LFDM_S_WX * np] = v.wx;
+    S[LFDM_S_UDOT * np] = v.udot;
+    S[LFDM_S_VDOT * np] = v.vdot;
+    S[LFDM_S_WXDOT * np] = va.wxdot;
+    S[LFDM_S_WZDOT * np] = va.wzdot;
+    S[LFDM_S_CRANKOMEGA * np] = v.crank;
+    S[LFDM_S_DOMEGA_CRANK * np] = va.dOmega_crank;
+    S[LFDM_S_CURRENT_GR * np] = (double)v.gear;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const size_t b = (size_t)(LFDM_S_TIRE0 + k * LFDM_S_TIRE_STRIDE) * np;
+        S[b + LFDM_T_XE * np] = ts[k].xe;
+        S[b + LFDM_T_YE * np] = ts[k].ye;
+        S[b + LFDM_T_XEDOT * np] = ts[k].xedot;
+        S[b + LFDM_T_YEDOT * np] = ts[k].yedot;
+        S[b + LFDM_T_OMEGA * np] = ts[k].omega;
+        S[b + LFDM_T_DOMEGA * np] = ta[k].dOmega;
+        S[b + LFDM_T_XT * np] = ta[k].xt;
+        S[b + LFDM_T_RSTAT * np] = ta[k].rStat;
+        S[b + LFDM_T_FX * np] = ta[k].fx;
+        S[b + LFDM_T_FY * np] = ta[k].fy;
+        S[b + LFDM_T_FZ * np] = ta[k].fz;
+        S[b + LFDM_T_VSX * np] = ta[k].vsx;
+        S[b + LFDM_T_VSY * np] = ta[k].vsy;
+        S[b + LFDM_T_MY * np] = ta[k].My;
+        S[b + LFDM_T_ENGTOR * np] = ta[k].engTor;
+    }
+    if (w.status) {
+        const bool bad = !(isfinite(v.x) && isfinite(v.y) && isfinite(v.u) && isfinite(v.v) && isfinite(v.psi) &&
+                           isfinite(v.wz) && isfinite(ts[0].omega) && isfinite(ts[1].omega) &&
+                           isfinite(ts[2].omega) && isfinite(ts[3].omega));
+        if (bad) w.status[vid] |= 1u;
+    }
+}
+
+template <int kCtl, bool kOut>
+static cudaError_t launch_mixed_t(const Window18& w, cudaStream_t stream) {
+    const int threads = w.threads;
+    const size_t smem = window18_mixed_smem(threads, w.nclasses);
+    auto kern = window18_mixed_kernel<kCtl, kOut>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<(w.n + threads - 1) / threads, threads, smem, stream>>>(w);
+    return cudaGetLastError();
+}
+
+template <int kCtl>
+static cudaError_t launch_mixed_o(const Window18& w, cudaStream_t s) {
+    return (w.resp && w.nsamples > 0) ? launch_mixed_t<kCtl, true>(w, s) : launch_mixed_t<kCtl, false>(w, s);
+}
+
+static cudaError_t launch_mixed(const Window18& w, cudaStream_t s) {
+    switch (w.ctl_mode) {
+        case CTL_TABLE: return launch_mixed_o<CTL_TABLE>(w, s);
+        case CTL_SCALAR: return launch_mixed_o<CTL_SCALAR>(w, s);
+        case CTL_SCHEDULE: return launch_mixed_o<CTL_SCHEDULE>(w, s);
+        default: return launch_mixed_o<CTL_ARRAY>(w, s);
+    }
+}
+
+void build_class_dev18f(const lfdm_class18& c, ClassDev18F* out) {
+    std::memset(out, 0, sizeof(*out));
+    out->nonLinearSteer = c.nonLinearSteer;
+    out->tcbool = c.tcbool;
+    out->throttleMod = c.throttleMod;
+    out->driveType = c.driveType;
+    out->whichWheels = c.whichWheels;
+    out->noGears = c.noGears;
+    for (int g = 0; g < c.noGears && g < LFDM_MAX_GEARS; ++g) {
+        out->gear[g] = (float)c.gearRatios[g];
+        out->down[g] = (float)c.shiftMap[g][0];
+        out->up[g] = (float)c.shiftMap[g][1];
+    }
+    auto mapf = [](const double (*pts)[2], int n, MapF& m) {
+        m.n = n;
+        for (int k = 0; k < n; ++k) {
+            m.x[k] = (float)pts[k][0];
+            m.y[k] = (float)pts[k][1];
+        }
+        for (int k = 0; k + 1 < n; ++k) {
+            m.dx[k] = m.x[k + 1] - m.x[k];
+            m.dy[k] = m.y[k + 1] - m.y[k];
+        }
+    };
+    mapf(c.steerMap, c.steerMapSize, out->steer);
+    mapf(c.powertrainMap, c.powertrainMapSize, out->pt);
+    mapf(c.lossesMap, c.lossesMapSize, out->loss);
+    mapf(c.CFmap, c.CFmapSize, out->cf);
+    mapf(c.TRmap, c.TRmapSize, out->tr);
+}
+size_t class_dev18f_size() { return sizeof(ClassDev18F); }
+
 template <bool kNr, int kCtl, bool kOut>
 static cudaError_t launch_t(const Window18& w, cudaStream_t stream) {
     const int threads = w.threads;
@@ -503,6 +766,10 @@ static cudaError_t launch_c(const Window18& w, cudaStream_t s) {
 cudaError_t launch_window18(const Window18& w, cudaStream_t stream) {
     if (w.n <= 0 || w.nsteps <= 0) return cudaSuccess;
     if (w.threads <= 0 || w.threads > 128 || (w.threads & 31)) return cudaErrorInvalidValue;
+    if (w.precision == LFDM_PREC_MIXED) {
+        if (w.tire_nr || !w.classes_f) return cudaErrorInvalidValue;
+        return launch_mixed(w, stream);
+    }
     return w.tire_nr ? launch_c<true>(w, stream) : launch_c<false>(w, stream);
 }
 

@@ -105,7 +105,7 @@ struct lfdm_solver {
     DevBuf<double> d_params, d_K, d_S, d_rows, d_aos, d_ctl, d_resp, d_sched;
     DevBuf<int64_t> d_off;
     DevBuf<int32_t> d_len, d_class_of, d_samples;
-    DevBuf<unsigned char> d_classes;
+    DevBuf<unsigned char> d_classes, d_classes_f;
     DevBuf<uint32_t> d_status;
     DevBuf<unsigned> d_bad;
     bool rows_device_only = false;  // driver rows live only in d_rows (bulk upload path)
@@ -176,6 +176,12 @@ int sync_device(lfdm_solver* h) {
             build_class_dev18(h->classes[i], reinterpret_cast<ClassDev18*>(buf.data() + i * cs));
         CK(h->d_classes.ensure(buf.size()));
         CK(cudaMemcpyAsync(h->d_classes.p, buf.data(), buf.size(), cudaMemcpyHostToDevice, h->stream));
+        const size_t csf = class_dev18f_size();
+        std::vector<unsigned char> buff(csf * std::max<size_t>(1, h->classes.size()));
+        for (size_t i = 0; i < h->classes.size(); ++i)
+            build_class_dev18f(h->classes[i], reinterpret_cast<ClassDev18F*>(buff.data() + i * csf));
+        CK(h->d_classes_f.ensure(buff.size()));
+        CK(cudaMemcpyAsync(h->d_classes_f.p, buff.data(), buff.size(), cudaMemcpyHostToDevice, h->stream));
         CK(h->d_class_of.ensure(N));
         CK(cudaMemcpyAsync(h->d_class_of.p, h->class_of.data(), N * sizeof(int32_t), cudaMemcpyHostToDevice,
                            h->stream));
@@ -333,6 +339,9 @@ int run_windows(lfdm_solver* h, double t0, double t_end, bool solve_all, int ctl
     w.dt = h->step;
     w.K = h->d_K.p;
     w.classes = reinterpret_cast<const ClassDev18*>(h->d_classes.p);
+    w.classes_f = reinterpret_cast<const ClassDev18F*>(h->d_classes_f.p);
+    if (h->precision == LFDM_PREC_MIXED && w.tire_nr)
+        return h->fail(LFDM_ERR_ARG, "the mixed-precision stepper supports TMeasy tires only");
     w.nclasses = (int)h->classes.size();
     w.class_of = h->d_class_of.p;
     w.S = h->d_S.p;
