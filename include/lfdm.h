@@ -102,6 +102,18 @@ enum { /* offsets inside one tire block */
     LFDM_T_FX, LFDM_T_FY, LFDM_T_FZ, LFDM_T_VSX, LFDM_T_VSY, LFDM_T_MY, LFDM_T_ENGTOR
 };
 
+/* Flat per-vehicle state vector, 11-DOF: VehicleState (11dof-gpu/dof11_gpu.cuh:704-765) then      */
+/* TMeasyState of the front and the rear tire (same 15-field block as the 18-DOF model).            */
+enum {
+    LFDM11_S_X = 0, LFDM11_S_Y, LFDM11_S_U, LFDM11_S_V, LFDM11_S_PSI, LFDM11_S_WZ, LFDM11_S_UDOT, LFDM11_S_VDOT,
+    LFDM11_S_WZDOT, LFDM11_S_CRANKOMEGA, LFDM11_S_DOMEGA_CRANK, LFDM11_S_CURRENT_GR,
+    LFDM11_S_TIRE0 = 12, /* front tire block; rear tire at LFDM11_S_TIRE0 + LFDM_S_TIRE_STRIDE */
+    LFDM11_S_COUNT = 42
+};
+/* 11-DOF response channels (11dof-gpu/dof11_halfImplicit_gpu.cu:893-904): time, x, y, u, v, psi, wz, */
+/* front wheel speed, rear wheel speed.                                                              */
+#define LFDM11_RESP_CHANNELS 9
+
 /* Response channels written every output sample, in this order (dof18_halfImplicit_gpu.cu:954-974): */
 /* time, x, y, u(vx), v(vy), phi(roll), psi(yaw), wx(roll rate), wz(yaw rate), wlf, wrf, wlr, wrr.  */
 #define LFDM18_RESP_CHANNELS 13

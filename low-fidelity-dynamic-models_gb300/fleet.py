@@ -59,6 +59,36 @@ def suv18() -> tuple[Class18, np.ndarray]:
     return vehicle_from_json(SUV18_VEHICLE, SUV_TIRE, TIRE_TMEASY)
 
 
+# The same SUV for the 11-DOF (single-track) model: its JSON holds only the 11-DOF keys.
+SUV11_VEHICLE = {k: v for k, v in SUV18_VEHICLE.items()
+                 if k not in ("jx", "jxz", "cf", "cr", "hrcf", "hrcr", "krof", "kror", "brof", "bror")}
+
+
+def suv11() -> tuple[Class18, np.ndarray]:
+    return vehicle_from_json(SUV11_VEHICLE, SUV_TIRE, TIRE_TMEASY, model=11)
+
+
+def fleet11(n: int, seed: int = 20261203, horizon: float = 10.0, table_dt: float = 0.01,
+            u0_range=(0.0, 20.0)) -> dict:
+    """The seeded 11-DOF SUV fleet: one shared parameter set, per-vehicle driver tables (sine steering,
+    throttle ramp, no brake) and initial speeds U[0, 20] m/s with the wheels rolling (omega = u0/r0)
+    and the gear/crank set as in initial_states. States follow the LFDM11_S_* layout."""
+    from ._abi import C
+    rng = np.random.default_rng(seed)
+    cls, base = suv11()
+    params = np.repeat(base[None, :], n, axis=0)
+    tables = driver_tables(n, rng, horizon, table_dt, params[:, P["maxsteer"]], brake_pulse=False)
+    s18 = initial_states(cls, params, rng, u0_range)
+    s = np.zeros((n, C["LFDM11_S_COUNT"]))
+    s[:, C["LFDM11_S_U"]] = s18[:, S["u"]]
+    s[:, C["LFDM11_S_CRANKOMEGA"]] = s18[:, S["crankomega"]]
+    s[:, C["LFDM11_S_CURRENT_GR"]] = s18[:, S["current_gr"]]
+    for k in range(2):
+        s[:, C["LFDM11_S_TIRE0"] + k * S_TIRE_STRIDE + T["omega"]] = s18[:, S_TIRE0 + T["omega"]]
+    return {"cls": [cls], "class_of": np.zeros(n, dtype=np.int32), "params": params, "tables": tables,
+            "states": s, "seed": seed, "horizon": horizon}
+
+
 def jitter_params(base: np.ndarray, n: int, rng: np.random.Generator, frac: float = 0.1) -> np.ndarray:
     """Per-vehicle copies of `base` with mass, Jz, CG position (a; b = wheelbase - a), tire vertical
     stiffness and peak-friction scale drawn uniformly within +/-frac of the base values. The

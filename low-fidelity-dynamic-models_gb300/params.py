@@ -73,18 +73,25 @@ def default_params() -> np.ndarray:
     return p
 
 
-def vehicle_from_json(veh, tire, tire_type: int = TIRE_TMEASY) -> tuple[Class18, np.ndarray]:
+_VEH_KEYS_11 = ["a", "b", "m", "h", "jz", "muf", "mur"]  # setVehParamsJSON, 11dof-gpu/dof11_gpu.cu:910-1044
+_DOUBLED_11 = ["jw", "rr", "pn", "pnmax", "cx", "cy", "kt", "dx", "dy", "fzrdynco", "rdyncocrit", "dfx0pn", "dfx0p2n",
+               "fxmpn", "fxmp2n", "fxspn", "fxsp2n", "dfy0pn", "dfy0p2n", "fympn", "fymp2n", "fyspn", "fysp2n"]
+_KEY_OF = {k.lower(): k for k in _TM_KEYS}
+
+
+def vehicle_from_json(veh, tire, tire_type: int = TIRE_TMEASY, model: int = 18) -> tuple[Class18, np.ndarray]:
     """Parse a vehicle JSON and a tire JSON (paths or dicts) the way Construct does.
 
     Returns the class record and the flat parameter vector with tireInit applied
     (d18SolverHalfImplicitGPU::Construct calls tireInit after loading, dof18_halfImplicit_gpu.cu:78).
+    model 11 reads the 11-DOF vehicle keys (11dof-gpu/dof11_gpu.cu:910-1044).
     """
     d = _load(veh)
     t = _load(tire)
     p = default_params()
     c = Class18()
     c.driveType, c.whichWheels = 1, 1
-    for k in _VEH_KEYS:
+    for k in (_VEH_KEYS_11 if model == 11 else _VEH_KEYS):
         p[P[k]] = float(d[k])
     c.nonLinearSteer = int(bool(d["nonLinearSteer"]))
     if c.nonLinearSteer:
@@ -118,6 +125,12 @@ def vehicle_from_json(veh, tire, tire_type: int = TIRE_TMEASY) -> tuple[Class18,
     if tire_type == TIRE_TMEASY:
         for k in _TM_KEYS:
             p[P[k.lower()]] = float(t[k])
+        if model == 11:
+            # the single-track tire stands for both wheels of an axle: setTireParamsJSON
+            # (11dof-gpu/dof11_gpu.cu:1046-1099) doubles the inertia, resistance, loads,
+            # stiffnesses, dampings, slopes and forces, and keeps r0, rdynco weights and slips
+            for k in _DOUBLED_11:
+                p[P[k]] = float(t[_KEY_OF[k]]) * 2.0
     elif tire_type == TIRE_TMEASY_NR:
         if t.get("highLevelParams", False):
             raise NotImplementedError("TMeasyNr high-level parameter guessing is not supported")

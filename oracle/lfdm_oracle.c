@@ -659,18 +659,288 @@ static void run_vehicle(const oracle18_args* a, int i) {
     store_state(a->states + (size_t)i * LFDM_S_COUNT, &v, t);
 }
 
+/* ---------------------------------------------------------------------------------------------- */
+/* 11-DOF model (11dof-gpu/dof11_gpu.cu, 11dof-gpu/dof11_halfImplicit_gpu.cu). The tire RHS,       */
+/* tmxy_combined, driveTorque and the lookups are the same functions as in the 18-DOF model.        */
+
+typedef struct {
+    double x, y, u, v, psi, wz, udot, vdot, wzdot, crankOmega, dOmega_crank;
+    int current_gr;
+} Veh11;
+
+/* computeTireLoads: dof11_gpu.cu:234-252 */
+static void computeTireLoads11(double* loads, const Veh11* v, const Par* pp) {
+    double huf = P(LFDM_P_R0);
+    double hur = P(LFDM_P_R0);
+    const double a = P(LFDM_P_A), b = P(LFDM_P_B), m = P(LFDM_P_M), h = P(LFDM_P_H);
+    const double muf = P(LFDM_P_MUF), mur = P(LFDM_P_MUR);
+    double Z1 = (m * G * b) / (2. * (a + b)) + (muf * G) / 2.;
+    double Z2 = ((m * h + muf * huf + mur * hur) * (v->udot - v->wz * v->v)) / (2. * (a + b));
+    loads[0] = (Z1 - Z2) > 0. ? (Z1 - Z2) : 0.;
+    double Z3 = (m * G * a) / (2. * (a + b)) + (mur * G) / 2.;
+    loads[1] = (Z3 + Z2) > 0. ? (Z3 + Z2) : 0.;
+}
+
+/* vehToTireTransform: dof11_gpu.cu:41-68 */
+static void vehToTireTransform11(Tire* t, const Veh11* v, const double* loads, const Par* pp, double steering) {
+    double delta = wheel_angle(pp, steering);
+    t[0].fz = loads[0];
+    t[0].vsy = v->v + v->wz * P(LFDM_P_A);
+    t[0].vsx = v->u * cos(delta) + t[0].vsy * sin(delta);
+    t[1].fz = loads[1];
+    t[1].vsy = v->v - v->wz * P(LFDM_P_B);
+    t[1].vsx = v->u;
+}
+
+/* tireToVehTransform: 11dof/dof11.cpp:100-124 — both front forces rotated by the wheel angle. (The  */
+/* GPU twin, 11dof-gpu/dof11_gpu.cu:98-123, computes the rotated lateral force but never stores it; */
+/* the reference's GPU test pin 104.805 m on double_lane4, tests/11dof_gpu.cu:77, holds only with    */
+/* the CPU behaviour, which is the one restated here.)                                              */
+static void tireToVehTransform11(Tire* t, const Par* pp, double steering) {
+    double delta = wheel_angle(pp, steering);
+    double fx = t[0].fx * cos(delta) - t[0].fy * sin(delta);
+    double fy = t[0].fx * sin(delta) + t[0].fy * cos(delta);
+    t[0].fx = fx;
+    t[0].fy = fy;
+}
+
+/* differentialSplit: dof11_gpu.cu:276-315 */
+static void differentialSplit11(double torque, double max_bias, double speed_rear, double speed_front,
+                                double* torque_rear, double* torque_front, int split, int whichWheels) {
+    double diff = fabs(speed_rear - speed_front);
+    if (split) {
+        double bias = 1;
+        if (diff > 0.5) bias = max_bias;
+        else if (diff > 0.25) bias = 4 * (max_bias - 1) * diff + (2 - max_bias);
+        double alpha = bias / (1 + bias);
+        double slow = alpha * torque;
+        double fast = torque - slow;
+        if (fabs(speed_rear) < fabs(speed_front)) {
+            *torque_rear = slow;
+            *torque_front = fast;
+        } else {
+            *torque_rear = fast;
+            *torque_front = slow;
+        }
+    } else {
+        if (whichWheels) {
+            *torque_rear = torque;
+            *torque_front = 0;
+        } else {
+            *torque_rear = 0;
+            *torque_front = torque;
+        }
+    }
+}
+
+/* computePowertrainRHS: dof11_gpu.cu:601-745 */
+static void powertrainRHS11(Veh11* v, Tire* t, const Par* pp, const double* controls) {
+    const lfdm_class18* c = pp->c;
+    double torque_t = 0;
+    double max_bias = 2;
+    const double throttle = controls[2], braking = controls[3];
+    if (c->tcbool) {
+        int tc_reverse_flow = 0;
+        double omega_t = 0.5 * (t[0].omega + t[1].omega);
+        double omega_out = omega_t / (c->gearRatios[v->current_gr]);
+        double omega_in = v->crankOmega;
+        double sr, cf, tr;
+        if ((omega_out < 1e-9) || (omega_in < 1e-9)) {
+            sr = 0;
+            cf = oracle_map_y(&c->CFmap[0][0], c->CFmapSize, sr);
+            tr = oracle_map_y(&c->TRmap[0][0], c->TRmapSize, sr);
+        } else {
+            sr = omega_out / omega_in;
+            if (sr > 1.) {
+                sr = 1. - (sr - 1.);
+                tc_reverse_flow = 1;
+            }
+            if (sr < 0) sr = 0;
+            cf = oracle_map_y(&c->CFmap[0][0], c->CFmapSize, sr);
+            tr = oracle_map_y(&c->TRmap[0][0], c->TRmapSize, sr);
+        }
+        double torque_in = -pow((omega_in / cf), 2);
+        if (tc_reverse_flow) torque_in = -torque_in;
+        double torque_out;
+        if (tc_reverse_flow) torque_out = -torque_in;
+        else torque_out = -tr * torque_in;
+        torque_t = torque_out / c->gearRatios[v->current_gr];
+        if ((v->u - 0) < 1e-9 && (torque_t < 0)) torque_t = 0;
+        v->dOmega_crank = (1. / P(LFDM_P_CRANKINERTIA)) * (driveTorque(pp, throttle, v->crankOmega) + torque_in);
+        if (omega_out > c->shiftMap[v->current_gr][1]) {
+            if (v->current_gr < c->noGears - 1) v->current_gr++;
+        } else if (omega_out < c->shiftMap[v->current_gr][0]) {
+            if (v->current_gr > 0) v->current_gr--;
+        }
+    } else {
+        v->crankOmega = 0.5 * (t[0].omega + t[1].omega) / c->gearRatios[v->current_gr];
+        torque_t = driveTorque(pp, throttle, v->crankOmega) / c->gearRatios[v->current_gr];
+        if ((v->u - 0) < 1e-9 && (torque_t < 0)) torque_t = 0;
+        if (v->crankOmega > c->shiftMap[v->current_gr][1]) {
+            if (v->current_gr < c->noGears - 1) v->current_gr++;
+        } else if (v->crankOmega < c->shiftMap[v->current_gr][0]) {
+            if (v->current_gr > 0) v->current_gr--;
+        }
+    }
+    differentialSplit11(torque_t, max_bias, t[1].omega, t[0].omega, &t[1].engTor, &t[0].engTor, c->driveType,
+                        c->whichWheels);
+    const double jw = P(LFDM_P_JW);
+    const double brake = P(LFDM_P_MAXBRAKETORQUE) * braking;
+    for (int k = 0; k < 2; ++k)
+        t[k].dOmega = (1 / jw) * (t[k].engTor + t[k].My - sgn(t[k].omega) * brake - t[k].fx * t[k].rStat);
+}
+
+/* computeVehRHS: dof11_gpu.cu:893-909 */
+static void vehRHS11(Veh11* v, const Par* pp, const double* fx, const double* fy) {
+    double mt = P(LFDM_P_M) + 2 * (P(LFDM_P_MUF) + P(LFDM_P_MUR));
+    v->vdot = -v->u * v->wz + (fy[0] + fy[1]) / mt;
+    v->udot = v->v * v->wz + (fx[0] + fx[1]) / mt;
+    v->wzdot = (P(LFDM_P_A) * fy[0] - P(LFDM_P_B) * fy[1]) / P(LFDM_P_JZ);
+}
+
+static void load_state11(const double* s, Veh11* v, Tire* t) {
+    v->x = s[LFDM11_S_X];
+    v->y = s[LFDM11_S_Y];
+    v->u = s[LFDM11_S_U];
+    v->v = s[LFDM11_S_V];
+    v->psi = s[LFDM11_S_PSI];
+    v->wz = s[LFDM11_S_WZ];
+    v->udot = s[LFDM11_S_UDOT];
+    v->vdot = s[LFDM11_S_VDOT];
+    v->wzdot = s[LFDM11_S_WZDOT];
+    v->crankOmega = s[LFDM11_S_CRANKOMEGA];
+    v->dOmega_crank = s[LFDM11_S_DOMEGA_CRANK];
+    v->current_gr = (int)s[LFDM11_S_CURRENT_GR];
+    for (int k = 0; k < 2; ++k) memcpy(&t[k], s + LFDM11_S_TIRE0 + k * LFDM_S_TIRE_STRIDE, sizeof(Tire));
+}
+static void store_state11(double* s, const Veh11* v, const Tire* t) {
+    s[LFDM11_S_X] = v->x;
+    s[LFDM11_S_Y] = v->y;
+    s[LFDM11_S_U] = v->u;
+    s[LFDM11_S_V] = v->v;
+    s[LFDM11_S_PSI] = v->psi;
+    s[LFDM11_S_WZ] = v->wz;
+    s[LFDM11_S_UDOT] = v->udot;
+    s[LFDM11_S_VDOT] = v->vdot;
+    s[LFDM11_S_WZDOT] = v->wzdot;
+    s[LFDM11_S_CRANKOMEGA] = v->crankOmega;
+    s[LFDM11_S_DOMEGA_CRANK] = v->dOmega_crank;
+    s[LFDM11_S_CURRENT_GR] = (double)v->current_gr;
+    for (int k = 0; k < 2; ++k) memcpy(s + LFDM11_S_TIRE0 + k * LFDM_S_TIRE_STRIDE, &t[k], sizeof(Tire));
+}
+
+/* rhsFun: 11dof-gpu/dof11_halfImplicit_gpu.cu:663-700 */
+static void rhs11(Veh11* v, Tire* t, const Par* pp, const double* controls, int nr) {
+    double loads[2] = {0., 0.};
+    computeTireLoads11(loads, v, pp);
+    vehToTireTransform11(t, v, loads, pp, controls[1]);
+    if (nr) {
+        tireRHS_Nr(&t[0], pp, controls[1]);
+        tireRHS_Nr(&t[1], pp, 0);
+    } else {
+        tireRHS_TM(&t[0], pp, controls[1]);
+        tireRHS_TM(&t[1], pp, 0);
+    }
+    powertrainRHS11(v, t, pp, controls);
+    tireToVehTransform11(t, pp, controls[1]);
+    double fx[2] = {t[0].fx, t[1].fx};
+    double fy[2] = {t[0].fy, t[1].fy};
+    vehRHS11(v, pp, fx, fy);
+}
+
+/* half-implicit update: 11dof-gpu/dof11_halfImplicit_gpu.cu:863-880 */
+static void update11(Veh11* v, Tire* t, const Par* pp, double step, int nr) {
+    for (int k = 0; k < 2; ++k) {
+        if (!nr) {
+            t[k].xe += t[k].xedot * step;
+            t[k].ye += t[k].yedot * step;
+        }
+        t[k].omega += t[k].dOmega * step;
+    }
+    if (pp->c->tcbool) v->crankOmega += v->dOmega_crank * step;
+    v->u += v->udot * step;
+    v->v += v->vdot * step;
+    v->wz += v->wzdot * step;
+    v->x += (v->u * cos(v->psi) - v->v * sin(v->psi)) * step;
+    v->y += (v->u * sin(v->psi) + v->v * cos(v->psi)) * step;
+    v->psi += v->wz * step;
+}
+
+static void window11(const oracle18_args* a, int i, Veh11* v, Tire* t, const Par* pp, double current_time,
+                     int64_t sample_base) {
+    const int nr = a->tire_type == LFDM_TIRE_TMEASY_NR;
+    const double step = a->dt;
+    double tt = current_time;
+    double kernel_time = 0;
+    int64_t stored = 0;
+    const double end_time = (tt + a->ksim) - step / 10.;
+    while (tt < end_time) {
+        double c[4];
+        controls_at(a, i, tt, c);
+        rhs11(v, t, pp, c, nr);
+        update11(v, t, pp, step, nr);
+        tt += step;
+        kernel_time += step;
+        if (a->resp && a->dtout > 0) {
+            if (fabs(kernel_time - (stored + 1) * a->dtout) < 1e-7) {
+                int64_t smp = sample_base + stored;
+                if (stored < a->samples_per_window && smp < a->resp_samples) {
+                    double* r = a->resp + (size_t)smp * LFDM11_RESP_CHANNELS * a->n;
+                    const double ch[LFDM11_RESP_CHANNELS] = {tt, v->x, v->y, v->u, v->v, v->psi, v->wz,
+                                                             t[0].omega, t[1].omega};
+                    for (int k = 0; k < LFDM11_RESP_CHANNELS; ++k) r[(size_t)k * a->n + i] = ch[k];
+                }
+                stored++;
+            }
+        }
+    }
+}
+
+static void run_vehicle11(const oracle18_args* a, int i) {
+    Veh11 v;
+    Tire t[2];
+    Par pp = {a->params + (size_t)i * LFDM_P_COUNT, &a->classes[a->class_of[i]]};
+    const int nr = a->tire_type == LFDM_TIRE_TMEASY_NR;
+    load_state11(a->states + (size_t)i * LFDM11_S_COUNT, &v, t);
+    if (a->schedule == 0) {
+        /* d11SolverHalfImplicit::Integrate (11dof/dof11_halfImplicit.cpp) */
+        double tt = a->t0;
+        while (tt < (a->tend - a->dt / 10.)) {
+            double c[4];
+            controls_at(a, i, tt, c);
+            rhs11(&v, t, &pp, c, nr);
+            update11(&v, t, &pp, a->dt, nr);
+            tt += a->dt;
+        }
+    } else if (a->schedule == 1) {
+        double current_time = a->t0;
+        int64_t w = 0;
+        while (current_time < a->tend) {
+            window11(a, i, &v, t, &pp, current_time, w * a->samples_per_window);
+            current_time = current_time + a->ksim;
+            ++w;
+        }
+    } else {
+        window11(a, i, &v, t, &pp, a->t0, 0);
+    }
+    store_state11(a->states + (size_t)i * LFDM11_S_COUNT, &v, t);
+}
+
+typedef void (*vehicle_fn)(const oracle18_args*, int);
+
 typedef struct {
     const oracle18_args* a;
+    vehicle_fn fn;
     int lo, hi;
 } Chunk;
 
 static void* worker(void* p) {
     Chunk* c = (Chunk*)p;
-    for (int i = c->lo; i < c->hi; ++i) run_vehicle(c->a, i);
+    for (int i = c->lo; i < c->hi; ++i) c->fn(c->a, i);
     return NULL;
 }
 
-int oracle18_run(const oracle18_args* a) {
+static int run_all(const oracle18_args* a, vehicle_fn fn) {
     if (!a || a->n < 0 || !a->classes || !a->class_of || !a->params || !a->states) return 1;
     if (!a->drv_rows && !a->ctl) return 1;
     if (a->drv_rows && (!a->drv_off || !a->drv_len)) return 1;
@@ -678,13 +948,14 @@ int oracle18_run(const oracle18_args* a) {
     int nt = a->nthreads < 1 ? 1 : a->nthreads;
     if (nt > a->n) nt = a->n > 0 ? a->n : 1;
     if (nt == 1) {
-        for (int i = 0; i < a->n; ++i) run_vehicle(a, i);
+        for (int i = 0; i < a->n; ++i) fn(a, i);
         return 0;
     }
     pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nt);
     Chunk* ch = (Chunk*)malloc(sizeof(Chunk) * nt);
     for (int k = 0; k < nt; ++k) {
         ch[k].a = a;
+        ch[k].fn = fn;
         ch[k].lo = (int)((long)a->n * k / nt);
         ch[k].hi = (int)((long)a->n * (k + 1) / nt);
         pthread_create(&th[k], NULL, worker, &ch[k]);
@@ -694,3 +965,6 @@ int oracle18_run(const oracle18_args* a) {
     free(ch);
     return 0;
 }
+
+int oracle18_run(const oracle18_args* a) { return run_all(a, run_vehicle); }
+int oracle11_run(const oracle18_args* a) { return run_all(a, run_vehicle11); }

@@ -46,6 +46,8 @@ typedef struct {
 
 /* Returns 0 on success, nonzero on bad arguments. */
 int oracle18_run(const oracle18_args* a);
+/* The 11-DOF model with the same arguments: states [n][LFDM11_S_COUNT], resp [samples][9][n]. */
+int oracle11_run(const oracle18_args* a);
 
 /* tireInit (18dof-gpu/dof18_gpu.cu:227-241) on one flat parameter vector. */
 void oracle_tire_init(double* params);

@@ -144,5 +144,67 @@ def main(ref: str) -> None:
     print(f"wrote {len(cases)} cases; e.g. {cases[0]['name']} x={cases[0]['expected_final'][0]!r}")
 
 
+def main11(ref: str) -> None:
+    """golden11.json: the reference's 11-DOF CPU solver (oracle/refrun11.cpp) on HMMWV fixtures and on
+    seeded 11-DOF SUV vehicles (one shared parameter set, as in the 11-DOF fleet)."""
+    refrun = os.path.join(ROOT, "oracle", "_ref", "refrun11")
+    d11 = os.path.join(ref, "11dof-gpu", "data")
+    veh = json.load(open(os.path.join(d11, "json", "HMMWV", "vehicle.json")))
+    tire = json.load(open(os.path.join(d11, "json", "HMMWV", "tmeasy.json")))
+    cases, jobs = [], []
+    S11 = {k: abi.C[f"LFDM11_S_{k.upper()}"] for k in ("u", "crankomega", "current_gr")}
+    with tempfile.TemporaryDirectory() as tmp:
+        def write(name, text):
+            p = os.path.join(tmp, name)
+            with open(p, "w") as f:
+                f.write(text)
+            return p
+
+        vj, tj = write("v.json", json.dumps(veh)), write("t.json", json.dumps(tire))
+        for name, drv, ksim, tend in (("hmmwv11_acc3_cpu", "acc3", 0.0, None), ("hmmwv11_acc3_gpu22", "acc3", 2.0, 22.0),
+                                      ("hmmwv11_dl4_gpu", "double_lane4", 2.0, 22.0)):
+            rows = lfdm.params.load_driver_table(os.path.join(d11, "input", drv + ".txt")).tolist()
+            tp = write(f"{name}.txt", "".join(" ".join(_fmt(v) for v in r) + "\n" for r in rows))
+            tend_v = tend if tend is not None else rows[-1][0]
+            jobs += [f"veh {vj}", f"tire {tj}", "tiretype 0", f"driver {tp}", "dt 0.001", f"tend {_fmt(tend_v)}",
+                     f"ksim {_fmt(ksim)}", "sample 100", "run"]
+            cases.append({"name": name, "vehicle": veh, "tire": tire, "tire_type": 0, "driver": rows, "dt": 0.001,
+                          "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
+                          "state": [0.0] * abi.C["LFDM11_S_COUNT"], "source": f"HMMWV 11-DOF json, {drv}.txt"})
+        fl = fleet.fleet11(8, seed=SEED, horizon=10.0)
+        sj, stj = write("sv.json", json.dumps(fleet.SUV11_VEHICLE)), write("st.json", json.dumps(fleet.SUV_TIRE))
+        for i in range(8):
+            rows = fl["tables"][i].tolist()
+            tp = write(f"s{i}.txt", "".join(" ".join(_fmt(v) for v in r) + "\n" for r in rows))
+            st = fl["states"][i]
+            w0 = float(st[abi.C["LFDM11_S_TIRE0"] + abi.T["omega"]])
+            jobs += [f"veh {sj}", f"tire {stj}", "tiretype 0", f"driver {tp}", "dt 0.001", "tend 10", "ksim 1",
+                     "sample 250", f"vs u {_fmt(st[S11['u']])}", f"vs crankOmega {_fmt(st[S11['crankomega']])}",
+                     f"gear {int(st[S11['current_gr']])}", f"ts 0 omega {_fmt(w0)}", f"ts 1 omega {_fmt(w0)}", "run"]
+            cases.append({"name": f"suv11_{i}", "vehicle": fleet.SUV11_VEHICLE, "tire": fleet.SUV_TIRE, "tire_type": 0,
+                          "driver": rows, "dt": 0.001, "tend": 10.0, "ksim": 1.0, "sample": 250, "vp": {}, "tp": {},
+                          "state": st.tolist(), "source": f"synthetic 11-DOF SUV fleet seed {SEED} vehicle {i}"})
+        out = subprocess.run([refrun], input="\n".join(jobs) + "\n", capture_output=True, text=True, check=True)
+    results, cur = [], {"samples": []}
+    for line in out.stdout.splitlines():
+        tok = line.split()
+        if tok and tok[0] == "S":
+            cur["samples"].append([int(tok[1])] + [float(v) for v in tok[2:]])
+        elif tok and tok[0] == "F":
+            cur["final"] = [float(v) for v in tok[1:]]
+        elif tok and tok[0] == "E":
+            results.append(cur)
+            cur = {"samples": []}
+    assert len(results) == len(cases)
+    for c, r in zip(cases, results):
+        c["expected_samples"] = r["samples"]
+        c["expected_final"] = r["final"]
+    with open(os.path.join(HERE, "golden11.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "model": 11, "cases": cases}, f, separators=(",", ":"))
+    print(f"wrote {len(cases)} 11-DOF cases; {cases[0]['name']} x={cases[0]['expected_final'][0]!r}")
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/wheeled_vehicle_models")
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/wheeled_vehicle_models"
+    main(ref)
+    main11(ref)

@@ -35,6 +35,8 @@ def lib(fma: bool = False):
         L = ctypes.CDLL(path)
         L.oracle18_run.argtypes = [ctypes.c_void_p]
         L.oracle18_run.restype = ctypes.c_int
+        L.oracle11_run.argtypes = [ctypes.c_void_p]
+        L.oracle11_run.restype = ctypes.c_int
         L.oracle_map_y.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
         L.oracle_map_y.restype = ctypes.c_double
         L.oracle_driver_input.argtypes = [ctypes.c_double, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
@@ -63,10 +65,11 @@ def _ptr(a):
 
 
 def run18(classes, class_of, params, states, tables=None, ctl=None, *, tire_type=0, dt=1e-3, t0=0.0,
-          tend=10.0, ksim=2.0, schedule=1, dtout=0.0, nthreads=1, fma=False):
-    """Advance `states` ([n][75], copied) with the oracle. `tables` is a list of per-vehicle
-    [rows][4] arrays or one [n][rows][4] array. schedule 0 = CPU solver, 1 = GPU Solve,
-    2 = one SolveStep window. Returns (states, resp or None)."""
+          tend=10.0, ksim=2.0, schedule=1, dtout=0.0, nthreads=1, fma=False, model=18):
+    """Advance `states` ([n][75] for 18-DOF, [n][42] for 11-DOF; copied) with the oracle. `tables` is
+    a list of per-vehicle [rows][4] arrays or one [n][rows][4] array. schedule 0 = CPU solver,
+    1 = GPU Solve, 2 = one SolveStep window. Returns (states, resp or None)."""
+    nch = 13 if model == 18 else 9
     n = params.shape[0]
     cls_arr = (type(classes[0]) * len(classes))(*classes)
     class_of = np.ascontiguousarray(class_of, dtype=np.int32)
@@ -96,12 +99,13 @@ def run18(classes, class_of, params, states, tables=None, ctl=None, *, tire_type
                 windows += 1
                 ct = ct + ksim
         nsamp = windows * spw
-        resp = np.full((nsamp, 13, n), np.nan, dtype=np.float64)
+        resp = np.full((nsamp, nch, n), np.nan, dtype=np.float64)
     a = _Args(n=n, tire_type=tire_type, classes=ctypes.addressof(cls_arr), class_of=_ptr(class_of),
               params=_ptr(params), states=_ptr(st), drv_rows=_ptr(rows), drv_off=_ptr(off), drv_len=_ptr(ln),
               ctl=_ptr(ctl_arr), dt=dt, t0=t0, tend=tend, ksim=ksim, schedule=schedule, dtout=dtout,
               resp=_ptr(resp), resp_samples=nsamp, samples_per_window=spw, nthreads=nthreads)
-    rc = lib(fma).oracle18_run(ctypes.byref(a))
+    fn = lib(fma).oracle18_run if model == 18 else lib(fma).oracle11_run
+    rc = fn(ctypes.byref(a))
     if rc != 0:
         raise RuntimeError(f"oracle18_run failed rc={rc}")
     return st, resp
