@@ -17,10 +17,11 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import Class18, P, P_COUNT, S, S_COUNT, T, S_TIRE0, S_TIRE_STRIDE, RESP18
+from ._abi import Class18, P, P_COUNT, S, S_COUNT, T, S_TIRE0, S_TIRE_STRIDE, RESP18, S11, S11_COUNT, S11_TIRE0, RESP11
 
-__all__ = ["lib", "LfdmError", "d18SolverHalfImplicitGPU", "TireType", "Class18", "P", "S", "T", "S_COUNT",
-           "P_COUNT", "RESP18", "S_TIRE0", "S_TIRE_STRIDE"]
+__all__ = ["lib", "LfdmError", "d18SolverHalfImplicitGPU", "d11SolverHalfImplicitGPU", "TireType", "Class18", "P",
+           "S", "T", "S_COUNT", "P_COUNT", "RESP18", "S_TIRE0", "S_TIRE_STRIDE", "S11", "S11_COUNT", "S11_TIRE0",
+           "RESP11"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "liblfdm.so")
@@ -143,13 +144,17 @@ def load_driver_file(path: str) -> np.ndarray:
     return rows
 
 
-class d18SolverHalfImplicitGPU:
-    """18-DOF batched half-implicit stepper on one GPU (reference: d18SolverHalfImplicitGPU)."""
+class _SolverGPU:
+    """Batched half-implicit stepper on one GPU; the model is fixed by the subclass."""
+
+    MODEL = 18
+    STATE_COUNT = S_COUNT
+    RESP_CHANNELS = RESP18
 
     def __init__(self, total_num_vehicles: int, device: int = 0):
         self._L = lib()
         h = ctypes.c_void_p()
-        rc = self._L.lfdm_create_on_device(18, int(total_num_vehicles), int(device), ctypes.byref(h))
+        rc = self._L.lfdm_create_on_device(self.MODEL, int(total_num_vehicles), int(device), ctypes.byref(h))
         if rc:
             raise LfdmError(rc, self._L.lfdm_last_error(None).decode())
         self._h = h
@@ -185,8 +190,8 @@ class d18SolverHalfImplicitGPU:
                                         driver_inputs_file.encode() if driver_inputs_file else None, int(type)))
 
     def Initialize(self, state: np.ndarray, num_vehicles: int):
-        """Copy one flat state (S_COUNT doubles, include/lfdm.h order) into the next num_vehicles."""
-        s = _f64(state, (S_COUNT,))
+        """Copy one flat state (STATE_COUNT doubles, include/lfdm.h order) into the next num_vehicles."""
+        s = _f64(state, (self.STATE_COUNT,))
         self._ck(self._L.lfdm_initialize(self._h, _ptr(s), int(num_vehicles)))
 
     def SetTimeStep(self, step: float):
@@ -248,7 +253,7 @@ class d18SolverHalfImplicitGPU:
         return out.value
 
     def GetSimState(self, vehicle_index: int) -> np.ndarray:
-        s = np.zeros(S_COUNT)
+        s = np.zeros(self.STATE_COUNT)
         self._ck(self._L.lfdm_get_sim_state(self._h, int(vehicle_index), _ptr(s)))
         return s
 
@@ -276,12 +281,12 @@ class d18SolverHalfImplicitGPU:
             self._ck(self._L.lfdm_set_driver_tables(self._h, int(first), t.shape[0], _ptr(t), t.shape[1]))
 
     def set_states(self, states: np.ndarray, first: int = 0):
-        s = _f64(states).reshape(-1, S_COUNT)
+        s = _f64(states).reshape(-1, self.STATE_COUNT)
         self._ck(self._L.lfdm_set_states(self._h, int(first), s.shape[0], _ptr(s)))
 
     def get_states(self, first: int = 0, count: int | None = None) -> np.ndarray:
         count = self.n - first if count is None else count
-        s = np.zeros((count, S_COUNT))
+        s = np.zeros((count, self.STATE_COUNT))
         self._ck(self._L.lfdm_get_states(self._h, int(first), int(count), _ptr(s)))
         return s
 
@@ -289,7 +294,7 @@ class d18SolverHalfImplicitGPU:
         self._ck(self._L.lfdm_set_precision(self._h, int(precision)))
 
     def set_response_buffer(self, buf: np.ndarray | None, output_freq: float = 100.0):
-        """Stream Solve's SoA response [sample][13][N] into `buf` (float64, C-contiguous); samples
+        """Stream Solve's SoA response [sample][RESP_CHANNELS][N] into `buf` (float64, C-contiguous); samples
         beyond its capacity wrap around."""
         if buf is None:
             self._ck(self._L.lfdm_set_response_buffer(self._h, None, 0, 1.0))
@@ -332,6 +337,25 @@ class d18SolverHalfImplicitGPU:
         w = np.zeros(self.n, dtype=np.uint32)
         self._ck(self._L.lfdm_get_status_words(self._h, 0, self.n, _ptr(w)))
         return w
+
+
+class d18SolverHalfImplicitGPU(_SolverGPU):
+    """18-DOF batched half-implicit stepper on one GPU (reference: 18dof-gpu/dof18_halfImplicit_gpu.cuh)."""
+
+    MODEL = 18
+    STATE_COUNT = S_COUNT
+    RESP_CHANNELS = RESP18
+
+
+class d11SolverHalfImplicitGPU(_SolverGPU):
+    """11-DOF batched half-implicit stepper on one GPU (reference: 11dof-gpu/dof11_halfImplicit_gpu.cuh).
+
+    States use the LFDM11_S_* layout (S11): chassis X, Y, u, v, psi, wz, their rates, crank speed,
+    crank acceleration, current gear, then the front and rear TMeasy tire blocks; FP64 only."""
+
+    MODEL = 11
+    STATE_COUNT = S11_COUNT
+    RESP_CHANNELS = RESP11
 
 
 def measure_fp64_peak(device: int = 0) -> float:

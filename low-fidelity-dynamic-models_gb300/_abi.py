@@ -45,12 +45,17 @@ MAX_GEARS = C["LFDM_MAX_GEARS"]
 RESP18 = C["LFDM18_RESP_CHANNELS"]
 S_TIRE0 = C["LFDM_S_TIRE0"]
 S_TIRE_STRIDE = C["LFDM_S_TIRE_STRIDE"]
+S11_COUNT = C["LFDM11_S_COUNT"]
+S11_TIRE0 = C["LFDM11_S_TIRE0"]
+RESP11 = C["LFDM11_RESP_CHANNELS"]
 
 # name -> index maps, e.g. P["m"] == LFDM_P_M, S["x"] == LFDM_S_X, T["omega"] == LFDM_T_OMEGA
 P = {k[len("LFDM_P_"):].lower(): v for k, v in C.items() if k.startswith("LFDM_P_") and k != "LFDM_P_COUNT"}
 S = {k[len("LFDM_S_"):].lower(): v for k, v in C.items() if k.startswith("LFDM_S_") and k not in (
     "LFDM_S_COUNT", "LFDM_S_TIRE0", "LFDM_S_TIRE_STRIDE")}
 T = {k[len("LFDM_T_"):].lower(): v for k, v in C.items() if k.startswith("LFDM_T_")}
+S11 = {k[len("LFDM11_S_"):].lower(): v for k, v in C.items() if k.startswith("LFDM11_S_") and k not in (
+    "LFDM11_S_COUNT", "LFDM11_S_TIRE0")}
 
 TIRE_TMEASY = C["LFDM_TIRE_TMEASY"]
 TIRE_TMEASY_NR = C["LFDM_TIRE_TMEASY_NR"]

@@ -44,6 +44,8 @@ enum K18 : int {
     K_CX, K_CY, K_DX, K_DY, K_FXMP2N, K_FYMP2N, K_RR,
     // TMeasyNr extras (dof18_gpu.cu:532-662)
     K_MU, K_VCOUL, K_FRB0, K_FRB1,
+    // 11-DOF yaw (11dof-gpu/dof11_gpu.cu:893-909)
+    K_INVJZ,
     K18_COUNT
 };
 

@@ -278,7 +278,7 @@ void tire_init(double* p) {
     p[LFDM_P_RDYNCOCRIT] = r1 + (r2 - r1) * (fz / pn - 1.);
 }
 
-bool load_vehicle18(const std::string& veh_path, const std::string& tire_path, int tire_type, lfdm_class18& c,
+bool load_vehicle(int model, const std::string& veh_path, const std::string& tire_path, int tire_type, lfdm_class18& c,
                     double* p, std::string& err) {
     default_vehicle(c, p);
     JVal vd, td;
@@ -295,7 +295,13 @@ bool load_vehicle18(const std::string& veh_path, const std::string& tire_path, i
               {"hrcr", LFDM_P_HRCR}, {"krof", LFDM_P_KROF}, {"kror", LFDM_P_KROR}, {"brof", LFDM_P_BROF},
               {"bror", LFDM_P_BROR}};
     bool ok = true;
-    for (auto& e : vk) ok = ok && v.num(e.k, p[e.i]);
+    for (auto& e : vk) {
+        // the 11-DOF vehicle file holds only a, b, m, h, jz, muf, mur (11dof-gpu/dof11_gpu.cu:910-1044)
+        if (model == LFDM_MODEL_11 && !(e.i == LFDM_P_A || e.i == LFDM_P_B || e.i == LFDM_P_M || e.i == LFDM_P_H ||
+                                        e.i == LFDM_P_JZ || e.i == LFDM_P_MUF || e.i == LFDM_P_MUR))
+            continue;
+        ok = ok && v.num(e.k, p[e.i]);
+    }
     bool b = false;
     ok = ok && v.boolean("nonLinearSteer", b);
     c.nonLinearSteer = b;
@@ -378,6 +384,19 @@ bool load_vehicle18(const std::string& veh_path, const std::string& tire_path, i
               {"sysP2n", LFDM_P_SYSP2N}};
     if (tire_type == LFDM_TIRE_TMEASY) {
         for (auto& e : tk) ok = ok && t.num(e.k, p[e.i]);
+        if (ok && model == LFDM_MODEL_11) {
+            // single-track tire = both wheels of an axle: setTireParamsJSON (11dof-gpu/dof11_gpu.cu:1046-1099)
+            // doubles these fields and keeps r0, the rdynco weights and the slips
+            static const int dbl[] = {LFDM_P_JW,     LFDM_P_RR,     LFDM_P_PN,       LFDM_P_PNMAX,      LFDM_P_CX,
+                                      LFDM_P_CY,     LFDM_P_KT,     LFDM_P_DX,       LFDM_P_DY,         LFDM_P_FZRDYNCO,
+                                      LFDM_P_RDYNCOCRIT, LFDM_P_DFX0PN, LFDM_P_DFX0P2N, LFDM_P_FXMPN, LFDM_P_FXMP2N,
+                                      LFDM_P_FXSPN,  LFDM_P_FXSP2N, LFDM_P_DFY0PN,   LFDM_P_DFY0P2N,    LFDM_P_FYMPN,
+                                      LFDM_P_FYMP2N, LFDM_P_FYSPN,  LFDM_P_FYSP2N};
+            for (int i : dbl) p[i] *= 2.;
+        }
+    } else if (model == LFDM_MODEL_11) {
+        err = tire_path + ": TMeasyNr tires are not available for the 11-DOF model";
+        return false;
     } else {
         const JVal* hl = td.get("highLevelParams");
         if (hl && hl->kind == JVal::Bool && hl->b) {

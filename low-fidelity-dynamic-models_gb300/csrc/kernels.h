@@ -52,9 +52,12 @@ size_t window18_smem(int threads, int nclasses);
 // Derived per-vehicle constants: params AoS [n][LFDM_P_COUNT] (device) -> K SoA [K18_COUNT][npad].
 cudaError_t launch_prepare18(const double* params_dev, int n, int npad, double* K_dev, cudaStream_t stream);
 
-// AoS [n][LFDM_S_COUNT] <-> SoA [LFDM_S_COUNT][npad] (device buffers).
-cudaError_t launch_states_to_soa(const double* aos, int n, int npad, double* soa, cudaStream_t stream);
-cudaError_t launch_states_to_aos(const double* soa, int n, int npad, double* aos, cudaStream_t stream);
+// AoS [n][ns] <-> SoA [ns][npad] (device buffers); ns = doubles per state vector of the model.
+cudaError_t launch_states_to_soa(const double* aos, int n, int ns, int npad, double* soa, cudaStream_t stream);
+cudaError_t launch_states_to_aos(const double* soa, int n, int ns, int npad, double* aos, cudaStream_t stream);
+
+// 11-DOF window (same Window18 fields; states in the LFDM11_S_* layout, 9 response channels).
+cudaError_t launch_window11(const Window18& w, cudaStream_t stream);
 
 // Counts table rows whose time is smaller than the previous row's (per vehicle, equal-length tables
 // of nrows rows each; shared != 0: one table). *bad_dev must be zeroed by the caller.

@@ -1,0 +1,314 @@
+// 11-DOF (single-track) stepper: right-hand side, half-implicit update and window kernel.
+//
+// Algorithm: rhsFun (11dof-gpu/dof11_halfImplicit_gpu.cu:663-700) and the Integrate update
+// (:855-880) with the physics of 11dof-gpu/dof11_gpu.cu, whose tire model, tmxy_combined, driveTorque
+// and lookups are the 18-DOF ones (shared here through dof18_device.cuh). The front lateral force
+// is rotated into the vehicle frame as in the reference's CPU solver (11dof/dof11.cpp:100-124); see
+// the oracle for the GPU-twin discrepancy. Derived constants come from the same prepare kernel
+// as the 18-DOF model (K_Z1F, K_Z4 and K_Z1R are exactly the 11-DOF axle-load terms).
+#include <cuda_runtime.h>
+
+#include "dof18_device.cuh"
+#include "kernels.h"
+#include "window_common.cuh"
+
+namespace lfdm {
+
+struct Veh11 {
+    double x, y, u, v, psi, wz, udot, vdot, crank;
+    int gear;
+};
+struct Veh11Aux {
+    double wzdot, dOmega_crank;
+};
+
+// differentialSplit (11dof-gpu/dof11_gpu.cu:276-315), max_bias = 2
+__device__ __forceinline__ void diff_split11(double torque, double w_rear, double w_front, double& t_rear,
+                                             double& t_front, int split, int whichWheels) {
+    if (split) {
+        const double diff = fabs(w_rear - w_front);
+        double alpha;
+        if (diff > 0.5) alpha = 2.0 / 3.0;
+        else if (diff > 0.25) {
+            const double bias = 4 * (2.0 - 1) * diff + (2 - 2.0);
+            alpha = bias / (1 + bias);
+        } else alpha = 0.5;
+        const double slow = alpha * torque;
+        const double fast = torque - slow;
+        if (fabs(w_rear) < fabs(w_front)) {
+            t_rear = slow;
+            t_front = fast;
+        } else {
+            t_rear = fast;
+            t_front = slow;
+        }
+    } else if (whichWheels) {
+        t_rear = torque;
+        t_front = 0;
+    } else {
+        t_rear = 0;
+        t_front = torque;
+    }
+}
+
+__device__ __forceinline__ void step11(Veh11& v, Veh11Aux& va, TireC* ts, TireAux* ta, const KView& K,
+                                       const ClassDev18& C, double steering, double throttle, double braking,
+                                       double dt) {
+    // computeTireLoads (dof11_gpu.cu:234-252)
+    {
+        const double Z2 = K(K_Z4) * fma(-v.wz, v.v, v.udot);
+        ta[0].fz = fmax(K(K_Z1F) - Z2, 0.0);
+        ta[1].fz = fmax(K(K_Z1R) + Z2, 0.0);
+    }
+    // vehToTireTransform (dof11_gpu.cu:41-68)
+    const double delta = C.nonLinearSteer ? map_y(C.steer, steering) : steering * K(K_MAXSTEER);
+    double cd = 1.0, sd = 0.0;
+    if (delta != 0.0) sincos(delta, &sd, &cd);
+    const double vsyf = fma(v.wz, K(K_A), v.v);
+    ta[0].vsy = vsyf;
+    ta[0].vsx = fma(v.u, cd, vsyf * sd);
+    ta[1].vsy = fma(-v.wz, K(K_B), v.v);
+    ta[1].vsx = v.u;
+    tire_rhs_tm<true>(ts[0], ta[0], K, cd, sd);
+    tire_rhs_tm<false>(ts[1], ta[1], K, 1.0, 0.0);
+    // computePowertrainRHS (dof11_gpu.cu:601-745)
+    double torque_t;
+    const int g = v.gear;
+    if (C.tcbool) {
+        bool reverse = false;
+        const double omega_out = 0.5 * (ts[0].omega + ts[1].omega) / C.gear[g];
+        const double omega_in = v.crank;
+        double sr = 0;
+        if (!((omega_out < 1e-9) || (omega_in < 1e-9))) {
+            sr = omega_out / omega_in;
+            if (sr > 1.) {
+                sr = 1. - (sr - 1.);
+                reverse = true;
+            }
+            if (sr < 0) sr = 0;
+        }
+        const double cf = map_y(C.cf, sr), tr = map_y(C.tr, sr);
+        const double r = omega_in / cf;
+        double torque_in = -(r * r);
+        if (reverse) torque_in = -torque_in;
+        const double torque_out = reverse ? -torque_in : -tr * torque_in;
+        torque_t = torque_out * C.invgear[g];
+        if (v.u < 1e-9 && torque_t < 0) torque_t = 0;
+        va.dOmega_crank = K(K_INVCI) * (drive_torque(C, throttle, v.crank) + torque_in);
+        if (omega_out > C.up[g]) {
+            if (g < C.noGears - 1) v.gear = g + 1;
+        } else if (omega_out < C.down[g]) {
+            if (g > 0) v.gear = g - 1;
+        }
+    } else {
+        v.crank = 0.5 * (ts[0].omega + ts[1].omega) / C.gear[g];
+        torque_t = drive_torque(C, throttle, v.crank) * C.invgear[g];
+        if (v.u < 1e-9 && torque_t < 0) torque_t = 0;
+        if (v.crank > C.up[g]) {
+            if (g < C.noGears - 1) v.gear = g + 1;
+        } else if (v.crank < C.down[g]) {
+            if (g > 0) v.gear = g - 1;
+        }
+    }
+    diff_split11(torque_t, ts[1].omega, ts[0].omega, ta[1].engTor, ta[0].engTor, C.driveType, C.whichWheels);
+    const double brake = K(K_MAXBRAKE) * braking, ijw = K(K_INVJW);
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+        ta[k].dOmega = ijw * (fma(-sgnd(ts[k].omega), brake, ta[k].engTor + ta[k].My) - ta[k].fx * ta[k].rStat);
+    // tireToVehTransform (11dof/dof11.cpp:100-124): both front forces rotated
+    {
+        const double fx = ta[0].fx, fy = ta[0].fy;
+        ta[0].fx = fma(fx, cd, -fy * sd);
+        ta[0].fy = fma(fx, sd, fy * cd);
+    }
+    // computeVehRHS (dof11_gpu.cu:893-909)
+    const double im = K(K_INVMT);
+    v.vdot = fma(-v.u, v.wz, (ta[0].fy + ta[1].fy) * im);
+    v.udot = fma(v.v, v.wz, (ta[0].fx + ta[1].fx) * im);
+    va.wzdot = fma(K(K_A), ta[0].fy, -K(K_B) * ta[1].fy) * K(K_INVJZ);
+    // half-implicit update (dof11_halfImplicit_gpu.cu:863-880)
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        ts[k].xe = fma(ts[k].xedot, dt, ts[k].xe);
+        ts[k].ye = fma(ts[k].yedot, dt, ts[k].ye);
+        ts[k].omega = fma(ta[k].dOmega, dt, ts[k].omega);
+    }
+    if (C.tcbool) v.crank = fma(va.dOmega_crank, dt, v.crank);
+    v.u = fma(v.udot, dt, v.u);
+    v.v = fma(v.vdot, dt, v.v);
+    v.wz = fma(va.wzdot, dt, v.wz);
+    double sp, cp;
+    sincos(v.psi, &sp, &cp);
+    v.x = fma(fma(v.u, cp, -v.v * sp), dt, v.x);
+    v.y = fma(fma(v.u, sp, v.v * cp), dt, v.y);
+    v.psi = fma(v.wz, dt, v.psi);
+}
+
+template <int kCtl, bool kOut>
+__global__ void __launch_bounds__(128) window11_kernel(const Window18 w) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int tid = threadIdx.x;
+    const bool cls_smem = w.nclasses <= kMaxSmemClasses;
+    ClassDev18* cls = reinterpret_cast<ClassDev18*>(smem);
+    double* ks = reinterpret_cast<double*>(smem + (cls_smem ? (size_t)w.nclasses * sizeof(ClassDev18) : 0));
+    if (cls_smem) {
+        const int4* src = reinterpret_cast<const int4*>(w.classes);
+        int4* dst = reinterpret_cast<int4*>(smem);
+        const int words = (int)(w.nclasses * sizeof(ClassDev18) / 16);
+        for (int i = tid; i < words; i += blockDim.x) dst[i] = __ldg(src + i);
+    }
+    const int vid = blockIdx.x * blockDim.x + tid;
+    const bool active = vid < w.n;
+    if (active) {
+#pragma unroll 4
+        for (int k = 0; k < K18_COUNT; ++k) ks[k * blockDim.x + tid] = __ldg(w.K + (size_t)k * w.npad + vid);
+    }
+    __syncthreads();
+    if (!active) return;
+    const KView K{ks + tid, (int)blockDim.x};
+    const int ci = __ldg(w.class_of + vid);
+    const ClassDev18& C = cls_smem ? cls[ci] : w.classes[ci];
+    const size_t np = (size_t)w.npad;
+    double* S = w.S + vid;
+
+    Veh11 v;
+    Veh11Aux va;
+    TireC ts[2];
+    TireAux ta[2];
+    v.x = S[LFDM11_S_X * np];
+    v.y = S[LFDM11_S_Y * np];
+    v.u = S[LFDM11_S_U * np];
+    v.v = S[LFDM11_S_V * np];
+    v.psi = S[LFDM11_S_PSI * np];
+    v.wz = S[LFDM11_S_WZ * np];
+    v.udot = S[LFDM11_S_UDOT * np];
+    v.vdot = S[LFDM11_S_VDOT * np];
+    v.crank = S[LFDM11_S_CRANKOMEGA * np];
+    v.gear = (int)S[LFDM11_S_CURRENT_GR * np];
+    va.wzdot = S[LFDM11_S_WZDOT * np];
+    va.dOmega_crank = S[LFDM11_S_DOMEGA_CRANK * np];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const size_t b = (size_t)(LFDM11_S_TIRE0 + k * LFDM_S_TIRE_STRIDE) * np;
+        ts[k].xe = S[b + LFDM_T_XE * np];
+        ts[k].ye = S[b + LFDM_T_YE * np];
+        ts[k].xedot = S[b + LFDM_T_XEDOT * np];
+        ts[k].yedot = S[b + LFDM_T_YEDOT * np];
+        ts[k].omega = S[b + LFDM_T_OMEGA * np];
+        ta[k].dOmega = S[b + LFDM_T_DOMEGA * np];
+        ta[k].xt = S[b + LFDM_T_XT * np];
+        ta[k].rStat = S[b + LFDM_T_RSTAT * np];
+        ta[k].fx = S[b + LFDM_T_FX * np];
+        ta[k].fy = S[b + LFDM_T_FY * np];
+        ta[k].fz = S[b + LFDM_T_FZ * np];
+        ta[k].vsx = S[b + LFDM_T_VSX * np];
+        ta[k].vsy = S[b + LFDM_T_VSY * np];
+        ta[k].My = S[b + LFDM_T_MY * np];
+        ta[k].engTor = S[b + LFDM_T_ENGTOR * np];
+    }
+    DriverCursor cur;
+    double steer = w.steer, thr = w.thr, brk = w.brk;
+    if (kCtl == CTL_TABLE) {
+        driver_begin(cur, w.rows + 4 * __ldg(w.row_off + vid), __ldg(w.row_len + vid), w.t0);
+    } else if (kCtl == CTL_ARRAY) {
+        steer = __ldg(w.ctl + vid);
+        thr = __ldg(w.ctl + np + vid);
+        brk = __ldg(w.ctl + 2 * np + vid);
+    }
+    int next_k = 0;
+    int next_step = (kOut && w.nsamples > 0) ? __ldg(w.sample_steps) : -1;
+    double t = w.t0;
+    const double dt = w.dt;
+    for (int s = 0; s < w.nsteps; ++s) {
+        if (kCtl == CTL_TABLE) {
+            driver_at(cur, t, steer, thr, brk);
+        } else if (kCtl == CTL_SCHEDULE) {
+            steer = __ldg(w.sched + 3 * s);
+            thr = __ldg(w.sched + 3 * s + 1);
+            brk = __ldg(w.sched + 3 * s + 2);
+        }
+        step11(v, va, ts, ta, K, C, steer, thr, brk, dt);
+        t += dt;
+        if (kOut && s + 1 == next_step) {
+            double* r = w.resp + (size_t)next_k * LFDM11_RESP_CHANNELS * w.n + vid;
+            const size_t n = (size_t)w.n;
+            r[0 * n] = t;
+            r[1 * n] = v.x;
+            r[2 * n] = v.y;
+            r[3 * n] = v.u;
+            r[4 * n] = v.v;
+            r[5 * n] = v.psi;
+            r[6 * n] = v.wz;
+            r[7 * n] = ts[0].omega;
+            r[8 * n] = ts[1].omega;
+            ++next_k;
+            next_step = next_k < w.nsamples ? __ldg(w.sample_steps + next_k) : -1;
+        }
+    }
+    S[LFDM11_S_X * np] = v.x;
+    S[LFDM11_S_Y * np] = v.y;
+    S[LFDM11_S_U * np] = v.u;
+    S[LFDM11_S_V * np] = v.v;
+    S[LFDM11_S_PSI * np] = v.psi;
+    S[LFDM11_S_WZ * np] = v.wz;
+    S[LFDM11_S_UDOT * np] = v.udot;
+    S[LFDM11_S_VDOT * np] = v.vdot;
+    S[LFDM11_S_WZDOT * np] = va.wzdot;
+    S[LFDM11_S_CRANKOMEGA * np] = v.crank;
+    S[LFDM11_S_DOMEGA_CRANK * np] = va.dOmega_crank;
+    S[LFDM11_S_CURRENT_GR * np] = (double)v.gear;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const size_t b = (size_t)(LFDM11_S_TIRE0 + k * LFDM_S_TIRE_STRIDE) * np;
+        S[b + LFDM_T_XE * np] = ts[k].xe;
+        S[b + LFDM_T_YE * np] = ts[k].ye;
+        S[b + LFDM_T_XEDOT * np] = ts[k].xedot;
+        S[b + LFDM_T_YEDOT * np] = ts[k].yedot;
+        S[b + LFDM_T_OMEGA * np] = ts[k].omega;
+        S[b + LFDM_T_DOMEGA * np] = ta[k].dOmega;
+        S[b + LFDM_T_XT * np] = ta[k].xt;
+        S[b + LFDM_T_RSTAT * np] = ta[k].rStat;
+        S[b + LFDM_T_FX * np] = ta[k].fx;
+        S[b + LFDM_T_FY * np] = ta[k].fy;
+        S[b + LFDM_T_FZ * np] = ta[k].fz;
+        S[b + LFDM_T_VSX * np] = ta[k].vsx;
+        S[b + LFDM_T_VSY * np] = ta[k].vsy;
+        S[b + LFDM_T_MY * np] = ta[k].My;
+        S[b + LFDM_T_ENGTOR * np] = ta[k].engTor;
+    }
+    if (w.status) {
+        const bool bad = !(isfinite(v.x) && isfinite(v.y) && isfinite(v.u) && isfinite(v.v) && isfinite(v.psi) &&
+                           isfinite(v.wz) && isfinite(ts[0].omega) && isfinite(ts[1].omega));
+        if (bad) w.status[vid] |= 1u;
+    }
+}
+
+template <int kCtl, bool kOut>
+static cudaError_t launch11_t(const Window18& w, cudaStream_t stream) {
+    const int threads = w.threads;
+    const size_t smem = window18_smem(threads, w.nclasses);
+    auto kern = window11_kernel<kCtl, kOut>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<(w.n + threads - 1) / threads, threads, smem, stream>>>(w);
+    return cudaGetLastError();
+}
+
+template <int kCtl>
+static cudaError_t launch11_o(const Window18& w, cudaStream_t s) {
+    return (w.resp && w.nsamples > 0) ? launch11_t<kCtl, true>(w, s) : launch11_t<kCtl, false>(w, s);
+}
+
+cudaError_t launch_window11(const Window18& w, cudaStream_t stream) {
+    if (w.n <= 0 || w.nsteps <= 0) return cudaSuccess;
+    if (w.threads <= 0 || w.threads > 128 || (w.threads & 31)) return cudaErrorInvalidValue;
+    if (w.tire_nr || w.precision != LFDM_PREC_FP64) return cudaErrorInvalidValue;
+    switch (w.ctl_mode) {
+        case CTL_TABLE: return launch11_o<CTL_TABLE>(w, stream);
+        case CTL_SCALAR: return launch11_o<CTL_SCALAR>(w, stream);
+        case CTL_SCHEDULE: return launch11_o<CTL_SCHEDULE>(w, stream);
+        default: return launch11_o<CTL_ARRAY>(w, stream);
+    }
+}
+
+}  // namespace lfdm

@@ -18,6 +18,7 @@
 #include "dof18_device.cuh"
 #include "dof18_mixed.cuh"
 #include "kernels.h"
+#include "window_common.cuh"
 
 namespace lfdm {
 
@@ -120,6 +121,7 @@ __global__ void prepare18_kernel(const double* __restrict__ P, int n, int npad, 
     put(K_VCOUL, p[LFDM_P_VCOULOMB]);
     put(K_FRB0, p[LFDM_P_FRBLEND_BEGIN]);
     put(K_FRB1, p[LFDM_P_FRBLEND_END]);
+    put(K_INVJZ, 1. / jz);
 }
 
 cudaError_t launch_prepare18(const double* params_dev, int n, int npad, double* K_dev, cudaStream_t stream) {
@@ -131,17 +133,17 @@ cudaError_t launch_prepare18(const double* params_dev, int n, int npad, double* 
 // ---------------------------------------------------------------------------------------------
 // state transposes
 
-__global__ void aos_to_soa_kernel(const double* __restrict__ aos, int n, int npad, double* __restrict__ soa) {
-    const size_t total = (size_t)n * LFDM_S_COUNT;
+__global__ void aos_to_soa_kernel(const double* __restrict__ aos, int n, int ns, int npad, double* __restrict__ soa) {
+    const size_t total = (size_t)n * ns;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        const size_t v = i / LFDM_S_COUNT, f = i % LFDM_S_COUNT;
+        const size_t v = i / ns, f = i % ns;
         soa[f * npad + v] = aos[i];
     }
 }
-__global__ void soa_to_aos_kernel(const double* __restrict__ soa, int n, int npad, double* __restrict__ aos) {
-    const size_t total = (size_t)n * LFDM_S_COUNT;
+__global__ void soa_to_aos_kernel(const double* __restrict__ soa, int n, int ns, int npad, double* __restrict__ aos) {
+    const size_t total = (size_t)n * ns;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        const size_t v = i / LFDM_S_COUNT, f = i % LFDM_S_COUNT;
+        const size_t v = i / ns, f = i % ns;
         aos[i] = soa[f * npad + v];
     }
 }
@@ -149,14 +151,14 @@ static int grid_for(size_t total) {
     size_t g = (total + 255) / 256;
     return (int)(g > 152 * 32 ? 152 * 32 : (g == 0 ? 1 : g));
 }
-cudaError_t launch_states_to_soa(const double* aos, int n, int npad, double* soa, cudaStream_t stream) {
+cudaError_t launch_states_to_soa(const double* aos, int n, int ns, int npad, double* soa, cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
-    aos_to_soa_kernel<<<grid_for((size_t)n * LFDM_S_COUNT), 256, 0, stream>>>(aos, n, npad, soa);
+    aos_to_soa_kernel<<<grid_for((size_t)n * ns), 256, 0, stream>>>(aos, n, ns, npad, soa);
     return cudaGetLastError();
 }
-cudaError_t launch_states_to_aos(const double* soa, int n, int npad, double* aos, cudaStream_t stream) {
+cudaError_t launch_states_to_aos(const double* soa, int n, int ns, int npad, double* aos, cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
-    soa_to_aos_kernel<<<grid_for((size_t)n * LFDM_S_COUNT), 256, 0, stream>>>(soa, n, npad, aos);
+    soa_to_aos_kernel<<<grid_for((size_t)n * ns), 256, 0, stream>>>(soa, n, ns, npad, aos);
     return cudaGetLastError();
 }
 
@@ -268,58 +270,10 @@ void build_class_dev18(const lfdm_class18& c, ClassDev18* out) {
 // ---------------------------------------------------------------------------------------------
 // window kernel
 
-constexpr int kMaxSmemClasses = 8;
 
 size_t window18_smem(int threads, int nclasses) {
     const size_t cls = nclasses <= kMaxSmemClasses ? (size_t)nclasses * sizeof(ClassDev18) : 0;
     return cls + (size_t)K18_COUNT * threads * sizeof(double);
-}
-
-struct DriverCursor {
-    const double* rows;
-    int len;
-    int r;         // first row with time >= t (valid while rows[0].t < t < rows[len-1].t)
-    double tfirst, tlast;
-};
-
-__device__ __forceinline__ void driver_begin(DriverCursor& c, const double* rows, int len, double t) {
-    c.rows = rows;
-    c.len = len;
-    c.tfirst = __ldg(rows);
-    c.tlast = __ldg(rows + 4 * (len - 1));
-    int l = 0, h = len;
-    while (l < h) {
-        int mid = (l + h) >> 1;
-        if (t <= __ldg(rows + 4 * mid)) h = mid;
-        else l = mid + 1;
-    }
-    c.r = l;
-}
-
-// GetDriverInput (utils/utils_gpu.cu:34-56) with a monotone cursor in place of the per-step
-// binary search; the segment found is the same lower_bound segment for non-decreasing tables.
-__device__ __forceinline__ void driver_at(DriverCursor& c, double t, double& st, double& th, double& br) {
-    if (t <= c.tfirst) {
-        st = __ldg(c.rows + 1);
-        th = __ldg(c.rows + 2);
-        br = __ldg(c.rows + 3);
-        return;
-    }
-    if (t >= c.tlast) {
-        const double* L = c.rows + 4 * (c.len - 1);
-        st = __ldg(L + 1);
-        th = __ldg(L + 2);
-        br = __ldg(L + 3);
-        return;
-    }
-    while (__ldg(c.rows + 4 * c.r) < t) ++c.r;
-    while (c.r > 1 && __ldg(c.rows + 4 * (c.r - 1)) >= t) --c.r;  // t moved backwards (new window)
-    const double2* L = reinterpret_cast<const double2*>(c.rows + 4 * (c.r - 1));
-    const double2 L01 = __ldg(L), L23 = __ldg(L + 1), R01 = __ldg(L + 2), R23 = __ldg(L + 3);
-    const double tbar = (t - L01.x) / (R01.x - L01.x);
-    st = L01.y + tbar * (R01.y - L01.y);
-    th = L23.x + tbar * (R23.x - L23.x);
-    br = L23.y + tbar * (R23.y - L23.y);
 }
 
 template <bool kNr, int kCtl, bool kOut>

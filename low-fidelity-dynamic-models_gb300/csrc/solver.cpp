@@ -59,6 +59,8 @@ struct DevBuf {
 
 struct lfdm_solver {
     int model = 18;
+    int ns = LFDM_S_COUNT;            // doubles per flat state vector of this model
+    int nresp = LFDM18_RESP_CHANNELS; // response channels of this model
     unsigned N = 0;
     int device = 0;
     int npad = 0;
@@ -210,11 +212,11 @@ int sync_device(lfdm_solver* h) {
         h->dirty_tables = false;
     }
     if (h->dirty_states) {
-        CK(h->d_S.ensure(LFDM_S_COUNT * np));
-        CK(h->d_aos.ensure(N * LFDM_S_COUNT));
-        CK(cudaMemcpyAsync(h->d_aos.p, h->states.data(), N * LFDM_S_COUNT * sizeof(double), cudaMemcpyHostToDevice,
+        CK(h->d_S.ensure(h->ns * np));
+        CK(h->d_aos.ensure(N * h->ns));
+        CK(cudaMemcpyAsync(h->d_aos.p, h->states.data(), N * h->ns * sizeof(double), cudaMemcpyHostToDevice,
                            h->stream));
-        CK(launch_states_to_soa(h->d_aos.p, (int)N, h->npad, h->d_S.p, h->stream));
+        CK(launch_states_to_soa(h->d_aos.p, (int)N, h->ns, h->npad, h->d_S.p, h->stream));
         h->dirty_states = false;
     }
     CK(h->d_status.ensure(N));
@@ -226,8 +228,8 @@ int pull_states(lfdm_solver* h) {
     if (!h->device_newer) return LFDM_OK;
     int rc = set_device(h);
     if (rc) return rc;
-    CK(launch_states_to_aos(h->d_S.p, (int)h->N, h->npad, h->d_aos.p, h->stream));
-    CK(cudaMemcpyAsync(h->states.data(), h->d_aos.p, (size_t)h->N * LFDM_S_COUNT * sizeof(double),
+    CK(launch_states_to_aos(h->d_S.p, (int)h->N, h->ns, h->npad, h->d_aos.p, h->stream));
+    CK(cudaMemcpyAsync(h->states.data(), h->d_aos.p, (size_t)h->N * h->ns * sizeof(double),
                        cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->device_newer = false;
@@ -264,13 +266,16 @@ int check_ready(lfdm_solver* h, bool need_tables) {
 }
 
 void csv_header(lfdm_solver* h) {
-    static const char* hdr[] = {"time", "x", "y", "vx", "vy", "roll", "yaw", "roll_rate", "yaw_rate",
-                                "wlf", "wrf", "wlr", "wrr"};
+    // 18dof-gpu/dof18_halfImplicit_gpu.cu SolveStep header; 11dof-gpu/dof11_halfImplicit_gpu.cu:561-569
+    static const char* hdr18[] = {"time", "x", "y", "vx", "vy", "roll", "yaw", "roll_rate", "yaw_rate",
+                                  "wlf", "wrf", "wlr", "wrr"};
+    static const char* hdr11[] = {"time", "x", "y", "vx", "vy", "yaw", "yaw_rate", "wf", "wr"};
+    const char* const* hdr = h->model == LFDM_MODEL_11 ? hdr11 : hdr18;
     for (unsigned k = 0; k < h->num_outs; ++k) {
         auto& os = h->csv[k];
-        for (const char* c : hdr) os << c << ",";
+        for (int c = 0; c < h->nresp; ++c) os << hdr[c] << ",";
         os << std::endl;
-        for (int c = 0; c < LFDM18_RESP_CHANNELS; ++c) os << 0 << ",";
+        for (int c = 0; c < h->nresp; ++c) os << 0 << ",";
         os << std::endl;
     }
 }
@@ -281,8 +286,8 @@ void csv_append(lfdm_solver* h, const double* resp, int samples) {
         const unsigned idx = h->store_all ? k : h->which_outs[k];
         auto& os = h->csv[k];
         for (int s = 0; s < samples; ++s) {
-            const double* r = resp + (size_t)s * LFDM18_RESP_CHANNELS * N;
-            for (int c = 0; c < LFDM18_RESP_CHANNELS; ++c) os << r[(size_t)c * N + idx] << ",";
+            const double* r = resp + (size_t)s * h->nresp * N;
+            for (int c = 0; c < h->nresp; ++c) os << r[(size_t)c * N + idx] << ",";
             os << std::endl;
         }
     }
@@ -314,7 +319,7 @@ int run_windows(lfdm_solver* h, double t0, double t_end, bool solve_all, int ctl
     const bool stream_resp = h->resp_host != nullptr && solve_all && !csv && !dev_resp;
     const double dtout = csv ? h->dtout : (stream_resp ? h->resp_dtout : (dev_resp ? h->resp_dev_dtout : 0.0));
     const int spw = dtout > 0 ? (int)std::ceil(h->ksim / dtout) : 0;
-    const size_t slot = (size_t)spw * LFDM18_RESP_CHANNELS * N;  // doubles per window buffer
+    const size_t slot = (size_t)spw * h->nresp * N;  // doubles per window buffer
     const int nbuf = stream_resp ? 2 : 1;
     if (dtout > 0 && !dev_resp) CK(h->d_resp.ensure(slot * nbuf));
     size_t dev_windows = 0;
@@ -363,7 +368,7 @@ int run_windows(lfdm_solver* h, double t0, double t_end, bool solve_all, int ctl
     size_t widx = 0;
     float total_ms = 0;
     if (!solve_all || t0 <= 0) h->resp_written = 0;
-    const size_t resp_cap_samples = stream_resp ? h->resp_cap / (LFDM18_RESP_CHANNELS * N) : 0;
+    const size_t resp_cap_samples = stream_resp ? h->resp_cap / (h->nresp * N) : 0;
     if (stream_resp && resp_cap_samples == 0)
         return h->fail(LFDM_ERR_CAPACITY, "response buffer holds less than one sample");
     for (;;) {
@@ -392,7 +397,7 @@ int run_windows(lfdm_solver* h, double t0, double t_end, bool solve_all, int ctl
         w.nsamples = dtout > 0 ? (int)samp.size() : 0;
         w.sample_steps = dtout > 0 ? h->d_samples.p + (size_t)b * (spw + 1) : nullptr;
         CK(cudaEventRecord(h->ev0, h->stream));
-        CK(launch_window18(w, h->stream));
+        CK(h->model == LFDM_MODEL_11 ? launch_window11(w, h->stream) : launch_window18(w, h->stream));
         CK(cudaEventRecord(h->ev1, h->stream));
         ++launches;
         if (stream_resp) {
@@ -400,7 +405,7 @@ int run_windows(lfdm_solver* h, double t0, double t_end, bool solve_all, int ctl
             CK(cudaStreamWaitEvent(h->copy_stream, h->win_done[b], 0));
             // window samples k land at global sample widx*spw + k (ring over the caller's buffer);
             // one copy per contiguous run of ring slots
-            const size_t per = LFDM18_RESP_CHANNELS * N;
+            const size_t per = h->nresp * N;
             for (int k = 0; k < w.nsamples;) {
                 const size_t gs = widx * (size_t)spw + k;
                 const size_t slot0 = gs % resp_cap_samples;
@@ -453,6 +458,8 @@ int append_vehicles(lfdm_solver* h, const lfdm_class18& cls, const double* param
                        h->constructed, n, h->N);
     if (tire_type != LFDM_TIRE_TMEASY && tire_type != LFDM_TIRE_TMEASY_NR)
         return h->fail(LFDM_ERR_ARG, "unknown tire type %d", tire_type);
+    if (h->model == LFDM_MODEL_11 && tire_type != LFDM_TIRE_TMEASY)
+        return h->fail(LFDM_ERR_ARG, "the 11-DOF model has only the TMeasy tire");
     if (h->tire_type >= 0 && h->tire_type != tire_type)
         return h->fail(LFDM_ERR_STATE, "all vehicles of a solver use one tire type");
     if (cls.noGears < 1 || cls.noGears > LFDM_MAX_GEARS) return h->fail(LFDM_ERR_ARG, "bad gear count %d", cls.noGears);
@@ -512,7 +519,7 @@ int lfdm_measure_fp64_peak(int device, double* dfma_per_s) {
 int lfdm_create_on_device(int model, unsigned total_num_vehicles, int device, lfdm_solver** out) {
     if (!out) return LFDM_ERR_ARG;
     *out = nullptr;
-    if (model != LFDM_MODEL_18) {
+    if (model != LFDM_MODEL_18 && model != LFDM_MODEL_11) {
         g_create_error = "model " + std::to_string(model) + " is not available in this build";
         return LFDM_ERR_ARG;
     }
@@ -532,6 +539,10 @@ int lfdm_create_on_device(int model, unsigned total_num_vehicles, int device, lf
     }
     std::unique_ptr<lfdm_solver> h(new lfdm_solver());
     h->model = model;
+    if (model == LFDM_MODEL_11) {
+        h->ns = LFDM11_S_COUNT;
+        h->nresp = LFDM11_RESP_CHANNELS;
+    }
     h->N = total_num_vehicles;
     h->device = device;
     h->npad = (int)((total_num_vehicles + 127) / 128 * 128);
@@ -550,7 +561,7 @@ int lfdm_create_on_device(int model, unsigned total_num_vehicles, int device, lf
     h->params.assign((size_t)h->N * LFDM_P_COUNT, 0.0);
     h->row_off.assign(h->N, 0);
     h->row_len.assign(h->N, 0);
-    h->states.assign((size_t)h->N * LFDM_S_COUNT, 0.0);
+    h->states.assign((size_t)h->N * h->ns, 0.0);
     *out = h.release();
     return LFDM_OK;
 }
@@ -581,7 +592,7 @@ int lfdm_construct(lfdm_solver* h, const char* veh_json, const char* tire_json, 
     lfdm_class18 cls;
     std::vector<double> p(LFDM_P_COUNT);
     std::string err;
-    if (!load_vehicle18(veh_json, tire_json, tire_type, cls, p.data(), err))
+    if (!load_vehicle(h->model, veh_json, tire_json, tire_type, cls, p.data(), err))
         return h->fail(err.rfind("cannot open", 0) == 0 ? LFDM_ERR_IO : LFDM_ERR_PARSE, "%s", err.c_str());
     std::vector<double> table;
     if (driver_file) {
@@ -694,7 +705,7 @@ int lfdm_initialize(lfdm_solver* h, const double* state, unsigned num_vehicles) 
     int rc = pull_states(h);
     if (rc) return rc;
     for (unsigned k = 0; k < num_vehicles; ++k)
-        std::memcpy(&h->states[(size_t)(h->initialized + k) * LFDM_S_COUNT], state, LFDM_S_COUNT * sizeof(double));
+        std::memcpy(&h->states[(size_t)(h->initialized + k) * h->ns], state, h->ns * sizeof(double));
     h->initialized += num_vehicles;
     h->dirty_states = true;
     return LFDM_OK;
@@ -707,7 +718,7 @@ int lfdm_set_states(lfdm_solver* h, unsigned first, unsigned count, const double
         int rc = pull_states(h);
         if (rc) return rc;
     }
-    std::memcpy(&h->states[(size_t)first * LFDM_S_COUNT], states, (size_t)count * LFDM_S_COUNT * sizeof(double));
+    std::memcpy(&h->states[(size_t)first * h->ns], states, (size_t)count * h->ns * sizeof(double));
     h->initialized = std::max(h->initialized, first + count);
     h->device_newer = false;
     h->dirty_states = true;
@@ -719,7 +730,7 @@ int lfdm_get_states(lfdm_solver* h, unsigned first, unsigned count, double* stat
     if ((size_t)first + count > h->N) return h->fail(LFDM_ERR_ARG, "index out of range");
     int rc = pull_states(h);
     if (rc) return rc;
-    std::memcpy(states, &h->states[(size_t)first * LFDM_S_COUNT], (size_t)count * LFDM_S_COUNT * sizeof(double));
+    std::memcpy(states, &h->states[(size_t)first * h->ns], (size_t)count * h->ns * sizeof(double));
     return LFDM_OK;
 }
 
@@ -730,10 +741,10 @@ int lfdm_get_sim_state(lfdm_solver* h, unsigned i, double* state) {
         int rc = set_device(h);
         if (rc) return rc;
         CK(cudaMemcpy2D(state, sizeof(double), h->d_S.p + i, (size_t)h->npad * sizeof(double), sizeof(double),
-                        LFDM_S_COUNT, cudaMemcpyDeviceToHost));
+                        h->ns, cudaMemcpyDeviceToHost));
         return LFDM_OK;
     }
-    std::memcpy(state, &h->states[(size_t)i * LFDM_S_COUNT], LFDM_S_COUNT * sizeof(double));
+    std::memcpy(state, &h->states[(size_t)i * h->ns], h->ns * sizeof(double));
     return LFDM_OK;
 }
 
@@ -786,6 +797,8 @@ int lfdm_set_precision(lfdm_solver* h, int precision) {
     if (!h) return LFDM_ERR_ARG;
     if (precision != LFDM_PREC_FP64 && precision != LFDM_PREC_MIXED)
         return h->fail(LFDM_ERR_ARG, "unknown precision %d", precision);
+    if (precision == LFDM_PREC_MIXED && h->model != LFDM_MODEL_18)
+        return h->fail(LFDM_ERR_ARG, "mixed precision is built for the 18-DOF model only");
     h->precision = precision;
     return LFDM_OK;
 }
@@ -977,7 +990,7 @@ int lfdm_parse_vehicle18(const char* veh_json, const char* tire_json, int tire_t
                          double* params, char* err, size_t err_len) {
     if (!veh_json || !tire_json || !cls || !params) return LFDM_ERR_ARG;
     std::string e;
-    if (!load_vehicle18(veh_json, tire_json, tire_type, *cls, params, e)) {
+    if (!load_vehicle(LFDM_MODEL_18, veh_json, tire_json, tire_type, *cls, params, e)) {
         if (err && err_len) std::snprintf(err, err_len, "%s", e.c_str());
         return e.rfind("cannot open", 0) == 0 ? LFDM_ERR_IO : LFDM_ERR_PARSE;
     }

@@ -75,6 +75,33 @@ def state_floors():
 RESP_FLOORS = np.array([1.0, 1, 1, 1, 1, 1, 1, 1, 1, 10, 10, 10, 10], dtype=np.float64)
 
 
+def state_floors11():
+    """Floors of the 11-DOF state vector (LFDM11_S_* layout), same scales as state_floors()."""
+    abi = pkg_mod("_abi")
+    fl = np.full(abi.S11_COUNT, np.inf)
+    S, T = abi.S11, abi.T
+    for k in ("x", "y", "u", "v", "psi", "wz", "udot", "vdot", "current_gr"):
+        fl[S[k]] = 1.0
+    fl[S["crankomega"]] = 10.0
+    for t in range(2):
+        b = abi.S11_TIRE0 + t * abi.S_TIRE_STRIDE
+        fl[b + T["omega"]] = 10.0
+        fl[b + T["xe"]] = 1e-3
+        fl[b + T["ye"]] = 1e-3
+    return fl
+
+
+# time, x, y, u, v, psi, wz, front and rear wheel speed
+RESP11_FLOORS = np.array([1.0, 1, 1, 1, 1, 1, 1, 10, 10], dtype=np.float64)
+
+
+def case_inputs11(case):
+    """(Class18, params[P], state[S11], table[rows][4]) of an 11-DOF golden case."""
+    params = pkg_mod("params")
+    cls, p = params.vehicle_from_json(case["vehicle"], case["tire"], case["tire_type"], model=11)
+    return cls, p, np.array(case["state"], dtype=np.float64), np.array(case["driver"], dtype=np.float64)
+
+
 def rel_err(a, b, floors):
     """Elementwise |a-b| / max(|b|, floor); inf floors mark fields that are not compared."""
     a = np.asarray(a, dtype=np.float64)

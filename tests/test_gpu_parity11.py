@@ -1,0 +1,188 @@
+"""11-DOF CUDA path (through the C ABI) against the reference's own 11-DOF CPU solver outputs
+(tests/golden/golden11.json) and the oracle.
+
+Same criteria as the 18-DOF parity tests: per state |gpu - ref| <= 1e-9 * max(|ref|, s_k) with
+the floors of conftest.state_floors11(); trajectories that are rounding-chaotic are held to
+max(1e-9, 100 x the reference algorithm's own deviation under FMA contraction), and a single
+window from many diverse states to 1e-12.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from conftest import RESP11_FLOORS, case_inputs11, pkg_mod, rel_err, state_floors11
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-9
+CHAOS_FACTOR = 100.0
+NT = os.cpu_count() or 1
+
+
+@pytest.fixture(scope="module")
+def golden11():
+    import json
+
+    from conftest import TESTS
+    with open(os.path.join(TESTS, "golden", "golden11.json")) as f:
+        return json.load(f)
+
+
+def _groups(cases):
+    g = {}
+    for c in cases:
+        if c["ksim"] > 0:
+            g.setdefault((c["ksim"], c["tend"], c["sample"]), []).append(c)
+    return g
+
+
+def _run_group(lfdm, cases, ksim, tend, freq):
+    n = len(cases)
+    sol = lfdm.d11SolverHalfImplicitGPU(n)
+    states = []
+    for i, c in enumerate(cases):
+        cls, p, s, tab = case_inputs11(c)
+        sol.construct_class(cls, p[None, :])
+        sol.set_driver_tables(tab[None, :, :], first=i)
+        states.append(s)
+    sol.set_states(np.array(states))
+    sol.SetTimeStep(cases[0]["dt"])
+    sol.SetKernelSimTime(ksim)
+    sol.SetEndTime(tend)
+    nsamp = int(round(tend * freq)) + 4
+    resp = np.full((nsamp, lfdm.RESP11, n), np.nan)
+    sol.set_response_buffer(resp, freq)
+    sol.Solve()
+    final = sol.get_states()
+    sol.close()
+    return final, resp
+
+
+def _fma_reference(case, dtout):
+    cls, p, s, tab = case_inputs11(case)
+    st, resp = O.run18([cls], [0], p[None], s[None], [tab], dt=case["dt"], tend=case["tend"], ksim=case["ksim"],
+                       schedule=1, dtout=dtout, fma=True, model=11)
+    return st[0], resp[:, :, 0]
+
+
+def test_golden11_trajectories_within_reference_sensitivity(built_lib, golden11):
+    """HMMWV (reference data files and driver tables) and seeded SUV cases: final state and every
+    sample within max(1e-9, 100 x the reference's FMA-build deviation)."""
+    fl = state_floors11()
+    for (ksim, tend, sample), cases in _groups(golden11["cases"]).items():
+        freq = 1.0 / (sample * cases[0]["dt"])
+        final, resp = _run_group(built_lib, cases, ksim, tend, freq)
+        for i, c in enumerate(cases):
+            fst, fresp = _fma_reference(c, sample * c["dt"])
+            exp_f = np.array(c["expected_final"])
+            e_gpu = rel_err(final[i], exp_f, fl).max()
+            e_fma = rel_err(fst, exp_f, fl).max()
+            assert e_gpu <= max(RTOL, CHAOS_FACTOR * e_fma), (c["name"], float(e_gpu), float(e_fma))
+            exp = np.array(c["expected_samples"])
+            e_gpu = rel_err(resp[: len(exp), :, i], exp[:, 1:], RESP11_FLOORS).max(axis=1)
+            e_fma = rel_err(fresp[: len(exp)], exp[:, 1:], RESP11_FLOORS).max(axis=1)
+            bound = np.maximum(RTOL, CHAOS_FACTOR * e_fma)
+            assert (e_gpu <= bound).all(), (c["name"], int(np.argmax(e_gpu > bound)), float(e_gpu.max()))
+
+
+def test_reference_11dof_gpu_test_pins(built_lib, golden11):
+    """tests/11dof_gpu.cu:76-77: x after 22 s of the HMMWV acceleration and double-lane-change
+    inputs is 198.72 and 104.805 m (the reference allows +-1 m)."""
+    by = {c["name"]: c for c in golden11["cases"]}
+    cases = [by["hmmwv11_acc3_gpu22"], by["hmmwv11_dl4_gpu"]]
+    final, _ = _run_group(built_lib, cases, 2.0, 22.0, 10.0)
+    X = pkg_mod("_abi").S11["x"]
+    assert abs(final[0, X] - 198.72) < 1
+    assert abs(final[1, X] - 104.805) < 1
+
+
+def _fleet(built_lib, n, horizon, ksim, seed):
+    fleet = pkg_mod("fleet")
+    f = fleet.fleet11(n, seed=seed, horizon=horizon)
+    sol = built_lib.d11SolverHalfImplicitGPU(n)
+    sol.construct_class(f["cls"][0], f["params"])
+    sol.set_driver_tables(f["tables"])
+    sol.set_states(f["states"])
+    sol.SetKernelSimTime(ksim)
+    sol.SetEndTime(horizon)
+    sol.Solve()
+    got = sol.get_states()
+    sol.close()
+    args = (f["cls"], f["class_of"], f["params"], f["states"], f["tables"])
+    ref, _ = O.run18(*args, tend=horizon, ksim=ksim, schedule=1, nthreads=NT, model=11)
+    fma, _ = O.run18(*args, tend=horizon, ksim=ksim, schedule=1, nthreads=NT, fma=True, model=11)
+    return got, ref, fma
+
+
+@pytest.mark.parametrize("n,horizon,ksim", [(512, 10.0, 1.0), (1, 1.0, 0.3), (33, 2.0, 0.7), (129, 1.5, 1.5)])
+def test_seeded_fleet11_within_reference_sensitivity(built_lib, n, horizon, ksim):
+    got, ref, fma = _fleet(built_lib, n, horizon, ksim, seed=20261203 + n)
+    fl = state_floors11()
+    e_gpu = rel_err(got, ref, fl).max(axis=1)
+    e_fma = rel_err(fma, ref, fl).max(axis=1)
+    print(f"fleet11 n={n}: gpu>1e-9 {int((e_gpu > RTOL).sum())} (reference FMA build {int((e_fma > RTOL).sum())}); "
+          f"median gpu {np.median(e_gpu):.2e} fma {np.median(e_fma):.2e}")
+    assert (e_gpu <= np.maximum(RTOL, CHAOS_FACTOR * e_fma)).all(), float(e_gpu.max())
+
+
+def test_one_window11_parity_from_diverse_states(built_lib):
+    """10 steps from states spread along the fleet's trajectories: rounding-level agreement."""
+    fleet = pkg_mod("fleet")
+    n = 512
+    f = fleet.fleet11(n, seed=7, horizon=10.0)
+    outs, ctls = [], []
+    st = f["states"]
+    for k in range(9):
+        st, _ = O.run18(f["cls"], f["class_of"], f["params"], st, f["tables"], t0=float(k), ksim=1.0, schedule=2,
+                        nthreads=NT, model=11)
+        outs.append(st.copy())
+        ctls.append(np.stack([O.driver_input(k + 1.0, f["tables"][i])[1:] for i in range(n)]))
+    S = np.concatenate(outs)
+    P = np.concatenate([f["params"]] * 9)
+    ctl = np.concatenate(ctls)
+    m = P.shape[0]
+    sol = built_lib.d11SolverHalfImplicitGPU(m)
+    sol.construct_class(f["cls"][0], P)
+    sol.set_states(S)
+    sol.SetKernelSimTime(0.01)
+    sol.SolveStep(0.0, ctl[:, 0], ctl[:, 1], ctl[:, 2])
+    got = sol.get_states()
+    sol.close()
+    ref, _ = O.run18(f["cls"], np.zeros(m, np.int32), P, S, ctl=ctl, t0=0.0, ksim=0.01, schedule=2, nthreads=NT,
+                     model=11)
+    e = rel_err(got, ref, state_floors11()).max(axis=1)
+    assert e.max() <= 1e-12, (float(e.max()), int(e.argmax()))
+
+
+def test_solvestep_scalar11(built_lib):
+    """SolveStep with scalar controls (11dof-gpu/dof11_halfImplicit_gpu.cu SolveStep) vs the oracle."""
+    fleet = pkg_mod("fleet")
+    n = 64
+    f = fleet.fleet11(n, seed=3, horizon=2.0)
+    sol = built_lib.d11SolverHalfImplicitGPU(n)
+    sol.construct_class(f["cls"][0], f["params"])
+    sol.set_states(f["states"])
+    sol.SetKernelSimTime(0.05)
+    t = 0.0
+    st = f["states"]
+    for k in range(4):
+        t_new = sol.SolveStep(t, 0.1, 0.5, 0.0)
+        ctl = np.tile([0.1, 0.5, 0.0], (n, 1))
+        st, _ = O.run18(f["cls"], f["class_of"], f["params"], st, ctl=ctl, t0=t, ksim=0.05, schedule=2, nthreads=NT,
+                        model=11)
+        t = t_new
+    got = sol.get_states()
+    sol.close()
+    e = rel_err(got, st, state_floors11()).max(axis=1)
+    assert e.max() <= 1e-11, float(e.max())
+
+
+def test_model11_rejects_mixed_and_nr(built_lib):
+    sol = built_lib.d11SolverHalfImplicitGPU(4)
+    with pytest.raises(built_lib.LfdmError):
+        sol.set_precision(pkg_mod("_abi").PREC_MIXED)
+    cls, p = pkg_mod("fleet").suv11()
+    with pytest.raises(built_lib.LfdmError):
+        sol.construct_class(cls, p[None, :], built_lib.TireType.TMeasyNr)
+    sol.close()
