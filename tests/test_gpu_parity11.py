@@ -2,9 +2,13 @@
 (tests/golden/golden11.json) and the oracle.
 
 Same criteria as the 18-DOF parity tests: per state |gpu - ref| <= 1e-9 * max(|ref|, s_k) with
-the floors of conftest.state_floors11(); trajectories that are rounding-chaotic are held to
-max(1e-9, 100 x the reference algorithm's own deviation under FMA contraction), and a single
-window from many diverse states to 1e-12.
+the floors of conftest.state_floors11(); a single window from many diverse states to 1e-12.
+Trajectories that are rounding-chaotic (wheel chatter of the light SUV wheels) are held to
+max(1e-9, 100 x the reference algorithm's sensitivity envelope): the largest deviation, sample by
+sample, among the reference algorithm built with FMA contraction and the reference algorithm
+started from the initial state with u scaled by 1 +- 1e-15. An envelope of several perturbations
+is needed because the host's libm and contraction differ between machines, so a single perturbed
+run can by chance stay close where the others (and the GPU) do not.
 """
 import os
 
@@ -59,30 +63,44 @@ def _run_group(lfdm, cases, ksim, tend, freq):
     return final, resp
 
 
-def _fma_reference(case, dtout):
+def _perturbed_runs(cls, class_of, params, states, tables, **kw):
+    """The reference algorithm under the three perturbations of the sensitivity envelope."""
+    U = pkg_mod("_abi").S11["u"]
+    out = [O.run18(cls, class_of, params, states, tables, fma=True, model=11, **kw)]
+    for eps in (1e-15, -1e-15):
+        s2 = np.array(states, dtype=np.float64, copy=True)
+        s2[:, U] *= 1.0 + eps
+        out.append(O.run18(cls, class_of, params, s2, tables, model=11, **kw))
+    return out
+
+
+def _envelope(case, dtout):
+    """(final-state envelope, per-sample response envelope) of a golden case, vs its expected values."""
     cls, p, s, tab = case_inputs11(case)
-    st, resp = O.run18([cls], [0], p[None], s[None], [tab], dt=case["dt"], tend=case["tend"], ksim=case["ksim"],
-                       schedule=1, dtout=dtout, fma=True, model=11)
-    return st[0], resp[:, :, 0]
+    runs = _perturbed_runs([cls], [0], p[None], s[None], [tab], dt=case["dt"], tend=case["tend"], ksim=case["ksim"],
+                           schedule=1, dtout=dtout)
+    exp_f = np.array(case["expected_final"])
+    exp = np.array(case["expected_samples"])
+    ef = max(rel_err(st[0], exp_f, state_floors11()).max() for st, _ in runs)
+    er = np.max([rel_err(r[: len(exp), :, 0], exp[:, 1:], RESP11_FLOORS).max(axis=1) for _, r in runs], axis=0)
+    return ef, er
 
 
 def test_golden11_trajectories_within_reference_sensitivity(built_lib, golden11):
     """HMMWV (reference data files and driver tables) and seeded SUV cases: final state and every
-    sample within max(1e-9, 100 x the reference's FMA-build deviation)."""
+    sample within max(1e-9, 100 x the reference algorithm's sensitivity envelope)."""
     fl = state_floors11()
     for (ksim, tend, sample), cases in _groups(golden11["cases"]).items():
         freq = 1.0 / (sample * cases[0]["dt"])
         final, resp = _run_group(built_lib, cases, ksim, tend, freq)
         for i, c in enumerate(cases):
-            fst, fresp = _fma_reference(c, sample * c["dt"])
+            env_f, env_r = _envelope(c, sample * c["dt"])
             exp_f = np.array(c["expected_final"])
             e_gpu = rel_err(final[i], exp_f, fl).max()
-            e_fma = rel_err(fst, exp_f, fl).max()
-            assert e_gpu <= max(RTOL, CHAOS_FACTOR * e_fma), (c["name"], float(e_gpu), float(e_fma))
+            assert e_gpu <= max(RTOL, CHAOS_FACTOR * env_f), (c["name"], float(e_gpu), float(env_f))
             exp = np.array(c["expected_samples"])
             e_gpu = rel_err(resp[: len(exp), :, i], exp[:, 1:], RESP11_FLOORS).max(axis=1)
-            e_fma = rel_err(fresp[: len(exp)], exp[:, 1:], RESP11_FLOORS).max(axis=1)
-            bound = np.maximum(RTOL, CHAOS_FACTOR * e_fma)
+            bound = np.maximum(RTOL, CHAOS_FACTOR * env_r)
             assert (e_gpu <= bound).all(), (c["name"], int(np.argmax(e_gpu > bound)), float(e_gpu.max()))
 
 
@@ -110,20 +128,24 @@ def _fleet(built_lib, n, horizon, ksim, seed):
     got = sol.get_states()
     sol.close()
     args = (f["cls"], f["class_of"], f["params"], f["states"], f["tables"])
-    ref, _ = O.run18(*args, tend=horizon, ksim=ksim, schedule=1, nthreads=NT, model=11)
-    fma, _ = O.run18(*args, tend=horizon, ksim=ksim, schedule=1, nthreads=NT, fma=True, model=11)
-    return got, ref, fma
+    kw = dict(tend=horizon, ksim=ksim, schedule=1, nthreads=NT)
+    ref, _ = O.run18(*args, model=11, **kw)
+    fl = state_floors11()
+    env = np.max([rel_err(st, ref, fl).max(axis=1) for st, _ in _perturbed_runs(*args, **kw)], axis=0)
+    return got, ref, env
 
 
 @pytest.mark.parametrize("n,horizon,ksim", [(512, 10.0, 1.0), (1, 1.0, 0.3), (33, 2.0, 0.7), (129, 1.5, 1.5)])
 def test_seeded_fleet11_within_reference_sensitivity(built_lib, n, horizon, ksim):
-    got, ref, fma = _fleet(built_lib, n, horizon, ksim, seed=20261203 + n)
-    fl = state_floors11()
-    e_gpu = rel_err(got, ref, fl).max(axis=1)
-    e_fma = rel_err(fma, ref, fl).max(axis=1)
-    print(f"fleet11 n={n}: gpu>1e-9 {int((e_gpu > RTOL).sum())} (reference FMA build {int((e_fma > RTOL).sum())}); "
-          f"median gpu {np.median(e_gpu):.2e} fma {np.median(e_fma):.2e}")
-    assert (e_gpu <= np.maximum(RTOL, CHAOS_FACTOR * e_fma)).all(), float(e_gpu.max())
+    """Vehicles the perturbations leave quiet (envelope <= 1e-13) agree within 1e-9; no more vehicles
+    exceed 1e-9 than under the perturbations (+5%); each stays within 100 x its envelope or 1e-9."""
+    got, ref, env = _fleet(built_lib, n, horizon, ksim, seed=20261203 + n)
+    e_gpu = rel_err(got, ref, state_floors11()).max(axis=1)
+    print(f"fleet11 n={n}: gpu>1e-9 {int((e_gpu > RTOL).sum())} (perturbed reference {int((env > RTOL).sum())}); "
+          f"median gpu {np.median(e_gpu):.2e} envelope {np.median(env):.2e}")
+    assert (e_gpu[env <= 1e-13] <= RTOL).all()
+    assert (e_gpu > RTOL).sum() <= (env > RTOL).sum() + 0.05 * n
+    assert (e_gpu <= np.maximum(RTOL, CHAOS_FACTOR * env)).all(), float(e_gpu.max())
 
 
 def test_one_window11_parity_from_diverse_states(built_lib):
