@@ -244,6 +244,20 @@ int lfdm_solve_step_schedule(lfdm_solver* h, double t, const double* ctl, unsign
 /* Step count and step start times of the window starting at t (times: [capacity] or NULL). */
 int lfdm_window_steps(lfdm_solver* h, double t, unsigned* nsteps, double* times, unsigned capacity);
 
+/* No counterpart in the reference (its solver owns and allocates all of its memory). One 18-DOF   */
+/* FP64 window of nsteps steps of dt from t0 over n <= LFDM_NOALLOC_MAX_VEHICLES device-resident    */
+/* vehicles of one class, with per-vehicle constant controls, that allocates nothing: its scratch  */
+/* (derived constants, SoA state and controls, class table; about 20 MB) is one fixed static device */
+/* array. params [n][LFDM_P_COUNT], states [n][LFDM_S_COUNT] (in/out) and steering/throttle/braking */
+/* [n] are DEVICE pointers; the work is enqueued on `stream` (a cudaStream_t, NULL = legacy default */
+/* stream) and the call returns without synchronising. Larger n fails with LFDM_ERR_CAPACITY.       */
+/* Every call on a device shares that scratch, so calls that overlap on the GPU race: serialise     */
+/* them. err (err_len bytes, may be NULL) receives a message on failure.                            */
+#define LFDM_NOALLOC_MAX_VEHICLES 16384
+int lfdm_step18_noalloc(const lfdm_class18* cls, int tire_type, const double* params, double* states,
+                        const double* steering, const double* throttle, const double* braking, unsigned n, double t0,
+                        double dt, unsigned nsteps, void* stream, char* err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -89,6 +89,7 @@ def _sig(lib):
         "lfdm_measure_fp64_peak": ([i, _c_dp], i),
         "lfdm_parse_vehicle18": ([cp, cp, i, vp, dp, ctypes.c_char_p, sz], i),
         "lfdm_load_driver_file": ([cp, dp, u, ctypes.POINTER(u), ctypes.c_char_p, sz], i),
+        "lfdm_step18_noalloc": ([vp, i, vp, vp, vp, vp, vp, u, d, d, u, vp, ctypes.c_char_p, sz], i),
     }
     for name, (args, res) in table.items():
         f = getattr(lib, name)
@@ -365,6 +366,24 @@ def measure_fp64_peak(device: int = 0) -> float:
     if rc:
         raise LfdmError(rc, "FP64 peak probe failed")
     return v.value
+
+
+NOALLOC_MAX_VEHICLES = _abi.C["LFDM_NOALLOC_MAX_VEHICLES"]
+
+
+def step18_noalloc(cls: Class18, params: int, states: int, steering: int, throttle: int, braking: int, n: int,
+                   t0: float, dt: float, nsteps: int, stream: int = 0, tire_type: int = TireType.TMeasy) -> None:
+    """lfdm_step18_noalloc: one FP64 18-DOF window over device-resident vehicles (device pointers,
+    e.g. torch CUDA tensors' data_ptr(): params [n][P_COUNT], states [n][S_COUNT] in/out, controls
+    [n] each), enqueued on `stream` without allocating; n <= NOALLOC_MAX_VEHICLES. Calls share one
+    static scratch array per device, so calls that overlap on the GPU race."""
+    err = ctypes.create_string_buffer(512)
+    rc = lib().lfdm_step18_noalloc(ctypes.byref(cls), int(tire_type), ctypes.c_void_p(params), ctypes.c_void_p(states),
+                                   ctypes.c_void_p(steering), ctypes.c_void_p(throttle), ctypes.c_void_p(braking),
+                                   int(n), float(t0), float(dt), int(nsteps), ctypes.c_void_p(stream) if stream else None,
+                                   err, 512)
+    if rc:
+        raise LfdmError(rc, err.value.decode())
 
 
 def register_host(a: np.ndarray) -> None:
