@@ -66,7 +66,10 @@ enum {
     /* TMeasyNr-only fields */
     LFDM_P_WIDTH, LFDM_P_RIM_RADIUS, LFDM_P_VCOULOMB, LFDM_P_FRBLEND_BEGIN, LFDM_P_FRBLEND_END,
     LFDM_P_BEARINGCAPACITY, LFDM_P_LI, LFDM_P_P_LI, LFDM_P_P_USE,
-    LFDM_P_COUNT /* = 64 */
+    /* 24-DOF only: pitch inertia (24dof-gpu/dof24_gpu.cuh VehicleParam::_jy) and the suspension  */
+    /* spring stiffness and damping (SuspensionParam::_ks, _bs)                                   */
+    LFDM_P_JY, LFDM_P_KS, LFDM_P_BS,
+    LFDM_P_COUNT /* = 67 */
 };
 
 /* Per-class data shared by all vehicles built from one vehicle JSON: flags, gears and maps.     */
@@ -110,6 +113,36 @@ enum {
     LFDM11_S_TIRE0 = 12, /* front tire block; rear tire at LFDM11_S_TIRE0 + LFDM_S_TIRE_STRIDE */
     LFDM11_S_COUNT = 42
 };
+/* Flat per-vehicle state vector, 24-DOF: VehicleState (24dof-gpu/dof24_gpu.cuh), then 4 x        */
+/* TMeasyState (23 fields) and 4 x SuspensionState (24 fields), LF, RF, LR, RR, in the field order */
+/* of the reference structs. current_gr is stored as a double holding an integer.                  */
+enum {
+    LFDM24_S_X = 0, LFDM24_S_Y, LFDM24_S_Z, LFDM24_S_U, LFDM24_S_V, LFDM24_S_W, LFDM24_S_PSI, LFDM24_S_WZ,
+    LFDM24_S_PHI, LFDM24_S_WX, LFDM24_S_THETA, LFDM24_S_WY, LFDM24_S_UDOT, LFDM24_S_VDOT, LFDM24_S_WDOT,
+    LFDM24_S_WXDOT, LFDM24_S_WYDOT, LFDM24_S_WZDOT, LFDM24_S_DTHETA, LFDM24_S_DPHI, LFDM24_S_DPSI,
+    LFDM24_S_CRANKOMEGA, LFDM24_S_DOMEGA_CRANK, LFDM24_S_CURRENT_GR,
+    LFDM24_S_TIRE0 = 24, /* tire k at LFDM24_S_TIRE0 + k * LFDM24_T_COUNT */
+    LFDM24_S_SUS0 = 116, /* suspension k at LFDM24_S_SUS0 + k * LFDM24_SUS_COUNT */
+    LFDM24_S_COUNT = 212
+};
+enum { /* TMeasyState of the 24-DOF model (24dof-gpu/dof24_gpu.cuh) */
+    LFDM24_T_XE = 0, LFDM24_T_YE, LFDM24_T_XEDOT, LFDM24_T_YEDOT, LFDM24_T_OMEGA, LFDM24_T_DOMEGA, LFDM24_T_XT,
+    LFDM24_T_DXT, LFDM24_T_RSTAT, LFDM24_T_FX, LFDM24_T_FY, LFDM24_T_FZ, LFDM24_T_FXG, LFDM24_T_FYG,
+    LFDM24_T_FZG, LFDM24_T_VGX, LFDM24_T_VGY, LFDM24_T_VGZ, LFDM24_T_VSX, LFDM24_T_VSY, LFDM24_T_VSZ,
+    LFDM24_T_MY, LFDM24_T_ENGTOR,
+    LFDM24_T_COUNT = 23
+};
+enum { /* SuspensionState (24dof-gpu/dof24_gpu.cuh) */
+    LFDM24_SUS_XS = 0, LFDM24_SUS_XSI, LFDM24_SUS_DXS, LFDM24_SUS_LS, LFDM24_SUS_LSI, LFDM24_SUS_US,
+    LFDM24_SUS_VS, LFDM24_SUS_WS, LFDM24_SUS_DUS, LFDM24_SUS_DVS, LFDM24_SUS_DWS, LFDM24_SUS_UU, LFDM24_SUS_VU,
+    LFDM24_SUS_WU, LFDM24_SUS_DUU, LFDM24_SUS_DVU, LFDM24_SUS_DWU, LFDM24_SUS_FXS, LFDM24_SUS_FYS,
+    LFDM24_SUS_FZS, LFDM24_SUS_FZD, LFDM24_SUS_MX, LFDM24_SUS_MY, LFDM24_SUS_MZ,
+    LFDM24_SUS_COUNT = 24
+};
+/* 24-DOF response channels (24dof-gpu/dof24_halfImplicit_gpu.cu:1086-1106): time, x, y, u, v,      */
+/* phi (roll), psi (yaw), theta (pitch), wx, wz, wy, wheel speeds LF, RF, LR, RR.                    */
+#define LFDM24_RESP_CHANNELS 15
+
 /* 11-DOF response channels (11dof-gpu/dof11_halfImplicit_gpu.cu:893-904): time, x, y, u, v, psi, wz, */
 /* front wheel speed, rear wheel speed.                                                              */
 #define LFDM11_RESP_CHANNELS 9
@@ -233,6 +266,10 @@ int lfdm_parse_vehicle18(const char* veh_json, const char* tire_json, int tire_t
                          double* params, char* err, size_t err_len);
 int lfdm_load_driver_file(const char* path, double* rows, unsigned capacity_rows, unsigned* nrows, char* err,
                           size_t err_len);
+/* The loaders of any model: 11 (11dof-gpu/dof11_gpu.cu:910-1099), 18, or 24 with its suspension   */
+/* file (24dof-gpu/dof24_gpu.cu setVehParamsJSON/setTireParamsJSON/setSuspensionParamsJSON).       */
+int lfdm_parse_vehicle(int model, const char* veh_json, const char* tire_json, const char* sus_json, int tire_type,
+                       lfdm_class18* cls, double* params, char* err, size_t err_len);
 
 /* Extension: one window whose controls follow a per-step schedule shared by all vehicles          */
 /* (ctl: [nsteps][3] {steering, throttle, braking}), the C-ABI form of the reference's functor      */

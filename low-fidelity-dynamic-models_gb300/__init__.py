@@ -88,6 +88,7 @@ def _sig(lib):
         "lfdm_solve_range": ([vp, d, d], i),
         "lfdm_measure_fp64_peak": ([i, _c_dp], i),
         "lfdm_parse_vehicle18": ([cp, cp, i, vp, dp, ctypes.c_char_p, sz], i),
+        "lfdm_parse_vehicle": ([i, cp, cp, cp, i, vp, dp, ctypes.c_char_p, sz], i),
         "lfdm_load_driver_file": ([cp, dp, u, ctypes.POINTER(u), ctypes.c_char_p, sz], i),
         "lfdm_step18_noalloc": ([vp, i, vp, vp, vp, vp, vp, u, d, d, u, vp, ctypes.c_char_p, sz], i),
     }
@@ -127,6 +128,19 @@ def parse_vehicle18(veh_json: str, tire_json: str, tire_type: int = TireType.TMe
     err = ctypes.create_string_buffer(512)
     rc = lib().lfdm_parse_vehicle18(veh_json.encode(), tire_json.encode(), tire_type, ctypes.byref(c), _ptr(p),
                                     err, 512)
+    if rc:
+        raise LfdmError(rc, err.value.decode())
+    return c, p
+
+
+def parse_vehicle(model: int, veh_json: str, tire_json: str, sus_json: str | None = None,
+                  tire_type: int = TireType.TMeasy):
+    """The library's loader for any model (11, 18, or 24 with its suspension JSON)."""
+    c = Class18()
+    p = np.zeros(P_COUNT)
+    err = ctypes.create_string_buffer(512)
+    rc = lib().lfdm_parse_vehicle(int(model), veh_json.encode(), tire_json.encode(),
+                                  sus_json.encode() if sus_json else None, tire_type, ctypes.byref(c), _ptr(p), err, 512)
     if rc:
         raise LfdmError(rc, err.value.decode())
     return c, p

@@ -268,6 +268,8 @@ void default_vehicle(lfdm_class18& c, double* p) {
     p[LFDM_P_WIDTH] = 0.245; p[LFDM_P_RIM_RADIUS] = 0.254; p[LFDM_P_VCOULOMB] = 1.0; p[LFDM_P_FRBLEND_BEGIN] = 1.;
     p[LFDM_P_FRBLEND_END] = 3.; p[LFDM_P_BEARINGCAPACITY] = 10000; p[LFDM_P_LI] = 90; p[LFDM_P_P_LI] = 1.;
     p[LFDM_P_P_USE] = 1.;
+    // 24-DOF: VehicleParam()::_jy and SuspensionParam() defaults (24dof-gpu/dof24_gpu.cuh)
+    p[LFDM_P_JY] = 3516.; p[LFDM_P_KS] = 150062.; p[LFDM_P_BS] = 19068.;
 }
 
 void tire_init(double* p) {
@@ -278,12 +280,26 @@ void tire_init(double* p) {
     p[LFDM_P_RDYNCOCRIT] = r1 + (r2 - r1) * (fz / pn - 1.);
 }
 
-bool load_vehicle(int model, const std::string& veh_path, const std::string& tire_path, int tire_type, lfdm_class18& c,
-                    double* p, std::string& err) {
+bool load_vehicle(int model, const std::string& veh_path, const std::string& tire_path, const std::string& sus_path,
+                  int tire_type, lfdm_class18& c, double* p, std::string& err) {
     default_vehicle(c, p);
     JVal vd, td;
     if (!load_json(veh_path, vd, err)) return false;
     if (!load_json(tire_path, td, err)) return false;
+    if (model == LFDM_MODEL_24) {
+        // setSuspensionParamsJSON (24dof-gpu/dof24_gpu.cu; CPU 24dof/dof24.cpp:2192-2212)
+        JVal sd;
+        if (sus_path.empty()) {
+            err = "the 24-DOF model needs a suspension JSON";
+            return false;
+        }
+        if (!load_json(sus_path, sd, err)) return false;
+        Ctx sc{&sd, sus_path, {}};
+        if (!(sc.num("ks", p[LFDM_P_KS]) && sc.num("bs", p[LFDM_P_BS]))) {
+            err = sc.err;
+            return false;
+        }
+    }
     const double rpm2rad = 3.141592653589793238462643383279 / 30;  // utils_gpu.cuh:13
     Ctx v{&vd, veh_path, {}};
     static const struct {
@@ -293,13 +309,18 @@ bool load_vehicle(int model, const std::string& veh_path, const std::string& tir
               {"jz", LFDM_P_JZ},     {"jx", LFDM_P_JX},     {"jxz", LFDM_P_JXZ},   {"cf", LFDM_P_CF},
               {"cr", LFDM_P_CR},     {"muf", LFDM_P_MUF},   {"mur", LFDM_P_MUR},   {"hrcf", LFDM_P_HRCF},
               {"hrcr", LFDM_P_HRCR}, {"krof", LFDM_P_KROF}, {"kror", LFDM_P_KROR}, {"brof", LFDM_P_BROF},
-              {"bror", LFDM_P_BROR}};
+              {"bror", LFDM_P_BROR}, {"jy", LFDM_P_JY}};
     bool ok = true;
     for (auto& e : vk) {
-        // the 11-DOF vehicle file holds only a, b, m, h, jz, muf, mur (11dof-gpu/dof11_gpu.cu:910-1044)
+        // the 11-DOF vehicle file holds only a, b, m, h, jz, muf, mur (11dof-gpu/dof11_gpu.cu:910-1044);
+        // the 24-DOF one adds jy and has no jxz or roll stiffness/damping (24dof/dof24.cpp:2217-2339)
         if (model == LFDM_MODEL_11 && !(e.i == LFDM_P_A || e.i == LFDM_P_B || e.i == LFDM_P_M || e.i == LFDM_P_H ||
                                         e.i == LFDM_P_JZ || e.i == LFDM_P_MUF || e.i == LFDM_P_MUR))
             continue;
+        const bool only18 = e.i == LFDM_P_JXZ || e.i == LFDM_P_KROF || e.i == LFDM_P_KROR || e.i == LFDM_P_BROF ||
+                            e.i == LFDM_P_BROR;
+        if (model == LFDM_MODEL_24 && only18) continue;
+        if (model == LFDM_MODEL_18 && e.i == LFDM_P_JY) continue;
         ok = ok && v.num(e.k, p[e.i]);
     }
     bool b = false;
@@ -394,8 +415,8 @@ bool load_vehicle(int model, const std::string& veh_path, const std::string& tir
                                       LFDM_P_FYMP2N, LFDM_P_FYSPN,  LFDM_P_FYSP2N};
             for (int i : dbl) p[i] *= 2.;
         }
-    } else if (model == LFDM_MODEL_11) {
-        err = tire_path + ": TMeasyNr tires are not available for the 11-DOF model";
+    } else if (model != LFDM_MODEL_18) {
+        err = tire_path + ": TMeasyNr tires are available for the 18-DOF model only";
         return false;
     } else {
         const JVal* hl = td.get("highLevelParams");

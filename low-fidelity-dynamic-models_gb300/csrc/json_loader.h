@@ -26,11 +26,12 @@ bool read_file(const std::string& path, std::string& out);
 void default_vehicle(lfdm_class18& c, double* p);
 // tireInit (18dof-gpu/dof18_gpu.cu:227-233) on a flat parameter vector.
 void tire_init(double* p);
-// Vehicle JSON + tire JSON -> class record + flat parameter vector (tireInit applied), for the 11-
-// or 18-DOF model (the 11-DOF files hold fewer vehicle keys and its tire loader doubles most tire
-// parameters).
-bool load_vehicle(int model, const std::string& veh_path, const std::string& tire_path, int tire_type,
-                  lfdm_class18& c, double* p, std::string& err);
+// Vehicle JSON + tire JSON (+ suspension JSON for the 24-DOF model, else empty) -> class record +
+// flat parameter vector (tireInit applied), for the 11-, 18- or 24-DOF model (the 11-DOF files hold
+// fewer vehicle keys and its tire loader doubles most tire parameters; the 24-DOF vehicle file has
+// jy instead of the roll-stiffness terms).
+bool load_vehicle(int model, const std::string& veh_path, const std::string& tire_path, const std::string& sus_path,
+                  int tire_type, lfdm_class18& c, double* p, std::string& err);
 // LoadDriverData (utils/utils_gpu.cu:7-31): rows of {t, steering, throttle, braking}.
 bool load_driver_file(const std::string& path, std::vector<double>& rows, std::string& err);
 

@@ -588,11 +588,13 @@ const char* lfdm_last_error(const lfdm_solver* h) { return h ? h->err.c_str() : 
 int lfdm_construct(lfdm_solver* h, const char* veh_json, const char* tire_json, const char* sus_json,
                    unsigned num_vehicles, const char* driver_file, int tire_type) {
     if (!h || !veh_json || !tire_json) return h ? h->fail(LFDM_ERR_ARG, "null path") : LFDM_ERR_ARG;
-    if (sus_json) return h->fail(LFDM_ERR_ARG, "suspension file given for an 18-DOF solver");
+    if (h->model == LFDM_MODEL_24 && !sus_json) return h->fail(LFDM_ERR_ARG, "the 24-DOF model needs a suspension file");
+    if (h->model != LFDM_MODEL_24 && sus_json)
+        return h->fail(LFDM_ERR_ARG, "suspension file given for a %d-DOF solver", h->model);
     lfdm_class18 cls;
     std::vector<double> p(LFDM_P_COUNT);
     std::string err;
-    if (!load_vehicle(h->model, veh_json, tire_json, tire_type, cls, p.data(), err))
+    if (!load_vehicle(h->model, veh_json, tire_json, sus_json ? sus_json : "", tire_type, cls, p.data(), err))
         return h->fail(err.rfind("cannot open", 0) == 0 ? LFDM_ERR_IO : LFDM_ERR_PARSE, "%s", err.c_str());
     std::vector<double> table;
     if (driver_file) {
@@ -990,7 +992,19 @@ int lfdm_parse_vehicle18(const char* veh_json, const char* tire_json, int tire_t
                          double* params, char* err, size_t err_len) {
     if (!veh_json || !tire_json || !cls || !params) return LFDM_ERR_ARG;
     std::string e;
-    if (!load_vehicle(LFDM_MODEL_18, veh_json, tire_json, tire_type, *cls, params, e)) {
+    if (!load_vehicle(LFDM_MODEL_18, veh_json, tire_json, "", tire_type, *cls, params, e)) {
+        if (err && err_len) std::snprintf(err, err_len, "%s", e.c_str());
+        return e.rfind("cannot open", 0) == 0 ? LFDM_ERR_IO : LFDM_ERR_PARSE;
+    }
+    return LFDM_OK;
+}
+
+int lfdm_parse_vehicle(int model, const char* veh_json, const char* tire_json, const char* sus_json, int tire_type,
+                       lfdm_class18* cls, double* params, char* err, size_t err_len) {
+    if (!veh_json || !tire_json || !cls || !params) return LFDM_ERR_ARG;
+    if (model != LFDM_MODEL_11 && model != LFDM_MODEL_18 && model != LFDM_MODEL_24) return LFDM_ERR_ARG;
+    std::string e;
+    if (!load_vehicle(model, veh_json, tire_json, sus_json ? sus_json : "", tire_type, *cls, params, e)) {
         if (err && err_len) std::snprintf(err, err_len, "%s", e.c_str());
         return e.rfind("cannot open", 0) == 0 ? LFDM_ERR_IO : LFDM_ERR_PARSE;
     }

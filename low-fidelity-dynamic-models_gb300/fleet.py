@@ -164,3 +164,71 @@ def fleet18(n: int, seed: int = 20261203, horizon: float = 10.0, table_dt: float
     states = initial_states(cls, params, rng, u0_range)
     return {"cls": [cls], "class_of": np.zeros(n, dtype=np.int32), "params": params, "tables": tables,
             "states": states, "seed": seed, "horizon": horizon}
+
+
+# The same SUV for the 24-DOF model: its JSON holds the 24-DOF keys (pitch inertia instead of the
+# roll-stiffness terms) and a suspension with ks = 4e4 N/m and bs = 4e3 N s/m at every corner.
+SUV24_VEHICLE = {k: v for k, v in SUV18_VEHICLE.items() if k not in ("jxz", "krof", "kror", "brof", "bror")}
+SUV24_VEHICLE["jy"] = 3400.0
+SUV24_SUS = {"ks": 4.0e4, "bs": 4.0e3}
+G = 9.81  # utils/utils_gpu.cuh
+
+
+def suv24() -> tuple[Class18, np.ndarray]:
+    return vehicle_from_json(SUV24_VEHICLE, SUV_TIRE, TIRE_TMEASY, model=24, sus=SUV24_SUS)
+
+
+def init_tire_sus24(params: np.ndarray, states: np.ndarray) -> np.ndarray:
+    """initializeTireSus (24dof-gpu/dof24_gpu.cu:34-90, applied by Initialize) on [n] flat 24-DOF
+    states in place: static tire loads and compressions, spring preload and strut lengths, unsprung
+    vertical speed = chassis w."""
+    from ._abi import C
+    p = np.atleast_2d(params)
+    s = np.atleast_2d(states)
+    a, b, m, ks = p[:, P["a"]], p[:, P["b"]], p[:, P["m"]], p[:, P["ks"]]
+    fz_f = (m * G * b) / (2 * (a + b)) + p[:, P["muf"]] * G
+    fz_r = (m * G * a) / (2 * (a + b)) + p[:, P["mur"]] * G
+    xsi_f = (m * G * b) / (2 * (a + b) * ks)
+    xsi_r = (m * G * a) / (2 * (a + b) * ks)
+    T0, TN, S0, SN = C["LFDM24_S_TIRE0"], C["LFDM24_T_COUNT"], C["LFDM24_S_SUS0"], C["LFDM24_SUS_COUNT"]
+    for k in range(4):
+        fz = fz_f if k < 2 else fz_r
+        xsi = xsi_f if k < 2 else xsi_r
+        t0, s0 = T0 + k * TN, S0 + k * SN
+        s[:, t0 + C["LFDM24_T_FZ"]] = fz
+        xt = fz / p[:, P["kt"]]
+        s[:, t0 + C["LFDM24_T_XT"]] = xt
+        s[:, s0 + C["LFDM24_SUS_XSI"]] = xsi
+        s[:, s0 + C["LFDM24_SUS_XS"]] = xsi
+        lsi = p[:, P["h"]] - (p[:, P["r0"]] - xt)
+        s[:, s0 + C["LFDM24_SUS_LSI"]] = lsi
+        s[:, s0 + C["LFDM24_SUS_LS"]] = lsi
+        s[:, s0 + C["LFDM24_SUS_WU"]] = s[:, C["LFDM24_S_W"]]
+    return states
+
+
+def initial_states24(cls: Class18, params: np.ndarray, rng: np.random.Generator, u0_range=(0.0, 20.0)) -> np.ndarray:
+    """[n][LFDM24_S_COUNT] states: the 18-DOF initial_states' speed, wheel spin, gear and crank,
+    followed by initializeTireSus."""
+    from ._abi import C
+    s18 = initial_states(cls, params, rng, u0_range)
+    s = np.zeros((params.shape[0], C["LFDM24_S_COUNT"]))
+    s[:, C["LFDM24_S_U"]] = s18[:, S["u"]]
+    s[:, C["LFDM24_S_CRANKOMEGA"]] = s18[:, S["crankomega"]]
+    s[:, C["LFDM24_S_CURRENT_GR"]] = s18[:, S["current_gr"]]
+    for k in range(4):
+        s[:, C["LFDM24_S_TIRE0"] + k * C["LFDM24_T_COUNT"] + C["LFDM24_T_OMEGA"]] = s18[:, S_TIRE0 + T["omega"]]
+    return init_tire_sus24(params, s)
+
+
+def fleet24(n: int, seed: int = 20261203, horizon: float = 10.0, table_dt: float = 0.01,
+            brake_pulse: bool = True, jitter: bool = True, u0_range=(0.0, 20.0)) -> dict:
+    """The seeded 24-DOF SUV fleet (same draws as fleet18: jittered parameters, driver tables, initial
+    speeds), with states in the LFDM24_S_* layout after initializeTireSus."""
+    rng = np.random.default_rng(seed)
+    cls, base = suv24()
+    params = jitter_params(base, n, rng) if jitter else np.repeat(base[None, :], n, axis=0)
+    tables = driver_tables(n, rng, horizon, table_dt, params[:, P["maxsteer"]], brake_pulse)
+    states = initial_states24(cls, params, rng, u0_range)
+    return {"cls": [cls], "class_of": np.zeros(n, dtype=np.int32), "params": params, "tables": tables,
+            "states": states, "seed": seed, "horizon": horizon}

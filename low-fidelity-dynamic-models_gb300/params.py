@@ -22,7 +22,9 @@ VEH_DEFAULTS = {  # VehicleParam() defaults, dof18_gpu.cuh:506-531
     "cf": 1.82, "cr": 1.82, "muf": 127.866, "mur": 129.98, "hrcf": 0.379, "hrcr": 0.327,
     "krof": 31000.0, "kror": 31000.0, "brof": 3300.0, "bror": 3300.0, "maxsteer": 0.6525249,
     "crankinertia": 1.1, "maxbraketorque": 4000.0,
+    "jy": 3516.0,  # 24-DOF VehicleParam() default, 24dof-gpu/dof24_gpu.cuh
 }
+SUS_DEFAULTS = {"ks": 150062.0, "bs": 19068.0}  # SuspensionParam() defaults, 24dof-gpu/dof24_gpu.cuh
 TM_DEFAULTS = {  # TMeasyParam() defaults, dof18_gpu.cuh:29-64
     "jw": 6.69, "rr": 0.015, "mu": 0.8, "r0": 0.4699, "pn": 8562.8266, "pnmax": 29969.893,
     "cx": 185004.42, "cy": 164448.37, "kt": 411121.0, "dx": 3700.0, "dy": 3488.0, "rdyncopn": 0.375,
@@ -68,7 +70,7 @@ def tire_init(p: np.ndarray) -> np.ndarray:
 
 def default_params() -> np.ndarray:
     p = np.zeros(P_COUNT, dtype=np.float64)
-    for k, v in {**VEH_DEFAULTS, **TM_DEFAULTS, **NR_DEFAULTS}.items():
+    for k, v in {**VEH_DEFAULTS, **TM_DEFAULTS, **NR_DEFAULTS, **SUS_DEFAULTS}.items():
         p[P[k]] = v
     return p
 
@@ -77,21 +79,30 @@ _VEH_KEYS_11 = ["a", "b", "m", "h", "jz", "muf", "mur"]  # setVehParamsJSON, 11d
 _DOUBLED_11 = ["jw", "rr", "pn", "pnmax", "cx", "cy", "kt", "dx", "dy", "fzrdynco", "rdyncocrit", "dfx0pn", "dfx0p2n",
                "fxmpn", "fxmp2n", "fxspn", "fxsp2n", "dfy0pn", "dfy0p2n", "fympn", "fymp2n", "fyspn", "fysp2n"]
 _KEY_OF = {k.lower(): k for k in _TM_KEYS}
+# setVehParamsJSON, 24dof-gpu/dof24_gpu.cu (24dof/dof24.cpp:2217-2339)
+_VEH_KEYS_24 = ["a", "b", "m", "h", "jz", "jx", "jy", "cf", "cr", "muf", "mur", "hrcf", "hrcr"]
 
 
-def vehicle_from_json(veh, tire, tire_type: int = TIRE_TMEASY, model: int = 18) -> tuple[Class18, np.ndarray]:
+def vehicle_from_json(veh, tire, tire_type: int = TIRE_TMEASY, model: int = 18, sus=None) -> tuple[Class18, np.ndarray]:
     """Parse a vehicle JSON and a tire JSON (paths or dicts) the way Construct does.
 
     Returns the class record and the flat parameter vector with tireInit applied
     (d18SolverHalfImplicitGPU::Construct calls tireInit after loading, dof18_halfImplicit_gpu.cu:78).
-    model 11 reads the 11-DOF vehicle keys (11dof-gpu/dof11_gpu.cu:910-1044).
+    model 11 reads the 11-DOF vehicle keys (11dof-gpu/dof11_gpu.cu:910-1044); model 24 the 24-DOF
+    ones and the suspension JSON `sus` (setSuspensionParamsJSON, 24dof/dof24.cpp:2192-2212).
     """
     d = _load(veh)
     t = _load(tire)
     p = default_params()
     c = Class18()
     c.driveType, c.whichWheels = 1, 1
-    for k in (_VEH_KEYS_11 if model == 11 else _VEH_KEYS):
+    if model == 24:
+        if sus is None:
+            raise ValueError("the 24-DOF model needs a suspension JSON")
+        s = _load(sus)
+        p[P["ks"]] = float(s["ks"])
+        p[P["bs"]] = float(s["bs"])
+    for k in {11: _VEH_KEYS_11, 24: _VEH_KEYS_24}.get(model, _VEH_KEYS):
         p[P[k]] = float(d[k])
     c.nonLinearSteer = int(bool(d["nonLinearSteer"]))
     if c.nonLinearSteer:

@@ -926,6 +926,479 @@ static void run_vehicle11(const oracle18_args* a, int i) {
     store_state11(a->states + (size_t)i * LFDM11_S_COUNT, &v, t);
 }
 
+/* ---------------------------------------------------------------------------------------------- */
+/* 24-DOF model (24dof/dof24.cpp, 24dof/dof24_halfImplicit.cpp; GPU twins 24dof-gpu/dof24_gpu.cu    */
+/* and 24dof-gpu/dof24_halfImplicit_gpu.cu, identical arithmetic except that the GPU driveTorque   */
+/* scales the shared engine map in place under throttleMod). TMeasy tires. Field order of the      */
+/* structs below is the reference structs' (24dof-gpu/dof24_gpu.cuh).                              */
+typedef struct {
+    double x, y, z, u, v, w, psi, wz, phi, wx, theta, wy, udot, vdot, wdot, wxdot, wydot, wzdot, dtheta, dphi,
+        dpsi, crankOmega, dOmega_crank;
+    int current_gr;
+} Veh24;
+typedef struct {
+    double xe, ye, xedot, yedot, omega, dOmega, xt, dxt, rStat, fx, fy, fz, fxg, fyg, fzg, vgx, vgy, vgz, vsx, vsy,
+        vsz, My, engTor;
+} Tire24;
+typedef struct {
+    double xs, xsi, dxs, ls, lsi, us, vs, ws, dus, dvs, dws, uu, vu, wu, duu, dvu, dwu, fxs, fys, fzs, fzd, mx, my,
+        mz;
+} Sus24;
+
+_Static_assert(sizeof(Tire24) == LFDM24_T_COUNT * sizeof(double), "Tire24 is the flat tire block");
+_Static_assert(sizeof(Sus24) == LFDM24_SUS_COUNT * sizeof(double), "Sus24 is the flat suspension block");
+
+static void load_state24(const double* s, Veh24* v, Tire24* t, Sus24* su) {
+    memcpy(v, s, LFDM24_S_CURRENT_GR * sizeof(double)); /* the doubles before current_gr */
+    v->current_gr = (int)s[LFDM24_S_CURRENT_GR];
+    for (int c = 0; c < 4; ++c) {
+        memcpy(&t[c], s + LFDM24_S_TIRE0 + c * LFDM24_T_COUNT, sizeof(Tire24));
+        memcpy(&su[c], s + LFDM24_S_SUS0 + c * LFDM24_SUS_COUNT, sizeof(Sus24));
+    }
+}
+static void store_state24(double* s, const Veh24* v, const Tire24* t, const Sus24* su) {
+    memcpy(s, v, LFDM24_S_CURRENT_GR * sizeof(double));
+    s[LFDM24_S_CURRENT_GR] = (double)v->current_gr;
+    for (int c = 0; c < 4; ++c) {
+        memcpy(s + LFDM24_S_TIRE0 + c * LFDM24_T_COUNT, &t[c], sizeof(Tire24));
+        memcpy(s + LFDM24_S_SUS0 + c * LFDM24_SUS_COUNT, &su[c], sizeof(Sus24));
+    }
+}
+
+/* initializeTireSus: dof24.cpp:34-88 (GPU: dof24_gpu.cu:34-90, called by Initialize) */
+static void init_tire_sus24(Veh24* v, Tire24* t, Sus24* su, const double* p) {
+    const double a = p[LFDM_P_A], b = p[LFDM_P_B], m = p[LFDM_P_M], ks = p[LFDM_P_KS];
+    double weight_split = ((m * G * b) / (2 * (a + b)) + p[LFDM_P_MUF] * G);
+    t[0].fz = t[1].fz = weight_split;
+    weight_split = ((m * G * a) / (2 * (a + b)) + p[LFDM_P_MUR] * G);
+    t[2].fz = t[3].fz = weight_split;
+    for (int c = 0; c < 4; ++c) t[c].xt = t[c].fz / p[LFDM_P_KT];
+    su[0].xsi = (m * G * b) / (2 * (a + b) * ks);
+    su[2].xsi = (m * G * a) / (2 * (a + b) * ks);
+    su[1].xsi = su[0].xsi;
+    su[3].xsi = su[2].xsi;
+    for (int c = 0; c < 4; ++c) su[c].xs = su[c].xsi;
+    for (int c = 0; c < 4; ++c) su[c].lsi = p[LFDM_P_H] - (p[LFDM_P_R0] - t[c].xt);
+    for (int c = 0; c < 4; ++c) su[c].ls = su[c].lsi;
+    for (int c = 0; c < 4; ++c) su[c].wu = v->w;
+}
+
+/* vehToSusTransform: dof24.cpp:148-229. Corner signs: LF (-cf/2, +a), RF (+cf/2, +a),           */
+/* LR (-cr/2, -b), RR (+cr/2, -b); uses the previous step's accelerations and dxs.                  */
+static void vehToSus24(const Veh24* v, Sus24* su, const Par* pp) {
+    const double cf = P(LFDM_P_CF), cr = P(LFDM_P_CR), a = P(LFDM_P_A), b = P(LFDM_P_B);
+    su[0].us = (-cf * v->wz / 2.) + v->u;
+    su[0].vs = a * v->wz + v->v;
+    su[0].ws = (cf * v->wx / 2.) - (a * v->wy) + v->w;
+    su[1].us = (cf * v->wz / 2.) + v->u;
+    su[1].vs = a * v->wz + v->v;
+    su[1].ws = (-cf * v->wx / 2.) - (a * v->wy) + v->w;
+    su[2].us = (-cr * v->wz / 2.) + v->u;
+    su[2].vs = -b * v->wz + v->v;
+    su[2].ws = (cr * v->wx / 2.) + b * v->wy + v->w;
+    su[3].us = (cr * v->wz / 2.) + v->u;
+    su[3].vs = -b * v->wz + v->v;
+    su[3].ws = (-cr * v->wx / 2.) + b * v->wy + v->w;
+    for (int c = 0; c < 4; ++c) su[c].ls = su[c].lsi - (su[c].xs - su[c].xsi);
+    for (int c = 0; c < 4; ++c) su[c].uu = su[c].us - su[c].ls * v->wy;
+    for (int c = 0; c < 4; ++c) su[c].vu = su[c].vs + su[c].ls * v->wx;
+    su[0].dus = (-cf * v->wzdot) / 2 + v->udot;
+    su[0].dvs = a * v->wzdot + v->vdot;
+    su[1].dus = (cf * v->wzdot) / 2 + v->udot;
+    su[1].dvs = a * v->wzdot + v->vdot;
+    su[2].dus = (-cr * v->wzdot) / 2 + v->udot;
+    su[2].dvs = -b * v->wzdot + v->vdot;
+    su[3].dus = (cr * v->wzdot) / 2 + v->udot;
+    su[3].dvs = (-b * v->wzdot) + v->vdot;
+    for (int c = 0; c < 4; ++c) {
+        su[c].duu = su[c].dus - (-su[c].dxs * v->wy + su[c].ls * v->wydot);
+        su[c].dvu = su[c].dvs + (-su[c].dxs * v->wx + su[c].ls * v->wxdot);
+    }
+}
+
+/* vehToTireTransform: dof24.cpp:313-384. The contact-patch lateral velocity is vgy unrotated. */
+static void vehToTire24(const Veh24* v, Tire24* t, const Sus24* su, const Par* pp, double steering) {
+    double delta = wheel_angle(pp, steering);
+    for (int c = 0; c < 4; ++c) {
+        t[c].vgx = cos(v->theta) * (su[c].uu - v->wy * t[c].rStat) +
+                   sin(v->theta) * (su[c].wu * cos(v->phi) + sin(v->phi) * (v->wx * t[c].rStat + su[c].vu));
+        t[c].vgy = cos(v->phi) * (su[c].vu + v->wx * t[c].rStat) - su[c].wu * sin(v->phi);
+    }
+    for (int c = 0; c < 2; ++c) {
+        t[c].vsy = t[c].vgy;
+        t[c].vsx = t[c].vgx * cos(delta) + t[c].vgy * sin(delta);
+    }
+    for (int c = 2; c < 4; ++c) {
+        t[c].vsy = t[c].vgy;
+        t[c].vsx = t[c].vgx;
+    }
+}
+
+/* computeTireRHS (TMeasy): dof24.cpp:827-986. Differs from the 18-DOF tire in the load (fz from */
+/* the integrated compression xt) and the loaded radius (divided by cos(theta) cos(phi)).         */
+static void tireRHS24(const Veh24* v, Tire24* ts, const Par* pp, double steering) {
+    double delta = wheel_angle(pp, steering);
+    ts->fz = ts->xt * P(LFDM_P_KT);
+    double fz = ts->fz;
+    double vsy = ts->vsy;
+    double vsx = ts->vsx;
+    const double pn = P(LFDM_P_PN), r0 = P(LFDM_P_R0);
+    ts->rStat = (r0 - ts->xt) / (cos(v->theta) * cos(v->phi));
+    if (fz <= 0) {
+        ts->xe = 0;
+        ts->ye = 0;
+        ts->omega = 0;
+        ts->xt = 0;
+        ts->rStat = r0;
+        ts->fz = 0;
+        ts->fx = 0;
+        ts->fy = 0;
+        ts->My = 0;
+        return;
+    }
+    double r_eff, rdynco;
+    if (fz <= P(LFDM_P_FZRDYNCO)) {
+        rdynco = InterpL(fz, P(LFDM_P_RDYNCOPN), P(LFDM_P_RDYNCOP2N), pn);
+        r_eff = rdynco * r0 + (1. - rdynco) * ts->rStat;
+    } else {
+        rdynco = P(LFDM_P_RDYNCOCRIT);
+        r_eff = rdynco * r0 + (1. - rdynco) * ts->rStat;
+    }
+    vsx = vsx - (ts->omega * r_eff);
+    double vta = r_eff * fabs(ts->omega) + 0.01;
+    double sx = -vsx / vta;
+    double alpha = atan2(vsy, vta) - delta;
+    double sy = -tan(alpha);
+    if (fz > P(LFDM_P_PNMAX)) fz = P(LFDM_P_PNMAX);
+    double dfx0 = InterpQ(fz, P(LFDM_P_DFX0PN), P(LFDM_P_DFX0P2N), pn);
+    double dfy0 = InterpQ(fz, P(LFDM_P_DFY0PN), P(LFDM_P_DFY0P2N), pn);
+    double fxm = InterpQ(fz, P(LFDM_P_FXMPN), P(LFDM_P_FXMP2N), pn);
+    double fym = InterpQ(fz, P(LFDM_P_FYMPN), P(LFDM_P_FYMP2N), pn);
+    double fxs = InterpQ(fz, P(LFDM_P_FXSPN), P(LFDM_P_FXSP2N), pn);
+    double fys = InterpQ(fz, P(LFDM_P_FYSPN), P(LFDM_P_FYSP2N), pn);
+    double sxm = InterpL(fz, P(LFDM_P_SXMPN), P(LFDM_P_SXMP2N), pn);
+    double sym = InterpL(fz, P(LFDM_P_SYMPN), P(LFDM_P_SYMP2N), pn);
+    double sxs = InterpL(fz, P(LFDM_P_SXSPN), P(LFDM_P_SXSP2N), pn);
+    double sys = InterpL(fz, P(LFDM_P_SYSPN), P(LFDM_P_SYSP2N), pn);
+    double hsxn = sxm / (sxm + sym) + (fxm / dfx0) / (fxm / dfx0 + fym / dfy0);
+    double hsyn = sym / (sxm + sym) + (fym / dfy0) / (fxm / dfx0 + fym / dfy0);
+    double sxn = sx / hsxn;
+    double syn = sy / hsyn;
+    double sc = hypot(sxn, syn);
+    double calpha, salpha;
+    if (sc > 0) {
+        calpha = sxn / sc;
+        salpha = syn / sc;
+    } else {
+        calpha = sqrt(2.) / 2.;
+        salpha = sqrt(2.) / 2.;
+    }
+    double df0 = hypot(dfx0 * calpha * hsxn, dfy0 * salpha * hsyn);
+    double fm = hypot(fxm * calpha, fym * salpha);
+    double sm = hypot(sxm * calpha / hsxn, sym * salpha / hsyn);
+    double fs = hypot(fxs * calpha, fys * salpha);
+    double ss = hypot(sxs * calpha / hsxn, sys * salpha / hsyn);
+    double f, fos;
+    tmxy_combined(&f, &fos, sc, df0, sm, fm, ss, fs);
+    double vx_min = 0., vx_max = 0.;
+    ts->My = -sineStep(vta, vx_min, 0., vx_max, 1.) * P(LFDM_P_RR) * fz * ts->rStat * sgn(ts->omega);
+    double vtxs = r_eff * fabs(ts->omega) * hsxn + 0.01;
+    double vtys = r_eff * fabs(ts->omega) * hsyn + 0.01;
+    const double cx = P(LFDM_P_CX), cy = P(LFDM_P_CY), dx = P(LFDM_P_DX), dy = P(LFDM_P_DY);
+    ts->xedot = (-vtxs * cx * ts->xe - fos * vsx) / (vtxs * dx + fos);
+    ts->yedot = (-vtys * cy * ts->ye - fos * (-sy * vta)) / (vtys * dy + fos);
+    double fxdyn = dx * (-vtxs * cx * ts->xe - fos * vsx) / (vtxs * dx + fos) + cx * ts->xe;
+    double fydyn = dy * ((-vtys * cy * ts->ye - fos * (-sy * vta)) / (vtys * dy + fos)) + (cy * ts->ye);
+    double fxstr = clampd(ts->xe * cx + ts->xedot * dx, -P(LFDM_P_FXMP2N), P(LFDM_P_FXMP2N));
+    double fystr = clampd(ts->ye * cy + ts->yedot * dy, -P(LFDM_P_FYMP2N), P(LFDM_P_FYMP2N));
+    double weightx = sineStep(fabs(vsx), 1., 1., 1.5, 0.);
+    double weighty = sineStep(fabs(-sy * vta), 1., 1., 1.5, 0.);
+    ts->fx = weightx * fxstr + (1. - weightx) * fxdyn;
+    ts->fy = weighty * fystr + (1. - weighty) * fydyn;
+}
+
+/* computeTireCompressionVelocity: dof24.cpp:1122-1150 */
+static void tireCompression24(const Veh24* v, Tire24* t, const Sus24* su) {
+    for (int c = 0; c < 4; ++c)
+        t[c].dxt = t[c].vsz - (cos(v->theta) * (su[c].wu * cos(v->phi) + su[c].vu * sin(v->phi)) -
+                               su[c].uu * sin(v->theta));
+}
+
+/* computePowertrainRHS: dof24.cpp:1338-1508 (the 18-DOF powertrain on the 24-DOF structs) */
+static void powertrain24(Veh24* v, Tire24* t, const Par* pp, const double* controls) {
+    const lfdm_class18* c = pp->c;
+    double torque_t = 0;
+    double max_bias = 2;
+    const double throttle = controls[2], braking = controls[3];
+    if (c->tcbool) {
+        int tc_reverse_flow = 0;
+        double omega_t = 0.25 * (t[0].omega + t[1].omega + t[2].omega + t[3].omega);
+        double omega_out = omega_t / (c->gearRatios[v->current_gr]);
+        double omega_in = v->crankOmega;
+        double sr, cf, tr;
+        if ((omega_out < 1e-9) || (omega_in < 1e-9)) {
+            sr = 0;
+            cf = oracle_map_y(&c->CFmap[0][0], c->CFmapSize, sr);
+            tr = oracle_map_y(&c->TRmap[0][0], c->TRmapSize, sr);
+        } else {
+            sr = omega_out / omega_in;
+            if (sr > 1.) {
+                sr = 1. - (sr - 1.);
+                tc_reverse_flow = 1;
+            }
+            if (sr < 0) sr = 0;
+            cf = oracle_map_y(&c->CFmap[0][0], c->CFmapSize, sr);
+            tr = oracle_map_y(&c->TRmap[0][0], c->TRmapSize, sr);
+        }
+        double torque_in = -pow((omega_in / cf), 2);
+        if (tc_reverse_flow) torque_in = -torque_in;
+        double torque_out;
+        if (tc_reverse_flow) torque_out = -torque_in;
+        else torque_out = -tr * torque_in;
+        torque_t = torque_out / c->gearRatios[v->current_gr];
+        /* reference: abs((u - 0) < 1e-9) && (torque_t < 0) — abs() of the comparison's result */
+        if ((v->u - 0) < 1e-9 && (torque_t < 0)) torque_t = 0;
+        v->dOmega_crank = (1. / P(LFDM_P_CRANKINERTIA)) * (driveTorque(pp, throttle, v->crankOmega) + torque_in);
+        if (omega_out > c->shiftMap[v->current_gr][1]) {
+            if (v->current_gr < c->noGears - 1) v->current_gr++;
+        } else if (omega_out < c->shiftMap[v->current_gr][0]) {
+            if (v->current_gr > 0) v->current_gr--;
+        }
+    } else {
+        v->crankOmega =
+            0.25 * (t[0].omega + t[1].omega + t[2].omega + t[3].omega) / c->gearRatios[v->current_gr];
+        torque_t = driveTorque(pp, throttle, v->crankOmega) / c->gearRatios[v->current_gr];
+        if ((v->u - 0) < 1e-9 && (torque_t < 0)) torque_t = 0;
+        if (v->crankOmega > c->shiftMap[v->current_gr][1]) {
+            if (v->current_gr < c->noGears - 1) v->current_gr++;
+        } else if (v->crankOmega < c->shiftMap[v->current_gr][0]) {
+            if (v->current_gr > 0) v->current_gr--;
+        }
+    }
+    double torque_front = 0, torque_rear = 0;
+    if (c->driveType) {
+        torque_front = torque_t * 0.5;
+        torque_rear = torque_t * 0.5;
+    } else {
+        if (c->whichWheels) {
+            torque_front = 0;
+            torque_rear = torque_t;
+        } else {
+            torque_front = torque_t;
+            torque_rear = 0;
+        }
+    }
+    differentialSplit(torque_front, max_bias, t[0].omega, t[1].omega, &t[0].engTor, &t[1].engTor);
+    differentialSplit(torque_rear, max_bias, t[2].omega, t[3].omega, &t[2].engTor, &t[3].engTor);
+    const double jw = P(LFDM_P_JW);
+    const double brake = P(LFDM_P_MAXBRAKETORQUE) * braking; /* brakeTorque: dof24.h:1484-1486 */
+    for (int k = 0; k < 4; ++k)
+        t[k].dOmega = (1 / jw) * (t[k].engTor + t[k].My - sgn(t[k].omega) * brake - t[k].fx * t[k].rStat);
+}
+
+/* tireToVehTransform: dof24.cpp:459-527 (front forces rotated by the wheel angle and stored back, */
+/* then all four expressed in the chassis frame through pitch and roll)                          */
+static void tireToVeh24(const Veh24* v, Tire24* t, const Par* pp, double steering) {
+    double delta = wheel_angle(pp, steering);
+    for (int k = 0; k < 2; ++k) {
+        double fx = t[k].fx * cos(delta) - t[k].fy * sin(delta);
+        double fy = t[k].fx * sin(delta) + t[k].fy * cos(delta);
+        t[k].fx = fx;
+        t[k].fy = fy;
+    }
+    for (int k = 0; k < 4; ++k) {
+        t[k].fxg = t[k].fx * cos(v->theta) - t[k].fz * sin(v->theta);
+        t[k].fyg = t[k].fx * sin(v->phi) * sin(v->theta) + t[k].fy * cos(v->phi) +
+                   t[k].fz * sin(v->phi) * cos(v->theta);
+        t[k].fzg = t[k].fx * sin(v->theta) * cos(v->phi) - t[k].fy * sin(v->phi) +
+                   t[k].fz * cos(v->phi) * cos(v->theta);
+    }
+}
+
+/* computeSusRHS: dof24.cpp:1182-1228 (uses the previous step's jacking force fzd and dxs, then   */
+/* sets the new dxs)                                                                              */
+static void susRHS24(const Veh24* v, const Tire24* t, Sus24* su, const Par* pp) {
+    const double theta = v->theta, phi = v->phi;
+    const double ks = P(LFDM_P_KS), bs = P(LFDM_P_BS);
+    for (int c = 0; c < 4; ++c) {
+        const double mu = c < 2 ? P(LFDM_P_MUF) : P(LFDM_P_MUR);
+        su[c].dwu = (1 / mu) * (cos(phi) * (cos(theta) * (t[c].fz - mu * G) + sin(theta) * t[c].fx) -
+                                sin(phi) * t[c].fy - su[c].fzd - su[c].xs * ks - su[c].dxs * bs -
+                                mu * (su[c].vu * v->wx - su[c].uu * v->wy));
+    }
+    for (int c = 0; c < 4; ++c) su[c].dxs = -su[c].ws + su[c].wu;
+}
+
+/* computeForcesThroughSus: dof24.cpp:599-679. The rear-right lateral force omits the cos(theta) */
+/* factor of the other three corners (:639 as in the reference; GPU twin dof24_gpu.cu:649).       */
+static void forcesThroughSus24(const Veh24* v, const Tire24* t, Sus24* su, const Par* pp) {
+    const double ks = P(LFDM_P_KS), bs = P(LFDM_P_BS);
+    for (int c = 0; c < 4; ++c) {
+        const double mu = c < 2 ? P(LFDM_P_MUF) : P(LFDM_P_MUR);
+        su[c].fxs = t[c].fxg + mu * G * sin(v->theta) - mu * su[c].duu + mu * v->wz * su[c].vu -
+                    mu * v->wy * su[c].wu;
+        if (c < 3)
+            su[c].fys = t[c].fyg - mu * G * sin(v->phi) * cos(v->theta) - mu * su[c].dvu + mu * v->wx * su[c].wu -
+                        mu * v->wz * su[c].uu;
+        else
+            su[c].fys = t[c].fyg - mu * G * sin(v->phi) - mu * su[c].dvu + mu * v->wx * su[c].wu -
+                        mu * v->wz * su[c].uu;
+        su[c].fzs = su[c].xs * ks + su[c].dxs * bs;
+    }
+    su[1].fzd = (t[1].fyg * t[1].rStat + su[1].fys * su[1].ls + t[0].fyg * t[0].rStat + su[0].fys * su[0].ls -
+                 (su[1].fys + su[0].fys) * P(LFDM_P_HRCF)) /
+                P(LFDM_P_CF);
+    su[0].fzd = -su[1].fzd;
+    su[3].fzd = (t[3].fyg * t[3].rStat + su[3].fys * su[3].ls + t[2].fyg * t[2].rStat + su[2].fys * su[2].ls -
+                 (su[3].fys + su[2].fys) * P(LFDM_P_HRCR)) /
+                P(LFDM_P_CR);
+    su[2].fzd = -su[3].fzd;
+    for (int c = 0; c < 4; ++c) su[c].mx = su[c].fys * (c < 2 ? P(LFDM_P_HRCF) : P(LFDM_P_HRCR));
+    for (int c = 0; c < 4; ++c) su[c].my = -(t[c].fxg * t[c].rStat + su[c].fxs * su[c].ls);
+    for (int c = 0; c < 4; ++c) su[c].mz = 0;
+}
+
+/* computeVehicleRHS: dof24.cpp:1682-1732 (the global dx, dy that only the Sundials solver reads are */
+/* not part of the GPU state and are left out)                                                      */
+static void vehRHS24(Veh24* v, const Sus24* su, const Par* pp) {
+    const double m = P(LFDM_P_M), a = P(LFDM_P_A), b = P(LFDM_P_B), cf = P(LFDM_P_CF), cr = P(LFDM_P_CR);
+    v->udot = v->wz * v->v - v->wy * v->w + (1 / m) * (su[0].fxs + su[1].fxs + su[2].fxs + su[3].fxs) +
+              G * sin(v->theta);
+    v->vdot = v->wx * v->w - v->wz * v->u + (1 / m) * (su[0].fys + su[1].fys + su[2].fys + su[3].fys) -
+              G * sin(v->phi) * cos(v->theta);
+    v->wdot = v->wy * v->u - v->wx * v->v +
+              (1 / m) * (su[0].fzs + su[1].fzs + su[2].fzs + su[3].fzs + su[0].fzd + su[1].fzd + su[2].fzd +
+                         su[3].fzd) -
+              G * cos(v->phi) * cos(v->theta);
+    v->wxdot = (1 / P(LFDM_P_JX)) * ((su[0].mx + su[1].mx + su[2].mx + su[3].mx) + (su[0].fzs - su[1].fzs) * (cf / 2.) +
+                                     (su[2].fzs - su[3].fzs) * (cr / 2.));
+    v->wydot = (1 / P(LFDM_P_JY)) *
+               ((su[0].my + su[1].my + su[2].my + su[3].my) + (su[2].fzs + su[3].fzs) * b - (su[0].fzs + su[1].fzs) * a);
+    v->wzdot = (1 / P(LFDM_P_JZ)) * ((su[0].mz + su[1].mz + su[2].mz + su[3].mz) + (su[0].fys + su[1].fys) * a -
+                                     (su[2].fys + su[3].fys) * b + (-su[0].fxs + su[1].fxs) * (cf / 2.) +
+                                     (-su[2].fxs + su[3].fxs) * (cr / 2.));
+    v->dtheta = v->wy * cos(v->phi) - v->wz * sin(v->phi);
+    v->dpsi = (v->wy * sin(v->phi) / cos(v->theta)) + (v->wz * cos(v->phi) / cos(v->theta));
+    v->dphi = v->wx + v->wy * sin(v->phi) * tan(v->theta) + v->wz * cos(v->phi) * tan(v->theta);
+}
+
+/* rhsFun: 24dof-gpu/dof24_halfImplicit_gpu.cu:728-775 (CPU 24dof/dof24_halfImplicit.cpp:594-650) */
+static void rhs24(Veh24* v, Tire24* t, Sus24* su, const Par* pp, const double* controls) {
+    const double steering = controls[1];
+    vehToSus24(v, su, pp);
+    vehToTire24(v, t, su, pp, steering);
+    tireRHS24(v, &t[0], pp, steering);
+    tireRHS24(v, &t[1], pp, steering);
+    tireRHS24(v, &t[2], pp, 0);
+    tireRHS24(v, &t[3], pp, 0);
+    tireCompression24(v, t, su);
+    powertrain24(v, t, pp, controls);
+    tireToVeh24(v, t, pp, steering);
+    susRHS24(v, t, su, pp);
+    forcesThroughSus24(v, t, su, pp);
+    vehRHS24(v, su, pp);
+}
+
+/* half-implicit update: 24dof-gpu/dof24_halfImplicit_gpu.cu:1016-1081 (CPU :199-283). Angles use  */
+/* the updated body rates, and x, y the updated yaw.                                              */
+static void update24(Veh24* v, Tire24* t, Sus24* su, const Par* pp, double step) {
+    for (int k = 0; k < 4; ++k) {
+        t[k].xe += t[k].xedot * step;
+        t[k].ye += t[k].yedot * step;
+        t[k].xt += t[k].dxt * step;
+        t[k].omega += t[k].dOmega * step;
+    }
+    for (int k = 0; k < 4; ++k) {
+        su[k].wu += su[k].dwu * step;
+        su[k].xs += su[k].dxs * step;
+    }
+    if (pp->c->tcbool) v->crankOmega += v->dOmega_crank * step;
+    v->u += v->udot * step;
+    v->v += v->vdot * step;
+    v->w += v->wdot * step;
+    v->wx += v->wxdot * step;
+    v->wy += v->wydot * step;
+    v->wz += v->wzdot * step;
+    v->dtheta = v->wy * cos(v->phi) - v->wz * sin(v->phi);
+    v->dpsi = (v->wy * sin(v->phi) / cos(v->theta)) + (v->wz * cos(v->phi) / cos(v->theta));
+    v->dphi = v->wx + v->wy * sin(v->phi) * tan(v->theta) + v->wz * cos(v->phi) * tan(v->theta);
+    v->theta += v->dtheta * step;
+    v->psi += v->dpsi * step;
+    v->phi += v->dphi * step;
+    v->x += (v->u * cos(v->psi) - v->v * sin(v->psi)) * step;
+    v->y += (v->u * sin(v->psi) + v->v * cos(v->psi)) * step;
+}
+
+/* one GPU launch window (Integrate, 24dof-gpu/dof24_halfImplicit_gpu.cu:955-1113) */
+static void window24(const oracle18_args* a, int i, Veh24* v, Tire24* t, Sus24* su, const Par* pp,
+                     double current_time, int64_t sample_base) {
+    const double step = a->dt;
+    double tt = current_time;
+    double kernel_time = 0;
+    int64_t stored = 0;
+    const double end_time = (tt + a->ksim) - step / 10.;
+    while (tt < end_time) {
+        double c[4];
+        controls_at(a, i, tt, c);
+        rhs24(v, t, su, pp, c);
+        update24(v, t, su, pp, step);
+        tt += step;
+        kernel_time += step;
+        if (a->resp && a->dtout > 0) {
+            if (fabs(kernel_time - (stored + 1) * a->dtout) < 1e-7) {
+                int64_t smp = sample_base + stored;
+                if (stored < a->samples_per_window && smp < a->resp_samples) {
+                    double* r = a->resp + (size_t)smp * LFDM24_RESP_CHANNELS * a->n;
+                    const double ch[LFDM24_RESP_CHANNELS] = {tt,         v->x,       v->y,       v->u,      v->v,
+                                                             v->phi,     v->psi,     v->theta,   v->wx,     v->wz,
+                                                             v->wy,      t[0].omega, t[1].omega, t[2].omega, t[3].omega};
+                    for (int k = 0; k < LFDM24_RESP_CHANNELS; ++k) r[(size_t)k * a->n + i] = ch[k];
+                }
+                stored++;
+            }
+        }
+    }
+}
+
+static void run_vehicle24(const oracle18_args* a, int i) {
+    Veh24 v;
+    Tire24 t[4];
+    Sus24 su[4];
+    Par pp = {a->params + (size_t)i * LFDM_P_COUNT, &a->classes[a->class_of[i]]};
+    load_state24(a->states + (size_t)i * LFDM24_S_COUNT, &v, t, su);
+    if (a->schedule == 0) {
+        /* d24SolverHalfImplicit::Integrate, 24dof/dof24_halfImplicit.cpp:188-297 */
+        double tt = a->t0;
+        while (tt < (a->tend - a->dt / 10.)) {
+            double c[4];
+            controls_at(a, i, tt, c);
+            rhs24(&v, t, su, &pp, c);
+            update24(&v, t, su, &pp, a->dt);
+            tt += a->dt;
+        }
+    } else if (a->schedule == 1) {
+        double current_time = a->t0;
+        int64_t w = 0;
+        while (current_time < a->tend) {
+            window24(a, i, &v, t, su, &pp, current_time, w * a->samples_per_window);
+            current_time = current_time + a->ksim;
+            ++w;
+        }
+    } else {
+        window24(a, i, &v, t, su, &pp, a->t0, 0);
+    }
+    store_state24(a->states + (size_t)i * LFDM24_S_COUNT, &v, t, su);
+}
+
+void oracle24_init_state(const double* params, double* state) {
+    Veh24 v;
+    Tire24 t[4];
+    Sus24 su[4];
+    load_state24(state, &v, t, su);
+    init_tire_sus24(&v, t, su, params);
+    store_state24(state, &v, t, su);
+}
+
 typedef void (*vehicle_fn)(const oracle18_args*, int);
 
 typedef struct {
@@ -968,3 +1441,4 @@ static int run_all(const oracle18_args* a, vehicle_fn fn) {
 
 int oracle18_run(const oracle18_args* a) { return run_all(a, run_vehicle); }
 int oracle11_run(const oracle18_args* a) { return run_all(a, run_vehicle11); }
+int oracle24_run(const oracle18_args* a) { return run_all(a, run_vehicle24); }

@@ -125,3 +125,46 @@ def case_inputs(case):
     if case["tp"]:
         params.tire_init(p)
     return cls, p, np.array(case["state"], dtype=np.float64), np.array(case["driver"], dtype=np.float64)
+
+
+def state_floors24():
+    """Floors of the 24-DOF state vector (LFDM24_S_* layout): positions 1 m, speeds 1 m/s, angles
+    1 rad, rates 1 rad/s, accelerations 1 m/s^2 (1 rad/s^2), wheel and crank speeds 10 rad/s, tire
+    deflections and compressions and spring compressions 1e-3 m, forces 1e3 N, moments 1e3 N m."""
+    abi = pkg_mod("_abi")
+    C = abi.C
+    fl = np.full(C["LFDM24_S_COUNT"], 1.0)
+    fl[C["LFDM24_S_CRANKOMEGA"]] = 10.0
+    fl[C["LFDM24_S_DOMEGA_CRANK"]] = 10.0
+    for k in range(4):
+        b = C["LFDM24_S_TIRE0"] + k * C["LFDM24_T_COUNT"]
+        for f in ("XE", "YE", "XT"):
+            fl[b + C[f"LFDM24_T_{f}"]] = 1e-3
+        for f in ("OMEGA", "DOMEGA"):
+            fl[b + C[f"LFDM24_T_{f}"]] = 10.0
+        for f in ("FX", "FY", "FZ", "FXG", "FYG", "FZG", "MY", "ENGTOR"):
+            fl[b + C[f"LFDM24_T_{f}"]] = 1e3
+        s = C["LFDM24_S_SUS0"] + k * C["LFDM24_SUS_COUNT"]
+        for f in ("XS", "XSI", "LS", "LSI"):
+            fl[s + C[f"LFDM24_SUS_{f}"]] = 1e-3
+        for f in ("FXS", "FYS", "FZS", "FZD", "MX", "MY", "MZ"):
+            fl[s + C[f"LFDM24_SUS_{f}"]] = 1e3
+    return fl
+
+
+# time, x, y, u, v, phi, psi, theta, wx, wz, wy, four wheel speeds
+RESP24_FLOORS = np.array([1.0] * 11 + [10.0] * 4, dtype=np.float64)
+
+
+def case_inputs24(case):
+    """(Class18, params[P], state[S24], table[rows][4]) of a 24-DOF golden case."""
+    params = pkg_mod("params")
+    abi = pkg_mod("_abi")
+    cls, p = params.vehicle_from_json(case["vehicle"], case["tire"], case["tire_type"], model=24, sus=case["sus"])
+    for k, v in case["vp"].items():
+        p[abi.P[k.lower()]] = v
+    for k, v in case["tp"].items():
+        p[abi.P[k.lower()]] = v
+    if case["tp"]:
+        params.tire_init(p)
+    return cls, p, np.array(case["state"], dtype=np.float64), np.array(case["driver"], dtype=np.float64)

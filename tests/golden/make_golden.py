@@ -204,7 +204,82 @@ def main11(ref: str) -> None:
     print(f"wrote {len(cases)} 11-DOF cases; {cases[0]['name']} x={cases[0]['expected_final'][0]!r}")
 
 
+def main24(ref: str) -> None:
+    """golden24.json: the reference's 24-DOF CPU solver (oracle/refrun24.cpp) on HMMWV fixtures and on
+    seeded 24-DOF SUV vehicles. Case states are the states after Initialize (initializeTireSus)."""
+    refrun = os.path.join(ROOT, "oracle", "_ref", "refrun24")
+    d24 = os.path.join(ref, "24dof-gpu", "data")
+    veh = json.load(open(os.path.join(d24, "json", "HMMWV", "vehicle.json")))
+    tire = json.load(open(os.path.join(d24, "json", "HMMWV", "tmeasy.json")))
+    sus = json.load(open(os.path.join(d24, "json", "HMMWV", "suspension.json")))
+    C = abi.C
+    cases, jobs = [], []
+    with tempfile.TemporaryDirectory() as tmp:
+        def write(name, text):
+            p = os.path.join(tmp, name)
+            with open(p, "w") as f:
+                f.write(text)
+            return p
+
+        vj, tj, sj = write("v.json", json.dumps(veh)), write("t.json", json.dumps(tire)), write("s.json", json.dumps(sus))
+        _, p_h = lfdm.params.vehicle_from_json(veh, tire, 0, model=24, sus=sus)
+        s_h = fleet.init_tire_sus24(p_h[None], np.zeros((1, C["LFDM24_S_COUNT"])))[0]
+        for name, drv, ksim, tend in (("hmmwv24_acc3_cpu", "acc3", 0.0, None), ("hmmwv24_acc3_gpu22", "acc3", 2.0, 22.0),
+                                      ("hmmwv24_dl4_gpu22", "double_lane4", 2.0, 22.0)):
+            rows = lfdm.params.load_driver_table(os.path.join(d24, "input", drv + ".txt")).tolist()
+            tp = write(f"{name}.txt", "".join(" ".join(_fmt(v) for v in r) + "\n" for r in rows))
+            tend_v = tend if tend is not None else rows[-1][0]
+            jobs += [f"veh {vj}", f"tire {tj}", f"sus {sj}", f"driver {tp}", "dt 0.001", f"tend {_fmt(tend_v)}",
+                     f"ksim {_fmt(ksim)}", "sample 100", "run"]
+            cases.append({"name": name, "vehicle": veh, "tire": tire, "sus": sus, "tire_type": 0, "driver": rows,
+                          "dt": 0.001, "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
+                          "state": s_h.tolist(), "source": f"HMMWV 24-DOF json, {drv}.txt"})
+        fl = fleet.fleet24(8, seed=SEED, horizon=10.0)
+        svj, stj, ssj = (write("sv.json", json.dumps(fleet.SUV24_VEHICLE)), write("st.json", json.dumps(fleet.SUV_TIRE)),
+                         write("ss.json", json.dumps(fleet.SUV24_SUS)))
+        P = abi.P
+        key = {"fxmpn": "fxmPn", "fxmp2n": "fxmP2n", "fxspn": "fxsPn", "fxsp2n": "fxsP2n", "fympn": "fymPn",
+               "fymp2n": "fymP2n", "fyspn": "fysPn", "fysp2n": "fysP2n", "kt": "kt"}
+        for i in range(8):
+            rows = fl["tables"][i].tolist()
+            tp = write(f"s{i}.txt", "".join(" ".join(_fmt(v) for v in r) + "\n" for r in rows))
+            st = fl["states"][i]
+            vp = {k: float(fl["params"][i, P[k]]) for k in ("m", "jz", "a", "b")}
+            tpv = {key[k]: float(fl["params"][i, P[k]]) for k in ["kt"] + list(fleet.FRICTION_FIELDS)}
+            w0 = float(st[C["LFDM24_S_TIRE0"] + C["LFDM24_T_OMEGA"]])
+            jobs += [f"veh {svj}", f"tire {stj}", f"sus {ssj}", f"driver {tp}", "dt 0.001", "tend 10", "ksim 1",
+                     "sample 250"]
+            jobs += [f"vp {k} {_fmt(v)}" for k, v in vp.items()] + [f"tp {k} {_fmt(v)}" for k, v in tpv.items()]
+            jobs += [f"vs u {_fmt(st[C['LFDM24_S_U']])}", f"vs crankOmega {_fmt(st[C['LFDM24_S_CRANKOMEGA']])}",
+                     f"gear {int(st[C['LFDM24_S_CURRENT_GR']])}"] + [f"ts {k} omega {_fmt(w0)}" for k in range(4)]
+            jobs += ["run"]
+            cases.append({"name": f"suv24_{i}", "vehicle": fleet.SUV24_VEHICLE, "tire": fleet.SUV_TIRE,
+                          "sus": fleet.SUV24_SUS, "tire_type": 0, "driver": rows, "dt": 0.001, "tend": 10.0,
+                          "ksim": 1.0, "sample": 250, "vp": vp, "tp": tpv, "state": st.tolist(),
+                          "source": f"synthetic 24-DOF SUV fleet seed {SEED} vehicle {i}"})
+        out = subprocess.run([refrun], input="\n".join(jobs) + "\n", capture_output=True, text=True, check=True)
+    results, cur = [], {"samples": []}
+    for line in out.stdout.splitlines():
+        tok = line.split()
+        if tok and tok[0] == "S":
+            cur["samples"].append([int(tok[1])] + [float(v) for v in tok[2:]])
+        elif tok and tok[0] == "F":
+            cur["final"] = [float(v) for v in tok[1:]]
+        elif tok and tok[0] == "E":
+            results.append(cur)
+            cur = {"samples": []}
+    assert len(results) == len(cases)
+    for c, r in zip(cases, results):
+        assert len(r["final"]) == C["LFDM24_S_COUNT"]
+        c["expected_samples"] = r["samples"]
+        c["expected_final"] = r["final"]
+    with open(os.path.join(HERE, "golden24.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py", "model": 24, "cases": cases}, f, separators=(",", ":"))
+    print(f"wrote {len(cases)} 24-DOF cases; {cases[0]['name']} x={cases[0]['expected_final'][0]!r}")
+
+
 if __name__ == "__main__":
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/wheeled_vehicle_models"
     main(ref)
     main11(ref)
+    main24(ref)

@@ -37,6 +37,9 @@ def lib(fma: bool = False):
         L.oracle18_run.restype = ctypes.c_int
         L.oracle11_run.argtypes = [ctypes.c_void_p]
         L.oracle11_run.restype = ctypes.c_int
+        L.oracle24_run.argtypes = [ctypes.c_void_p]
+        L.oracle24_run.restype = ctypes.c_int
+        L.oracle24_init_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.oracle_map_y.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
         L.oracle_map_y.restype = ctypes.c_double
         L.oracle_driver_input.argtypes = [ctypes.c_double, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
@@ -69,7 +72,7 @@ def run18(classes, class_of, params, states, tables=None, ctl=None, *, tire_type
     """Advance `states` ([n][75] for 18-DOF, [n][42] for 11-DOF; copied) with the oracle. `tables` is
     a list of per-vehicle [rows][4] arrays or one [n][rows][4] array. schedule 0 = CPU solver,
     1 = GPU Solve, 2 = one SolveStep window. Returns (states, resp or None)."""
-    nch = 13 if model == 18 else 9
+    nch = {18: 13, 11: 9, 24: 15}[model]
     n = params.shape[0]
     cls_arr = (type(classes[0]) * len(classes))(*classes)
     class_of = np.ascontiguousarray(class_of, dtype=np.int32)
@@ -104,11 +107,19 @@ def run18(classes, class_of, params, states, tables=None, ctl=None, *, tire_type
               params=_ptr(params), states=_ptr(st), drv_rows=_ptr(rows), drv_off=_ptr(off), drv_len=_ptr(ln),
               ctl=_ptr(ctl_arr), dt=dt, t0=t0, tend=tend, ksim=ksim, schedule=schedule, dtout=dtout,
               resp=_ptr(resp), resp_samples=nsamp, samples_per_window=spw, nthreads=nthreads)
-    fn = lib(fma).oracle18_run if model == 18 else lib(fma).oracle11_run
+    fn = {18: lib(fma).oracle18_run, 11: lib(fma).oracle11_run, 24: lib(fma).oracle24_run}[model]
     rc = fn(ctypes.byref(a))
     if rc != 0:
         raise RuntimeError(f"oracle18_run failed rc={rc}")
     return st, resp
+
+
+def init_state24(params, state) -> np.ndarray:
+    """initializeTireSus applied to a copy of one flat 24-DOF state (what Initialize does)."""
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    st = np.array(state, dtype=np.float64, copy=True)
+    lib().oracle24_init_state(p.ctypes.data, st.ctypes.data)
+    return st
 
 
 def map_y(points, x) -> float:

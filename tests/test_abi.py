@@ -10,7 +10,7 @@ import tempfile
 import numpy as np
 import pytest
 
-from conftest import ROOT, case_inputs, pkg_mod
+from conftest import ROOT, TESTS, case_inputs, pkg_mod
 
 HEADER = os.path.join(ROOT, "include", "lfdm.h")
 
@@ -41,7 +41,7 @@ def test_struct_layout_matches_header(tmp_path):
     assert ctypes.sizeof(abi.Class18) == size
     assert abi.Class18.gearRatios.offset == off_g
     assert abi.Class18.TRmap.offset == off_tr
-    assert abi.P_COUNT == 64 and abi.S_COUNT == 75 and abi.RESP18 == 13
+    assert abi.P_COUNT == 67 and abi.S_COUNT == 75 and abi.RESP18 == 13
 
 
 def _write(tmp, name, obj):
@@ -68,6 +68,30 @@ def test_cpp_loader_matches_python_loader(built_lib, golden18):
             c_cls, c_p = built_lib.parse_vehicle18(vj, tj, 0)
             py_cls, py_p = params.vehicle_from_json(case["vehicle"], case["tire"], 0)
             assert np.array_equal(c_p, py_p)
+            assert bytes(c_cls) == bytes(py_cls)
+    assert len(seen) >= 2
+
+
+@pytest.mark.parametrize("model", [11, 24])
+def test_cpp_loader_matches_python_loader_11_24(built_lib, model):
+    """The library's 11- and 24-DOF loaders (tire doubling, jy, suspension file) against the Python
+    loader, on every distinct vehicle of the model's golden fixtures."""
+    params = pkg_mod("params")
+    with open(os.path.join(TESTS, "golden", f"golden{model}.json")) as f:
+        cases = json.load(f)["cases"]
+    seen = set()
+    with tempfile.TemporaryDirectory() as tmp:
+        for case in cases:
+            key = json.dumps([case["vehicle"], case["tire"], case.get("sus")], sort_keys=True)
+            if key in seen:
+                continue
+            seen.add(key)
+            vj = _write(tmp, "v.json", case["vehicle"])
+            tj = _write(tmp, "t.json", case["tire"])
+            sj = _write(tmp, "s.json", case["sus"]) if model == 24 else None
+            c_cls, c_p = built_lib.parse_vehicle(model, vj, tj, sj)
+            py_cls, py_p = params.vehicle_from_json(case["vehicle"], case["tire"], 0, model=model, sus=case.get("sus"))
+            assert np.array_equal(c_p, py_p), np.nonzero(c_p != py_p)
             assert bytes(c_cls) == bytes(py_cls)
     assert len(seen) >= 2
 
