@@ -17,11 +17,12 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import Class18, P, P_COUNT, S, S_COUNT, T, S_TIRE0, S_TIRE_STRIDE, RESP18, S11, S11_COUNT, S11_TIRE0, RESP11
+from ._abi import (Class18, P, P_COUNT, S, S_COUNT, T, S_TIRE0, S_TIRE_STRIDE, RESP18, S11, S11_COUNT, S11_TIRE0,
+                   RESP11, S24, S24_COUNT, RESP24)
 
 __all__ = ["lib", "LfdmError", "d18SolverHalfImplicitGPU", "d11SolverHalfImplicitGPU", "TireType", "Class18", "P",
            "S", "T", "S_COUNT", "P_COUNT", "RESP18", "S_TIRE0", "S_TIRE_STRIDE", "S11", "S11_COUNT", "S11_TIRE0",
-           "RESP11"]
+           "RESP11", "d24SolverHalfImplicitGPU", "S24", "S24_COUNT", "RESP24"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "liblfdm.so")
@@ -371,6 +372,25 @@ class d11SolverHalfImplicitGPU(_SolverGPU):
     MODEL = 11
     STATE_COUNT = S11_COUNT
     RESP_CHANNELS = RESP11
+
+
+class d24SolverHalfImplicitGPU(_SolverGPU):
+    """24-DOF batched half-implicit stepper on one GPU (reference: 24dof-gpu/dof24_halfImplicit_gpu.cuh).
+
+    States use the LFDM24_S_* layout (S24, 212 doubles): VehicleState, 4 TMeasyState, 4
+    SuspensionState. Construct takes the suspension JSON after the tire JSON, and Initialize applies
+    initializeTireSus with each vehicle's parameters, as the reference does; set_states copies raw
+    states. FP64, TMeasy tires."""
+
+    MODEL = 24
+    STATE_COUNT = S24_COUNT
+    RESP_CHANNELS = RESP24
+
+    def Construct(self, vehicle_params_file: str, tire_params_file: str, sus_params_file: str,  # noqa: N802
+                  num_vehicles: int, driver_inputs_file: str | None = None, type: int = TireType.TMeasy):  # noqa: A002
+        self._ck(self._L.lfdm_construct(self._h, vehicle_params_file.encode(), tire_params_file.encode(),
+                                        sus_params_file.encode(), int(num_vehicles),
+                                        driver_inputs_file.encode() if driver_inputs_file else None, int(type)))
 
 
 def measure_fp64_peak(device: int = 0) -> float:

@@ -48,6 +48,8 @@ S_TIRE_STRIDE = C["LFDM_S_TIRE_STRIDE"]
 S11_COUNT = C["LFDM11_S_COUNT"]
 S11_TIRE0 = C["LFDM11_S_TIRE0"]
 RESP11 = C["LFDM11_RESP_CHANNELS"]
+S24_COUNT = C["LFDM24_S_COUNT"]
+RESP24 = C["LFDM24_RESP_CHANNELS"]
 
 # name -> index maps, e.g. P["m"] == LFDM_P_M, S["x"] == LFDM_S_X, T["omega"] == LFDM_T_OMEGA
 P = {k[len("LFDM_P_"):].lower(): v for k, v in C.items() if k.startswith("LFDM_P_") and k != "LFDM_P_COUNT"}
@@ -56,6 +58,8 @@ S = {k[len("LFDM_S_"):].lower(): v for k, v in C.items() if k.startswith("LFDM_S
 T = {k[len("LFDM_T_"):].lower(): v for k, v in C.items() if k.startswith("LFDM_T_")}
 S11 = {k[len("LFDM11_S_"):].lower(): v for k, v in C.items() if k.startswith("LFDM11_S_") and k not in (
     "LFDM11_S_COUNT", "LFDM11_S_TIRE0")}
+S24 = {k[len("LFDM24_S_"):].lower(): v for k, v in C.items() if k.startswith("LFDM24_S_") and k not in (
+    "LFDM24_S_COUNT", "LFDM24_S_TIRE0", "LFDM24_S_SUS0")}
 
 TIRE_TMEASY = C["LFDM_TIRE_TMEASY"]
 TIRE_TMEASY_NR = C["LFDM_TIRE_TMEASY_NR"]

@@ -28,22 +28,25 @@ constexpr double kSqrt2Over2 = 0.70710678118654757;               // sqrt(2.)/2.
 // ---------------------------------------------------------------------------------------------
 // Per-vehicle derived constants (FP64), SoA [K18_COUNT][n_pad] in HBM, staged per block.
 enum K18 : int {
-    K_A = 0, K_B, K_CF2, K_CR2, K_MAXSTEER,
-    // computeTireLoads (dof18_gpu.cu:305-340)
-    K_Z1F, K_Z2F, K_Z3FK, K_Z3FB, K_Z4, K_Z1R, K_Z2R, K_Z3RK, K_Z3RB,
-    // computeVehRHS (dof18_gpu.cu:1017-1068)
-    K_MT, K_INVMT, K_E2WU, K_E3PHI, K_E3WX, K_E3WU, K_UWZ2, K_UWZWX,
-    K_CV1, K_CV2, K_CV3, K_CX2, K_CX3, K_CZ2,
-    // powertrain
-    K_INVCI, K_MAXBRAKE, K_INVJW,
+    // Shared prefix [0, KT_COUNT), also the head of the 24-DOF constants (K24 in dof24_device.cuh):
     // computeTireRHS (dof18_gpu.cu:379-530)
-    K_R0, K_INVKT, K_INVPN, K_PNMAX, K_FZRD, K_RDPN, K_DRD, K_RDCRIT,
+    K_R0 = 0, K_INVKT, K_INVPN, K_PNMAX, K_FZRD, K_RDPN, K_DRD, K_RDCRIT,
     K_Q1DFX0, K_Q2DFX0, K_Q1DFY0, K_Q2DFY0, K_Q1FXM, K_Q2FXM, K_Q1FYM, K_Q2FYM, K_Q1FXS, K_Q2FXS, K_Q1FYS,
     K_Q2FYS,
     K_LSXM, K_DSXM, K_LSYM, K_DSYM, K_LSXS, K_DSXS, K_LSYS, K_DSYS,
     K_CX, K_CY, K_DX, K_DY, K_FXMP2N, K_FYMP2N, K_RR,
     // TMeasyNr extras (dof18_gpu.cu:532-662)
     K_MU, K_VCOUL, K_FRB0, K_FRB1,
+    // powertrain and steering
+    K_INVCI, K_MAXBRAKE, K_INVJW, K_MAXSTEER,
+    KT_COUNT,
+    // 18-DOF (and 11-DOF) only
+    K_A = KT_COUNT, K_B, K_CF2, K_CR2,
+    // computeTireLoads (dof18_gpu.cu:305-340)
+    K_Z1F, K_Z2F, K_Z3FK, K_Z3FB, K_Z4, K_Z1R, K_Z2R, K_Z3RK, K_Z3RB,
+    // computeVehRHS (dof18_gpu.cu:1017-1068)
+    K_MT, K_INVMT, K_E2WU, K_E3PHI, K_E3WX, K_E3WU, K_UWZ2, K_UWZWX,
+    K_CV1, K_CV2, K_CV3, K_CX2, K_CX3, K_CZ2,
     // 11-DOF yaw (11dof-gpu/dof11_gpu.cu:893-909)
     K_INVJZ,
     K18_COUNT
@@ -121,6 +124,54 @@ __device__ __forceinline__ double sine_step(double x, double x1, double y1, doub
 
 __device__ __forceinline__ double sgnd(double v) { return (double)((0. < v) - (v < 0.)); }
 
+// The shared prefix [0, KT_COUNT) of the derived constants from one flat parameter vector p:
+// tire curve coefficients (InterpQ(fz,w1,w2,pn) = fzn*(Q1 - Q2*fzn), InterpL(fz,w1,w2,pn) =
+// w1 + (w2-w1)*(fzn-1) with fzn = fz/pn, utils_gpu.cuh:86-93), powertrain and steering constants.
+template <typename Put>
+__device__ __forceinline__ void prepare_shared_k(const double* p, Put& put) {
+    put(K_MAXSTEER, p[LFDM_P_MAXSTEER]);
+    put(K_INVCI, 1. / p[LFDM_P_CRANKINERTIA]);
+    put(K_MAXBRAKE, p[LFDM_P_MAXBRAKETORQUE]);
+    put(K_INVJW, 1 / p[LFDM_P_JW]);
+    put(K_R0, p[LFDM_P_R0]);
+    put(K_INVKT, 1. / p[LFDM_P_KT]);
+    put(K_INVPN, 1. / p[LFDM_P_PN]);
+    put(K_PNMAX, p[LFDM_P_PNMAX]);
+    put(K_FZRD, p[LFDM_P_FZRDYNCO]);
+    put(K_RDPN, p[LFDM_P_RDYNCOPN]);
+    put(K_DRD, p[LFDM_P_RDYNCOP2N] - p[LFDM_P_RDYNCOPN]);
+    put(K_RDCRIT, p[LFDM_P_RDYNCOCRIT]);
+    auto q = [&](int k1, int k2, double w1, double w2) {
+        put(k1, 2. * w1 - 0.5 * w2);
+        put(k2, w1 - 0.5 * w2);
+    };
+    q(K_Q1DFX0, K_Q2DFX0, p[LFDM_P_DFX0PN], p[LFDM_P_DFX0P2N]);
+    q(K_Q1DFY0, K_Q2DFY0, p[LFDM_P_DFY0PN], p[LFDM_P_DFY0P2N]);
+    q(K_Q1FXM, K_Q2FXM, p[LFDM_P_FXMPN], p[LFDM_P_FXMP2N]);
+    q(K_Q1FYM, K_Q2FYM, p[LFDM_P_FYMPN], p[LFDM_P_FYMP2N]);
+    q(K_Q1FXS, K_Q2FXS, p[LFDM_P_FXSPN], p[LFDM_P_FXSP2N]);
+    q(K_Q1FYS, K_Q2FYS, p[LFDM_P_FYSPN], p[LFDM_P_FYSP2N]);
+    auto l = [&](int k1, int k2, double w1, double w2) {
+        put(k1, w1);
+        put(k2, w2 - w1);
+    };
+    l(K_LSXM, K_DSXM, p[LFDM_P_SXMPN], p[LFDM_P_SXMP2N]);
+    l(K_LSYM, K_DSYM, p[LFDM_P_SYMPN], p[LFDM_P_SYMP2N]);
+    l(K_LSXS, K_DSXS, p[LFDM_P_SXSPN], p[LFDM_P_SXSP2N]);
+    l(K_LSYS, K_DSYS, p[LFDM_P_SYSPN], p[LFDM_P_SYSP2N]);
+    put(K_CX, p[LFDM_P_CX]);
+    put(K_CY, p[LFDM_P_CY]);
+    put(K_DX, p[LFDM_P_DX]);
+    put(K_DY, p[LFDM_P_DY]);
+    put(K_FXMP2N, p[LFDM_P_FXMP2N]);
+    put(K_FYMP2N, p[LFDM_P_FYMP2N]);
+    put(K_RR, p[LFDM_P_RR]);
+    put(K_MU, p[LFDM_P_MU]);
+    put(K_VCOUL, p[LFDM_P_VCOULOMB]);
+    put(K_FRB0, p[LFDM_P_FRBLEND_BEGIN]);
+    put(K_FRB1, p[LFDM_P_FRBLEND_END]);
+}
+
 // ---------------------------------------------------------------------------------------------
 // Carried state of one vehicle (registers).
 struct TireC {
@@ -189,34 +240,16 @@ __device__ __forceinline__ void tmxy(double& f, double& fos, double s, double df
     }
 }
 
-// computeTireRHS, TMeasy (dof18_gpu.cu:379-530). (c, s) = (cos, sin) of this tire's wheel angle;
-// steered says whether the angle may be nonzero. Writes xedot/yedot (left stale when the wheel is
-// off the ground, as in the reference) and the aux values.
+// The part of computeTireRHS, TMeasy (dof18_gpu.cu:379-530; 24dof-gpu/dof24_gpu.cu), that follows
+// the loaded and effective radii: slips, curve parameters, combined force, rolling resistance,
+// relaxation rates and the structural/dynamic blend. fz > 0 is the unclamped load, ta.rStat the
+// loaded radius. (c, s) = (cos, sin) of this tire's wheel angle; steered says whether the angle
+// may be nonzero.
 template <bool kSteered>
-__device__ __forceinline__ void tire_rhs_tm(TireC& ts, TireAux& ta, const KView& K, double c, double s) {
-    double fz = ta.fz;
-    const double vsy = ta.vsy;
-    if (fz <= 0) {
-        ts.xe = 0;
-        ts.ye = 0;
-        ts.omega = 0;
-        ta.xt = 0;
-        ta.rStat = K(K_R0);
-        ta.fx = 0;
-        ta.fy = 0;
-        ta.My = 0;
-        return;
-    }
+__device__ __forceinline__ void tire_core_tm(TireC& ts, TireAux& ta, const KView& K, double c, double s, double fz,
+                                             double r_eff) {
     const double omega = ts.omega;
-    ta.xt = fz * K(K_INVKT);
-    ta.rStat = K(K_R0) - ta.xt;
-    double r_eff;
-    if (fz <= K(K_FZRD)) {
-        double rdynco = fma(K(K_DRD), fma(fz, K(K_INVPN), -1.0), K(K_RDPN));
-        r_eff = fma(rdynco, ta.xt, ta.rStat);
-    } else {
-        r_eff = fma(K(K_RDCRIT), ta.xt, ta.rStat);
-    }
+    const double vsy = ta.vsy;
     const double vsx = fma(-omega, r_eff, ta.vsx);
     const double rw = r_eff * fabs(omega);
     const double vta = rw + 0.01;
@@ -294,6 +327,35 @@ __device__ __forceinline__ void tire_rhs_tm(TireC& ts, TireAux& ta, const KView&
     const double wy = sine_step(fabs(sy * vta), 1., 1., 1.5, 0.);
     ta.fx = (wx == 0.0) ? fxdyn : fma(wx, fxstr, (1. - wx) * fxdyn);
     ta.fy = (wy == 0.0) ? fydyn : fma(wy, fystr, (1. - wy) * fydyn);
+}
+
+// computeTireRHS, TMeasy (dof18_gpu.cu:379-530). (c, s) = (cos, sin) of this tire's wheel angle;
+// steered says whether the angle may be nonzero. Writes xedot/yedot (left stale when the wheel is
+// off the ground, as in the reference) and the aux values.
+template <bool kSteered>
+__device__ __forceinline__ void tire_rhs_tm(TireC& ts, TireAux& ta, const KView& K, double c, double s) {
+    const double fz = ta.fz;
+    if (fz <= 0) {
+        ts.xe = 0;
+        ts.ye = 0;
+        ts.omega = 0;
+        ta.xt = 0;
+        ta.rStat = K(K_R0);
+        ta.fx = 0;
+        ta.fy = 0;
+        ta.My = 0;
+        return;
+    }
+    ta.xt = fz * K(K_INVKT);
+    ta.rStat = K(K_R0) - ta.xt;
+    double r_eff;
+    if (fz <= K(K_FZRD)) {
+        double rdynco = fma(K(K_DRD), fma(fz, K(K_INVPN), -1.0), K(K_RDPN));
+        r_eff = fma(rdynco, ta.xt, ta.rStat);
+    } else {
+        r_eff = fma(K(K_RDCRIT), ta.xt, ta.rStat);
+    }
+    tire_core_tm<kSteered>(ts, ta, K, c, s, fz, r_eff);
 }
 
 // computeCombinedCoulombForce (dof18_gpu.cu:287-303)

@@ -59,6 +59,11 @@ cudaError_t launch_states_to_aos(const double* soa, int n, int ns, int npad, dou
 // 11-DOF window (same Window18 fields; states in the LFDM11_S_* layout, 9 response channels).
 cudaError_t launch_window11(const Window18& w, cudaStream_t stream);
 
+// 24-DOF window (states in the LFDM24_S_* layout, 15 response channels, K from launch_prepare24).
+cudaError_t launch_window24(const Window18& w, cudaStream_t stream);
+cudaError_t launch_prepare24(const double* params_dev, int n, int npad, double* K_dev, cudaStream_t stream);
+int k24_count();
+
 // Counts table rows whose time is smaller than the previous row's (per vehicle, equal-length tables
 // of nrows rows each; shared != 0: one table). *bad_dev must be zeroed by the caller.
 cudaError_t launch_check_tables(const double* rows, long long ntables, int nrows, unsigned* bad_dev,

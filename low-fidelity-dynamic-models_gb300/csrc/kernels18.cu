@@ -36,17 +36,17 @@ __global__ void prepare18_kernel(const double* __restrict__ P, int n, int npad, 
     if (i >= n) return;
     const double* p = P + (size_t)i * LFDM_P_COUNT;
     auto put = [&](int k, double v) { K[(size_t)k * npad + i] = v; };
+    prepare_shared_k(p, put);
     const double a = p[LFDM_P_A], b = p[LFDM_P_B], h = p[LFDM_P_H], m = p[LFDM_P_M];
     const double jz = p[LFDM_P_JZ], jx = p[LFDM_P_JX], jxz = p[LFDM_P_JXZ];
     const double cf = p[LFDM_P_CF], cr = p[LFDM_P_CR], muf = p[LFDM_P_MUF], mur = p[LFDM_P_MUR];
     const double hrcf = p[LFDM_P_HRCF], hrcr = p[LFDM_P_HRCR];
     const double krof = p[LFDM_P_KROF], kror = p[LFDM_P_KROR], brof = p[LFDM_P_BROF], bror = p[LFDM_P_BROR];
-    const double r0 = p[LFDM_P_R0], pn = p[LFDM_P_PN];
+    const double r0 = p[LFDM_P_R0];
     put(K_A, a);
     put(K_B, b);
     put(K_CF2, cf / 2.);
     put(K_CR2, cr / 2.);
-    put(K_MAXSTEER, p[LFDM_P_MAXSTEER]);
     // computeTireLoads (dof18_gpu.cu:305-340), huf = hur = r0
     const double huf = r0, hur = r0;
     put(K_Z1F, (m * kG * b) / (2. * (a + b)) + (muf * kG) / 2.);
@@ -79,48 +79,6 @@ __global__ void prepare18_kernel(const double* __restrict__ P, int n, int npad, 
     put(K_CX2, (jxz * mt - A1 * A3) / denom);
     put(K_CX3, (A1 * A1 - jz * mt) / denom);
     put(K_CZ2, (A3 * A3 - A2 * mt) / denom);
-    put(K_INVCI, 1. / p[LFDM_P_CRANKINERTIA]);
-    put(K_MAXBRAKE, p[LFDM_P_MAXBRAKETORQUE]);
-    put(K_INVJW, 1 / p[LFDM_P_JW]);
-    // computeTireRHS (dof18_gpu.cu:379-530); InterpQ(fz,w1,w2,pn) = fzn*(Q1 - Q2*fzn),
-    // InterpL(fz,w1,w2,pn) = w1 + (w2-w1)*(fzn-1) with fzn = fz/pn (utils_gpu.cuh:86-93)
-    put(K_R0, r0);
-    put(K_INVKT, 1. / p[LFDM_P_KT]);
-    put(K_INVPN, 1. / pn);
-    put(K_PNMAX, p[LFDM_P_PNMAX]);
-    put(K_FZRD, p[LFDM_P_FZRDYNCO]);
-    put(K_RDPN, p[LFDM_P_RDYNCOPN]);
-    put(K_DRD, p[LFDM_P_RDYNCOP2N] - p[LFDM_P_RDYNCOPN]);
-    put(K_RDCRIT, p[LFDM_P_RDYNCOCRIT]);
-    auto q = [&](int k1, int k2, double w1, double w2) {
-        put(k1, 2. * w1 - 0.5 * w2);
-        put(k2, w1 - 0.5 * w2);
-    };
-    q(K_Q1DFX0, K_Q2DFX0, p[LFDM_P_DFX0PN], p[LFDM_P_DFX0P2N]);
-    q(K_Q1DFY0, K_Q2DFY0, p[LFDM_P_DFY0PN], p[LFDM_P_DFY0P2N]);
-    q(K_Q1FXM, K_Q2FXM, p[LFDM_P_FXMPN], p[LFDM_P_FXMP2N]);
-    q(K_Q1FYM, K_Q2FYM, p[LFDM_P_FYMPN], p[LFDM_P_FYMP2N]);
-    q(K_Q1FXS, K_Q2FXS, p[LFDM_P_FXSPN], p[LFDM_P_FXSP2N]);
-    q(K_Q1FYS, K_Q2FYS, p[LFDM_P_FYSPN], p[LFDM_P_FYSP2N]);
-    auto l = [&](int k1, int k2, double w1, double w2) {
-        put(k1, w1);
-        put(k2, w2 - w1);
-    };
-    l(K_LSXM, K_DSXM, p[LFDM_P_SXMPN], p[LFDM_P_SXMP2N]);
-    l(K_LSYM, K_DSYM, p[LFDM_P_SYMPN], p[LFDM_P_SYMP2N]);
-    l(K_LSXS, K_DSXS, p[LFDM_P_SXSPN], p[LFDM_P_SXSP2N]);
-    l(K_LSYS, K_DSYS, p[LFDM_P_SYSPN], p[LFDM_P_SYSP2N]);
-    put(K_CX, p[LFDM_P_CX]);
-    put(K_CY, p[LFDM_P_CY]);
-    put(K_DX, p[LFDM_P_DX]);
-    put(K_DY, p[LFDM_P_DY]);
-    put(K_FXMP2N, p[LFDM_P_FXMP2N]);
-    put(K_FYMP2N, p[LFDM_P_FYMP2N]);
-    put(K_RR, p[LFDM_P_RR]);
-    put(K_MU, p[LFDM_P_MU]);
-    put(K_VCOUL, p[LFDM_P_VCOULOMB]);
-    put(K_FRB0, p[LFDM_P_FRBLEND_BEGIN]);
-    put(K_FRB1, p[LFDM_P_FRBLEND_END]);
     put(K_INVJZ, 1. / jz);
 }
 

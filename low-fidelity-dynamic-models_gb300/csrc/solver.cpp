@@ -167,6 +167,29 @@ void window_schedule(double t0, double ksim, double dt, double dtout, int spw, i
     nsteps = s;
 }
 
+// initializeTireSus (24dof-gpu/dof24_gpu.cu:34-90), which the reference's Initialize applies to
+// each vehicle's state (dof24_halfImplicit_gpu.cu:311-345): static tire loads and compressions,
+// spring preload and strut lengths from the vehicle's parameters p; unsprung vertical speed = w.
+void init_tire_sus24(const double* p, double* s) {
+    const double G = 9.81;  // utils/utils_gpu.cuh
+    const double a = p[LFDM_P_A], b = p[LFDM_P_B], m = p[LFDM_P_M], ks = p[LFDM_P_KS];
+    const double fz_f = (m * G * b) / (2 * (a + b)) + p[LFDM_P_MUF] * G;
+    const double fz_r = (m * G * a) / (2 * (a + b)) + p[LFDM_P_MUR] * G;
+    const double xsi_f = (m * G * b) / (2 * (a + b) * ks);
+    const double xsi_r = (m * G * a) / (2 * (a + b) * ks);
+    for (int c = 0; c < 4; ++c) {
+        double* t = s + LFDM24_S_TIRE0 + c * LFDM24_T_COUNT;
+        double* su = s + LFDM24_S_SUS0 + c * LFDM24_SUS_COUNT;
+        t[LFDM24_T_FZ] = c < 2 ? fz_f : fz_r;
+        t[LFDM24_T_XT] = t[LFDM24_T_FZ] / p[LFDM_P_KT];
+        su[LFDM24_SUS_XSI] = c < 2 ? xsi_f : xsi_r;
+        su[LFDM24_SUS_XS] = su[LFDM24_SUS_XSI];
+        su[LFDM24_SUS_LSI] = p[LFDM_P_H] - (p[LFDM_P_R0] - t[LFDM24_T_XT]);
+        su[LFDM24_SUS_LS] = su[LFDM24_SUS_LSI];
+        su[LFDM24_SUS_WU] = s[LFDM24_S_W];
+    }
+}
+
 int sync_device(lfdm_solver* h) {
     int rc = set_device(h);
     if (rc) return rc;
@@ -192,10 +215,11 @@ int sync_device(lfdm_solver* h) {
     }
     if (h->dirty_params) {
         CK(h->d_params.ensure(N * LFDM_P_COUNT));
-        CK(h->d_K.ensure((size_t)k18_count() * np));
+        CK(h->d_K.ensure((size_t)(h->model == LFDM_MODEL_24 ? k24_count() : k18_count()) * np));
         CK(cudaMemcpyAsync(h->d_params.p, h->params.data(), N * LFDM_P_COUNT * sizeof(double),
                            cudaMemcpyHostToDevice, h->stream));
-        CK(launch_prepare18(h->d_params.p, (int)N, h->npad, h->d_K.p, h->stream));
+        CK(h->model == LFDM_MODEL_24 ? launch_prepare24(h->d_params.p, (int)N, h->npad, h->d_K.p, h->stream)
+                                     : launch_prepare18(h->d_params.p, (int)N, h->npad, h->d_K.p, h->stream));
         h->dirty_params = false;
     }
     if (h->dirty_tables) {
@@ -270,7 +294,10 @@ void csv_header(lfdm_solver* h) {
     static const char* hdr18[] = {"time", "x", "y", "vx", "vy", "roll", "yaw", "roll_rate", "yaw_rate",
                                   "wlf", "wrf", "wlr", "wrr"};
     static const char* hdr11[] = {"time", "x", "y", "vx", "vy", "yaw", "yaw_rate", "wf", "wr"};
-    const char* const* hdr = h->model == LFDM_MODEL_11 ? hdr11 : hdr18;
+    // 24dof-gpu/dof24_halfImplicit_gpu.cu:608-622
+    static const char* hdr24[] = {"time",      "x",        "y",          "vx",  "vy",  "roll", "yaw", "pitch",
+                                  "roll_rate", "yaw_rate", "pitch_rate", "wlf", "wrf", "wlr",  "wrr"};
+    const char* const* hdr = h->model == LFDM_MODEL_11 ? hdr11 : h->model == LFDM_MODEL_24 ? hdr24 : hdr18;
     for (unsigned k = 0; k < h->num_outs; ++k) {
         auto& os = h->csv[k];
         for (int c = 0; c < h->nresp; ++c) os << hdr[c] << ",";
@@ -397,7 +424,9 @@ int run_windows(lfdm_solver* h, double t0, double t_end, bool solve_all, int ctl
         w.nsamples = dtout > 0 ? (int)samp.size() : 0;
         w.sample_steps = dtout > 0 ? h->d_samples.p + (size_t)b * (spw + 1) : nullptr;
         CK(cudaEventRecord(h->ev0, h->stream));
-        CK(h->model == LFDM_MODEL_11 ? launch_window11(w, h->stream) : launch_window18(w, h->stream));
+        CK(h->model == LFDM_MODEL_11   ? launch_window11(w, h->stream)
+           : h->model == LFDM_MODEL_24 ? launch_window24(w, h->stream)
+                                       : launch_window18(w, h->stream));
         CK(cudaEventRecord(h->ev1, h->stream));
         ++launches;
         if (stream_resp) {
@@ -458,8 +487,8 @@ int append_vehicles(lfdm_solver* h, const lfdm_class18& cls, const double* param
                        h->constructed, n, h->N);
     if (tire_type != LFDM_TIRE_TMEASY && tire_type != LFDM_TIRE_TMEASY_NR)
         return h->fail(LFDM_ERR_ARG, "unknown tire type %d", tire_type);
-    if (h->model == LFDM_MODEL_11 && tire_type != LFDM_TIRE_TMEASY)
-        return h->fail(LFDM_ERR_ARG, "the 11-DOF model has only the TMeasy tire");
+    if (h->model != LFDM_MODEL_18 && tire_type != LFDM_TIRE_TMEASY)
+        return h->fail(LFDM_ERR_ARG, "the %d-DOF model is built with the TMeasy tire only", h->model);
     if (h->tire_type >= 0 && h->tire_type != tire_type)
         return h->fail(LFDM_ERR_STATE, "all vehicles of a solver use one tire type");
     if (cls.noGears < 1 || cls.noGears > LFDM_MAX_GEARS) return h->fail(LFDM_ERR_ARG, "bad gear count %d", cls.noGears);
@@ -519,7 +548,7 @@ int lfdm_measure_fp64_peak(int device, double* dfma_per_s) {
 int lfdm_create_on_device(int model, unsigned total_num_vehicles, int device, lfdm_solver** out) {
     if (!out) return LFDM_ERR_ARG;
     *out = nullptr;
-    if (model != LFDM_MODEL_18 && model != LFDM_MODEL_11) {
+    if (model != LFDM_MODEL_18 && model != LFDM_MODEL_11 && model != LFDM_MODEL_24) {
         g_create_error = "model " + std::to_string(model) + " is not available in this build";
         return LFDM_ERR_ARG;
     }
@@ -542,6 +571,9 @@ int lfdm_create_on_device(int model, unsigned total_num_vehicles, int device, lf
     if (model == LFDM_MODEL_11) {
         h->ns = LFDM11_S_COUNT;
         h->nresp = LFDM11_RESP_CHANNELS;
+    } else if (model == LFDM_MODEL_24) {
+        h->ns = LFDM24_S_COUNT;
+        h->nresp = LFDM24_RESP_CHANNELS;
     }
     h->N = total_num_vehicles;
     h->device = device;
@@ -704,10 +736,16 @@ int lfdm_initialize(lfdm_solver* h, const double* state, unsigned num_vehicles) 
                        "Number of vehicles added makes the vehicle count greater than the total number of vehicles "
                        "(%u + %u > %u)",
                        h->initialized, num_vehicles, h->N);
+    if (h->model == LFDM_MODEL_24 && h->initialized + num_vehicles > h->constructed)
+        return h->fail(LFDM_ERR_STATE, "24-DOF vehicles must be constructed before Initialize (initializeTireSus "
+                                       "uses their parameters)");
     int rc = pull_states(h);
     if (rc) return rc;
-    for (unsigned k = 0; k < num_vehicles; ++k)
-        std::memcpy(&h->states[(size_t)(h->initialized + k) * h->ns], state, h->ns * sizeof(double));
+    for (unsigned k = 0; k < num_vehicles; ++k) {
+        double* dst = &h->states[(size_t)(h->initialized + k) * h->ns];
+        std::memcpy(dst, state, h->ns * sizeof(double));
+        if (h->model == LFDM_MODEL_24) init_tire_sus24(&h->params[(size_t)(h->initialized + k) * LFDM_P_COUNT], dst);
+    }
     h->initialized += num_vehicles;
     h->dirty_states = true;
     return LFDM_OK;

@@ -130,18 +130,20 @@ def case_inputs(case):
 def state_floors24():
     """Floors of the 24-DOF state vector (LFDM24_S_* layout): positions 1 m, speeds 1 m/s, angles
     1 rad, rates 1 rad/s, accelerations 1 m/s^2 (1 rad/s^2), wheel and crank speeds 10 rad/s, tire
-    deflections and compressions and spring compressions 1e-3 m, forces 1e3 N, moments 1e3 N m."""
+    deflections and compressions and spring compressions 1e-3 m, forces 1e3 N, moments 1e3 N m, wheel
+    and crank accelerations 1e3 rad/s^2 (differences of torques of order 1e3 N m over inertias of
+    order 1 kg m^2)."""
     abi = pkg_mod("_abi")
     C = abi.C
     fl = np.full(C["LFDM24_S_COUNT"], 1.0)
     fl[C["LFDM24_S_CRANKOMEGA"]] = 10.0
-    fl[C["LFDM24_S_DOMEGA_CRANK"]] = 10.0
+    fl[C["LFDM24_S_DOMEGA_CRANK"]] = 1e3
     for k in range(4):
         b = C["LFDM24_S_TIRE0"] + k * C["LFDM24_T_COUNT"]
         for f in ("XE", "YE", "XT"):
             fl[b + C[f"LFDM24_T_{f}"]] = 1e-3
-        for f in ("OMEGA", "DOMEGA"):
-            fl[b + C[f"LFDM24_T_{f}"]] = 10.0
+        fl[b + C["LFDM24_T_OMEGA"]] = 10.0
+        fl[b + C["LFDM24_T_DOMEGA"]] = 1e3
         for f in ("FX", "FY", "FZ", "FXG", "FYG", "FZG", "MY", "ENGTOR"):
             fl[b + C[f"LFDM24_T_{f}"]] = 1e3
         s = C["LFDM24_S_SUS0"] + k * C["LFDM24_SUS_COUNT"]
