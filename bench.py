@@ -33,6 +33,7 @@ sys.path.insert(0, ROOT)
 PKG = "low-fidelity-dynamic-models_gb300"
 SEED = 20261203
 W_ALG_18 = 1391  # FP64 source-level operations per 18-DOF vehicle-step of the reference algorithm
+W_ALG = {11: 675, 18: 1391, 24: 1941}  # the same count for the three models
 METRIC = "18-DOF vehicle-steps/s on 1 GB300: FP64 plain vs mixed at stated error; adjoint/fwd"
 
 
@@ -47,6 +48,7 @@ def _args():
     ap.add_argument("--threads", type=int, default=0, help="threads per block (0: library default)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-models", action="store_true", help="skip the 11/24-DOF throughput lines")
     ap.add_argument("--error-vehicles", type=int, default=65536)
     ap.add_argument("--error-horizon", type=float, default=20.0)
     ap.add_argument("--cpu-sample", type=int, default=8192, help="vehicles in the CPU-baseline sample")
@@ -218,6 +220,34 @@ def _mixed_error(lfdm, fleet, dev, n, horizon):
             "speed_mps": st(spd), "frac_position_within_1cm": float((pos <= 0.01).mean())}
 
 
+def _model_rate(lfdm, fleet, dev, model: int, n: int, windows: int, ksim: float, peak_tflops: float) -> dict:
+    """FP64 vehicle-steps/s of one model's window kernel on its seeded SUV fleet: `windows` timed
+    windows of ksim seconds after one warm-up window (device time, CUDA events)."""
+    gen = {11: fleet.fleet11, 18: fleet.fleet18, 24: fleet.fleet24}[model]
+    cls_ = {11: lfdm.d11SolverHalfImplicitGPU, 18: lfdm.d18SolverHalfImplicitGPU, 24: lfdm.d24SolverHalfImplicitGPU}
+    horizon = (windows + 1) * ksim
+    f = gen(n, seed=SEED + model, horizon=horizon)
+    sol = cls_[model](n, device=dev)
+    sol.construct_class(f["cls"][0], f["params"])
+    sol.set_driver_tables(f["tables"])
+    sol.set_states(f["states"])
+    sol.SetKernelSimTime(ksim)
+    sol.SetEndTime(horizon)
+    sol.solve_range(-0.5 * ksim, 0.5 * ksim)
+    sol.solve_range(0.5 * ksim, (windows + 0.5) * ksim)
+    ms, launches = sol.last_kernel_ms()
+    finite = bool(np.isfinite(sol.get_states()[:, :8]).all())
+    sol.close()
+    vsteps = n * int(round(ksim / 1e-3)) * windows
+    rate = vsteps / (ms * 1e-3)
+    achieved = W_ALG[model] * rate / 1e12
+    return {"model": f"{model}dof-tmeasy", "vehicles": n, "value": rate, "unit": "vehicle-steps/s",
+            "ms_per_window": ms / windows, "gpu_launches": launches, "finite_states": finite,
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",
+                         "frac": achieved / peak_tflops,
+                         "algorithmic": f"{W_ALG[model]} FP64 ops per vehicle-step (reference op count)"}}
+
+
 def run_ours(a, dist: Dist):
     import torch
 
@@ -330,6 +360,16 @@ def run_ours(a, dist: Dist):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
 
+    # the other two models: the 11-DOF small config (1,024 vehicles, 10 s) and 11/24-DOF at scale
+    models = None
+    if not a.no_models:
+        c0 = _model_rate(lfdm, fleet, dev, 11, 1024, 9, 1.0, peak)
+        c0["config"] = "11-DOF SUV, one parameter set, 1,024 vehicles, 10 s (1 warm-up + 9 timed 1 s windows)"
+        models = {"11dof_1024": c0,
+                  "11dof_scale": _model_rate(lfdm, fleet, dev, 11, n, 2, ksim, peak),
+                  "24dof_scale": _model_rate(lfdm, fleet, dev, 24, n, 2, ksim, peak)}
+        models["24dof_scale"]["config"] = "24-DOF SUV fleet (ks 4e4 N/m, bs 4e3 N s/m), jittered as the 18-DOF fleet"
+
     cpu = None
     if dist.rank == 0:
         cores = os.cpu_count() or 1
@@ -356,6 +396,7 @@ def run_ours(a, dist: Dist):
             "cpu_baseline": cpu,
             "e2e": e2e,
             "mixed": mixed,
+            "models": models,
             "gpu_launches": launches,
             "clocks": clocks,
             "wall_s_timed": wall,
