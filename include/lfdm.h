@@ -281,6 +281,49 @@ int lfdm_solve_step_schedule(lfdm_solver* h, double t, const double* ctl, unsign
 /* Step count and step start times of the window starting at t (times: [capacity] or NULL). */
 int lfdm_window_steps(lfdm_solver* h, double t, unsigned* nsteps, double* times, unsigned capacity);
 
+/* ------------------------------------------------------------------------------------------ */
+/* Mixed-DOF fleets (no counterpart class in the reference, whose solvers hold one model and one */
+/* end time each: d18SolverHalfImplicitGPU, d24SolverHalfImplicitGPU). A fleet holds 18-DOF and   */
+/* 24-DOF TMeasy vehicles of any number of parameter classes, each with its own end time, and      */
+/* steps them in one persistent launch (a CUDA graph of one or a few launches). Every vehicle gets */
+/* what the reference's Solve() computes for it with m_tend = its end time and the fleet's         */
+/* kernel_sim_time (dof18_halfImplicit_gpu.cu:404-494): same step times, steps and output samples. */
+typedef struct lfdm_fleet lfdm_fleet;
+int lfdm_fleet_create(int device, lfdm_fleet** out);
+int lfdm_fleet_destroy(lfdm_fleet* f);
+const char* lfdm_fleet_last_error(const lfdm_fleet* f);
+/* Appends n vehicles of one model (LFDM_MODEL_18 or LFDM_MODEL_24) and one class: params          */
+/* [n][LFDM_P_COUNT], states [n][model's state count], end times [n] (s), driver rows [nrows][4]   */
+/* with each vehicle's first row and row count (vehicles may share a table). With rows == NULL the */
+/* row offsets index the rows already added by lfdm_fleet_add_rows (tables shared across calls).   */
+int lfdm_fleet_add(lfdm_fleet* f, int model, const lfdm_class18* cls, unsigned n, const double* params,
+                   const double* states, const double* horizons, const double* rows, size_t nrows,
+                   const int64_t* row_off, const int32_t* row_len);
+/* Appends driver rows [nrows][4] shared by later lfdm_fleet_add calls; *first_row = their index. */
+int lfdm_fleet_add_rows(lfdm_fleet* f, const double* rows, size_t nrows, int64_t* first_row);
+int lfdm_fleet_set_time_step(lfdm_fleet* f, double dt);
+int lfdm_fleet_set_kernel_sim_time(lfdm_fleet* f, double ksim);
+/* Output interval of the device response buffers (0: none); samples as SetOutput's (:342-399). */
+int lfdm_fleet_set_output(lfdm_fleet* f, double dtout);
+/* Launch configuration: threads per block (32..128), resident blocks per SM (0: as many as fit)  */
+/* and steps per launch (0: the whole horizon in one launch).                                      */
+int lfdm_fleet_set_launch(lfdm_fleet* f, unsigned threads, unsigned blocks_per_sm, unsigned steps_per_launch);
+int lfdm_fleet_get_launch(lfdm_fleet* f, unsigned* threads, unsigned* blocks_per_sm, unsigned* steps_per_launch);
+/* Autotuner: times the candidate configurations on the first pilot_steps steps (states restored) */
+/* and keeps the fastest; *best_ms receives its pilot time.                                        */
+int lfdm_fleet_tune(lfdm_fleet* f, unsigned pilot_steps, double* best_ms);
+/* Steps every vehicle from its current state over its horizon. */
+int lfdm_fleet_solve(lfdm_fleet* f);
+int lfdm_fleet_last_ms(lfdm_fleet* f, double* ms, unsigned* launches);
+int lfdm_fleet_info(lfdm_fleet* f, unsigned* n18, unsigned* n24, long long* total_steps, double* vehicle_steps,
+                    unsigned* nsamples);
+/* States of one model's vehicles in the order they were added. */
+int lfdm_fleet_get_states(lfdm_fleet* f, int model, unsigned first, unsigned count, double* out);
+int lfdm_fleet_set_states(lfdm_fleet* f, int model, unsigned first, unsigned count, const double* states);
+/* Response of one model, [nsamples][channels][n] in add order (out NULL: only *nsamples). */
+int lfdm_fleet_get_response(lfdm_fleet* f, int model, double* out, size_t capacity, unsigned* nsamples);
+int lfdm_fleet_get_status_words(lfdm_fleet* f, int model, uint32_t* out);
+
 /* No counterpart in the reference (its solver owns and allocates all of its memory). One 18-DOF   */
 /* FP64 window of nsteps steps of dt from t0 over n <= LFDM_NOALLOC_MAX_VEHICLES device-resident    */
 /* vehicles of one class, with per-vehicle constant controls, that allocates nothing: its scratch  */

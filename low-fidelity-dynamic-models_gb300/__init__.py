@@ -22,7 +22,7 @@ from ._abi import (Class18, P, P_COUNT, S, S_COUNT, T, S_TIRE0, S_TIRE_STRIDE, R
 
 __all__ = ["lib", "LfdmError", "d18SolverHalfImplicitGPU", "d11SolverHalfImplicitGPU", "TireType", "Class18", "P",
            "S", "T", "S_COUNT", "P_COUNT", "RESP18", "S_TIRE0", "S_TIRE_STRIDE", "S11", "S11_COUNT", "S11_TIRE0",
-           "RESP11", "d24SolverHalfImplicitGPU", "S24", "S24_COUNT", "RESP24"]
+           "RESP11", "d24SolverHalfImplicitGPU", "S24", "S24_COUNT", "RESP24", "Fleet"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "liblfdm.so")
@@ -92,6 +92,25 @@ def _sig(lib):
         "lfdm_parse_vehicle": ([i, cp, cp, cp, i, vp, dp, ctypes.c_char_p, sz], i),
         "lfdm_load_driver_file": ([cp, dp, u, ctypes.POINTER(u), ctypes.c_char_p, sz], i),
         "lfdm_step18_noalloc": ([vp, i, vp, vp, vp, vp, vp, u, d, d, u, vp, ctypes.c_char_p, sz], i),
+        "lfdm_fleet_create": ([i, ctypes.POINTER(vp)], i),
+        "lfdm_fleet_destroy": ([vp], i),
+        "lfdm_fleet_last_error": ([vp], cp),
+        "lfdm_fleet_add": ([vp, i, vp, u, dp, dp, dp, dp, sz, vp, vp], i),
+        "lfdm_fleet_add_rows": ([vp, dp, sz, ctypes.POINTER(ctypes.c_int64)], i),
+        "lfdm_fleet_set_time_step": ([vp, d], i),
+        "lfdm_fleet_set_kernel_sim_time": ([vp, d], i),
+        "lfdm_fleet_set_output": ([vp, d], i),
+        "lfdm_fleet_set_launch": ([vp, u, u, u], i),
+        "lfdm_fleet_get_launch": ([vp, ctypes.POINTER(u), ctypes.POINTER(u), ctypes.POINTER(u)], i),
+        "lfdm_fleet_tune": ([vp, u, _c_dp], i),
+        "lfdm_fleet_solve": ([vp], i),
+        "lfdm_fleet_last_ms": ([vp, _c_dp, ctypes.POINTER(u)], i),
+        "lfdm_fleet_info": ([vp, ctypes.POINTER(u), ctypes.POINTER(u), ctypes.POINTER(ctypes.c_longlong), _c_dp,
+                             ctypes.POINTER(u)], i),
+        "lfdm_fleet_get_states": ([vp, i, u, u, dp], i),
+        "lfdm_fleet_set_states": ([vp, i, u, u, dp], i),
+        "lfdm_fleet_get_response": ([vp, i, dp, sz, ctypes.POINTER(u)], i),
+        "lfdm_fleet_get_status_words": ([vp, i, dp], i),
     }
     for name, (args, res) in table.items():
         f = getattr(lib, name)
@@ -400,6 +419,118 @@ def measure_fp64_peak(device: int = 0) -> float:
     if rc:
         raise LfdmError(rc, "FP64 peak probe failed")
     return v.value
+
+
+class Fleet:
+    """Mixed 18/24-DOF fleet with per-vehicle end times, stepped in one persistent launch captured in
+    a CUDA graph (lfdm_fleet_* in include/lfdm.h). Vehicles are added per (model, class) group with
+    numpy arrays; states and responses come back in add order per model."""
+
+    NCH = {18: RESP18, 24: RESP24}
+    NS = {18: S_COUNT, 24: S24_COUNT}
+
+    def __init__(self, device: int = 0, dt: float = 1e-3, kernel_sim_time: float = 1.0, output_dt: float = 0.0):
+        self._L = lib()
+        h = ctypes.c_void_p()
+        rc = self._L.lfdm_fleet_create(int(device), ctypes.byref(h))
+        if rc:
+            raise LfdmError(rc, self._L.lfdm_fleet_last_error(None).decode())
+        self._h = h
+        self.count = {18: 0, 24: 0}
+        self._ck(self._L.lfdm_fleet_set_time_step(h, float(dt)))
+        self._ck(self._L.lfdm_fleet_set_kernel_sim_time(h, float(kernel_sim_time)))
+        self._ck(self._L.lfdm_fleet_set_output(h, float(output_dt)))
+
+    def _ck(self, rc: int):
+        if rc:
+            raise LfdmError(rc, self._L.lfdm_fleet_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.lfdm_fleet_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_rows(self, rows: np.ndarray) -> int:
+        """Driver rows [nrows][4] shared by later add(..., rows=None) calls; returns their first index."""
+        r = _f64(rows).reshape(-1, 4)
+        first = ctypes.c_int64()
+        self._ck(self._L.lfdm_fleet_add_rows(self._h, _ptr(r), r.shape[0], ctypes.byref(first)))
+        return first.value
+
+    def add(self, model: int, cls: Class18, params: np.ndarray, states: np.ndarray, horizons: np.ndarray,
+            rows: np.ndarray | None, row_off: np.ndarray, row_len: np.ndarray):
+        """Append vehicles: params [n][P_COUNT], states [n][states of the model], horizons [n] end times
+        (s), driver rows [nrows][4] with per-vehicle first row and row count (rows None: row_off
+        indexes the rows given to add_rows)."""
+        if model not in self.NS:
+            raise LfdmError(_abi.C["LFDM_ERR_ARG"], f"the fleet holds 18-DOF and 24-DOF vehicles (model {model})")
+        p = _f64(params).reshape(-1, P_COUNT)
+        n = p.shape[0]
+        st = _f64(states).reshape(n, self.NS[model])
+        hz = _f64(horizons).reshape(n)
+        r = _f64(rows).reshape(-1, 4) if rows is not None else None
+        off = np.ascontiguousarray(row_off, dtype=np.int64).reshape(n)
+        ln = np.ascontiguousarray(row_len, dtype=np.int32).reshape(n)
+        self._ck(self._L.lfdm_fleet_add(self._h, int(model), ctypes.byref(cls), n, _ptr(p), _ptr(st), _ptr(hz),
+                                        _ptr(r), r.shape[0] if r is not None else 0, _ptr(off), _ptr(ln)))
+        self.count[model] += n
+
+    def set_launch(self, threads: int = 128, blocks_per_sm: int = 0, steps_per_launch: int = 0):
+        self._ck(self._L.lfdm_fleet_set_launch(self._h, int(threads), int(blocks_per_sm), int(steps_per_launch)))
+
+    def get_launch(self) -> tuple[int, int, int]:
+        a, b, c = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint()
+        self._ck(self._L.lfdm_fleet_get_launch(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def tune(self, pilot_steps: int = 500) -> float:
+        ms = ctypes.c_double()
+        self._ck(self._L.lfdm_fleet_tune(self._h, int(pilot_steps), ctypes.byref(ms)))
+        return ms.value
+
+    def solve(self):
+        self._ck(self._L.lfdm_fleet_solve(self._h))
+
+    def last_ms(self) -> tuple[float, int]:
+        ms, n = ctypes.c_double(), ctypes.c_uint()
+        self._ck(self._L.lfdm_fleet_last_ms(self._h, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
+    def info(self) -> dict:
+        a, b, s, v, k = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_longlong(), ctypes.c_double(), ctypes.c_uint()
+        self._ck(self._L.lfdm_fleet_info(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(s), ctypes.byref(v),
+                                         ctypes.byref(k)))
+        return {"n18": a.value, "n24": b.value, "total_steps": s.value, "vehicle_steps": v.value, "nsamples": k.value}
+
+    def get_states(self, model: int) -> np.ndarray:
+        out = np.zeros((self.count[model], self.NS[model]))
+        if out.size:
+            self._ck(self._L.lfdm_fleet_get_states(self._h, int(model), 0, out.shape[0], _ptr(out)))
+        return out
+
+    def set_states(self, model: int, states: np.ndarray):
+        st = _f64(states).reshape(self.count[model], self.NS[model])
+        self._ck(self._L.lfdm_fleet_set_states(self._h, int(model), 0, st.shape[0], _ptr(st)))
+
+    def get_response(self, model: int) -> np.ndarray:
+        k = ctypes.c_uint()
+        self._ck(self._L.lfdm_fleet_get_response(self._h, int(model), None, 0, ctypes.byref(k)))
+        out = np.zeros((k.value, self.NCH[model], self.count[model]))
+        if out.size:
+            self._ck(self._L.lfdm_fleet_get_response(self._h, int(model), _ptr(out), out.size, ctypes.byref(k)))
+        return out
+
+    def status_words(self, model: int) -> np.ndarray:
+        w = np.zeros(self.count[model], dtype=np.uint32)
+        if w.size:
+            self._ck(self._L.lfdm_fleet_get_status_words(self._h, int(model), _ptr(w)))
+        return w
 
 
 NOALLOC_MAX_VEHICLES = _abi.C["LFDM_NOALLOC_MAX_VEHICLES"]

@@ -57,8 +57,12 @@ def build(verbose: bool = False, force: bool = False, extra_nvcc: list[str] | No
     objs = []
     for src in cu:
         obj = os.path.join(OUT, os.path.basename(src) + ".o")
-        cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills",
-               "-c", src, "-o", obj, *(extra_nvcc or [])]
+        # --fmad=false: only the fma() calls written in the source fuse. Implicit contraction of a
+        # multiply and an add depends on the surrounding code (a product with a second use is not
+        # fused), so the same device function could round differently in the window kernels and in
+        # the fleet kernel; with it off, every kernel that runs a step computes it bit for bit alike.
+        cmd = [nvcc, *ARCH, "-O3", "--fmad=false", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas",
+               "-warn-spills", "-c", src, "-o", obj, *(extra_nvcc or [])]
         jobs.append((cmd, obj))
     for src in cpp:
         obj = os.path.join(OUT, os.path.basename(src) + ".o")

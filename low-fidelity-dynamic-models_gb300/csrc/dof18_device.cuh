@@ -190,6 +190,86 @@ struct VehAux {
     double wxdot, wzdot, dOmega_crank;
 };
 
+// The 18-DOF state of one vehicle from / to its SoA column S (S[field * np]).
+__device__ __forceinline__ void load_state18(const double* S, size_t np, VehC& v, VehAux& va, TireC* ts,
+                                             TireAux* ta) {
+    v.x = S[LFDM_S_X * np];
+    v.y = S[LFDM_S_Y * np];
+    v.u = S[LFDM_S_U * np];
+    v.v = S[LFDM_S_V * np];
+    v.psi = S[LFDM_S_PSI * np];
+    v.wz = S[LFDM_S_WZ * np];
+    v.phi = S[LFDM_S_PHI * np];
+    v.wx = S[LFDM_S_WX * np];
+    v.udot = S[LFDM_S_UDOT * np];
+    v.vdot = S[LFDM_S_VDOT * np];
+    v.crank = S[LFDM_S_CRANKOMEGA * np];
+    v.gear = (int)S[LFDM_S_CURRENT_GR * np];
+    va.wxdot = S[LFDM_S_WXDOT * np];
+    va.wzdot = S[LFDM_S_WZDOT * np];
+    va.dOmega_crank = S[LFDM_S_DOMEGA_CRANK * np];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const size_t b = (size_t)(LFDM_S_TIRE0 + k * LFDM_S_TIRE_STRIDE) * np;
+        ts[k].xe = S[b + LFDM_T_XE * np];
+        ts[k].ye = S[b + LFDM_T_YE * np];
+        ts[k].xedot = S[b + LFDM_T_XEDOT * np];
+        ts[k].yedot = S[b + LFDM_T_YEDOT * np];
+        ts[k].omega = S[b + LFDM_T_OMEGA * np];
+        ta[k].dOmega = S[b + LFDM_T_DOMEGA * np];
+        ta[k].xt = S[b + LFDM_T_XT * np];
+        ta[k].rStat = S[b + LFDM_T_RSTAT * np];
+        ta[k].fx = S[b + LFDM_T_FX * np];
+        ta[k].fy = S[b + LFDM_T_FY * np];
+        ta[k].fz = S[b + LFDM_T_FZ * np];
+        ta[k].vsx = S[b + LFDM_T_VSX * np];
+        ta[k].vsy = S[b + LFDM_T_VSY * np];
+        ta[k].My = S[b + LFDM_T_MY * np];
+        ta[k].engTor = S[b + LFDM_T_ENGTOR * np];
+    }
+}
+__device__ __forceinline__ void store_state18(double* S, size_t np, const VehC& v, const VehAux& va, const TireC* ts,
+                                              const TireAux* ta) {
+    S[LFDM_S_X * np] = v.x;
+    S[LFDM_S_Y * np] = v.y;
+    S[LFDM_S_U * np] = v.u;
+    S[LFDM_S_V * np] = v.v;
+    S[LFDM_S_PSI * np] = v.psi;
+    S[LFDM_S_WZ * np] = v.wz;
+    S[LFDM_S_PHI * np] = v.phi;
+    S[LFDM_S_WX * np] = v.wx;
+    S[LFDM_S_UDOT * np] = v.udot;
+    S[LFDM_S_VDOT * np] = v.vdot;
+    S[LFDM_S_WXDOT * np] = va.wxdot;
+    S[LFDM_S_WZDOT * np] = va.wzdot;
+    S[LFDM_S_CRANKOMEGA * np] = v.crank;
+    S[LFDM_S_DOMEGA_CRANK * np] = va.dOmega_crank;
+    S[LFDM_S_CURRENT_GR * np] = (double)v.gear;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const size_t b = (size_t)(LFDM_S_TIRE0 + k * LFDM_S_TIRE_STRIDE) * np;
+        S[b + LFDM_T_XE * np] = ts[k].xe;
+        S[b + LFDM_T_YE * np] = ts[k].ye;
+        S[b + LFDM_T_XEDOT * np] = ts[k].xedot;
+        S[b + LFDM_T_YEDOT * np] = ts[k].yedot;
+        S[b + LFDM_T_OMEGA * np] = ts[k].omega;
+        S[b + LFDM_T_DOMEGA * np] = ta[k].dOmega;
+        S[b + LFDM_T_XT * np] = ta[k].xt;
+        S[b + LFDM_T_RSTAT * np] = ta[k].rStat;
+        S[b + LFDM_T_FX * np] = ta[k].fx;
+        S[b + LFDM_T_FY * np] = ta[k].fy;
+        S[b + LFDM_T_FZ * np] = ta[k].fz;
+        S[b + LFDM_T_VSX * np] = ta[k].vsx;
+        S[b + LFDM_T_VSY * np] = ta[k].vsy;
+        S[b + LFDM_T_MY * np] = ta[k].My;
+        S[b + LFDM_T_ENGTOR * np] = ta[k].engTor;
+    }
+}
+__device__ __forceinline__ bool state18_finite(const VehC& v, const TireC* ts) {
+    return isfinite(v.x) && isfinite(v.y) && isfinite(v.u) && isfinite(v.v) && isfinite(v.psi) && isfinite(v.wz) &&
+           isfinite(ts[0].omega) && isfinite(ts[1].omega) && isfinite(ts[2].omega) && isfinite(ts[3].omega);
+}
+
 // Constant accessor: K(i) reads derived constant i of this thread's vehicle.
 struct KView {
     const double* base;  // base + i*stride

@@ -1,0 +1,174 @@
+// Mixed-DOF fleet kernel: one persistent launch steps a fleet of 18-DOF and 24-DOF vehicles with
+// different parameter classes and horizons.
+//
+// The reference solves one model, one end time and (per Construct) one parameter set per solver
+// (d18SolverHalfImplicitGPU / d24SolverHalfImplicitGPU, m_tend global), so an uneven fleet needs one
+// solver run per model and horizon group. Here the vehicles of each model are sorted by their step
+// count (longest first) and cut into tiles of 32 (one warp). The tiles of both models form one work
+// list ordered by estimated cost (steps x per-step cost of the model), largest first. A persistent
+// grid (SMs x resident blocks) pulls tiles from that list with one atomic per tile and runs each
+// tile's vehicles over the steps of this launch, keeping their state in registers, so long-horizon
+// vehicles start first and short ones fill the tail (longest-processing-time-first scheduling).
+//
+// Each vehicle follows exactly the reference's per-vehicle schedule: the step start times are the
+// ones the reference's Solve loop produces (windows of kernel_sim_time from t = 0, t restarting at
+// each window start; computed on the host in the same FP64 arithmetic), the vehicle runs the steps
+// of the windows that start before its own end time, and response samples are taken at the steps
+// the reference samples. A launch covers a contiguous range of global steps; the host may split a
+// horizon over several launches (steps per launch is a tuning knob). Per-warp shared memory holds
+// the tile's derived constants; class tables are read through L1.
+#include <cuda_runtime.h>
+
+#include "dof24_device.cuh"
+#include "fleet.h"
+#include "window_common.cuh"
+
+namespace lfdm {
+
+constexpr int kFleetKMax = (int)K18_COUNT > (int)K24_COUNT ? (int)K18_COUNT : (int)K24_COUNT;
+
+size_t fleet_smem_per_warp() { return (size_t)kFleetKMax * 32 * sizeof(double); }
+
+__device__ __forceinline__ void run_tile18(const FleetLaunch& L, const FleetTile& T, double* ks, int lane) {
+    const FleetModelDev& M = L.m18;
+    if (lane >= T.count) return;
+    const int i = T.first + lane;
+    const int nst = min(__ldg(M.nsteps + i), L.s_end);
+    if (nst <= L.s_begin) return;
+    const size_t np = (size_t)M.npad;
+#pragma unroll 4
+    for (int k = 0; k < K18_COUNT; ++k) ks[k * 32 + lane] = __ldg(M.K + (size_t)k * np + i);
+    const KView K{ks + lane, 32};
+    const ClassDev18& C = M.classes[__ldg(M.class_of + i)];
+    double* S = M.S + i;
+    VehC v;
+    VehAux va;
+    TireC ts[4];
+    TireAux ta[4];
+    load_state18(S, np, v, va, ts, ta);
+    DriverCursor cur;
+    driver_begin(cur, L.rows + 4 * __ldg(M.row_off + i), __ldg(M.row_len + i), __ldg(L.step_t + L.s_begin));
+    double steer, thr, brk;
+    for (int s = L.s_begin; s < nst; ++s) {
+        const double t = __ldg(L.step_t + s);
+        driver_at(cur, t, steer, thr, brk);
+        step18<false>(v, va, ts, ta, K, C, steer, thr, brk, L.dt);
+        const int k = __ldg(L.step_sample + s);
+        if (M.resp && k >= 0 && k < L.nsamples) {
+            double* r = M.resp + (size_t)k * LFDM18_RESP_CHANNELS * M.n + i;
+            const size_t n = (size_t)M.n;
+            r[0 * n] = t + L.dt;
+            r[1 * n] = v.x;
+            r[2 * n] = v.y;
+            r[3 * n] = v.u;
+            r[4 * n] = v.v;
+            r[5 * n] = v.phi;
+            r[6 * n] = v.psi;
+            r[7 * n] = v.wx;
+            r[8 * n] = v.wz;
+            r[9 * n] = ts[0].omega;
+            r[10 * n] = ts[1].omega;
+            r[11 * n] = ts[2].omega;
+            r[12 * n] = ts[3].omega;
+        }
+    }
+    store_state18(S, np, v, va, ts, ta);
+    if (!state18_finite(v, ts)) M.status[i] |= 1u;
+}
+
+__device__ __forceinline__ void run_tile24(const FleetLaunch& L, const FleetTile& T, double* ks, int lane) {
+    const FleetModelDev& M = L.m24;
+    if (lane >= T.count) return;
+    const int i = T.first + lane;
+    const int nst = min(__ldg(M.nsteps + i), L.s_end);
+    if (nst <= L.s_begin) return;
+    const size_t np = (size_t)M.npad;
+#pragma unroll 4
+    for (int k = 0; k < K24_COUNT; ++k) ks[k * 32 + lane] = __ldg(M.K + (size_t)k * np + i);
+    const KView K{ks + lane, 32};
+    const ClassDev18& C = M.classes[__ldg(M.class_of + i)];
+    double* S = M.S + i;
+    VehC v;
+    Veh24X vx;
+    VehAux va;
+    TireC ts[4];
+    TireAux ta[4];
+    Sus24C su[4];
+    Corner24K ck[4];
+    load_state24(S, np, v, vx, va, ts, ta, su, ck);
+    DriverCursor cur;
+    driver_begin(cur, L.rows + 4 * __ldg(M.row_off + i), __ldg(M.row_len + i), __ldg(L.step_t + L.s_begin));
+    double steer, thr, brk;
+    auto sample = [&](int s, double t) {
+        const int k = __ldg(L.step_sample + s);
+        if (M.resp && k >= 0 && k < L.nsamples) {
+            double* r = M.resp + (size_t)k * LFDM24_RESP_CHANNELS * M.n + i;
+            const size_t n = (size_t)M.n;
+            r[0 * n] = t + L.dt;
+            r[1 * n] = v.x;
+            r[2 * n] = v.y;
+            r[3 * n] = v.u;
+            r[4 * n] = v.v;
+            r[5 * n] = v.phi;
+            r[6 * n] = v.psi;
+            r[7 * n] = vx.theta;
+            r[8 * n] = v.wx;
+            r[9 * n] = v.wz;
+            r[10 * n] = vx.wy;
+            r[11 * n] = ts[0].omega;
+            r[12 * n] = ts[1].omega;
+            r[13 * n] = ts[2].omega;
+            r[14 * n] = ts[3].omega;
+        }
+    };
+    const int last = nst - 1;
+    for (int s = L.s_begin; s <= last; ++s) {
+        const double t = __ldg(L.step_t + s);
+        driver_at(cur, t, steer, thr, brk);
+        // the step that ends this launch's range for the vehicle also writes the values the
+        // reference leaves in its state structs (as the window kernel does for a window's last step)
+        step24(v, vx, va, ts, ta, su, ck, K, C, steer, thr, brk, L.dt, S, np, s == last);
+        sample(s, t);
+    }
+    store_state24(S, np, v, vx, va, ts, ta, su, C.tcbool);
+    if (!state24_finite(v, vx, ts)) M.status[i] |= 1u;
+}
+
+__global__ void __launch_bounds__(128) fleet_kernel(const FleetLaunch L) {
+    extern __shared__ __align__(16) double fleet_smem[];
+    const int lane = threadIdx.x & 31;
+    double* ks = fleet_smem + (size_t)(threadIdx.x >> 5) * kFleetKMax * 32;
+    for (;;) {
+        int tile = 0;
+        if (lane == 0) tile = atomicAdd(L.queue, 1);
+        tile = __shfl_sync(0xffffffffu, tile, 0);
+        if (tile >= L.ntiles) break;
+        const FleetTile T = L.tiles[tile];
+        if (T.nsteps_max > L.s_begin) {
+            if (T.model == LFDM_MODEL_24) run_tile24(L, T, ks, lane);
+            else run_tile18(L, T, ks, lane);
+        }
+        __syncwarp();
+    }
+}
+
+// Raises the kernel's dynamic shared-memory limit to what 4 warps per block need (every
+// configuration uses at most that); called before any launch or occupancy query, outside capture.
+cudaError_t fleet_kernel_setup() {
+    return cudaFuncSetAttribute(fleet_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(fleet_smem_per_warp() * 4));
+}
+
+cudaError_t fleet_occupancy(int threads, int* blocks_per_sm) {
+    const size_t smem = fleet_smem_per_warp() * (threads / 32);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fleet_kernel, threads, smem);
+}
+
+cudaError_t launch_fleet(const FleetLaunch& L, int blocks, int threads, cudaStream_t stream) {
+    if (threads <= 0 || threads > 128 || (threads & 31) || blocks <= 0) return cudaErrorInvalidValue;
+    const size_t smem = fleet_smem_per_warp() * (threads / 32);
+    fleet_kernel<<<blocks, threads, smem, stream>>>(L);
+    return cudaGetLastError();
+}
+
+}  // namespace lfdm

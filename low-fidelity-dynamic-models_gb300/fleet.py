@@ -232,3 +232,67 @@ def fleet24(n: int, seed: int = 20261203, horizon: float = 10.0, table_dt: float
     states = initial_states24(cls, params, rng, u0_range)
     return {"cls": [cls], "class_of": np.zeros(n, dtype=np.int32), "params": params, "tables": tables,
             "states": states, "seed": seed, "horizon": horizon}
+
+
+# Mixed-DOF fleet: four parameter classes around the SUV (mass 1,300 / 1,700 / 2,100 / 2,800 kg;
+# inertias and the tire's nominal load scaled with the mass so that the force curves keep their
+# shape relative to the load), 18-DOF and 24-DOF vehicles, log-uniform end times.
+CLASS_MASSES = (1300.0, 1700.0, 2100.0, 2800.0)
+
+
+def suv_tire(pn: float) -> dict:
+    """SUV_TIRE with the nominal load pn and the load-proportional entries scaled with it."""
+    t = dict(SUV_TIRE)
+    s = pn / _PN
+    for k in ("pn", "pnmax", "dfx0Pn", "dfx0P2n", "fxmPn", "fxmP2n", "fxsPn", "fxsP2n", "dfy0Pn", "dfy0P2n", "fymPn",
+              "fymP2n", "fysPn", "fysP2n"):
+        t[k] = SUV_TIRE[k] * s
+    return t
+
+
+def class_vehicle(model: int, mass: float) -> tuple[Class18, np.ndarray]:
+    """The SUV scaled to `mass` for the 18- or 24-DOF model."""
+    s = mass / SUV18_VEHICLE["m"]
+    base = SUV24_VEHICLE if model == 24 else SUV18_VEHICLE
+    veh = dict(base, m=mass, jz=base["jz"] * s, jx=base["jx"] * s)
+    if model == 24:
+        veh["jy"] = base["jy"] * s
+        return vehicle_from_json(veh, suv_tire(_PN * s), TIRE_TMEASY, model=24, sus=SUV24_SUS)
+    return vehicle_from_json(veh, suv_tire(_PN * s), TIRE_TMEASY)
+
+
+def mixed_fleet(n: int, seed: int = 20261203, frac24: float = 0.4, horizon_range=(2.0, 20.0), n_tables: int = 4096,
+                table_dt: float = 0.01, u0_range=(0.0, 20.0)) -> dict:
+    """The seeded mixed fleet: vehicles split 1 - frac24 : frac24 between the 18- and 24-DOF models,
+    spread evenly over the four mass classes, jittered +/-10% (mass, Jz, CG position, tire vertical
+    stiffness, peak friction), end times log-uniform in horizon_range, and driver tables drawn from
+    n_tables shared seeded tables (the 18-DOF families with a brake pulse) covering the longest
+    horizon. Returns dict(rows [nrows][4], groups=[dict(model, cls, params, states, horizons,
+    row_off, row_len, mass)])."""
+    rng = np.random.default_rng(seed)
+    hmax = float(horizon_range[1])
+    rows_per = int(round(hmax / table_dt)) + 1
+    tables = driver_tables(n_tables, rng, hmax, table_dt, SUV18_VEHICLE["maxSteer"], brake_pulse=True)
+    rows = tables.reshape(-1, 4)
+    n24 = int(round(n * frac24))
+    counts = {18: n - n24, 24: n24}
+    groups = []
+    lo, hi = np.log(horizon_range[0]), np.log(horizon_range[1])
+    for model in (18, 24):
+        m_total = counts[model]
+        for ci, mass in enumerate(CLASS_MASSES):
+            k = m_total // len(CLASS_MASSES) + (1 if ci < m_total % len(CLASS_MASSES) else 0)
+            if k == 0:
+                continue
+            cls, base = class_vehicle(model, mass)
+            params = jitter_params(base, k, rng)
+            if model == 24:
+                states = initial_states24(cls, params, rng, u0_range)
+            else:
+                states = initial_states(cls, params, rng, u0_range)
+            horizons = np.exp(rng.uniform(lo, hi, size=k))
+            tix = rng.integers(0, n_tables, size=k)
+            groups.append({"model": model, "cls": cls, "params": params, "states": states, "horizons": horizons,
+                           "row_off": (tix * rows_per).astype(np.int64),
+                           "row_len": np.full(k, rows_per, dtype=np.int32), "mass": mass})
+    return {"rows": rows, "groups": groups, "seed": seed}
