@@ -282,6 +282,26 @@ int lfdm_solve_step_schedule(lfdm_solver* h, double t, const double* ctl, unsign
 int lfdm_window_steps(lfdm_solver* h, double t, unsigned* nsteps, double* times, unsigned capacity);
 
 /* ------------------------------------------------------------------------------------------ */
+/* Differentiable 18-DOF rollout (no counterpart in the reference; its Sundials solver offers     */
+/* forward sensitivities for map parameters only, 18dof/dof18_sundials.h:42-49). nsteps FP64       */
+/* steps of dt from the solver's current states (unchanged) with per-step controls ctl            */
+/* [nsteps][3][N] = {steering, throttle, braking} (DEVICE pointers, row stride N); per vehicle      */
+/* loss[N] = sum over steps of e_lat^2 + e_head^2 + weight_u*|u_k|^2 on the state after each step, */
+/* e_lat = -(x - xr) sin(psir) + (y - yr) cos(psir), e_head = psi - psir, ref [nsteps][3][N] =    */
+/* {xr, yr, psir}. The forward stores a checkpoint every ckpt_every steps; the backward (same      */
+/* arguments) recomputes each segment and runs the hand-written adjoint of the step: grad_ctl      */
+/* [nsteps][3][N], grad_params [5][N] (mass, Jz, CG-to-front distance a with b held, tire friction */
+/* scale on fxmPn..fysP2n at scale 1, tire vertical stiffness kt), grad_state0 [31][N] or NULL     */
+/* (adjoint of x, y, u, v, psi, wz, phi, wx, udot, vdot, crank, then xe, ye, xedot, yedot, omega   */
+/* of the 4 tires, each block of 4). 18-DOF TMeasy, throttleMod off.                               */
+int lfdm_traj18_forward(lfdm_solver* h, const double* ctl, const double* ref, unsigned nsteps, double weight_u,
+                        unsigned ckpt_every, double* loss);
+int lfdm_traj18_backward(lfdm_solver* h, const double* ctl, const double* ref, unsigned nsteps, double weight_u,
+                         unsigned ckpt_every, double* grad_ctl, double* grad_params, double* grad_state0);
+/* CUDA-event times of the last forward and backward kernels. */
+int lfdm_traj18_last_ms(lfdm_solver* h, double* forward_ms, double* backward_ms);
+
+/* ------------------------------------------------------------------------------------------ */
 /* Mixed-DOF fleets (no counterpart class in the reference, whose solvers hold one model and one */
 /* end time each: d18SolverHalfImplicitGPU, d24SolverHalfImplicitGPU). A fleet holds 18-DOF and   */
 /* 24-DOF TMeasy vehicles of any number of parameter classes, each with its own end time, and      */

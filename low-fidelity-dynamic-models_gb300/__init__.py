@@ -22,7 +22,8 @@ from ._abi import (Class18, P, P_COUNT, S, S_COUNT, T, S_TIRE0, S_TIRE_STRIDE, R
 
 __all__ = ["lib", "LfdmError", "d18SolverHalfImplicitGPU", "d11SolverHalfImplicitGPU", "TireType", "Class18", "P",
            "S", "T", "S_COUNT", "P_COUNT", "RESP18", "S_TIRE0", "S_TIRE_STRIDE", "S11", "S11_COUNT", "S11_TIRE0",
-           "RESP11", "d24SolverHalfImplicitGPU", "S24", "S24_COUNT", "RESP24", "Fleet"]
+           "RESP11", "d24SolverHalfImplicitGPU", "S24", "S24_COUNT", "RESP24", "Fleet", "Rollout18",
+           "ROLLOUT_PARAMS"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "liblfdm.so")
@@ -92,6 +93,9 @@ def _sig(lib):
         "lfdm_parse_vehicle": ([i, cp, cp, cp, i, vp, dp, ctypes.c_char_p, sz], i),
         "lfdm_load_driver_file": ([cp, dp, u, ctypes.POINTER(u), ctypes.c_char_p, sz], i),
         "lfdm_step18_noalloc": ([vp, i, vp, vp, vp, vp, vp, u, d, d, u, vp, ctypes.c_char_p, sz], i),
+        "lfdm_traj18_forward": ([vp, vp, vp, u, d, u, vp], i),
+        "lfdm_traj18_backward": ([vp, vp, vp, u, d, u, vp, vp, vp], i),
+        "lfdm_traj18_last_ms": ([vp, _c_dp, _c_dp], i),
         "lfdm_fleet_create": ([i, ctypes.POINTER(vp)], i),
         "lfdm_fleet_destroy": ([vp], i),
         "lfdm_fleet_last_error": ([vp], cp),
@@ -531,6 +535,119 @@ class Fleet:
         if w.size:
             self._ck(self._L.lfdm_fleet_get_status_words(self._h, int(model), _ptr(w)))
         return w
+
+
+# Parameters of the differentiable rollout, in the order of grad_params / theta.
+ROLLOUT_PARAMS = ("m", "jz", "a", "friction_scale", "kt")
+_FRICTION = ("fxmpn", "fxmp2n", "fxspn", "fxsp2n", "fympn", "fymp2n", "fyspn", "fysp2n")
+
+
+class Rollout18:
+    """Differentiable rollout of a d18SolverHalfImplicitGPU's vehicles (lfdm_traj18_*): `nsteps` FP64
+    steps from the solver's current states with per-step controls, loss per vehicle = sum over steps
+    of the squared lateral and heading error to a reference path + weight_u |u|^2, gradients by the
+    hand-written adjoint with a checkpoint every `ckpt_every` steps.
+
+    `loss(controls, ref, theta)` is a torch autograd function of the controls [nsteps, 3, N] and of
+    theta [5, N], offsets of (mass, Jz, CG-to-front distance a with b held, tire friction scale
+    around 1, tire vertical stiffness) applied to the solver's parameters for the rollout."""
+
+    def __init__(self, solver: "d18SolverHalfImplicitGPU", nsteps: int, ckpt_every: int = 100,
+                 weight_u: float = 1e-3):
+        import torch  # noqa: F401  (the rollout works on CUDA tensors)
+        self.solver = solver
+        self.n = solver.n
+        self.nsteps = int(nsteps)
+        self.ckpt = int(ckpt_every)
+        self.weight_u = float(weight_u)
+        self._base = solver.get_params()
+        self._fwd_token = None
+
+    def _apply_theta(self, theta):
+        t = theta.detach().cpu().numpy() if theta is not None else None
+        if t is None or not t.any():
+            self.solver.set_params(self._base)
+            return
+        p = self._base.copy()
+        p[:, P["m"]] += t[0]
+        p[:, P["jz"]] += t[1]
+        p[:, P["a"]] += t[2]
+        for f in _FRICTION:
+            p[:, P[f]] *= 1.0 + t[3]
+        p[:, P["kt"]] += t[4]
+        self.solver.set_params(p)
+
+    def forward_raw(self, controls, ref, loss):
+        self.solver._ck(self.solver._L.lfdm_traj18_forward(
+            self.solver._h, ctypes.c_void_p(controls.data_ptr()), ctypes.c_void_p(ref.data_ptr()), self.nsteps,
+            self.weight_u, self.ckpt, ctypes.c_void_p(loss.data_ptr())))
+
+    def backward_raw(self, controls, ref, grad_ctl, grad_params, grad_state0=None):
+        self.solver._ck(self.solver._L.lfdm_traj18_backward(
+            self.solver._h, ctypes.c_void_p(controls.data_ptr()), ctypes.c_void_p(ref.data_ptr()), self.nsteps,
+            self.weight_u, self.ckpt, ctypes.c_void_p(grad_ctl.data_ptr()), ctypes.c_void_p(grad_params.data_ptr()),
+            ctypes.c_void_p(grad_state0.data_ptr()) if grad_state0 is not None else None))
+
+    def last_ms(self) -> tuple[float, float]:
+        f, b = ctypes.c_double(), ctypes.c_double()
+        self.solver._ck(self.solver._L.lfdm_traj18_last_ms(self.solver._h, ctypes.byref(f), ctypes.byref(b)))
+        return f.value, b.value
+
+    def loss(self, controls, ref, theta=None):
+        import torch
+        if theta is None:
+            theta = torch.zeros(5, self.n, dtype=torch.float64, device=controls.device)
+        return _rollout_fn()(controls, theta, ref, self)
+
+
+_ROLLOUT_FN = None
+
+
+def _rollout_fn():
+    """The torch.autograd.Function of Rollout18.loss (built on first use: torch is imported lazily)."""
+    global _ROLLOUT_FN
+    if _ROLLOUT_FN is not None:
+        return _ROLLOUT_FN.apply
+    import torch
+
+    class _Fn(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, controls, theta, ref, ro):
+            controls = controls.detach().contiguous()
+            ref = ref.detach().contiguous()
+            if controls.dtype != torch.float64 or controls.shape != (ro.nsteps, 3, ro.n):
+                raise ValueError(f"controls must be float64 [{ro.nsteps}, 3, {ro.n}]")
+            if ref.dtype != torch.float64 or ref.shape != (ro.nsteps, 3, ro.n):
+                raise ValueError(f"ref must be float64 [{ro.nsteps}, 3, {ro.n}]")
+            loss = torch.empty(ro.n, dtype=torch.float64, device=controls.device)
+            ro._apply_theta(theta)
+            ro.forward_raw(controls, ref, loss)
+            ro._fwd_token = object()
+            ctx.token = ro._fwd_token
+            ctx.ro = ro
+            ctx.save_for_backward(controls, theta, ref)
+            return loss
+
+        @staticmethod
+        def backward(ctx, gl):
+            controls, theta, ref = ctx.saved_tensors
+            ro = ctx.ro
+            ro._apply_theta(theta)
+            if ro._fwd_token is not ctx.token:  # another rollout ran since: rebuild the checkpoints
+                tmp = torch.empty(ro.n, dtype=torch.float64, device=controls.device)
+                ro.forward_raw(controls, ref, tmp)
+                ro._fwd_token = ctx.token
+            gctl = torch.empty_like(controls)
+            gp = torch.empty(5, ro.n, dtype=torch.float64, device=controls.device)
+            ro.backward_raw(controls, ref, gctl, gp)
+            # friction scale: the adjoint returns d loss / d scale at the current fields, i.e. per unit
+            # of (1 + theta3)
+            gp[3] = gp[3] / (1.0 + theta[3])
+            gl = gl.contiguous()
+            return gctl * gl[None, None, :], gp * gl[None, :], None, None
+
+    _ROLLOUT_FN = _Fn
+    return _ROLLOUT_FN.apply
 
 
 NOALLOC_MAX_VEHICLES = _abi.C["LFDM_NOALLOC_MAX_VEHICLES"]

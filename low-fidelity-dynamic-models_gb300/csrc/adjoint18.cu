@@ -1,0 +1,248 @@
+// Differentiable 18-DOF rollout: forward kernel (loss, checkpoints) and backward kernel (adjoint
+// through the half-implicit steps with checkpointing and per-segment recomputation).
+//
+// Rollout: nsteps steps of step18<false> from the solver's current states with per-step controls
+// ctl[k][3][n] = {steering, throttle, braking}. Loss per vehicle (after every step k):
+//   e_lat = -(x - xr) sin(psir) + (y - yr) cos(psir), e_head = psi - psir,
+//   L += e_lat^2 + e_head^2 + w (steering^2 + throttle^2 + braking^2),
+// with the reference path ref[k][3][n] = {xr, yr, psir} at the end of step k.
+// Backward: the forward stores the state every `ckpt` steps. The backward runs the segments last to
+// first: it recomputes the segment from its checkpoint with fwd18_tape (dof18_adjoint.cuh), storing
+// each step's tape in HBM, then sweeps the segment backwards with rev18, writing the control
+// gradients and accumulating the adjoints of the parameter-dependent constants; at the end those
+// are contracted with dK/dp (forward-mode dual numbers through the prepare formulas) for the
+// parameter gradients: mass, Jz, CG-to-front distance a (b held), tire friction scale (a common
+// factor on the peak and sliding forces fxmPn..fysP2n, derivative at scale 1), tire vertical
+// stiffness kt.
+#include <cuda_runtime.h>
+
+#include "adjoint18.h"
+#include "dof18_adjoint.cuh"
+
+namespace lfdm {
+
+constexpr int kCkptFields = 32;  // VehC (11 doubles + gear) and 4 x TireC (5 doubles)
+
+__device__ __forceinline__ void store_ckpt(double* P, size_t np, const VehC& v, const TireC* ts) {
+    const double vals[12] = {v.x, v.y, v.u, v.v, v.psi, v.wz, v.phi, v.wx, v.udot, v.vdot, v.crank, (double)v.gear};
+#pragma unroll
+    for (int f = 0; f < 12; ++f) P[f * np] = vals[f];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        P[(12 + 5 * k) * np] = ts[k].xe;
+        P[(13 + 5 * k) * np] = ts[k].ye;
+        P[(14 + 5 * k) * np] = ts[k].xedot;
+        P[(15 + 5 * k) * np] = ts[k].yedot;
+        P[(16 + 5 * k) * np] = ts[k].omega;
+    }
+}
+__device__ __forceinline__ void load_ckpt(const double* P, size_t np, VehC& v, TireC* ts) {
+    v.x = P[0];
+    v.y = P[1 * np];
+    v.u = P[2 * np];
+    v.v = P[3 * np];
+    v.psi = P[4 * np];
+    v.wz = P[5 * np];
+    v.phi = P[6 * np];
+    v.wx = P[7 * np];
+    v.udot = P[8 * np];
+    v.vdot = P[9 * np];
+    v.crank = P[10 * np];
+    v.gear = (int)P[11 * np];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        ts[k].xe = P[(12 + 5 * k) * np];
+        ts[k].ye = P[(13 + 5 * k) * np];
+        ts[k].xedot = P[(14 + 5 * k) * np];
+        ts[k].yedot = P[(15 + 5 * k) * np];
+        ts[k].omega = P[(16 + 5 * k) * np];
+    }
+}
+
+__device__ __forceinline__ double step_loss(const AdjLaunch& A, int k, int vid, double x, double y, double psi,
+                                            double st, double th, double br) {
+    const size_t nu = (size_t)A.n;
+    const double* R = A.ref + (size_t)k * 3 * nu + vid;
+    const double xr = __ldg(R), yr = __ldg(R + nu), pr = __ldg(R + 2 * nu);
+    double sr, cr;
+    sincos(pr, &sr, &cr);
+    const double el = fma(-(x - xr), sr, (y - yr) * cr);
+    const double eh = psi - pr;
+    return fma(el, el, eh * eh) + A.weight_u * fma(st, st, fma(th, th, br * br));
+}
+
+__global__ void __launch_bounds__(128) traj18_forward_kernel(const AdjLaunch A) {
+    const int vid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (vid >= A.n) return;
+    const size_t np = (size_t)A.npad;
+    const KView K{A.K + vid, A.npad};
+    const ClassDev18& C = A.classes[__ldg(A.class_of + vid)];
+    VehC v;
+    VehAux va;
+    TireC ts[4];
+    TireAux ta[4];
+    load_state18(A.S0 + vid, np, v, va, ts, ta);
+    const size_t nu = (size_t)A.n;
+    double loss = 0;
+    for (int k = 0; k < A.nsteps; ++k) {
+        if (k % A.ckpt == 0) store_ckpt(A.ckpts + (size_t)(k / A.ckpt) * kCkptFields * np + vid, np, v, ts);
+        const double* U = A.ctl + (size_t)k * 3 * nu + vid;
+        const double st = __ldg(U), th = __ldg(U + nu), br = __ldg(U + 2 * nu);
+        step18<false>(v, va, ts, ta, K, C, st, th, br, A.dt);
+        loss += step_loss(A, k, vid, v.x, v.y, v.psi, st, th, br);
+    }
+    A.loss[vid] = loss;
+}
+
+// dual number for the parameter derivatives of the derived constants
+struct Dual {
+    double v, d;
+};
+__device__ __forceinline__ Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+__device__ __forceinline__ Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+__device__ __forceinline__ Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+__device__ __forceinline__ Dual operator/(Dual a, Dual b) { return {a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)}; }
+__device__ __forceinline__ Dual cst(double v) { return {v, 0.0}; }
+
+// d K_kb / d parameter `which` (0 m, 1 jz, 2 a with b held, 3 friction scale, 4 kt) for the
+// constants with an adjoint (the prepare formulas of prepare18_kernel and prepare_shared_k).
+__device__ void dK_dparam(const double* p, int which, double* out) {
+    const Dual G = cst(kG);
+    const Dual m = {p[LFDM_P_M], which == 0 ? 1.0 : 0.0};
+    const Dual jz = {p[LFDM_P_JZ], which == 1 ? 1.0 : 0.0};
+    const Dual a = {p[LFDM_P_A], which == 2 ? 1.0 : 0.0};
+    const Dual b = cst(p[LFDM_P_B]), h = cst(p[LFDM_P_H]), jx = cst(p[LFDM_P_JX]), jxz = cst(p[LFDM_P_JXZ]);
+    const Dual cf = cst(p[LFDM_P_CF]), cr = cst(p[LFDM_P_CR]), muf = cst(p[LFDM_P_MUF]), mur = cst(p[LFDM_P_MUR]);
+    const Dual hrcf = cst(p[LFDM_P_HRCF]), hrcr = cst(p[LFDM_P_HRCR]);
+    const Dual kr = cst(p[LFDM_P_KROF] + p[LFDM_P_KROR]);
+    const Dual r0 = cst(p[LFDM_P_R0]);
+    const Dual two = cst(2.0), half = cst(0.5);
+    auto fr = [&](int idx) { return Dual{p[idx], which == 3 ? p[idx] : 0.0}; };  // friction-scaled field
+    const Dual kt = {p[LFDM_P_KT], which == 4 ? 1.0 : 0.0};
+    const Dual ab = a + b;
+    const Dual huf = r0, hur = r0;
+    out[KB_Z1F] = (m * G * b / (two * ab) + muf * G / two).d;
+    out[KB_Z2F] = (muf * huf / cf + m * b * (h - hrcf) / (cf * ab)).d;
+    out[KB_Z4] = ((m * h + muf * huf + mur * hur) / (two * ab)).d;
+    out[KB_Z1R] = (m * G * a / (two * ab) + mur * G / two).d;
+    out[KB_Z2R] = (mur * hur / cr + m * a * (h - hrcr) / (cr * ab)).d;
+    const Dual mt = m + two * (muf + mur);
+    const Dual hrc = (hrcf * b + hrcr * a) / ab;
+    const Dual A1 = mur * b - muf * a;
+    const Dual A2 = jx + m * hrc * hrc;
+    const Dual A3 = hrc * m;
+    const Dual den = A2 * A1 * A1 - two * A1 * A3 * jxz + jz * A3 * A3 + mt * jxz * jxz - A2 * jz * mt;
+    out[KB_MT] = mt.d;
+    out[KB_INVMT] = (cst(1.0) / mt).d;
+    out[KB_E2WU] = (cst(0.0) - muf * a + mur * b).d;
+    out[KB_E3PHI] = (m * G * hrc - kr).d;
+    out[KB_E3WU] = (hrc * m).d;
+    out[KB_UWZ2] = (cst(0.0) - mur * b + muf * a).d;
+    out[KB_UWZWX] = (two * hrc * m).d;
+    out[KB_CV1] = ((jxz * jxz - A2 * jz) / den).d;
+    out[KB_CV2] = ((A3 * jxz - A1 * A2) / den).d;
+    out[KB_CV3] = ((A1 * jxz - A3 * jz) / den).d;
+    out[KB_CX2] = ((jxz * mt - A1 * A3) / den).d;
+    out[KB_CX3] = ((A1 * A1 - jz * mt) / den).d;
+    out[KB_CZ2] = ((A3 * A3 - A2 * mt) / den).d;
+    out[KB_A] = a.d;
+    auto q1 = [&](int i1, int i2) { return (two * fr(i1) - half * fr(i2)).d; };
+    auto q2 = [&](int i1, int i2) { return (fr(i1) - half * fr(i2)).d; };
+    out[KB_Q1FXM] = q1(LFDM_P_FXMPN, LFDM_P_FXMP2N);
+    out[KB_Q2FXM] = q2(LFDM_P_FXMPN, LFDM_P_FXMP2N);
+    out[KB_Q1FYM] = q1(LFDM_P_FYMPN, LFDM_P_FYMP2N);
+    out[KB_Q2FYM] = q2(LFDM_P_FYMPN, LFDM_P_FYMP2N);
+    out[KB_Q1FXS] = q1(LFDM_P_FXSPN, LFDM_P_FXSP2N);
+    out[KB_Q2FXS] = q2(LFDM_P_FXSPN, LFDM_P_FXSP2N);
+    out[KB_Q1FYS] = q1(LFDM_P_FYSPN, LFDM_P_FYSP2N);
+    out[KB_Q2FYS] = q2(LFDM_P_FYSPN, LFDM_P_FYSP2N);
+    out[KB_FXMP2N] = fr(LFDM_P_FXMP2N).d;
+    out[KB_FYMP2N] = fr(LFDM_P_FYMP2N).d;
+    out[KB_INVKT] = (cst(1.0) / kt).d;
+}
+
+__global__ void __launch_bounds__(128) traj18_backward_kernel(const AdjLaunch A) {
+    const int vid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (vid >= A.n) return;
+    const size_t np = (size_t)A.npad, nu = (size_t)A.n;
+    const KView K{A.K + vid, A.npad};
+    const ClassDev18& C = A.classes[__ldg(A.class_of + vid)];
+    const KBar kb{A.kbar + vid, A.npad};
+#pragma unroll 1
+    for (int i = 0; i < KB_COUNT; ++i) kb.base[i * (size_t)A.npad] = 0.0;
+    Adj18 L = {};
+    const int nseg = (A.nsteps + A.ckpt - 1) / A.ckpt;
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+        const int k0 = seg * A.ckpt, k1 = min(A.nsteps, k0 + A.ckpt);
+        VehC v;
+        VehAux va = {};
+        TireC ts[4];
+        TireAux ta[4] = {};
+        load_ckpt(A.ckpts + (size_t)seg * kCkptFields * np + vid, np, v, ts);
+        for (int k = k0; k < k1; ++k) {
+            const double* U = A.ctl + (size_t)k * 3 * nu + vid;
+            StepTape T;
+            fwd18_tape(v, va, ts, ta, T, K, C, __ldg(U), __ldg(U + nu), __ldg(U + 2 * nu), A.dt);
+            const double* tp = reinterpret_cast<const double*>(&T);
+            double* dst = A.tape + (size_t)(k - k0) * kStepTapeDoubles * np + vid;
+#pragma unroll 8
+            for (int f = 0; f < kStepTapeDoubles; ++f) dst[f * np] = tp[f];
+        }
+        for (int k = k1 - 1; k >= k0; --k) {
+            StepTape T;
+            double* tp = reinterpret_cast<double*>(&T);
+            const double* src = A.tape + (size_t)(k - k0) * kStepTapeDoubles * np + vid;
+#pragma unroll 8
+            for (int f = 0; f < kStepTapeDoubles; ++f) tp[f] = src[f * np];
+            // loss of step k on the state after it
+            {
+                const double* R = A.ref + (size_t)k * 3 * nu + vid;
+                const double xr = __ldg(R), yr = __ldg(R + nu), pr = __ldg(R + 2 * nu);
+                double sr, cr;
+                sincos(pr, &sr, &cr);
+                const double el = fma(-(T.x1 - xr), sr, (T.y1 - yr) * cr);
+                L.x += -2.0 * el * sr;
+                L.y += 2.0 * el * cr;
+                L.psi += 2.0 * (T.psi1 - pr);
+            }
+            double sb = 2.0 * A.weight_u * T.steer, tb = 2.0 * A.weight_u * T.thr, bb = 2.0 * A.weight_u * T.brk;
+            rev18(T, K, C, kb, A.dt, L, sb, tb, bb);
+            double* G = A.grad_ctl + (size_t)k * 3 * nu + vid;
+            G[0] = sb;
+            G[nu] = tb;
+            G[2 * nu] = bb;
+        }
+    }
+    if (A.grad_state0) {
+        const double* l = &L.x;
+#pragma unroll 1
+        for (int f = 0; f < kAdj18Count; ++f) A.grad_state0[f * nu + vid] = l[f];
+    }
+    // parameter gradients
+    const double* p = A.params + (size_t)vid * LFDM_P_COUNT;
+#pragma unroll 1
+    for (int j = 0; j < 5; ++j) {
+        double d[KB_COUNT];
+        dK_dparam(p, j, d);
+        double gsum = 0;
+#pragma unroll 1
+        for (int i = 0; i < KB_COUNT; ++i) gsum = fma(kb.base[i * (size_t)A.npad], d[i], gsum);
+        A.grad_params[j * nu + vid] = gsum;
+    }
+}
+
+cudaError_t launch_traj18_forward(const AdjLaunch& A, cudaStream_t stream) {
+    if (A.n <= 0 || A.nsteps <= 0) return cudaSuccess;
+    traj18_forward_kernel<<<(A.n + 127) / 128, 128, 0, stream>>>(A);
+    return cudaGetLastError();
+}
+cudaError_t launch_traj18_backward(const AdjLaunch& A, cudaStream_t stream) {
+    if (A.n <= 0 || A.nsteps <= 0) return cudaSuccess;
+    traj18_backward_kernel<<<(A.n + 127) / 128, 128, 0, stream>>>(A);
+    return cudaGetLastError();
+}
+size_t traj18_tape_doubles_per_step() { return (size_t)kStepTapeDoubles; }
+int traj18_ckpt_fields() { return kCkptFields; }
+int traj18_state_adjoints() { return kAdj18Count; }
+
+}  // namespace lfdm

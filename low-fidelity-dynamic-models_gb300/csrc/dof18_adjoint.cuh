@@ -1,0 +1,1056 @@
+// Hand-written adjoint (reverse mode) of one 18-DOF TMeasy half-implicit step.
+//
+// fwd18_tape() runs the same arithmetic as step18<false> (dof18_device.cuh; reference rhsFun
+// 18dof-gpu/dof18_halfImplicit_gpu.cu:685-729 and the update :913-946) and records on a tape
+// the intermediates the reverse sweep needs; rev18() propagates the adjoint of the state after the
+// step back to the state before it, to the step's controls and to the derived constants that
+// depend on the differentiable parameters (mass, Jz, CG-to-front distance a, tire peak/sliding
+// friction scale, tire vertical stiffness). The tape is written to HBM by a segment's forward
+// recomputation and read back by its reverse sweep, so each step's forward arithmetic runs twice
+// in total (rollout and recomputation) and the reverse sweep does not recompute it.
+//
+// Branches (wheel lift-off, tmxy_combined regimes, clamps, sineStep bands, converter flow
+// direction, differential bias band, gear shifts, map segments) are differentiated on the branch
+// the forward step took; the gear is piecewise constant and carries no adjoint. Supported: TMeasy
+// tires, linear or mapped steering, with or without torque converter, throttleMod off.
+#pragma once
+
+#include "dof18_device.cuh"
+
+namespace lfdm {
+
+// Derived constants that depend on the differentiable parameters; their adjoints are accumulated
+// per vehicle and contracted with dK/dp at the end of the backward pass.
+enum KB : int {
+    KB_Z1F = 0, KB_Z2F, KB_Z4, KB_Z1R, KB_Z2R, KB_MT, KB_INVMT, KB_E2WU, KB_E3PHI, KB_E3WU, KB_UWZ2, KB_UWZWX,
+    KB_CV1, KB_CV2, KB_CV3, KB_CX2, KB_CX3, KB_CZ2, KB_A,
+    KB_Q1FXM, KB_Q2FXM, KB_Q1FYM, KB_Q2FYM, KB_Q1FXS, KB_Q2FXS, KB_Q1FYS, KB_Q2FYS, KB_FXMP2N, KB_FYMP2N,
+    KB_INVKT,
+    KB_COUNT
+};
+// The K18 index of each KB entry.
+__device__ __forceinline__ int kb_to_k(int i) {
+    switch (i) {
+        case KB_Z1F: return K_Z1F;
+        case KB_Z2F: return K_Z2F;
+        case KB_Z4: return K_Z4;
+        case KB_Z1R: return K_Z1R;
+        case KB_Z2R: return K_Z2R;
+        case KB_MT: return K_MT;
+        case KB_INVMT: return K_INVMT;
+        case KB_E2WU: return K_E2WU;
+        case KB_E3PHI: return K_E3PHI;
+        case KB_E3WU: return K_E3WU;
+        case KB_UWZ2: return K_UWZ2;
+        case KB_UWZWX: return K_UWZWX;
+        case KB_CV1: return K_CV1;
+        case KB_CV2: return K_CV2;
+        case KB_CV3: return K_CV3;
+        case KB_CX2: return K_CX2;
+        case KB_CX3: return K_CX3;
+        case KB_CZ2: return K_CZ2;
+        case KB_A: return K_A;
+        case KB_Q1FXM: return K_Q1FXM;
+        case KB_Q2FXM: return K_Q2FXM;
+        case KB_Q1FYM: return K_Q1FYM;
+        case KB_Q2FYM: return K_Q2FYM;
+        case KB_Q1FXS: return K_Q1FXS;
+        case KB_Q2FXS: return K_Q2FXS;
+        case KB_Q1FYS: return K_Q1FYS;
+        case KB_Q2FYS: return K_Q2FYS;
+        case KB_FXMP2N: return K_FXMP2N;
+        case KB_FYMP2N: return K_FYMP2N;
+        default: return K_INVKT;
+    }
+}
+
+// Accumulator of the constant adjoints (strided per-vehicle column).
+struct KBar {
+    double* base;
+    int stride;
+    __device__ __forceinline__ void add(int i, double v) const { base[i * stride] += v; }
+};
+
+// The differentiable state of one vehicle (the carried state of step18 minus the gear).
+struct Adj18 {
+    double x, y, u, v, psi, wz, phi, wx, udot, vdot, crank;
+    double xe[4], ye[4], xedot[4], yedot[4], om[4];
+};
+constexpr int kAdj18Count = 31;
+
+// Per-tire tape of one step.
+struct TireTape {
+    double on;                       // 1: wheel on the ground (fz > 0)
+    double fz, xt, rStat, r_eff, rdynco, fzrd;  // fzrd: 1 when fz <= fzRdynco (rdynco interpolated)
+    double om, xe, ye, vsx, vsy, rw, vta, sx, sy, N, D;  // N, D: the steered sy = -N / D
+    double fzc, fzcl, fzn;           // fzcl: 1 when fz was limited to pnmax
+    double dfx0, dfy0, fxm, fym, fxs, fys, sxm, sym, sxs, sys;
+    double ssum, fsum, fxd, fyd, hsxn, hsyn, ihx, ihy, sxn, syn, sc, isc, calpha, salpha, qpos;
+    double df0, fm, sm, fs, ss, fos;
+    double vtxs, vtys, numx, numy, denx, deny, xedot, yedot;
+    double Fx, Fy, fxstr, fystr, clx, cly, wxw, wyw, dwx, dwy;  // clx/cly: -1/0/+1 clamp side
+    double fx, fy, My, sgn;
+};
+// Step tape: inputs, tire tapes and the vehicle-level intermediates.
+struct StepTape {
+    double u, v, psi, wz, phi, wx, udot, vdot, crank, gear;
+    double lat, lon, fzarg[4];
+    double delta, cd, sd, dslope;   // dslope: d delta / d steering
+    double vsyf, vsyr, wcf, wcr;
+    // powertrain
+    double omega_t, omega_out, omega_in, sr, srmode, cf, tr, cfs, trs, r, torque_in, torque_out, torque_t,
+        tclip, rev, dt_map, dt_slope, tf, trr, alf, alr, dalf, dalr, slowf, slowr, dOc;
+    double thr, brk, steer;
+    double fxr[4], fyr[4];          // forces after the front rotation
+    double wu, E1, E2, E3, inner;
+    double u1, v1, wx1, wz1;        // updated speeds
+    double sp, cp;
+    double x1, y1, psi1;            // position and yaw after the step (the loss reads them)
+    TireTape t[4];
+};
+constexpr int kStepTapeDoubles = (int)(sizeof(StepTape) / sizeof(double));
+static_assert(sizeof(StepTape) % sizeof(double) == 0, "the step tape is a flat array of doubles");
+
+// map slope of the segment getMapY uses at x (0 where the map clamps)
+__device__ __forceinline__ double map_slope(const MapDev& m, double x) {
+    if (x <= m.x[0] || x >= m.x[m.n - 1]) return 0.0;
+    const int r = lower_bound_x(m.x, m.n, x);
+    return m.dy[r - 1] / m.dx[r - 1];
+}
+// sineStep(x, 1, 1, 1.5, 0) and its derivative
+__device__ __forceinline__ void sine_step_w(double x, double& y, double& dy) {
+    if (x <= 1.0) {
+        y = 1.0;
+        dy = 0.0;
+        return;
+    }
+    if (x >= 1.5) {
+        y = 0.0;
+        dy = 0.0;
+        return;
+    }
+    y = sine_step(x, 1., 1., 1.5, 0.);
+    const double u = (x - 1.0) / 0.5;
+    dy = -2.0 + 2.0 * cos(k2Pi * u);
+}
+
+// ---------------------------------------------------------------------------------------------
+// forward with tape (the arithmetic of tire_rhs_tm / tire_core_tm / powertrain_rhs / step18)
+
+template <bool kSteered>
+__device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, TireTape& T, const KView& K, double c, double s) {
+    const double fz = ta.fz;
+    T.fz = fz;
+    T.om = ts.omega;
+    T.xe = ts.xe;
+    T.ye = ts.ye;
+    T.vsy = ta.vsy;
+    T.on = fz > 0 ? 1.0 : 0.0;
+    if (fz <= 0) {
+        ts.xe = 0;
+        ts.ye = 0;
+        ts.omega = 0;
+        ta.xt = 0;
+        ta.rStat = K(K_R0);
+        ta.fx = 0;
+        ta.fy = 0;
+        ta.My = 0;
+        T.rStat = ta.rStat;
+        T.fx = T.fy = T.My = 0;
+        return;
+    }
+    ta.xt = fz * K(K_INVKT);
+    ta.rStat = K(K_R0) - ta.xt;
+    T.xt = ta.xt;
+    T.rStat = ta.rStat;
+    if (fz <= K(K_FZRD)) {
+        T.fzrd = 1.0;
+        T.rdynco = fma(K(K_DRD), fma(fz, K(K_INVPN), -1.0), K(K_RDPN));
+    } else {
+        T.fzrd = 0.0;
+        T.rdynco = K(K_RDCRIT);
+    }
+    const double r_eff = fma(T.rdynco, ta.xt, ta.rStat);
+    T.r_eff = r_eff;
+    const double omega = ts.omega;
+    const double vsy = ta.vsy;
+    const double vsx = fma(-omega, r_eff, ta.vsx);
+    T.vsx = vsx;
+    const double rw = r_eff * fabs(omega);
+    const double vta = rw + 0.01;
+    const double ivta = 1.0 / vta;
+    T.rw = rw;
+    T.vta = vta;
+    const double sx = -vsx * ivta;
+    double sy;
+    if (kSteered) {
+        T.N = vsy * c - vta * s;
+        T.D = vta * c + vsy * s;
+        sy = -(vsy * c - vta * s) / (vta * c + vsy * s);
+    } else {
+        sy = -vsy * ivta;
+    }
+    T.sx = sx;
+    T.sy = sy;
+    const double fzc = fmin(fz, K(K_PNMAX));
+    T.fzc = fzc;
+    T.fzcl = fz > K(K_PNMAX) ? 1.0 : 0.0;
+    const double fzn = fzc * K(K_INVPN);
+    T.fzn = fzn;
+    const double dfx0 = fzn * fma(-K(K_Q2DFX0), fzn, K(K_Q1DFX0));
+    const double dfy0 = fzn * fma(-K(K_Q2DFY0), fzn, K(K_Q1DFY0));
+    const double fxm = fzn * fma(-K(K_Q2FXM), fzn, K(K_Q1FXM));
+    const double fym = fzn * fma(-K(K_Q2FYM), fzn, K(K_Q1FYM));
+    const double fxs = fzn * fma(-K(K_Q2FXS), fzn, K(K_Q1FXS));
+    const double fys = fzn * fma(-K(K_Q2FYS), fzn, K(K_Q1FYS));
+    const double fzn1 = fzn - 1.0;
+    const double sxm = fma(K(K_DSXM), fzn1, K(K_LSXM));
+    const double sym = fma(K(K_DSYM), fzn1, K(K_LSYM));
+    const double sxs = fma(K(K_DSXS), fzn1, K(K_LSXS));
+    const double sys = fma(K(K_DSYS), fzn1, K(K_LSYS));
+    T.dfx0 = dfx0; T.dfy0 = dfy0; T.fxm = fxm; T.fym = fym; T.fxs = fxs; T.fys = fys;
+    T.sxm = sxm; T.sym = sym; T.sxs = sxs; T.sys = sys;
+    const double ssum = sxm + sym;
+    const double fxd = fxm * dfy0, fyd = fym * dfx0;
+    const double fsum = fxd + fyd;
+    const double r12 = 1.0 / (ssum * fsum);
+    const double issum = fsum * r12, ifsum = ssum * r12;
+    const double hsxn = fma(sxm, issum, fxd * ifsum);
+    const double hsyn = fma(sym, issum, fyd * ifsum);
+    const double rh = 1.0 / (hsxn * hsyn);
+    const double ihx = hsyn * rh, ihy = hsxn * rh;
+    T.ssum = ssum; T.fsum = fsum; T.fxd = fxd; T.fyd = fyd; T.hsxn = hsxn; T.hsyn = hsyn; T.ihx = ihx; T.ihy = ihy;
+    const double sxn = sx * ihx;
+    const double syn = sy * ihy;
+    const double q = fma(sxn, sxn, syn * syn);
+    double sc, calpha, salpha, isc = 0;
+    if (q > 0) {
+        isc = rsqrt(q);
+        sc = q * isc;
+        calpha = sxn * isc;
+        salpha = syn * isc;
+    } else {
+        sc = 0;
+        calpha = kSqrt2Over2;
+        salpha = kSqrt2Over2;
+    }
+    T.sxn = sxn; T.syn = syn; T.sc = sc; T.isc = isc; T.calpha = calpha; T.salpha = salpha;
+    T.qpos = q > 0 ? 1.0 : 0.0;
+    auto hyp = [](double a, double b) { return sqrt(fma(a, a, b * b)); };
+    const double df0 = hyp(dfx0 * calpha * hsxn, dfy0 * salpha * hsyn);
+    const double fm = hyp(fxm * calpha, fym * salpha);
+    const double cax = calpha * ihx, say = salpha * ihy;
+    const double sm = hyp(sxm * cax, sym * say);
+    const double fs = hyp(fxs * calpha, fys * salpha);
+    const double ss = hyp(sxs * cax, sys * say);
+    T.df0 = df0; T.fm = fm; T.sm = sm; T.fs = fs; T.ss = ss;
+    double f, fos;
+    tmxy(f, fos, sc, df0, sm, fm, ss, fs);
+    T.fos = fos;
+    T.sgn = sgnd(omega);
+    ta.My = -K(K_RR) * fzc * ta.rStat * T.sgn;
+    const double vtxs = fma(rw, hsxn, 0.01);
+    const double vtys = fma(rw, hsyn, 0.01);
+    const double cx = K(K_CX), cy = K(K_CY), dx = K(K_DX), dy = K(K_DY);
+    const double numx = fma(-vtxs * cx, ts.xe, -fos * vsx);
+    const double numy = fma(-vtys * cy, ts.ye, fos * (sy * vta));
+    const double denx = fma(vtxs, dx, fos), deny = fma(vtys, dy, fos);
+    const double rd = 1.0 / (denx * deny);
+    ts.xedot = numx * (deny * rd);
+    ts.yedot = numy * (denx * rd);
+    T.vtxs = vtxs; T.vtys = vtys; T.numx = numx; T.numy = numy; T.denx = denx; T.deny = deny;
+    T.xedot = ts.xedot; T.yedot = ts.yedot;
+    const double fxdyn = fma(dx, ts.xedot, cx * ts.xe);
+    const double fydyn = fma(dy, ts.yedot, cy * ts.ye);
+    const double Gx = fma(ts.xe, cx, ts.xedot * dx);
+    const double Gy = fma(ts.ye, cy, ts.yedot * dy);
+    const double fxstr = fmin(fmax(Gx, -K(K_FXMP2N)), K(K_FXMP2N));
+    const double fystr = fmin(fmax(Gy, -K(K_FYMP2N)), K(K_FYMP2N));
+    T.Fx = fxdyn; T.Fy = fydyn; T.fxstr = fxstr; T.fystr = fystr;
+    T.clx = Gx > K(K_FXMP2N) ? 1.0 : (Gx < -K(K_FXMP2N) ? -1.0 : 0.0);
+    T.cly = Gy > K(K_FYMP2N) ? 1.0 : (Gy < -K(K_FYMP2N) ? -1.0 : 0.0);
+    double wx, wy, dwx, dwy;
+    sine_step_w(fabs(vsx), wx, dwx);
+    sine_step_w(fabs(sy * vta), wy, dwy);
+    T.wxw = wx; T.wyw = wy; T.dwx = dwx; T.dwy = dwy;
+    ta.fx = (wx == 0.0) ? fxdyn : fma(wx, fxstr, (1. - wx) * fxdyn);
+    ta.fy = (wy == 0.0) ? fydyn : fma(wy, fystr, (1. - wy) * fydyn);
+    T.fx = ta.fx;
+    T.fy = ta.fy;
+    T.My = ta.My;
+}
+
+// One step18<false> with its tape; v/va/ts/ta as in step18.
+__device__ __forceinline__ void fwd18_tape(VehC& v, VehAux& va, TireC* ts, TireAux* ta, StepTape& T, const KView& K,
+                                           const ClassDev18& C, double steering, double throttle, double braking,
+                                           double dt) {
+    T.u = v.u; T.v = v.v; T.psi = v.psi; T.wz = v.wz; T.phi = v.phi; T.wx = v.wx;
+    T.udot = v.udot; T.vdot = v.vdot; T.crank = v.crank; T.gear = (double)v.gear;
+    T.steer = steering; T.thr = throttle; T.brk = braking;
+    {
+        const double lat = fma(v.wz, v.u, v.vdot);
+        const double lon = fma(-v.wz, v.v, v.udot);
+        T.lat = lat;
+        T.lon = lon;
+        const double Z4 = K(K_Z4) * lon;
+        const double Z2f = K(K_Z2F) * lat;
+        const double Z3f = fma(K(K_Z3FK), v.phi, K(K_Z3FB) * v.wx);
+        const double Z2r = K(K_Z2R) * lat;
+        const double Z3r = fma(K(K_Z3RK), v.phi, K(K_Z3RB) * v.wx);
+        const double Af = K(K_Z1F) - Z4, Bf = Z2f + Z3f;
+        const double Ar = K(K_Z1R) + Z4, Br = Z2r + Z3r;
+        T.fzarg[0] = Af - Bf;
+        T.fzarg[1] = Af + Bf;
+        T.fzarg[2] = Ar - Br;
+        T.fzarg[3] = Ar + Br;
+        ta[0].fz = fmax(Af - Bf, 0.0);
+        ta[1].fz = fmax(Af + Bf, 0.0);
+        ta[2].fz = fmax(Ar - Br, 0.0);
+        ta[3].fz = fmax(Ar + Br, 0.0);
+    }
+    double delta;
+    if (C.nonLinearSteer) {
+        delta = map_y(C.steer, steering);
+        T.dslope = map_slope(C.steer, steering);
+    } else {
+        delta = steering * K(K_MAXSTEER);
+        T.dslope = K(K_MAXSTEER);
+    }
+    double cd = 1.0, sd = 0.0;
+    if (delta != 0.0) sincos(delta, &sd, &cd);
+    T.delta = delta;
+    T.cd = cd;
+    T.sd = sd;
+    {
+        const double vsyf = fma(v.wz, K(K_A), v.v);
+        const double vsyr = fma(-v.wz, K(K_B), v.v);
+        const double wcf = v.wz * K(K_CF2), wcr = v.wz * K(K_CR2);
+        T.vsyf = vsyf; T.vsyr = vsyr; T.wcf = wcf; T.wcr = wcr;
+        ta[0].vsy = vsyf;
+        ta[1].vsy = vsyf;
+        ta[0].vsx = fma(v.u - wcf, cd, vsyf * sd);
+        ta[1].vsx = fma(v.u + wcf, cd, vsyf * sd);
+        ta[2].vsy = vsyr;
+        ta[3].vsy = vsyr;
+        ta[2].vsx = v.u - wcr;
+        ta[3].vsx = v.u + wcr;
+    }
+    tire_fwd_tape<true>(ts[0], ta[0], T.t[0], K, cd, sd);
+    tire_fwd_tape<true>(ts[1], ta[1], T.t[1], K, cd, sd);
+    tire_fwd_tape<false>(ts[2], ta[2], T.t[2], K, 1.0, 0.0);
+    tire_fwd_tape<false>(ts[3], ta[3], T.t[3], K, 1.0, 0.0);
+    // powertrain (powertrain_rhs<false>) with its tape
+    {
+        double torque_t;
+        const int g = v.gear;
+        T.rev = 0;
+        T.tclip = 0;
+        if (C.tcbool) {
+            bool reverse = false;
+            const double omega_t = 0.25 * (((ts[0].omega + ts[1].omega) + ts[2].omega) + ts[3].omega);
+            const double omega_out = omega_t / C.gear[g];
+            const double omega_in = v.crank;
+            T.omega_t = omega_t;
+            T.omega_out = omega_out;
+            T.omega_in = omega_in;
+            double sr;
+            if ((omega_out < 1e-9) || (omega_in < 1e-9)) {
+                sr = 0;
+                T.srmode = 0;  // constant
+            } else {
+                sr = omega_out / omega_in;
+                T.srmode = 1;
+                if (sr > 1.) {
+                    sr = 1. - (sr - 1.);
+                    reverse = true;
+                }
+                if (sr < 0) {
+                    sr = 0;
+                    T.srmode = 0;
+                }
+            }
+            T.sr = sr;
+            T.rev = reverse ? 1.0 : 0.0;
+            const double cf = map_y(C.cf, sr), tr = map_y(C.tr, sr);
+            T.cf = cf;
+            T.tr = tr;
+            T.cfs = map_slope(C.cf, sr);
+            T.trs = map_slope(C.tr, sr);
+            const double r = omega_in / cf;
+            T.r = r;
+            double torque_in = -(r * r);
+            if (reverse) torque_in = -torque_in;
+            T.torque_in = torque_in;
+            const double torque_out = reverse ? -torque_in : -tr * torque_in;
+            T.torque_out = torque_out;
+            torque_t = torque_out * C.invgear[g];
+            if (v.u < 1e-9 && torque_t < 0) {
+                torque_t = 0;
+                T.tclip = 1;
+            }
+            const double dtq = drive_torque(C, throttle, v.crank);
+            T.dt_map = map_y(C.pt, v.crank);
+            T.dt_slope = fma(map_slope(C.pt, v.crank), throttle, map_slope(C.loss, v.crank));
+            va.dOmega_crank = K(K_INVCI) * (dtq + torque_in);
+            if (omega_out > C.up[g]) {
+                if (g < C.noGears - 1) v.gear = g + 1;
+            } else if (omega_out < C.down[g]) {
+                if (g > 0) v.gear = g - 1;
+            }
+        } else {
+            v.crank = 0.25 * (((ts[0].omega + ts[1].omega) + ts[2].omega) + ts[3].omega) / C.gear[g];
+            T.omega_in = v.crank;
+            torque_t = drive_torque(C, throttle, v.crank) * C.invgear[g];
+            T.dt_map = map_y(C.pt, v.crank);
+            T.dt_slope = fma(map_slope(C.pt, v.crank), throttle, map_slope(C.loss, v.crank));
+            if (v.u < 1e-9 && torque_t < 0) {
+                torque_t = 0;
+                T.tclip = 1;
+            }
+            if (v.crank > C.up[g]) {
+                if (g < C.noGears - 1) v.gear = g + 1;
+            } else if (v.crank < C.down[g]) {
+                if (g > 0) v.gear = g - 1;
+            }
+        }
+        T.torque_t = torque_t;
+        double tf, trr;
+        if (C.driveType) {
+            tf = torque_t * 0.5;
+            trr = torque_t * 0.5;
+        } else if (C.whichWheels) {
+            tf = 0;
+            trr = torque_t;
+        } else {
+            tf = torque_t;
+            trr = 0;
+        }
+        T.tf = tf;
+        T.trr = trr;
+        // differential split with the bias and its slope recorded
+        auto split = [&](double torque, double wl, double wr, double& tl, double& tR, double& alpha, double& dal,
+                         double& slowleft) {
+            const double diff = fabs(wl - wr);
+            if (diff > 0.5) {
+                alpha = 2.0 / 3.0;
+                dal = 0;
+            } else if (diff > 0.25) {
+                const double bias = 4 * (2.0 - 1) * diff + (2 - 2.0);
+                alpha = bias / (1 + bias);
+                dal = 4.0 / ((1 + bias) * (1 + bias));
+            } else {
+                alpha = 0.5;
+                dal = 0;
+            }
+            const double slow = alpha * torque;
+            const double fast = torque - slow;
+            if (fabs(wl) < fabs(wr)) {
+                tl = slow;
+                tR = fast;
+                slowleft = 1;
+            } else {
+                tl = fast;
+                tR = slow;
+                slowleft = 0;
+            }
+        };
+        split(tf, ts[0].omega, ts[1].omega, ta[0].engTor, ta[1].engTor, T.alf, T.dalf, T.slowf);
+        split(trr, ts[2].omega, ts[3].omega, ta[2].engTor, ta[3].engTor, T.alr, T.dalr, T.slowr);
+        const double brake = K(K_MAXBRAKE) * braking;
+        const double ijw = K(K_INVJW);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            ta[k].dOmega =
+                ijw * (fma(-sgnd(ts[k].omega), brake, ta[k].engTor + ta[k].My) - ta[k].fx * ta[k].rStat);
+        T.dOc = va.dOmega_crank;
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const double fx = ta[k].fx, fy = ta[k].fy;
+        ta[k].fx = fma(fx, cd, -fy * sd);
+        ta[k].fy = fma(fx, sd, fy * cd);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        T.fxr[k] = ta[k].fx;
+        T.fyr[k] = ta[k].fy;
+    }
+    {
+        const double fx0 = ta[0].fx, fx1 = ta[1].fx, fx2 = ta[2].fx, fx3 = ta[3].fx;
+        const double fy0 = ta[0].fy, fy1 = ta[1].fy, fy2 = ta[2].fy, fy3 = ta[3].fy;
+        const double wu = v.wz * v.u;
+        const double fyf = fy0 + fy1, fyr = fy2 + fy3;
+        const double E1 = fma(-K(K_MT), wu, fyf + fyr);
+        const double E2 = fma(K(K_E2WU), wu,
+                              fma(fx3 - fx2, K(K_CR2), fma(fx1 - fx0, K(K_CF2), fma(fyf, K(K_A), -fyr * K(K_B)))));
+        const double E3 = fma(K(K_E3WU), wu, fma(K(K_E3PHI), v.phi, K(K_E3WX) * v.wx));
+        const double sfx = ((fx0 + fx1) + fx2) + fx3;
+        const double inner = fma(K(K_UWZ2), v.wz * v.wz, fma(-K(K_UWZWX), v.wz * v.wx, sfx));
+        T.wu = wu; T.E1 = E1; T.E2 = E2; T.E3 = E3; T.inner = inner;
+        v.udot = fma(K(K_INVMT), inner, v.wz * v.v);
+        v.vdot = fma(K(K_CV1), E1, fma(K(K_CV2), E2, K(K_CV3) * E3));
+        va.wxdot = fma(K(K_CV3), E1, fma(K(K_CX2), E2, K(K_CX3) * E3));
+        va.wzdot = fma(K(K_CV2), E1, fma(K(K_CZ2), E2, K(K_CX2) * E3));
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        ts[k].xe = fma(ts[k].xedot, dt, ts[k].xe);
+        ts[k].ye = fma(ts[k].yedot, dt, ts[k].ye);
+        ts[k].omega = fma(ta[k].dOmega, dt, ts[k].omega);
+    }
+    if (C.tcbool) v.crank = fma(va.dOmega_crank, dt, v.crank);
+    v.u = fma(v.udot, dt, v.u);
+    v.v = fma(v.vdot, dt, v.v);
+    v.wx = fma(va.wxdot, dt, v.wx);
+    v.wz = fma(va.wzdot, dt, v.wz);
+    T.u1 = v.u; T.v1 = v.v; T.wx1 = v.wx; T.wz1 = v.wz;
+    double sp, cp;
+    sincos(v.psi, &sp, &cp);
+    T.sp = sp;
+    T.cp = cp;
+    v.x = fma(fma(v.u, cp, -v.v * sp), dt, v.x);
+    v.y = fma(fma(v.u, sp, v.v * cp), dt, v.y);
+    v.psi = fma(v.wz, dt, v.psi);
+    v.phi = fma(v.wx, dt, v.phi);
+    T.x1 = v.x;
+    T.y1 = v.y;
+    T.psi1 = v.psi;
+}
+
+// ---------------------------------------------------------------------------------------------
+// reverse sweep
+
+// tmxy_combined (dof18_gpu.cu:243-285): adjoints of (s, df0, sm, fm, ss, fs) from that of fos, on
+// the regime the forward took (the intermediates are recomputed; they are cheap).
+__device__ __forceinline__ void tmxy_rev(double s, double df0, double sm, double fm, double ss, double fs, double fosb,
+                                         double& sb, double& df0b, double& smb, double& fmb, double& ssb,
+                                         double& fsb) {
+    double df0loc = 0.0, ism = 0.0;
+    bool dsel = false;
+    if (sm > 0.0) {
+        ism = 1.0 / sm;
+        const double c2 = 2.0 * fm * ism;
+        df0loc = fmax(c2, df0);
+        dsel = c2 >= df0;
+    }
+    if (!(s > 0.0 && df0loc > 0.0) || fosb == 0.0) return;
+    double df0locb = 0.0;
+    if (s > ss) {  // full sliding: fos = fs / s
+        fsb += fosb / s;
+        sb += -fs / (s * s) * fosb;
+        return;
+    }
+    if (s < sm) {  // adhesion: fos = df0loc / dn
+        const double p = df0loc * sm / fm - 2.0;
+        const double sn = s * ism;
+        const double dn = fma(sn + p, sn, 1.0);
+        const double dnb = -df0loc / (dn * dn) * fosb;
+        df0locb += fosb / dn;
+        const double snb = (2.0 * sn + p) * dnb;
+        const double pb = sn * dnb;
+        df0locb += sm / fm * pb;
+        smb += df0loc / fm * pb;
+        fmb += -df0loc * sm / (fm * fm) * pb;
+        sb += snb * ism;
+        smb += -s * ism * ism * snb;
+    } else {
+        const double q = fm * ism;
+        const double a = q * q / (df0loc * sm);
+        const double sstar = sm + (fm - fs) / (a * (ss - sm));
+        double f, ab = 0.0, sstarb = 0.0;
+        double b = 0.0, sn3 = 0.0;
+        if (sstar <= ss) {
+            if (s <= sstar) {
+                f = fm - a * (s - sm) * (s - sm);
+            } else {
+                b = a * (sstar - sm) / (ss - sstar);
+                f = fs + b * (ss - s) * (ss - s);
+            }
+        } else {
+            sn3 = (s - sm) / (ss - sm);
+            f = fm - (fm - fs) * sn3 * sn3 * (3.0 - 2.0 * sn3);
+        }
+        const double fb = fosb / s;  // fos = f / s
+        sb += -f / (s * s) * fosb;
+        if (sstar <= ss) {
+            if (s <= sstar) {
+                fmb += fb;
+                ab += -(s - sm) * (s - sm) * fb;
+                sb += -2.0 * a * (s - sm) * fb;
+                smb += 2.0 * a * (s - sm) * fb;
+            } else {
+                fsb += fb;
+                const double bb = (ss - s) * (ss - s) * fb;
+                ssb += 2.0 * b * (ss - s) * fb;
+                sb += -2.0 * b * (ss - s) * fb;
+                const double d = ss - sstar;
+                ab += (sstar - sm) / d * bb;
+                sstarb += (a / d + a * (sstar - sm) / (d * d)) * bb;
+                smb += -a / d * bb;
+                ssb += -a * (sstar - sm) / (d * d) * bb;
+            }
+        } else {
+            const double g = sn3 * sn3 * (3.0 - 2.0 * sn3);
+            fmb += fb * (1.0 - g);
+            fsb += fb * g;
+            const double snb = -(fm - fs) * (6.0 * sn3 - 6.0 * sn3 * sn3) * fb;
+            const double d = ss - sm;
+            sb += snb / d;
+            smb += snb * (-1.0 / d + (s - sm) / (d * d));
+            ssb += -snb * (s - sm) / (d * d);
+        }
+        if (sstarb != 0.0) {  // sstar = sm + (fm - fs) / (a (ss - sm))
+            const double den = a * (ss - sm);
+            smb += sstarb;
+            fmb += sstarb / den;
+            fsb += -sstarb / den;
+            const double denb = -(fm - fs) / (den * den) * sstarb;
+            ab += (ss - sm) * denb;
+            ssb += a * denb;
+            smb += -a * denb;
+        }
+        if (ab != 0.0) {  // a = q^2 / (df0loc sm), q = fm / sm
+            const double qb = 2.0 * q / (df0loc * sm) * ab;
+            df0locb += -q * q / (df0loc * df0loc * sm) * ab;
+            smb += -q * q / (df0loc * sm * sm) * ab;
+            fmb += qb * ism;
+            smb += -fm * ism * ism * qb;
+        }
+    }
+    if (dsel) {  // df0loc = max(2 fm / sm, df0)
+        fmb += 2.0 * ism * df0locb;
+        smb += -2.0 * fm * ism * ism * df0locb;
+    } else {
+        df0b += df0locb;
+    }
+}
+
+// Tire adjoint (on-ground tire): from the adjoints of the core outputs (xedot, yedot, fx, fy, My as
+// the tire model returns them, before any frame rotation) and of rStat, to those of the inputs
+// (xe, ye, omega, vsx before the slip correction, vsy, fz, cos/sin of the wheel angle).
+template <bool kSteered>
+__device__ __forceinline__ void tire_rev(const TireTape& T, const KView& K, const KBar& kb, double xedotb,
+                                         double yedotb, double fxb, double fyb, double Myb, double rStatb, double& xeb,
+                                         double& yeb, double& omb, double& vsxinb, double& vsyb, double& fzb,
+                                         double& cb, double& sb_, double c, double s) {
+    const double cx = K(K_CX), cy = K(K_CY), dx = K(K_DX), dy = K(K_DY);
+    double vsxb = 0, syb = 0, vtab = 0, fosb = 0, rwb = 0, hsxnb = 0, hsynb = 0, fzcb = 0, sxb = 0;
+    // blend of structural and dynamic forces
+    const double wxb = (T.fxstr - T.Fx) * fxb, wyb = (T.fystr - T.Fy) * fyb;
+    const double fxstrb = T.wxw * fxb, fystrb = T.wyw * fyb;
+    const double Fxb = (1.0 - T.wxw) * fxb, Fyb = (1.0 - T.wyw) * fyb;
+    vsxb += T.dwx * (T.vsx >= 0 ? 1.0 : -1.0) * wxb;
+    {
+        const double arg = T.sy * T.vta;
+        const double argb = T.dwy * (arg >= 0 ? 1.0 : -1.0) * wyb;
+        syb += T.vta * argb;
+        vtab += T.sy * argb;
+    }
+    double Gxb = 0, Gyb = 0;
+    if (T.clx == 0.0) Gxb = fxstrb;
+    else kb.add(KB_FXMP2N, T.clx * fxstrb);
+    if (T.cly == 0.0) Gyb = fystrb;
+    else kb.add(KB_FYMP2N, T.cly * fystrb);
+    xeb += cx * (Gxb + Fxb);
+    xedotb += dx * (Gxb + Fxb);
+    yeb += cy * (Gyb + Fyb);
+    yedotb += dy * (Gyb + Fyb);
+    // relaxation rates
+    const double numxb = xedotb / T.denx, denxb = -T.xedot / T.denx * xedotb;
+    const double numyb = yedotb / T.deny, denyb = -T.yedot / T.deny * yedotb;
+    double vtxsb = -cx * T.xe * numxb + dx * denxb;
+    xeb += -T.vtxs * cx * numxb;
+    fosb += -T.vsx * numxb + denxb;
+    vsxb += -T.fos * numxb;
+    double vtysb = -cy * T.ye * numyb + dy * denyb;
+    yeb += -T.vtys * cy * numyb;
+    fosb += T.sy * T.vta * numyb + denyb;
+    syb += T.fos * T.vta * numyb;
+    vtab += T.fos * T.sy * numyb;
+    rwb += T.hsxn * vtxsb + T.hsyn * vtysb;
+    hsxnb += T.rw * vtxsb;
+    hsynb += T.rw * vtysb;
+    // rolling resistance (no adjoint through sgn)
+    fzcb += -K(K_RR) * T.rStat * T.sgn * Myb;
+    rStatb += -K(K_RR) * T.fzc * T.sgn * Myb;
+    // combined-slip force curve
+    double scb = 0, df0b = 0, smb = 0, fmb = 0, ssb = 0, fsb = 0;
+    tmxy_rev(T.sc, T.df0, T.sm, T.fm, T.ss, T.fs, fosb, scb, df0b, smb, fmb, ssb, fsb);
+    double calphab = 0, salphab = 0, caxb = 0, sayb = 0, ihxb = 0, ihyb = 0;
+    double dfx0b = 0, dfy0b = 0, fxmb = 0, fymb = 0, fxsb = 0, fysb = 0, sxmb = 0, symb = 0, sxsb = 0, sysb = 0;
+    const double cax = T.calpha * T.ihx, say = T.salpha * T.ihy;
+    auto hyp_rev = [](double a, double b, double h, double hb, double& ab, double& bb) {
+        if (h > 0) {
+            ab += a / h * hb;
+            bb += b / h * hb;
+        }
+    };
+    {
+        double Pb = 0, Qb = 0;
+        hyp_rev(T.sxs * cax, T.sys * say, T.ss, ssb, Pb, Qb);
+        sxsb += cax * Pb;
+        caxb += T.sxs * Pb;
+        sysb += say * Qb;
+        sayb += T.sys * Qb;
+    }
+    {
+        double Pb = 0, Qb = 0;
+        hyp_rev(T.fxs * T.calpha, T.fys * T.salpha, T.fs, fsb, Pb, Qb);
+        fxsb += T.calpha * Pb;
+        calphab += T.fxs * Pb;
+        fysb += T.salpha * Qb;
+        salphab += T.fys * Qb;
+    }
+    {
+        double Pb = 0, Qb = 0;
+        hyp_rev(T.sxm * cax, T.sym * say, T.sm, smb, Pb, Qb);
+        sxmb += cax * Pb;
+        caxb += T.sxm * Pb;
+        symb += say * Qb;
+        sayb += T.sym * Qb;
+    }
+    calphab += T.ihx * caxb;
+    ihxb += T.calpha * caxb;
+    salphab += T.ihy * sayb;
+    ihyb += T.salpha * sayb;
+    {
+        double Pb = 0, Qb = 0;
+        hyp_rev(T.fxm * T.calpha, T.fym * T.salpha, T.fm, fmb, Pb, Qb);
+        fxmb += T.calpha * Pb;
+        calphab += T.fxm * Pb;
+        fymb += T.salpha * Qb;
+        salphab += T.fym * Qb;
+    }
+    {
+        double Pb = 0, Qb = 0;
+        hyp_rev(T.dfx0 * T.calpha * T.hsxn, T.dfy0 * T.salpha * T.hsyn, T.df0, df0b, Pb, Qb);
+        dfx0b += T.calpha * T.hsxn * Pb;
+        calphab += T.dfx0 * T.hsxn * Pb;
+        hsxnb += T.dfx0 * T.calpha * Pb;
+        dfy0b += T.salpha * T.hsyn * Qb;
+        salphab += T.dfy0 * T.hsyn * Qb;
+        hsynb += T.dfy0 * T.salpha * Qb;
+    }
+    double sxnb = 0, synb = 0;
+    if (T.qpos != 0.0) {
+        const double iscb = T.sxn * calphab + T.syn * salphab;
+        sxnb += T.isc * calphab;
+        synb += T.isc * salphab;
+        const double sct = scb - iscb * T.isc * T.isc;
+        sxnb += T.sxn / T.sc * sct;
+        synb += T.syn / T.sc * sct;
+    }
+    sxb += T.ihx * sxnb;
+    ihxb += T.sx * sxnb;
+    syb += T.ihy * synb;
+    ihyb += T.sy * synb;
+    hsxnb += -T.ihx * T.ihx * ihxb;
+    hsynb += -T.ihy * T.ihy * ihyb;
+    {
+        const double ssumb = -(T.sxm * hsxnb + T.sym * hsynb) / (T.ssum * T.ssum);
+        const double fsumb = -(T.fxd * hsxnb + T.fyd * hsynb) / (T.fsum * T.fsum);
+        sxmb += hsxnb / T.ssum + ssumb;
+        symb += hsynb / T.ssum + ssumb;
+        const double fxdb = hsxnb / T.fsum + fsumb;
+        const double fydb = hsynb / T.fsum + fsumb;
+        fxmb += T.dfy0 * fxdb;
+        dfy0b += T.fxm * fxdb;
+        fymb += T.dfx0 * fydb;
+        dfx0b += T.fym * fydb;
+    }
+    // curve parameters from the normalised load
+    const double fzn = T.fzn;
+    double fznb = 0;
+    fznb += fma(-2.0 * K(K_Q2DFX0), fzn, K(K_Q1DFX0)) * dfx0b;
+    fznb += fma(-2.0 * K(K_Q2DFY0), fzn, K(K_Q1DFY0)) * dfy0b;
+    fznb += fma(-2.0 * K(K_Q2FXM), fzn, K(K_Q1FXM)) * fxmb;
+    fznb += fma(-2.0 * K(K_Q2FYM), fzn, K(K_Q1FYM)) * fymb;
+    fznb += fma(-2.0 * K(K_Q2FXS), fzn, K(K_Q1FXS)) * fxsb;
+    fznb += fma(-2.0 * K(K_Q2FYS), fzn, K(K_Q1FYS)) * fysb;
+    kb.add(KB_Q1FXM, fzn * fxmb);
+    kb.add(KB_Q2FXM, -fzn * fzn * fxmb);
+    kb.add(KB_Q1FYM, fzn * fymb);
+    kb.add(KB_Q2FYM, -fzn * fzn * fymb);
+    kb.add(KB_Q1FXS, fzn * fxsb);
+    kb.add(KB_Q2FXS, -fzn * fzn * fxsb);
+    kb.add(KB_Q1FYS, fzn * fysb);
+    kb.add(KB_Q2FYS, -fzn * fzn * fysb);
+    fznb += K(K_DSXM) * sxmb + K(K_DSYM) * symb + K(K_DSXS) * sxsb + K(K_DSYS) * sysb;
+    fzcb += K(K_INVPN) * fznb;
+    if (T.fzcl == 0.0) fzb += fzcb;
+    // slips
+    const double ivta = 1.0 / T.vta;
+    vsxb += -ivta * sxb;
+    vtab += T.vsx * ivta * ivta * sxb;
+    if (kSteered) {
+        const double Nb = -syb / T.D, Db = T.N / (T.D * T.D) * syb;
+        vsyb += c * Nb + s * Db;
+        vtab += -s * Nb + c * Db;
+        cb += T.vsy * Nb + T.vta * Db;
+        sb_ += -T.vta * Nb + T.vsy * Db;
+    } else {
+        vsyb += -ivta * syb;
+        vtab += T.vsy * ivta * ivta * syb;
+    }
+    rwb += vtab;
+    double reffb = fabs(T.om) * rwb;
+    omb += T.r_eff * T.sgn * rwb;
+    vsxinb += vsxb;
+    omb += -T.r_eff * vsxb;
+    reffb += -T.om * vsxb;
+    // r_eff = rdynco xt + rStat, rStat = r0 - xt, xt = fz / kt
+    double xtb = T.rdynco * reffb;
+    rStatb += reffb;
+    if (T.fzrd != 0.0) fzb += K(K_DRD) * K(K_INVPN) * (T.xt * reffb);  // rdynco interpolated in fz
+    xtb += -rStatb;
+    fzb += K(K_INVKT) * xtb;
+    kb.add(KB_INVKT, T.fz * xtb);
+}
+
+// One step's reverse sweep. L: on entry the adjoint of the state after the step, on return that of
+// the state before it; the adjoints of the step's controls are added to steerb/thrb/brkb and those
+// of the differentiable constants to kb.
+__device__ __forceinline__ void rev18(const StepTape& T, const KView& K, const ClassDev18& C, const KBar& kb,
+                                      double dt, Adj18& L, double& steerb, double& thrb, double& brkb) {
+    const int g = (int)T.gear;
+    // half-implicit update: x, y with the updated speeds and the old yaw; yaw and roll with the
+    // updated rates
+    double u1b = dt * fma(T.cp, L.x, T.sp * L.y);
+    double v1b = dt * fma(-T.sp, L.x, T.cp * L.y);
+    double psib = L.psi + dt * ((-T.u1 * T.sp - T.v1 * T.cp) * L.x + (T.u1 * T.cp - T.v1 * T.sp) * L.y);
+    double wz1b = dt * L.psi + L.wz;
+    double wx1b = dt * L.phi + L.wx;
+    const double phib0 = L.phi;
+    u1b += L.u;
+    v1b += L.v;
+    double ub = u1b, vb = v1b, wxb = wx1b, wzb = wz1b, phib = phib0;
+    const double udotb = dt * u1b + L.udot;  // the new accelerations are also carried to the next step
+    const double vdotb = dt * v1b + L.vdot;
+    const double wxdotb = dt * wx1b, wzdotb = dt * wz1b;
+    double crankb = 0, dOcb = 0, crank_outb = 0;
+    if (C.tcbool) {
+        crankb = L.crank;
+        dOcb = dt * L.crank;
+    } else {
+        crank_outb = L.crank;
+    }
+    double om_midb[4], dOmb[4], xedotnb[4], yedotnb[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        om_midb[k] = L.om[k];
+        dOmb[k] = dt * L.om[k];
+        xedotnb[k] = fma(dt, L.xe[k], L.xedot[k]);
+        yedotnb[k] = fma(dt, L.ye[k], L.yedot[k]);
+    }
+    // vehicle RHS
+    double fxrb[4], fyrb[4];
+    {
+        const double innerb = K(K_INVMT) * udotb;
+        kb.add(KB_INVMT, T.inner * udotb);
+        wzb += T.v * udotb;
+        vb += T.wz * udotb;
+        wzb += (2.0 * K(K_UWZ2) * T.wz - K(K_UWZWX) * T.wx) * innerb;
+        wxb += -K(K_UWZWX) * T.wz * innerb;
+        kb.add(KB_UWZ2, T.wz * T.wz * innerb);
+        kb.add(KB_UWZWX, -T.wz * T.wx * innerb);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            fxrb[k] = innerb;
+            fyrb[k] = 0;
+        }
+        const double E1b = K(K_CV1) * vdotb + K(K_CV3) * wxdotb + K(K_CV2) * wzdotb;
+        const double E2b = K(K_CV2) * vdotb + K(K_CX2) * wxdotb + K(K_CZ2) * wzdotb;
+        const double E3b = K(K_CV3) * vdotb + K(K_CX3) * wxdotb + K(K_CX2) * wzdotb;
+        kb.add(KB_CV1, T.E1 * vdotb);
+        kb.add(KB_CV2, T.E2 * vdotb + T.E1 * wzdotb);
+        kb.add(KB_CV3, T.E3 * vdotb + T.E1 * wxdotb);
+        kb.add(KB_CX2, T.E2 * wxdotb + T.E3 * wzdotb);
+        kb.add(KB_CX3, T.E3 * wxdotb);
+        kb.add(KB_CZ2, T.E2 * wzdotb);
+        double wub = K(K_E3WU) * E3b;
+        phib += K(K_E3PHI) * E3b;
+        wxb += K(K_E3WX) * E3b;
+        kb.add(KB_E3WU, T.wu * E3b);
+        kb.add(KB_E3PHI, T.phi * E3b);
+        const double fyf = T.fyr[0] + T.fyr[1], fyr = T.fyr[2] + T.fyr[3];
+        wub += K(K_E2WU) * E2b;
+        fxrb[3] += K(K_CR2) * E2b;
+        fxrb[2] -= K(K_CR2) * E2b;
+        fxrb[1] += K(K_CF2) * E2b;
+        fxrb[0] -= K(K_CF2) * E2b;
+        double fyfb = K(K_A) * E2b, fyrb_ = -K(K_B) * E2b;
+        kb.add(KB_E2WU, T.wu * E2b);
+        kb.add(KB_A, fyf * E2b);
+        wub += -K(K_MT) * E1b;
+        fyfb += E1b;
+        fyrb_ += E1b;
+        kb.add(KB_MT, -T.wu * E1b);
+        (void)fyr;
+        fyrb[0] += fyfb;
+        fyrb[1] += fyfb;
+        fyrb[2] += fyrb_;
+        fyrb[3] += fyrb_;
+        wzb += T.u * wub;
+        ub += T.wz * wub;
+    }
+    // front forces rotated into the vehicle frame
+    double fxb[4], fyb[4], cdb = 0, sdb = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (k < 2) {
+            const double fx = T.t[k].fx, fy = T.t[k].fy;
+            fxb[k] = fma(T.cd, fxrb[k], T.sd * fyrb[k]);
+            fyb[k] = fma(-T.sd, fxrb[k], T.cd * fyrb[k]);
+            cdb += fma(fx, fxrb[k], fy * fyrb[k]);
+            sdb += fma(-fy, fxrb[k], fx * fyrb[k]);
+        } else {
+            fxb[k] = fxrb[k];
+            fyb[k] = fyrb[k];
+        }
+    }
+    // powertrain
+    double Myb[4], rStatb[4], engb[4], brakeb = 0;
+    double om_mid[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        om_mid[k] = T.t[k].on != 0.0 ? T.t[k].om : 0.0;
+        const double gk = K(K_INVJW) * dOmb[k];
+        engb[k] = gk;
+        Myb[k] = gk;
+        brakeb += -sgnd(om_mid[k]) * gk;
+        fxb[k] += -T.t[k].rStat * gk;
+        rStatb[k] = -T.t[k].fx * gk;
+    }
+    brkb += K(K_MAXBRAKE) * brakeb;
+    auto split_rev = [](double torque, double alpha, double dal, double slowleft, double tlb, double trb, double wl,
+                        double wr, double& wlb, double& wrb) {
+        const double slowb = slowleft != 0.0 ? tlb : trb;
+        const double fastb = slowleft != 0.0 ? trb : tlb;
+        const double alphab = torque * (slowb - fastb);
+        const double diffb = dal * alphab;
+        if (diffb != 0.0) {
+            const double sg = (wl - wr) >= 0 ? 1.0 : -1.0;
+            wlb += sg * diffb;
+            wrb -= sg * diffb;
+        }
+        return alpha * slowb + (1.0 - alpha) * fastb;
+    };
+    const double tfb = split_rev(T.tf, T.alf, T.dalf, T.slowf, engb[0], engb[1], om_mid[0], om_mid[1], om_midb[0],
+                                 om_midb[1]);
+    const double trrb = split_rev(T.trr, T.alr, T.dalr, T.slowr, engb[2], engb[3], om_mid[2], om_mid[3], om_midb[2],
+                                  om_midb[3]);
+    double torque_tb = C.driveType ? 0.5 * (tfb + trrb) : (C.whichWheels ? trrb : tfb);
+    if (T.tclip != 0.0) torque_tb = 0;
+    if (C.tcbool) {
+        const double torque_outb = C.invgear[g] * torque_tb;
+        double torque_inb = 0, trb = 0;
+        if (T.rev != 0.0) {
+            torque_inb += -torque_outb;
+        } else {
+            trb = -T.torque_in * torque_outb;
+            torque_inb += -T.tr * torque_outb;
+        }
+        const double dtqb = K(K_INVCI) * dOcb;
+        torque_inb += K(K_INVCI) * dOcb;
+        thrb += T.dt_map * dtqb;
+        crankb += T.dt_slope * dtqb;
+        const double rb = (T.rev != 0.0 ? 2.0 * T.r : -2.0 * T.r) * torque_inb;
+        double omega_inb = rb / T.cf;
+        const double cfb = -T.r / T.cf * rb;
+        const double srb = T.cfs * cfb + T.trs * trb;
+        double omega_outb = 0;
+        if (T.srmode != 0.0) {
+            const double sr0b = T.rev != 0.0 ? -srb : srb;
+            omega_outb += sr0b / T.omega_in;
+            omega_inb += -(T.omega_out / T.omega_in) / T.omega_in * sr0b;
+        }
+        const double omega_tb = omega_outb / C.gear[g];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) om_midb[k] += 0.25 * omega_tb;
+        crankb += omega_inb;
+    } else {
+        const double dtqb = C.invgear[g] * torque_tb;
+        thrb += T.dt_map * dtqb;
+        crank_outb += T.dt_slope * dtqb;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) om_midb[k] += 0.25 * crank_outb / C.gear[g];
+    }
+    // tires
+    double vsxinb[4], vsyb[4], fzb[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        vsxinb[k] = vsyb[k] = fzb[k] = 0;
+        if (T.t[k].on != 0.0) {
+            double xeb = L.xe[k], yeb = L.ye[k], omb = om_midb[k];
+            if (k < 2)
+                tire_rev<true>(T.t[k], K, kb, xedotnb[k], yedotnb[k], fxb[k], fyb[k], Myb[k], rStatb[k], xeb, yeb,
+                               omb, vsxinb[k], vsyb[k], fzb[k], cdb, sdb, T.cd, T.sd);
+            else {
+                double cdum = 0, sdum = 0;
+                tire_rev<false>(T.t[k], K, kb, xedotnb[k], yedotnb[k], fxb[k], fyb[k], Myb[k], rStatb[k], xeb, yeb,
+                                omb, vsxinb[k], vsyb[k], fzb[k], cdum, sdum, 1.0, 0.0);
+            }
+            L.xe[k] = xeb;
+            L.ye[k] = yeb;
+            L.om[k] = omb;
+            L.xedot[k] = 0;
+            L.yedot[k] = 0;
+        } else {  // lifted wheel: xe, ye, omega were zeroed; the stale rates carry
+            L.xe[k] = 0;
+            L.ye[k] = 0;
+            L.om[k] = 0;
+            L.xedot[k] = xedotnb[k];
+            L.yedot[k] = yedotnb[k];
+        }
+    }
+    // vehicle-to-tire transform
+    {
+        const double vsyfb = vsyb[0] + vsyb[1] + T.sd * (vsxinb[0] + vsxinb[1]);
+        sdb += T.vsyf * (vsxinb[0] + vsxinb[1]);
+        cdb += (T.u - T.wcf) * vsxinb[0] + (T.u + T.wcf) * vsxinb[1];
+        ub += T.cd * (vsxinb[0] + vsxinb[1]) + vsxinb[2] + vsxinb[3];
+        const double wcfb = T.cd * (vsxinb[1] - vsxinb[0]);
+        const double wcrb = vsxinb[3] - vsxinb[2];
+        const double vsyrb = vsyb[2] + vsyb[3];
+        wzb += K(K_A) * vsyfb - K(K_B) * vsyrb + K(K_CF2) * wcfb + K(K_CR2) * wcrb;
+        vb += vsyfb + vsyrb;
+        kb.add(KB_A, T.wz * vsyfb);
+    }
+    // wheel angle
+    steerb += T.dslope * (T.cd * sdb - T.sd * cdb);
+    // tire loads (with the previous step's accelerations)
+    double udot_oldb, vdot_oldb;
+    {
+        const double g0 = T.fzarg[0] > 0 ? 1.0 : 0.0, g1 = T.fzarg[1] > 0 ? 1.0 : 0.0;
+        const double g2 = T.fzarg[2] > 0 ? 1.0 : 0.0, g3 = T.fzarg[3] > 0 ? 1.0 : 0.0;
+        const double Afb = fzb[0] * g0 + fzb[1] * g1, Bfb = -fzb[0] * g0 + fzb[1] * g1;
+        const double Arb = fzb[2] * g2 + fzb[3] * g3, Brb = -fzb[2] * g2 + fzb[3] * g3;
+        const double Z4b = -Afb + Arb;
+        kb.add(KB_Z1F, Afb);
+        kb.add(KB_Z1R, Arb);
+        const double latb = K(K_Z2F) * Bfb + K(K_Z2R) * Brb;
+        kb.add(KB_Z2F, T.lat * Bfb);
+        kb.add(KB_Z2R, T.lat * Brb);
+        phib += K(K_Z3FK) * Bfb + K(K_Z3RK) * Brb;
+        wxb += K(K_Z3FB) * Bfb + K(K_Z3RB) * Brb;
+        const double lonb = K(K_Z4) * Z4b;
+        kb.add(KB_Z4, T.lon * Z4b);
+        wzb += T.u * latb - T.v * lonb;
+        ub += T.wz * latb;
+        vb += -T.wz * lonb;
+        vdot_oldb = latb;
+        udot_oldb = lonb;
+    }
+    // L.x, L.y are unchanged (x and y enter the next state with unit weight)
+    L.u = ub;
+    L.v = vb;
+    L.psi = psib;
+    L.wz = wzb;
+    L.phi = phib;
+    L.wx = wxb;
+    L.udot = udot_oldb;
+    L.vdot = vdot_oldb;
+    L.crank = C.tcbool ? crankb : 0.0;
+}
+
+}  // namespace lfdm

@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "../../include/lfdm.h"
+#include "adjoint18.h"
 #include "json_loader.h"
 #include "kernels.h"
 
@@ -110,6 +111,11 @@ struct lfdm_solver {
     DevBuf<unsigned char> d_classes, d_classes_f;
     DevBuf<uint32_t> d_status;
     DevBuf<unsigned> d_bad;
+    // differentiable rollout (lfdm_traj18_*)
+    DevBuf<double> d_adj_ckpt, d_adj_tape, d_adj_kbar;
+    unsigned adj_nsteps = 0, adj_ckpt = 0;
+    bool adj_valid = false;
+    double adj_fwd_ms = 0, adj_bwd_ms = 0;
     bool rows_device_only = false;  // driver rows live only in d_rows (bulk upload path)
     bool dirty_params = true, dirty_classes = true, dirty_tables = true, dirty_states = true;
     bool device_newer = false;  // device state newer than host mirror
@@ -927,6 +933,94 @@ int lfdm_solve_range(lfdm_solver* h, double t_begin, double t_end) {
     int rc = check_ready(h, true);
     if (rc) return rc;
     return run_windows(h, t_begin, t_end, true, CTL_TABLE, 0, 0, 0, nullptr, nullptr, 0, false);
+}
+
+static int traj_guard(lfdm_solver* h, const double* ctl, const double* ref, unsigned nsteps, unsigned ckpt) {
+    if (!ctl || !ref || nsteps == 0 || ckpt == 0) return h->fail(LFDM_ERR_ARG, "null array or zero steps");
+    if (h->model != LFDM_MODEL_18) return h->fail(LFDM_ERR_ARG, "the differentiable rollout is the 18-DOF model's");
+    if (h->tire_type == LFDM_TIRE_TMEASY_NR) return h->fail(LFDM_ERR_ARG, "the differentiable rollout needs TMeasy");
+    if (h->precision != LFDM_PREC_FP64) return h->fail(LFDM_ERR_ARG, "the differentiable rollout is FP64");
+    for (const lfdm_class18& c : h->classes)
+        if (c.throttleMod) return h->fail(LFDM_ERR_ARG, "throttleMod is not differentiated");
+    int rc = check_ready(h, false);
+    if (rc) return rc;
+    return sync_device(h);
+}
+
+static AdjLaunch traj_launch(lfdm_solver* h, const double* ctl, const double* ref, unsigned nsteps, double weight_u,
+                             unsigned ckpt) {
+    AdjLaunch A;
+    A.n = (int)h->N;
+    A.npad = h->npad;
+    A.nsteps = (int)nsteps;
+    A.ckpt = (int)ckpt;
+    A.dt = h->step;
+    A.weight_u = weight_u;
+    A.K = h->d_K.p;
+    A.classes = reinterpret_cast<const ClassDev18*>(h->d_classes.p);
+    A.class_of = h->d_class_of.p;
+    A.params = h->d_params.p;
+    A.S0 = h->d_S.p;
+    A.ctl = ctl;
+    A.ref = ref;
+    A.ckpts = h->d_adj_ckpt.p;
+    A.tape = h->d_adj_tape.p;
+    A.kbar = h->d_adj_kbar.p;
+    return A;
+}
+
+int lfdm_traj18_forward(lfdm_solver* h, const double* ctl, const double* ref, unsigned nsteps, double weight_u,
+                        unsigned ckpt_every, double* loss) {
+    if (!h) return LFDM_ERR_ARG;
+    if (!loss) return h->fail(LFDM_ERR_ARG, "null loss array");
+    int rc = traj_guard(h, ctl, ref, nsteps, ckpt_every);
+    if (rc) return rc;
+    const size_t nseg = (nsteps + ckpt_every - 1) / ckpt_every;
+    CK(h->d_adj_ckpt.ensure(nseg * (size_t)traj18_ckpt_fields() * h->npad));
+    AdjLaunch A = traj_launch(h, ctl, ref, nsteps, weight_u, ckpt_every);
+    A.loss = loss;
+    CK(cudaEventRecord(h->ev0, h->stream));
+    CK(launch_traj18_forward(A, h->stream));
+    CK(cudaEventRecord(h->ev1, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    h->adj_fwd_ms = ms;
+    h->adj_nsteps = nsteps;
+    h->adj_ckpt = ckpt_every;
+    h->adj_valid = true;
+    return LFDM_OK;
+}
+
+int lfdm_traj18_backward(lfdm_solver* h, const double* ctl, const double* ref, unsigned nsteps, double weight_u,
+                         unsigned ckpt_every, double* grad_ctl, double* grad_params, double* grad_state0) {
+    if (!h) return LFDM_ERR_ARG;
+    if (!grad_ctl || !grad_params) return h->fail(LFDM_ERR_ARG, "null gradient array");
+    int rc = traj_guard(h, ctl, ref, nsteps, ckpt_every);
+    if (rc) return rc;
+    if (!h->adj_valid || h->adj_nsteps != nsteps || h->adj_ckpt != ckpt_every)
+        return h->fail(LFDM_ERR_STATE, "call lfdm_traj18_forward with the same steps and checkpoint interval first");
+    CK(h->d_adj_tape.ensure((size_t)ckpt_every * traj18_tape_doubles_per_step() * h->npad));
+    CK(h->d_adj_kbar.ensure((size_t)30 * h->npad));
+    AdjLaunch A = traj_launch(h, ctl, ref, nsteps, weight_u, ckpt_every);
+    A.grad_ctl = grad_ctl;
+    A.grad_params = grad_params;
+    A.grad_state0 = grad_state0;
+    CK(cudaEventRecord(h->ev0, h->stream));
+    CK(launch_traj18_backward(A, h->stream));
+    CK(cudaEventRecord(h->ev1, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    h->adj_bwd_ms = ms;
+    return LFDM_OK;
+}
+
+int lfdm_traj18_last_ms(lfdm_solver* h, double* forward_ms, double* backward_ms) {
+    if (!h) return LFDM_ERR_ARG;
+    if (forward_ms) *forward_ms = h->adj_fwd_ms;
+    if (backward_ms) *backward_ms = h->adj_bwd_ms;
+    return LFDM_OK;
 }
 
 int lfdm_solve(lfdm_solver* h) {

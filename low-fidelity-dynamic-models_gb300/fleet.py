@@ -138,6 +138,12 @@ def initial_states(cls: Class18, params: np.ndarray, rng: np.random.Generator,
     speed, and the crank spins at that speed (converter locked)."""
     n = params.shape[0]
     u0 = rng.uniform(u0_range[0], u0_range[1], size=n)
+    return states_at_speed(cls, params, u0)
+
+
+def states_at_speed(cls: Class18, params: np.ndarray, u0: np.ndarray) -> np.ndarray:
+    """initial_states with the given initial speeds u0 [n]."""
+    n = params.shape[0]
     s = np.zeros((n, S_COUNT), dtype=np.float64)
     s[:, S["u"]] = u0
     w = u0 / params[:, P["r0"]]
@@ -151,6 +157,26 @@ def initial_states(cls: Class18, params: np.ndarray, rng: np.random.Generator,
     s[:, S["current_gr"]] = gear
     s[:, S["crankomega"]] = w / gears[gear]
     return s
+
+
+def clothoid_refs(n: int, nsteps: int, dt: float, rng: np.random.Generator, curvature=(-0.05, 0.05),
+                  speed=(5.0, 25.0)) -> tuple[np.ndarray, np.ndarray]:
+    """Seeded reference paths for the differentiable rollout: per vehicle a clothoid segment from the
+    origin along +x whose curvature grows linearly from 0 to kappa ~ U[curvature] 1/m over the
+    horizon, traversed at speed v ~ U[speed] m/s. Returns (ref [nsteps][3][n] = {x, y, yaw} at the
+    end of each step, v [n])."""
+    kappa = rng.uniform(curvature[0], curvature[1], size=n)
+    v = rng.uniform(speed[0], speed[1], size=n)
+    sub = 8  # integration sub-steps per time step
+    ts = np.arange(1, nsteps * sub + 1) * (dt / sub)
+    S = v * nsteps * dt
+    s = ts[:, None] * v[None, :]
+    psi = kappa[None, :] * s * s / (2.0 * S[None, :])
+    ds = v * dt / sub
+    x = np.cumsum(np.cos(psi) * ds[None, :], axis=0)
+    y = np.cumsum(np.sin(psi) * ds[None, :], axis=0)
+    ref = np.stack([x[sub - 1::sub], y[sub - 1::sub], psi[sub - 1::sub]], axis=1)
+    return np.ascontiguousarray(ref), v
 
 
 def fleet18(n: int, seed: int = 20261203, horizon: float = 10.0, table_dt: float = 0.01,
