@@ -51,6 +51,8 @@ def _args():
     ap.add_argument("--no-models", action="store_true", help="skip the 11/24-DOF throughput lines")
     ap.add_argument("--no-fleet", action="store_true", help="skip the mixed-DOF fleet line")
     ap.add_argument("--fleet-vehicles", type=int, default=250_000)
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-rollout line")
+    ap.add_argument("--adjoint-vehicles", type=int, default=65_536)
     ap.add_argument("--error-vehicles", type=int, default=65536)
     ap.add_argument("--error-horizon", type=float, default=20.0)
     ap.add_argument("--cpu-sample", type=int, default=8192, help="vehicles in the CPU-baseline sample")
@@ -315,6 +317,49 @@ def _fleet_bench(lfdm, fleet, dev, n: int, torch) -> dict:
             "speedup_vs_per_group": value / base_value, "finite_states": finite}
 
 
+def _adjoint_bench(lfdm, fleet, dev, n: int, nsteps: int, torch) -> dict:
+    """The differentiable-rollout config: 18-DOF FP64, n vehicles, nsteps steps of 1e-3 s, a
+    checkpoint every 100 steps, seeded clothoid reference paths (curvature U[-0.05, 0.05] 1/m, speed
+    U[5, 25] m/s), loss = squared lateral + heading error + 1e-3 |u|^2; gradients with respect to
+    the per-step controls and 5 parameters; one forward and one backward, CUDA-event timed."""
+    rng = np.random.default_rng(SEED + 4)
+    dt = 1e-3
+    cls, base = fleet.suv18()
+    params = fleet.jitter_params(base, n, rng)
+    ref, v = fleet.clothoid_refs(n, nsteps, dt, rng)
+    sol = lfdm.d18SolverHalfImplicitGPU(n, device=dev)
+    sol.construct_class(cls, params)
+    sol.set_states(fleet.states_at_speed(cls, params, v))
+    sol.SetTimeStep(dt)
+    gdev = torch.device("cuda", dev)
+    t = np.arange(nsteps) * dt
+    ctl = np.zeros((nsteps, 3, n))
+    ctl[:, 0, :] = rng.uniform(-0.08, 0.08, n)[None, :] * np.sin(2 * np.pi * rng.uniform(0.5, 2.0, n)[None, :]
+                                                                 * t[:, None])
+    ctl[:, 1, :] = rng.uniform(0.2, 0.5, n)[None, :]
+    c = torch.tensor(ctl, dtype=torch.float64, device=gdev)
+    r = torch.tensor(ref, dtype=torch.float64, device=gdev)
+    del ctl, ref
+    ro = lfdm.Rollout18(sol, nsteps, ckpt_every=100)
+    loss = torch.empty(n, dtype=torch.float64, device=gdev)
+    gc = torch.empty_like(c)
+    gp = torch.empty(5, n, dtype=torch.float64, device=gdev)
+    # one untimed pass (module load, buffer allocation), then the measured pass
+    for _ in range(2):
+        ro.forward_raw(c, r, loss)
+        ro.backward_raw(c, r, gc, gp)
+    fwd, bwd = ro.last_ms()
+    finite = bool(torch.isfinite(gc).all().item() and torch.isfinite(gp).all().item())
+    sol.close()
+    vs = n * nsteps
+    return {"config": f"18-DOF FP64 adjoint, {n} vehicles, {nsteps} steps (dt 1e-3 s), checkpoint every 100 "
+                      "steps, clothoid reference paths, gradients for 3 x nsteps controls and 5 parameters",
+            "forward_ms": fwd, "backward_ms": bwd, "backward_over_forward": bwd / fwd,
+            "forward_vehicle_steps_per_s": vs / (fwd * 1e-3), "gradients_finite": finite,
+            "checked": "tests/test_gpu_adjoint18.py: central differences h=1e-6 of the GPU rollout and of the "
+                       "reference algorithm (oracle)"}
+
+
 def run_ours(a, dist: Dist):
     import torch
 
@@ -439,6 +484,9 @@ def run_ours(a, dist: Dist):
     fleet_line = None
     if not a.no_fleet:
         fleet_line = _fleet_bench(lfdm, fleet, dev, a.fleet_vehicles, torch)
+    adjoint_line = None
+    if not a.no_adjoint:
+        adjoint_line = _adjoint_bench(lfdm, fleet, dev, a.adjoint_vehicles, 2000, torch)
 
     cpu = None
     if dist.rank == 0:
@@ -468,6 +516,7 @@ def run_ours(a, dist: Dist):
             "mixed": mixed,
             "models": models,
             "fleet": fleet_line,
+            "adjoint": adjoint_line,
             "gpu_launches": launches,
             "clocks": clocks,
             "wall_s_timed": wall,

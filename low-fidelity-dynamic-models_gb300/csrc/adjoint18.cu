@@ -18,6 +18,7 @@
 
 #include "adjoint18.h"
 #include "dof18_adjoint.cuh"
+#include "window_common.cuh"
 
 namespace lfdm {
 
@@ -71,12 +72,54 @@ __device__ __forceinline__ double step_loss(const AdjLaunch& A, int k, int vid, 
     return fma(el, el, eh * eh) + A.weight_u * fma(st, st, fma(th, th, br * br));
 }
 
+// Shared memory of the rollout kernels: the classes (when cls_smem), the derived constants of the
+// block's vehicles [K18_COUNT][blockDim] and, for the backward kernel, the adjoints of the
+// parameter-dependent constants [KB_COUNT][blockDim]. Every access of the inner step then stays in
+// shared memory instead of interleaving with the tape's HBM stores and loads. Both kernels are
+// register-bound to two 128-thread blocks per SM; the classes are staged only while two blocks
+// still fit in the SM's 228 KB (1 KB of it reserved per block).
+size_t traj18_smem(int threads, int nclasses, bool backward, bool* cls_smem) {
+    const size_t base = (size_t)(K18_COUNT + (backward ? KB_COUNT : 0)) * threads * sizeof(double);
+    const size_t cls = (size_t)nclasses * sizeof(ClassDev18);
+    const bool in = nclasses <= kMaxSmemClasses && 2 * (base + cls + 1024) <= 228 * 1024;
+    if (cls_smem) *cls_smem = in;
+    return base + (in ? cls : 0);
+}
+
+struct RolloutSmem {
+    const ClassDev18* cls;  // classes (shared or global)
+    double* ks;             // [K18_COUNT][blockDim]
+    double* kb;             // [KB_COUNT][blockDim] (backward)
+};
+
+__device__ __forceinline__ RolloutSmem stage_rollout(const AdjLaunch& A, unsigned char* smem, int vid) {
+    const int tid = threadIdx.x;
+    RolloutSmem r;
+    r.cls = A.cls_smem ? reinterpret_cast<const ClassDev18*>(smem) : A.classes;
+    r.ks = reinterpret_cast<double*>(smem + (A.cls_smem ? (size_t)A.nclasses * sizeof(ClassDev18) : 0));
+    r.kb = r.ks + (size_t)K18_COUNT * blockDim.x;
+    if (A.cls_smem) {
+        const int4* src = reinterpret_cast<const int4*>(A.classes);
+        int4* dst = reinterpret_cast<int4*>(smem);
+        const int words = (int)(A.nclasses * sizeof(ClassDev18) / 16);
+        for (int i = tid; i < words; i += blockDim.x) dst[i] = __ldg(src + i);
+    }
+    if (vid < A.n) {
+#pragma unroll 4
+        for (int k = 0; k < K18_COUNT; ++k) r.ks[k * blockDim.x + tid] = __ldg(A.K + (size_t)k * A.npad + vid);
+    }
+    __syncthreads();
+    return r;
+}
+
 __global__ void __launch_bounds__(128) traj18_forward_kernel(const AdjLaunch A) {
+    extern __shared__ __align__(16) unsigned char smem[];
     const int vid = blockIdx.x * blockDim.x + threadIdx.x;
+    const RolloutSmem sm = stage_rollout(A, smem, vid);
     if (vid >= A.n) return;
     const size_t np = (size_t)A.npad;
-    const KView K{A.K + vid, A.npad};
-    const ClassDev18& C = A.classes[__ldg(A.class_of + vid)];
+    const KView K{sm.ks + threadIdx.x, (int)blockDim.x};
+    const ClassDev18& C = sm.cls[__ldg(A.class_of + vid)];
     VehC v;
     VehAux va;
     TireC ts[4];
@@ -162,14 +205,16 @@ __device__ void dK_dparam(const double* p, int which, double* out) {
 }
 
 __global__ void __launch_bounds__(128) traj18_backward_kernel(const AdjLaunch A) {
+    extern __shared__ __align__(16) unsigned char smem[];
     const int vid = blockIdx.x * blockDim.x + threadIdx.x;
+    const RolloutSmem sm = stage_rollout(A, smem, vid);
     if (vid >= A.n) return;
     const size_t np = (size_t)A.npad, nu = (size_t)A.n;
-    const KView K{A.K + vid, A.npad};
-    const ClassDev18& C = A.classes[__ldg(A.class_of + vid)];
-    const KBar kb{A.kbar + vid, A.npad};
+    const KView K{sm.ks + threadIdx.x, (int)blockDim.x};
+    const ClassDev18& C = sm.cls[__ldg(A.class_of + vid)];
+    const KBar kb{sm.kb + threadIdx.x, (int)blockDim.x};
 #pragma unroll 1
-    for (int i = 0; i < KB_COUNT; ++i) kb.base[i * (size_t)A.npad] = 0.0;
+    for (int i = 0; i < KB_COUNT; ++i) kb.base[i * blockDim.x] = 0.0;
     Adj18 L = {};
     const int nseg = (A.nsteps + A.ckpt - 1) / A.ckpt;
     for (int seg = nseg - 1; seg >= 0; --seg) {
@@ -181,31 +226,24 @@ __global__ void __launch_bounds__(128) traj18_backward_kernel(const AdjLaunch A)
         load_ckpt(A.ckpts + (size_t)seg * kCkptFields * np + vid, np, v, ts);
         for (int k = k0; k < k1; ++k) {
             const double* U = A.ctl + (size_t)k * 3 * nu + vid;
-            StepTape T;
+            const TapeRef T{A.tape + (size_t)(k - k0) * kStepTapeDoubles * np + vid, np};
             fwd18_tape(v, va, ts, ta, T, K, C, __ldg(U), __ldg(U + nu), __ldg(U + 2 * nu), A.dt);
-            const double* tp = reinterpret_cast<const double*>(&T);
-            double* dst = A.tape + (size_t)(k - k0) * kStepTapeDoubles * np + vid;
-#pragma unroll 8
-            for (int f = 0; f < kStepTapeDoubles; ++f) dst[f * np] = tp[f];
         }
         for (int k = k1 - 1; k >= k0; --k) {
-            StepTape T;
-            double* tp = reinterpret_cast<double*>(&T);
-            const double* src = A.tape + (size_t)(k - k0) * kStepTapeDoubles * np + vid;
-#pragma unroll 8
-            for (int f = 0; f < kStepTapeDoubles; ++f) tp[f] = src[f * np];
+            const TapeRef T{A.tape + (size_t)(k - k0) * kStepTapeDoubles * np + vid, np};
             // loss of step k on the state after it
             {
                 const double* R = A.ref + (size_t)k * 3 * nu + vid;
                 const double xr = __ldg(R), yr = __ldg(R + nu), pr = __ldg(R + 2 * nu);
                 double sr, cr;
                 sincos(pr, &sr, &cr);
-                const double el = fma(-(T.x1 - xr), sr, (T.y1 - yr) * cr);
+                const double el = fma(-(T.at(TS_(x1)) - xr), sr, (T.at(TS_(y1)) - yr) * cr);
                 L.x += -2.0 * el * sr;
                 L.y += 2.0 * el * cr;
-                L.psi += 2.0 * (T.psi1 - pr);
+                L.psi += 2.0 * (T.at(TS_(psi1)) - pr);
             }
-            double sb = 2.0 * A.weight_u * T.steer, tb = 2.0 * A.weight_u * T.thr, bb = 2.0 * A.weight_u * T.brk;
+            double sb = 2.0 * A.weight_u * T.at(TS_(steer)), tb = 2.0 * A.weight_u * T.at(TS_(thr)),
+                   bb = 2.0 * A.weight_u * T.at(TS_(brk));
             rev18(T, K, C, kb, A.dt, L, sb, tb, bb);
             double* G = A.grad_ctl + (size_t)k * 3 * nu + vid;
             G[0] = sb;
@@ -214,8 +252,9 @@ __global__ void __launch_bounds__(128) traj18_backward_kernel(const AdjLaunch A)
         }
     }
     if (A.grad_state0) {
+        // fully unrolled so that L stays in registers (a runtime index would put it on the stack)
         const double* l = &L.x;
-#pragma unroll 1
+#pragma unroll
         for (int f = 0; f < kAdj18Count; ++f) A.grad_state0[f * nu + vid] = l[f];
     }
     // parameter gradients
@@ -226,20 +265,27 @@ __global__ void __launch_bounds__(128) traj18_backward_kernel(const AdjLaunch A)
         dK_dparam(p, j, d);
         double gsum = 0;
 #pragma unroll 1
-        for (int i = 0; i < KB_COUNT; ++i) gsum = fma(kb.base[i * (size_t)A.npad], d[i], gsum);
+        for (int i = 0; i < KB_COUNT; ++i) gsum = fma(kb.base[i * blockDim.x], d[i], gsum);
         A.grad_params[j * nu + vid] = gsum;
     }
 }
 
-cudaError_t launch_traj18_forward(const AdjLaunch& A, cudaStream_t stream) {
+static cudaError_t launch_rollout(void (*kern)(const AdjLaunch), const AdjLaunch& A, bool backward,
+                                  cudaStream_t stream) {
     if (A.n <= 0 || A.nsteps <= 0) return cudaSuccess;
-    traj18_forward_kernel<<<(A.n + 127) / 128, 128, 0, stream>>>(A);
+    constexpr int threads = 128;
+    AdjLaunch L = A;
+    const size_t smem = traj18_smem(threads, A.nclasses, backward, &L.cls_smem);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<(A.n + threads - 1) / threads, threads, smem, stream>>>(L);
     return cudaGetLastError();
 }
+cudaError_t launch_traj18_forward(const AdjLaunch& A, cudaStream_t stream) {
+    return launch_rollout(traj18_forward_kernel, A, false, stream);
+}
 cudaError_t launch_traj18_backward(const AdjLaunch& A, cudaStream_t stream) {
-    if (A.n <= 0 || A.nsteps <= 0) return cudaSuccess;
-    traj18_backward_kernel<<<(A.n + 127) / 128, 128, 0, stream>>>(A);
-    return cudaGetLastError();
+    return launch_rollout(traj18_backward_kernel, A, true, stream);
 }
 size_t traj18_tape_doubles_per_step() { return (size_t)kStepTapeDoubles; }
 int traj18_ckpt_fields() { return kCkptFields; }

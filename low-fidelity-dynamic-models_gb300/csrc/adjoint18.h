@@ -19,6 +19,8 @@ struct AdjLaunch {
     double dt = 1e-3, weight_u = 1e-3;
     const double* K = nullptr;             // [K18 count][npad]
     const ClassDev18* classes = nullptr;
+    int nclasses = 0;
+    bool cls_smem = false;                 // classes staged in shared memory (set by the launcher)
     const int32_t* class_of = nullptr;     // [n]
     const double* params = nullptr;        // [n][LFDM_P_COUNT] (device)
     const double* S0 = nullptr;            // [LFDM_S_COUNT][npad] initial states (SoA)
@@ -27,7 +29,6 @@ struct AdjLaunch {
     double* loss = nullptr;                // [n]
     double* ckpts = nullptr;               // [nsteps / ckpt][checkpoint fields][npad]
     double* tape = nullptr;                // [ckpt][tape doubles][npad]
-    double* kbar = nullptr;                // [30][npad] adjoints of the parameter-dependent constants
     double* grad_ctl = nullptr;            // [nsteps][3][n]
     double* grad_params = nullptr;         // [5][n]: mass, Jz, a, friction scale, kt
     double* grad_state0 = nullptr;         // [31][n] or nullptr
@@ -36,6 +37,7 @@ struct AdjLaunch {
 cudaError_t launch_traj18_forward(const AdjLaunch& A, cudaStream_t stream);
 cudaError_t launch_traj18_backward(const AdjLaunch& A, cudaStream_t stream);
 size_t traj18_tape_doubles_per_step();
+size_t traj18_smem(int threads, int nclasses, bool backward, bool* cls_smem);
 int traj18_ckpt_fields();
 int traj18_state_adjoints();
 

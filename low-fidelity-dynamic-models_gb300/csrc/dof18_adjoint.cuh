@@ -15,6 +15,8 @@
 // tires, linear or mapped steering, with or without torque converter, throttleMod off.
 #pragma once
 
+#include <cstddef>
+
 #include "dof18_device.cuh"
 
 namespace lfdm {
@@ -87,7 +89,7 @@ struct TireTape {
     double dfx0, dfy0, fxm, fym, fxs, fys, sxm, sym, sxs, sys;
     double ssum, fsum, fxd, fyd, hsxn, hsyn, ihx, ihy, sxn, syn, sc, isc, calpha, salpha, qpos;
     double df0, fm, sm, fs, ss, fos;
-    double vtxs, vtys, numx, numy, denx, deny, xedot, yedot;
+    double vtxs, vtys, numx, numy, denx, deny, xedot, yedot, idenx, ideny, issum, ifsum, ivta;
     double Fx, Fy, fxstr, fystr, clx, cly, wxw, wyw, dwx, dwy;  // clx/cly: -1/0/+1 clamp side
     double fx, fy, My, sgn;
 };
@@ -110,6 +112,21 @@ struct StepTape {
 };
 constexpr int kStepTapeDoubles = (int)(sizeof(StepTape) / sizeof(double));
 static_assert(sizeof(StepTape) % sizeof(double) == 0, "the step tape is a flat array of doubles");
+constexpr int kTireTapeDoubles = (int)(sizeof(TireTape) / sizeof(double));
+
+// A vehicle's column of the step tape in HBM ([tape doubles][npad]): field i lives at p[i * s]. The
+// forward recomputation writes each field once, where it is computed, and the reverse sweep reads
+// it where it is used, so no tape is held in registers or on the stack.
+struct TapeRef {
+    double* p;
+    size_t s;
+    __device__ __forceinline__ double& at(int i) const { return p[i * s]; }
+};
+#define TS_(f) ((int)(offsetof(StepTape, f) / sizeof(double)))
+#define TT_(f) ((int)(offsetof(TireTape, f) / sizeof(double)))
+__device__ __forceinline__ TapeRef tire_ref(const TapeRef& T, int k) {
+    return {T.p + (size_t)(TS_(t) + k * kTireTapeDoubles) * T.s, T.s};
+}
 
 // map slope of the segment getMapY uses at x (0 where the map clamps)
 __device__ __forceinline__ double map_slope(const MapDev& m, double x) {
@@ -138,14 +155,14 @@ __device__ __forceinline__ void sine_step_w(double x, double& y, double& dy) {
 // forward with tape (the arithmetic of tire_rhs_tm / tire_core_tm / powertrain_rhs / step18)
 
 template <bool kSteered>
-__device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, TireTape& T, const KView& K, double c, double s) {
+__device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, const TapeRef& T, const KView& K, double c, double s) {
     const double fz = ta.fz;
-    T.fz = fz;
-    T.om = ts.omega;
-    T.xe = ts.xe;
-    T.ye = ts.ye;
-    T.vsy = ta.vsy;
-    T.on = fz > 0 ? 1.0 : 0.0;
+    T.at(TT_(fz)) = fz;
+    T.at(TT_(om)) = ts.omega;
+    T.at(TT_(xe)) = ts.xe;
+    T.at(TT_(ye)) = ts.ye;
+    T.at(TT_(vsy)) = ta.vsy;
+    T.at(TT_(on)) = fz > 0 ? 1.0 : 0.0;
     if (fz <= 0) {
         ts.xe = 0;
         ts.ye = 0;
@@ -155,48 +172,49 @@ __device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, TireTape& 
         ta.fx = 0;
         ta.fy = 0;
         ta.My = 0;
-        T.rStat = ta.rStat;
-        T.fx = T.fy = T.My = 0;
+        T.at(TT_(rStat)) = ta.rStat;
+        T.at(TT_(fx)) = T.at(TT_(fy)) = T.at(TT_(My)) = 0;
         return;
     }
     ta.xt = fz * K(K_INVKT);
     ta.rStat = K(K_R0) - ta.xt;
-    T.xt = ta.xt;
-    T.rStat = ta.rStat;
+    T.at(TT_(xt)) = ta.xt;
+    T.at(TT_(rStat)) = ta.rStat;
     if (fz <= K(K_FZRD)) {
-        T.fzrd = 1.0;
-        T.rdynco = fma(K(K_DRD), fma(fz, K(K_INVPN), -1.0), K(K_RDPN));
+        T.at(TT_(fzrd)) = 1.0;
+        T.at(TT_(rdynco)) = fma(K(K_DRD), fma(fz, K(K_INVPN), -1.0), K(K_RDPN));
     } else {
-        T.fzrd = 0.0;
-        T.rdynco = K(K_RDCRIT);
+        T.at(TT_(fzrd)) = 0.0;
+        T.at(TT_(rdynco)) = K(K_RDCRIT);
     }
-    const double r_eff = fma(T.rdynco, ta.xt, ta.rStat);
-    T.r_eff = r_eff;
+    const double r_eff = fma(T.at(TT_(rdynco)), ta.xt, ta.rStat);
+    T.at(TT_(r_eff)) = r_eff;
     const double omega = ts.omega;
     const double vsy = ta.vsy;
     const double vsx = fma(-omega, r_eff, ta.vsx);
-    T.vsx = vsx;
+    T.at(TT_(vsx)) = vsx;
     const double rw = r_eff * fabs(omega);
     const double vta = rw + 0.01;
     const double ivta = 1.0 / vta;
-    T.rw = rw;
-    T.vta = vta;
+    T.at(TT_(rw)) = rw;
+    T.at(TT_(vta)) = vta;
+    T.at(TT_(ivta)) = ivta;
     const double sx = -vsx * ivta;
     double sy;
     if (kSteered) {
-        T.N = vsy * c - vta * s;
-        T.D = vta * c + vsy * s;
+        T.at(TT_(N)) = vsy * c - vta * s;
+        T.at(TT_(D)) = vta * c + vsy * s;
         sy = -(vsy * c - vta * s) / (vta * c + vsy * s);
     } else {
         sy = -vsy * ivta;
     }
-    T.sx = sx;
-    T.sy = sy;
+    T.at(TT_(sx)) = sx;
+    T.at(TT_(sy)) = sy;
     const double fzc = fmin(fz, K(K_PNMAX));
-    T.fzc = fzc;
-    T.fzcl = fz > K(K_PNMAX) ? 1.0 : 0.0;
+    T.at(TT_(fzc)) = fzc;
+    T.at(TT_(fzcl)) = fz > K(K_PNMAX) ? 1.0 : 0.0;
     const double fzn = fzc * K(K_INVPN);
-    T.fzn = fzn;
+    T.at(TT_(fzn)) = fzn;
     const double dfx0 = fzn * fma(-K(K_Q2DFX0), fzn, K(K_Q1DFX0));
     const double dfy0 = fzn * fma(-K(K_Q2DFY0), fzn, K(K_Q1DFY0));
     const double fxm = fzn * fma(-K(K_Q2FXM), fzn, K(K_Q1FXM));
@@ -208,8 +226,8 @@ __device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, TireTape& 
     const double sym = fma(K(K_DSYM), fzn1, K(K_LSYM));
     const double sxs = fma(K(K_DSXS), fzn1, K(K_LSXS));
     const double sys = fma(K(K_DSYS), fzn1, K(K_LSYS));
-    T.dfx0 = dfx0; T.dfy0 = dfy0; T.fxm = fxm; T.fym = fym; T.fxs = fxs; T.fys = fys;
-    T.sxm = sxm; T.sym = sym; T.sxs = sxs; T.sys = sys;
+    T.at(TT_(dfx0)) = dfx0; T.at(TT_(dfy0)) = dfy0; T.at(TT_(fxm)) = fxm; T.at(TT_(fym)) = fym; T.at(TT_(fxs)) = fxs; T.at(TT_(fys)) = fys;
+    T.at(TT_(sxm)) = sxm; T.at(TT_(sym)) = sym; T.at(TT_(sxs)) = sxs; T.at(TT_(sys)) = sys;
     const double ssum = sxm + sym;
     const double fxd = fxm * dfy0, fyd = fym * dfx0;
     const double fsum = fxd + fyd;
@@ -219,7 +237,7 @@ __device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, TireTape& 
     const double hsyn = fma(sym, issum, fyd * ifsum);
     const double rh = 1.0 / (hsxn * hsyn);
     const double ihx = hsyn * rh, ihy = hsxn * rh;
-    T.ssum = ssum; T.fsum = fsum; T.fxd = fxd; T.fyd = fyd; T.hsxn = hsxn; T.hsyn = hsyn; T.ihx = ihx; T.ihy = ihy;
+    T.at(TT_(ssum)) = ssum; T.at(TT_(fsum)) = fsum; T.at(TT_(issum)) = issum; T.at(TT_(ifsum)) = ifsum; T.at(TT_(fxd)) = fxd; T.at(TT_(fyd)) = fyd; T.at(TT_(hsxn)) = hsxn; T.at(TT_(hsyn)) = hsyn; T.at(TT_(ihx)) = ihx; T.at(TT_(ihy)) = ihy;
     const double sxn = sx * ihx;
     const double syn = sy * ihy;
     const double q = fma(sxn, sxn, syn * syn);
@@ -234,8 +252,8 @@ __device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, TireTape& 
         calpha = kSqrt2Over2;
         salpha = kSqrt2Over2;
     }
-    T.sxn = sxn; T.syn = syn; T.sc = sc; T.isc = isc; T.calpha = calpha; T.salpha = salpha;
-    T.qpos = q > 0 ? 1.0 : 0.0;
+    T.at(TT_(sxn)) = sxn; T.at(TT_(syn)) = syn; T.at(TT_(sc)) = sc; T.at(TT_(isc)) = isc; T.at(TT_(calpha)) = calpha; T.at(TT_(salpha)) = salpha;
+    T.at(TT_(qpos)) = q > 0 ? 1.0 : 0.0;
     auto hyp = [](double a, double b) { return sqrt(fma(a, a, b * b)); };
     const double df0 = hyp(dfx0 * calpha * hsxn, dfy0 * salpha * hsyn);
     const double fm = hyp(fxm * calpha, fym * salpha);
@@ -243,12 +261,12 @@ __device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, TireTape& 
     const double sm = hyp(sxm * cax, sym * say);
     const double fs = hyp(fxs * calpha, fys * salpha);
     const double ss = hyp(sxs * cax, sys * say);
-    T.df0 = df0; T.fm = fm; T.sm = sm; T.fs = fs; T.ss = ss;
+    T.at(TT_(df0)) = df0; T.at(TT_(fm)) = fm; T.at(TT_(sm)) = sm; T.at(TT_(fs)) = fs; T.at(TT_(ss)) = ss;
     double f, fos;
     tmxy(f, fos, sc, df0, sm, fm, ss, fs);
-    T.fos = fos;
-    T.sgn = sgnd(omega);
-    ta.My = -K(K_RR) * fzc * ta.rStat * T.sgn;
+    T.at(TT_(fos)) = fos;
+    T.at(TT_(sgn)) = sgnd(omega);
+    ta.My = -K(K_RR) * fzc * ta.rStat * T.at(TT_(sgn));
     const double vtxs = fma(rw, hsxn, 0.01);
     const double vtys = fma(rw, hsyn, 0.01);
     const double cx = K(K_CX), cy = K(K_CY), dx = K(K_DX), dy = K(K_DY);
@@ -258,40 +276,42 @@ __device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, TireTape& 
     const double rd = 1.0 / (denx * deny);
     ts.xedot = numx * (deny * rd);
     ts.yedot = numy * (denx * rd);
-    T.vtxs = vtxs; T.vtys = vtys; T.numx = numx; T.numy = numy; T.denx = denx; T.deny = deny;
-    T.xedot = ts.xedot; T.yedot = ts.yedot;
+    T.at(TT_(idenx)) = deny * rd;
+    T.at(TT_(ideny)) = denx * rd;
+    T.at(TT_(vtxs)) = vtxs; T.at(TT_(vtys)) = vtys; T.at(TT_(numx)) = numx; T.at(TT_(numy)) = numy; T.at(TT_(denx)) = denx; T.at(TT_(deny)) = deny;
+    T.at(TT_(xedot)) = ts.xedot; T.at(TT_(yedot)) = ts.yedot;
     const double fxdyn = fma(dx, ts.xedot, cx * ts.xe);
     const double fydyn = fma(dy, ts.yedot, cy * ts.ye);
     const double Gx = fma(ts.xe, cx, ts.xedot * dx);
     const double Gy = fma(ts.ye, cy, ts.yedot * dy);
     const double fxstr = fmin(fmax(Gx, -K(K_FXMP2N)), K(K_FXMP2N));
     const double fystr = fmin(fmax(Gy, -K(K_FYMP2N)), K(K_FYMP2N));
-    T.Fx = fxdyn; T.Fy = fydyn; T.fxstr = fxstr; T.fystr = fystr;
-    T.clx = Gx > K(K_FXMP2N) ? 1.0 : (Gx < -K(K_FXMP2N) ? -1.0 : 0.0);
-    T.cly = Gy > K(K_FYMP2N) ? 1.0 : (Gy < -K(K_FYMP2N) ? -1.0 : 0.0);
+    T.at(TT_(Fx)) = fxdyn; T.at(TT_(Fy)) = fydyn; T.at(TT_(fxstr)) = fxstr; T.at(TT_(fystr)) = fystr;
+    T.at(TT_(clx)) = Gx > K(K_FXMP2N) ? 1.0 : (Gx < -K(K_FXMP2N) ? -1.0 : 0.0);
+    T.at(TT_(cly)) = Gy > K(K_FYMP2N) ? 1.0 : (Gy < -K(K_FYMP2N) ? -1.0 : 0.0);
     double wx, wy, dwx, dwy;
     sine_step_w(fabs(vsx), wx, dwx);
     sine_step_w(fabs(sy * vta), wy, dwy);
-    T.wxw = wx; T.wyw = wy; T.dwx = dwx; T.dwy = dwy;
+    T.at(TT_(wxw)) = wx; T.at(TT_(wyw)) = wy; T.at(TT_(dwx)) = dwx; T.at(TT_(dwy)) = dwy;
     ta.fx = (wx == 0.0) ? fxdyn : fma(wx, fxstr, (1. - wx) * fxdyn);
     ta.fy = (wy == 0.0) ? fydyn : fma(wy, fystr, (1. - wy) * fydyn);
-    T.fx = ta.fx;
-    T.fy = ta.fy;
-    T.My = ta.My;
+    T.at(TT_(fx)) = ta.fx;
+    T.at(TT_(fy)) = ta.fy;
+    T.at(TT_(My)) = ta.My;
 }
 
 // One step18<false> with its tape; v/va/ts/ta as in step18.
-__device__ __forceinline__ void fwd18_tape(VehC& v, VehAux& va, TireC* ts, TireAux* ta, StepTape& T, const KView& K,
+__device__ __forceinline__ void fwd18_tape(VehC& v, VehAux& va, TireC* ts, TireAux* ta, const TapeRef& T, const KView& K,
                                            const ClassDev18& C, double steering, double throttle, double braking,
                                            double dt) {
-    T.u = v.u; T.v = v.v; T.psi = v.psi; T.wz = v.wz; T.phi = v.phi; T.wx = v.wx;
-    T.udot = v.udot; T.vdot = v.vdot; T.crank = v.crank; T.gear = (double)v.gear;
-    T.steer = steering; T.thr = throttle; T.brk = braking;
+    T.at(TS_(u)) = v.u; T.at(TS_(v)) = v.v; T.at(TS_(psi)) = v.psi; T.at(TS_(wz)) = v.wz; T.at(TS_(phi)) = v.phi; T.at(TS_(wx)) = v.wx;
+    T.at(TS_(udot)) = v.udot; T.at(TS_(vdot)) = v.vdot; T.at(TS_(crank)) = v.crank; T.at(TS_(gear)) = (double)v.gear;
+    T.at(TS_(steer)) = steering; T.at(TS_(thr)) = throttle; T.at(TS_(brk)) = braking;
     {
         const double lat = fma(v.wz, v.u, v.vdot);
         const double lon = fma(-v.wz, v.v, v.udot);
-        T.lat = lat;
-        T.lon = lon;
+        T.at(TS_(lat)) = lat;
+        T.at(TS_(lon)) = lon;
         const double Z4 = K(K_Z4) * lon;
         const double Z2f = K(K_Z2F) * lat;
         const double Z3f = fma(K(K_Z3FK), v.phi, K(K_Z3FB) * v.wx);
@@ -299,10 +319,10 @@ __device__ __forceinline__ void fwd18_tape(VehC& v, VehAux& va, TireC* ts, TireA
         const double Z3r = fma(K(K_Z3RK), v.phi, K(K_Z3RB) * v.wx);
         const double Af = K(K_Z1F) - Z4, Bf = Z2f + Z3f;
         const double Ar = K(K_Z1R) + Z4, Br = Z2r + Z3r;
-        T.fzarg[0] = Af - Bf;
-        T.fzarg[1] = Af + Bf;
-        T.fzarg[2] = Ar - Br;
-        T.fzarg[3] = Ar + Br;
+        T.at(TS_(fzarg) + 0) = Af - Bf;
+        T.at(TS_(fzarg) + 1) = Af + Bf;
+        T.at(TS_(fzarg) + 2) = Ar - Br;
+        T.at(TS_(fzarg) + 3) = Ar + Br;
         ta[0].fz = fmax(Af - Bf, 0.0);
         ta[1].fz = fmax(Af + Bf, 0.0);
         ta[2].fz = fmax(Ar - Br, 0.0);
@@ -311,21 +331,21 @@ __device__ __forceinline__ void fwd18_tape(VehC& v, VehAux& va, TireC* ts, TireA
     double delta;
     if (C.nonLinearSteer) {
         delta = map_y(C.steer, steering);
-        T.dslope = map_slope(C.steer, steering);
+        T.at(TS_(dslope)) = map_slope(C.steer, steering);
     } else {
         delta = steering * K(K_MAXSTEER);
-        T.dslope = K(K_MAXSTEER);
+        T.at(TS_(dslope)) = K(K_MAXSTEER);
     }
     double cd = 1.0, sd = 0.0;
     if (delta != 0.0) sincos(delta, &sd, &cd);
-    T.delta = delta;
-    T.cd = cd;
-    T.sd = sd;
+    T.at(TS_(delta)) = delta;
+    T.at(TS_(cd)) = cd;
+    T.at(TS_(sd)) = sd;
     {
         const double vsyf = fma(v.wz, K(K_A), v.v);
         const double vsyr = fma(-v.wz, K(K_B), v.v);
         const double wcf = v.wz * K(K_CF2), wcr = v.wz * K(K_CR2);
-        T.vsyf = vsyf; T.vsyr = vsyr; T.wcf = wcf; T.wcr = wcr;
+        T.at(TS_(vsyf)) = vsyf; T.at(TS_(vsyr)) = vsyr; T.at(TS_(wcf)) = wcf; T.at(TS_(wcr)) = wcr;
         ta[0].vsy = vsyf;
         ta[1].vsy = vsyf;
         ta[0].vsx = fma(v.u - wcf, cd, vsyf * sd);
@@ -335,62 +355,62 @@ __device__ __forceinline__ void fwd18_tape(VehC& v, VehAux& va, TireC* ts, TireA
         ta[2].vsx = v.u - wcr;
         ta[3].vsx = v.u + wcr;
     }
-    tire_fwd_tape<true>(ts[0], ta[0], T.t[0], K, cd, sd);
-    tire_fwd_tape<true>(ts[1], ta[1], T.t[1], K, cd, sd);
-    tire_fwd_tape<false>(ts[2], ta[2], T.t[2], K, 1.0, 0.0);
-    tire_fwd_tape<false>(ts[3], ta[3], T.t[3], K, 1.0, 0.0);
+    tire_fwd_tape<true>(ts[0], ta[0], tire_ref(T, 0), K, cd, sd);
+    tire_fwd_tape<true>(ts[1], ta[1], tire_ref(T, 1), K, cd, sd);
+    tire_fwd_tape<false>(ts[2], ta[2], tire_ref(T, 2), K, 1.0, 0.0);
+    tire_fwd_tape<false>(ts[3], ta[3], tire_ref(T, 3), K, 1.0, 0.0);
     // powertrain (powertrain_rhs<false>) with its tape
     {
         double torque_t;
         const int g = v.gear;
-        T.rev = 0;
-        T.tclip = 0;
+        T.at(TS_(rev)) = 0;
+        T.at(TS_(tclip)) = 0;
         if (C.tcbool) {
             bool reverse = false;
             const double omega_t = 0.25 * (((ts[0].omega + ts[1].omega) + ts[2].omega) + ts[3].omega);
             const double omega_out = omega_t / C.gear[g];
             const double omega_in = v.crank;
-            T.omega_t = omega_t;
-            T.omega_out = omega_out;
-            T.omega_in = omega_in;
+            T.at(TS_(omega_t)) = omega_t;
+            T.at(TS_(omega_out)) = omega_out;
+            T.at(TS_(omega_in)) = omega_in;
             double sr;
             if ((omega_out < 1e-9) || (omega_in < 1e-9)) {
                 sr = 0;
-                T.srmode = 0;  // constant
+                T.at(TS_(srmode)) = 0;  // constant
             } else {
                 sr = omega_out / omega_in;
-                T.srmode = 1;
+                T.at(TS_(srmode)) = 1;
                 if (sr > 1.) {
                     sr = 1. - (sr - 1.);
                     reverse = true;
                 }
                 if (sr < 0) {
                     sr = 0;
-                    T.srmode = 0;
+                    T.at(TS_(srmode)) = 0;
                 }
             }
-            T.sr = sr;
-            T.rev = reverse ? 1.0 : 0.0;
+            T.at(TS_(sr)) = sr;
+            T.at(TS_(rev)) = reverse ? 1.0 : 0.0;
             const double cf = map_y(C.cf, sr), tr = map_y(C.tr, sr);
-            T.cf = cf;
-            T.tr = tr;
-            T.cfs = map_slope(C.cf, sr);
-            T.trs = map_slope(C.tr, sr);
+            T.at(TS_(cf)) = cf;
+            T.at(TS_(tr)) = tr;
+            T.at(TS_(cfs)) = map_slope(C.cf, sr);
+            T.at(TS_(trs)) = map_slope(C.tr, sr);
             const double r = omega_in / cf;
-            T.r = r;
+            T.at(TS_(r)) = r;
             double torque_in = -(r * r);
             if (reverse) torque_in = -torque_in;
-            T.torque_in = torque_in;
+            T.at(TS_(torque_in)) = torque_in;
             const double torque_out = reverse ? -torque_in : -tr * torque_in;
-            T.torque_out = torque_out;
+            T.at(TS_(torque_out)) = torque_out;
             torque_t = torque_out * C.invgear[g];
             if (v.u < 1e-9 && torque_t < 0) {
                 torque_t = 0;
-                T.tclip = 1;
+                T.at(TS_(tclip)) = 1;
             }
             const double dtq = drive_torque(C, throttle, v.crank);
-            T.dt_map = map_y(C.pt, v.crank);
-            T.dt_slope = fma(map_slope(C.pt, v.crank), throttle, map_slope(C.loss, v.crank));
+            T.at(TS_(dt_map)) = map_y(C.pt, v.crank);
+            T.at(TS_(dt_slope)) = fma(map_slope(C.pt, v.crank), throttle, map_slope(C.loss, v.crank));
             va.dOmega_crank = K(K_INVCI) * (dtq + torque_in);
             if (omega_out > C.up[g]) {
                 if (g < C.noGears - 1) v.gear = g + 1;
@@ -399,13 +419,13 @@ __device__ __forceinline__ void fwd18_tape(VehC& v, VehAux& va, TireC* ts, TireA
             }
         } else {
             v.crank = 0.25 * (((ts[0].omega + ts[1].omega) + ts[2].omega) + ts[3].omega) / C.gear[g];
-            T.omega_in = v.crank;
+            T.at(TS_(omega_in)) = v.crank;
             torque_t = drive_torque(C, throttle, v.crank) * C.invgear[g];
-            T.dt_map = map_y(C.pt, v.crank);
-            T.dt_slope = fma(map_slope(C.pt, v.crank), throttle, map_slope(C.loss, v.crank));
+            T.at(TS_(dt_map)) = map_y(C.pt, v.crank);
+            T.at(TS_(dt_slope)) = fma(map_slope(C.pt, v.crank), throttle, map_slope(C.loss, v.crank));
             if (v.u < 1e-9 && torque_t < 0) {
                 torque_t = 0;
-                T.tclip = 1;
+                T.at(TS_(tclip)) = 1;
             }
             if (v.crank > C.up[g]) {
                 if (g < C.noGears - 1) v.gear = g + 1;
@@ -413,7 +433,7 @@ __device__ __forceinline__ void fwd18_tape(VehC& v, VehAux& va, TireC* ts, TireA
                 if (g > 0) v.gear = g - 1;
             }
         }
-        T.torque_t = torque_t;
+        T.at(TS_(torque_t)) = torque_t;
         double tf, trr;
         if (C.driveType) {
             tf = torque_t * 0.5;
@@ -425,8 +445,8 @@ __device__ __forceinline__ void fwd18_tape(VehC& v, VehAux& va, TireC* ts, TireA
             tf = torque_t;
             trr = 0;
         }
-        T.tf = tf;
-        T.trr = trr;
+        T.at(TS_(tf)) = tf;
+        T.at(TS_(trr)) = trr;
         // differential split with the bias and its slope recorded
         auto split = [&](double torque, double wl, double wr, double& tl, double& tR, double& alpha, double& dal,
                          double& slowleft) {
@@ -454,15 +474,15 @@ __device__ __forceinline__ void fwd18_tape(VehC& v, VehAux& va, TireC* ts, TireA
                 slowleft = 0;
             }
         };
-        split(tf, ts[0].omega, ts[1].omega, ta[0].engTor, ta[1].engTor, T.alf, T.dalf, T.slowf);
-        split(trr, ts[2].omega, ts[3].omega, ta[2].engTor, ta[3].engTor, T.alr, T.dalr, T.slowr);
+        split(tf, ts[0].omega, ts[1].omega, ta[0].engTor, ta[1].engTor, T.at(TS_(alf)), T.at(TS_(dalf)), T.at(TS_(slowf)));
+        split(trr, ts[2].omega, ts[3].omega, ta[2].engTor, ta[3].engTor, T.at(TS_(alr)), T.at(TS_(dalr)), T.at(TS_(slowr)));
         const double brake = K(K_MAXBRAKE) * braking;
         const double ijw = K(K_INVJW);
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             ta[k].dOmega =
                 ijw * (fma(-sgnd(ts[k].omega), brake, ta[k].engTor + ta[k].My) - ta[k].fx * ta[k].rStat);
-        T.dOc = va.dOmega_crank;
+        T.at(TS_(dOc)) = va.dOmega_crank;
     }
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
@@ -472,8 +492,8 @@ __device__ __forceinline__ void fwd18_tape(VehC& v, VehAux& va, TireC* ts, TireA
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        T.fxr[k] = ta[k].fx;
-        T.fyr[k] = ta[k].fy;
+        T.at(TS_(fxr) + k) = ta[k].fx;
+        T.at(TS_(fyr) + k) = ta[k].fy;
     }
     {
         const double fx0 = ta[0].fx, fx1 = ta[1].fx, fx2 = ta[2].fx, fx3 = ta[3].fx;
@@ -486,7 +506,7 @@ __device__ __forceinline__ void fwd18_tape(VehC& v, VehAux& va, TireC* ts, TireA
         const double E3 = fma(K(K_E3WU), wu, fma(K(K_E3PHI), v.phi, K(K_E3WX) * v.wx));
         const double sfx = ((fx0 + fx1) + fx2) + fx3;
         const double inner = fma(K(K_UWZ2), v.wz * v.wz, fma(-K(K_UWZWX), v.wz * v.wx, sfx));
-        T.wu = wu; T.E1 = E1; T.E2 = E2; T.E3 = E3; T.inner = inner;
+        T.at(TS_(wu)) = wu; T.at(TS_(E1)) = E1; T.at(TS_(E2)) = E2; T.at(TS_(E3)) = E3; T.at(TS_(inner)) = inner;
         v.udot = fma(K(K_INVMT), inner, v.wz * v.v);
         v.vdot = fma(K(K_CV1), E1, fma(K(K_CV2), E2, K(K_CV3) * E3));
         va.wxdot = fma(K(K_CV3), E1, fma(K(K_CX2), E2, K(K_CX3) * E3));
@@ -503,18 +523,18 @@ __device__ __forceinline__ void fwd18_tape(VehC& v, VehAux& va, TireC* ts, TireA
     v.v = fma(v.vdot, dt, v.v);
     v.wx = fma(va.wxdot, dt, v.wx);
     v.wz = fma(va.wzdot, dt, v.wz);
-    T.u1 = v.u; T.v1 = v.v; T.wx1 = v.wx; T.wz1 = v.wz;
+    T.at(TS_(u1)) = v.u; T.at(TS_(v1)) = v.v; T.at(TS_(wx1)) = v.wx; T.at(TS_(wz1)) = v.wz;
     double sp, cp;
     sincos(v.psi, &sp, &cp);
-    T.sp = sp;
-    T.cp = cp;
+    T.at(TS_(sp)) = sp;
+    T.at(TS_(cp)) = cp;
     v.x = fma(fma(v.u, cp, -v.v * sp), dt, v.x);
     v.y = fma(fma(v.u, sp, v.v * cp), dt, v.y);
     v.psi = fma(v.wz, dt, v.psi);
     v.phi = fma(v.wx, dt, v.phi);
-    T.x1 = v.x;
-    T.y1 = v.y;
-    T.psi1 = v.psi;
+    T.at(TS_(x1)) = v.x;
+    T.at(TS_(y1)) = v.y;
+    T.at(TS_(psi1)) = v.psi;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -535,28 +555,33 @@ __device__ __forceinline__ void tmxy_rev(double s, double df0, double sm, double
     }
     if (!(s > 0.0 && df0loc > 0.0) || fosb == 0.0) return;
     double df0locb = 0.0;
+    const double is = 1.0 / s;
     if (s > ss) {  // full sliding: fos = fs / s
-        fsb += fosb / s;
-        sb += -fs / (s * s) * fosb;
+        fsb += fosb * is;
+        sb += -fs * is * is * fosb;
         return;
     }
     if (s < sm) {  // adhesion: fos = df0loc / dn
-        const double p = df0loc * sm / fm - 2.0;
+        const double ifm = 1.0 / fm;
+        const double p = df0loc * sm * ifm - 2.0;
         const double sn = s * ism;
         const double dn = fma(sn + p, sn, 1.0);
-        const double dnb = -df0loc / (dn * dn) * fosb;
-        df0locb += fosb / dn;
+        const double idn = 1.0 / dn;
+        const double dnb = -df0loc * idn * idn * fosb;
+        df0locb += fosb * idn;
         const double snb = (2.0 * sn + p) * dnb;
         const double pb = sn * dnb;
-        df0locb += sm / fm * pb;
-        smb += df0loc / fm * pb;
-        fmb += -df0loc * sm / (fm * fm) * pb;
+        df0locb += sm * ifm * pb;
+        smb += df0loc * ifm * pb;
+        fmb += -df0loc * sm * ifm * ifm * pb;
         sb += snb * ism;
         smb += -s * ism * ism * snb;
     } else {
         const double q = fm * ism;
-        const double a = q * q / (df0loc * sm);
-        const double sstar = sm + (fm - fs) / (a * (ss - sm));
+        const double idsm = 1.0 / (df0loc * sm);
+        const double a = q * q * idsm;
+        const double ida = 1.0 / (a * (ss - sm));
+        const double sstar = sm + (fm - fs) * ida;
         double f, ab = 0.0, sstarb = 0.0;
         double b = 0.0, sn3 = 0.0;
         if (sstar <= ss) {
@@ -570,8 +595,8 @@ __device__ __forceinline__ void tmxy_rev(double s, double df0, double sm, double
             sn3 = (s - sm) / (ss - sm);
             f = fm - (fm - fs) * sn3 * sn3 * (3.0 - 2.0 * sn3);
         }
-        const double fb = fosb / s;  // fos = f / s
-        sb += -f / (s * s) * fosb;
+        const double fb = fosb * is;  // fos = f / s
+        sb += -f * is * is * fosb;
         if (sstar <= ss) {
             if (s <= sstar) {
                 fmb += fb;
@@ -583,36 +608,35 @@ __device__ __forceinline__ void tmxy_rev(double s, double df0, double sm, double
                 const double bb = (ss - s) * (ss - s) * fb;
                 ssb += 2.0 * b * (ss - s) * fb;
                 sb += -2.0 * b * (ss - s) * fb;
-                const double d = ss - sstar;
-                ab += (sstar - sm) / d * bb;
-                sstarb += (a / d + a * (sstar - sm) / (d * d)) * bb;
-                smb += -a / d * bb;
-                ssb += -a * (sstar - sm) / (d * d) * bb;
+                const double id = 1.0 / (ss - sstar);
+                ab += (sstar - sm) * id * bb;
+                sstarb += (a * id + a * (sstar - sm) * id * id) * bb;
+                smb += -a * id * bb;
+                ssb += -a * (sstar - sm) * id * id * bb;
             }
         } else {
             const double g = sn3 * sn3 * (3.0 - 2.0 * sn3);
             fmb += fb * (1.0 - g);
             fsb += fb * g;
             const double snb = -(fm - fs) * (6.0 * sn3 - 6.0 * sn3 * sn3) * fb;
-            const double d = ss - sm;
-            sb += snb / d;
-            smb += snb * (-1.0 / d + (s - sm) / (d * d));
-            ssb += -snb * (s - sm) / (d * d);
+            const double id = 1.0 / (ss - sm);
+            sb += snb * id;
+            smb += snb * (-id + (s - sm) * id * id);
+            ssb += -snb * (s - sm) * id * id;
         }
         if (sstarb != 0.0) {  // sstar = sm + (fm - fs) / (a (ss - sm))
-            const double den = a * (ss - sm);
             smb += sstarb;
-            fmb += sstarb / den;
-            fsb += -sstarb / den;
-            const double denb = -(fm - fs) / (den * den) * sstarb;
+            fmb += sstarb * ida;
+            fsb += -sstarb * ida;
+            const double denb = -(fm - fs) * ida * ida * sstarb;
             ab += (ss - sm) * denb;
             ssb += a * denb;
             smb += -a * denb;
         }
         if (ab != 0.0) {  // a = q^2 / (df0loc sm), q = fm / sm
-            const double qb = 2.0 * q / (df0loc * sm) * ab;
-            df0locb += -q * q / (df0loc * df0loc * sm) * ab;
-            smb += -q * q / (df0loc * sm * sm) * ab;
+            const double qb = 2.0 * q * idsm * ab;
+            df0locb += -a / df0loc * ab;
+            smb += -a * ism * ab;
             fmb += qb * ism;
             smb += -fm * ism * ism * qb;
         }
@@ -629,137 +653,140 @@ __device__ __forceinline__ void tmxy_rev(double s, double df0, double sm, double
 // the tire model returns them, before any frame rotation) and of rStat, to those of the inputs
 // (xe, ye, omega, vsx before the slip correction, vsy, fz, cos/sin of the wheel angle).
 template <bool kSteered>
-__device__ __forceinline__ void tire_rev(const TireTape& T, const KView& K, const KBar& kb, double xedotb,
+__device__ __forceinline__ void tire_rev(const TapeRef& T, const KView& K, const KBar& kb, double xedotb,
                                          double yedotb, double fxb, double fyb, double Myb, double rStatb, double& xeb,
                                          double& yeb, double& omb, double& vsxinb, double& vsyb, double& fzb,
                                          double& cb, double& sb_, double c, double s) {
     const double cx = K(K_CX), cy = K(K_CY), dx = K(K_DX), dy = K(K_DY);
     double vsxb = 0, syb = 0, vtab = 0, fosb = 0, rwb = 0, hsxnb = 0, hsynb = 0, fzcb = 0, sxb = 0;
     // blend of structural and dynamic forces
-    const double wxb = (T.fxstr - T.Fx) * fxb, wyb = (T.fystr - T.Fy) * fyb;
-    const double fxstrb = T.wxw * fxb, fystrb = T.wyw * fyb;
-    const double Fxb = (1.0 - T.wxw) * fxb, Fyb = (1.0 - T.wyw) * fyb;
-    vsxb += T.dwx * (T.vsx >= 0 ? 1.0 : -1.0) * wxb;
+    const double wxb = (T.at(TT_(fxstr)) - T.at(TT_(Fx))) * fxb, wyb = (T.at(TT_(fystr)) - T.at(TT_(Fy))) * fyb;
+    const double fxstrb = T.at(TT_(wxw)) * fxb, fystrb = T.at(TT_(wyw)) * fyb;
+    const double Fxb = (1.0 - T.at(TT_(wxw))) * fxb, Fyb = (1.0 - T.at(TT_(wyw))) * fyb;
+    vsxb += T.at(TT_(dwx)) * (T.at(TT_(vsx)) >= 0 ? 1.0 : -1.0) * wxb;
     {
-        const double arg = T.sy * T.vta;
-        const double argb = T.dwy * (arg >= 0 ? 1.0 : -1.0) * wyb;
-        syb += T.vta * argb;
-        vtab += T.sy * argb;
+        const double arg = T.at(TT_(sy)) * T.at(TT_(vta));
+        const double argb = T.at(TT_(dwy)) * (arg >= 0 ? 1.0 : -1.0) * wyb;
+        syb += T.at(TT_(vta)) * argb;
+        vtab += T.at(TT_(sy)) * argb;
     }
     double Gxb = 0, Gyb = 0;
-    if (T.clx == 0.0) Gxb = fxstrb;
-    else kb.add(KB_FXMP2N, T.clx * fxstrb);
-    if (T.cly == 0.0) Gyb = fystrb;
-    else kb.add(KB_FYMP2N, T.cly * fystrb);
+    if (T.at(TT_(clx)) == 0.0) Gxb = fxstrb;
+    else kb.add(KB_FXMP2N, T.at(TT_(clx)) * fxstrb);
+    if (T.at(TT_(cly)) == 0.0) Gyb = fystrb;
+    else kb.add(KB_FYMP2N, T.at(TT_(cly)) * fystrb);
     xeb += cx * (Gxb + Fxb);
     xedotb += dx * (Gxb + Fxb);
     yeb += cy * (Gyb + Fyb);
     yedotb += dy * (Gyb + Fyb);
     // relaxation rates
-    const double numxb = xedotb / T.denx, denxb = -T.xedot / T.denx * xedotb;
-    const double numyb = yedotb / T.deny, denyb = -T.yedot / T.deny * yedotb;
-    double vtxsb = -cx * T.xe * numxb + dx * denxb;
-    xeb += -T.vtxs * cx * numxb;
-    fosb += -T.vsx * numxb + denxb;
-    vsxb += -T.fos * numxb;
-    double vtysb = -cy * T.ye * numyb + dy * denyb;
-    yeb += -T.vtys * cy * numyb;
-    fosb += T.sy * T.vta * numyb + denyb;
-    syb += T.fos * T.vta * numyb;
-    vtab += T.fos * T.sy * numyb;
-    rwb += T.hsxn * vtxsb + T.hsyn * vtysb;
-    hsxnb += T.rw * vtxsb;
-    hsynb += T.rw * vtysb;
+    const double idenx = T.at(TT_(idenx)), ideny = T.at(TT_(ideny));
+    const double numxb = xedotb * idenx, denxb = -T.at(TT_(xedot)) * idenx * xedotb;
+    const double numyb = yedotb * ideny, denyb = -T.at(TT_(yedot)) * ideny * yedotb;
+    double vtxsb = -cx * T.at(TT_(xe)) * numxb + dx * denxb;
+    xeb += -T.at(TT_(vtxs)) * cx * numxb;
+    fosb += -T.at(TT_(vsx)) * numxb + denxb;
+    vsxb += -T.at(TT_(fos)) * numxb;
+    double vtysb = -cy * T.at(TT_(ye)) * numyb + dy * denyb;
+    yeb += -T.at(TT_(vtys)) * cy * numyb;
+    fosb += T.at(TT_(sy)) * T.at(TT_(vta)) * numyb + denyb;
+    syb += T.at(TT_(fos)) * T.at(TT_(vta)) * numyb;
+    vtab += T.at(TT_(fos)) * T.at(TT_(sy)) * numyb;
+    rwb += T.at(TT_(hsxn)) * vtxsb + T.at(TT_(hsyn)) * vtysb;
+    hsxnb += T.at(TT_(rw)) * vtxsb;
+    hsynb += T.at(TT_(rw)) * vtysb;
     // rolling resistance (no adjoint through sgn)
-    fzcb += -K(K_RR) * T.rStat * T.sgn * Myb;
-    rStatb += -K(K_RR) * T.fzc * T.sgn * Myb;
+    fzcb += -K(K_RR) * T.at(TT_(rStat)) * T.at(TT_(sgn)) * Myb;
+    rStatb += -K(K_RR) * T.at(TT_(fzc)) * T.at(TT_(sgn)) * Myb;
     // combined-slip force curve
     double scb = 0, df0b = 0, smb = 0, fmb = 0, ssb = 0, fsb = 0;
-    tmxy_rev(T.sc, T.df0, T.sm, T.fm, T.ss, T.fs, fosb, scb, df0b, smb, fmb, ssb, fsb);
+    tmxy_rev(T.at(TT_(sc)), T.at(TT_(df0)), T.at(TT_(sm)), T.at(TT_(fm)), T.at(TT_(ss)), T.at(TT_(fs)), fosb, scb, df0b, smb, fmb, ssb, fsb);
     double calphab = 0, salphab = 0, caxb = 0, sayb = 0, ihxb = 0, ihyb = 0;
     double dfx0b = 0, dfy0b = 0, fxmb = 0, fymb = 0, fxsb = 0, fysb = 0, sxmb = 0, symb = 0, sxsb = 0, sysb = 0;
-    const double cax = T.calpha * T.ihx, say = T.salpha * T.ihy;
+    const double cax = T.at(TT_(calpha)) * T.at(TT_(ihx)), say = T.at(TT_(salpha)) * T.at(TT_(ihy));
     auto hyp_rev = [](double a, double b, double h, double hb, double& ab, double& bb) {
-        if (h > 0) {
-            ab += a / h * hb;
-            bb += b / h * hb;
+        if (h > 0 && hb != 0.0) {
+            const double t = hb / h;
+            ab += a * t;
+            bb += b * t;
         }
     };
     {
         double Pb = 0, Qb = 0;
-        hyp_rev(T.sxs * cax, T.sys * say, T.ss, ssb, Pb, Qb);
+        hyp_rev(T.at(TT_(sxs)) * cax, T.at(TT_(sys)) * say, T.at(TT_(ss)), ssb, Pb, Qb);
         sxsb += cax * Pb;
-        caxb += T.sxs * Pb;
+        caxb += T.at(TT_(sxs)) * Pb;
         sysb += say * Qb;
-        sayb += T.sys * Qb;
+        sayb += T.at(TT_(sys)) * Qb;
     }
     {
         double Pb = 0, Qb = 0;
-        hyp_rev(T.fxs * T.calpha, T.fys * T.salpha, T.fs, fsb, Pb, Qb);
-        fxsb += T.calpha * Pb;
-        calphab += T.fxs * Pb;
-        fysb += T.salpha * Qb;
-        salphab += T.fys * Qb;
+        hyp_rev(T.at(TT_(fxs)) * T.at(TT_(calpha)), T.at(TT_(fys)) * T.at(TT_(salpha)), T.at(TT_(fs)), fsb, Pb, Qb);
+        fxsb += T.at(TT_(calpha)) * Pb;
+        calphab += T.at(TT_(fxs)) * Pb;
+        fysb += T.at(TT_(salpha)) * Qb;
+        salphab += T.at(TT_(fys)) * Qb;
     }
     {
         double Pb = 0, Qb = 0;
-        hyp_rev(T.sxm * cax, T.sym * say, T.sm, smb, Pb, Qb);
+        hyp_rev(T.at(TT_(sxm)) * cax, T.at(TT_(sym)) * say, T.at(TT_(sm)), smb, Pb, Qb);
         sxmb += cax * Pb;
-        caxb += T.sxm * Pb;
+        caxb += T.at(TT_(sxm)) * Pb;
         symb += say * Qb;
-        sayb += T.sym * Qb;
+        sayb += T.at(TT_(sym)) * Qb;
     }
-    calphab += T.ihx * caxb;
-    ihxb += T.calpha * caxb;
-    salphab += T.ihy * sayb;
-    ihyb += T.salpha * sayb;
+    calphab += T.at(TT_(ihx)) * caxb;
+    ihxb += T.at(TT_(calpha)) * caxb;
+    salphab += T.at(TT_(ihy)) * sayb;
+    ihyb += T.at(TT_(salpha)) * sayb;
     {
         double Pb = 0, Qb = 0;
-        hyp_rev(T.fxm * T.calpha, T.fym * T.salpha, T.fm, fmb, Pb, Qb);
-        fxmb += T.calpha * Pb;
-        calphab += T.fxm * Pb;
-        fymb += T.salpha * Qb;
-        salphab += T.fym * Qb;
+        hyp_rev(T.at(TT_(fxm)) * T.at(TT_(calpha)), T.at(TT_(fym)) * T.at(TT_(salpha)), T.at(TT_(fm)), fmb, Pb, Qb);
+        fxmb += T.at(TT_(calpha)) * Pb;
+        calphab += T.at(TT_(fxm)) * Pb;
+        fymb += T.at(TT_(salpha)) * Qb;
+        salphab += T.at(TT_(fym)) * Qb;
     }
     {
         double Pb = 0, Qb = 0;
-        hyp_rev(T.dfx0 * T.calpha * T.hsxn, T.dfy0 * T.salpha * T.hsyn, T.df0, df0b, Pb, Qb);
-        dfx0b += T.calpha * T.hsxn * Pb;
-        calphab += T.dfx0 * T.hsxn * Pb;
-        hsxnb += T.dfx0 * T.calpha * Pb;
-        dfy0b += T.salpha * T.hsyn * Qb;
-        salphab += T.dfy0 * T.hsyn * Qb;
-        hsynb += T.dfy0 * T.salpha * Qb;
+        hyp_rev(T.at(TT_(dfx0)) * T.at(TT_(calpha)) * T.at(TT_(hsxn)), T.at(TT_(dfy0)) * T.at(TT_(salpha)) * T.at(TT_(hsyn)), T.at(TT_(df0)), df0b, Pb, Qb);
+        dfx0b += T.at(TT_(calpha)) * T.at(TT_(hsxn)) * Pb;
+        calphab += T.at(TT_(dfx0)) * T.at(TT_(hsxn)) * Pb;
+        hsxnb += T.at(TT_(dfx0)) * T.at(TT_(calpha)) * Pb;
+        dfy0b += T.at(TT_(salpha)) * T.at(TT_(hsyn)) * Qb;
+        salphab += T.at(TT_(dfy0)) * T.at(TT_(hsyn)) * Qb;
+        hsynb += T.at(TT_(dfy0)) * T.at(TT_(salpha)) * Qb;
     }
     double sxnb = 0, synb = 0;
-    if (T.qpos != 0.0) {
-        const double iscb = T.sxn * calphab + T.syn * salphab;
-        sxnb += T.isc * calphab;
-        synb += T.isc * salphab;
-        const double sct = scb - iscb * T.isc * T.isc;
-        sxnb += T.sxn / T.sc * sct;
-        synb += T.syn / T.sc * sct;
+    if (T.at(TT_(qpos)) != 0.0) {
+        const double iscb = T.at(TT_(sxn)) * calphab + T.at(TT_(syn)) * salphab;
+        sxnb += T.at(TT_(isc)) * calphab;
+        synb += T.at(TT_(isc)) * salphab;
+        const double sct = scb - iscb * T.at(TT_(isc)) * T.at(TT_(isc));
+        sxnb += T.at(TT_(sxn)) * T.at(TT_(isc)) * sct;
+        synb += T.at(TT_(syn)) * T.at(TT_(isc)) * sct;
     }
-    sxb += T.ihx * sxnb;
-    ihxb += T.sx * sxnb;
-    syb += T.ihy * synb;
-    ihyb += T.sy * synb;
-    hsxnb += -T.ihx * T.ihx * ihxb;
-    hsynb += -T.ihy * T.ihy * ihyb;
+    sxb += T.at(TT_(ihx)) * sxnb;
+    ihxb += T.at(TT_(sx)) * sxnb;
+    syb += T.at(TT_(ihy)) * synb;
+    ihyb += T.at(TT_(sy)) * synb;
+    hsxnb += -T.at(TT_(ihx)) * T.at(TT_(ihx)) * ihxb;
+    hsynb += -T.at(TT_(ihy)) * T.at(TT_(ihy)) * ihyb;
     {
-        const double ssumb = -(T.sxm * hsxnb + T.sym * hsynb) / (T.ssum * T.ssum);
-        const double fsumb = -(T.fxd * hsxnb + T.fyd * hsynb) / (T.fsum * T.fsum);
-        sxmb += hsxnb / T.ssum + ssumb;
-        symb += hsynb / T.ssum + ssumb;
-        const double fxdb = hsxnb / T.fsum + fsumb;
-        const double fydb = hsynb / T.fsum + fsumb;
-        fxmb += T.dfy0 * fxdb;
-        dfy0b += T.fxm * fxdb;
-        fymb += T.dfx0 * fydb;
-        dfx0b += T.fym * fydb;
+        const double issum = T.at(TT_(issum)), ifsum = T.at(TT_(ifsum));
+        const double ssumb = -(T.at(TT_(sxm)) * hsxnb + T.at(TT_(sym)) * hsynb) * (issum * issum);
+        const double fsumb = -(T.at(TT_(fxd)) * hsxnb + T.at(TT_(fyd)) * hsynb) * (ifsum * ifsum);
+        sxmb += hsxnb * issum + ssumb;
+        symb += hsynb * issum + ssumb;
+        const double fxdb = hsxnb * ifsum + fsumb;
+        const double fydb = hsynb * ifsum + fsumb;
+        fxmb += T.at(TT_(dfy0)) * fxdb;
+        dfy0b += T.at(TT_(fxm)) * fxdb;
+        fymb += T.at(TT_(dfx0)) * fydb;
+        dfx0b += T.at(TT_(fym)) * fydb;
     }
     // curve parameters from the normalised load
-    const double fzn = T.fzn;
+    const double fzn = T.at(TT_(fzn));
     double fznb = 0;
     fznb += fma(-2.0 * K(K_Q2DFX0), fzn, K(K_Q1DFX0)) * dfx0b;
     fznb += fma(-2.0 * K(K_Q2DFY0), fzn, K(K_Q1DFY0)) * dfy0b;
@@ -777,47 +804,48 @@ __device__ __forceinline__ void tire_rev(const TireTape& T, const KView& K, cons
     kb.add(KB_Q2FYS, -fzn * fzn * fysb);
     fznb += K(K_DSXM) * sxmb + K(K_DSYM) * symb + K(K_DSXS) * sxsb + K(K_DSYS) * sysb;
     fzcb += K(K_INVPN) * fznb;
-    if (T.fzcl == 0.0) fzb += fzcb;
+    if (T.at(TT_(fzcl)) == 0.0) fzb += fzcb;
     // slips
-    const double ivta = 1.0 / T.vta;
+    const double ivta = T.at(TT_(ivta));
     vsxb += -ivta * sxb;
-    vtab += T.vsx * ivta * ivta * sxb;
+    vtab += T.at(TT_(vsx)) * ivta * ivta * sxb;
     if (kSteered) {
-        const double Nb = -syb / T.D, Db = T.N / (T.D * T.D) * syb;
+        const double iD = 1.0 / T.at(TT_(D));
+        const double Nb = -syb * iD, Db = T.at(TT_(N)) * (iD * iD) * syb;
         vsyb += c * Nb + s * Db;
         vtab += -s * Nb + c * Db;
-        cb += T.vsy * Nb + T.vta * Db;
-        sb_ += -T.vta * Nb + T.vsy * Db;
+        cb += T.at(TT_(vsy)) * Nb + T.at(TT_(vta)) * Db;
+        sb_ += -T.at(TT_(vta)) * Nb + T.at(TT_(vsy)) * Db;
     } else {
         vsyb += -ivta * syb;
-        vtab += T.vsy * ivta * ivta * syb;
+        vtab += T.at(TT_(vsy)) * ivta * ivta * syb;
     }
     rwb += vtab;
-    double reffb = fabs(T.om) * rwb;
-    omb += T.r_eff * T.sgn * rwb;
+    double reffb = fabs(T.at(TT_(om))) * rwb;
+    omb += T.at(TT_(r_eff)) * T.at(TT_(sgn)) * rwb;
     vsxinb += vsxb;
-    omb += -T.r_eff * vsxb;
-    reffb += -T.om * vsxb;
+    omb += -T.at(TT_(r_eff)) * vsxb;
+    reffb += -T.at(TT_(om)) * vsxb;
     // r_eff = rdynco xt + rStat, rStat = r0 - xt, xt = fz / kt
-    double xtb = T.rdynco * reffb;
+    double xtb = T.at(TT_(rdynco)) * reffb;
     rStatb += reffb;
-    if (T.fzrd != 0.0) fzb += K(K_DRD) * K(K_INVPN) * (T.xt * reffb);  // rdynco interpolated in fz
+    if (T.at(TT_(fzrd)) != 0.0) fzb += K(K_DRD) * K(K_INVPN) * (T.at(TT_(xt)) * reffb);  // rdynco interpolated in fz
     xtb += -rStatb;
     fzb += K(K_INVKT) * xtb;
-    kb.add(KB_INVKT, T.fz * xtb);
+    kb.add(KB_INVKT, T.at(TT_(fz)) * xtb);
 }
 
 // One step's reverse sweep. L: on entry the adjoint of the state after the step, on return that of
 // the state before it; the adjoints of the step's controls are added to steerb/thrb/brkb and those
 // of the differentiable constants to kb.
-__device__ __forceinline__ void rev18(const StepTape& T, const KView& K, const ClassDev18& C, const KBar& kb,
+__device__ __forceinline__ void rev18(const TapeRef& T, const KView& K, const ClassDev18& C, const KBar& kb,
                                       double dt, Adj18& L, double& steerb, double& thrb, double& brkb) {
-    const int g = (int)T.gear;
+    const int g = (int)T.at(TS_(gear));
     // half-implicit update: x, y with the updated speeds and the old yaw; yaw and roll with the
     // updated rates
-    double u1b = dt * fma(T.cp, L.x, T.sp * L.y);
-    double v1b = dt * fma(-T.sp, L.x, T.cp * L.y);
-    double psib = L.psi + dt * ((-T.u1 * T.sp - T.v1 * T.cp) * L.x + (T.u1 * T.cp - T.v1 * T.sp) * L.y);
+    double u1b = dt * fma(T.at(TS_(cp)), L.x, T.at(TS_(sp)) * L.y);
+    double v1b = dt * fma(-T.at(TS_(sp)), L.x, T.at(TS_(cp)) * L.y);
+    double psib = L.psi + dt * ((-T.at(TS_(u1)) * T.at(TS_(sp)) - T.at(TS_(v1)) * T.at(TS_(cp))) * L.x + (T.at(TS_(u1)) * T.at(TS_(cp)) - T.at(TS_(v1)) * T.at(TS_(sp))) * L.y);
     double wz1b = dt * L.psi + L.wz;
     double wx1b = dt * L.phi + L.wx;
     const double phib0 = L.phi;
@@ -846,13 +874,13 @@ __device__ __forceinline__ void rev18(const StepTape& T, const KView& K, const C
     double fxrb[4], fyrb[4];
     {
         const double innerb = K(K_INVMT) * udotb;
-        kb.add(KB_INVMT, T.inner * udotb);
-        wzb += T.v * udotb;
-        vb += T.wz * udotb;
-        wzb += (2.0 * K(K_UWZ2) * T.wz - K(K_UWZWX) * T.wx) * innerb;
-        wxb += -K(K_UWZWX) * T.wz * innerb;
-        kb.add(KB_UWZ2, T.wz * T.wz * innerb);
-        kb.add(KB_UWZWX, -T.wz * T.wx * innerb);
+        kb.add(KB_INVMT, T.at(TS_(inner)) * udotb);
+        wzb += T.at(TS_(v)) * udotb;
+        vb += T.at(TS_(wz)) * udotb;
+        wzb += (2.0 * K(K_UWZ2) * T.at(TS_(wz)) - K(K_UWZWX) * T.at(TS_(wx))) * innerb;
+        wxb += -K(K_UWZWX) * T.at(TS_(wz)) * innerb;
+        kb.add(KB_UWZ2, T.at(TS_(wz)) * T.at(TS_(wz)) * innerb);
+        kb.add(KB_UWZWX, -T.at(TS_(wz)) * T.at(TS_(wx)) * innerb);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             fxrb[k] = innerb;
@@ -861,46 +889,46 @@ __device__ __forceinline__ void rev18(const StepTape& T, const KView& K, const C
         const double E1b = K(K_CV1) * vdotb + K(K_CV3) * wxdotb + K(K_CV2) * wzdotb;
         const double E2b = K(K_CV2) * vdotb + K(K_CX2) * wxdotb + K(K_CZ2) * wzdotb;
         const double E3b = K(K_CV3) * vdotb + K(K_CX3) * wxdotb + K(K_CX2) * wzdotb;
-        kb.add(KB_CV1, T.E1 * vdotb);
-        kb.add(KB_CV2, T.E2 * vdotb + T.E1 * wzdotb);
-        kb.add(KB_CV3, T.E3 * vdotb + T.E1 * wxdotb);
-        kb.add(KB_CX2, T.E2 * wxdotb + T.E3 * wzdotb);
-        kb.add(KB_CX3, T.E3 * wxdotb);
-        kb.add(KB_CZ2, T.E2 * wzdotb);
+        kb.add(KB_CV1, T.at(TS_(E1)) * vdotb);
+        kb.add(KB_CV2, T.at(TS_(E2)) * vdotb + T.at(TS_(E1)) * wzdotb);
+        kb.add(KB_CV3, T.at(TS_(E3)) * vdotb + T.at(TS_(E1)) * wxdotb);
+        kb.add(KB_CX2, T.at(TS_(E2)) * wxdotb + T.at(TS_(E3)) * wzdotb);
+        kb.add(KB_CX3, T.at(TS_(E3)) * wxdotb);
+        kb.add(KB_CZ2, T.at(TS_(E2)) * wzdotb);
         double wub = K(K_E3WU) * E3b;
         phib += K(K_E3PHI) * E3b;
         wxb += K(K_E3WX) * E3b;
-        kb.add(KB_E3WU, T.wu * E3b);
-        kb.add(KB_E3PHI, T.phi * E3b);
-        const double fyf = T.fyr[0] + T.fyr[1], fyr = T.fyr[2] + T.fyr[3];
+        kb.add(KB_E3WU, T.at(TS_(wu)) * E3b);
+        kb.add(KB_E3PHI, T.at(TS_(phi)) * E3b);
+        const double fyf = T.at(TS_(fyr) + 0) + T.at(TS_(fyr) + 1), fyr = T.at(TS_(fyr) + 2) + T.at(TS_(fyr) + 3);
         wub += K(K_E2WU) * E2b;
         fxrb[3] += K(K_CR2) * E2b;
         fxrb[2] -= K(K_CR2) * E2b;
         fxrb[1] += K(K_CF2) * E2b;
         fxrb[0] -= K(K_CF2) * E2b;
         double fyfb = K(K_A) * E2b, fyrb_ = -K(K_B) * E2b;
-        kb.add(KB_E2WU, T.wu * E2b);
+        kb.add(KB_E2WU, T.at(TS_(wu)) * E2b);
         kb.add(KB_A, fyf * E2b);
         wub += -K(K_MT) * E1b;
         fyfb += E1b;
         fyrb_ += E1b;
-        kb.add(KB_MT, -T.wu * E1b);
+        kb.add(KB_MT, -T.at(TS_(wu)) * E1b);
         (void)fyr;
         fyrb[0] += fyfb;
         fyrb[1] += fyfb;
         fyrb[2] += fyrb_;
         fyrb[3] += fyrb_;
-        wzb += T.u * wub;
-        ub += T.wz * wub;
+        wzb += T.at(TS_(u)) * wub;
+        ub += T.at(TS_(wz)) * wub;
     }
     // front forces rotated into the vehicle frame
     double fxb[4], fyb[4], cdb = 0, sdb = 0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         if (k < 2) {
-            const double fx = T.t[k].fx, fy = T.t[k].fy;
-            fxb[k] = fma(T.cd, fxrb[k], T.sd * fyrb[k]);
-            fyb[k] = fma(-T.sd, fxrb[k], T.cd * fyrb[k]);
+            const double fx = tire_ref(T, k).at(TT_(fx)), fy = tire_ref(T, k).at(TT_(fy));
+            fxb[k] = fma(T.at(TS_(cd)), fxrb[k], T.at(TS_(sd)) * fyrb[k]);
+            fyb[k] = fma(-T.at(TS_(sd)), fxrb[k], T.at(TS_(cd)) * fyrb[k]);
             cdb += fma(fx, fxrb[k], fy * fyrb[k]);
             sdb += fma(-fy, fxrb[k], fx * fyrb[k]);
         } else {
@@ -913,13 +941,13 @@ __device__ __forceinline__ void rev18(const StepTape& T, const KView& K, const C
     double om_mid[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        om_mid[k] = T.t[k].on != 0.0 ? T.t[k].om : 0.0;
+        om_mid[k] = tire_ref(T, k).at(TT_(on)) != 0.0 ? tire_ref(T, k).at(TT_(om)) : 0.0;
         const double gk = K(K_INVJW) * dOmb[k];
         engb[k] = gk;
         Myb[k] = gk;
         brakeb += -sgnd(om_mid[k]) * gk;
-        fxb[k] += -T.t[k].rStat * gk;
-        rStatb[k] = -T.t[k].fx * gk;
+        fxb[k] += -tire_ref(T, k).at(TT_(rStat)) * gk;
+        rStatb[k] = -tire_ref(T, k).at(TT_(fx)) * gk;
     }
     brkb += K(K_MAXBRAKE) * brakeb;
     auto split_rev = [](double torque, double alpha, double dal, double slowleft, double tlb, double trb, double wl,
@@ -935,59 +963,61 @@ __device__ __forceinline__ void rev18(const StepTape& T, const KView& K, const C
         }
         return alpha * slowb + (1.0 - alpha) * fastb;
     };
-    const double tfb = split_rev(T.tf, T.alf, T.dalf, T.slowf, engb[0], engb[1], om_mid[0], om_mid[1], om_midb[0],
+    const double tfb = split_rev(T.at(TS_(tf)), T.at(TS_(alf)), T.at(TS_(dalf)), T.at(TS_(slowf)), engb[0], engb[1], om_mid[0], om_mid[1], om_midb[0],
                                  om_midb[1]);
-    const double trrb = split_rev(T.trr, T.alr, T.dalr, T.slowr, engb[2], engb[3], om_mid[2], om_mid[3], om_midb[2],
+    const double trrb = split_rev(T.at(TS_(trr)), T.at(TS_(alr)), T.at(TS_(dalr)), T.at(TS_(slowr)), engb[2], engb[3], om_mid[2], om_mid[3], om_midb[2],
                                   om_midb[3]);
     double torque_tb = C.driveType ? 0.5 * (tfb + trrb) : (C.whichWheels ? trrb : tfb);
-    if (T.tclip != 0.0) torque_tb = 0;
+    if (T.at(TS_(tclip)) != 0.0) torque_tb = 0;
     if (C.tcbool) {
         const double torque_outb = C.invgear[g] * torque_tb;
         double torque_inb = 0, trb = 0;
-        if (T.rev != 0.0) {
+        if (T.at(TS_(rev)) != 0.0) {
             torque_inb += -torque_outb;
         } else {
-            trb = -T.torque_in * torque_outb;
-            torque_inb += -T.tr * torque_outb;
+            trb = -T.at(TS_(torque_in)) * torque_outb;
+            torque_inb += -T.at(TS_(tr)) * torque_outb;
         }
         const double dtqb = K(K_INVCI) * dOcb;
         torque_inb += K(K_INVCI) * dOcb;
-        thrb += T.dt_map * dtqb;
-        crankb += T.dt_slope * dtqb;
-        const double rb = (T.rev != 0.0 ? 2.0 * T.r : -2.0 * T.r) * torque_inb;
-        double omega_inb = rb / T.cf;
-        const double cfb = -T.r / T.cf * rb;
-        const double srb = T.cfs * cfb + T.trs * trb;
+        thrb += T.at(TS_(dt_map)) * dtqb;
+        crankb += T.at(TS_(dt_slope)) * dtqb;
+        const double rb = (T.at(TS_(rev)) != 0.0 ? 2.0 * T.at(TS_(r)) : -2.0 * T.at(TS_(r))) * torque_inb;
+        const double icf = 1.0 / T.at(TS_(cf));
+        double omega_inb = rb * icf;
+        const double cfb = -T.at(TS_(r)) * icf * rb;
+        const double srb = T.at(TS_(cfs)) * cfb + T.at(TS_(trs)) * trb;
         double omega_outb = 0;
-        if (T.srmode != 0.0) {
-            const double sr0b = T.rev != 0.0 ? -srb : srb;
-            omega_outb += sr0b / T.omega_in;
-            omega_inb += -(T.omega_out / T.omega_in) / T.omega_in * sr0b;
+        if (T.at(TS_(srmode)) != 0.0) {
+            const double sr0b = T.at(TS_(rev)) != 0.0 ? -srb : srb;
+            const double iin = 1.0 / T.at(TS_(omega_in));
+            omega_outb += sr0b * iin;
+            omega_inb += -T.at(TS_(omega_out)) * iin * iin * sr0b;
         }
-        const double omega_tb = omega_outb / C.gear[g];
+        const double omega_tb = omega_outb * C.invgear[g];
 #pragma unroll
         for (int k = 0; k < 4; ++k) om_midb[k] += 0.25 * omega_tb;
         crankb += omega_inb;
     } else {
         const double dtqb = C.invgear[g] * torque_tb;
-        thrb += T.dt_map * dtqb;
-        crank_outb += T.dt_slope * dtqb;
+        thrb += T.at(TS_(dt_map)) * dtqb;
+        crank_outb += T.at(TS_(dt_slope)) * dtqb;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) om_midb[k] += 0.25 * crank_outb / C.gear[g];
+        for (int k = 0; k < 4; ++k) om_midb[k] += 0.25 * crank_outb * C.invgear[g];
     }
     // tires
     double vsxinb[4], vsyb[4], fzb[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         vsxinb[k] = vsyb[k] = fzb[k] = 0;
-        if (T.t[k].on != 0.0) {
+        if (tire_ref(T, k).at(TT_(on)) != 0.0) {
             double xeb = L.xe[k], yeb = L.ye[k], omb = om_midb[k];
             if (k < 2)
-                tire_rev<true>(T.t[k], K, kb, xedotnb[k], yedotnb[k], fxb[k], fyb[k], Myb[k], rStatb[k], xeb, yeb,
-                               omb, vsxinb[k], vsyb[k], fzb[k], cdb, sdb, T.cd, T.sd);
+                tire_rev<true>(tire_ref(T, k), K, kb, xedotnb[k], yedotnb[k], fxb[k], fyb[k], Myb[k], rStatb[k], xeb, yeb,
+                               omb, vsxinb[k], vsyb[k], fzb[k], cdb, sdb, T.at(TS_(cd)), T.at(TS_(sd)));
             else {
                 double cdum = 0, sdum = 0;
-                tire_rev<false>(T.t[k], K, kb, xedotnb[k], yedotnb[k], fxb[k], fyb[k], Myb[k], rStatb[k], xeb, yeb,
+                tire_rev<false>(tire_ref(T, k), K, kb, xedotnb[k], yedotnb[k], fxb[k], fyb[k], Myb[k], rStatb[k], xeb, yeb,
                                 omb, vsxinb[k], vsyb[k], fzb[k], cdum, sdum, 1.0, 0.0);
             }
             L.xe[k] = xeb;
@@ -1005,39 +1035,39 @@ __device__ __forceinline__ void rev18(const StepTape& T, const KView& K, const C
     }
     // vehicle-to-tire transform
     {
-        const double vsyfb = vsyb[0] + vsyb[1] + T.sd * (vsxinb[0] + vsxinb[1]);
-        sdb += T.vsyf * (vsxinb[0] + vsxinb[1]);
-        cdb += (T.u - T.wcf) * vsxinb[0] + (T.u + T.wcf) * vsxinb[1];
-        ub += T.cd * (vsxinb[0] + vsxinb[1]) + vsxinb[2] + vsxinb[3];
-        const double wcfb = T.cd * (vsxinb[1] - vsxinb[0]);
+        const double vsyfb = vsyb[0] + vsyb[1] + T.at(TS_(sd)) * (vsxinb[0] + vsxinb[1]);
+        sdb += T.at(TS_(vsyf)) * (vsxinb[0] + vsxinb[1]);
+        cdb += (T.at(TS_(u)) - T.at(TS_(wcf))) * vsxinb[0] + (T.at(TS_(u)) + T.at(TS_(wcf))) * vsxinb[1];
+        ub += T.at(TS_(cd)) * (vsxinb[0] + vsxinb[1]) + vsxinb[2] + vsxinb[3];
+        const double wcfb = T.at(TS_(cd)) * (vsxinb[1] - vsxinb[0]);
         const double wcrb = vsxinb[3] - vsxinb[2];
         const double vsyrb = vsyb[2] + vsyb[3];
         wzb += K(K_A) * vsyfb - K(K_B) * vsyrb + K(K_CF2) * wcfb + K(K_CR2) * wcrb;
         vb += vsyfb + vsyrb;
-        kb.add(KB_A, T.wz * vsyfb);
+        kb.add(KB_A, T.at(TS_(wz)) * vsyfb);
     }
     // wheel angle
-    steerb += T.dslope * (T.cd * sdb - T.sd * cdb);
+    steerb += T.at(TS_(dslope)) * (T.at(TS_(cd)) * sdb - T.at(TS_(sd)) * cdb);
     // tire loads (with the previous step's accelerations)
     double udot_oldb, vdot_oldb;
     {
-        const double g0 = T.fzarg[0] > 0 ? 1.0 : 0.0, g1 = T.fzarg[1] > 0 ? 1.0 : 0.0;
-        const double g2 = T.fzarg[2] > 0 ? 1.0 : 0.0, g3 = T.fzarg[3] > 0 ? 1.0 : 0.0;
+        const double g0 = T.at(TS_(fzarg) + 0) > 0 ? 1.0 : 0.0, g1 = T.at(TS_(fzarg) + 1) > 0 ? 1.0 : 0.0;
+        const double g2 = T.at(TS_(fzarg) + 2) > 0 ? 1.0 : 0.0, g3 = T.at(TS_(fzarg) + 3) > 0 ? 1.0 : 0.0;
         const double Afb = fzb[0] * g0 + fzb[1] * g1, Bfb = -fzb[0] * g0 + fzb[1] * g1;
         const double Arb = fzb[2] * g2 + fzb[3] * g3, Brb = -fzb[2] * g2 + fzb[3] * g3;
         const double Z4b = -Afb + Arb;
         kb.add(KB_Z1F, Afb);
         kb.add(KB_Z1R, Arb);
         const double latb = K(K_Z2F) * Bfb + K(K_Z2R) * Brb;
-        kb.add(KB_Z2F, T.lat * Bfb);
-        kb.add(KB_Z2R, T.lat * Brb);
+        kb.add(KB_Z2F, T.at(TS_(lat)) * Bfb);
+        kb.add(KB_Z2R, T.at(TS_(lat)) * Brb);
         phib += K(K_Z3FK) * Bfb + K(K_Z3RK) * Brb;
         wxb += K(K_Z3FB) * Bfb + K(K_Z3RB) * Brb;
         const double lonb = K(K_Z4) * Z4b;
-        kb.add(KB_Z4, T.lon * Z4b);
-        wzb += T.u * latb - T.v * lonb;
-        ub += T.wz * latb;
-        vb += -T.wz * lonb;
+        kb.add(KB_Z4, T.at(TS_(lon)) * Z4b);
+        wzb += T.at(TS_(u)) * latb - T.at(TS_(v)) * lonb;
+        ub += T.at(TS_(wz)) * latb;
+        vb += -T.at(TS_(wz)) * lonb;
         vdot_oldb = latb;
         udot_oldb = lonb;
     }

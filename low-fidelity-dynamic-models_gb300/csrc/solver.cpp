@@ -112,7 +112,7 @@ struct lfdm_solver {
     DevBuf<uint32_t> d_status;
     DevBuf<unsigned> d_bad;
     // differentiable rollout (lfdm_traj18_*)
-    DevBuf<double> d_adj_ckpt, d_adj_tape, d_adj_kbar;
+    DevBuf<double> d_adj_ckpt, d_adj_tape;
     unsigned adj_nsteps = 0, adj_ckpt = 0;
     bool adj_valid = false;
     double adj_fwd_ms = 0, adj_bwd_ms = 0;
@@ -958,6 +958,7 @@ static AdjLaunch traj_launch(lfdm_solver* h, const double* ctl, const double* re
     A.weight_u = weight_u;
     A.K = h->d_K.p;
     A.classes = reinterpret_cast<const ClassDev18*>(h->d_classes.p);
+    A.nclasses = (int)h->classes.size();
     A.class_of = h->d_class_of.p;
     A.params = h->d_params.p;
     A.S0 = h->d_S.p;
@@ -965,7 +966,6 @@ static AdjLaunch traj_launch(lfdm_solver* h, const double* ctl, const double* re
     A.ref = ref;
     A.ckpts = h->d_adj_ckpt.p;
     A.tape = h->d_adj_tape.p;
-    A.kbar = h->d_adj_kbar.p;
     return A;
 }
 
@@ -1001,7 +1001,6 @@ int lfdm_traj18_backward(lfdm_solver* h, const double* ctl, const double* ref, u
     if (!h->adj_valid || h->adj_nsteps != nsteps || h->adj_ckpt != ckpt_every)
         return h->fail(LFDM_ERR_STATE, "call lfdm_traj18_forward with the same steps and checkpoint interval first");
     CK(h->d_adj_tape.ensure((size_t)ckpt_every * traj18_tape_doubles_per_step() * h->npad));
-    CK(h->d_adj_kbar.ensure((size_t)30 * h->npad));
     AdjLaunch A = traj_launch(h, ctl, ref, nsteps, weight_u, ckpt_every);
     A.grad_ctl = grad_ctl;
     A.grad_params = grad_params;
