@@ -288,8 +288,9 @@ int lfdm_window_steps(lfdm_solver* h, double t, unsigned* nsteps, double* times,
 /* [nsteps][3][N] = {steering, throttle, braking} (DEVICE pointers, row stride N); per vehicle      */
 /* loss[N] = sum over steps of e_lat^2 + e_head^2 + weight_u*|u_k|^2 on the state after each step, */
 /* e_lat = -(x - xr) sin(psir) + (y - yr) cos(psir), e_head = psi - psir, ref [nsteps][3][N] =    */
-/* {xr, yr, psir}. The forward stores a checkpoint every ckpt_every steps; the backward (same      */
-/* arguments) recomputes each segment and runs the hand-written adjoint of the step: grad_ctl      */
+/* {xr, yr, psir}. The forward stores a checkpoint every ckpt_every steps and the last segment's   */
+/* step tape; the backward (same arguments) recomputes each earlier segment and runs the           */
+/* hand-written adjoint of the step: grad_ctl                                                      */
 /* [nsteps][3][N], grad_params [5][N] (mass, Jz, CG-to-front distance a with b held, tire friction */
 /* scale on fxmPn..fysP2n at scale 1, tire vertical stiffness kt), grad_state0 [31][N] or NULL     */
 /* (adjoint of x, y, u, v, psi, wz, phi, wx, udot, vdot, crank, then xe, ye, xedot, yedot, omega   */

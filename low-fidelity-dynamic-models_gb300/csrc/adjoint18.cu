@@ -6,8 +6,9 @@
 //   e_lat = -(x - xr) sin(psir) + (y - yr) cos(psir), e_head = psi - psir,
 //   L += e_lat^2 + e_head^2 + w (steering^2 + throttle^2 + braking^2),
 // with the reference path ref[k][3][n] = {xr, yr, psir} at the end of step k.
-// Backward: the forward stores the state every `ckpt` steps. The backward runs the segments last to
-// first: it recomputes the segment from its checkpoint with fwd18_tape (dof18_adjoint.cuh), storing
+// Backward: the forward stores the state every `ckpt` steps and runs the last segment with
+// fwd18_tape, leaving that segment's tape in HBM. The backward runs the segments last to first: it
+// recomputes each earlier segment from its checkpoint with fwd18_tape (dof18_adjoint.cuh), storing
 // each step's tape in HBM, then sweeps the segment backwards with rev18, writing the control
 // gradients and accumulating the adjoints of the parameter-dependent constants; at the end those
 // are contracted with dK/dp (forward-mode dual numbers through the prepare formulas) for the
@@ -127,11 +128,19 @@ __global__ void __launch_bounds__(128) traj18_forward_kernel(const AdjLaunch A) 
     load_state18(A.S0 + vid, np, v, va, ts, ta);
     const size_t nu = (size_t)A.n;
     double loss = 0;
+    // the last segment runs with its tape (the backward starts there and then needs no recompute);
+    // fwd18_tape and step18 round identically, so the states do not depend on which one ran
+    const int klast = ((A.nsteps - 1) / A.ckpt) * A.ckpt;
     for (int k = 0; k < A.nsteps; ++k) {
         if (k % A.ckpt == 0) store_ckpt(A.ckpts + (size_t)(k / A.ckpt) * kCkptFields * np + vid, np, v, ts);
         const double* U = A.ctl + (size_t)k * 3 * nu + vid;
         const double st = __ldg(U), th = __ldg(U + nu), br = __ldg(U + 2 * nu);
-        step18<false>(v, va, ts, ta, K, C, st, th, br, A.dt);
+        if (k < klast) {
+            step18<false>(v, va, ts, ta, K, C, st, th, br, A.dt);
+        } else {
+            const TapeRef T{A.tape + (size_t)(k - klast) * kStepTapeDoubles * np + vid, np};
+            fwd18_tape(v, va, ts, ta, T, K, C, st, th, br, A.dt);
+        }
         loss += step_loss(A, k, vid, v.x, v.y, v.psi, st, th, br);
     }
     A.loss[vid] = loss;
@@ -219,15 +228,17 @@ __global__ void __launch_bounds__(128) traj18_backward_kernel(const AdjLaunch A)
     const int nseg = (A.nsteps + A.ckpt - 1) / A.ckpt;
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int k0 = seg * A.ckpt, k1 = min(A.nsteps, k0 + A.ckpt);
-        VehC v;
-        VehAux va = {};
-        TireC ts[4];
-        TireAux ta[4] = {};
-        load_ckpt(A.ckpts + (size_t)seg * kCkptFields * np + vid, np, v, ts);
-        for (int k = k0; k < k1; ++k) {
-            const double* U = A.ctl + (size_t)k * 3 * nu + vid;
-            const TapeRef T{A.tape + (size_t)(k - k0) * kStepTapeDoubles * np + vid, np};
-            fwd18_tape(v, va, ts, ta, T, K, C, __ldg(U), __ldg(U + nu), __ldg(U + 2 * nu), A.dt);
+        if (seg < nseg - 1) {  // the forward left the last segment's tape in place
+            VehC v;
+            VehAux va = {};
+            TireC ts[4];
+            TireAux ta[4] = {};
+            load_ckpt(A.ckpts + (size_t)seg * kCkptFields * np + vid, np, v, ts);
+            for (int k = k0; k < k1; ++k) {
+                const double* U = A.ctl + (size_t)k * 3 * nu + vid;
+                const TapeRef T{A.tape + (size_t)(k - k0) * kStepTapeDoubles * np + vid, np};
+                fwd18_tape(v, va, ts, ta, T, K, C, __ldg(U), __ldg(U + nu), __ldg(U + 2 * nu), A.dt);
+            }
         }
         for (int k = k1 - 1; k >= k0; --k) {
             const TapeRef T{A.tape + (size_t)(k - k0) * kStepTapeDoubles * np + vid, np};

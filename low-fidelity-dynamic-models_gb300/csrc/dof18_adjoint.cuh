@@ -11,7 +11,11 @@
 //
 // Branches (wheel lift-off, tmxy_combined regimes, clamps, sineStep bands, converter flow
 // direction, differential bias band, gear shifts, map segments) are differentiated on the branch
-// the forward step took; the gear is piecewise constant and carries no adjoint. Supported: TMeasy
+// the forward step took; the gear is piecewise constant and carries no adjoint.
+//
+// The library is compiled without implicit multiply-add contraction (so that every kernel that runs
+// a forward step rounds it alike); the reverse sweep, which no other kernel has to match, writes
+// its sums of products as explicit fma() instead, halving the FP64 instructions of those updates. Supported: TMeasy
 // tires, linear or mapped steering, with or without torque converter, throttleMod off.
 #pragma once
 
@@ -71,6 +75,7 @@ struct KBar {
     double* base;
     int stride;
     __device__ __forceinline__ void add(int i, double v) const { base[i * stride] += v; }
+    __device__ __forceinline__ double& at(int i) const { return base[i * stride]; }
 };
 
 // The differentiable state of one vehicle (the carried state of step18 minus the gear).
@@ -557,31 +562,31 @@ __device__ __forceinline__ void tmxy_rev(double s, double df0, double sm, double
     double df0locb = 0.0;
     const double is = 1.0 / s;
     if (s > ss) {  // full sliding: fos = fs / s
-        fsb += fosb * is;
-        sb += -fs * is * is * fosb;
+        fsb = fma(fosb, is, fsb);
+        sb = fma(-fs * is * is, fosb, sb);
         return;
     }
     if (s < sm) {  // adhesion: fos = df0loc / dn
         const double ifm = 1.0 / fm;
-        const double p = df0loc * sm * ifm - 2.0;
+        const double p = fma(df0loc * sm, ifm, -2.0);
         const double sn = s * ism;
         const double dn = fma(sn + p, sn, 1.0);
         const double idn = 1.0 / dn;
         const double dnb = -df0loc * idn * idn * fosb;
-        df0locb += fosb * idn;
-        const double snb = (2.0 * sn + p) * dnb;
+        df0locb = fma(fosb, idn, df0locb);
+        const double snb = (fma(2.0, sn, p)) * dnb;
         const double pb = sn * dnb;
-        df0locb += sm * ifm * pb;
-        smb += df0loc * ifm * pb;
-        fmb += -df0loc * sm * ifm * ifm * pb;
-        sb += snb * ism;
-        smb += -s * ism * ism * snb;
+        df0locb = fma(sm * ifm, pb, df0locb);
+        smb = fma(df0loc * ifm, pb, smb);
+        fmb = fma(-df0loc * sm * ifm * ifm, pb, fmb);
+        sb = fma(snb, ism, sb);
+        smb = fma(-s * ism * ism, snb, smb);
     } else {
         const double q = fm * ism;
         const double idsm = 1.0 / (df0loc * sm);
         const double a = q * q * idsm;
         const double ida = 1.0 / (a * (ss - sm));
-        const double sstar = sm + (fm - fs) * ida;
+        const double sstar = fma((fm - fs), ida, sm);
         double f, ab = 0.0, sstarb = 0.0;
         double b = 0.0, sn3 = 0.0;
         if (sstar <= ss) {
@@ -596,54 +601,54 @@ __device__ __forceinline__ void tmxy_rev(double s, double df0, double sm, double
             f = fm - (fm - fs) * sn3 * sn3 * (3.0 - 2.0 * sn3);
         }
         const double fb = fosb * is;  // fos = f / s
-        sb += -f * is * is * fosb;
+        sb = fma(-f * is * is, fosb, sb);
         if (sstar <= ss) {
             if (s <= sstar) {
                 fmb += fb;
-                ab += -(s - sm) * (s - sm) * fb;
-                sb += -2.0 * a * (s - sm) * fb;
-                smb += 2.0 * a * (s - sm) * fb;
+                ab = fma(-(s - sm) * (s - sm), fb, ab);
+                sb = fma(-2.0 * a * (s - sm), fb, sb);
+                smb = fma(2.0 * a * (s - sm), fb, smb);
             } else {
                 fsb += fb;
                 const double bb = (ss - s) * (ss - s) * fb;
-                ssb += 2.0 * b * (ss - s) * fb;
-                sb += -2.0 * b * (ss - s) * fb;
+                ssb = fma(2.0 * b * (ss - s), fb, ssb);
+                sb = fma(-2.0 * b * (ss - s), fb, sb);
                 const double id = 1.0 / (ss - sstar);
-                ab += (sstar - sm) * id * bb;
-                sstarb += (a * id + a * (sstar - sm) * id * id) * bb;
-                smb += -a * id * bb;
-                ssb += -a * (sstar - sm) * id * id * bb;
+                ab = fma((sstar - sm) * id, bb, ab);
+                sstarb = fma((fma(a, id, a * (sstar - sm) * id * id)), bb, sstarb);
+                smb = fma(-a * id, bb, smb);
+                ssb = fma(-a * (sstar - sm) * id * id, bb, ssb);
             }
         } else {
-            const double g = sn3 * sn3 * (3.0 - 2.0 * sn3);
-            fmb += fb * (1.0 - g);
-            fsb += fb * g;
-            const double snb = -(fm - fs) * (6.0 * sn3 - 6.0 * sn3 * sn3) * fb;
+            const double g = sn3 * sn3 * (fma(-2.0, sn3, 3.0));
+            fmb = fma(fb, (1.0 - g), fmb);
+            fsb = fma(fb, g, fsb);
+            const double snb = -(fm - fs) * (fma(6.0, sn3, -(6.0 * sn3) * sn3)) * fb;
             const double id = 1.0 / (ss - sm);
-            sb += snb * id;
-            smb += snb * (-id + (s - sm) * id * id);
-            ssb += -snb * (s - sm) * id * id;
+            sb = fma(snb, id, sb);
+            smb = fma(snb, (fma((s - sm) * id, id, -id)), smb);
+            ssb = fma(-snb * (s - sm) * id, id, ssb);
         }
         if (sstarb != 0.0) {  // sstar = sm + (fm - fs) / (a (ss - sm))
             smb += sstarb;
-            fmb += sstarb * ida;
-            fsb += -sstarb * ida;
+            fmb = fma(sstarb, ida, fmb);
+            fsb = fma(-sstarb, ida, fsb);
             const double denb = -(fm - fs) * ida * ida * sstarb;
-            ab += (ss - sm) * denb;
-            ssb += a * denb;
-            smb += -a * denb;
+            ab = fma((ss - sm), denb, ab);
+            ssb = fma(a, denb, ssb);
+            smb = fma(-a, denb, smb);
         }
         if (ab != 0.0) {  // a = q^2 / (df0loc sm), q = fm / sm
             const double qb = 2.0 * q * idsm * ab;
             df0locb += -a / df0loc * ab;
-            smb += -a * ism * ab;
-            fmb += qb * ism;
-            smb += -fm * ism * ism * qb;
+            smb = fma(-a * ism, ab, smb);
+            fmb = fma(qb, ism, fmb);
+            smb = fma(-fm * ism * ism, qb, smb);
         }
     }
     if (dsel) {  // df0loc = max(2 fm / sm, df0)
-        fmb += 2.0 * ism * df0locb;
-        smb += -2.0 * fm * ism * ism * df0locb;
+        fmb = fma(2.0 * ism, df0locb, fmb);
+        smb = fma(-2.0 * fm * ism * ism, df0locb, smb);
     } else {
         df0b += df0locb;
     }
@@ -663,41 +668,41 @@ __device__ __forceinline__ void tire_rev(const TapeRef& T, const KView& K, const
     const double wxb = (T.at(TT_(fxstr)) - T.at(TT_(Fx))) * fxb, wyb = (T.at(TT_(fystr)) - T.at(TT_(Fy))) * fyb;
     const double fxstrb = T.at(TT_(wxw)) * fxb, fystrb = T.at(TT_(wyw)) * fyb;
     const double Fxb = (1.0 - T.at(TT_(wxw))) * fxb, Fyb = (1.0 - T.at(TT_(wyw))) * fyb;
-    vsxb += T.at(TT_(dwx)) * (T.at(TT_(vsx)) >= 0 ? 1.0 : -1.0) * wxb;
+    vsxb = fma(T.at(TT_(dwx)) * (T.at(TT_(vsx)) >= 0 ? 1.0 : -1.0), wxb, vsxb);
     {
         const double arg = T.at(TT_(sy)) * T.at(TT_(vta));
         const double argb = T.at(TT_(dwy)) * (arg >= 0 ? 1.0 : -1.0) * wyb;
-        syb += T.at(TT_(vta)) * argb;
-        vtab += T.at(TT_(sy)) * argb;
+        syb = fma(T.at(TT_(vta)), argb, syb);
+        vtab = fma(T.at(TT_(sy)), argb, vtab);
     }
     double Gxb = 0, Gyb = 0;
     if (T.at(TT_(clx)) == 0.0) Gxb = fxstrb;
-    else kb.add(KB_FXMP2N, T.at(TT_(clx)) * fxstrb);
+    else kb.at(KB_FXMP2N) = fma(T.at(TT_(clx)), fxstrb, kb.at(KB_FXMP2N));
     if (T.at(TT_(cly)) == 0.0) Gyb = fystrb;
-    else kb.add(KB_FYMP2N, T.at(TT_(cly)) * fystrb);
-    xeb += cx * (Gxb + Fxb);
-    xedotb += dx * (Gxb + Fxb);
-    yeb += cy * (Gyb + Fyb);
-    yedotb += dy * (Gyb + Fyb);
+    else kb.at(KB_FYMP2N) = fma(T.at(TT_(cly)), fystrb, kb.at(KB_FYMP2N));
+    xeb = fma(cx, (Gxb + Fxb), xeb);
+    xedotb = fma(dx, (Gxb + Fxb), xedotb);
+    yeb = fma(cy, (Gyb + Fyb), yeb);
+    yedotb = fma(dy, (Gyb + Fyb), yedotb);
     // relaxation rates
     const double idenx = T.at(TT_(idenx)), ideny = T.at(TT_(ideny));
     const double numxb = xedotb * idenx, denxb = -T.at(TT_(xedot)) * idenx * xedotb;
     const double numyb = yedotb * ideny, denyb = -T.at(TT_(yedot)) * ideny * yedotb;
-    double vtxsb = -cx * T.at(TT_(xe)) * numxb + dx * denxb;
-    xeb += -T.at(TT_(vtxs)) * cx * numxb;
-    fosb += -T.at(TT_(vsx)) * numxb + denxb;
-    vsxb += -T.at(TT_(fos)) * numxb;
-    double vtysb = -cy * T.at(TT_(ye)) * numyb + dy * denyb;
-    yeb += -T.at(TT_(vtys)) * cy * numyb;
-    fosb += T.at(TT_(sy)) * T.at(TT_(vta)) * numyb + denyb;
-    syb += T.at(TT_(fos)) * T.at(TT_(vta)) * numyb;
-    vtab += T.at(TT_(fos)) * T.at(TT_(sy)) * numyb;
-    rwb += T.at(TT_(hsxn)) * vtxsb + T.at(TT_(hsyn)) * vtysb;
-    hsxnb += T.at(TT_(rw)) * vtxsb;
-    hsynb += T.at(TT_(rw)) * vtysb;
+    double vtxsb = fma(-cx * T.at(TT_(xe)), numxb, dx * denxb);
+    xeb = fma(-T.at(TT_(vtxs)) * cx, numxb, xeb);
+    fosb = fma(-T.at(TT_(vsx)), numxb, fosb + denxb);
+    vsxb = fma(-T.at(TT_(fos)), numxb, vsxb);
+    double vtysb = fma(-cy * T.at(TT_(ye)), numyb, dy * denyb);
+    yeb = fma(-T.at(TT_(vtys)) * cy, numyb, yeb);
+    fosb = fma(T.at(TT_(sy)) * T.at(TT_(vta)), numyb, fosb + denyb);
+    syb = fma(T.at(TT_(fos)) * T.at(TT_(vta)), numyb, syb);
+    vtab = fma(T.at(TT_(fos)) * T.at(TT_(sy)), numyb, vtab);
+    rwb = fma(T.at(TT_(hsxn)), vtxsb, fma(T.at(TT_(hsyn)), vtysb, rwb));
+    hsxnb = fma(T.at(TT_(rw)), vtxsb, hsxnb);
+    hsynb = fma(T.at(TT_(rw)), vtysb, hsynb);
     // rolling resistance (no adjoint through sgn)
-    fzcb += -K(K_RR) * T.at(TT_(rStat)) * T.at(TT_(sgn)) * Myb;
-    rStatb += -K(K_RR) * T.at(TT_(fzc)) * T.at(TT_(sgn)) * Myb;
+    fzcb = fma(-K(K_RR) * T.at(TT_(rStat)) * T.at(TT_(sgn)), Myb, fzcb);
+    rStatb = fma(-K(K_RR) * T.at(TT_(fzc)) * T.at(TT_(sgn)), Myb, rStatb);
     // combined-slip force curve
     double scb = 0, df0b = 0, smb = 0, fmb = 0, ssb = 0, fsb = 0;
     tmxy_rev(T.at(TT_(sc)), T.at(TT_(df0)), T.at(TT_(sm)), T.at(TT_(fm)), T.at(TT_(ss)), T.at(TT_(fs)), fosb, scb, df0b, smb, fmb, ssb, fsb);
@@ -707,132 +712,132 @@ __device__ __forceinline__ void tire_rev(const TapeRef& T, const KView& K, const
     auto hyp_rev = [](double a, double b, double h, double hb, double& ab, double& bb) {
         if (h > 0 && hb != 0.0) {
             const double t = hb / h;
-            ab += a * t;
-            bb += b * t;
+            ab = fma(a, t, ab);
+            bb = fma(b, t, bb);
         }
     };
     {
         double Pb = 0, Qb = 0;
         hyp_rev(T.at(TT_(sxs)) * cax, T.at(TT_(sys)) * say, T.at(TT_(ss)), ssb, Pb, Qb);
-        sxsb += cax * Pb;
-        caxb += T.at(TT_(sxs)) * Pb;
-        sysb += say * Qb;
-        sayb += T.at(TT_(sys)) * Qb;
+        sxsb = fma(cax, Pb, sxsb);
+        caxb = fma(T.at(TT_(sxs)), Pb, caxb);
+        sysb = fma(say, Qb, sysb);
+        sayb = fma(T.at(TT_(sys)), Qb, sayb);
     }
     {
         double Pb = 0, Qb = 0;
         hyp_rev(T.at(TT_(fxs)) * T.at(TT_(calpha)), T.at(TT_(fys)) * T.at(TT_(salpha)), T.at(TT_(fs)), fsb, Pb, Qb);
-        fxsb += T.at(TT_(calpha)) * Pb;
-        calphab += T.at(TT_(fxs)) * Pb;
-        fysb += T.at(TT_(salpha)) * Qb;
-        salphab += T.at(TT_(fys)) * Qb;
+        fxsb = fma(T.at(TT_(calpha)), Pb, fxsb);
+        calphab = fma(T.at(TT_(fxs)), Pb, calphab);
+        fysb = fma(T.at(TT_(salpha)), Qb, fysb);
+        salphab = fma(T.at(TT_(fys)), Qb, salphab);
     }
     {
         double Pb = 0, Qb = 0;
         hyp_rev(T.at(TT_(sxm)) * cax, T.at(TT_(sym)) * say, T.at(TT_(sm)), smb, Pb, Qb);
-        sxmb += cax * Pb;
-        caxb += T.at(TT_(sxm)) * Pb;
-        symb += say * Qb;
-        sayb += T.at(TT_(sym)) * Qb;
+        sxmb = fma(cax, Pb, sxmb);
+        caxb = fma(T.at(TT_(sxm)), Pb, caxb);
+        symb = fma(say, Qb, symb);
+        sayb = fma(T.at(TT_(sym)), Qb, sayb);
     }
-    calphab += T.at(TT_(ihx)) * caxb;
-    ihxb += T.at(TT_(calpha)) * caxb;
-    salphab += T.at(TT_(ihy)) * sayb;
-    ihyb += T.at(TT_(salpha)) * sayb;
+    calphab = fma(T.at(TT_(ihx)), caxb, calphab);
+    ihxb = fma(T.at(TT_(calpha)), caxb, ihxb);
+    salphab = fma(T.at(TT_(ihy)), sayb, salphab);
+    ihyb = fma(T.at(TT_(salpha)), sayb, ihyb);
     {
         double Pb = 0, Qb = 0;
         hyp_rev(T.at(TT_(fxm)) * T.at(TT_(calpha)), T.at(TT_(fym)) * T.at(TT_(salpha)), T.at(TT_(fm)), fmb, Pb, Qb);
-        fxmb += T.at(TT_(calpha)) * Pb;
-        calphab += T.at(TT_(fxm)) * Pb;
-        fymb += T.at(TT_(salpha)) * Qb;
-        salphab += T.at(TT_(fym)) * Qb;
+        fxmb = fma(T.at(TT_(calpha)), Pb, fxmb);
+        calphab = fma(T.at(TT_(fxm)), Pb, calphab);
+        fymb = fma(T.at(TT_(salpha)), Qb, fymb);
+        salphab = fma(T.at(TT_(fym)), Qb, salphab);
     }
     {
         double Pb = 0, Qb = 0;
         hyp_rev(T.at(TT_(dfx0)) * T.at(TT_(calpha)) * T.at(TT_(hsxn)), T.at(TT_(dfy0)) * T.at(TT_(salpha)) * T.at(TT_(hsyn)), T.at(TT_(df0)), df0b, Pb, Qb);
-        dfx0b += T.at(TT_(calpha)) * T.at(TT_(hsxn)) * Pb;
-        calphab += T.at(TT_(dfx0)) * T.at(TT_(hsxn)) * Pb;
-        hsxnb += T.at(TT_(dfx0)) * T.at(TT_(calpha)) * Pb;
-        dfy0b += T.at(TT_(salpha)) * T.at(TT_(hsyn)) * Qb;
-        salphab += T.at(TT_(dfy0)) * T.at(TT_(hsyn)) * Qb;
-        hsynb += T.at(TT_(dfy0)) * T.at(TT_(salpha)) * Qb;
+        dfx0b = fma(T.at(TT_(calpha)) * T.at(TT_(hsxn)), Pb, dfx0b);
+        calphab = fma(T.at(TT_(dfx0)) * T.at(TT_(hsxn)), Pb, calphab);
+        hsxnb = fma(T.at(TT_(dfx0)) * T.at(TT_(calpha)), Pb, hsxnb);
+        dfy0b = fma(T.at(TT_(salpha)) * T.at(TT_(hsyn)), Qb, dfy0b);
+        salphab = fma(T.at(TT_(dfy0)) * T.at(TT_(hsyn)), Qb, salphab);
+        hsynb = fma(T.at(TT_(dfy0)) * T.at(TT_(salpha)), Qb, hsynb);
     }
     double sxnb = 0, synb = 0;
     if (T.at(TT_(qpos)) != 0.0) {
-        const double iscb = T.at(TT_(sxn)) * calphab + T.at(TT_(syn)) * salphab;
-        sxnb += T.at(TT_(isc)) * calphab;
-        synb += T.at(TT_(isc)) * salphab;
-        const double sct = scb - iscb * T.at(TT_(isc)) * T.at(TT_(isc));
-        sxnb += T.at(TT_(sxn)) * T.at(TT_(isc)) * sct;
-        synb += T.at(TT_(syn)) * T.at(TT_(isc)) * sct;
+        const double iscb = fma(T.at(TT_(sxn)), calphab, T.at(TT_(syn)) * salphab);
+        sxnb = fma(T.at(TT_(isc)), calphab, sxnb);
+        synb = fma(T.at(TT_(isc)), salphab, synb);
+        const double sct = fma(-(iscb * T.at(TT_(isc))), T.at(TT_(isc)), scb);
+        sxnb = fma(T.at(TT_(sxn)) * T.at(TT_(isc)), sct, sxnb);
+        synb = fma(T.at(TT_(syn)) * T.at(TT_(isc)), sct, synb);
     }
-    sxb += T.at(TT_(ihx)) * sxnb;
-    ihxb += T.at(TT_(sx)) * sxnb;
-    syb += T.at(TT_(ihy)) * synb;
-    ihyb += T.at(TT_(sy)) * synb;
-    hsxnb += -T.at(TT_(ihx)) * T.at(TT_(ihx)) * ihxb;
-    hsynb += -T.at(TT_(ihy)) * T.at(TT_(ihy)) * ihyb;
+    sxb = fma(T.at(TT_(ihx)), sxnb, sxb);
+    ihxb = fma(T.at(TT_(sx)), sxnb, ihxb);
+    syb = fma(T.at(TT_(ihy)), synb, syb);
+    ihyb = fma(T.at(TT_(sy)), synb, ihyb);
+    hsxnb = fma(-T.at(TT_(ihx)) * T.at(TT_(ihx)), ihxb, hsxnb);
+    hsynb = fma(-T.at(TT_(ihy)) * T.at(TT_(ihy)), ihyb, hsynb);
     {
         const double issum = T.at(TT_(issum)), ifsum = T.at(TT_(ifsum));
         const double ssumb = -(T.at(TT_(sxm)) * hsxnb + T.at(TT_(sym)) * hsynb) * (issum * issum);
         const double fsumb = -(T.at(TT_(fxd)) * hsxnb + T.at(TT_(fyd)) * hsynb) * (ifsum * ifsum);
-        sxmb += hsxnb * issum + ssumb;
-        symb += hsynb * issum + ssumb;
-        const double fxdb = hsxnb * ifsum + fsumb;
-        const double fydb = hsynb * ifsum + fsumb;
-        fxmb += T.at(TT_(dfy0)) * fxdb;
-        dfy0b += T.at(TT_(fxm)) * fxdb;
-        fymb += T.at(TT_(dfx0)) * fydb;
-        dfx0b += T.at(TT_(fym)) * fydb;
+        sxmb = fma(hsxnb, issum, sxmb + ssumb);
+        symb = fma(hsynb, issum, symb + ssumb);
+        const double fxdb = fma(hsxnb, ifsum, fsumb);
+        const double fydb = fma(hsynb, ifsum, fsumb);
+        fxmb = fma(T.at(TT_(dfy0)), fxdb, fxmb);
+        dfy0b = fma(T.at(TT_(fxm)), fxdb, dfy0b);
+        fymb = fma(T.at(TT_(dfx0)), fydb, fymb);
+        dfx0b = fma(T.at(TT_(fym)), fydb, dfx0b);
     }
     // curve parameters from the normalised load
     const double fzn = T.at(TT_(fzn));
     double fznb = 0;
-    fznb += fma(-2.0 * K(K_Q2DFX0), fzn, K(K_Q1DFX0)) * dfx0b;
-    fznb += fma(-2.0 * K(K_Q2DFY0), fzn, K(K_Q1DFY0)) * dfy0b;
-    fznb += fma(-2.0 * K(K_Q2FXM), fzn, K(K_Q1FXM)) * fxmb;
-    fznb += fma(-2.0 * K(K_Q2FYM), fzn, K(K_Q1FYM)) * fymb;
-    fznb += fma(-2.0 * K(K_Q2FXS), fzn, K(K_Q1FXS)) * fxsb;
-    fznb += fma(-2.0 * K(K_Q2FYS), fzn, K(K_Q1FYS)) * fysb;
-    kb.add(KB_Q1FXM, fzn * fxmb);
-    kb.add(KB_Q2FXM, -fzn * fzn * fxmb);
-    kb.add(KB_Q1FYM, fzn * fymb);
-    kb.add(KB_Q2FYM, -fzn * fzn * fymb);
-    kb.add(KB_Q1FXS, fzn * fxsb);
-    kb.add(KB_Q2FXS, -fzn * fzn * fxsb);
-    kb.add(KB_Q1FYS, fzn * fysb);
-    kb.add(KB_Q2FYS, -fzn * fzn * fysb);
-    fznb += K(K_DSXM) * sxmb + K(K_DSYM) * symb + K(K_DSXS) * sxsb + K(K_DSYS) * sysb;
-    fzcb += K(K_INVPN) * fznb;
+    fznb = fma(fma(-2.0 * K(K_Q2DFX0), fzn, K(K_Q1DFX0)), dfx0b, fznb);
+    fznb = fma(fma(-2.0 * K(K_Q2DFY0), fzn, K(K_Q1DFY0)), dfy0b, fznb);
+    fznb = fma(fma(-2.0 * K(K_Q2FXM), fzn, K(K_Q1FXM)), fxmb, fznb);
+    fznb = fma(fma(-2.0 * K(K_Q2FYM), fzn, K(K_Q1FYM)), fymb, fznb);
+    fznb = fma(fma(-2.0 * K(K_Q2FXS), fzn, K(K_Q1FXS)), fxsb, fznb);
+    fznb = fma(fma(-2.0 * K(K_Q2FYS), fzn, K(K_Q1FYS)), fysb, fznb);
+    kb.at(KB_Q1FXM) = fma(fzn, fxmb, kb.at(KB_Q1FXM));
+    kb.at(KB_Q2FXM) = fma(-fzn * fzn, fxmb, kb.at(KB_Q2FXM));
+    kb.at(KB_Q1FYM) = fma(fzn, fymb, kb.at(KB_Q1FYM));
+    kb.at(KB_Q2FYM) = fma(-fzn * fzn, fymb, kb.at(KB_Q2FYM));
+    kb.at(KB_Q1FXS) = fma(fzn, fxsb, kb.at(KB_Q1FXS));
+    kb.at(KB_Q2FXS) = fma(-fzn * fzn, fxsb, kb.at(KB_Q2FXS));
+    kb.at(KB_Q1FYS) = fma(fzn, fysb, kb.at(KB_Q1FYS));
+    kb.at(KB_Q2FYS) = fma(-fzn * fzn, fysb, kb.at(KB_Q2FYS));
+    fznb = fma(K(K_DSXM), sxmb, fma(K(K_DSYM), symb, fma(K(K_DSXS), sxsb, fma(K(K_DSYS), sysb, fznb))));
+    fzcb = fma(K(K_INVPN), fznb, fzcb);
     if (T.at(TT_(fzcl)) == 0.0) fzb += fzcb;
     // slips
     const double ivta = T.at(TT_(ivta));
-    vsxb += -ivta * sxb;
-    vtab += T.at(TT_(vsx)) * ivta * ivta * sxb;
+    vsxb = fma(-ivta, sxb, vsxb);
+    vtab = fma(T.at(TT_(vsx)) * ivta * ivta, sxb, vtab);
     if (kSteered) {
         const double iD = 1.0 / T.at(TT_(D));
         const double Nb = -syb * iD, Db = T.at(TT_(N)) * (iD * iD) * syb;
-        vsyb += c * Nb + s * Db;
-        vtab += -s * Nb + c * Db;
-        cb += T.at(TT_(vsy)) * Nb + T.at(TT_(vta)) * Db;
-        sb_ += -T.at(TT_(vta)) * Nb + T.at(TT_(vsy)) * Db;
+        vsyb = fma(c, Nb, fma(s, Db, vsyb));
+        vtab = fma(-s, Nb, fma(c, Db, vtab));
+        cb = fma(T.at(TT_(vsy)), Nb, fma(T.at(TT_(vta)), Db, cb));
+        sb_ = fma(-T.at(TT_(vta)), Nb, fma(T.at(TT_(vsy)), Db, sb_));
     } else {
-        vsyb += -ivta * syb;
-        vtab += T.at(TT_(vsy)) * ivta * ivta * syb;
+        vsyb = fma(-ivta, syb, vsyb);
+        vtab = fma(T.at(TT_(vsy)) * ivta * ivta, syb, vtab);
     }
     rwb += vtab;
     double reffb = fabs(T.at(TT_(om))) * rwb;
-    omb += T.at(TT_(r_eff)) * T.at(TT_(sgn)) * rwb;
+    omb = fma(T.at(TT_(r_eff)) * T.at(TT_(sgn)), rwb, omb);
     vsxinb += vsxb;
-    omb += -T.at(TT_(r_eff)) * vsxb;
-    reffb += -T.at(TT_(om)) * vsxb;
+    omb = fma(-T.at(TT_(r_eff)), vsxb, omb);
+    reffb = fma(-T.at(TT_(om)), vsxb, reffb);
     // r_eff = rdynco xt + rStat, rStat = r0 - xt, xt = fz / kt
     double xtb = T.at(TT_(rdynco)) * reffb;
     rStatb += reffb;
     if (T.at(TT_(fzrd)) != 0.0) fzb += K(K_DRD) * K(K_INVPN) * (T.at(TT_(xt)) * reffb);  // rdynco interpolated in fz
     xtb += -rStatb;
-    fzb += K(K_INVKT) * xtb;
-    kb.add(KB_INVKT, T.at(TT_(fz)) * xtb);
+    fzb = fma(K(K_INVKT), xtb, fzb);
+    kb.at(KB_INVKT) = fma(T.at(TT_(fz)), xtb, kb.at(KB_INVKT));
 }
 
 // One step's reverse sweep. L: on entry the adjoint of the state after the step, on return that of
@@ -845,15 +850,15 @@ __device__ __forceinline__ void rev18(const TapeRef& T, const KView& K, const Cl
     // updated rates
     double u1b = dt * fma(T.at(TS_(cp)), L.x, T.at(TS_(sp)) * L.y);
     double v1b = dt * fma(-T.at(TS_(sp)), L.x, T.at(TS_(cp)) * L.y);
-    double psib = L.psi + dt * ((-T.at(TS_(u1)) * T.at(TS_(sp)) - T.at(TS_(v1)) * T.at(TS_(cp))) * L.x + (T.at(TS_(u1)) * T.at(TS_(cp)) - T.at(TS_(v1)) * T.at(TS_(sp))) * L.y);
-    double wz1b = dt * L.psi + L.wz;
-    double wx1b = dt * L.phi + L.wx;
+    double psib = fma(dt, (fma((fma(-T.at(TS_(u1)), T.at(TS_(sp)), -(T.at(TS_(v1))) * T.at(TS_(cp)))), L.x, (fma(T.at(TS_(u1)), T.at(TS_(cp)), -(T.at(TS_(v1))) * T.at(TS_(sp)))) * L.y)), L.psi);
+    double wz1b = fma(dt, L.psi, L.wz);
+    double wx1b = fma(dt, L.phi, L.wx);
     const double phib0 = L.phi;
     u1b += L.u;
     v1b += L.v;
     double ub = u1b, vb = v1b, wxb = wx1b, wzb = wz1b, phib = phib0;
-    const double udotb = dt * u1b + L.udot;  // the new accelerations are also carried to the next step
-    const double vdotb = dt * v1b + L.vdot;
+    const double udotb = fma(dt, u1b, L.udot);  // the new accelerations are also carried to the next step
+    const double vdotb = fma(dt, v1b, L.vdot);
     const double wxdotb = dt * wx1b, wzdotb = dt * wz1b;
     double crankb = 0, dOcb = 0, crank_outb = 0;
     if (C.tcbool) {
@@ -874,52 +879,52 @@ __device__ __forceinline__ void rev18(const TapeRef& T, const KView& K, const Cl
     double fxrb[4], fyrb[4];
     {
         const double innerb = K(K_INVMT) * udotb;
-        kb.add(KB_INVMT, T.at(TS_(inner)) * udotb);
-        wzb += T.at(TS_(v)) * udotb;
-        vb += T.at(TS_(wz)) * udotb;
-        wzb += (2.0 * K(K_UWZ2) * T.at(TS_(wz)) - K(K_UWZWX) * T.at(TS_(wx))) * innerb;
-        wxb += -K(K_UWZWX) * T.at(TS_(wz)) * innerb;
-        kb.add(KB_UWZ2, T.at(TS_(wz)) * T.at(TS_(wz)) * innerb);
-        kb.add(KB_UWZWX, -T.at(TS_(wz)) * T.at(TS_(wx)) * innerb);
+        kb.at(KB_INVMT) = fma(T.at(TS_(inner)), udotb, kb.at(KB_INVMT));
+        wzb = fma(T.at(TS_(v)), udotb, wzb);
+        vb = fma(T.at(TS_(wz)), udotb, vb);
+        wzb = fma((fma(2.0 * K(K_UWZ2), T.at(TS_(wz)), -K(K_UWZWX) * T.at(TS_(wx)))), innerb, wzb);
+        wxb = fma(-K(K_UWZWX) * T.at(TS_(wz)), innerb, wxb);
+        kb.at(KB_UWZ2) = fma(T.at(TS_(wz)) * T.at(TS_(wz)), innerb, kb.at(KB_UWZ2));
+        kb.at(KB_UWZWX) = fma(-T.at(TS_(wz)) * T.at(TS_(wx)), innerb, kb.at(KB_UWZWX));
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             fxrb[k] = innerb;
             fyrb[k] = 0;
         }
-        const double E1b = K(K_CV1) * vdotb + K(K_CV3) * wxdotb + K(K_CV2) * wzdotb;
-        const double E2b = K(K_CV2) * vdotb + K(K_CX2) * wxdotb + K(K_CZ2) * wzdotb;
-        const double E3b = K(K_CV3) * vdotb + K(K_CX3) * wxdotb + K(K_CX2) * wzdotb;
-        kb.add(KB_CV1, T.at(TS_(E1)) * vdotb);
-        kb.add(KB_CV2, T.at(TS_(E2)) * vdotb + T.at(TS_(E1)) * wzdotb);
-        kb.add(KB_CV3, T.at(TS_(E3)) * vdotb + T.at(TS_(E1)) * wxdotb);
-        kb.add(KB_CX2, T.at(TS_(E2)) * wxdotb + T.at(TS_(E3)) * wzdotb);
-        kb.add(KB_CX3, T.at(TS_(E3)) * wxdotb);
-        kb.add(KB_CZ2, T.at(TS_(E2)) * wzdotb);
+        const double E1b = fma(K(K_CV1), vdotb, fma(K(K_CV3), wxdotb, K(K_CV2) * wzdotb));
+        const double E2b = fma(K(K_CV2), vdotb, fma(K(K_CX2), wxdotb, K(K_CZ2) * wzdotb));
+        const double E3b = fma(K(K_CV3), vdotb, fma(K(K_CX3), wxdotb, K(K_CX2) * wzdotb));
+        kb.at(KB_CV1) = fma(T.at(TS_(E1)), vdotb, kb.at(KB_CV1));
+        kb.at(KB_CV2) = fma(T.at(TS_(E2)), vdotb, fma(T.at(TS_(E1)), wzdotb, kb.at(KB_CV2)));
+        kb.at(KB_CV3) = fma(T.at(TS_(E3)), vdotb, fma(T.at(TS_(E1)), wxdotb, kb.at(KB_CV3)));
+        kb.at(KB_CX2) = fma(T.at(TS_(E2)), wxdotb, fma(T.at(TS_(E3)), wzdotb, kb.at(KB_CX2)));
+        kb.at(KB_CX3) = fma(T.at(TS_(E3)), wxdotb, kb.at(KB_CX3));
+        kb.at(KB_CZ2) = fma(T.at(TS_(E2)), wzdotb, kb.at(KB_CZ2));
         double wub = K(K_E3WU) * E3b;
-        phib += K(K_E3PHI) * E3b;
-        wxb += K(K_E3WX) * E3b;
-        kb.add(KB_E3WU, T.at(TS_(wu)) * E3b);
-        kb.add(KB_E3PHI, T.at(TS_(phi)) * E3b);
+        phib = fma(K(K_E3PHI), E3b, phib);
+        wxb = fma(K(K_E3WX), E3b, wxb);
+        kb.at(KB_E3WU) = fma(T.at(TS_(wu)), E3b, kb.at(KB_E3WU));
+        kb.at(KB_E3PHI) = fma(T.at(TS_(phi)), E3b, kb.at(KB_E3PHI));
         const double fyf = T.at(TS_(fyr) + 0) + T.at(TS_(fyr) + 1), fyr = T.at(TS_(fyr) + 2) + T.at(TS_(fyr) + 3);
-        wub += K(K_E2WU) * E2b;
-        fxrb[3] += K(K_CR2) * E2b;
+        wub = fma(K(K_E2WU), E2b, wub);
+        fxrb[3] = fma(K(K_CR2), E2b, fxrb[3]);
         fxrb[2] -= K(K_CR2) * E2b;
-        fxrb[1] += K(K_CF2) * E2b;
+        fxrb[1] = fma(K(K_CF2), E2b, fxrb[1]);
         fxrb[0] -= K(K_CF2) * E2b;
         double fyfb = K(K_A) * E2b, fyrb_ = -K(K_B) * E2b;
-        kb.add(KB_E2WU, T.at(TS_(wu)) * E2b);
-        kb.add(KB_A, fyf * E2b);
-        wub += -K(K_MT) * E1b;
+        kb.at(KB_E2WU) = fma(T.at(TS_(wu)), E2b, kb.at(KB_E2WU));
+        kb.at(KB_A) = fma(fyf, E2b, kb.at(KB_A));
+        wub = fma(-K(K_MT), E1b, wub);
         fyfb += E1b;
         fyrb_ += E1b;
-        kb.add(KB_MT, -T.at(TS_(wu)) * E1b);
+        kb.at(KB_MT) = fma(-T.at(TS_(wu)), E1b, kb.at(KB_MT));
         (void)fyr;
         fyrb[0] += fyfb;
         fyrb[1] += fyfb;
         fyrb[2] += fyrb_;
         fyrb[3] += fyrb_;
-        wzb += T.at(TS_(u)) * wub;
-        ub += T.at(TS_(wz)) * wub;
+        wzb = fma(T.at(TS_(u)), wub, wzb);
+        ub = fma(T.at(TS_(wz)), wub, ub);
     }
     // front forces rotated into the vehicle frame
     double fxb[4], fyb[4], cdb = 0, sdb = 0;
@@ -945,11 +950,11 @@ __device__ __forceinline__ void rev18(const TapeRef& T, const KView& K, const Cl
         const double gk = K(K_INVJW) * dOmb[k];
         engb[k] = gk;
         Myb[k] = gk;
-        brakeb += -sgnd(om_mid[k]) * gk;
-        fxb[k] += -tire_ref(T, k).at(TT_(rStat)) * gk;
+        brakeb = fma(-sgnd(om_mid[k]), gk, brakeb);
+        fxb[k] = fma(-tire_ref(T, k).at(TT_(rStat)), gk, fxb[k]);
         rStatb[k] = -tire_ref(T, k).at(TT_(fx)) * gk;
     }
-    brkb += K(K_MAXBRAKE) * brakeb;
+    brkb = fma(K(K_MAXBRAKE), brakeb, brkb);
     auto split_rev = [](double torque, double alpha, double dal, double slowleft, double tlb, double trb, double wl,
                         double wr, double& wlb, double& wrb) {
         const double slowb = slowleft != 0.0 ? tlb : trb;
@@ -958,7 +963,7 @@ __device__ __forceinline__ void rev18(const TapeRef& T, const KView& K, const Cl
         const double diffb = dal * alphab;
         if (diffb != 0.0) {
             const double sg = (wl - wr) >= 0 ? 1.0 : -1.0;
-            wlb += sg * diffb;
+            wlb = fma(sg, diffb, wlb);
             wrb -= sg * diffb;
         }
         return alpha * slowb + (1.0 - alpha) * fastb;
@@ -976,23 +981,23 @@ __device__ __forceinline__ void rev18(const TapeRef& T, const KView& K, const Cl
             torque_inb += -torque_outb;
         } else {
             trb = -T.at(TS_(torque_in)) * torque_outb;
-            torque_inb += -T.at(TS_(tr)) * torque_outb;
+            torque_inb = fma(-T.at(TS_(tr)), torque_outb, torque_inb);
         }
         const double dtqb = K(K_INVCI) * dOcb;
-        torque_inb += K(K_INVCI) * dOcb;
-        thrb += T.at(TS_(dt_map)) * dtqb;
-        crankb += T.at(TS_(dt_slope)) * dtqb;
+        torque_inb = fma(K(K_INVCI), dOcb, torque_inb);
+        thrb = fma(T.at(TS_(dt_map)), dtqb, thrb);
+        crankb = fma(T.at(TS_(dt_slope)), dtqb, crankb);
         const double rb = (T.at(TS_(rev)) != 0.0 ? 2.0 * T.at(TS_(r)) : -2.0 * T.at(TS_(r))) * torque_inb;
         const double icf = 1.0 / T.at(TS_(cf));
         double omega_inb = rb * icf;
         const double cfb = -T.at(TS_(r)) * icf * rb;
-        const double srb = T.at(TS_(cfs)) * cfb + T.at(TS_(trs)) * trb;
+        const double srb = fma(T.at(TS_(cfs)), cfb, T.at(TS_(trs)) * trb);
         double omega_outb = 0;
         if (T.at(TS_(srmode)) != 0.0) {
             const double sr0b = T.at(TS_(rev)) != 0.0 ? -srb : srb;
             const double iin = 1.0 / T.at(TS_(omega_in));
-            omega_outb += sr0b * iin;
-            omega_inb += -T.at(TS_(omega_out)) * iin * iin * sr0b;
+            omega_outb = fma(sr0b, iin, omega_outb);
+            omega_inb = fma(-T.at(TS_(omega_out)) * iin * iin, sr0b, omega_inb);
         }
         const double omega_tb = omega_outb * C.invgear[g];
 #pragma unroll
@@ -1000,8 +1005,8 @@ __device__ __forceinline__ void rev18(const TapeRef& T, const KView& K, const Cl
         crankb += omega_inb;
     } else {
         const double dtqb = C.invgear[g] * torque_tb;
-        thrb += T.at(TS_(dt_map)) * dtqb;
-        crank_outb += T.at(TS_(dt_slope)) * dtqb;
+        thrb = fma(T.at(TS_(dt_map)), dtqb, thrb);
+        crank_outb = fma(T.at(TS_(dt_slope)), dtqb, crank_outb);
 #pragma unroll
         for (int k = 0; k < 4; ++k) om_midb[k] += 0.25 * crank_outb * C.invgear[g];
     }
@@ -1035,39 +1040,39 @@ __device__ __forceinline__ void rev18(const TapeRef& T, const KView& K, const Cl
     }
     // vehicle-to-tire transform
     {
-        const double vsyfb = vsyb[0] + vsyb[1] + T.at(TS_(sd)) * (vsxinb[0] + vsxinb[1]);
-        sdb += T.at(TS_(vsyf)) * (vsxinb[0] + vsxinb[1]);
-        cdb += (T.at(TS_(u)) - T.at(TS_(wcf))) * vsxinb[0] + (T.at(TS_(u)) + T.at(TS_(wcf))) * vsxinb[1];
-        ub += T.at(TS_(cd)) * (vsxinb[0] + vsxinb[1]) + vsxinb[2] + vsxinb[3];
+        const double vsyfb = fma(T.at(TS_(sd)), (vsxinb[0] + vsxinb[1]), vsyb[0] + vsyb[1]);
+        sdb = fma(T.at(TS_(vsyf)), (vsxinb[0] + vsxinb[1]), sdb);
+        cdb = fma((T.at(TS_(u)) - T.at(TS_(wcf))), vsxinb[0], fma((T.at(TS_(u)) + T.at(TS_(wcf))), vsxinb[1], cdb));
+        ub = fma(T.at(TS_(cd)), (vsxinb[0] + vsxinb[1]), ub + vsxinb[2] + vsxinb[3]);
         const double wcfb = T.at(TS_(cd)) * (vsxinb[1] - vsxinb[0]);
         const double wcrb = vsxinb[3] - vsxinb[2];
         const double vsyrb = vsyb[2] + vsyb[3];
-        wzb += K(K_A) * vsyfb - K(K_B) * vsyrb + K(K_CF2) * wcfb + K(K_CR2) * wcrb;
+        wzb = fma(K(K_A), vsyfb, fma(-K(K_B), vsyrb, fma(K(K_CF2), wcfb, fma(K(K_CR2), wcrb, wzb))));
         vb += vsyfb + vsyrb;
-        kb.add(KB_A, T.at(TS_(wz)) * vsyfb);
+        kb.at(KB_A) = fma(T.at(TS_(wz)), vsyfb, kb.at(KB_A));
     }
     // wheel angle
-    steerb += T.at(TS_(dslope)) * (T.at(TS_(cd)) * sdb - T.at(TS_(sd)) * cdb);
+    steerb = fma(T.at(TS_(dslope)), (fma(T.at(TS_(cd)), sdb, -(T.at(TS_(sd))) * cdb)), steerb);
     // tire loads (with the previous step's accelerations)
     double udot_oldb, vdot_oldb;
     {
         const double g0 = T.at(TS_(fzarg) + 0) > 0 ? 1.0 : 0.0, g1 = T.at(TS_(fzarg) + 1) > 0 ? 1.0 : 0.0;
         const double g2 = T.at(TS_(fzarg) + 2) > 0 ? 1.0 : 0.0, g3 = T.at(TS_(fzarg) + 3) > 0 ? 1.0 : 0.0;
-        const double Afb = fzb[0] * g0 + fzb[1] * g1, Bfb = -fzb[0] * g0 + fzb[1] * g1;
-        const double Arb = fzb[2] * g2 + fzb[3] * g3, Brb = -fzb[2] * g2 + fzb[3] * g3;
+        const double Afb = fma(fzb[0], g0, fzb[1] * g1), Bfb = fma(-fzb[0], g0, fzb[1] * g1);
+        const double Arb = fma(fzb[2], g2, fzb[3] * g3), Brb = fma(-fzb[2], g2, fzb[3] * g3);
         const double Z4b = -Afb + Arb;
         kb.add(KB_Z1F, Afb);
         kb.add(KB_Z1R, Arb);
-        const double latb = K(K_Z2F) * Bfb + K(K_Z2R) * Brb;
-        kb.add(KB_Z2F, T.at(TS_(lat)) * Bfb);
-        kb.add(KB_Z2R, T.at(TS_(lat)) * Brb);
-        phib += K(K_Z3FK) * Bfb + K(K_Z3RK) * Brb;
-        wxb += K(K_Z3FB) * Bfb + K(K_Z3RB) * Brb;
+        const double latb = fma(K(K_Z2F), Bfb, K(K_Z2R) * Brb);
+        kb.at(KB_Z2F) = fma(T.at(TS_(lat)), Bfb, kb.at(KB_Z2F));
+        kb.at(KB_Z2R) = fma(T.at(TS_(lat)), Brb, kb.at(KB_Z2R));
+        phib = fma(K(K_Z3FK), Bfb, fma(K(K_Z3RK), Brb, phib));
+        wxb = fma(K(K_Z3FB), Bfb, fma(K(K_Z3RB), Brb, wxb));
         const double lonb = K(K_Z4) * Z4b;
-        kb.add(KB_Z4, T.at(TS_(lon)) * Z4b);
-        wzb += T.at(TS_(u)) * latb - T.at(TS_(v)) * lonb;
-        ub += T.at(TS_(wz)) * latb;
-        vb += -T.at(TS_(wz)) * lonb;
+        kb.at(KB_Z4) = fma(T.at(TS_(lon)), Z4b, kb.at(KB_Z4));
+        wzb = fma(T.at(TS_(u)), latb, fma(-(T.at(TS_(v))), lonb, wzb));
+        ub = fma(T.at(TS_(wz)), latb, ub);
+        vb = fma(-T.at(TS_(wz)), lonb, vb);
         vdot_oldb = latb;
         udot_oldb = lonb;
     }

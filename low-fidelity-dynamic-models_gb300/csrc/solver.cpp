@@ -977,6 +977,7 @@ int lfdm_traj18_forward(lfdm_solver* h, const double* ctl, const double* ref, un
     if (rc) return rc;
     const size_t nseg = (nsteps + ckpt_every - 1) / ckpt_every;
     CK(h->d_adj_ckpt.ensure(nseg * (size_t)traj18_ckpt_fields() * h->npad));
+    CK(h->d_adj_tape.ensure((size_t)ckpt_every * traj18_tape_doubles_per_step() * h->npad));
     AdjLaunch A = traj_launch(h, ctl, ref, nsteps, weight_u, ckpt_every);
     A.loss = loss;
     CK(cudaEventRecord(h->ev0, h->stream));
