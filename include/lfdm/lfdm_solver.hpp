@@ -1,0 +1,172 @@
+// C++ drop-in layer over liblfdm's C ABI (../lfdm.h). The three model headers beside this one,
+// dof11_halfImplicit_gpu.cuh, dof18_halfImplicit_gpu.cuh and dof24_halfImplicit_gpu.cuh, carry the
+// names the reference's GPU solver headers export (11dof-gpu/dof11_halfImplicit_gpu.cuh:16,
+// 18dof-gpu/dof18_halfImplicit_gpu.cuh:15-343, 24dof-gpu/dof24_halfImplicit_gpu.cuh:15): the
+// classes d11/d18/d24SolverHalfImplicitGPU with the same constructor, Construct/Initialize
+// overloads, setters, Solve, SolveStep, GetSimState and GetTireType, and the state structs of the
+// namespaces d11GPU/d18GPU/d24GPU with the same field names. Code written against the reference
+// compiles against these headers (add include/lfdm to the include path) and links with
+// -llfdm; every method forwards to one or two lfdm_* calls.
+//
+// Header-only, plain C++17: nvcc is not needed to compile a caller.
+//
+// Errors. The reference prints CUDA errors and carries on (utils/utils_gpu.cuh CHECK_CUDA_ERROR),
+// asserts (compiled out in Release) or calls exit() (SolveStep with CSV output set). Here every
+// failing lfdm_* call prints "lfdm: <method>: <message>" to stderr and the method returns, so a
+// program behaves as it did against the reference; define LFDM_CPP_THROW before including to get a
+// std::runtime_error instead.
+//
+// Differences a caller can see:
+//  - SolveStep(t, func): the reference launches a kernel that calls a __device__ functor at every
+//    step. A C ABI cannot carry a device functor, so the functor is called on the host, once per
+//    step of the window, at the step's start time (the times the reference's kernel passes it),
+//    and the window runs with that control schedule. The functor therefore has to be callable on
+//    the host: mark its operator() __host__ __device__ when compiling with nvcc.
+//  - The public m_sim_data / m_sim_states arrays are not exposed; parameters and states of
+//    individual vehicles are read and written through handle() and the lfdm_get/set_params and
+//    lfdm_get/set_states extensions of lfdm.h.
+#pragma once
+
+#include <cstddef>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../lfdm.h"
+
+#ifndef LFDM_TIRE_TYPE_DEFINED
+#define LFDM_TIRE_TYPE_DEFINED
+// 18dof-gpu/dof18_gpu.cuh:12 (the 11- and 24-DOF headers declare the same enum; here it is
+// declared once, so several model headers can be included together).
+enum class TireType { TMeasy, TMeasyNr };
+#endif
+
+#ifndef LFDM_DRIVER_INPUT_DEFINED
+#define LFDM_DRIVER_INPUT_DEFINED
+// utils/utils_gpu.cuh:29-40: one row of a driver table, and what a SolveStep functor fills in.
+struct DriverInput {
+    DriverInput() : m_time(0), m_steering(0), m_throttle(0), m_braking(0) {}
+    DriverInput(double time, double steering, double throttle, double braking)
+        : m_time(time), m_steering(steering), m_throttle(throttle), m_braking(braking) {}
+    double m_time;
+    double m_steering;
+    double m_throttle;
+    double m_braking;
+};
+#endif
+
+namespace lfdm_cpp {
+
+inline void check(int rc, const lfdm_solver* h, const char* what) {
+    if (rc == LFDM_OK) return;
+    const char* m = lfdm_last_error(h);
+    const std::string msg = std::string(what) + ": " + (m ? m : "error");
+#ifdef LFDM_CPP_THROW
+    throw std::runtime_error(msg);
+#else
+    std::fprintf(stderr, "lfdm: %s\n", msg.c_str());
+#endif
+}
+
+inline int tire_code(TireType t) { return t == TireType::TMeasyNr ? LFDM_TIRE_TMEASY_NR : LFDM_TIRE_TMEASY; }
+
+// Copy between a struct's double fields (listed as member pointers, in the struct's field order)
+// and a slice of the flat per-vehicle state vector of lfdm.h.
+template <typename S, std::size_t N>
+inline void put(const S& s, double S::*const (&fields)[N], double* dst) {
+    for (std::size_t i = 0; i < N; ++i) dst[i] = s.*fields[i];
+}
+template <typename S, std::size_t N>
+inline void get(S& s, double S::*const (&fields)[N], const double* src) {
+    for (std::size_t i = 0; i < N; ++i) s.*fields[i] = src[i];
+}
+
+// What the three solver classes share: lifetime, setters, Solve and SolveStep.
+template <int Model>
+class SolverBase {
+  public:
+    explicit SolverBase(unsigned int total_num_vehicles) {
+        check(lfdm_create(Model, total_num_vehicles, &h_), nullptr, "constructor");
+    }
+    ~SolverBase() {
+        if (h_) lfdm_destroy(h_);
+    }
+    SolverBase(const SolverBase&) = delete;
+    SolverBase& operator=(const SolverBase&) = delete;
+
+    void SetEndTime(double tend) { check(lfdm_set_end_time(h_, tend), h_, "SetEndTime"); }
+    void SetTimeStep(double step) { check(lfdm_set_time_step(h_, step), h_, "SetTimeStep"); }
+    void SetKernelSimTime(double time) { check(lfdm_set_kernel_sim_time(h_, time), h_, "SetKernelSimTime"); }
+    void SetHostDumpTime(double time) { check(lfdm_set_host_dump_time(h_, time), h_, "SetHostDumpTime"); }
+    void SetThreadsPerBlock(unsigned int threads) {
+        check(lfdm_set_threads_per_block(h_, threads), h_, "SetThreadsPerBlock");
+    }
+    double GetStep() {
+        double v = 0;
+        check(lfdm_get_step(h_, &v), h_, "GetStep");
+        return v;
+    }
+    double GetEndTime() {
+        double v = 0;
+        check(lfdm_get_end_time(h_, &v), h_, "GetEndTime");
+        return v;
+    }
+    void SetOutput(const std::string& output_file, double output_freq, bool store_all = false,
+                   unsigned int no_outs = 50) {
+        check(lfdm_set_output(h_, output_file.c_str(), output_freq, store_all ? 1 : 0, no_outs), h_, "SetOutput");
+    }
+    void Solve() { check(lfdm_solve(h_), h_, "Solve"); }
+    double SolveStep(double t, double steering, double throttle, double braking) {
+        double t_out = t;
+        check(lfdm_solve_step(h_, t, steering, throttle, braking, &t_out), h_, "SolveStep");
+        return t_out;
+    }
+    // Functor form (18dof-gpu/dof18_halfImplicit_gpu.cuh:234-287): func(t, DriverInput*) is called on
+    // the host at each step start time of the window [t, t + kernel_sim_time).
+    template <typename Func>
+    double SolveStep(double t, Func func) {
+        unsigned int n = 0;
+        check(lfdm_window_steps(h_, t, &n, nullptr, 0), h_, "SolveStep");
+        std::vector<double> times(n), ctl(3 * static_cast<std::size_t>(n));
+        if (n) check(lfdm_window_steps(h_, t, &n, times.data(), n), h_, "SolveStep");
+        for (unsigned int k = 0; k < n; ++k) {
+            DriverInput d(times[k], 0.0, 0.0, 0.0);
+            func(times[k], &d);
+            ctl[3 * k] = d.m_steering;
+            ctl[3 * k + 1] = d.m_throttle;
+            ctl[3 * k + 2] = d.m_braking;
+        }
+        double t_out = t;
+        check(lfdm_solve_step_schedule(h_, t, ctl.data(), n, 0, &t_out), h_, "SolveStep");
+        return t_out;
+    }
+    TireType GetTireType() const {
+        int t = LFDM_TIRE_TMEASY;
+        check(lfdm_get_tire_type(h_, &t), h_, "GetTireType");
+        return t == LFDM_TIRE_TMEASY_NR ? TireType::TMeasyNr : TireType::TMeasy;
+    }
+    // Extension: the C-ABI handle, for the lfdm_* calls that have no method here (per-vehicle
+    // parameters, states and controls, response buffers, precision, timing).
+    lfdm_solver* handle() const { return h_; }
+
+  protected:
+    void construct(const std::string& veh, const std::string& tire, const std::string* sus, unsigned int n,
+                   const std::string* driver, TireType type) {
+        check(lfdm_construct(h_, veh.c_str(), tire.c_str(), sus ? sus->c_str() : nullptr, n,
+                             driver ? driver->c_str() : nullptr, tire_code(type)),
+              h_, "Construct");
+    }
+    void initialize(const std::vector<double>& flat, unsigned int n) {
+        check(lfdm_initialize(h_, flat.data(), n), h_, "Initialize");
+    }
+    std::vector<double> flat_state(unsigned int i, std::size_t count) {
+        std::vector<double> s(count, 0.0);
+        check(lfdm_get_sim_state(h_, i, s.data()), h_, "GetSimState");
+        return s;
+    }
+
+    lfdm_solver* h_ = nullptr;
+};
+
+}  // namespace lfdm_cpp

@@ -39,6 +39,18 @@ def golden18():
 
 
 @pytest.fixture(scope="session")
+def golden11_cases():
+    with open(os.path.join(TESTS, "golden", "golden11.json")) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="session")
+def golden24_cases():
+    with open(os.path.join(TESTS, "golden", "golden24.json")) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="session")
 def built_lib():
     """Build liblfdm.so if needed (nvcc cross-compiles without a GPU)."""
     pkg_mod("build").build()
