@@ -261,14 +261,15 @@ __device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, const Tape
     T.at(TT_(qpos)) = q > 0 ? 1.0 : 0.0;
     auto hyp = [](double a, double b) { return sqrt(fma(a, a, b * b)); };
     const double df0 = hyp(dfx0 * calpha * hsxn, dfy0 * salpha * hsyn);
-    const double fm = hyp(fxm * calpha, fym * salpha);
+    double fm, ifm, sm, ism;
+    hyp_rcp(fxm * calpha, fym * salpha, fm, ifm);
     const double cax = calpha * ihx, say = salpha * ihy;
-    const double sm = hyp(sxm * cax, sym * say);
+    hyp_rcp(sxm * cax, sym * say, sm, ism);
     const double fs = hyp(fxs * calpha, fys * salpha);
     const double ss = hyp(sxs * cax, sys * say);
     T.at(TT_(df0)) = df0; T.at(TT_(fm)) = fm; T.at(TT_(sm)) = sm; T.at(TT_(fs)) = fs; T.at(TT_(ss)) = ss;
     double f, fos;
-    tmxy(f, fos, sc, df0, sm, fm, ss, fs);
+    tmxy_rcp(f, fos, sc, isc, df0, sm, ism, fm, ifm, ss, fs);
     T.at(TT_(fos)) = fos;
     T.at(TT_(sgn)) = sgnd(omega);
     ta.My = -K(K_RR) * fzc * ta.rStat * T.at(TT_(sgn));

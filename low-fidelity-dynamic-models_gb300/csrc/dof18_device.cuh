@@ -61,6 +61,7 @@ struct MapDev {
     double y[LFDM_MAX_MAP];
     double dx[LFDM_MAX_MAP];     // x[k+1] - x[k]
     double dy[LFDM_MAX_MAP];     // y[k+1] - y[k]
+    double idx[LFDM_MAX_MAP];    // 1 / dx[k]
 };
 struct ClassDev18 {
     int nonLinearSteer, tcbool, throttleMod, driveType, whichWheels, noGears;
@@ -82,15 +83,17 @@ __device__ __forceinline__ int lower_bound_x(const double* a, int n, double x) {
     return l;
 }
 
-// getMapY (utils/utils_gpu.cu:60-75): clamp outside, linear interpolation inside. The quotient is
-// kept as a division: at a grid point it is exactly 1 (or 0), so an engine at rest sees exactly the
-// tabulated loss torque (0 at 0 rad/s) and stays at rest, as in the reference.
+// getMapY (utils/utils_gpu.cu:60-75): clamp outside, linear interpolation inside. The quotient
+// (x - x[l]) / dx[l] is a product with the segment's stored reciprocal, except at the segment's
+// right grid point, where it is exactly 1 as the reference's division gives: a map evaluated at a
+// grid point returns the tabulated value (an engine at rest sees exactly the loss torque at
+// 0 rad/s and stays at rest, as in the reference).
 __device__ __forceinline__ double map_y(const MapDev& m, double x) {
     if (x <= m.x[0]) return m.y[0];
     if (x >= m.x[m.n - 1]) return m.y[m.n - 1];
-    int r = lower_bound_x(m.x, m.n, x);
-    int l = r - 1;
-    double mbar = (x - m.x[l]) / m.dx[l];
+    const int r = lower_bound_x(m.x, m.n, x);
+    const int l = r - 1;
+    const double mbar = (x == m.x[r]) ? 1.0 : (x - m.x[l]) * m.idx[l];
     return fma(mbar, m.dy[l], m.y[l]);
 }
 
@@ -277,6 +280,59 @@ struct KView {
     __device__ __forceinline__ double operator()(int i) const { return base[i * stride]; }
 };
 
+// tmxy_combined (dof18_gpu.cu:243-285) given the reciprocals of s, sm and fm (is, ism, ifm; the
+// TMeasy tire has them from the rsqrt of the squared norms it takes anyway): the full-sliding and
+// adhesion regimes, which nearly every step is in, then need one division (1/dn) instead of four.
+__device__ __forceinline__ void tmxy_rcp(double& f, double& fos, double s, double is, double df0, double sm,
+                                         double ism, double fm, double ifm, double ss, double fs) {
+    double df0loc = 0.0;
+    if (sm > 0.0) df0loc = fmax(2.0 * fm * ism, df0);
+    if (s > 0.0 && df0loc > 0.0) {
+        if (s > ss) {
+            f = fs;
+            fos = fs * is;
+        } else if (s < sm) {  // adhesion
+            const double p = df0loc * sm * ifm - 2.0;
+            const double sn = s * ism;
+            const double dn = fma(sn + p, sn, 1.0);
+            const double idn = 1.0 / dn;
+            f = df0loc * sm * sn * idn;
+            fos = df0loc * idn;
+        } else {
+            const double q = fm * ism;
+            const double a = q * q / (df0loc * sm);
+            const double sstar = sm + (fm - fs) / (a * (ss - sm));
+            if (sstar <= ss) {
+                if (s <= sstar) {
+                    f = fm - a * (s - sm) * (s - sm);
+                } else {
+                    const double b = a * (sstar - sm) / (ss - sstar);
+                    f = fs + b * (ss - s) * (ss - s);
+                }
+            } else {
+                const double sn = (s - sm) / (ss - sm);
+                f = fm - (fm - fs) * sn * sn * (3.0 - 2.0 * sn);
+            }
+            fos = f * is;
+        }
+    } else {
+        f = 0.0;
+        fos = 0.0;
+    }
+}
+
+// sqrt(a^2 + b^2) and its reciprocal from one rsqrt (0 and 0 for a zero vector)
+__device__ __forceinline__ void hyp_rcp(double a, double b, double& h, double& ih) {
+    const double q = fma(a, a, b * b);
+    if (q > 0.0) {
+        ih = rsqrt(q);
+        h = q * ih;
+    } else {
+        h = 0.0;
+        ih = 0.0;
+    }
+}
+
 // tmxy_combined (dof18_gpu.cu:243-285)
 __device__ __forceinline__ void tmxy(double& f, double& fos, double s, double df0, double sm, double fm,
                                      double ss, double fs) {
@@ -367,9 +423,9 @@ __device__ __forceinline__ void tire_core_tm(TireC& ts, TireAux& ta, const KView
     const double sxn = sx * ihx;
     const double syn = sy * ihy;
     const double q = fma(sxn, sxn, syn * syn);
-    double sc, calpha, salpha;
+    double sc, calpha, salpha, isc = 0.0;
     if (q > 0) {
-        const double isc = rsqrt(q);
+        isc = rsqrt(q);
         sc = q * isc;
         calpha = sxn * isc;
         salpha = syn * isc;
@@ -380,13 +436,14 @@ __device__ __forceinline__ void tire_core_tm(TireC& ts, TireAux& ta, const KView
     }
     auto hyp = [](double a, double b) { return sqrt(fma(a, a, b * b)); };
     const double df0 = hyp(dfx0 * calpha * hsxn, dfy0 * salpha * hsyn);
-    const double fm = hyp(fxm * calpha, fym * salpha);
+    double fm, ifm, sm, ism;
+    hyp_rcp(fxm * calpha, fym * salpha, fm, ifm);
     const double cax = calpha * ihx, say = salpha * ihy;
-    const double sm = hyp(sxm * cax, sym * say);
+    hyp_rcp(sxm * cax, sym * say, sm, ism);
     const double fs = hyp(fxs * calpha, fys * salpha);
     const double ss = hyp(sxs * cax, sys * say);
     double f, fos;
-    tmxy(f, fos, sc, df0, sm, fm, ss, fs);
+    tmxy_rcp(f, fos, sc, isc, df0, sm, ism, fm, ifm, ss, fs);
     (void)f;
     // rolling resistance: sineStep(vta, 0, 0, 0, 1) == 1 for vta >= 0.01
     ta.My = -K(K_RR) * fz * ta.rStat * sgnd(omega);

@@ -201,6 +201,7 @@ static void build_map(const double (*pts)[2], int n, MapDev& m) {
     for (int k = 0; k + 1 < n; ++k) {
         m.dx[k] = m.x[k + 1] - m.x[k];
         m.dy[k] = m.y[k + 1] - m.y[k];
+        m.idx[k] = 1.0 / m.dx[k];
     }
 }
 
