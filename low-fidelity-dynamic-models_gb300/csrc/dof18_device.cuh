@@ -125,7 +125,33 @@ __device__ __forceinline__ double sine_step(double x, double x1, double y1, doub
     return y1 + dy * u - (dy / k2Pi) * sin(k2Pi * u);
 }
 
-__device__ __forceinline__ double sgnd(double v) { return (double)((0. < v) - (v < 0.)); }
+// Order tests on the IEEE-754 bit pattern, evaluated on the integer pipe instead of the FP64 pipe
+// (on this GPU the FP64 pipe is the bottleneck of the step). For non-NaN operands they give exactly
+// the results of the floating-point comparisons: a positive double's pattern is a positive int64,
+// and the patterns of non-negative doubles (+0 included, -0 excluded) are ordered as their values.
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ bool gt0(double x) { return dbits(x) > 0; }                    // x > 0
+__device__ __forceinline__ bool gt_nn(double a, double b) { return dbits(a) > dbits(b); }  // a > b, a, b >= +0
+__device__ __forceinline__ double max_nn(double a, double b) { return gt_nn(a, b) ? a : b; }
+__device__ __forceinline__ double min_nn(double a, double b) { return gt_nn(a, b) ? b : a; }
+__device__ __forceinline__ double pos_part(double x) { return gt0(x) ? x : 0.0; }         // max(x, 0)
+__device__ __forceinline__ bool is_zero(double x) { return (static_cast<unsigned long long>(dbits(x)) << 1) == 0; }
+
+// sgn (utils/utils_gpu.cuh): -1, 0 or 1 (0 for both zeros)
+__device__ __forceinline__ double sgnd(double v) {
+    const unsigned long long u = static_cast<unsigned long long>(dbits(v));
+    return (u << 1) == 0 ? 0.0 : ((u >> 63) ? -1.0 : 1.0);
+}
+
+// sineStep for x >= 0 and 0 <= x1 < x2 (the tire blends): the same value, integer bound tests
+__device__ __forceinline__ double sine_step_nn(double x, double x1, double y1, double x2, double y2) {
+    if (!gt_nn(x, x1)) return y1;
+    if (!gt_nn(x2, x)) return y2;
+    const double dx = x2 - x1;
+    const double dy = y2 - y1;
+    const double u = (x - x1) / dx;
+    return y1 + dy * u - (dy / k2Pi) * sin(k2Pi * u);
+}
 
 // The shared prefix [0, KT_COUNT) of the derived constants from one flat parameter vector p:
 // tire curve coefficients (InterpQ(fz,w1,w2,pn) = fzn*(Q1 - Q2*fzn), InterpL(fz,w1,w2,pn) =
@@ -286,12 +312,12 @@ struct KView {
 __device__ __forceinline__ void tmxy_rcp(double& f, double& fos, double s, double is, double df0, double sm,
                                          double ism, double fm, double ifm, double ss, double fs) {
     double df0loc = 0.0;
-    if (sm > 0.0) df0loc = fmax(2.0 * fm * ism, df0);
-    if (s > 0.0 && df0loc > 0.0) {
-        if (s > ss) {
+    if (gt0(sm)) df0loc = max_nn(2.0 * fm * ism, df0);
+    if (gt0(s) && gt0(df0loc)) {
+        if (gt_nn(s, ss)) {
             f = fs;
             fos = fs * is;
-        } else if (s < sm) {  // adhesion
+        } else if (gt_nn(sm, s)) {  // adhesion
             const double p = df0loc * sm * ifm - 2.0;
             const double sn = s * ism;
             const double dn = fma(sn + p, sn, 1.0);
@@ -324,7 +350,7 @@ __device__ __forceinline__ void tmxy_rcp(double& f, double& fos, double s, doubl
 // sqrt(a^2 + b^2) and its reciprocal from one rsqrt (0 and 0 for a zero vector)
 __device__ __forceinline__ void hyp_rcp(double a, double b, double& h, double& ih) {
     const double q = fma(a, a, b * b);
-    if (q > 0.0) {
+    if (gt0(q)) {
         ih = rsqrt(q);
         h = q * ih;
     } else {
@@ -397,7 +423,7 @@ __device__ __forceinline__ void tire_core_tm(TireC& ts, TireAux& ta, const KView
     } else {
         sy = -vsy * ivta;
     }
-    fz = fmin(fz, K(K_PNMAX));
+    fz = min_nn(fz, K(K_PNMAX));
     const double fzn = fz * K(K_INVPN);
     const double dfx0 = fzn * fma(-K(K_Q2DFX0), fzn, K(K_Q1DFX0));
     const double dfy0 = fzn * fma(-K(K_Q2DFY0), fzn, K(K_Q1DFY0));
@@ -424,7 +450,7 @@ __device__ __forceinline__ void tire_core_tm(TireC& ts, TireAux& ta, const KView
     const double syn = sy * ihy;
     const double q = fma(sxn, sxn, syn * syn);
     double sc, calpha, salpha, isc = 0.0;
-    if (q > 0) {
+    if (gt0(q)) {
         isc = rsqrt(q);
         sc = q * isc;
         calpha = sxn * isc;
@@ -460,10 +486,10 @@ __device__ __forceinline__ void tire_core_tm(TireC& ts, TireAux& ta, const KView
     const double fydyn = fma(dy, ts.yedot, cy * ts.ye);
     const double fxstr = fmin(fmax(fma(ts.xe, cx, ts.xedot * dx), -K(K_FXMP2N)), K(K_FXMP2N));
     const double fystr = fmin(fmax(fma(ts.ye, cy, ts.yedot * dy), -K(K_FYMP2N)), K(K_FYMP2N));
-    const double wx = sine_step(fabs(vsx), 1., 1., 1.5, 0.);
-    const double wy = sine_step(fabs(sy * vta), 1., 1., 1.5, 0.);
-    ta.fx = (wx == 0.0) ? fxdyn : fma(wx, fxstr, (1. - wx) * fxdyn);
-    ta.fy = (wy == 0.0) ? fydyn : fma(wy, fystr, (1. - wy) * fydyn);
+    const double wx = sine_step_nn(fabs(vsx), 1., 1., 1.5, 0.);
+    const double wy = sine_step_nn(fabs(sy * vta), 1., 1., 1.5, 0.);
+    ta.fx = is_zero(wx) ? fxdyn : fma(wx, fxstr, (1. - wx) * fxdyn);
+    ta.fy = is_zero(wy) ? fydyn : fma(wy, fystr, (1. - wy) * fydyn);
 }
 
 // computeTireRHS, TMeasy (dof18_gpu.cu:379-530). (c, s) = (cos, sin) of this tire's wheel angle;
@@ -472,7 +498,7 @@ __device__ __forceinline__ void tire_core_tm(TireC& ts, TireAux& ta, const KView
 template <bool kSteered>
 __device__ __forceinline__ void tire_rhs_tm(TireC& ts, TireAux& ta, const KView& K, double c, double s) {
     const double fz = ta.fz;
-    if (fz <= 0) {
+    if (!gt0(fz)) {
         ts.xe = 0;
         ts.ye = 0;
         ts.omega = 0;
@@ -486,7 +512,7 @@ __device__ __forceinline__ void tire_rhs_tm(TireC& ts, TireAux& ta, const KView&
     ta.xt = fz * K(K_INVKT);
     ta.rStat = K(K_R0) - ta.xt;
     double r_eff;
-    if (fz <= K(K_FZRD)) {
+    if (!gt_nn(fz, K(K_FZRD))) {
         double rdynco = fma(K(K_DRD), fma(fz, K(K_INVPN), -1.0), K(K_RDPN));
         r_eff = fma(rdynco, ta.xt, ta.rStat);
     } else {
@@ -589,14 +615,14 @@ __device__ __forceinline__ void tire_rhs_nr(TireC& ts, TireAux& ta, const KView&
 __device__ __forceinline__ void diff_split(double torque, double wl, double wr, double& tl, double& tr) {
     double diff = fabs(wl - wr);
     double alpha;
-    if (diff > 0.5) alpha = 2.0 / 3.0;          // bias = max_bias = 2
-    else if (diff > 0.25) {
+    if (gt_nn(diff, 0.5)) alpha = 2.0 / 3.0;    // bias = max_bias = 2
+    else if (gt_nn(diff, 0.25)) {
         double bias = 4 * (2.0 - 1) * diff + (2 - 2.0);
         alpha = bias / (1 + bias);
     } else alpha = 0.5;                          // bias = 1
     double slow = alpha * torque;
     double fast = torque - slow;
-    if (fabs(wl) < fabs(wr)) {
+    if (gt_nn(fabs(wr), fabs(wl))) {
         tl = slow;
         tr = fast;
     } else {
@@ -699,10 +725,10 @@ __device__ __forceinline__ void step18(VehC& v, VehAux& va, TireC* ts, TireAux* 
         const double Z3r = fma(K(K_Z3RK), v.phi, K(K_Z3RB) * v.wx);
         const double Af = K(K_Z1F) - Z4, Bf = Z2f + Z3f;
         const double Ar = K(K_Z1R) + Z4, Br = Z2r + Z3r;
-        ta[0].fz = fmax(Af - Bf, 0.0);
-        ta[1].fz = fmax(Af + Bf, 0.0);
-        ta[2].fz = fmax(Ar - Br, 0.0);
-        ta[3].fz = fmax(Ar + Br, 0.0);
+        ta[0].fz = pos_part(Af - Bf);
+        ta[1].fz = pos_part(Af + Bf);
+        ta[2].fz = pos_part(Ar - Br);
+        ta[3].fz = pos_part(Ar + Br);
     }
     // vehToTireTransform (dof18_gpu.cu:71-109)
     double delta;
