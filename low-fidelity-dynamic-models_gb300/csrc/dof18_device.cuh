@@ -18,6 +18,7 @@
 #include <cstdint>
 
 #include "../../include/lfdm.h"
+#include "fp_order.cuh"
 
 namespace lfdm {
 
@@ -62,6 +63,7 @@ struct MapDev {
     double dx[LFDM_MAX_MAP];     // x[k+1] - x[k]
     double dy[LFDM_MAX_MAP];     // y[k+1] - y[k]
     double idx[LFDM_MAX_MAP];    // 1 / dx[k]
+    long long kx[LFDM_MAX_MAP];  // order keys of x[k] (okey)
 };
 struct ClassDev18 {
     int nonLinearSteer, tcbool, throttleMod, driveType, whichWheels, noGears;
@@ -71,6 +73,18 @@ struct ClassDev18 {
     double up[LFDM_MAX_GEARS];
     MapDev steer, pt, loss, cf, tr;
 };
+
+// lower_bound over the order keys of a sorted array: first k with x <= a[k]
+// (utils/utils_gpu.cu:109-121), with integer compares.
+__device__ __forceinline__ int lower_bound_key(const long long* a, int n, long long k) {
+    int l = 0, h = n;
+    while (l < h) {
+        int mid = (l + h) >> 1;
+        if (k <= a[mid]) h = mid;
+        else l = mid + 1;
+    }
+    return l;
+}
 
 // lower_bound over a sorted key array: first k with x <= a[k] (utils/utils_gpu.cu:109-121).
 __device__ __forceinline__ int lower_bound_x(const double* a, int n, double x) {
@@ -89,11 +103,12 @@ __device__ __forceinline__ int lower_bound_x(const double* a, int n, double x) {
 // grid point returns the tabulated value (an engine at rest sees exactly the loss torque at
 // 0 rad/s and stays at rest, as in the reference).
 __device__ __forceinline__ double map_y(const MapDev& m, double x) {
-    if (x <= m.x[0]) return m.y[0];
-    if (x >= m.x[m.n - 1]) return m.y[m.n - 1];
-    const int r = lower_bound_x(m.x, m.n, x);
+    const long long k = okey(x);
+    if (k <= m.kx[0]) return m.y[0];
+    if (k >= m.kx[m.n - 1]) return m.y[m.n - 1];
+    const int r = lower_bound_key(m.kx, m.n, k);
     const int l = r - 1;
-    const double mbar = (x == m.x[r]) ? 1.0 : (x - m.x[l]) * m.idx[l];
+    const double mbar = (k == m.kx[r]) ? 1.0 : (x - m.x[l]) * m.idx[l];
     return fma(mbar, m.dy[l], m.y[l]);
 }
 
@@ -124,18 +139,6 @@ __device__ __forceinline__ double sine_step(double x, double x1, double y1, doub
     double u = (x - x1) / dx;
     return y1 + dy * u - (dy / k2Pi) * sin(k2Pi * u);
 }
-
-// Order tests on the IEEE-754 bit pattern, evaluated on the integer pipe instead of the FP64 pipe
-// (on this GPU the FP64 pipe is the bottleneck of the step). For non-NaN operands they give exactly
-// the results of the floating-point comparisons: a positive double's pattern is a positive int64,
-// and the patterns of non-negative doubles (+0 included, -0 excluded) are ordered as their values.
-__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
-__device__ __forceinline__ bool gt0(double x) { return dbits(x) > 0; }                    // x > 0
-__device__ __forceinline__ bool gt_nn(double a, double b) { return dbits(a) > dbits(b); }  // a > b, a, b >= +0
-__device__ __forceinline__ double max_nn(double a, double b) { return gt_nn(a, b) ? a : b; }
-__device__ __forceinline__ double min_nn(double a, double b) { return gt_nn(a, b) ? b : a; }
-__device__ __forceinline__ double pos_part(double x) { return gt0(x) ? x : 0.0; }         // max(x, 0)
-__device__ __forceinline__ bool is_zero(double x) { return (static_cast<unsigned long long>(dbits(x)) << 1) == 0; }
 
 // sgn (utils/utils_gpu.cuh): -1, 0 or 1 (0 for both zeros)
 __device__ __forceinline__ double sgnd(double v) {
@@ -484,8 +487,8 @@ __device__ __forceinline__ void tire_core_tm(TireC& ts, TireAux& ta, const KView
     ts.yedot = numy * (denx * rd);
     const double fxdyn = fma(dx, ts.xedot, cx * ts.xe);
     const double fydyn = fma(dy, ts.yedot, cy * ts.ye);
-    const double fxstr = fmin(fmax(fma(ts.xe, cx, ts.xedot * dx), -K(K_FXMP2N)), K(K_FXMP2N));
-    const double fystr = fmin(fmax(fma(ts.ye, cy, ts.yedot * dy), -K(K_FYMP2N)), K(K_FYMP2N));
+    const double fxstr = clamp_sym(fma(ts.xe, cx, ts.xedot * dx), K(K_FXMP2N));
+    const double fystr = clamp_sym(fma(ts.ye, cy, ts.yedot * dy), K(K_FYMP2N));
     const double wx = sine_step_nn(fabs(vsx), 1., 1., 1.5, 0.);
     const double wy = sine_step_nn(fabs(sy * vta), 1., 1., 1.5, 0.);
     ta.fx = is_zero(wx) ? fxdyn : fma(wx, fxstr, (1. - wx) * fxdyn);
@@ -654,15 +657,15 @@ __device__ __forceinline__ void powertrain_rhs(VehC& v, VehAux& va, TireC* ts, T
         const double omega_out = omega_t / C.gear[g];
         const double omega_in = v.crank;
         double sr, cf, tr;
-        if ((omega_out < 1e-9) || (omega_in < 1e-9)) {
+        if (lt_(omega_out, 1e-9) || lt_(omega_in, 1e-9)) {
             sr = 0;
         } else {
             sr = omega_out / omega_in;
-            if (sr > 1.) {
+            if (gt_nn(sr, 1.)) {
                 sr = 1. - (sr - 1.);
                 reverse = true;
             }
-            if (sr < 0) sr = 0;
+            if (lt_(sr, 0.0)) sr = 0;
         }
         cf = map_y(C.cf, sr);
         tr = map_y(C.tr, sr);
@@ -671,20 +674,20 @@ __device__ __forceinline__ void powertrain_rhs(VehC& v, VehAux& va, TireC* ts, T
         if (reverse) torque_in = -torque_in;
         const double torque_out = reverse ? -torque_in : -tr * torque_in;
         torque_t = torque_out * C.invgear[g];
-        if (v.u < 1e-9 && torque_t < 0) torque_t = 0;
+        if (lt_(v.u, 1e-9) && lt_(torque_t, 0.0)) torque_t = 0;
         va.dOmega_crank = K(K_INVCI) * (drive_torque(C, throttle, v.crank) + torque_in);
-        if (omega_out > C.up[g]) {
+        if (lt_(C.up[g], omega_out)) {
             if (g < C.noGears - 1) v.gear = g + 1;
-        } else if (omega_out < C.down[g]) {
+        } else if (lt_(omega_out, C.down[g])) {
             if (g > 0) v.gear = g - 1;
         }
     } else {
         v.crank = 0.25 * (((ts[0].omega + ts[1].omega) + ts[2].omega) + ts[3].omega) / C.gear[g];
         torque_t = drive_torque(C, throttle, v.crank) * C.invgear[g];
-        if (v.u < 1e-9 && torque_t < 0) torque_t = 0;
-        if (v.crank > C.up[g]) {
+        if (lt_(v.u, 1e-9) && lt_(torque_t, 0.0)) torque_t = 0;
+        if (lt_(C.up[g], v.crank)) {
             if (g < C.noGears - 1) v.gear = g + 1;
-        } else if (v.crank < C.down[g]) {
+        } else if (lt_(v.crank, C.down[g])) {
             if (g > 0) v.gear = g - 1;
         }
     }
@@ -735,7 +738,7 @@ __device__ __forceinline__ void step18(VehC& v, VehAux& va, TireC* ts, TireAux* 
     if (C.nonLinearSteer) delta = map_y(C.steer, steering);
     else delta = steering * K(K_MAXSTEER);
     double cd = 1.0, sd = 0.0;
-    if (delta != 0.0) sincos(delta, &sd, &cd);
+    if (!is_zero(delta)) sincos(delta, &sd, &cd);
     {
         const double vsyf = fma(v.wz, K(K_A), v.v);
         const double vsyr = fma(-v.wz, K(K_B), v.v);

@@ -110,7 +110,7 @@ __device__ __forceinline__ void step24(VehC& v, Veh24X& vx, VehAux& va, TireC* t
     if (C.nonLinearSteer) delta = map_y(C.steer, steering);
     else delta = steering * K(K_MAXSTEER);
     double cd = 1.0, sd = 0.0;
-    if (delta != 0.0) sincos(delta, &sd, &cd);
+    if (!is_zero(delta)) sincos(delta, &sd, &cd);
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
         const double r = ta[c].rStat;

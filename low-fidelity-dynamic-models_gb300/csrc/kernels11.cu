@@ -63,7 +63,7 @@ __device__ __forceinline__ void step11(Veh11& v, Veh11Aux& va, TireC* ts, TireAu
     // vehToTireTransform (dof11_gpu.cu:41-68)
     const double delta = C.nonLinearSteer ? map_y(C.steer, steering) : steering * K(K_MAXSTEER);
     double cd = 1.0, sd = 0.0;
-    if (delta != 0.0) sincos(delta, &sd, &cd);
+    if (!is_zero(delta)) sincos(delta, &sd, &cd);
     const double vsyf = fma(v.wz, K(K_A), v.v);
     ta[0].vsy = vsyf;
     ta[0].vsx = fma(v.u, cd, vsyf * sd);

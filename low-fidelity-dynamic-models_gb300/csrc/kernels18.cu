@@ -191,6 +191,13 @@ cudaError_t measure_dfma_rate(double* rate) {
 // ---------------------------------------------------------------------------------------------
 // class tables
 
+// okey (dof18_device.cuh) on the host: an int64 ordered as the double values, both zeros at 0
+static long long order_key(double x) {
+    long long b;
+    std::memcpy(&b, &x, sizeof b);
+    return b >= 0 ? b : -(b & 0x7FFFFFFFFFFFFFFFLL);
+}
+
 static void build_map(const double (*pts)[2], int n, MapDev& m) {
     std::memset(&m, 0, sizeof(m));
     m.n = n;
@@ -203,6 +210,7 @@ static void build_map(const double (*pts)[2], int n, MapDev& m) {
         m.dy[k] = m.y[k + 1] - m.y[k];
         m.idx[k] = 1.0 / m.dx[k];
     }
+    for (int k = 0; k < n; ++k) m.kx[k] = order_key(m.x[k]);
 }
 
 void build_class_dev18(const lfdm_class18& c, ClassDev18* out) {
@@ -337,21 +345,22 @@ struct DriverCursorF {
 
 __device__ __forceinline__ void driver_at_f(DriverCursorF& d, double t, float& st, float& th, float& br) {
     DriverCursor& c = d.c;
-    if (t <= c.tfirst) {
+    const long long kt = okey(t);
+    if (kt <= c.kfirst) {
         st = (float)__ldg(c.rows + 1);
         th = (float)__ldg(c.rows + 2);
         br = (float)__ldg(c.rows + 3);
         return;
     }
-    if (t >= c.tlast) {
+    if (kt >= c.klast) {
         const double* L = c.rows + 4 * (c.len - 1);
         st = (float)__ldg(L + 1);
         th = (float)__ldg(L + 2);
         br = (float)__ldg(L + 3);
         return;
     }
-    while (__ldg(c.rows + 4 * c.r) < t) ++c.r;
-    while (c.r > 1 && __ldg(c.rows + 4 * (c.r - 1)) >= t) --c.r;
+    while (okey(__ldg(c.rows + 4 * c.r)) < kt) ++c.r;
+    while (c.r > 1 && okey(__ldg(c.rows + 4 * (c.r - 1))) >= kt) --c.r;
     if (d.seg != c.r) {
         const double2* L = reinterpret_cast<const double2*>(c.rows + 4 * (c.r - 1));
         const double2 L01 = __ldg(L), L23 = __ldg(L + 1), R01 = __ldg(L + 2), R23 = __ldg(L + 3);

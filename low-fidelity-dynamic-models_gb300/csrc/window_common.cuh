@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include "fp_order.cuh"
+
 namespace lfdm {
 
 constexpr int kMaxSmemClasses = 8;
@@ -11,14 +13,14 @@ struct DriverCursor {
     const double* rows;
     int len;
     int r;  // first row with time >= t (valid while rows[0].t < t < rows[len-1].t)
-    double tfirst, tlast;
+    long long kfirst, klast;  // order keys of the first and last row times
 };
 
 __device__ __forceinline__ void driver_begin(DriverCursor& c, const double* rows, int len, double t) {
     c.rows = rows;
     c.len = len;
-    c.tfirst = __ldg(rows);
-    c.tlast = __ldg(rows + 4 * (len - 1));
+    c.kfirst = okey(__ldg(rows));
+    c.klast = okey(__ldg(rows + 4 * (len - 1)));
     int l = 0, h = len;
     while (l < h) {
         int mid = (l + h) >> 1;
@@ -29,23 +31,25 @@ __device__ __forceinline__ void driver_begin(DriverCursor& c, const double* rows
 }
 
 // GetDriverInput (utils/utils_gpu.cu:34-56) with a monotone cursor in place of the per-step
-// binary search; the segment found is the same lower_bound segment for non-decreasing tables.
+// binary search; the segment found is the same lower_bound segment for non-decreasing tables. The
+// time tests compare order keys (integer pipe), with the results of the floating-point tests.
 __device__ __forceinline__ void driver_at(DriverCursor& c, double t, double& st, double& th, double& br) {
-    if (t <= c.tfirst) {
+    const long long kt = okey(t);
+    if (kt <= c.kfirst) {
         st = __ldg(c.rows + 1);
         th = __ldg(c.rows + 2);
         br = __ldg(c.rows + 3);
         return;
     }
-    if (t >= c.tlast) {
+    if (kt >= c.klast) {
         const double* L = c.rows + 4 * (c.len - 1);
         st = __ldg(L + 1);
         th = __ldg(L + 2);
         br = __ldg(L + 3);
         return;
     }
-    while (__ldg(c.rows + 4 * c.r) < t) ++c.r;
-    while (c.r > 1 && __ldg(c.rows + 4 * (c.r - 1)) >= t) --c.r;  // t moved backwards (new window)
+    while (okey(__ldg(c.rows + 4 * c.r)) < kt) ++c.r;
+    while (c.r > 1 && okey(__ldg(c.rows + 4 * (c.r - 1))) >= kt) --c.r;  // t moved backwards (new window)
     const double2* L = reinterpret_cast<const double2*>(c.rows + 4 * (c.r - 1));
     const double2 L01 = __ldg(L), L23 = __ldg(L + 1), R01 = __ldg(L + 2), R23 = __ldg(L + 3);
     const double tbar = (t - L01.x) / (R01.x - L01.x);
