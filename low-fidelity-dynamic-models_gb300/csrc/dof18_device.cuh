@@ -537,31 +537,15 @@ __device__ __forceinline__ void coulomb(double& fx, double& fy, double mu, doubl
     }
 }
 
-// computeTireRHS, TMeasyNr (dof18_gpu.cu:532-662)
+// The part of computeTireRHS, TMeasyNr (dof18_gpu.cu:532-662; 24dof-gpu/dof24_gpu.cu:990-1119),
+// that follows the loaded and effective radii: Coulomb force, slips, curve parameters, combined
+// force, blend and rolling resistance. fz > 0 is the unclamped load, ta.rStat the loaded radius.
 template <bool kSteered>
-__device__ __forceinline__ void tire_rhs_nr(TireC& ts, TireAux& ta, const KView& K, double c, double s) {
-    double fz = ta.fz;
+__device__ __forceinline__ void tire_core_nr(TireC& ts, TireAux& ta, const KView& K, double c, double s, double fz,
+                                             double r_eff) {
     const double vsy = ta.vsy;
-    if (fz <= 0) {
-        ts.omega = 0;
-        ta.xt = 0;
-        ta.rStat = K(K_R0);
-        ta.fx = 0;
-        ta.fy = 0;
-        ta.My = 0;
-        return;
-    }
     const double omega = ts.omega;
     const double mu = K(K_MU);
-    ta.xt = fz * K(K_INVKT);
-    ta.rStat = K(K_R0) - ta.xt;
-    double r_eff;
-    if (fz <= K(K_FZRD)) {
-        double rdynco = fma(K(K_DRD), fma(fz, K(K_INVPN), -1.0), K(K_RDPN));
-        r_eff = fma(rdynco, ta.xt, ta.rStat);
-    } else {
-        r_eff = fma(K(K_RDCRIT), ta.xt, ta.rStat);
-    }
     const double vsx = fma(-omega, r_eff, ta.vsx);
     const double vta = r_eff * fabs(omega) + 0.01;
     double Fx0, Fy0;
@@ -612,6 +596,31 @@ __device__ __forceinline__ void tire_rhs_nr(TireC& ts, TireAux& ta, const KView&
     ta.fx = fma(1.0 - frblend, Fx0, frblend * Fx);
     ta.fy = fma(1.0 - frblend, Fy0, frblend * Fy);
     ta.My = -K(K_RR) * fz * ta.rStat * tanh(omega);
+}
+
+// computeTireRHS, TMeasyNr (dof18_gpu.cu:532-662)
+template <bool kSteered>
+__device__ __forceinline__ void tire_rhs_nr(TireC& ts, TireAux& ta, const KView& K, double c, double s) {
+    const double fz = ta.fz;
+    if (!gt0(fz)) {
+        ts.omega = 0;
+        ta.xt = 0;
+        ta.rStat = K(K_R0);
+        ta.fx = 0;
+        ta.fy = 0;
+        ta.My = 0;
+        return;
+    }
+    ta.xt = fz * K(K_INVKT);
+    ta.rStat = K(K_R0) - ta.xt;
+    double r_eff;
+    if (!gt_nn(fz, K(K_FZRD))) {
+        double rdynco = fma(K(K_DRD), fma(fz, K(K_INVPN), -1.0), K(K_RDPN));
+        r_eff = fma(rdynco, ta.xt, ta.rStat);
+    } else {
+        r_eff = fma(K(K_RDCRIT), ta.xt, ta.rStat);
+    }
+    tire_core_nr<kSteered>(ts, ta, K, c, s, fz, r_eff);
 }
 
 // differentialSplit (dof18_gpu.cu:42-69) with max_bias = 2.

@@ -69,6 +69,7 @@ struct Corner24K {
 // One rhsFun + half-implicit update. sink: also write the step's non-carried values to S. The flag
 // is a run-time value on purpose: every step runs the same compiled arithmetic (a separate
 // instantiation for storing steps could fuse multiplies and adds differently and round differently).
+template <bool kNr>
 __device__ __forceinline__ void step24(VehC& v, Veh24X& vx, VehAux& va, TireC* ts, TireAux* ta, Sus24C* su,
                                        const Corner24K* ck, const KView& K, const ClassDev18& C, double steering,
                                        double throttle, double braking, double dt, double* S, size_t np, bool sink) {
@@ -131,9 +132,11 @@ __device__ __forceinline__ void step24(VehC& v, Veh24X& vx, VehAux& va, TireC* t
         const double fz = xt * kt;
         ta[c].fz = fz;
         ta[c].rStat = (r0 - xt) * icc;
-        if (fz <= 0) {
-            ts[c].xe = 0;
-            ts[c].ye = 0;
+        if (!gt0(fz)) {
+            if (!kNr) {
+                ts[c].xe = 0;
+                ts[c].ye = 0;
+            }
             ts[c].omega = 0;
             ta[c].xt = 0;
             ta[c].rStat = r0;
@@ -144,10 +147,15 @@ __device__ __forceinline__ void step24(VehC& v, Veh24X& vx, VehAux& va, TireC* t
         } else {
             const double rs = ta[c].rStat;
             const double rdynco =
-                fz <= K(K_FZRD) ? fma(K(K_DRD), fma(fz, K(K_INVPN), -1.0), K(K_RDPN)) : K(K_RDCRIT);
+                !gt_nn(fz, K(K_FZRD)) ? fma(K(K_DRD), fma(fz, K(K_INVPN), -1.0), K(K_RDPN)) : K(K_RDCRIT);
             const double r_eff = fma(rdynco, r0 - rs, rs);
-            if (c < 2) tire_core_tm<true>(ts[c], ta[c], K, cd, sd, fz, r_eff);
-            else tire_core_tm<false>(ts[c], ta[c], K, 1.0, 0.0, fz, r_eff);
+            if (kNr) {  // computeTireRHS, TMeasyNr (24dof-gpu/dof24_gpu.cu:990-1119)
+                if (c < 2) tire_core_nr<true>(ts[c], ta[c], K, cd, sd, fz, r_eff);
+                else tire_core_nr<false>(ts[c], ta[c], K, 1.0, 0.0, fz, r_eff);
+            } else {
+                if (c < 2) tire_core_tm<true>(ts[c], ta[c], K, cd, sd, fz, r_eff);
+                else tire_core_tm<false>(ts[c], ta[c], K, 1.0, 0.0, fz, r_eff);
+            }
         }
     }
     // computeTireCompressionVelocity
@@ -240,8 +248,10 @@ __device__ __forceinline__ void step24(VehC& v, Veh24X& vx, VehAux& va, TireC* t
     // half-implicit update (dof24_halfImplicit_gpu.cu:1016-1081)
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-        ts[c].xe = fma(ts[c].xedot, dt, ts[c].xe);
-        ts[c].ye = fma(ts[c].yedot, dt, ts[c].ye);
+        if (!kNr) {  // the TMeasyNr tire has no deflection states
+            ts[c].xe = fma(ts[c].xedot, dt, ts[c].xe);
+            ts[c].ye = fma(ts[c].yedot, dt, ts[c].ye);
+        }
         ta[c].xt = fma(dxt[c], dt, ta[c].xt);
         ts[c].omega = fma(ta[c].dOmega, dt, ts[c].omega);
         su[c].wu = fma(dwu[c], dt, su[c].wu);

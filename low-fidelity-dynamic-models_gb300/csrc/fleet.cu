@@ -127,7 +127,7 @@ __device__ __forceinline__ void run_tile24(const FleetLaunch& L, const FleetTile
         driver_at(cur, t, steer, thr, brk);
         // the step that ends this launch's range for the vehicle also writes the values the
         // reference leaves in its state structs (as the window kernel does for a window's last step)
-        step24(v, vx, va, ts, ta, su, ck, K, C, steer, thr, brk, L.dt, S, np, s == last);
+        step24<false>(v, vx, va, ts, ta, su, ck, K, C, steer, thr, brk, L.dt, S, np, s == last);
         sample(s, t);
     }
     store_state24(S, np, v, vx, va, ts, ta, su, C.tcbool);

@@ -280,6 +280,113 @@ void tire_init(double* p) {
     p[LFDM_P_RDYNCOCRIT] = r1 + (r2 - r1) * (fz / pn - 1.);
 }
 
+// Maximum tire load [kg] by load index 0..279, the table of GetTireMaxLoad
+// (18dof-gpu/dof18_gpu.cu:1470-1503; the 11- and 24-DOF models hold the same numbers). Indices past
+// the end take the last entry.
+static const double kLoadIndexKg[] = {
+    45, 46.5, 47.5, 48.7, 50, 51.5, 53, 54.5, 56, 58,  // LI 0-9
+    60, 61.5, 63, 65, 67, 69, 71, 73, 75, 77.5,  // LI 10-19
+    80.0, 82.5, 85.0, 87.5, 90.0, 92.5, 95.0, 97.5, 100.0, 103,  // LI 20-29
+    106, 109, 112, 115, 118, 121, 125, 128, 132, 136,  // LI 30-39
+    140, 145, 150, 155, 160, 165, 170, 175, 180, 185,  // LI 40-49
+    190, 195, 200, 206, 212, 218, 224, 230, 236, 243,  // LI 50-59
+    250, 257, 265, 272, 280, 290, 300, 307, 315, 325,  // LI 60-69
+    335, 345, 355, 365, 375, 387, 400, 412, 425, 437,  // LI 70-79
+    450, 462, 475, 487, 500, 515, 530, 545, 560, 580,  // LI 80-89
+    600, 615, 630, 650, 670, 690, 710, 730, 750, 775,  // LI 90-99
+    800, 825, 850, 875, 900, 925, 950, 975, 1000, 1030,  // LI 100-109
+    1060, 1090, 1120, 1150, 1180, 1215, 1250, 1285, 1320, 1360,  // LI 110-119
+    1400, 1450, 1500, 1550, 1600, 1650, 1700, 1750, 1800, 1850,  // LI 120-129
+    1900, 1950, 2000, 2060, 2120, 2180, 2240, 2300, 2360, 2430,  // LI 130-139
+    2500, 2575, 2650, 2725, 2800, 2900, 3000, 3075, 3150, 3250,  // LI 140-149
+    3350, 3450, 3550, 3650, 3750, 3875, 4000, 4125, 4250, 4375,  // LI 150-159
+    4500, 4625, 4750, 4875, 5000, 5150, 5300, 5450, 5600, 5850,  // LI 160-169
+    6000, 6150, 6300, 6500, 6700, 6900, 7100, 7300, 7500, 7750,  // LI 170-179
+    8000, 8250, 8500, 8750, 9000, 9250, 9500, 9750, 10000, 10300,  // LI 180-189
+    10600, 10900, 11200, 11500, 11800, 12150, 12500, 12850, 13200, 13600,  // LI 190-199
+    14000, 14500, 15000, 15550, 16000, 16500, 17000, 17500, 18000, 18500,  // LI 200-209
+    19000, 19500, 20000, 20600, 21200, 21800, 22400, 23000, 23600, 24300,  // LI 210-219
+    25000, 25750, 26500, 27250, 28000, 29000, 30000, 30750, 31500, 32500,  // LI 220-229
+    33500, 34500, 35500, 36500, 37500, 38750, 40000, 41250, 42500, 43750,  // LI 230-239
+    45000, 46250, 47500, 48750, 50000, 51500, 53000, 54500, 56000, 58000,  // LI 240-249
+    60000, 61500, 63000, 65000, 67000, 69000, 71000, 73000, 75000, 77500,  // LI 250-259
+    80000, 82500, 85000, 87500, 90000, 92500, 95000, 97500, 100000, 103000,  // LI 260-269
+    106000, 109000, 112000, 115000, 118000, 121000, 125000, 128500, 132000, 136000,  // LI 270-279
+};
+
+// Load-normalised TMeasy curve parameters of GuessPassCar70Par and GuessTruck80Par
+// (18dof-gpu/dof18_gpu.cu:1516-1615): force entries (dfx0, fxm, fxs, dfy0, fym, fys; Pn then P2n) as
+// multiples of pn (of 2 pn for P2n), then the slips (sxm, sxs, sym, sys; Pn then P2n).
+struct TireGuess {
+    double force[12];
+    double slip[8];
+};
+static const TireGuess kPassCar70 = {
+    {18.3741, 19.4669, 1.1292, 1.0896, 0.80149, 0.76917, 15.9826, 12.8509, 1.0009, 0.91367, 0.8336, 0.77336},
+    {0.13913, 0.13913, 0.66667, 0.66667, 0.14852, 0.18504, 0.96524, 1.0714}};
+static const TireGuess kTruck80 = {
+    {17.7764, 14.5301, 0.89965, 0.77751, 0.46183, 0.42349, 7.4013, 6.8505, 0.75876, 0.72628, 0.68276, 0.65319},
+    {0.10811, 0.12389, 0.66667, 0.66667, 0.33167, 0.33216, 1.0296, 1.0296}};
+
+// TMeasyNr "highLevelParams": design values from the file, curve parameters guessed from the tire's
+// width, aspect ratio, rim and load capacity (load index or maximum bearing capacity). two = 2 for
+// the single-track 11-DOF model, whose loader doubles the axle quantities.
+static bool tmeasy_nr_high_level(Ctx& t, const JVal& td, double two, double* p) {
+    bool ok = t.num("jw", p[LFDM_P_JW]) && t.num("rr", p[LFDM_P_RR]) && t.num("mu", p[LFDM_P_MU]) &&
+              t.num("r0", p[LFDM_P_R0]) && t.num("rdyncoPn", p[LFDM_P_RDYNCOPN]) &&
+              t.num("rdyncoP2n", p[LFDM_P_RDYNCOP2N]) && t.num("fzRdynco", p[LFDM_P_FZRDYNCO]) &&
+              t.num("rdyncoCrit", p[LFDM_P_RDYNCOCRIT]);
+    if (!ok) return false;
+    for (int i : {LFDM_P_JW, LFDM_P_RR, LFDM_P_MU, LFDM_P_FZRDYNCO, LFDM_P_RDYNCOCRIT}) p[i] *= two;
+    auto opt = [&](const char* k, double def) {
+        const JVal* x = td.get(k);
+        return (x && x->kind == JVal::Num) ? x->d : def;
+    };
+    p[LFDM_P_VCOULOMB] = opt("vCoulomb", 1.0);
+    p[LFDM_P_FRBLEND_BEGIN] = opt("frblendBegin", 1.0);
+    p[LFDM_P_FRBLEND_END] = opt("frblendEnd", 3.0);
+    double width = 0, rim_radius = 0;
+    if (!(t.num("width", width) && t.num("rimRadius", rim_radius))) return false;
+    double p_li = opt("inflationPressureDesign", 0.0), p_use = opt("inflationPressureUse", 0.0);
+    if (!(p_use > 0.0 && p_li > 0.0)) p_li = p_use = 1.0;
+    p[LFDM_P_P_LI] = p_li;
+    p[LFDM_P_P_USE] = p_use;
+    double load = 0;
+    const JVal* li = td.get("loadIndex");
+    if (li && li->kind == JVal::Num) {
+        const unsigned idx = (unsigned)li->d;
+        p[LFDM_P_LI] = idx;
+        const unsigned n = sizeof(kLoadIndexKg) / sizeof(kLoadIndexKg[0]);
+        load = kLoadIndexKg[idx < n ? idx : n - 1] * 9.81;
+    } else {
+        if (!t.num("maximumBearingCapacity", load)) return false;
+        p[LFDM_P_BEARINGCAPACITY] = load;
+    }
+    const JVal* vt = td.get("vehicleType");
+    if (!vt || vt->kind != JVal::Str) {
+        if (t.err.empty()) t.err = t.file + ": missing key \"vehicleType\"";
+        return false;
+    }
+    const TireGuess& g = vt->s == "Truck" ? kTruck80 : kPassCar70;
+    // GuessPassCar70Par / GuessTruck80Par with ratio = (r0 - rim radius) / width, rim diameter
+    // 2 rim radius: section height width * ratio, deflection at the rated load 0.16 of it
+    const double ratio = (p[LFDM_P_R0] - rim_radius) / width;
+    const double defl_max = 0.16 * (width * ratio);
+    const double pn = 0.5 * load * std::pow(p_use / p_li, 0.8);
+    p[LFDM_P_PN] = pn;
+    p[LFDM_P_PNMAX] = 3.5 * pn;
+    p[LFDM_P_KT] = load / defl_max;
+    p[LFDM_P_RIM_RADIUS] = 0.5 * (2 * rim_radius);
+    p[LFDM_P_WIDTH] = width;
+    static const int fk[12] = {LFDM_P_DFX0PN, LFDM_P_DFX0P2N, LFDM_P_FXMPN, LFDM_P_FXMP2N, LFDM_P_FXSPN, LFDM_P_FXSP2N,
+                               LFDM_P_DFY0PN, LFDM_P_DFY0P2N, LFDM_P_FYMPN, LFDM_P_FYMP2N, LFDM_P_FYSPN, LFDM_P_FYSP2N};
+    static const int sk[8] = {LFDM_P_SXMPN, LFDM_P_SXMP2N, LFDM_P_SXSPN, LFDM_P_SXSP2N,
+                              LFDM_P_SYMPN, LFDM_P_SYMP2N, LFDM_P_SYSPN, LFDM_P_SYSP2N};
+    for (int i = 0; i < 12; ++i) p[fk[i]] = ((i % 2) ? (g.force[i] * 2.0) * pn : g.force[i] * pn) * two;
+    for (int i = 0; i < 8; ++i) p[sk[i]] = g.slip[i];
+    return true;
+}
+
 bool load_vehicle(int model, const std::string& veh_path, const std::string& tire_path, const std::string& sus_path,
                   int tire_type, lfdm_class18& c, double* p, std::string& err) {
     default_vehicle(c, p);
@@ -415,18 +522,25 @@ bool load_vehicle(int model, const std::string& veh_path, const std::string& tir
                                       LFDM_P_FYMP2N, LFDM_P_FYSPN,  LFDM_P_FYSP2N};
             for (int i : dbl) p[i] *= 2.;
         }
-    } else if (model != LFDM_MODEL_18) {
-        err = tire_path + ": TMeasyNr tires are available for the 18-DOF model only";
-        return false;
     } else {
+        // setTireParamsJSON for TMeasyNr (18dof-gpu/dof18_gpu.cu:1278-1466; 24-DOF the same,
+        // 24dof-gpu/dof24_gpu.cu:1847-2070; 11-DOF doubling the axle quantities, 11dof-gpu/dof11_gpu.cu:1101-1290)
+        const double two = model == LFDM_MODEL_11 ? 2.0 : 1.0;
         const JVal* hl = td.get("highLevelParams");
         if (hl && hl->kind == JVal::Bool && hl->b) {
-            err = tire_path + ": TMeasyNr high-level parameters (load-index guessing) are not supported";
-            return false;
-        }
-        for (auto& e : tk) {
-            if (e.i == LFDM_P_CX || e.i == LFDM_P_CY || e.i == LFDM_P_DX || e.i == LFDM_P_DY) continue;
-            ok = ok && t.num(e.k, p[e.i]);
+            ok = tmeasy_nr_high_level(t, td, two, p);
+        } else {
+            for (auto& e : tk) {
+                if (e.i == LFDM_P_CX || e.i == LFDM_P_CY || e.i == LFDM_P_DX || e.i == LFDM_P_DY) continue;
+                ok = ok && t.num(e.k, p[e.i]);
+            }
+            if (ok && model == LFDM_MODEL_11) {
+                static const int dbl[] = {LFDM_P_JW,     LFDM_P_RR,     LFDM_P_PN,      LFDM_P_PNMAX,  LFDM_P_KT,
+                                          LFDM_P_FZRDYNCO, LFDM_P_RDYNCOCRIT, LFDM_P_DFX0PN, LFDM_P_DFX0P2N,
+                                          LFDM_P_FXMPN,  LFDM_P_FXMP2N, LFDM_P_FXSPN,   LFDM_P_FXSP2N, LFDM_P_DFY0PN,
+                                          LFDM_P_DFY0P2N, LFDM_P_FYMPN, LFDM_P_FYMP2N,  LFDM_P_FYSPN,  LFDM_P_FYSP2N};
+                for (int i : dbl) p[i] *= 2.;
+            }
         }
     }
     if (!ok) {

@@ -51,14 +51,15 @@ __device__ __forceinline__ void diff_split11(double torque, double w_rear, doubl
     }
 }
 
+template <bool kNr>
 __device__ __forceinline__ void step11(Veh11& v, Veh11Aux& va, TireC* ts, TireAux* ta, const KView& K,
                                        const ClassDev18& C, double steering, double throttle, double braking,
                                        double dt) {
     // computeTireLoads (dof11_gpu.cu:234-252)
     {
         const double Z2 = K(K_Z4) * fma(-v.wz, v.v, v.udot);
-        ta[0].fz = fmax(K(K_Z1F) - Z2, 0.0);
-        ta[1].fz = fmax(K(K_Z1R) + Z2, 0.0);
+        ta[0].fz = pos_part(K(K_Z1F) - Z2);
+        ta[1].fz = pos_part(K(K_Z1R) + Z2);
     }
     // vehToTireTransform (dof11_gpu.cu:41-68)
     const double delta = C.nonLinearSteer ? map_y(C.steer, steering) : steering * K(K_MAXSTEER);
@@ -69,8 +70,13 @@ __device__ __forceinline__ void step11(Veh11& v, Veh11Aux& va, TireC* ts, TireAu
     ta[0].vsx = fma(v.u, cd, vsyf * sd);
     ta[1].vsy = fma(-v.wz, K(K_B), v.v);
     ta[1].vsx = v.u;
-    tire_rhs_tm<true>(ts[0], ta[0], K, cd, sd);
-    tire_rhs_tm<false>(ts[1], ta[1], K, 1.0, 0.0);
+    if (kNr) {  // computeTireRHS, TMeasyNr (11dof-gpu/dof11_gpu.cu:470-599)
+        tire_rhs_nr<true>(ts[0], ta[0], K, cd, sd);
+        tire_rhs_nr<false>(ts[1], ta[1], K, 1.0, 0.0);
+    } else {
+        tire_rhs_tm<true>(ts[0], ta[0], K, cd, sd);
+        tire_rhs_tm<false>(ts[1], ta[1], K, 1.0, 0.0);
+    }
     // computePowertrainRHS (dof11_gpu.cu:601-745)
     double torque_t;
     const int g = v.gear;
@@ -79,13 +85,13 @@ __device__ __forceinline__ void step11(Veh11& v, Veh11Aux& va, TireC* ts, TireAu
         const double omega_out = 0.5 * (ts[0].omega + ts[1].omega) / C.gear[g];
         const double omega_in = v.crank;
         double sr = 0;
-        if (!((omega_out < 1e-9) || (omega_in < 1e-9))) {
+        if (!(lt_(omega_out, 1e-9) || lt_(omega_in, 1e-9))) {
             sr = omega_out / omega_in;
-            if (sr > 1.) {
+            if (gt_nn(sr, 1.)) {
                 sr = 1. - (sr - 1.);
                 reverse = true;
             }
-            if (sr < 0) sr = 0;
+            if (lt_(sr, 0.0)) sr = 0;
         }
         const double cf = map_y(C.cf, sr), tr = map_y(C.tr, sr);
         const double r = omega_in / cf;
@@ -93,20 +99,20 @@ __device__ __forceinline__ void step11(Veh11& v, Veh11Aux& va, TireC* ts, TireAu
         if (reverse) torque_in = -torque_in;
         const double torque_out = reverse ? -torque_in : -tr * torque_in;
         torque_t = torque_out * C.invgear[g];
-        if (v.u < 1e-9 && torque_t < 0) torque_t = 0;
+        if (lt_(v.u, 1e-9) && lt_(torque_t, 0.0)) torque_t = 0;
         va.dOmega_crank = K(K_INVCI) * (drive_torque(C, throttle, v.crank) + torque_in);
-        if (omega_out > C.up[g]) {
+        if (lt_(C.up[g], omega_out)) {
             if (g < C.noGears - 1) v.gear = g + 1;
-        } else if (omega_out < C.down[g]) {
+        } else if (lt_(omega_out, C.down[g])) {
             if (g > 0) v.gear = g - 1;
         }
     } else {
         v.crank = 0.5 * (ts[0].omega + ts[1].omega) / C.gear[g];
         torque_t = drive_torque(C, throttle, v.crank) * C.invgear[g];
-        if (v.u < 1e-9 && torque_t < 0) torque_t = 0;
-        if (v.crank > C.up[g]) {
+        if (lt_(v.u, 1e-9) && lt_(torque_t, 0.0)) torque_t = 0;
+        if (lt_(C.up[g], v.crank)) {
             if (g < C.noGears - 1) v.gear = g + 1;
-        } else if (v.crank < C.down[g]) {
+        } else if (lt_(v.crank, C.down[g])) {
             if (g > 0) v.gear = g - 1;
         }
     }
@@ -129,8 +135,10 @@ __device__ __forceinline__ void step11(Veh11& v, Veh11Aux& va, TireC* ts, TireAu
     // half-implicit update (dof11_halfImplicit_gpu.cu:863-880)
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
-        ts[k].xe = fma(ts[k].xedot, dt, ts[k].xe);
-        ts[k].ye = fma(ts[k].yedot, dt, ts[k].ye);
+        if (!kNr) {  // the TMeasyNr tire has no deflection states
+            ts[k].xe = fma(ts[k].xedot, dt, ts[k].xe);
+            ts[k].ye = fma(ts[k].yedot, dt, ts[k].ye);
+        }
         ts[k].omega = fma(ta[k].dOmega, dt, ts[k].omega);
     }
     if (C.tcbool) v.crank = fma(va.dOmega_crank, dt, v.crank);
@@ -144,7 +152,7 @@ __device__ __forceinline__ void step11(Veh11& v, Veh11Aux& va, TireC* ts, TireAu
     v.psi = fma(v.wz, dt, v.psi);
 }
 
-template <int kCtl, bool kOut>
+template <bool kNr, int kCtl, bool kOut>
 __global__ void __launch_bounds__(128) window11_kernel(const Window18 w) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
@@ -227,7 +235,7 @@ __global__ void __launch_bounds__(128) window11_kernel(const Window18 w) {
             thr = __ldg(w.sched + 3 * s + 1);
             brk = __ldg(w.sched + 3 * s + 2);
         }
-        step11(v, va, ts, ta, K, C, steer, thr, brk, dt);
+        step11<kNr>(v, va, ts, ta, K, C, steer, thr, brk, dt);
         t += dt;
         if (kOut && s + 1 == next_step) {
             double* r = w.resp + (size_t)next_k * LFDM11_RESP_CHANNELS * w.n + vid;
@@ -283,32 +291,36 @@ __global__ void __launch_bounds__(128) window11_kernel(const Window18 w) {
     }
 }
 
-template <int kCtl, bool kOut>
+template <bool kNr, int kCtl, bool kOut>
 static cudaError_t launch11_t(const Window18& w, cudaStream_t stream) {
     const int threads = w.threads;
     const size_t smem = window18_smem(threads, w.nclasses);
-    auto kern = window11_kernel<kCtl, kOut>;
+    auto kern = window11_kernel<kNr, kCtl, kOut>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<(w.n + threads - 1) / threads, threads, smem, stream>>>(w);
     return cudaGetLastError();
 }
 
-template <int kCtl>
+template <bool kNr, int kCtl>
 static cudaError_t launch11_o(const Window18& w, cudaStream_t s) {
-    return (w.resp && w.nsamples > 0) ? launch11_t<kCtl, true>(w, s) : launch11_t<kCtl, false>(w, s);
+    return (w.resp && w.nsamples > 0) ? launch11_t<kNr, kCtl, true>(w, s) : launch11_t<kNr, kCtl, false>(w, s);
+}
+template <bool kNr>
+static cudaError_t launch11_c(const Window18& w, cudaStream_t stream) {
+    switch (w.ctl_mode) {
+        case CTL_TABLE: return launch11_o<kNr, CTL_TABLE>(w, stream);
+        case CTL_SCALAR: return launch11_o<kNr, CTL_SCALAR>(w, stream);
+        case CTL_SCHEDULE: return launch11_o<kNr, CTL_SCHEDULE>(w, stream);
+        default: return launch11_o<kNr, CTL_ARRAY>(w, stream);
+    }
 }
 
 cudaError_t launch_window11(const Window18& w, cudaStream_t stream) {
     if (w.n <= 0 || w.nsteps <= 0) return cudaSuccess;
     if (w.threads <= 0 || w.threads > 128 || (w.threads & 31)) return cudaErrorInvalidValue;
-    if (w.tire_nr || w.precision != LFDM_PREC_FP64) return cudaErrorInvalidValue;
-    switch (w.ctl_mode) {
-        case CTL_TABLE: return launch11_o<CTL_TABLE>(w, stream);
-        case CTL_SCALAR: return launch11_o<CTL_SCALAR>(w, stream);
-        case CTL_SCHEDULE: return launch11_o<CTL_SCHEDULE>(w, stream);
-        default: return launch11_o<CTL_ARRAY>(w, stream);
-    }
+    if (w.precision != LFDM_PREC_FP64) return cudaErrorInvalidValue;
+    return w.tire_nr ? launch11_c<true>(w, stream) : launch11_c<false>(w, stream);
 }
 
 }  // namespace lfdm

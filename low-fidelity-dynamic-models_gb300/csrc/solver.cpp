@@ -493,8 +493,6 @@ int append_vehicles(lfdm_solver* h, const lfdm_class18& cls, const double* param
                        h->constructed, n, h->N);
     if (tire_type != LFDM_TIRE_TMEASY && tire_type != LFDM_TIRE_TMEASY_NR)
         return h->fail(LFDM_ERR_ARG, "unknown tire type %d", tire_type);
-    if (h->model != LFDM_MODEL_18 && tire_type != LFDM_TIRE_TMEASY)
-        return h->fail(LFDM_ERR_ARG, "the %d-DOF model is built with the TMeasy tire only", h->model);
     if (h->tire_type >= 0 && h->tire_type != tire_type)
         return h->fail(LFDM_ERR_STATE, "all vehicles of a solver use one tire type");
     if (cls.noGears < 1 || cls.noGears > LFDM_MAX_GEARS) return h->fail(LFDM_ERR_ARG, "bad gear count %d", cls.noGears);

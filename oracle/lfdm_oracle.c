@@ -332,33 +332,13 @@ static void tireRHS_TM(Tire* ts, const Par* pp, double steering) {
 }
 
 /* computeTireRHS, TMeasyNr: dof18_gpu.cu:532-662 */
-static void tireRHS_Nr(Tire* ts, const Par* pp, double steering) {
-    double delta = wheel_angle(pp, steering);
-    double fz = ts->fz;
-    double vsy = ts->vsy;
-    double vsx = ts->vsx;
-    if (fz <= 0) {
-        ts->omega = 0;
-        ts->xt = 0;
-        ts->rStat = P(LFDM_P_R0);
-        ts->fx = 0;
-        ts->fy = 0;
-        ts->My = 0;
-        return;
-    }
-    const double pn = P(LFDM_P_PN), r0 = P(LFDM_P_R0), mu = P(LFDM_P_MU);
-    ts->xt = fz / P(LFDM_P_KT);
-    ts->rStat = r0 - ts->xt;
-    double r_eff, rdynco;
-    if (fz <= P(LFDM_P_FZRDYNCO)) {
-        rdynco = InterpL(fz, P(LFDM_P_RDYNCOPN), P(LFDM_P_RDYNCOP2N), pn);
-        r_eff = rdynco * r0 + (1. - rdynco) * ts->rStat;
-    } else {
-        rdynco = P(LFDM_P_RDYNCOCRIT);
-        r_eff = rdynco * r0 + (1. - rdynco) * ts->rStat;
-    }
-    vsx = vsx - (ts->omega * r_eff);
-    double vta = r_eff * fabs(ts->omega) + 0.01;
+/* The TMeasyNr tire from the effective radius on (dof18_gpu.cu:532-662; 24dof/dof24.cpp:988-1108):
+   fz > 0 is the unclamped load, r_eff the effective radius, rStat the loaded radius. */
+static void tireNr_core(double* fx_out, double* fy_out, double* My_out, double fz, double r_eff, double rStat,
+                        double omega, double vsx_in, double vsy, double vsx_raw, double delta, const Par* pp) {
+    const double pn = P(LFDM_P_PN), mu = P(LFDM_P_MU);
+    double vsx = vsx_in - (omega * r_eff);
+    double vta = r_eff * fabs(omega) + 0.01;
     double Fx0 = 0, Fy0 = 0;
     coulomb(&Fx0, &Fy0, mu, vsx, vsy, fz, P(LFDM_P_VCOULOMB));
     double sx = -vsx / vta;
@@ -375,7 +355,7 @@ static void tireRHS_Nr(Tire* ts, const Par* pp, double steering) {
     double sym = InterpL(fz, P(LFDM_P_SYMPN), P(LFDM_P_SYMP2N), pn);
     double sxs = InterpL(fz, P(LFDM_P_SXSPN), P(LFDM_P_SXSP2N), pn);
     double sys = InterpL(fz, P(LFDM_P_SYSPN), P(LFDM_P_SYSP2N), pn);
-    double frblend = sineStep(fabs(ts->vsx), P(LFDM_P_FRBLEND_BEGIN), 0., P(LFDM_P_FRBLEND_END), 1.);
+    double frblend = sineStep(fabs(vsx_raw), P(LFDM_P_FRBLEND_BEGIN), 0., P(LFDM_P_FRBLEND_END), 1.);
     double sc = hypot(sx, sy);
     double salpha = 0, calpha = 0;
     if (sc > 0) {
@@ -402,9 +382,36 @@ static void tireRHS_Nr(Tire* ts, const Par* pp, double steering) {
     }
     Fx = (1.0 - frblend) * Fx0 + frblend * Fx;
     Fy = (1.0 - frblend) * Fy0 + frblend * Fy;
-    ts->My = -P(LFDM_P_RR) * fz * ts->rStat * tanh(ts->omega);
-    ts->fx = Fx;
-    ts->fy = Fy;
+    *My_out = -P(LFDM_P_RR) * fz * rStat * tanh(omega);
+    *fx_out = Fx;
+    *fy_out = Fy;
+}
+
+
+static void tireRHS_Nr(Tire* ts, const Par* pp, double steering) {
+    double delta = wheel_angle(pp, steering);
+    double fz = ts->fz;
+    if (fz <= 0) {
+        ts->omega = 0;
+        ts->xt = 0;
+        ts->rStat = P(LFDM_P_R0);
+        ts->fx = 0;
+        ts->fy = 0;
+        ts->My = 0;
+        return;
+    }
+    const double pn = P(LFDM_P_PN), r0 = P(LFDM_P_R0);
+    ts->xt = fz / P(LFDM_P_KT);
+    ts->rStat = r0 - ts->xt;
+    double r_eff, rdynco;
+    if (fz <= P(LFDM_P_FZRDYNCO)) {
+        rdynco = InterpL(fz, P(LFDM_P_RDYNCOPN), P(LFDM_P_RDYNCOP2N), pn);
+        r_eff = rdynco * r0 + (1. - rdynco) * ts->rStat;
+    } else {
+        rdynco = P(LFDM_P_RDYNCOCRIT);
+        r_eff = rdynco * r0 + (1. - rdynco) * ts->rStat;
+    }
+    tireNr_core(&ts->fx, &ts->fy, &ts->My, fz, r_eff, ts->rStat, ts->omega, ts->vsx, ts->vsy, ts->vsx, delta, pp);
 }
 
 /* computePowertrainRHS: dof18_gpu.cu:664-839 (same body for both tire types) */
@@ -1117,6 +1124,34 @@ static void tireRHS24(const Veh24* v, Tire24* ts, const Par* pp, double steering
     ts->fy = weighty * fystr + (1. - weighty) * fydyn;
 }
 
+/* computeTireRHS, TMeasyNr: 24dof/dof24.cpp:988-1108 (GPU 24dof-gpu/dof24_gpu.cu:990-1119) */
+static void tireRHS24_Nr(const Veh24* v, Tire24* ts, const Par* pp, double steering) {
+    double delta = wheel_angle(pp, steering);
+    ts->fz = ts->xt * P(LFDM_P_KT);
+    double fz = ts->fz;
+    const double pn = P(LFDM_P_PN), r0 = P(LFDM_P_R0);
+    ts->rStat = (r0 - ts->xt) / (cos(v->theta) * cos(v->phi));
+    if (fz <= 0) {
+        ts->omega = 0;
+        ts->xt = 0;
+        ts->rStat = r0;
+        ts->fx = 0;
+        ts->fy = 0;
+        ts->fz = 0;
+        ts->My = 0;
+        return;
+    }
+    double r_eff, rdynco;
+    if (fz <= P(LFDM_P_FZRDYNCO)) {
+        rdynco = InterpL(fz, P(LFDM_P_RDYNCOPN), P(LFDM_P_RDYNCOP2N), pn);
+        r_eff = rdynco * r0 + (1. - rdynco) * ts->rStat;
+    } else {
+        rdynco = P(LFDM_P_RDYNCOCRIT);
+        r_eff = rdynco * r0 + (1. - rdynco) * ts->rStat;
+    }
+    tireNr_core(&ts->fx, &ts->fy, &ts->My, fz, r_eff, ts->rStat, ts->omega, ts->vsx, ts->vsy, ts->vsx, delta, pp);
+}
+
 /* computeTireCompressionVelocity: dof24.cpp:1122-1150 */
 static void tireCompression24(const Veh24* v, Tire24* t, const Sus24* su) {
     for (int c = 0; c < 4; ++c)
@@ -1283,14 +1318,21 @@ static void vehRHS24(Veh24* v, const Sus24* su, const Par* pp) {
 }
 
 /* rhsFun: 24dof-gpu/dof24_halfImplicit_gpu.cu:728-775 (CPU 24dof/dof24_halfImplicit.cpp:594-650) */
-static void rhs24(Veh24* v, Tire24* t, Sus24* su, const Par* pp, const double* controls) {
+static void rhs24(Veh24* v, Tire24* t, Sus24* su, const Par* pp, const double* controls, int nr) {
     const double steering = controls[1];
     vehToSus24(v, su, pp);
     vehToTire24(v, t, su, pp, steering);
-    tireRHS24(v, &t[0], pp, steering);
-    tireRHS24(v, &t[1], pp, steering);
-    tireRHS24(v, &t[2], pp, 0);
-    tireRHS24(v, &t[3], pp, 0);
+    if (nr) {
+        tireRHS24_Nr(v, &t[0], pp, steering);
+        tireRHS24_Nr(v, &t[1], pp, steering);
+        tireRHS24_Nr(v, &t[2], pp, 0);
+        tireRHS24_Nr(v, &t[3], pp, 0);
+    } else {
+        tireRHS24(v, &t[0], pp, steering);
+        tireRHS24(v, &t[1], pp, steering);
+        tireRHS24(v, &t[2], pp, 0);
+        tireRHS24(v, &t[3], pp, 0);
+    }
     tireCompression24(v, t, su);
     powertrain24(v, t, pp, controls);
     tireToVeh24(v, t, pp, steering);
@@ -1301,10 +1343,12 @@ static void rhs24(Veh24* v, Tire24* t, Sus24* su, const Par* pp, const double* c
 
 /* half-implicit update: 24dof-gpu/dof24_halfImplicit_gpu.cu:1016-1081 (CPU :199-283). Angles use  */
 /* the updated body rates, and x, y the updated yaw.                                              */
-static void update24(Veh24* v, Tire24* t, Sus24* su, const Par* pp, double step) {
+static void update24(Veh24* v, Tire24* t, Sus24* su, const Par* pp, double step, int nr) {
     for (int k = 0; k < 4; ++k) {
-        t[k].xe += t[k].xedot * step;
-        t[k].ye += t[k].yedot * step;
+        if (!nr) {
+            t[k].xe += t[k].xedot * step;
+            t[k].ye += t[k].yedot * step;
+        }
         t[k].xt += t[k].dxt * step;
         t[k].omega += t[k].dOmega * step;
     }
@@ -1337,11 +1381,12 @@ static void window24(const oracle18_args* a, int i, Veh24* v, Tire24* t, Sus24* 
     double kernel_time = 0;
     int64_t stored = 0;
     const double end_time = (tt + a->ksim) - step / 10.;
+    const int nr = a->tire_type == LFDM_TIRE_TMEASY_NR;
     while (tt < end_time) {
         double c[4];
         controls_at(a, i, tt, c);
-        rhs24(v, t, su, pp, c);
-        update24(v, t, su, pp, step);
+        rhs24(v, t, su, pp, c, nr);
+        update24(v, t, su, pp, step, nr);
         tt += step;
         kernel_time += step;
         if (a->resp && a->dtout > 0) {
@@ -1369,11 +1414,12 @@ static void run_vehicle24(const oracle18_args* a, int i) {
     if (a->schedule == 0) {
         /* d24SolverHalfImplicit::Integrate, 24dof/dof24_halfImplicit.cpp:188-297 */
         double tt = a->t0;
+        const int nr = a->tire_type == LFDM_TIRE_TMEASY_NR;
         while (tt < (a->tend - a->dt / 10.)) {
             double c[4];
             controls_at(a, i, tt, c);
-            rhs24(&v, t, su, &pp, c);
-            update24(&v, t, su, &pp, a->dt);
+            rhs24(&v, t, su, &pp, c, nr);
+            update24(&v, t, su, &pp, a->dt, nr);
             tt += a->dt;
         }
     } else if (a->schedule == 1) {

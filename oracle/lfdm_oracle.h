@@ -2,8 +2,7 @@
  * ORACLE — test infrastructure only. Nothing in the product links, loads or calls this.
  *
  * CPU restatement (plain C, FP64, no FMA contraction) of the reference's batched half-implicit
- * stepper for the 18-DOF model (TMeasy and TMeasyNr tires) and the 11-DOF and 24-DOF models
- * (TMeasy). It is the checker the CUDA path is compared against in tests/, smoke() and bench.py's
+ * stepper for the 18-, 11- and 24-DOF models with TMeasy and TMeasyNr tires. It is the checker the CUDA path is compared against in tests/, smoke() and bench.py's
  * CPU-baseline leg. It is pinned against the reference's own CPU solvers (oracle/refrun{11,18,24}.cpp,
  * built by `make ref`) through the golden fixtures in tests/golden/.
  */
@@ -48,7 +47,7 @@ typedef struct {
 int oracle18_run(const oracle18_args* a);
 /* The 11-DOF model with the same arguments: states [n][LFDM11_S_COUNT], resp [samples][9][n]. */
 int oracle11_run(const oracle18_args* a);
-/* The 24-DOF model (TMeasy): states [n][LFDM24_S_COUNT], resp [samples][15][n]. */
+/* The 24-DOF model: states [n][LFDM24_S_COUNT], resp [samples][15][n]. */
 int oracle24_run(const oracle18_args* a);
 /* initializeTireSus (24dof/dof24.cpp:34-88) applied to one flat 24-DOF state, as Initialize does. */
 void oracle24_init_state(const double* params, double* state);

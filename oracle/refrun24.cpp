@@ -13,7 +13,7 @@
 //               t restarts at k*ksim, each window runs while t < k*ksim + ksim - dt/10.
 //
 // Job format (stdin, whitespace separated, several jobs per stream):
-//   veh <json> | tire <json> | sus <json> | driver <txt> | dt <v> | tend <v> | ksim <v>
+//   veh <json> | tire <json> | sus <json> | tiretype 0|1 | driver <txt> | dt <v> | tend <v> | ksim <v>
 //   vp <field> <v> | tp <field> <v> | sp <field> <v> | vs <field> <v> | ts <tire 0..3> <field> <v>
 //   gear <initial gear> | sample <every n steps> | run
 // Parameters are set before Initialize, which applies initializeTireSus (dof24.cpp:34-88).
@@ -37,6 +37,7 @@ namespace {
 
 struct Job {
     std::string veh, tire, sus, driver;
+    int tiretype = 0;  // 0 TMeasy, 1 TMeasyNr
     double dt = 1e-3, tend = -1, ksim = 0;
     int sample = 0;
     std::vector<std::pair<std::string, double>> vp, tp, sp, vs;
@@ -92,31 +93,67 @@ void print_tire(const TMeasyState& s) {
                         s._vgy, s._vgz, s._vsx,   s._vsy,   s._vsz,   s._My,     s._engTor};
     for (double x : d) std::printf(" %.17g", x);
 }
+// TMeasyNr: the same 23-field block with the deflections and their rates at 0
+void print_tire(const TMeasyNrState& s) {
+    const double d[] = {0.0,    0.0,     0.0,     0.0,    s._omega, s._dOmega, s._xt,  s._dxt,
+                        s._rStat, s._fx, s._fy,   s._fz,  s._fxg,   s._fyg,    s._fzg, s._vgx,
+                        s._vgy, s._vgz,  s._vsx,  s._vsy, s._vsz,   s._My,     s._engTor};
+    for (double x : d) std::printf(" %.17g", x);
+}
 void print_sus(const SuspensionState& s) {
     const double d[] = {s._xs,  s._xsi, s._dxs, s._ls,  s._lsi, s._us,  s._vs,  s._ws,  s._dus, s._dvs, s._dws, s._uu,
                         s._vu,  s._wu,  s._duu, s._dvu, s._dwu, s._fxs, s._fys, s._fzs, s._fzd, s._mx,  s._my,  s._mz};
     for (double x : d) std::printf(" %.17g", x);
 }
 
+template <typename TS>
+void run_job(const Job& job, d24SolverHalfImplicit& solver, TS* const tires[4]);
+
 void run(const Job& job) {
     d24SolverHalfImplicit solver;
     solver.SetTimeStep(job.dt);
-    solver.Construct(job.veh, job.tire, job.sus, job.driver);
+    const bool nr = job.tiretype != 0;
+    solver.Construct(job.veh, job.tire, job.sus, job.driver, nr ? d24::TireType::TMeasyNr : d24::TireType::TMeasy);
     for (auto& kv : job.vp) *field(solver.m_veh_param, kVehParam, kv.first, "vehicle param") = kv.second;
-    for (auto& kv : job.tp) *field(solver.m_tireTM_param, kTireParam, kv.first, "tire param") = kv.second;
-    if (!job.tp.empty()) tireInit(solver.m_tireTM_param);
+    if (!job.tp.empty()) {
+        if (nr) {
+            std::fprintf(stderr, "tire parameter overrides are for TMeasy jobs\n");
+            std::exit(2);
+        }
+        for (auto& kv : job.tp) *field(solver.m_tireTM_param, kTireParam, kv.first, "tire param") = kv.second;
+        tireInit(solver.m_tireTM_param);
+    }
     for (auto& kv : job.sp) *field(solver.m_sus_param, kSusParam, kv.first, "suspension param") = kv.second;
     VehicleState vs;
     for (auto& kv : job.vs) *field(vs, kVehState, kv.first, "vehicle state") = kv.second;
     if (job.gear >= 0) vs._current_gr = job.gear;
-    TMeasyState ts[4];
-    for (auto& kv : job.ts) *field(ts[kv.first.first], kTireState, kv.first.second, "tire state") = kv.second;
     SuspensionState ss[4];
-    solver.Initialize(vs, ts[0], ts[1], ts[2], ts[3], ss[0], ss[1], ss[2], ss[3]);
+    if (!nr) {
+        TMeasyState ts[4];
+        for (auto& kv : job.ts) *field(ts[kv.first.first], kTireState, kv.first.second, "tire state") = kv.second;
+        solver.Initialize(vs, ts[0], ts[1], ts[2], ts[3], ss[0], ss[1], ss[2], ss[3]);
+        TMeasyState* const tires[4] = {&solver.m_tireTMlf_state, &solver.m_tireTMrf_state, &solver.m_tireTMlr_state,
+                                       &solver.m_tireTMrr_state};
+        run_job(job, solver, tires);
+    } else {
+        TMeasyNrState ts[4];
+        for (auto& kv : job.ts) {
+            if (kv.first.second != "omega") {
+                std::fprintf(stderr, "TMeasyNr tire state %s\n", kv.first.second.c_str());
+                std::exit(2);
+            }
+            ts[kv.first.first]._omega = kv.second;
+        }
+        solver.Initialize(vs, ts[0], ts[1], ts[2], ts[3], ss[0], ss[1], ss[2], ss[3]);
+        TMeasyNrState* const tires[4] = {&solver.m_tireTMNrlf_state, &solver.m_tireTMNrrf_state,
+                                         &solver.m_tireTMNrlr_state, &solver.m_tireTMNrrr_state};
+        run_job(job, solver, tires);
+    }
+}
 
+template <typename TS>
+void run_job(const Job& job, d24SolverHalfImplicit& solver, TS* const tires[4]) {
     VehicleState& v = solver.m_veh_state;
-    TMeasyState* const tires[4] = {&solver.m_tireTMlf_state, &solver.m_tireTMrf_state, &solver.m_tireTMlr_state,
-                                   &solver.m_tireTMrr_state};
     SuspensionState* const sus[4] = {&solver.m_suslf_state, &solver.m_susrf_state, &solver.m_suslr_state,
                                       &solver.m_susrr_state};
     DriverData drv;
@@ -164,6 +201,7 @@ int main() {
         else if (key == "tire") std::cin >> job.tire;
         else if (key == "sus") std::cin >> job.sus;
         else if (key == "driver") std::cin >> job.driver;
+        else if (key == "tiretype") std::cin >> job.tiretype;
         else if (key == "dt") std::cin >> job.dt;
         else if (key == "tend") std::cin >> job.tend;
         else if (key == "ksim") std::cin >> job.ksim;

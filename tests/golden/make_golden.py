@@ -100,6 +100,20 @@ def main(ref: str) -> None:
             meta.append({"name": name, "vehicle": veh_hmmwv, "tire": tire_hmmwv, "tire_type": 0, "driver": rows,
                          "dt": 0.001, "tend": tend_v, "ksim": ksim, "sample": sample, "vp": {}, "tp": {},
                          "state": [0.0] * abi.S_COUNT, "source": f"HMMWV vehicle.json + tmeasy.json, {drv}.txt"})
+        # TMeasyNr: the reference's Sedan files (high-level tire parameters, load index 97) on acc05,
+        # the case of the reference test dof18HiNr (tests/18dof.cpp), under both schedules
+        veh_sedan = json.load(open(os.path.join(d18, "json", "Sedan", "vehicle.json")))
+        tire_sedan = json.load(open(os.path.join(d18, "json", "Sedan", "tmeasyNr.json")))
+        vsj, tsj = write_json("sedan_vehicle.json", veh_sedan), write_json("sedan_tmeasyNr.json", tire_sedan)
+        for name, ksim, tend in (("sedan_nr_acc05_cpu", 0.0, None), ("sedan_nr_acc05_gpu", 2.0, 10.0)):
+            rows = lfdm.params.load_driver_table(os.path.join(d18, "input", "acc05.txt")).tolist()
+            tp = write_table(f"{name}.txt", rows)
+            tend_v = tend if tend is not None else rows[-1][0]
+            jobs += [f"veh {vsj}", f"tire {tsj}", "tiretype 1", f"driver {tp}", "dt 0.001", f"tend {_fmt(tend_v)}",
+                     f"ksim {_fmt(ksim)}", "sample 100", "run"]
+            meta.append({"name": name, "vehicle": veh_sedan, "tire": tire_sedan, "tire_type": 1, "driver": rows,
+                         "dt": 0.001, "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
+                         "state": [0.0] * abi.S_COUNT, "source": "Sedan vehicle.json + tmeasyNr.json, acc05.txt"})
         # seeded synthetic SUV fleet (GPU schedule, 1 s windows)
         n_syn = 12
         fl = fleet.fleet18(n_syn, seed=SEED, horizon=10.0)
@@ -171,6 +185,19 @@ def main11(ref: str) -> None:
             cases.append({"name": name, "vehicle": veh, "tire": tire, "tire_type": 0, "driver": rows, "dt": 0.001,
                           "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
                           "state": [0.0] * abi.C["LFDM11_S_COUNT"], "source": f"HMMWV 11-DOF json, {drv}.txt"})
+        # TMeasyNr: Sedan files on acc05 (reference test dof11HiNr, tests/11dof.cpp)
+        veh_s = json.load(open(os.path.join(d11, "json", "Sedan", "vehicle.json")))
+        tire_s = json.load(open(os.path.join(d11, "json", "Sedan", "tmeasyNr.json")))
+        vsj, tsj = write("sv_sedan.json", json.dumps(veh_s)), write("st_sedan.json", json.dumps(tire_s))
+        for name, ksim, tend in (("sedan11_nr_acc05_cpu", 0.0, None), ("sedan11_nr_acc05_gpu", 2.0, 10.0)):
+            rows = lfdm.params.load_driver_table(os.path.join(d11, "input", "acc05.txt")).tolist()
+            tp = write(f"{name}.txt", "".join(" ".join(_fmt(v) for v in r) + "\n" for r in rows))
+            tend_v = tend if tend is not None else rows[-1][0]
+            jobs += [f"veh {vsj}", f"tire {tsj}", "tiretype 1", f"driver {tp}", "dt 0.001", f"tend {_fmt(tend_v)}",
+                     f"ksim {_fmt(ksim)}", "sample 100", "run"]
+            cases.append({"name": name, "vehicle": veh_s, "tire": tire_s, "tire_type": 1, "driver": rows, "dt": 0.001,
+                          "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
+                          "state": [0.0] * abi.C["LFDM11_S_COUNT"], "source": "Sedan 11-DOF json, tmeasyNr, acc05.txt"})
         fl = fleet.fleet11(8, seed=SEED, horizon=10.0)
         sj, stj = write("sv.json", json.dumps(fleet.SUV11_VEHICLE)), write("st.json", json.dumps(fleet.SUV_TIRE))
         for i in range(8):
@@ -234,6 +261,22 @@ def main24(ref: str) -> None:
             cases.append({"name": name, "vehicle": veh, "tire": tire, "sus": sus, "tire_type": 0, "driver": rows,
                           "dt": 0.001, "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
                           "state": s_h.tolist(), "source": f"HMMWV 24-DOF json, {drv}.txt"})
+        # TMeasyNr: Sedan vehicle and tire with the HMMWV suspension on acc05 (reference test dof24HiNr,
+        # tests/24dof.cpp)
+        veh_s = json.load(open(os.path.join(d24, "json", "Sedan", "vehicle.json")))
+        tire_s = json.load(open(os.path.join(d24, "json", "Sedan", "tmeasyNr.json")))
+        vsj, tsj = write("v_sedan.json", json.dumps(veh_s)), write("t_sedan.json", json.dumps(tire_s))
+        _, p_s = lfdm.params.vehicle_from_json(veh_s, tire_s, 1, model=24, sus=sus)
+        s_s = fleet.init_tire_sus24(p_s[None], np.zeros((1, C["LFDM24_S_COUNT"])))[0]
+        for name, ksim, tend in (("sedan24_nr_acc05_cpu", 0.0, None), ("sedan24_nr_acc05_gpu", 2.0, 10.0)):
+            rows = lfdm.params.load_driver_table(os.path.join(d24, "input", "acc05.txt")).tolist()
+            tp = write(f"{name}.txt", "".join(" ".join(_fmt(v) for v in r) + "\n" for r in rows))
+            tend_v = tend if tend is not None else rows[-1][0]
+            jobs += [f"veh {vsj}", f"tire {tsj}", f"sus {sj}", "tiretype 1", f"driver {tp}", "dt 0.001",
+                     f"tend {_fmt(tend_v)}", f"ksim {_fmt(ksim)}", "sample 100", "run"]
+            cases.append({"name": name, "vehicle": veh_s, "tire": tire_s, "sus": sus, "tire_type": 1, "driver": rows,
+                          "dt": 0.001, "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
+                          "state": s_s.tolist(), "source": "Sedan 24-DOF json, tmeasyNr, HMMWV suspension, acc05.txt"})
         fl = fleet.fleet24(8, seed=SEED, horizon=10.0)
         svj, stj, ssj = (write("sv.json", json.dumps(fleet.SUV24_VEHICLE)), write("st.json", json.dumps(fleet.SUV_TIRE)),
                          write("ss.json", json.dumps(fleet.SUV24_SUS)))

@@ -65,8 +65,8 @@ def test_cpp_loader_matches_python_loader(built_lib, golden18):
             seen.add(key)
             vj = _write(tmp, "v.json", case["vehicle"])
             tj = _write(tmp, "t.json", case["tire"])
-            c_cls, c_p = built_lib.parse_vehicle18(vj, tj, 0)
-            py_cls, py_p = params.vehicle_from_json(case["vehicle"], case["tire"], 0)
+            c_cls, c_p = built_lib.parse_vehicle18(vj, tj, case["tire_type"])
+            py_cls, py_p = params.vehicle_from_json(case["vehicle"], case["tire"], case["tire_type"])
             assert np.array_equal(c_p, py_p)
             assert bytes(c_cls) == bytes(py_cls)
     assert len(seen) >= 2
@@ -74,8 +74,8 @@ def test_cpp_loader_matches_python_loader(built_lib, golden18):
 
 @pytest.mark.parametrize("model", [11, 24])
 def test_cpp_loader_matches_python_loader_11_24(built_lib, model):
-    """The library's 11- and 24-DOF loaders (tire doubling, jy, suspension file) against the Python
-    loader, on every distinct vehicle of the model's golden fixtures."""
+    """The library's 11- and 24-DOF loaders (tire doubling, jy, suspension file, TMeasyNr high-level
+    parameters) against the Python loader, on every distinct vehicle of the model's golden fixtures."""
     params = pkg_mod("params")
     with open(os.path.join(TESTS, "golden", f"golden{model}.json")) as f:
         cases = json.load(f)["cases"]
@@ -89,8 +89,9 @@ def test_cpp_loader_matches_python_loader_11_24(built_lib, model):
             vj = _write(tmp, "v.json", case["vehicle"])
             tj = _write(tmp, "t.json", case["tire"])
             sj = _write(tmp, "s.json", case["sus"]) if model == 24 else None
-            c_cls, c_p = built_lib.parse_vehicle(model, vj, tj, sj)
-            py_cls, py_p = params.vehicle_from_json(case["vehicle"], case["tire"], 0, model=model, sus=case.get("sus"))
+            c_cls, c_p = built_lib.parse_vehicle(model, vj, tj, sj, case["tire_type"])
+            py_cls, py_p = params.vehicle_from_json(case["vehicle"], case["tire"], case["tire_type"], model=model,
+                                                    sus=case.get("sus"))
             assert np.array_equal(c_p, py_p), np.nonzero(c_p != py_p)
             assert bytes(c_cls) == bytes(py_cls)
     assert len(seen) >= 2

@@ -37,7 +37,7 @@ def _groups(cases):
     g = {}
     for c in cases:
         if c["ksim"] > 0:
-            g.setdefault((c["ksim"], c["tend"], c["sample"]), []).append(c)
+            g.setdefault((c["ksim"], c["tend"], c["sample"], c["tire_type"]), []).append(c)
     return g
 
 
@@ -47,7 +47,7 @@ def _run_group(lfdm, cases, ksim, tend, freq):
     states = []
     for i, c in enumerate(cases):
         cls, p, s, tab = case_inputs11(c)
-        sol.construct_class(cls, p[None, :])
+        sol.construct_class(cls, p[None, :], c["tire_type"])
         sol.set_driver_tables(tab[None, :, :], first=i)
         states.append(s)
     sol.set_states(np.array(states))
@@ -77,7 +77,8 @@ def _perturbed_runs(cls, class_of, params, states, tables, **kw):
 def _envelope(case, dtout):
     """(final-state envelope, per-sample response envelope) of a golden case, vs its expected values."""
     cls, p, s, tab = case_inputs11(case)
-    runs = _perturbed_runs([cls], [0], p[None], s[None], [tab], dt=case["dt"], tend=case["tend"], ksim=case["ksim"],
+    runs = _perturbed_runs([cls], [0], p[None], s[None], [tab], tire_type=case["tire_type"], dt=case["dt"],
+                           tend=case["tend"], ksim=case["ksim"],
                            schedule=1, dtout=dtout)
     exp_f = np.array(case["expected_final"])
     exp = np.array(case["expected_samples"])
@@ -90,7 +91,7 @@ def test_golden11_trajectories_within_reference_sensitivity(built_lib, golden11)
     """HMMWV (reference data files and driver tables) and seeded SUV cases: final state and every
     sample within max(1e-9, 100 x the reference algorithm's sensitivity envelope)."""
     fl = state_floors11()
-    for (ksim, tend, sample), cases in _groups(golden11["cases"]).items():
+    for (ksim, tend, sample, _tire), cases in _groups(golden11["cases"]).items():
         freq = 1.0 / (sample * cases[0]["dt"])
         final, resp = _run_group(built_lib, cases, ksim, tend, freq)
         for i, c in enumerate(cases):
@@ -200,11 +201,12 @@ def test_solvestep_scalar11(built_lib):
     assert e.max() <= 1e-11, float(e.max())
 
 
-def test_model11_rejects_mixed_and_nr(built_lib):
+def test_model11_rejects_mixed_and_mixed_tire_types(built_lib):
     sol = built_lib.d11SolverHalfImplicitGPU(4)
     with pytest.raises(built_lib.LfdmError):
         sol.set_precision(pkg_mod("_abi").PREC_MIXED)
     cls, p = pkg_mod("fleet").suv11()
-    with pytest.raises(built_lib.LfdmError):
-        sol.construct_class(cls, p[None, :], built_lib.TireType.TMeasyNr)
+    sol.construct_class(cls, p[None, :], built_lib.TireType.TMeasyNr)
+    with pytest.raises(built_lib.LfdmError):  # one tire type per solver
+        sol.construct_class(cls, p[None, :], built_lib.TireType.TMeasy)
     sol.close()

@@ -40,7 +40,7 @@ def _groups(cases):
     g = {}
     for c in cases:
         if c["ksim"] > 0:
-            g.setdefault((c["ksim"], c["tend"], c["sample"]), []).append(c)
+            g.setdefault((c["ksim"], c["tend"], c["sample"], c["tire_type"]), []).append(c)
     return g
 
 
@@ -50,7 +50,7 @@ def _run_group(lfdm, cases, ksim, tend, freq):
     states = []
     for i, c in enumerate(cases):
         cls, p, s, tab = case_inputs24(c)
-        sol.construct_class(cls, p[None, :])
+        sol.construct_class(cls, p[None, :], c["tire_type"])
         sol.set_driver_tables(tab[None, :, :], first=i)
         states.append(s)
     sol.set_states(np.array(states))
@@ -81,13 +81,13 @@ def test_golden24_trajectories_within_reference_sensitivity(built_lib, golden24)
     """HMMWV (reference data files and driver tables, 22 s) and seeded SUV cases: the full final
     state and every sample within max(1e-9, 100 x the sensitivity envelope)."""
     fl = state_floors24()
-    for (ksim, tend, sample), cases in _groups(golden24["cases"]).items():
+    for (ksim, tend, sample, _tire), cases in _groups(golden24["cases"]).items():
         freq = 1.0 / (sample * cases[0]["dt"])
         final, resp = _run_group(built_lib, cases, ksim, tend, freq)
         for i, c in enumerate(cases):
             cls, p, s, tab = case_inputs24(c)
-            runs = _perturbed_runs([cls], [0], p[None], s[None], [tab], dt=c["dt"], tend=c["tend"], ksim=c["ksim"],
-                                   schedule=1, dtout=sample * c["dt"])
+            runs = _perturbed_runs([cls], [0], p[None], s[None], [tab], tire_type=c["tire_type"], dt=c["dt"],
+                                   tend=c["tend"], ksim=c["ksim"], schedule=1, dtout=sample * c["dt"])
             exp_f = np.array(c["expected_final"])
             exp = np.array(c["expected_samples"])
             env_f = max(rel_err(st[0], exp_f, fl).max() for st, _ in runs)
@@ -216,13 +216,14 @@ def test_one_window24_parity_from_diverse_states(built_lib):
     assert e.max() <= 1e-12, (float(e.max()), int(e.max(axis=1).argmax()), int(e.max(axis=0).argmax()))
 
 
-def test_model24_rejects_mixed_nr_and_missing_suspension(built_lib):
+def test_model24_rejects_mixed_tire_types_and_missing_suspension(built_lib):
     sol = built_lib.d24SolverHalfImplicitGPU(4)
     with pytest.raises(built_lib.LfdmError):
         sol.set_precision(pkg_mod("_abi").PREC_MIXED)
-    cls, p = pkg_mod("fleet").suv24()
-    with pytest.raises(built_lib.LfdmError):
-        sol.construct_class(cls, p[None, :], built_lib.TireType.TMeasyNr)
     with pytest.raises(built_lib.LfdmError):
         sol.Initialize(np.zeros(built_lib.S24_COUNT), 1)  # Initialize needs the vehicle's parameters
+    cls, p = pkg_mod("fleet").suv24()
+    sol.construct_class(cls, p[None, :], built_lib.TireType.TMeasyNr)
+    with pytest.raises(built_lib.LfdmError):  # one tire type per solver
+        sol.construct_class(cls, p[None, :], built_lib.TireType.TMeasy)
     sol.close()

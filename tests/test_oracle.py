@@ -40,6 +40,10 @@ def test_reference_test_goldens(golden18):
     assert abs(by["hmmwv_acc3_cpu"]["expected_final"][0] - 88.5335) < 1.0
     assert abs(by["hmmwv_acc3_gpu"]["expected_final"][0] - 88.5335) < 1.0
     assert abs(by["hmmwv_dl4_gpu"]["expected_final"][0] - 106.548) < 1.0
+    # TMeasyNr with high-level tire parameters: tests/18dof.cpp dof18HiNr (114.973)
+    assert abs(by["sedan_nr_acc05_cpu"]["expected_final"][0] - 114.973) < 1.0
+    st, _ = _run_case(by["sedan_nr_acc05_cpu"])
+    assert st[0, 0] == pytest.approx(114.973, abs=1e-3)
     st, _ = _run_case(by["hmmwv_acc3_cpu"])
     assert st[0, 0] == pytest.approx(88.533467841729632, abs=1e-9)
 

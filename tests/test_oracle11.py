@@ -28,8 +28,8 @@ def inputs11(case):
 def run_case(case, dtout=0.0):
     cls, p, s, tab = inputs11(case)
     sched = 0 if case["ksim"] == 0 else 1
-    return O.run18([cls], [0], p[None], s[None], [tab], dt=case["dt"], tend=case["tend"], ksim=case["ksim"] or 1.0,
-                   schedule=sched, dtout=dtout, model=11)
+    return O.run18([cls], [0], p[None], s[None], [tab], tire_type=case["tire_type"], dt=case["dt"], tend=case["tend"],
+                   ksim=case["ksim"] or 1.0, schedule=sched, dtout=dtout, model=11)
 
 
 def test_golden11_final_states(golden11):
@@ -61,3 +61,5 @@ def test_reference_11dof_test_pins(golden11):
     assert abs(by["hmmwv11_acc3_cpu"]["expected_final"][0] - 70.6758) < 1
     assert abs(by["hmmwv11_acc3_gpu22"]["expected_final"][0] - 198.72) < 1
     assert abs(by["hmmwv11_dl4_gpu"]["expected_final"][0] - 104.805) < 1
+    # TMeasyNr with high-level tire parameters: tests/11dof.cpp dof11HiNr (115.1)
+    assert abs(by["sedan11_nr_acc05_cpu"]["expected_final"][0] - 115.1) < 1

@@ -23,8 +23,8 @@ def golden24():
 def run_case(case, dtout=0.0):
     cls, p, s, tab = case_inputs24(case)
     sched = 0 if case["ksim"] == 0 else 1
-    return O.run18([cls], [0], p[None], s[None], [tab], dt=case["dt"], tend=case["tend"], ksim=case["ksim"] or 1.0,
-                   schedule=sched, dtout=dtout, model=24)
+    return O.run18([cls], [0], p[None], s[None], [tab], tire_type=case["tire_type"], dt=case["dt"], tend=case["tend"],
+                   ksim=case["ksim"] or 1.0, schedule=sched, dtout=dtout, model=24)
 
 
 def test_golden24_final_states(golden24):
@@ -57,6 +57,8 @@ def test_reference_24dof_test_pins(golden24):
     assert abs(by["hmmwv24_acc3_cpu"]["expected_final"][0] - 89.1625) < 1
     assert abs(by["hmmwv24_acc3_gpu22"]["expected_final"][0] - 235.685) < 1
     assert abs(by["hmmwv24_dl4_gpu22"]["expected_final"][0] - 91.5211) < 1
+    # TMeasyNr with high-level tire parameters: tests/24dof.cpp dof24HiNr (114.938)
+    assert abs(by["sedan24_nr_acc05_cpu"]["expected_final"][0] - 114.938) < 1
 
 
 def test_init_tire_sus24_matches_oracle():
