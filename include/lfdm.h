@@ -302,6 +302,19 @@ int lfdm_traj18_backward(lfdm_solver* h, const double* ctl, const double* ref, u
 /* CUDA-event times of the last forward and backward kernels. */
 int lfdm_traj18_last_ms(lfdm_solver* h, double* forward_ms, double* backward_ms);
 
+/* Exact Jacobians of the 18-DOF right-hand side for every vehicle (extension; the reference's GPU  */
+/* solver has none, its CPU solver takes central differences: IntegrateStepWithJacobian,           */
+/* GetJacobianState, GetJacobianControls, 18dof/dof18_halfImplicit.cpp:356-520). At each vehicle's  */
+/* current state and the controls ctl [3][N] (DEVICE, steering/throttle/braking; braking enters no  */
+/* derivative): jac_state [ny][ny][N] = d rhs_r / d y_c and jac_ctl [ny][2][N] = d rhs_r /          */
+/* d (steering, throttle), DEVICE arrays, in the reference's packed order (packY/packYDOT, :879-1018): */
+/* y = {xe, ye} of LF, RF, LR, RR, omega x 4, crank speed (torque converter only), x, y, u, v, psi,  */
+/* wz, phi, wx; ny = 21 with a torque converter, 20 without (*ny). reference_point = 1 differentiates */
+/* where PerturbRhsFun does (a fresh vehicle state: previous accelerations 0, first gear); 0 at the   */
+/* full current state. TMeasy tires; all vehicles with or all without a torque converter.            */
+int lfdm_rhs_jacobian18(lfdm_solver* h, const double* ctl, int reference_point, double* jac_state, double* jac_ctl,
+                        int* ny);
+
 /* ------------------------------------------------------------------------------------------ */
 /* Mixed-DOF fleets (no counterpart class in the reference, whose solvers hold one model and one */
 /* end time each: d18SolverHalfImplicitGPU, d24SolverHalfImplicitGPU). A fleet holds 18-DOF and   */

@@ -96,6 +96,7 @@ def _sig(lib):
         "lfdm_traj18_forward": ([vp, vp, vp, u, d, u, vp], i),
         "lfdm_traj18_backward": ([vp, vp, vp, u, d, u, vp, vp, vp], i),
         "lfdm_traj18_last_ms": ([vp, _c_dp, _c_dp], i),
+        "lfdm_rhs_jacobian18": ([vp, vp, i, vp, vp, ctypes.POINTER(i)], i),
         "lfdm_fleet_create": ([i, ctypes.POINTER(vp)], i),
         "lfdm_fleet_destroy": ([vp], i),
         "lfdm_fleet_last_error": ([vp], cp),
@@ -198,6 +199,7 @@ class _SolverGPU:
             raise LfdmError(rc, self._L.lfdm_last_error(None).decode())
         self._h = h
         self.n = int(total_num_vehicles)
+        self.device = int(device)
 
     # -- plumbing -----------------------------------------------------------------------------
     def _ck(self, rc: int):
@@ -384,6 +386,29 @@ class d18SolverHalfImplicitGPU(_SolverGPU):
     MODEL = 18
     STATE_COUNT = S_COUNT
     RESP_CHANNELS = RESP18
+
+    def rhs_jacobian(self, steering, throttle, braking=0.0, reference_point: bool = True):
+        """Exact Jacobians of the right-hand side at every vehicle's current state (lfdm_rhs_jacobian18;
+        the reference CPU solver's GetJacobianState / GetJacobianControls by central differences,
+        18dof/dof18_halfImplicit.cpp:356-520). Controls are scalars or arrays of N. Returns
+        (jac_state [N, ny, ny], jac_controls [N, ny, 2]) in the reference's packed order, ny = 21 with a
+        torque converter and 20 without; reference_point selects the point the reference
+        differentiates at (previous accelerations 0, first gear) rather than the full current state."""
+        import torch
+        dev = torch.device("cuda", self.device)
+        n = self.n
+        ctl = torch.tensor(np.stack([np.broadcast_to(np.asarray(x, dtype=np.float64), (n,))
+                                     for x in (steering, throttle, braking)]), dtype=torch.float64, device=dev)
+        js = torch.empty(21 * 21 * n, dtype=torch.float64, device=dev)
+        ju = torch.empty(21 * 2 * n, dtype=torch.float64, device=dev)
+        ny = ctypes.c_int()
+        self._ck(self._L.lfdm_rhs_jacobian18(self._h, ctypes.c_void_p(ctl.data_ptr()), int(bool(reference_point)),
+                                             ctypes.c_void_p(js.data_ptr()), ctypes.c_void_p(ju.data_ptr()),
+                                             ctypes.byref(ny)))
+        m = ny.value
+        jac_state = js[: m * m * n].reshape(m, m, n).permute(2, 0, 1).cpu().numpy()
+        jac_ctl = ju[: m * 2 * n].reshape(m, 2, n).permute(2, 0, 1).cpu().numpy()
+        return jac_state, jac_ctl
 
 
 class d11SolverHalfImplicitGPU(_SolverGPU):

@@ -841,41 +841,22 @@ __device__ __forceinline__ void tire_rev(const TapeRef& T, const KView& K, const
     kb.at(KB_INVKT) = fma(T.at(TT_(fz)), xtb, kb.at(KB_INVKT));
 }
 
-// One step's reverse sweep. L: on entry the adjoint of the state after the step, on return that of
-// the state before it; the adjoints of the step's controls are added to steerb/thrb/brkb and those
-// of the differentiable constants to kb.
-__device__ __forceinline__ void rev18(const TapeRef& T, const KView& K, const ClassDev18& C, const KBar& kb,
-                                      double dt, Adj18& L, double& steerb, double& thrb, double& brkb) {
+// Reverse of one right-hand-side evaluation (rhsFun): from the adjoints of its outputs (udotb,
+// vdotb, wxdotb, wzdotb: chassis accelerations; dOcb: crank acceleration with a torque converter;
+// crank_outb: the crank speed the powertrain computes from the wheel speeds without one; dOmb,
+// xedotnb, yedotnb: wheel accelerations and deflection rates) to those of the state it reads, which
+// are added to ub, vb, wxb, wzb, phib, crankb and om_midb; L.xe/L.ye hold on entry what the caller
+// carries for the deflections and receive (with L.om, L.xedot, L.yedot, L.udot, L.vdot) the
+// totals. The adjoints of the controls are added to steerb/thrb/brkb, those of the parameter
+// constants to kb.
+__device__ __forceinline__ void rev18_rhs(const TapeRef& T, const KView& K, const ClassDev18& C, const KBar& kb,
+                                          const double udotb, const double vdotb, const double wxdotb,
+                                          const double wzdotb, const double dOcb, double crank_outb,
+                                          const double* dOmb, const double* xedotnb, const double* yedotnb,
+                                          double& ub, double& vb, double& wxb, double& wzb, double& phib,
+                                          double& crankb, double* om_midb, Adj18& L, double& steerb, double& thrb,
+                                          double& brkb) {
     const int g = (int)T.at(TS_(gear));
-    // half-implicit update: x, y with the updated speeds and the old yaw; yaw and roll with the
-    // updated rates
-    double u1b = dt * fma(T.at(TS_(cp)), L.x, T.at(TS_(sp)) * L.y);
-    double v1b = dt * fma(-T.at(TS_(sp)), L.x, T.at(TS_(cp)) * L.y);
-    double psib = fma(dt, (fma((fma(-T.at(TS_(u1)), T.at(TS_(sp)), -(T.at(TS_(v1))) * T.at(TS_(cp)))), L.x, (fma(T.at(TS_(u1)), T.at(TS_(cp)), -(T.at(TS_(v1))) * T.at(TS_(sp)))) * L.y)), L.psi);
-    double wz1b = fma(dt, L.psi, L.wz);
-    double wx1b = fma(dt, L.phi, L.wx);
-    const double phib0 = L.phi;
-    u1b += L.u;
-    v1b += L.v;
-    double ub = u1b, vb = v1b, wxb = wx1b, wzb = wz1b, phib = phib0;
-    const double udotb = fma(dt, u1b, L.udot);  // the new accelerations are also carried to the next step
-    const double vdotb = fma(dt, v1b, L.vdot);
-    const double wxdotb = dt * wx1b, wzdotb = dt * wz1b;
-    double crankb = 0, dOcb = 0, crank_outb = 0;
-    if (C.tcbool) {
-        crankb = L.crank;
-        dOcb = dt * L.crank;
-    } else {
-        crank_outb = L.crank;
-    }
-    double om_midb[4], dOmb[4], xedotnb[4], yedotnb[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        om_midb[k] = L.om[k];
-        dOmb[k] = dt * L.om[k];
-        xedotnb[k] = fma(dt, L.xe[k], L.xedot[k]);
-        yedotnb[k] = fma(dt, L.ye[k], L.yedot[k]);
-    }
     // vehicle RHS
     double fxrb[4], fyrb[4];
     {
@@ -1077,6 +1058,46 @@ __device__ __forceinline__ void rev18(const TapeRef& T, const KView& K, const Cl
         vdot_oldb = latb;
         udot_oldb = lonb;
     }
+    L.udot = udot_oldb;
+    L.vdot = vdot_oldb;
+}
+
+// One step's reverse sweep. L: on entry the adjoint of the state after the step, on return that of
+// the state before it; the adjoints of the step's controls are added to steerb/thrb/brkb and those
+// of the differentiable constants to kb.
+__device__ __forceinline__ void rev18(const TapeRef& T, const KView& K, const ClassDev18& C, const KBar& kb,
+                                      double dt, Adj18& L, double& steerb, double& thrb, double& brkb) {
+    // half-implicit update: x, y with the updated speeds and the old yaw; yaw and roll with the
+    // updated rates
+    double u1b = dt * fma(T.at(TS_(cp)), L.x, T.at(TS_(sp)) * L.y);
+    double v1b = dt * fma(-T.at(TS_(sp)), L.x, T.at(TS_(cp)) * L.y);
+    double psib = fma(dt, (fma((fma(-T.at(TS_(u1)), T.at(TS_(sp)), -(T.at(TS_(v1))) * T.at(TS_(cp)))), L.x, (fma(T.at(TS_(u1)), T.at(TS_(cp)), -(T.at(TS_(v1))) * T.at(TS_(sp)))) * L.y)), L.psi);
+    double wz1b = fma(dt, L.psi, L.wz);
+    double wx1b = fma(dt, L.phi, L.wx);
+    const double phib0 = L.phi;
+    u1b += L.u;
+    v1b += L.v;
+    double ub = u1b, vb = v1b, wxb = wx1b, wzb = wz1b, phib = phib0;
+    const double udotb = fma(dt, u1b, L.udot);  // the new accelerations are also carried to the next step
+    const double vdotb = fma(dt, v1b, L.vdot);
+    const double wxdotb = dt * wx1b, wzdotb = dt * wz1b;
+    double crankb = 0, dOcb = 0, crank_outb = 0;
+    if (C.tcbool) {
+        crankb = L.crank;
+        dOcb = dt * L.crank;
+    } else {
+        crank_outb = L.crank;
+    }
+    double om_midb[4], dOmb[4], xedotnb[4], yedotnb[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        om_midb[k] = L.om[k];
+        dOmb[k] = dt * L.om[k];
+        xedotnb[k] = fma(dt, L.xe[k], L.xedot[k]);
+        yedotnb[k] = fma(dt, L.ye[k], L.yedot[k]);
+    }
+    rev18_rhs(T, K, C, kb, udotb, vdotb, wxdotb, wzdotb, dOcb, crank_outb, dOmb, xedotnb, yedotnb, ub, vb, wxb, wzb,
+              phib, crankb, om_midb, L, steerb, thrb, brkb);
     // L.x, L.y are unchanged (x and y enter the next state with unit weight)
     L.u = ub;
     L.v = vb;
@@ -1084,8 +1105,6 @@ __device__ __forceinline__ void rev18(const TapeRef& T, const KView& K, const Cl
     L.wz = wzb;
     L.phi = phib;
     L.wx = wxb;
-    L.udot = udot_oldb;
-    L.vdot = vdot_oldb;
     L.crank = C.tcbool ? crankb : 0.0;
 }
 

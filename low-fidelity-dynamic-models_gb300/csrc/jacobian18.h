@@ -1,0 +1,30 @@
+// Batched exact Jacobians of the 18-DOF right-hand side (jacobian18.cu).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace lfdm {
+
+struct ClassDev18;
+
+struct JacLaunch {
+    int n = 0, npad = 0;
+    const double* K = nullptr;             // [K18 count][npad]
+    const ClassDev18* classes = nullptr;
+    int nclasses = 0;
+    bool cls_smem = false;                 // set by the launcher
+    const int32_t* class_of = nullptr;     // [n]
+    const double* S = nullptr;             // [LFDM_S_COUNT][npad] states (SoA)
+    const double* ctl = nullptr;           // [3][n] steering, throttle, braking
+    int reference_point = 1;               // 1: PerturbRhsFun's fresh state; 0: the full current state
+    double* tape = nullptr;                // [tape doubles][npad] scratch
+    double* jac_state = nullptr;           // [ny][ny][n]
+    double* jac_ctl = nullptr;             // [ny][2][n]
+};
+
+cudaError_t launch_rhs_jacobian18(const JacLaunch& A, cudaStream_t stream);
+
+}  // namespace lfdm

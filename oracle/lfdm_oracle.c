@@ -572,6 +572,53 @@ static void rhs(Veh* v, Tire* t, const Par* pp, const double* controls, int nr) 
     vehRHS(v, pp, fx, fy);
 }
 
+/* PerturbRhsFun (18dof/dof18_halfImplicit.cpp:679-745) with unpackY / packYDOT (:954-1101): the
+   right-hand side at the packed states y, TMeasy tires. */
+int oracle18_rhs(const lfdm_class18* cls, const double* params, const double* full_state, const double* y,
+                 const double* ctl, double* ydot) {
+    Par pp_ = {params, cls};
+    const Par* pp = &pp_;
+    Veh v;
+    Tire t[4];
+    memset(&v, 0, sizeof v);
+    memset(t, 0, sizeof t);
+    if (full_state) load_state(full_state, &v, t);
+    const int tc = cls->tcbool != 0;
+    int i = 0;
+    for (int k = 0; k < 4; ++k) {
+        t[k].xe = y[i++];
+        t[k].ye = y[i++];
+    }
+    for (int k = 0; k < 4; ++k) t[k].omega = y[i++];
+    if (tc) v.crankOmega = y[i++];
+    v.x = y[i++];
+    v.y = y[i++];
+    v.u = y[i++];
+    v.v = y[i++];
+    v.psi = y[i++];
+    v.wz = y[i++];
+    v.phi = y[i++];
+    v.wx = y[i++];
+    const double controls[4] = {0.0, ctl[0], ctl[1], ctl[2]};
+    rhs(&v, t, pp, controls, 0);
+    i = 0;
+    for (int k = 0; k < 4; ++k) {
+        ydot[i++] = t[k].xedot;
+        ydot[i++] = t[k].yedot;
+    }
+    for (int k = 0; k < 4; ++k) ydot[i++] = t[k].dOmega;
+    if (tc) ydot[i++] = v.dOmega_crank;
+    ydot[i++] = (v.u * cos(v.psi) - v.v * sin(v.psi)); /* computeVehRHS, 18dof/dof18.cpp:1075-1077 */
+    ydot[i++] = (v.u * sin(v.psi) + v.v * cos(v.psi));
+    ydot[i++] = v.udot;
+    ydot[i++] = v.vdot;
+    ydot[i++] = v.wz;
+    ydot[i++] = v.wzdot;
+    ydot[i++] = v.wx;
+    ydot[i++] = v.wxdot;
+    return i;
+}
+
 /* half-implicit update: dof18_halfImplicit_gpu.cu:913-946 */
 static void update(Veh* v, Tire* t, const Par* pp, double step, int nr) {
     for (int k = 0; k < 4; ++k) {

@@ -52,6 +52,14 @@ int oracle24_run(const oracle18_args* a);
 /* initializeTireSus (24dof/dof24.cpp:34-88) applied to one flat 24-DOF state, as Initialize does. */
 void oracle24_init_state(const double* params, double* state);
 
+/* PerturbRhsFun (18dof/dof18_halfImplicit.cpp:679-745): the 18-DOF right-hand side at the packed
+   states y (packY order: {xe, ye} x 4 tires, omega x 4, crank speed with a torque converter, x, y, u,
+   v, psi, wz, phi, wx) with ctl {steering, throttle, braking}, into ydot (packYDOT order). The other
+   state fields come from full_state [LFDM_S_COUNT] when given, else are those of a freshly
+   constructed state (0, first gear), as in the reference. TMeasy tires. Returns the count. */
+int oracle18_rhs(const lfdm_class18* cls, const double* params, const double* full_state, const double* y,
+                 const double* ctl, double* ydot);
+
 /* tireInit (18dof-gpu/dof18_gpu.cu:227-241) on one flat parameter vector. */
 void oracle_tire_init(double* params);
 

@@ -44,6 +44,8 @@ def lib(fma: bool = False):
         L.oracle_map_y.restype = ctypes.c_double
         L.oracle_driver_input.argtypes = [ctypes.c_double, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.oracle_tire_init.argtypes = [ctypes.c_void_p]
+        L.oracle18_rhs.argtypes = [ctypes.c_void_p] * 6
+        L.oracle18_rhs.restype = ctypes.c_int
         _libs[path] = L
     return _libs[path]
 
@@ -131,4 +133,30 @@ def driver_input(t, rows) -> np.ndarray:
     r = np.ascontiguousarray(np.asarray(rows, dtype=np.float64).reshape(-1, 4))
     out = np.zeros(4)
     lib().oracle_driver_input(float(t), r.ctypes.data, r.shape[0], out.ctypes.data)
+    return out
+
+
+def pack_y18(state, tc: bool) -> np.ndarray:
+    """packY (18dof/dof18_halfImplicit.cpp:879-921) of a flat 18-DOF state (include/lfdm.h order)."""
+    s = np.asarray(state, dtype=np.float64)
+    T0, TS = 15, 15
+    y = []
+    for k in range(4):
+        y += [s[T0 + k * TS + 0], s[T0 + k * TS + 1]]
+    y += [s[T0 + k * TS + 4] for k in range(4)]
+    if tc:
+        y.append(s[12])
+    y += [s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7]]
+    return np.array(y)
+
+
+def rhs18(cls, params, y, ctl, full_state=None) -> np.ndarray:
+    """The reference's PerturbRhsFun (oracle18_rhs): the 18-DOF right-hand side at packed states y."""
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    c = np.ascontiguousarray(ctl, dtype=np.float64)
+    out = np.zeros(len(y))
+    fs = None if full_state is None else np.ascontiguousarray(full_state, dtype=np.float64)
+    n = lib().oracle18_rhs(ctypes.byref(cls), _ptr(p), None if fs is None else _ptr(fs), _ptr(y), _ptr(c), _ptr(out))
+    assert n == len(y)
     return out

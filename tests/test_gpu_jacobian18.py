@@ -1,0 +1,119 @@
+"""Exact right-hand-side Jacobians of the 18-DOF model on the GPU (lfdm_rhs_jacobian18) against
+central differences of the reference algorithm's own right-hand side (the oracle's restatement of
+PerturbRhsFun, 18dof/dof18_halfImplicit.cpp:679-745), in the reference's packed order, at the point
+the reference differentiates at (fresh vehicle state) and at the full current state.
+
+Tolerance, over the entries that are not zero in both (relative to max(|entry|, 1e-7 x the row's
+largest entry)): median <= 1e-6 and at least 95 % <= 1e-5 against small-step central differences.
+The remainder are entries whose +-h perturbation crosses a branch of the tire curve or the
+drivetrain, which a finite difference straddles and the exact derivative does not. Against the reference's own scheme (steps
+of 1e-3 of each state) the agreement is at its truncation error: median <= 1e-4."""
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from conftest import pkg_mod
+
+pytestmark = pytest.mark.gpu
+
+
+def _fleet(lfdm, n=48, seed=11):
+    fleet = pkg_mod("fleet")
+    f = fleet.fleet18(n, seed=seed, horizon=3.0)
+    sol = lfdm.d18SolverHalfImplicitGPU(n)
+    sol.construct_class(f["cls"][0], f["params"])
+    sol.set_driver_tables(f["tables"])
+    sol.set_states(f["states"])
+    sol.SetKernelSimTime(1.0)
+    sol.SetEndTime(2.0)
+    sol.Solve()  # diverse speeds, slips and gears after 2 s of the seeded drivers
+    rng = np.random.default_rng(seed)
+    ctl = np.stack([rng.uniform(-0.3, 0.3, n), rng.uniform(0.0, 1.0, n), rng.uniform(0.0, 0.3, n)])
+    return f, sol, sol.get_states(), ctl
+
+
+def _fd(cls, p, y, ctl, full_state, steps):
+    m = len(y)
+    J = np.zeros((m, m))
+    for c in range(m):
+        h = steps[c]
+        yp, ym = y.copy(), y.copy()
+        yp[c] += h
+        ym[c] -= h
+        J[:, c] = (O.rhs18(cls, p, yp, ctl, full_state) - O.rhs18(cls, p, ym, ctl, full_state)) / (2 * h)
+    Ju = np.zeros((m, 2))
+    for c in range(2):
+        h = 1e-7
+        cp, cm = np.array(ctl, dtype=float), np.array(ctl, dtype=float)
+        cp[c] += h
+        cm[c] -= h
+        Ju[:, c] = (O.rhs18(cls, p, y, cp, full_state) - O.rhs18(cls, p, y, cm, full_state)) / (2 * h)
+    return J, Ju
+
+
+def _rel(a, b):
+    """Relative differences of the entries that are not zero in both (structural zeros excluded)."""
+    scale = np.maximum(np.abs(b).max(axis=1, keepdims=True), 1e-300)
+    floor = 1e-7 * scale
+    e = np.abs(a - b) / np.maximum(np.abs(b), floor)
+    keep = (np.abs(a) > floor) | (np.abs(b) > floor)
+    return e[keep]
+
+
+@pytest.mark.parametrize("reference_point", [True, False])
+def test_jacobian_matches_central_differences_of_the_reference_rhs(built_lib, reference_point):
+    f, sol, states, ctl = _fleet(built_lib)
+    js, ju = sol.rhs_jacobian(ctl[0], ctl[1], ctl[2], reference_point=reference_point)
+    sol.close()
+    cls = f["cls"][0]
+    tc = bool(cls.tcbool)
+    assert js.shape[1:] == (21 if tc else 20,) * 2 and ju.shape[2] == 2
+    errs, errs_u = [], []
+    for i in range(states.shape[0]):
+        y = O.pack_y18(states[i], tc)
+        full = None if reference_point else states[i]
+        steps = 1e-6 * np.maximum(np.abs(y), 1e-2)
+        J, Ju = _fd(cls, f["params"][i], y, ctl[:, i], full, steps)
+        errs.append(_rel(js[i], J))
+        errs_u.append(_rel(ju[i], Ju))
+    e, eu = np.concatenate(errs), np.concatenate(errs_u)
+    print(f"state Jacobian ({e.size} nonzero entries): median {np.median(e):.1e}, 95% {np.quantile(e, 0.95):.1e}; "
+          f"controls: median {np.median(eu):.1e}, 95% {np.quantile(eu, 0.95):.1e}")
+    assert np.median(e) <= 1e-6 and (e <= 1e-5).mean() >= 0.95
+    assert np.median(eu) <= 1e-6 and (eu <= 1e-5).mean() >= 0.95
+
+
+def test_jacobian_agrees_with_the_reference_scheme(built_lib):
+    """IntegrateStepWithJacobian's own differences: steps of 1e-3 of each state (1e-3 where the state
+    is below 1e-8), 1e-3 on steering and throttle, braking 0."""
+    f, sol, states, ctl = _fleet(built_lib, n=16, seed=5)
+    js, ju = sol.rhs_jacobian(ctl[0], ctl[1], 0.0)
+    sol.close()
+    cls = f["cls"][0]
+    tc = bool(cls.tcbool)
+    errs = []
+    for i in range(states.shape[0]):
+        y = O.pack_y18(states[i], tc)
+        steps = np.abs(y * 1e-3)
+        steps[steps < 1e-8] = 1e-3
+        J, _ = _fd(cls, f["params"][i], y, [ctl[0, i], ctl[1, i], 0.0], None, steps)
+        errs.append(_rel(js[i], J))
+    e = np.concatenate(errs)
+    print(f"vs the reference's 1e-3 differences ({e.size} nonzero entries): median {np.median(e):.1e}")
+    assert np.median(e) <= 1e-4
+
+
+def test_kinematic_rows_and_errors(built_lib):
+    f, sol, states, ctl = _fleet(built_lib, n=8, seed=2)
+    js, _ = sol.rhs_jacobian(ctl[0], ctl[1], ctl[2])
+    o = 13 if f["cls"][0].tcbool else 12
+    psi, u, v = states[:, 4], states[:, 2], states[:, 3]
+    assert np.allclose(js[:, o, o + 2], np.cos(psi), rtol=1e-15, atol=1e-15)
+    assert np.allclose(js[:, o + 1, o + 4], u * np.cos(psi) - v * np.sin(psi), rtol=1e-13, atol=1e-13)
+    assert np.all(js[:, o + 4, o + 5] == 1.0) and np.all(js[:, o + 6, o + 7] == 1.0)
+    sol.close()
+    s11 = built_lib.d11SolverHalfImplicitGPU(2)
+    jac = built_lib.d18SolverHalfImplicitGPU.rhs_jacobian.__get__(s11)  # the 18-DOF call on an 11-DOF solver
+    with pytest.raises(built_lib.LfdmError):
+        jac(0.0, 0.0)
+    s11.close()
