@@ -464,6 +464,10 @@ def run_ours(a, dist: Dist):
     # HBM view of the same kernel: algorithmic bytes per window (state in/out, constants, the
     # window's table rows, the response written)
     alg_bytes = n * (2 * 75 * 8 + 70 * 8 + (rows_w := int(round(ksim / 0.01)) + 1) * 32 + spw * 13 * 8)
+    # DRAM bytes of one window launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu
+    # capture of this default configuration (300,000 vehicles, 1 s windows, 100 Hz outputs; the
+    # summary is profiles/window18_fp64.md); other configurations have no capture and report null
+    traffic = 1687990272 + 3257568768 if (n == 300_000 and ksim == 1.0 and spw == 100) else None
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -503,14 +507,15 @@ def run_ours(a, dist: Dist):
             "config": dict(_config(a), parallelism=f"replicas x{dist.world}" if dist.world > 1 else "1 GPU"),
             "rtf": (kms_max * 1e-3) / (K * ksim),
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak, "traffic": traffic,
                          "peak_source": "measured live: DFMA throughput kernel (lfdm_measure_fp64_peak), "
                                         "x2 flop/FMA; MEASURED_PEAKS.json has no FP64 figure",
                          "algorithmic": f"{W_ALG_18} FP64 ops per vehicle-step (reference op count) x "
                                         f"{n * steps_per_window} vehicle-steps per launch"},
             "roofline_hbm": {"bound": "hbm", "achieved": alg_bytes / (launch_ms * 1e-3) / 1e9, "peak": hbm_peak,
                              "unit": "GB/s", "frac": alg_bytes / (launch_ms * 1e-3) / 1e9 / hbm_peak,
-                             "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+                             "traffic": traffic, "algorithmic_bytes": alg_bytes,
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "mixed": mixed,
