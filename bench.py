@@ -197,30 +197,50 @@ def _config(a, n_override=None):
 
 def _mixed_error(lfdm, fleet, dev, n, horizon):
     """End-of-horizon error of the mixed form against the FP64 form: the seeded fleet with initial
-    speeds U[0.5, 30] m/s (near-standstill starts stress the low-speed slip path)."""
+    speeds U[0.5, 30] m/s (near-standstill starts stress the low-speed slip path). Also the FP64
+    form's own sensitivity: the same FP64 run from initial speeds u (1 + eps) for eps = 1e-15 (FP64
+    rounding level) and 1e-7 (FP32 rounding level). Vehicles the 1e-15 run moves by more than 1 cm are
+    rounding-chaotic (no FP64 implementation with other rounding holds them to 1 cm either); those
+    the 1e-7 run moves that far are beyond what any FP32-based arithmetic can hold. The mixed error
+    is also reported over the vehicles each run leaves within 1 cm."""
     f = fleet.fleet18(n, seed=SEED + 7, horizon=horizon, u0_range=(0.5, 30.0))
+    S = lfdm.S
     out = {}
-    for prec in (0, 1):
+    for key, prec, eps in (("fp64", 0, 0.0), ("mixed", 1, 0.0), ("fp64_1e-15", 0, 1e-15), ("fp64_1e-7", 0, 1e-7)):
         s = lfdm.d18SolverHalfImplicitGPU(n, device=dev)
         s.construct_class(f["cls"][0], f["params"])
         s.set_driver_tables(f["tables"])
-        s.set_states(f["states"])
+        st0 = np.array(f["states"], copy=True)
+        st0[:, S["u"]] *= 1.0 + eps
+        s.set_states(st0)
         s.SetKernelSimTime(1.0)
         s.SetEndTime(horizon)
         s.set_precision(prec)
         s.Solve()
-        out[prec] = s.get_states()
+        out[key] = s.get_states()
         s.close()
-    S = lfdm.S
-    a, b = out[0], out[1]
-    pos = np.hypot(b[:, S["x"]] - a[:, S["x"]], b[:, S["y"]] - a[:, S["y"]])
+    a, b = out["fp64"], out["mixed"]
+
+    def dpos(x, y):
+        return np.hypot(y[:, S["x"]] - x[:, S["x"]], y[:, S["y"]] - x[:, S["y"]])
+
+    pos = dpos(a, b)
     yaw = np.abs(b[:, S["psi"]] - a[:, S["psi"]])
     spd = np.abs(np.hypot(b[:, S["u"]], b[:, S["v"]]) - np.hypot(a[:, S["u"]], a[:, S["v"]]))
 
     def st(e):
         return {"max": float(e.max()), "p99": float(np.quantile(e, 0.99)), "p50": float(np.median(e))}
 
+    sens = {}
+    for eps in ("1e-15", "1e-7"):
+        d = dpos(a, out["fp64_" + eps])
+        stable = d <= 0.01
+        sens["u0_x(1+" + eps + ")"] = {
+            "position_m": st(d), "frac_within_1cm": float(stable.mean()),
+            "mixed_frac_within_1cm_on_these_stable": float((pos[stable] <= 0.01).mean()) if stable.any() else None}
+
     return {"vehicles": n, "horizon_s": horizon, "u0_range": [0.5, 30.0], "position_m": st(pos), "yaw_rad": st(yaw),
+            "fp64_sensitivity": sens,
             "speed_mps": st(spd), "frac_position_within_1cm": float((pos <= 0.01).mean())}
 
 
