@@ -572,23 +572,23 @@ static void rhs(Veh* v, Tire* t, const Par* pp, const double* controls, int nr) 
     vehRHS(v, pp, fx, fy);
 }
 
-/* PerturbRhsFun (18dof/dof18_halfImplicit.cpp:679-745) with unpackY / packYDOT (:954-1101): the
-   right-hand side at the packed states y, TMeasy tires. */
-int oracle18_rhs(const lfdm_class18* cls, const double* params, const double* full_state, const double* y,
-                 const double* ctl, double* ydot) {
-    Par pp_ = {params, cls};
-    const Par* pp = &pp_;
+/* PerturbRhsFun (18dof/dof18_halfImplicit.cpp:679-745) with unpackY / packYDOT (:879-1101): the
+   right-hand side at the packed states y, unpacked into a fresh state (all fields 0, first gear) or
+   into full_state. TMeasyNr tires carry no deflection states. */
+static int perturb18(const Par* pp, const double* full_state, const double* y, const double* ctl, double* ydot,
+                     int nr) {
     Veh v;
     Tire t[4];
     memset(&v, 0, sizeof v);
     memset(t, 0, sizeof t);
     if (full_state) load_state(full_state, &v, t);
-    const int tc = cls->tcbool != 0;
+    const int tc = pp->c->tcbool != 0;
     int i = 0;
-    for (int k = 0; k < 4; ++k) {
-        t[k].xe = y[i++];
-        t[k].ye = y[i++];
-    }
+    if (!nr)
+        for (int k = 0; k < 4; ++k) {
+            t[k].xe = y[i++];
+            t[k].ye = y[i++];
+        }
     for (int k = 0; k < 4; ++k) t[k].omega = y[i++];
     if (tc) v.crankOmega = y[i++];
     v.x = y[i++];
@@ -600,12 +600,13 @@ int oracle18_rhs(const lfdm_class18* cls, const double* params, const double* fu
     v.phi = y[i++];
     v.wx = y[i++];
     const double controls[4] = {0.0, ctl[0], ctl[1], ctl[2]};
-    rhs(&v, t, pp, controls, 0);
+    rhs(&v, t, pp, controls, nr);
     i = 0;
-    for (int k = 0; k < 4; ++k) {
-        ydot[i++] = t[k].xedot;
-        ydot[i++] = t[k].yedot;
-    }
+    if (!nr)
+        for (int k = 0; k < 4; ++k) {
+            ydot[i++] = t[k].xedot;
+            ydot[i++] = t[k].yedot;
+        }
     for (int k = 0; k < 4; ++k) ydot[i++] = t[k].dOmega;
     if (tc) ydot[i++] = v.dOmega_crank;
     ydot[i++] = (v.u * cos(v.psi) - v.v * sin(v.psi)); /* computeVehRHS, 18dof/dof18.cpp:1075-1077 */
@@ -617,6 +618,12 @@ int oracle18_rhs(const lfdm_class18* cls, const double* params, const double* fu
     ydot[i++] = v.wx;
     ydot[i++] = v.wxdot;
     return i;
+}
+
+int oracle18_rhs(const lfdm_class18* cls, const double* params, const double* full_state, const double* y,
+                 const double* ctl, double* ydot) {
+    Par pp = {params, cls};
+    return perturb18(&pp, full_state, y, ctl, ydot, 0);
 }
 
 /* half-implicit update: dof18_halfImplicit_gpu.cu:913-946 */
@@ -1535,3 +1542,212 @@ static int run_all(const oracle18_args* a, vehicle_fn fn) {
 int oracle18_run(const oracle18_args* a) { return run_all(a, run_vehicle); }
 int oracle11_run(const oracle18_args* a) { return run_all(a, run_vehicle11); }
 int oracle24_run(const oracle18_args* a) { return run_all(a, run_vehicle24); }
+
+/* ---------------------------------------------------------------------------------------------- */
+/* PerturbRhsFun of the 11- and 24-DOF solvers and IntegrateStepWithJacobian's central differences  */
+
+/* 11dof/dof11_halfImplicit.cpp:606-667 with packY / packYDOT / unpackY (:769-929) */
+static int perturb11(const Par* pp, const double* full_state, const double* y, const double* ctl, double* ydot,
+                     int nr) {
+    Veh11 v;
+    Tire t[2];
+    memset(&v, 0, sizeof v);
+    memset(t, 0, sizeof t);
+    if (full_state) load_state11(full_state, &v, t);
+    const int tc = pp->c->tcbool != 0;
+    int i = 0;
+    if (!nr)
+        for (int k = 0; k < 2; ++k) {
+            t[k].xe = y[i++];
+            t[k].ye = y[i++];
+        }
+    for (int k = 0; k < 2; ++k) t[k].omega = y[i++];
+    if (tc) v.crankOmega = y[i++];
+    v.x = y[i++];
+    v.y = y[i++];
+    v.u = y[i++];
+    v.v = y[i++];
+    v.psi = y[i++];
+    v.wz = y[i++];
+    const double controls[4] = {0.0, ctl[0], ctl[1], ctl[2]};
+    rhs11(&v, t, pp, controls, nr);
+    i = 0;
+    if (!nr)
+        for (int k = 0; k < 2; ++k) {
+            ydot[i++] = t[k].xedot;
+            ydot[i++] = t[k].yedot;
+        }
+    for (int k = 0; k < 2; ++k) ydot[i++] = t[k].dOmega;
+    if (tc) ydot[i++] = v.dOmega_crank;
+    ydot[i++] = v.u * cos(v.psi) - v.v * sin(v.psi); /* computeVehRHS, 11dof/dof11.cpp:904-905 */
+    ydot[i++] = v.u * sin(v.psi) + v.v * cos(v.psi);
+    ydot[i++] = v.udot;
+    ydot[i++] = v.vdot;
+    ydot[i++] = v.wz;
+    ydot[i++] = v.wzdot;
+    return i;
+}
+
+/* 24dof/dof24_halfImplicit.cpp:787-880 with packY / packYDOT / unpackY (:1015-1386). The reference's
+   TMeasyNr branch of PerturbRhsFun evaluates default-constructed states without unpacking y (its
+   state Jacobian is identically zero); here both branches unpack y. */
+static int perturb24(const Par* pp, const double* full_state, const double* y, const double* ctl, double* ydot,
+                     int nr) {
+    Veh24 v;
+    Tire24 t[4];
+    Sus24 su[4];
+    memset(&v, 0, sizeof v);
+    memset(t, 0, sizeof t);
+    memset(su, 0, sizeof su);
+    if (full_state) load_state24(full_state, &v, t, su);
+    const int tc = pp->c->tcbool != 0;
+    int i = 0;
+    for (int c = 0; c < 4; ++c) {
+        if (!nr) {
+            t[c].xe = y[i++];
+            t[c].ye = y[i++];
+        }
+        t[c].xt = y[i++];
+    }
+    for (int c = 0; c < 4; ++c) t[c].omega = y[i++];
+    for (int c = 0; c < 4; ++c) {
+        su[c].wu = y[i++];
+        su[c].xs = y[i++];
+    }
+    if (tc) v.crankOmega = y[i++];
+    v.x = y[i++];
+    v.y = y[i++];
+    v.u = y[i++];
+    v.v = y[i++];
+    v.w = y[i++];
+    v.wz = y[i++];
+    v.wx = y[i++];
+    v.wy = y[i++];
+    v.psi = y[i++];
+    v.phi = y[i++];
+    v.theta = y[i++];
+    const double controls[4] = {0.0, ctl[0], ctl[1], ctl[2]};
+    rhs24(&v, t, su, pp, controls, nr);
+    i = 0;
+    for (int c = 0; c < 4; ++c) {
+        if (!nr) {
+            ydot[i++] = t[c].xedot;
+            ydot[i++] = t[c].yedot;
+        }
+        ydot[i++] = t[c].dxt;
+    }
+    for (int c = 0; c < 4; ++c) ydot[i++] = t[c].dOmega;
+    for (int c = 0; c < 4; ++c) {
+        ydot[i++] = su[c].dwu;
+        ydot[i++] = su[c].dxs;
+    }
+    if (tc) ydot[i++] = v.dOmega_crank;
+    ydot[i++] = (v.u * cos(v.psi) - v.v * sin(v.psi)); /* computeVehicleRHS, 24dof/dof24.cpp:1729-1731 */
+    ydot[i++] = (v.u * sin(v.psi) + v.v * cos(v.psi));
+    ydot[i++] = v.udot;
+    ydot[i++] = v.vdot;
+    ydot[i++] = v.wdot;
+    ydot[i++] = v.wzdot;
+    ydot[i++] = v.wxdot;
+    ydot[i++] = v.wydot;
+    ydot[i++] = v.dpsi;
+    ydot[i++] = v.dphi;
+    ydot[i++] = v.dtheta;
+    return i;
+}
+
+/* packY of a flat state (the same field order as the unpacking above) */
+static int pack_state(int model, int nr, int tc, const double* s, double* y) {
+    int i = 0;
+    if (model == LFDM_MODEL_18) {
+        Veh v;
+        Tire t[4];
+        load_state(s, &v, t);
+        if (!nr)
+            for (int k = 0; k < 4; ++k) {
+                y[i++] = t[k].xe;
+                y[i++] = t[k].ye;
+            }
+        for (int k = 0; k < 4; ++k) y[i++] = t[k].omega;
+        if (tc) y[i++] = v.crankOmega;
+        const double r[8] = {v.x, v.y, v.u, v.v, v.psi, v.wz, v.phi, v.wx};
+        for (int k = 0; k < 8; ++k) y[i++] = r[k];
+    } else if (model == LFDM_MODEL_11) {
+        Veh11 v;
+        Tire t[2];
+        load_state11(s, &v, t);
+        if (!nr)
+            for (int k = 0; k < 2; ++k) {
+                y[i++] = t[k].xe;
+                y[i++] = t[k].ye;
+            }
+        for (int k = 0; k < 2; ++k) y[i++] = t[k].omega;
+        if (tc) y[i++] = v.crankOmega;
+        const double r[6] = {v.x, v.y, v.u, v.v, v.psi, v.wz};
+        for (int k = 0; k < 6; ++k) y[i++] = r[k];
+    } else {
+        Veh24 v;
+        Tire24 t[4];
+        Sus24 su[4];
+        load_state24(s, &v, t, su);
+        for (int c = 0; c < 4; ++c) {
+            if (!nr) {
+                y[i++] = t[c].xe;
+                y[i++] = t[c].ye;
+            }
+            y[i++] = t[c].xt;
+        }
+        for (int c = 0; c < 4; ++c) y[i++] = t[c].omega;
+        for (int c = 0; c < 4; ++c) {
+            y[i++] = su[c].wu;
+            y[i++] = su[c].xs;
+        }
+        if (tc) y[i++] = v.crankOmega;
+        const double r[11] = {v.x, v.y, v.u, v.v, v.w, v.wz, v.wx, v.wy, v.psi, v.phi, v.theta};
+        for (int k = 0; k < 11; ++k) y[i++] = r[k];
+    }
+    return i;
+}
+
+int oracle_rhs(int model, int tire_type, const lfdm_class18* cls, const double* params, const double* full_state,
+               const double* y, const double* ctl, double* ydot) {
+    Par pp = {params, cls};
+    const int nr = tire_type == LFDM_TIRE_TMEASY_NR;
+    if (model == LFDM_MODEL_18) return perturb18(&pp, full_state, y, ctl, ydot, nr);
+    if (model == LFDM_MODEL_11) return perturb11(&pp, full_state, y, ctl, ydot, nr);
+    if (model == LFDM_MODEL_24) return perturb24(&pp, full_state, y, ctl, ydot, nr);
+    return -1;
+}
+
+/* IntegrateStepWithJacobian's Jacobian block (18dof/dof18_halfImplicit.cpp:356-449; the 11- and
+   24-DOF solvers repeat it, 11dof/dof11_halfImplicit.cpp:335-429, 24dof/dof24_halfImplicit.cpp:402-494):
+   each packed state perturbed by +-|1e-3 y_i| (1e-3 where that is below 1e-8), steering and throttle
+   by +-1e-3 with braking 0. */
+int oracle_jacobian_fd(int model, int tire_type, const lfdm_class18* cls, const double* params, const double* state,
+                       const double* ctl, int full_point, double* jac_state, double* jac_ctl) {
+    enum { MAXY = 40 };
+    const int nr = tire_type == LFDM_TIRE_TMEASY_NR;
+    double y[MAXY], yp[MAXY], ym[MAXY], dp[MAXY], dm[MAXY];
+    const int ny = pack_state(model, nr, cls->tcbool != 0, state, y);
+    const double* full = full_point ? state : NULL;
+    for (int i = 0; i < ny; ++i) {
+        double del = fabs(y[i] * 1e-3);
+        if (del < 1e-8) del = 1e-3;
+        memcpy(yp, y, sizeof(double) * ny);
+        memcpy(ym, y, sizeof(double) * ny);
+        yp[i] = yp[i] + del;
+        ym[i] = ym[i] - del;
+        if (oracle_rhs(model, tire_type, cls, params, full, yp, ctl, dp) != ny) return -1;
+        if (oracle_rhs(model, tire_type, cls, params, full, ym, ctl, dm) != ny) return -1;
+        for (int j = 0; j < ny; ++j) jac_state[j * ny + i] = (dp[j] - dm[j]) / (2 * del);
+    }
+    for (int i = 0; i < 2; ++i) {
+        double cp[3] = {ctl[0], ctl[1], 0.0}, cm[3] = {ctl[0], ctl[1], 0.0};
+        cp[i] = cp[i] + 1e-3;
+        cm[i] = cm[i] - 1e-3;
+        if (oracle_rhs(model, tire_type, cls, params, full, y, cp, dp) != ny) return -1;
+        if (oracle_rhs(model, tire_type, cls, params, full, y, cm, dm) != ny) return -1;
+        for (int j = 0; j < ny; ++j) jac_ctl[j * 2 + i] = (dp[j] - dm[j]) / (2 * 1e-3);
+    }
+    return ny;
+}

@@ -60,6 +60,19 @@ void oracle24_init_state(const double* params, double* state);
 int oracle18_rhs(const lfdm_class18* cls, const double* params, const double* full_state, const double* y,
                  const double* ctl, double* ydot);
 
+/* PerturbRhsFun of the model (LFDM_MODEL_11/18/24) and tire type: the right-hand side at packed
+   states y (the reference's packY order; TMeasyNr tires have no deflection states) into ydot
+   (packYDOT order), with the other fields from full_state or a fresh state. Returns the count. */
+int oracle_rhs(int model, int tire_type, const lfdm_class18* cls, const double* params, const double* full_state,
+               const double* y, const double* ctl, double* ydot);
+
+/* IntegrateStepWithJacobian's central-difference Jacobians at the flat state `state`:
+   jac_state [ny][ny] (d ydot_j / d y_i at [j][i]) and jac_ctl [ny][2] (steering, throttle), each
+   right-hand side evaluated at a fresh state (full_point 0, as the reference) or on top of `state`
+   (full_point 1). Returns ny, or -1. */
+int oracle_jacobian_fd(int model, int tire_type, const lfdm_class18* cls, const double* params, const double* state,
+                       const double* ctl, int full_point, double* jac_state, double* jac_ctl);
+
 /* tireInit (18dof-gpu/dof18_gpu.cu:227-241) on one flat parameter vector. */
 void oracle_tire_init(double* params);
 

@@ -17,9 +17,10 @@
 // Job format (stdin, whitespace separated, several jobs per stream):
 //   veh <json> | tire <json> | tiretype 0|1 | driver <txt> | dt <v> | tend <v> | ksim <v>
 //   vp <field> <v> | tp <field> <v> | vs <field> <v> | ts <tire 0..3> <field> <v>
-//   gear <initial gear> | sample <every n steps> | run
+//   gear <initial gear> | sample <every n steps> | jac 0|1 | run
 // Output per job: "S step t x y u v phi psi wx wz wlf wrf wlr wrr" rows, then one "F ..." row
-// with the full packed state (75 doubles, TMeasy) and "E" on its own line.
+// with the full packed state (75 doubles, TMeasy) and "E" on its own line; with jac 1, the
+// reference's Jacobians at that final state (print_jacobian) come before "E".
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -43,6 +44,7 @@ struct Job {
     std::vector<std::pair<std::string, double>> vp, tp, vs;
     std::vector<std::pair<std::pair<int, std::string>, double>> ts;
     int gear = -1;
+    int jac = 0;
 };
 
 double* vparam_field(VehicleParam& p, const std::string& k) {
@@ -134,6 +136,21 @@ void print_tm(const TMeasyNrState& s) {
                 s._engTor);
 }
 
+// The reference's own finite-difference Jacobians (IntegrateStepWithJacobian) at the current state
+// with the driver's controls at time t: "C steering throttle braking", then "JS" with the state
+// Jacobian row-major (GetJacobianState) and "JC" with the control Jacobian (GetJacobianControls).
+template <typename Solver>
+void print_jacobian(Solver& solver, const DriverData& drv, double t) {
+    DriverInput c = GetDriverInput(t, drv);
+    solver.IntegrateStepWithJacobian(t, c.m_throttle, c.m_steering, c.m_braking, true);
+    std::printf("\nC %.17g %.17g %.17g\nJS", c.m_steering, c.m_throttle, c.m_braking);
+    for (const auto& row : solver.GetJacobianState())
+        for (double x : row) std::printf(" %.17g", x);
+    std::printf("\nJC");
+    for (const auto& row : solver.GetJacobianControls())
+        for (double x : row) std::printf(" %.17g", x);
+}
+
 template <typename TS>
 void run_job(const Job& job, d18SolverHalfImplicit& solver, TS* const tires[4]) {
     VehicleState& v = solver.m_veh_state;
@@ -147,9 +164,11 @@ void run_job(const Job& job, d18SolverHalfImplicit& solver, TS* const tires[4]) 
                     v._x, v._y, v._u, v._v, v._phi, v._psi, v._wx, v._wz, tires[0]->_omega, tires[1]->_omega,
                     tires[2]->_omega, tires[3]->_omega);
     };
+    double t_last = 0;
     auto one = [&](double t) {
         DriverInput c = GetDriverInput(t, drv);
         double tn = solver.IntegrateStep(t, c.m_throttle, c.m_steering, c.m_braking);
+        t_last = tn;
         ++step;
         if (job.sample > 0 && step % job.sample == 0)
             sample(tn);
@@ -174,6 +193,7 @@ void run_job(const Job& job, d18SolverHalfImplicit& solver, TS* const tires[4]) 
                 v._dOmega_crank, v._current_gr);
     for (int i = 0; i < 4; ++i)
         print_tm(*tires[i]);
+    if (job.jac) print_jacobian(solver, drv, t_last);
     std::printf("\nE\n");
     std::fflush(stdout);
 }
@@ -232,6 +252,7 @@ int main() {
         else if (key == "ksim") std::cin >> job.ksim;
         else if (key == "sample") std::cin >> job.sample;
         else if (key == "gear") std::cin >> job.gear;
+        else if (key == "jac") std::cin >> job.jac;
         else if (key == "vp" || key == "tp" || key == "vs") {
             std::string f;
             double v;

@@ -15,11 +15,12 @@
 // Job format (stdin, whitespace separated, several jobs per stream):
 //   veh <json> | tire <json> | sus <json> | tiretype 0|1 | driver <txt> | dt <v> | tend <v> | ksim <v>
 //   vp <field> <v> | tp <field> <v> | sp <field> <v> | vs <field> <v> | ts <tire 0..3> <field> <v>
-//   gear <initial gear> | sample <every n steps> | run
+//   gear <initial gear> | sample <every n steps> | jac 0|1 | run
 // Parameters are set before Initialize, which applies initializeTireSus (dof24.cpp:34-88).
 // Output per job: "S step t x y u v phi psi theta wx wz wy wlf wrf wlr wrr" rows, one "F ..." row
 // with the state in the GPU struct layout (212 doubles: VehicleState without the CPU-only dx, dy,
-// tor; 4 x TMeasyState; 4 x SuspensionState) and "E" on its own line.
+// tor; 4 x TMeasyState; 4 x SuspensionState) and "E" on its own line; with jac 1, the
+// reference's Jacobians at that final state (print_jacobian) come before "E".
 #include <cstddef>
 #include <cstdio>
 #include <cstdlib>
@@ -43,6 +44,7 @@ struct Job {
     std::vector<std::pair<std::string, double>> vp, tp, sp, vs;
     std::vector<std::pair<std::pair<int, std::string>, double>> ts;
     int gear = -1;
+    int jac = 0;
 };
 
 template <typename T>
@@ -151,6 +153,21 @@ void run(const Job& job) {
     }
 }
 
+// The reference's own finite-difference Jacobians (IntegrateStepWithJacobian) at the current state
+// with the driver's controls at time t: "C steering throttle braking", then "JS" with the state
+// Jacobian row-major (GetJacobianState) and "JC" with the control Jacobian (GetJacobianControls).
+template <typename Solver>
+void print_jacobian(Solver& solver, const DriverData& drv, double t) {
+    DriverInput c = GetDriverInput(t, drv);
+    solver.IntegrateStepWithJacobian(t, c.m_throttle, c.m_steering, c.m_braking, true);
+    std::printf("\nC %.17g %.17g %.17g\nJS", c.m_steering, c.m_throttle, c.m_braking);
+    for (const auto& row : solver.GetJacobianState())
+        for (double x : row) std::printf(" %.17g", x);
+    std::printf("\nJC");
+    for (const auto& row : solver.GetJacobianControls())
+        for (double x : row) std::printf(" %.17g", x);
+}
+
 template <typename TS>
 void run_job(const Job& job, d24SolverHalfImplicit& solver, TS* const tires[4]) {
     VehicleState& v = solver.m_veh_state;
@@ -161,9 +178,11 @@ void run_job(const Job& job, d24SolverHalfImplicit& solver, TS* const tires[4]) 
     const double dt = job.dt;
     const double tend = job.tend > 0 ? job.tend : drv.back().m_time;
     long step = 0;
+    double t_last = 0;
     auto one = [&](double t) {
         DriverInput c = GetDriverInput(t, drv);
         double tn = solver.IntegrateStep(t, c.m_throttle, c.m_steering, c.m_braking);
+        t_last = tn;
         ++step;
         if (job.sample > 0 && step % job.sample == 0)
             std::printf("S %ld %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g\n",
@@ -187,6 +206,7 @@ void run_job(const Job& job, d24SolverHalfImplicit& solver, TS* const tires[4]) 
     print_veh(v);
     for (int i = 0; i < 4; ++i) print_tire(*tires[i]);
     for (int i = 0; i < 4; ++i) print_sus(*sus[i]);
+    if (job.jac) print_jacobian(solver, drv, t_last);
     std::printf("\nE\n");
     std::fflush(stdout);
 }
@@ -207,6 +227,7 @@ int main() {
         else if (key == "ksim") std::cin >> job.ksim;
         else if (key == "sample") std::cin >> job.sample;
         else if (key == "gear") std::cin >> job.gear;
+        else if (key == "jac") std::cin >> job.jac;
         else if (key == "vp" || key == "tp" || key == "sp" || key == "vs") {
             std::string f;
             double v;

@@ -32,28 +32,48 @@ abi = import_module("low-fidelity-dynamic-models_gb300._abi")
 
 REFRUN = os.path.join(ROOT, "oracle", "_ref", "refrun18")
 SEED = 20261203
+# cases that also record the reference's IntegrateStepWithJacobian output at their final state (the
+# first two vehicles of each synthetic fleet as well)
+JAC_CASES = {"hmmwv_dl4_gpu", "sedan_nr_acc05_gpu", "hmmwv11_dl4_gpu", "sedan11_nr_acc05_gpu", "hmmwv24_dl4_gpu22",
+             "sedan24_nr_acc05_gpu"}
 
 
 def _fmt(x: float) -> str:
     return repr(float(x))
 
 
-def run_ref(job_lines: list[str]) -> list[dict]:
-    out = subprocess.run([REFRUN], input="\n".join(job_lines) + "\n", capture_output=True, text=True, check=True)
+def parse_ref(stdout: str) -> list[dict]:
+    """Rows of refrun{11,18,24}: S (samples), F (final state), with jac 1 also C (the controls of
+    the Jacobian), JS and JC (the reference's state and control Jacobians, row-major); E ends a job."""
     results, cur = [], {"samples": []}
-    for line in out.stdout.splitlines():
+    for line in stdout.splitlines():
         tok = line.split()
         if not tok:
             continue
         if tok[0] == "S":
             cur["samples"].append([int(tok[1])] + [float(v) for v in tok[2:]])
         elif tok[0] == "F":
-            vals = [float(v) for v in tok[1:]]
-            cur["final"] = vals
+            cur["final"] = [float(v) for v in tok[1:]]
+        elif tok[0] in ("C", "JS", "JC"):
+            cur[tok[0]] = [float(v) for v in tok[1:]]
         elif tok[0] == "E":
             results.append(cur)
             cur = {"samples": []}
     return results
+
+
+def run_ref(job_lines: list[str]) -> list[dict]:
+    out = subprocess.run([REFRUN], input="\n".join(job_lines) + "\n", capture_output=True, text=True, check=True)
+    return parse_ref(out.stdout)
+
+
+def add_jacobian(case: dict, r: dict) -> None:
+    """The reference's IntegrateStepWithJacobian output at the case's final state, if requested."""
+    if "JS" not in r:
+        return
+    ny = int(round(len(r["JS"]) ** 0.5))
+    assert ny * ny == len(r["JS"]) and len(r["JC"]) == 2 * ny
+    case["jacobian"] = {"controls": r["C"], "state": r["JS"], "ny": ny, "control": r["JC"]}
 
 
 def final_to_state(final: list[float]) -> list[float]:
@@ -96,7 +116,7 @@ def main(ref: str) -> None:
             tp = write_table(f"{name}.txt", rows)
             tend_v = tend if tend is not None else rows[-1][0]
             jobs += [f"veh {vj}", f"tire {tj}", "tiretype 0", f"driver {tp}", "dt 0.001", f"tend {_fmt(tend_v)}",
-                     f"ksim {_fmt(ksim)}", f"sample {sample}", "run"]
+                     f"ksim {_fmt(ksim)}", f"sample {sample}", f"jac {int(name in JAC_CASES)}", "run"]
             meta.append({"name": name, "vehicle": veh_hmmwv, "tire": tire_hmmwv, "tire_type": 0, "driver": rows,
                          "dt": 0.001, "tend": tend_v, "ksim": ksim, "sample": sample, "vp": {}, "tp": {},
                          "state": [0.0] * abi.S_COUNT, "source": f"HMMWV vehicle.json + tmeasy.json, {drv}.txt"})
@@ -110,7 +130,7 @@ def main(ref: str) -> None:
             tp = write_table(f"{name}.txt", rows)
             tend_v = tend if tend is not None else rows[-1][0]
             jobs += [f"veh {vsj}", f"tire {tsj}", "tiretype 1", f"driver {tp}", "dt 0.001", f"tend {_fmt(tend_v)}",
-                     f"ksim {_fmt(ksim)}", "sample 100", "run"]
+                     f"ksim {_fmt(ksim)}", "sample 100", f"jac {int(name in JAC_CASES)}", "run"]
             meta.append({"name": name, "vehicle": veh_sedan, "tire": tire_sedan, "tire_type": 1, "driver": rows,
                          "dt": 0.001, "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
                          "state": [0.0] * abi.S_COUNT, "source": "Sedan vehicle.json + tmeasyNr.json, acc05.txt"})
@@ -138,7 +158,7 @@ def main(ref: str) -> None:
                      "ksim 1", "sample 250"]
             lines += [f"vp {k} {_fmt(v)}" for k, v in vp.items()] + [f"tp {k} {_fmt(v)}" for k, v in tpv.items()]
             lines += [f"vs u {_fmt(u0)}", f"vs crankOmega {_fmt(crank)}", f"gear {gear}"]
-            lines += [f"ts {k} omega {_fmt(w0)}" for k in range(4)] + ["run"]
+            lines += [f"ts {k} omega {_fmt(w0)}" for k in range(4)] + [f"jac {int(i < 2)}", "run"]
             jobs += lines
             meta.append({"name": f"suv_fleet_{i}", "vehicle": fleet.SUV18_VEHICLE, "tire": fleet.SUV_TIRE,
                          "tire_type": 0, "driver": rows, "dt": 0.001, "tend": 10.0, "ksim": 1.0, "sample": 250,
@@ -149,6 +169,7 @@ def main(ref: str) -> None:
     for m, r in zip(meta, results):
         m["expected_samples"] = r["samples"]
         m["expected_final"] = final_to_state(r["final"])
+        add_jacobian(m, r)
         cases.append(m)
     out = {"generator": "tests/golden/make_golden.py", "reference_solver": "d18SolverHalfImplicit (CPU), "
            "replayed step by step through IntegrateStep; ksim>0 uses the GPU solver's window schedule",
@@ -181,7 +202,7 @@ def main11(ref: str) -> None:
             tp = write(f"{name}.txt", "".join(" ".join(_fmt(v) for v in r) + "\n" for r in rows))
             tend_v = tend if tend is not None else rows[-1][0]
             jobs += [f"veh {vj}", f"tire {tj}", "tiretype 0", f"driver {tp}", "dt 0.001", f"tend {_fmt(tend_v)}",
-                     f"ksim {_fmt(ksim)}", "sample 100", "run"]
+                     f"ksim {_fmt(ksim)}", "sample 100", f"jac {int(name in JAC_CASES)}", "run"]
             cases.append({"name": name, "vehicle": veh, "tire": tire, "tire_type": 0, "driver": rows, "dt": 0.001,
                           "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
                           "state": [0.0] * abi.C["LFDM11_S_COUNT"], "source": f"HMMWV 11-DOF json, {drv}.txt"})
@@ -194,7 +215,7 @@ def main11(ref: str) -> None:
             tp = write(f"{name}.txt", "".join(" ".join(_fmt(v) for v in r) + "\n" for r in rows))
             tend_v = tend if tend is not None else rows[-1][0]
             jobs += [f"veh {vsj}", f"tire {tsj}", "tiretype 1", f"driver {tp}", "dt 0.001", f"tend {_fmt(tend_v)}",
-                     f"ksim {_fmt(ksim)}", "sample 100", "run"]
+                     f"ksim {_fmt(ksim)}", "sample 100", f"jac {int(name in JAC_CASES)}", "run"]
             cases.append({"name": name, "vehicle": veh_s, "tire": tire_s, "tire_type": 1, "driver": rows, "dt": 0.001,
                           "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
                           "state": [0.0] * abi.C["LFDM11_S_COUNT"], "source": "Sedan 11-DOF json, tmeasyNr, acc05.txt"})
@@ -207,25 +228,18 @@ def main11(ref: str) -> None:
             w0 = float(st[abi.C["LFDM11_S_TIRE0"] + abi.T["omega"]])
             jobs += [f"veh {sj}", f"tire {stj}", "tiretype 0", f"driver {tp}", "dt 0.001", "tend 10", "ksim 1",
                      "sample 250", f"vs u {_fmt(st[S11['u']])}", f"vs crankOmega {_fmt(st[S11['crankomega']])}",
-                     f"gear {int(st[S11['current_gr']])}", f"ts 0 omega {_fmt(w0)}", f"ts 1 omega {_fmt(w0)}", "run"]
+                     f"gear {int(st[S11['current_gr']])}", f"ts 0 omega {_fmt(w0)}", f"ts 1 omega {_fmt(w0)}",
+                     f"jac {int(i < 2)}", "run"]
             cases.append({"name": f"suv11_{i}", "vehicle": fleet.SUV11_VEHICLE, "tire": fleet.SUV_TIRE, "tire_type": 0,
                           "driver": rows, "dt": 0.001, "tend": 10.0, "ksim": 1.0, "sample": 250, "vp": {}, "tp": {},
                           "state": st.tolist(), "source": f"synthetic 11-DOF SUV fleet seed {SEED} vehicle {i}"})
         out = subprocess.run([refrun], input="\n".join(jobs) + "\n", capture_output=True, text=True, check=True)
-    results, cur = [], {"samples": []}
-    for line in out.stdout.splitlines():
-        tok = line.split()
-        if tok and tok[0] == "S":
-            cur["samples"].append([int(tok[1])] + [float(v) for v in tok[2:]])
-        elif tok and tok[0] == "F":
-            cur["final"] = [float(v) for v in tok[1:]]
-        elif tok and tok[0] == "E":
-            results.append(cur)
-            cur = {"samples": []}
+    results = parse_ref(out.stdout)
     assert len(results) == len(cases)
     for c, r in zip(cases, results):
         c["expected_samples"] = r["samples"]
         c["expected_final"] = r["final"]
+        add_jacobian(c, r)
     with open(os.path.join(HERE, "golden11.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "model": 11, "cases": cases}, f, separators=(",", ":"))
     print(f"wrote {len(cases)} 11-DOF cases; {cases[0]['name']} x={cases[0]['expected_final'][0]!r}")
@@ -257,7 +271,7 @@ def main24(ref: str) -> None:
             tp = write(f"{name}.txt", "".join(" ".join(_fmt(v) for v in r) + "\n" for r in rows))
             tend_v = tend if tend is not None else rows[-1][0]
             jobs += [f"veh {vj}", f"tire {tj}", f"sus {sj}", f"driver {tp}", "dt 0.001", f"tend {_fmt(tend_v)}",
-                     f"ksim {_fmt(ksim)}", "sample 100", "run"]
+                     f"ksim {_fmt(ksim)}", "sample 100", f"jac {int(name in JAC_CASES)}", "run"]
             cases.append({"name": name, "vehicle": veh, "tire": tire, "sus": sus, "tire_type": 0, "driver": rows,
                           "dt": 0.001, "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
                           "state": s_h.tolist(), "source": f"HMMWV 24-DOF json, {drv}.txt"})
@@ -273,7 +287,7 @@ def main24(ref: str) -> None:
             tp = write(f"{name}.txt", "".join(" ".join(_fmt(v) for v in r) + "\n" for r in rows))
             tend_v = tend if tend is not None else rows[-1][0]
             jobs += [f"veh {vsj}", f"tire {tsj}", f"sus {sj}", "tiretype 1", f"driver {tp}", "dt 0.001",
-                     f"tend {_fmt(tend_v)}", f"ksim {_fmt(ksim)}", "sample 100", "run"]
+                     f"tend {_fmt(tend_v)}", f"ksim {_fmt(ksim)}", "sample 100", f"jac {int(name in JAC_CASES)}", "run"]
             cases.append({"name": name, "vehicle": veh_s, "tire": tire_s, "sus": sus, "tire_type": 1, "driver": rows,
                           "dt": 0.001, "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
                           "state": s_s.tolist(), "source": "Sedan 24-DOF json, tmeasyNr, HMMWV suspension, acc05.txt"})
@@ -295,27 +309,19 @@ def main24(ref: str) -> None:
             jobs += [f"vp {k} {_fmt(v)}" for k, v in vp.items()] + [f"tp {k} {_fmt(v)}" for k, v in tpv.items()]
             jobs += [f"vs u {_fmt(st[C['LFDM24_S_U']])}", f"vs crankOmega {_fmt(st[C['LFDM24_S_CRANKOMEGA']])}",
                      f"gear {int(st[C['LFDM24_S_CURRENT_GR']])}"] + [f"ts {k} omega {_fmt(w0)}" for k in range(4)]
-            jobs += ["run"]
+            jobs += [f"jac {int(i < 2)}", "run"]
             cases.append({"name": f"suv24_{i}", "vehicle": fleet.SUV24_VEHICLE, "tire": fleet.SUV_TIRE,
                           "sus": fleet.SUV24_SUS, "tire_type": 0, "driver": rows, "dt": 0.001, "tend": 10.0,
                           "ksim": 1.0, "sample": 250, "vp": vp, "tp": tpv, "state": st.tolist(),
                           "source": f"synthetic 24-DOF SUV fleet seed {SEED} vehicle {i}"})
         out = subprocess.run([refrun], input="\n".join(jobs) + "\n", capture_output=True, text=True, check=True)
-    results, cur = [], {"samples": []}
-    for line in out.stdout.splitlines():
-        tok = line.split()
-        if tok and tok[0] == "S":
-            cur["samples"].append([int(tok[1])] + [float(v) for v in tok[2:]])
-        elif tok and tok[0] == "F":
-            cur["final"] = [float(v) for v in tok[1:]]
-        elif tok and tok[0] == "E":
-            results.append(cur)
-            cur = {"samples": []}
+    results = parse_ref(out.stdout)
     assert len(results) == len(cases)
     for c, r in zip(cases, results):
         assert len(r["final"]) == C["LFDM24_S_COUNT"]
         c["expected_samples"] = r["samples"]
         c["expected_final"] = r["final"]
+        add_jacobian(c, r)
     with open(os.path.join(HERE, "golden24.json"), "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "model": 24, "cases": cases}, f, separators=(",", ":"))
     print(f"wrote {len(cases)} 24-DOF cases; {cases[0]['name']} x={cases[0]['expected_final'][0]!r}")

@@ -46,6 +46,11 @@ def lib(fma: bool = False):
         L.oracle_tire_init.argtypes = [ctypes.c_void_p]
         L.oracle18_rhs.argtypes = [ctypes.c_void_p] * 6
         L.oracle18_rhs.restype = ctypes.c_int
+        L.oracle_rhs.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 6
+        L.oracle_rhs.restype = ctypes.c_int
+        L.oracle_jacobian_fd.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 4 + [ctypes.c_int] + \
+            [ctypes.c_void_p] * 2
+        L.oracle_jacobian_fd.restype = ctypes.c_int
         _libs[path] = L
     return _libs[path]
 
@@ -160,3 +165,30 @@ def rhs18(cls, params, y, ctl, full_state=None) -> np.ndarray:
     n = lib().oracle18_rhs(ctypes.byref(cls), _ptr(p), None if fs is None else _ptr(fs), _ptr(y), _ptr(c), _ptr(out))
     assert n == len(y)
     return out
+
+
+def rhs(model, tire_type, cls, params, y, ctl, full_state=None) -> np.ndarray:
+    """PerturbRhsFun of the 11-, 18- or 24-DOF model (oracle_rhs) at packed states y."""
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    c = np.ascontiguousarray(ctl, dtype=np.float64)
+    fs = None if full_state is None else np.ascontiguousarray(full_state, dtype=np.float64)
+    out = np.zeros(len(y))
+    n = lib().oracle_rhs(model, tire_type, ctypes.byref(cls), _ptr(p), None if fs is None else _ptr(fs), _ptr(y),
+                         _ptr(c), _ptr(out))
+    assert n == len(y), (n, len(y))
+    return out
+
+
+def jacobian_fd(model, tire_type, cls, params, state, ctl, full_point=False):
+    """IntegrateStepWithJacobian's central differences (oracle_jacobian_fd) at a flat state:
+    (state Jacobian [ny][ny], control Jacobian [ny][2])."""
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    s = np.ascontiguousarray(state, dtype=np.float64)
+    c = np.ascontiguousarray(ctl, dtype=np.float64)
+    js, jc = np.zeros(40 * 40), np.zeros(40 * 2)
+    ny = lib().oracle_jacobian_fd(model, tire_type, ctypes.byref(cls), _ptr(p), _ptr(s), _ptr(c), int(full_point),
+                                  _ptr(js), _ptr(jc))
+    assert ny > 0
+    return js[:ny * ny].reshape(ny, ny), jc[:2 * ny].reshape(ny, 2)
+
