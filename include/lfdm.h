@@ -315,6 +315,20 @@ int lfdm_traj18_last_ms(lfdm_solver* h, double* forward_ms, double* backward_ms)
 int lfdm_rhs_jacobian18(lfdm_solver* h, const double* ctl, int reference_point, double* jac_state, double* jac_ctl,
                         int* ny);
 
+/* The reference's own Jacobian scheme for every model and tire type, batched over vehicles        */
+/* (replaces IntegrateStepWithJacobian's Jacobian block: 11dof/dof11_halfImplicit.cpp:335-429,     */
+/* 18dof/dof18_halfImplicit.cpp:356-449, 24dof/dof24_halfImplicit.cpp:402-494): every packed state   */
+/* perturbed by +-|1e-3 y_i| (1e-3 where that is below 1e-8), steering and throttle by +-1e-3 with   */
+/* braking 0, central differences of PerturbRhsFun. Same arguments and layout as                    */
+/* lfdm_rhs_jacobian18, in each model's packed order (packY/packYDOT): 11-DOF {xe, ye} x 2, omega  */
+/* x 2, crank, x, y, u, v, psi, wz (ny 13/12 TMeasy, 9/8 TMeasyNr); 18-DOF as above (ny 21/20,     */
+/* 13/12); 24-DOF {xe, ye, xt} x 4, omega x 4, {wu, xs} x 4, crank, x, y, u, v, w, wz, wx, wy, psi, */
+/* phi, theta (ny 36/35 TMeasy, 28/27 TMeasyNr with xt only). The crank speed is a state only with */
+/* a torque converter. The reference's 24-DOF TMeasyNr PerturbRhsFun does not unpack the perturbed  */
+/* states (its state Jacobian is zero); this one does.                                              */
+int lfdm_rhs_jacobian_fd(lfdm_solver* h, const double* ctl, int reference_point, double* jac_state, double* jac_ctl,
+                         int* ny);
+
 /* ------------------------------------------------------------------------------------------ */
 /* Mixed-DOF fleets (no counterpart class in the reference, whose solvers hold one model and one */
 /* end time each: d18SolverHalfImplicitGPU, d24SolverHalfImplicitGPU). A fleet holds 18-DOF and   */

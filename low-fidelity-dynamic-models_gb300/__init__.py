@@ -97,6 +97,7 @@ def _sig(lib):
         "lfdm_traj18_backward": ([vp, vp, vp, u, d, u, vp, vp, vp], i),
         "lfdm_traj18_last_ms": ([vp, _c_dp, _c_dp], i),
         "lfdm_rhs_jacobian18": ([vp, vp, i, vp, vp, ctypes.POINTER(i)], i),
+        "lfdm_rhs_jacobian_fd": ([vp, vp, i, vp, vp, ctypes.POINTER(i)], i),
         "lfdm_fleet_create": ([i, ctypes.POINTER(vp)], i),
         "lfdm_fleet_destroy": ([vp], i),
         "lfdm_fleet_last_error": ([vp], cp),
@@ -380,6 +381,33 @@ class _SolverGPU:
         return w
 
 
+    def _jacobian(self, fn, steering, throttle, braking, reference_point):
+        import torch
+        dev = torch.device("cuda", self.device)
+        n = self.n
+        ctl = torch.tensor(np.stack([np.broadcast_to(np.asarray(x, dtype=np.float64), (n,))
+                                     for x in (steering, throttle, braking)]), dtype=torch.float64, device=dev)
+        js = torch.empty(36 * 36 * n, dtype=torch.float64, device=dev)
+        ju = torch.empty(36 * 2 * n, dtype=torch.float64, device=dev)
+        ny = ctypes.c_int()
+        self._ck(fn(self._h, ctypes.c_void_p(ctl.data_ptr()), int(bool(reference_point)), ctypes.c_void_p(js.data_ptr()),
+                    ctypes.c_void_p(ju.data_ptr()), ctypes.byref(ny)))
+        m = ny.value
+        jac_state = js[: m * m * n].reshape(m, m, n).permute(2, 0, 1).cpu().numpy()
+        jac_ctl = ju[: m * 2 * n].reshape(m, 2, n).permute(2, 0, 1).cpu().numpy()
+        return jac_state, jac_ctl
+
+    def rhs_jacobian_fd(self, steering, throttle, braking=0.0, reference_point: bool = True):
+        """The reference's IntegrateStepWithJacobian Jacobians for every vehicle (lfdm_rhs_jacobian_fd):
+        central differences of the right-hand side with the reference's perturbations, any model and
+        tire type, at every vehicle's current state. Controls are scalars or arrays of N; braking enters
+        only the state Jacobian (the control differences use braking 0, as the reference does). Returns
+        (jac_state [N, ny, ny], jac_controls [N, ny, 2]) in the model's packed order (packY / packYDOT);
+        reference_point differentiates where PerturbRhsFun does (the packed states in a fresh state)
+        rather than on top of the full current state."""
+        return self._jacobian(self._L.lfdm_rhs_jacobian_fd, steering, throttle, braking, reference_point)
+
+
 class d18SolverHalfImplicitGPU(_SolverGPU):
     """18-DOF batched half-implicit stepper on one GPU (reference: 18dof-gpu/dof18_halfImplicit_gpu.cuh)."""
 
@@ -393,22 +421,9 @@ class d18SolverHalfImplicitGPU(_SolverGPU):
         18dof/dof18_halfImplicit.cpp:356-520). Controls are scalars or arrays of N. Returns
         (jac_state [N, ny, ny], jac_controls [N, ny, 2]) in the reference's packed order, ny = 21 with a
         torque converter and 20 without; reference_point selects the point the reference
-        differentiates at (previous accelerations 0, first gear) rather than the full current state."""
-        import torch
-        dev = torch.device("cuda", self.device)
-        n = self.n
-        ctl = torch.tensor(np.stack([np.broadcast_to(np.asarray(x, dtype=np.float64), (n,))
-                                     for x in (steering, throttle, braking)]), dtype=torch.float64, device=dev)
-        js = torch.empty(21 * 21 * n, dtype=torch.float64, device=dev)
-        ju = torch.empty(21 * 2 * n, dtype=torch.float64, device=dev)
-        ny = ctypes.c_int()
-        self._ck(self._L.lfdm_rhs_jacobian18(self._h, ctypes.c_void_p(ctl.data_ptr()), int(bool(reference_point)),
-                                             ctypes.c_void_p(js.data_ptr()), ctypes.c_void_p(ju.data_ptr()),
-                                             ctypes.byref(ny)))
-        m = ny.value
-        jac_state = js[: m * m * n].reshape(m, m, n).permute(2, 0, 1).cpu().numpy()
-        jac_ctl = ju[: m * 2 * n].reshape(m, 2, n).permute(2, 0, 1).cpu().numpy()
-        return jac_state, jac_ctl
+        differentiates at (previous accelerations 0, first gear) rather than the full current state.
+        TMeasy tires; rhs_jacobian_fd covers every tire by the reference's difference scheme."""
+        return self._jacobian(self._L.lfdm_rhs_jacobian18, steering, throttle, braking, reference_point)
 
 
 class d11SolverHalfImplicitGPU(_SolverGPU):

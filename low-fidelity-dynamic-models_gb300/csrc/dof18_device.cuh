@@ -720,12 +720,12 @@ __device__ __forceinline__ void powertrain_rhs(VehC& v, VehAux& va, TireC* ts, T
         ta[k].dOmega = ijw * (fma(-sgnd(ts[k].omega), brake, ta[k].engTor + ta[k].My) - ta[k].fx * ta[k].rStat);
 }
 
-// One right-hand-side evaluation (rhsFun, dof18_halfImplicit_gpu.cu:685-729) followed by the
-// half-implicit update (:913-946). steering/throttle/braking are this step's driver inputs.
+// One right-hand-side evaluation (rhsFun, dof18_halfImplicit_gpu.cu:685-729): tire loads, tire
+// forces and deflection rates, powertrain (wheel and crank accelerations, gear), chassis
+// accelerations. steering/throttle/braking are the driver inputs.
 template <bool kNr>
-__device__ __forceinline__ void step18(VehC& v, VehAux& va, TireC* ts, TireAux* ta, const KView& K,
-                                       const ClassDev18& C, double steering, double throttle, double braking,
-                                       double dt) {
+__device__ __forceinline__ void rhs18(VehC& v, VehAux& va, TireC* ts, TireAux* ta, const KView& K,
+                                      const ClassDev18& C, double steering, double throttle, double braking) {
     // computeTireLoads (dof18_gpu.cu:305-340); udot/vdot are the previous step's accelerations.
     {
         const double lat = fma(v.wz, v.u, v.vdot);
@@ -796,7 +796,12 @@ __device__ __forceinline__ void step18(VehC& v, VehAux& va, TireC* ts, TireAux* 
         va.wxdot = fma(K(K_CV3), E1, fma(K(K_CX2), E2, K(K_CX3) * E3));
         va.wzdot = fma(K(K_CV2), E1, fma(K(K_CZ2), E2, K(K_CX2) * E3));
     }
-    // half-implicit update (dof18_halfImplicit_gpu.cu:913-946)
+}
+
+// The half-implicit update (dof18_halfImplicit_gpu.cu:913-946) with the rates of rhs18.
+template <bool kNr>
+__device__ __forceinline__ void update18(VehC& v, const VehAux& va, TireC* ts, const TireAux* ta, const ClassDev18& C,
+                                         double dt) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         if (!kNr) {
@@ -816,6 +821,15 @@ __device__ __forceinline__ void step18(VehC& v, VehAux& va, TireC* ts, TireAux* 
     v.y = fma(fma(v.u, sp, v.v * cp), dt, v.y);
     v.psi = fma(v.wz, dt, v.psi);
     v.phi = fma(v.wx, dt, v.phi);
+}
+
+// One step: rhs18 followed by update18.
+template <bool kNr>
+__device__ __forceinline__ void step18(VehC& v, VehAux& va, TireC* ts, TireAux* ta, const KView& K,
+                                       const ClassDev18& C, double steering, double throttle, double braking,
+                                       double dt) {
+    rhs18<kNr>(v, va, ts, ta, K, C, steering, throttle, braking);
+    update18<kNr>(v, va, ts, ta, C, dt);
 }
 
 }  // namespace lfdm

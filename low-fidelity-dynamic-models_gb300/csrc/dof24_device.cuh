@@ -66,13 +66,20 @@ struct Corner24K {
         if (sink) S[(size_t)(field) * np] = (value); \
     } while (0)
 
-// One rhsFun + half-implicit update. sink: also write the step's non-carried values to S. The flag
-// is a run-time value on purpose: every step runs the same compiled arithmetic (a separate
-// instantiation for storing steps could fuse multiplies and adds differently and round differently).
+// Rates of one right-hand-side evaluation that are not held in the carried state, with the pitch
+// and roll sines and cosines the update reuses.
+struct Rhs24 {
+    double dxt[4], dwu[4], wdot, sth, cth, sph, cph;
+};
+
+// One right-hand-side evaluation (rhsFun, 24dof-gpu/dof24_halfImplicit_gpu.cu:728-775). sink: also
+// write the step's non-carried values to S. The flag is a run-time value on purpose: every step runs
+// the same compiled arithmetic (a separate instantiation for storing steps could fuse multiplies
+// and adds differently and round differently).
 template <bool kNr>
-__device__ __forceinline__ void step24(VehC& v, Veh24X& vx, VehAux& va, TireC* ts, TireAux* ta, Sus24C* su,
-                                       const Corner24K* ck, const KView& K, const ClassDev18& C, double steering,
-                                       double throttle, double braking, double dt, double* S, size_t np, bool sink) {
+__device__ __forceinline__ void rhs24(VehC& v, Veh24X& vx, VehAux& va, TireC* ts, TireAux* ta, Sus24C* su,
+                                      const Corner24K* ck, const KView& K, const ClassDev18& C, double steering,
+                                      double throttle, double braking, Rhs24& R, double* S, size_t np, bool sink) {
     const double cf2 = K(K24_CF2), cr2 = K(K24_CR2), a = K(K24_A), b = K(K24_B);
     double sth, cth, sph, cph;
     sincos(vx.theta, &sth, &cth);
@@ -245,7 +252,26 @@ __device__ __forceinline__ void step24(VehC& v, Veh24X& vx, VehAux& va, TireC* t
     vx.wzdot = K(K24_INVJZ) * fma(fys[0] + fys[1], a, fma(-(fys[2] + fys[3]), b,
                                                         fma(fxs[1] - fxs[0], cf2, (fxs[3] - fxs[2]) * cr2)));
     SINK(LFDM24_S_WDOT, wdot);
-    // half-implicit update (dof24_halfImplicit_gpu.cu:1016-1081)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        R.dxt[c] = dxt[c];
+        R.dwu[c] = dwu[c];
+    }
+    R.wdot = wdot;
+    R.sth = sth;
+    R.cth = cth;
+    R.sph = sph;
+    R.cph = cph;
+}
+
+// The half-implicit update (dof24_halfImplicit_gpu.cu:1016-1081) with the rates of rhs24.
+template <bool kNr>
+__device__ __forceinline__ void update24(VehC& v, Veh24X& vx, const VehAux& va, TireC* ts, TireAux* ta, Sus24C* su,
+                                         const ClassDev18& C, const Rhs24& R, double dt, double* S, size_t np,
+                                         bool sink) {
+    const double* dxt = R.dxt;
+    const double* dwu = R.dwu;
+    const double wdot = R.wdot, sth = R.sth, cth = R.cth, sph = R.sph, cph = R.cph;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
         if (!kNr) {  // the TMeasyNr tire has no deflection states
@@ -282,6 +308,16 @@ __device__ __forceinline__ void step24(VehC& v, Veh24X& vx, VehAux& va, TireC* t
     v.y = fma(fma(v.u, sp, v.v * cp), dt, v.y);
 }
 #undef SINK
+
+// One step: rhs24 followed by update24.
+template <bool kNr>
+__device__ __forceinline__ void step24(VehC& v, Veh24X& vx, VehAux& va, TireC* ts, TireAux* ta, Sus24C* su,
+                                       const Corner24K* ck, const KView& K, const ClassDev18& C, double steering,
+                                       double throttle, double braking, double dt, double* S, size_t np, bool sink) {
+    Rhs24 R;
+    rhs24<kNr>(v, vx, va, ts, ta, su, ck, K, C, steering, throttle, braking, R, S, np, sink);
+    update24<kNr>(v, vx, va, ts, ta, su, C, R, dt, S, np, sink);
+}
 
 // The carried 24-DOF state of one vehicle from / to its SoA column S (S[field * np]); the fields a
 // step writes only from a window's last step are written by step24 with sink set.

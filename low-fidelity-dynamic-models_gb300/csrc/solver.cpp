@@ -29,6 +29,7 @@
 #include "../../include/lfdm.h"
 #include "adjoint18.h"
 #include "jacobian18.h"
+#include "jacobian_fd.h"
 #include "json_loader.h"
 #include "kernels.h"
 
@@ -1050,6 +1051,40 @@ int lfdm_rhs_jacobian18(lfdm_solver* h, const double* ctl, int reference_point, 
     CK(launch_rhs_jacobian18(A, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     if (ny) *ny = tc ? 21 : 20;
+    return LFDM_OK;
+}
+
+int lfdm_rhs_jacobian_fd(lfdm_solver* h, const double* ctl, int reference_point, double* jac_state, double* jac_ctl,
+                         int* ny) {
+    if (!h) return LFDM_ERR_ARG;
+    if (!ctl || !jac_state || !jac_ctl) return h->fail(LFDM_ERR_ARG, "null array");
+    if (h->precision != LFDM_PREC_FP64) return h->fail(LFDM_ERR_ARG, "the right-hand-side Jacobian is FP64");
+    if (h->classes.empty()) return h->fail(LFDM_ERR_STATE, "no vehicles constructed");
+    const int tc = h->classes[0].tcbool != 0;
+    for (const lfdm_class18& c : h->classes)
+        if ((c.tcbool != 0) != (tc != 0))
+            return h->fail(LFDM_ERR_ARG, "all vehicles must agree on the torque converter (it sets the state count)");
+    int rc = check_ready(h, false);
+    if (rc) return rc;
+    rc = sync_device(h);
+    if (rc) return rc;
+    JacFdLaunch A;
+    A.model = (int)h->model;
+    A.tire_nr = h->tire_type == LFDM_TIRE_TMEASY_NR ? 1 : 0;
+    A.n = (int)h->N;
+    A.npad = h->npad;
+    A.K = h->d_K.p;
+    A.classes = reinterpret_cast<const ClassDev18*>(h->d_classes.p);
+    A.nclasses = (int)h->classes.size();
+    A.class_of = h->d_class_of.p;
+    A.S = h->d_S.p;
+    A.ctl = ctl;
+    A.reference_point = reference_point ? 1 : 0;
+    A.jac_state = jac_state;
+    A.jac_ctl = jac_ctl;
+    CK(launch_rhs_jacobian_fd(A, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (ny) *ny = jac_fd_ny(A.model, A.tire_nr != 0, tc != 0);
     return LFDM_OK;
 }
 
