@@ -53,6 +53,8 @@ def _args():
     ap.add_argument("--fleet-vehicles", type=int, default=250_000)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-rollout line")
     ap.add_argument("--adjoint-vehicles", type=int, default=65_536)
+    ap.add_argument("--no-jacobian", action="store_true", help="skip the right-hand-side Jacobian line")
+    ap.add_argument("--jacobian-vehicles", type=int, default=65_536)
     ap.add_argument("--error-vehicles", type=int, default=65536)
     ap.add_argument("--error-horizon", type=float, default=20.0)
     ap.add_argument("--cpu-sample", type=int, default=8192, help="vehicles in the CPU-baseline sample")
@@ -380,6 +382,66 @@ def _adjoint_bench(lfdm, fleet, dev, n: int, nsteps: int, torch) -> dict:
                        "reference algorithm (oracle)"}
 
 
+def _jacobian_bench(lfdm, fleet, dev, n: int, cpu_sample: int, torch) -> dict:
+    """Right-hand-side Jacobians of every vehicle of the seeded 11/18/24-DOF SUV fleets after 1 s of
+    their drivers (TMeasy, torque converter): the reference's difference scheme
+    (lfdm_rhs_jacobian_fd; 2 ny + 4 right-hand sides per vehicle) and, for the 18-DOF model, the
+    exact Jacobian (lfdm_rhs_jacobian18). Each figure is the host wall time of the C-ABI call (it
+    returns after its stream synchronizes), best of 3 after one untimed call. Beside them, the same
+    scheme on all host cores over the same vehicles: the oracle's restatement of
+    IntegrateStepWithJacobian's Jacobian block, pinned bit for bit to the reference's CPU solvers."""
+    import ctypes
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    gdev = torch.device("cuda", dev)
+    rng = np.random.default_rng(SEED + 5)
+    out = {"config": f"{n} vehicles per model, seeded SUV fleets after 1 s of their drivers, controls "
+                     "steering U[-0.3, 0.3], throttle U[0, 1], braking 0; reference point (fresh state)",
+           "timing": "host wall time of the C-ABI call (returns after its stream synchronizes), best of 3"}
+    cores = os.cpu_count() or 1
+    for model, make in ((11, fleet.fleet11), (18, fleet.fleet18), (24, fleet.fleet24)):
+        f = make(n, seed=SEED + 5, horizon=2.0)
+        sol = getattr(lfdm, f"d{model}SolverHalfImplicitGPU")(n, device=dev)
+        sol.construct_class(f["cls"][0], f["params"])
+        sol.set_driver_tables(f["tables"])
+        sol.set_states(f["states"])
+        sol.SetKernelSimTime(1.0)
+        sol.SetEndTime(1.0)
+        sol.Solve()
+        ctl_h = np.stack([rng.uniform(-0.3, 0.3, n), rng.uniform(0.0, 1.0, n), np.zeros(n)])
+        ctl = torch.tensor(ctl_h, dtype=torch.float64, device=gdev)
+        js = torch.empty(36 * 36 * n, dtype=torch.float64, device=gdev)
+        ju = torch.empty(36 * 2 * n, dtype=torch.float64, device=gdev)
+        ny = ctypes.c_int()
+        fns = [("fd", sol._L.lfdm_rhs_jacobian_fd)] + ([("exact", sol._L.lfdm_rhs_jacobian18)] if model == 18 else [])
+        for name, fn in fns:
+            def call():
+                t0 = time.perf_counter()
+                rc = fn(sol._h, ctypes.c_void_p(ctl.data_ptr()), 1, ctypes.c_void_p(js.data_ptr()),
+                        ctypes.c_void_p(ju.data_ptr()), ctypes.byref(ny))
+                if rc:
+                    raise RuntimeError(f"{name} Jacobian failed: {rc}")
+                return time.perf_counter() - t0
+            call()
+            best = min(call() for _ in range(3))
+            out[f"{model}dof_{name}"] = {"ms": best * 1e3, "jacobians_per_s": n / best, "ny": ny.value,
+                                         "finite": bool(torch.isfinite(js[: ny.value ** 2 * n]).all().item())}
+        # the reference's scheme on the host cores (a bounded sample)
+        m = min(cpu_sample, n)
+        states = sol.get_states(0, m)
+        sol.close()
+        t0 = time.perf_counter()
+        oracle_lib.jacobian_fd_batch(model, 0, f["cls"][0], f["params"][:m], states, ctl_h[:, :m], nthreads=cores)
+        secs = time.perf_counter() - t0
+        out[f"{model}dof_fd"]["cpu_reference_scheme"] = {
+            "jacobians_per_s": m / secs, "cores": cores, "kind": "port",
+            "sample": f"{m} vehicles ({secs:.2f} s wall), oracle_jacobian_fd_batch (oracle/lfdm_oracle.c) on "
+                      "all host cores"}
+        out[f"{model}dof_fd"]["speedup_vs_cpu"] = out[f"{model}dof_fd"]["jacobians_per_s"] / (m / secs)
+    return out
+
+
 def run_ours(a, dist: Dist):
     import torch
 
@@ -511,6 +573,9 @@ def run_ours(a, dist: Dist):
     adjoint_line = None
     if not a.no_adjoint:
         adjoint_line = _adjoint_bench(lfdm, fleet, dev, a.adjoint_vehicles, 2000, torch)
+    jacobian_line = None
+    if not a.no_jacobian and dist.rank == 0:
+        jacobian_line = _jacobian_bench(lfdm, fleet, dev, a.jacobian_vehicles, a.jacobian_vehicles, torch)
 
     cpu = None
     if dist.rank == 0:
@@ -542,6 +607,7 @@ def run_ours(a, dist: Dist):
             "models": models,
             "fleet": fleet_line,
             "adjoint": adjoint_line,
+            "jacobian": jacobian_line,
             "gpu_launches": launches,
             "clocks": clocks,
             "wall_s_timed": wall,

@@ -1751,3 +1751,49 @@ int oracle_jacobian_fd(int model, int tire_type, const lfdm_class18* cls, const 
     }
     return ny;
 }
+
+typedef struct {
+    int model, tire_type, full_point, lo, hi, rc;
+    const lfdm_class18* cls;
+    const double *params, *states, *ctl;
+    double *jac_state, *jac_ctl;
+} JacChunk;
+
+static void* jac_worker(void* p) {
+    JacChunk* c = (JacChunk*)p;
+    const int sc = c->model == LFDM_MODEL_18 ? LFDM_S_COUNT : c->model == LFDM_MODEL_11 ? LFDM11_S_COUNT : LFDM24_S_COUNT;
+    for (int i = c->lo; i < c->hi; ++i) {
+        const double ctl[3] = {c->ctl[3 * i], c->ctl[3 * i + 1], c->ctl[3 * i + 2]};
+        if (oracle_jacobian_fd(c->model, c->tire_type, c->cls, c->params + (size_t)i * LFDM_P_COUNT,
+                               c->states + (size_t)i * sc, ctl, c->full_point, c->jac_state + (size_t)i * 36 * 36,
+                               c->jac_ctl + (size_t)i * 36 * 2) < 0)
+            c->rc = 1;
+    }
+    return NULL;
+}
+
+int oracle_jacobian_fd_batch(int model, int tire_type, const lfdm_class18* cls, const double* params,
+                             const double* states, const double* ctl, int n, int full_point, int nthreads,
+                             double* jac_state, double* jac_ctl) {
+    if (n < 0 || !cls || !params || !states || !ctl || !jac_state || !jac_ctl) return 1;
+    if (model != LFDM_MODEL_11 && model != LFDM_MODEL_18 && model != LFDM_MODEL_24) return 1;
+    int nt = nthreads < 1 ? 1 : nthreads;
+    if (nt > n) nt = n > 0 ? n : 1;
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nt);
+    JacChunk* ch = (JacChunk*)malloc(sizeof(JacChunk) * nt);
+    for (int k = 0; k < nt; ++k) {
+        JacChunk c = {model, tire_type, full_point, (int)((long)n * k / nt), (int)((long)n * (k + 1) / nt), 0,
+                      cls, params, states, ctl, jac_state, jac_ctl};
+        ch[k] = c;
+        pthread_create(&th[k], NULL, jac_worker, &ch[k]);
+    }
+    int rc = 0;
+    for (int k = 0; k < nt; ++k) {
+        pthread_join(th[k], NULL);
+        rc |= ch[k].rc;
+    }
+    free(th);
+    free(ch);
+    return rc;
+}
+

@@ -73,6 +73,13 @@ int oracle_rhs(int model, int tire_type, const lfdm_class18* cls, const double* 
 int oracle_jacobian_fd(int model, int tire_type, const lfdm_class18* cls, const double* params, const double* state,
                        const double* ctl, int full_point, double* jac_state, double* jac_ctl);
 
+/* oracle_jacobian_fd for n vehicles of one class on nthreads host threads: params [n][LFDM_P_COUNT],
+   states [n][state count of the model], ctl [n][3]; jac_state [n][36 * 36] and jac_ctl [n][36 * 2]
+   (the first ny * ny and ny * 2 values of each block used). Returns 0, or 1 on bad arguments. */
+int oracle_jacobian_fd_batch(int model, int tire_type, const lfdm_class18* cls, const double* params,
+                             const double* states, const double* ctl, int n, int full_point, int nthreads,
+                             double* jac_state, double* jac_ctl);
+
 /* tireInit (18dof-gpu/dof18_gpu.cu:227-241) on one flat parameter vector. */
 void oracle_tire_init(double* params);
 

@@ -51,6 +51,9 @@ def lib(fma: bool = False):
         L.oracle_jacobian_fd.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 4 + [ctypes.c_int] + \
             [ctypes.c_void_p] * 2
         L.oracle_jacobian_fd.restype = ctypes.c_int
+        L.oracle_jacobian_fd_batch.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 4 + \
+            [ctypes.c_int] * 3 + [ctypes.c_void_p] * 2
+        L.oracle_jacobian_fd_batch.restype = ctypes.c_int
         _libs[path] = L
     return _libs[path]
 
@@ -191,4 +194,19 @@ def jacobian_fd(model, tire_type, cls, params, state, ctl, full_point=False):
                                   _ptr(js), _ptr(jc))
     assert ny > 0
     return js[:ny * ny].reshape(ny, ny), jc[:2 * ny].reshape(ny, 2)
+
+
+def jacobian_fd_batch(model, tire_type, cls, params, states, ctl, full_point=False, nthreads=1):
+    """oracle_jacobian_fd over n vehicles of one class on nthreads host threads; ctl [3][n]. Returns
+    (state Jacobians [n][ny][ny], control Jacobians [n][ny][2])."""
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    s = np.ascontiguousarray(states, dtype=np.float64)
+    n = s.shape[0]
+    c = np.ascontiguousarray(np.asarray(ctl, dtype=np.float64).T)
+    js, jc = np.zeros((n, 36 * 36)), np.zeros((n, 36 * 2))
+    rc = lib().oracle_jacobian_fd_batch(model, tire_type, ctypes.byref(cls), _ptr(p), _ptr(s), _ptr(c), n,
+                                        int(full_point), int(nthreads), _ptr(js), _ptr(jc))
+    assert rc == 0
+    ny = {11: 12, 18: 20, 24: 35}[model] - (0 if tire_type == 0 else {11: 4, 18: 8, 24: 8}[model]) + int(bool(cls.tcbool))
+    return js[:, : ny * ny].reshape(n, ny, ny), jc[:, : 2 * ny].reshape(n, ny, 2)
 

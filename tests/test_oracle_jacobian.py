@@ -122,3 +122,16 @@ def _pack(model, tire_type, tc, s):
         y += [s[C["LFDM24_S_CRANKOMEGA"]]] if tc else []
         y += [s[C[f"LFDM24_S_{f}"]] for f in ("X", "Y", "U", "V", "W", "WZ", "WX", "WY", "PSI", "PHI", "THETA")]
     return np.array(y)
+
+
+@pytest.mark.parametrize("model", [11, 18, 24])
+def test_threaded_batch_equals_the_single_vehicle_jacobians(model):
+    fleet = __import__("conftest").pkg_mod("fleet")
+    n = 12
+    f = {11: fleet.fleet11, 18: fleet.fleet18, 24: fleet.fleet24}[model](n, seed=9, horizon=2.0)
+    rng = np.random.default_rng(model)
+    ctl = np.stack([rng.uniform(-0.3, 0.3, n), rng.uniform(0.0, 1.0, n), rng.uniform(0.0, 0.2, n)])
+    js, jc = O.jacobian_fd_batch(model, 0, f["cls"][0], f["params"], f["states"], ctl, full_point=True, nthreads=4)
+    for i in range(n):
+        a, b = O.jacobian_fd(model, 0, f["cls"][0], f["params"][i], f["states"][i], ctl[:, i], full_point=True)
+        assert np.array_equal(js[i], a) and np.array_equal(jc[i], b)
