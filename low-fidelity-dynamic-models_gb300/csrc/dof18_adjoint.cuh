@@ -200,21 +200,8 @@ __device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, const Tape
     T.at(TT_(vsx)) = vsx;
     const double rw = r_eff * fabs(omega);
     const double vta = rw + 0.01;
-    const double ivta = 1.0 / vta;
     T.at(TT_(rw)) = rw;
     T.at(TT_(vta)) = vta;
-    T.at(TT_(ivta)) = ivta;
-    const double sx = -vsx * ivta;
-    double sy;
-    if (kSteered) {
-        T.at(TT_(N)) = vsy * c - vta * s;
-        T.at(TT_(D)) = vta * c + vsy * s;
-        sy = -(vsy * c - vta * s) / (vta * c + vsy * s);
-    } else {
-        sy = -vsy * ivta;
-    }
-    T.at(TT_(sx)) = sx;
-    T.at(TT_(sy)) = sy;
     const double fzc = fmin(fz, K(K_PNMAX));
     T.at(TT_(fzc)) = fzc;
     T.at(TT_(fzcl)) = fz > K(K_PNMAX) ? 1.0 : 0.0;
@@ -236,7 +223,30 @@ __device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, const Tape
     const double ssum = sxm + sym;
     const double fxd = fxm * dfy0, fyd = fym * dfx0;
     const double fsum = fxd + fyd;
-    const double r12 = 1.0 / (ssum * fsum);
+    // one division for 1/(ssum fsum), 1/vta and the steered wheel's 1/D, as in tire_core_tm
+    const double p12 = ssum * fsum;
+    double r12, ivta, sy;
+    if (kSteered) {
+        const double den = fma(vta, c, vsy * s);
+        const double num = fma(vsy, c, -vta * s);
+        T.at(TT_(N)) = num;
+        T.at(TT_(D)) = den;
+        const double pv = vta * den;
+        const double r = 1.0 / (p12 * pv);
+        r12 = pv * r;
+        const double ipv = p12 * r;
+        ivta = den * ipv;
+        sy = -num * (vta * ipv);
+    } else {
+        const double r = 1.0 / (p12 * vta);
+        r12 = vta * r;
+        ivta = p12 * r;
+        sy = -vsy * ivta;
+    }
+    const double sx = -vsx * ivta;
+    T.at(TT_(ivta)) = ivta;
+    T.at(TT_(sx)) = sx;
+    T.at(TT_(sy)) = sy;
     const double issum = fsum * r12, ifsum = ssum * r12;
     const double hsxn = fma(sxm, issum, fxd * ifsum);
     const double hsyn = fma(sym, issum, fyd * ifsum);

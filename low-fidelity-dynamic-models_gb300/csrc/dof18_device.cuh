@@ -418,14 +418,6 @@ __device__ __forceinline__ void tire_core_tm(TireC& ts, TireAux& ta, const KView
     const double vsx = fma(-omega, r_eff, ta.vsx);
     const double rw = r_eff * fabs(omega);
     const double vta = rw + 0.01;
-    const double ivta = 1.0 / vta;
-    const double sx = -vsx * ivta;
-    double sy;
-    if (kSteered) {
-        sy = -(vsy * c - vta * s) / (vta * c + vsy * s);
-    } else {
-        sy = -vsy * ivta;
-    }
     fz = min_nn(fz, K(K_PNMAX));
     const double fzn = fz * K(K_INVPN);
     const double dfx0 = fzn * fma(-K(K_Q2DFX0), fzn, K(K_Q1DFX0));
@@ -439,11 +431,29 @@ __device__ __forceinline__ void tire_core_tm(TireC& ts, TireAux& ta, const KView
     const double sym = fma(K(K_DSYM), fzn1, K(K_LSYM));
     const double sxs = fma(K(K_DSXS), fzn1, K(K_LSXS));
     const double sys = fma(K(K_DSYS), fzn1, K(K_LSYS));
-    // hsxn = sxm/(sxm+sym) + (fxm/dfx0)/(fxm/dfx0 + fym/dfy0): one reciprocal for both quotients
+    // hsxn = sxm/(sxm+sym) + (fxm/dfx0)/(fxm/dfx0 + fym/dfy0). One division gives 1/(ssum fsum) for
+    // both quotients, 1/vta for the slips and, on a steered wheel, 1/(vta c + vsy s) for the
+    // lateral slip -(vsy c - vta s)/(vta c + vsy s) (sy = -tan(atan2(vsy, vta) - delta)).
     const double ssum = sxm + sym;
     const double fxd = fxm * dfy0, fyd = fym * dfx0;
     const double fsum = fxd + fyd;
-    const double r12 = 1.0 / (ssum * fsum);
+    const double p12 = ssum * fsum;
+    double r12, ivta, sy;
+    if (kSteered) {
+        const double den = fma(vta, c, vsy * s);
+        const double pv = vta * den;
+        const double r = 1.0 / (p12 * pv);
+        r12 = pv * r;
+        const double ipv = p12 * r;
+        ivta = den * ipv;
+        sy = -fma(vsy, c, -vta * s) * (vta * ipv);
+    } else {
+        const double r = 1.0 / (p12 * vta);
+        r12 = vta * r;
+        ivta = p12 * r;
+        sy = -vsy * ivta;
+    }
+    const double sx = -vsx * ivta;
     const double issum = fsum * r12, ifsum = ssum * r12;
     const double hsxn = fma(sxm, issum, fxd * ifsum);
     const double hsyn = fma(sym, issum, fyd * ifsum);
