@@ -278,22 +278,22 @@ __device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, const Tape
     const double fs = hyp(fxs * calpha, fys * salpha);
     const double ss = hyp(sxs * cax, sys * say);
     T.at(TT_(df0)) = df0; T.at(TT_(fm)) = fm; T.at(TT_(sm)) = sm; T.at(TT_(fs)) = fs; T.at(TT_(ss)) = ss;
-    double f, fos;
-    tmxy_rcp(f, fos, sc, isc, df0, sm, ism, fm, ifm, ss, fs);
-    T.at(TT_(fos)) = fos;
+    double fn, fd;
+    tmxy_frac(fn, fd, sc, isc, df0, sm, ism, fm, ifm, ss, fs);
+    T.at(TT_(fos)) = fn / fd;  // the ratio itself, for the reverse
     T.at(TT_(sgn)) = sgnd(omega);
     ta.My = -K(K_RR) * fzc * ta.rStat * T.at(TT_(sgn));
     const double vtxs = fma(rw, hsxn, 0.01);
     const double vtys = fma(rw, hsyn, 0.01);
     const double cx = K(K_CX), cy = K(K_CY), dx = K(K_DX), dy = K(K_DY);
-    const double numx = fma(-vtxs * cx, ts.xe, -fos * vsx);
-    const double numy = fma(-vtys * cy, ts.ye, fos * (sy * vta));
-    const double denx = fma(vtxs, dx, fos), deny = fma(vtys, dy, fos);
+    const double numx = fma(-vtxs * cx, ts.xe * fd, -fn * vsx);
+    const double numy = fma(-vtys * cy, ts.ye * fd, fn * (sy * vta));
+    const double denx = fma(vtxs * dx, fd, fn), deny = fma(vtys * dy, fd, fn);
     const double rd = 1.0 / (denx * deny);
     ts.xedot = numx * (deny * rd);
     ts.yedot = numy * (denx * rd);
-    T.at(TT_(idenx)) = deny * rd;
-    T.at(TT_(ideny)) = denx * rd;
+    T.at(TT_(idenx)) = fd * (deny * rd);  // 1 / (vtxs dx + fos)
+    T.at(TT_(ideny)) = fd * (denx * rd);
     T.at(TT_(vtxs)) = vtxs; T.at(TT_(vtys)) = vtys; T.at(TT_(numx)) = numx; T.at(TT_(numy)) = numy; T.at(TT_(denx)) = denx; T.at(TT_(deny)) = deny;
     T.at(TT_(xedot)) = ts.xedot; T.at(TT_(yedot)) = ts.yedot;
     const double fxdyn = fma(dx, ts.xedot, cx * ts.xe);

@@ -310,27 +310,29 @@ struct KView {
 };
 
 // tmxy_combined (dof18_gpu.cu:243-285) given the reciprocals of s, sm and fm (is, ism, ifm; the
-// TMeasy tire has them from the rsqrt of the squared norms it takes anyway): the full-sliding and
-// adhesion regimes, which nearly every step is in, then need one division (1/dn) instead of four.
-__device__ __forceinline__ void tmxy_rcp(double& f, double& fos, double s, double is, double df0, double sm,
-                                         double ism, double fm, double ifm, double ss, double fs) {
+// TMeasy tire has them from the rsqrt of the squared norms it takes anyway). Returns the ratio of
+// the combined force to the combined slip, fos = f / s, as a fraction fn / fd: in the adhesion
+// regime, which nearly every step is in, fos = df0 / dn and the caller folds 1/dn into its own
+// division; elsewhere fd = 1 and no division is taken (the full-sliding and transition regimes use
+// is = 1/s).
+__device__ __forceinline__ void tmxy_frac(double& fn, double& fd, double s, double is, double df0, double sm,
+                                          double ism, double fm, double ifm, double ss, double fs) {
+    fd = 1.0;
     double df0loc = 0.0;
     if (gt0(sm)) df0loc = max_nn(2.0 * fm * ism, df0);
     if (gt0(s) && gt0(df0loc)) {
         if (gt_nn(s, ss)) {
-            f = fs;
-            fos = fs * is;
-        } else if (gt_nn(sm, s)) {  // adhesion
+            fn = fs * is;
+        } else if (gt_nn(sm, s)) {  // adhesion: f = df0 sm sn / dn, s = sm sn
             const double p = df0loc * sm * ifm - 2.0;
             const double sn = s * ism;
-            const double dn = fma(sn + p, sn, 1.0);
-            const double idn = 1.0 / dn;
-            f = df0loc * sm * sn * idn;
-            fos = df0loc * idn;
+            fd = fma(sn + p, sn, 1.0);
+            fn = df0loc;
         } else {
             const double q = fm * ism;
             const double a = q * q / (df0loc * sm);
             const double sstar = sm + (fm - fs) / (a * (ss - sm));
+            double f;
             if (sstar <= ss) {
                 if (s <= sstar) {
                     f = fm - a * (s - sm) * (s - sm);
@@ -342,11 +344,10 @@ __device__ __forceinline__ void tmxy_rcp(double& f, double& fos, double s, doubl
                 const double sn = (s - sm) / (ss - sm);
                 f = fm - (fm - fs) * sn * sn * (3.0 - 2.0 * sn);
             }
-            fos = f * is;
+            fn = f * is;
         }
     } else {
-        f = 0.0;
-        fos = 0.0;
+        fn = 0.0;
     }
 }
 
@@ -481,17 +482,18 @@ __device__ __forceinline__ void tire_core_tm(TireC& ts, TireAux& ta, const KView
     hyp_rcp(sxm * cax, sym * say, sm, ism);
     const double fs = hyp(fxs * calpha, fys * salpha);
     const double ss = hyp(sxs * cax, sys * say);
-    double f, fos;
-    tmxy_rcp(f, fos, sc, isc, df0, sm, ism, fm, ifm, ss, fs);
-    (void)f;
+    double fn, fd;
+    tmxy_frac(fn, fd, sc, isc, df0, sm, ism, fm, ifm, ss, fs);
     // rolling resistance: sineStep(vta, 0, 0, 0, 1) == 1 for vta >= 0.01
     ta.My = -K(K_RR) * fz * ta.rStat * sgnd(omega);
     const double vtxs = fma(rw, hsxn, 0.01);
     const double vtys = fma(rw, hsyn, 0.01);
     const double cx = K(K_CX), cy = K(K_CY), dx = K(K_DX), dy = K(K_DY);
-    const double numx = fma(-vtxs * cx, ts.xe, -fos * vsx);
-    const double numy = fma(-vtys * cy, ts.ye, fos * (sy * vta));
-    const double denx = fma(vtxs, dx, fos), deny = fma(vtys, dy, fos);
+    // xedot = (-vtxs cx xe - fos vsx) / (vtxs dx + fos) with fos = fn / fd, numerator and denominator
+    // scaled by fd (likewise yedot); one division for both rates
+    const double numx = fma(-vtxs * cx, ts.xe * fd, -fn * vsx);
+    const double numy = fma(-vtys * cy, ts.ye * fd, fn * (sy * vta));
+    const double denx = fma(vtxs * dx, fd, fn), deny = fma(vtys * dy, fd, fn);
     const double rd = 1.0 / (denx * deny);
     ts.xedot = numx * (deny * rd);
     ts.yedot = numy * (denx * rd);
