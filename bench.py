@@ -57,7 +57,7 @@ def _args():
     ap.add_argument("--jacobian-vehicles", type=int, default=65_536)
     ap.add_argument("--error-vehicles", type=int, default=65536)
     ap.add_argument("--error-horizon", type=float, default=20.0)
-    ap.add_argument("--cpu-sample", type=int, default=8192, help="vehicles in the CPU-baseline sample")
+    ap.add_argument("--cpu-sample", type=int, default=32768, help="vehicles in the CPU-baseline sample")
     return ap.parse_args()
 
 
