@@ -62,7 +62,7 @@ def _worst(a, b, ac, bc, name, k=3):
     return out
 
 
-def _judge(e, what, worst=()):
+def _assess(e, what, worst=()):
     print(f"{what}: {e.size} entries, median {np.median(e):.1e}, 99% {np.quantile(e, 0.99):.1e}, "
           f"max {e.max():.1e}, above {TOL:g}: {(e > TOL).mean():.2%}")
     for w in worst[:6]:
@@ -80,8 +80,8 @@ def _compare(pairs, what):
         es.append(e1)
         ec.append(e2)
         w += _worst(a, b, ac, bc, name)
-    _judge(np.concatenate(es), what + ", state Jacobians", w)
-    _judge(np.concatenate(ec), what + ", control Jacobians")
+    _assess(np.concatenate(es), what + ", state Jacobians", w)
+    _assess(np.concatenate(ec), what + ", control Jacobians")
 
 
 def _solver(lfdm, model, cls, params, states, tire_type):
