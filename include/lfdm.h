@@ -309,9 +309,11 @@ int lfdm_traj18_last_ms(lfdm_solver* h, double* forward_ms, double* backward_ms)
 /* derivative): jac_state [ny][ny][N] = d rhs_r / d y_c and jac_ctl [ny][2][N] = d rhs_r /          */
 /* d (steering, throttle), DEVICE arrays, in the reference's packed order (packY/packYDOT, :879-1018): */
 /* y = {xe, ye} of LF, RF, LR, RR, omega x 4, crank speed (torque converter only), x, y, u, v, psi,  */
-/* wz, phi, wx; ny = 21 with a torque converter, 20 without (*ny). reference_point = 1 differentiates */
-/* where PerturbRhsFun does (a fresh vehicle state: previous accelerations 0, first gear); 0 at the   */
-/* full current state. TMeasy tires; all vehicles with or all without a torque converter.            */
+/* wz, phi, wx; ny = 21 with a torque converter, 20 without (*ny); with TMeasyNr tires (no          */
+/* deflection states) y = omega x 4, crank speed, x, y, u, v, psi, wz, phi, wx and ny = 13 or 12.     */
+/* reference_point = 1 differentiates where PerturbRhsFun does (a fresh vehicle state: previous      */
+/* accelerations 0, first gear); 0 at the full current state. All vehicles with or all without a    */
+/* torque converter.                                                                                */
 int lfdm_rhs_jacobian18(lfdm_solver* h, const double* ctl, int reference_point, double* jac_state, double* jac_ctl,
                         int* ny);
 

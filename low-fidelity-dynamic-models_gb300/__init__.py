@@ -420,9 +420,10 @@ class d18SolverHalfImplicitGPU(_SolverGPU):
         the reference CPU solver's GetJacobianState / GetJacobianControls by central differences,
         18dof/dof18_halfImplicit.cpp:356-520). Controls are scalars or arrays of N. Returns
         (jac_state [N, ny, ny], jac_controls [N, ny, 2]) in the reference's packed order, ny = 21 with a
-        torque converter and 20 without; reference_point selects the point the reference
-        differentiates at (previous accelerations 0, first gear) rather than the full current state.
-        TMeasy tires; rhs_jacobian_fd covers every tire by the reference's difference scheme."""
+        torque converter and 20 without (13 and 12 with TMeasyNr tires, which have no deflection
+        states); reference_point selects the point the reference differentiates at (previous
+        accelerations 0, first gear) rather than the full current state. rhs_jacobian_fd gives the
+        reference's own difference scheme for every model."""
         return self._jacobian(self._L.lfdm_rhs_jacobian18, steering, throttle, braking, reference_point)
 
 

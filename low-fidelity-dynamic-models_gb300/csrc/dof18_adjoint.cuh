@@ -16,7 +16,8 @@
 // The library is compiled without implicit multiply-add contraction (so that every kernel that runs
 // a forward step rounds it alike); the reverse sweep, which no other kernel has to match, writes
 // its sums of products as explicit fma() instead, halving the FP64 instructions of those updates. Supported: TMeasy
-// tires, linear or mapped steering, with or without torque converter, throttleMod off.
+// tires (and, for the right-hand-side Jacobian, TMeasyNr tires: tire_fwd_tape_nr / tire_rev_nr),
+// linear or mapped steering, with or without torque converter, throttleMod off.
 #pragma once
 
 #include <cstddef>
@@ -98,6 +99,32 @@ struct TireTape {
     double Fx, Fy, fxstr, fystr, clx, cly, wxw, wyw, dwx, dwy;  // clx/cly: -1/0/+1 clamp side
     double fx, fy, My, sgn;
 };
+// Per-tire tape of a TMeasyNr tire, in the slots of TireTape: the fields the vehicle-level sweep
+// reads (on, om, rStat, fx, fy, My) sit at the same offsets as in TireTape, the rest of the head in
+// slots the TMeasy tire uses for its own intermediates.
+struct TireTapeNrHead {
+    double on, fz, xt, rStat, r_eff, rdynco, fzrd, om;  // as TireTape
+    double vsxin, vsx, vsy, vta, sx, sy, N, D;
+    double tx, ty, a0, b0, h0, clamp, Fx0, Fy0;          // Coulomb force: tanh terms, before/after the clamp
+    double fzc, fzcl, fzn, dfx0, dfy0, fxm, fym, fxs, fys, sxm, sym, sxs, sys;
+    double w, dw;                                        // slip blend (frblend) and its slope in |vsx|
+    double qpos, q, isc, sc, calpha, salpha;
+    double df0, hfm, hsm, hfs, hss, fm, sm, fs, ss, f, fos, Fx, Fy, th;  // th = tanh(omega)
+};
+struct TireTapeNr {
+    TireTapeNrHead h;
+    double pad[(offsetof(TireTape, fx) - sizeof(TireTapeNrHead)) / sizeof(double)];
+    double fx, fy, My;
+};
+static_assert(offsetof(TireTapeNr, h) == 0, "the head starts the tire tape");
+static_assert(offsetof(TireTapeNrHead, on) == offsetof(TireTape, on) &&
+                  offsetof(TireTapeNrHead, rStat) == offsetof(TireTape, rStat) &&
+                  offsetof(TireTapeNrHead, om) == offsetof(TireTape, om),
+              "shared tire tape fields");
+static_assert(offsetof(TireTapeNr, fx) == offsetof(TireTape, fx) && offsetof(TireTapeNr, fy) == offsetof(TireTape, fy) &&
+                  offsetof(TireTapeNr, My) == offsetof(TireTape, My) && sizeof(TireTapeNr) <= sizeof(TireTape),
+              "the TMeasyNr tape fits the TMeasy slots");
+
 // Step tape: inputs, tire tapes and the vehicle-level intermediates.
 struct StepTape {
     double u, v, psi, wz, phi, wx, udot, vdot, crank, gear;
@@ -129,6 +156,7 @@ struct TapeRef {
 };
 #define TS_(f) ((int)(offsetof(StepTape, f) / sizeof(double)))
 #define TT_(f) ((int)(offsetof(TireTape, f) / sizeof(double)))
+#define TN_(f) ((int)(offsetof(TireTapeNrHead, f) / sizeof(double)))
 __device__ __forceinline__ TapeRef tire_ref(const TapeRef& T, int k) {
     return {T.p + (size_t)(TS_(t) + k * kTireTapeDoubles) * T.s, T.s};
 }
@@ -316,7 +344,150 @@ __device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, const Tape
     T.at(TT_(My)) = ta.My;
 }
 
-// One step18<false> with its tape; v/va/ts/ta as in step18.
+// sineStep(x, x1, 0, x2, 1) (the TMeasyNr slip blend) and its slope
+__device__ __forceinline__ void sine_step01(double x, double x1, double x2, double& y, double& dy) {
+    y = sine_step(x, x1, 0., x2, 1.);
+    if (x <= x1 || x >= x2) {
+        dy = 0.0;
+        return;
+    }
+    const double u = (x - x1) / (x2 - x1);
+    dy = (1.0 - cos(k2Pi * u)) / (x2 - x1);
+}
+
+// The arithmetic of tire_rhs_nr / tire_core_nr (dof18_device.cuh) with its tape.
+template <bool kSteered>
+__device__ __forceinline__ void tire_fwd_tape_nr(TireC& ts, TireAux& ta, const TapeRef& T, const KView& K, double c,
+                                                 double s) {
+    const double fz = ta.fz;
+    T.at(TN_(fz)) = fz;
+    T.at(TN_(om)) = ts.omega;
+    T.at(TN_(vsy)) = ta.vsy;
+    T.at(TN_(vsxin)) = ta.vsx;
+    T.at(TN_(on)) = gt0(fz) ? 1.0 : 0.0;
+    if (!gt0(fz)) {
+        ts.omega = 0;
+        ta.xt = 0;
+        ta.rStat = K(K_R0);
+        ta.fx = 0;
+        ta.fy = 0;
+        ta.My = 0;
+        T.at(TN_(rStat)) = ta.rStat;
+        T.at(TT_(fx)) = T.at(TT_(fy)) = T.at(TT_(My)) = 0;
+        return;
+    }
+    ta.xt = fz * K(K_INVKT);
+    ta.rStat = K(K_R0) - ta.xt;
+    T.at(TN_(xt)) = ta.xt;
+    T.at(TN_(rStat)) = ta.rStat;
+    double rdynco;
+    if (!gt_nn(fz, K(K_FZRD))) {
+        T.at(TN_(fzrd)) = 1.0;
+        rdynco = fma(K(K_DRD), fma(fz, K(K_INVPN), -1.0), K(K_RDPN));
+    } else {
+        T.at(TN_(fzrd)) = 0.0;
+        rdynco = K(K_RDCRIT);
+    }
+    T.at(TN_(rdynco)) = rdynco;
+    const double r_eff = fma(rdynco, ta.xt, ta.rStat);
+    T.at(TN_(r_eff)) = r_eff;
+    const double vsy = ta.vsy;
+    const double omega = ts.omega;
+    const double mu = K(K_MU);
+    const double vsx = fma(-omega, r_eff, ta.vsx);
+    const double vta = r_eff * fabs(omega) + 0.01;
+    T.at(TN_(vsx)) = vsx;
+    T.at(TN_(vta)) = vta;
+    // computeCombinedCoulombForce
+    const double vcoul = K(K_VCOUL);
+    const double tx = tanh(-2.0 * vsx / vcoul), ty = tanh(-2.0 * vsy / vcoul);
+    double Fx0 = tx * fz * mu, Fy0 = ty * fz * mu;
+    T.at(TN_(tx)) = tx; T.at(TN_(ty)) = ty; T.at(TN_(a0)) = Fx0; T.at(TN_(b0)) = Fy0;
+    const double h0 = sqrt(fma(Fx0, Fx0, Fy0 * Fy0));
+    T.at(TN_(h0)) = h0;
+    T.at(TN_(clamp)) = 0.0;
+    if (h0 > fz * mu) {
+        const double g = fz * mu / h0;
+        Fx0 *= g;
+        Fy0 *= g;
+        T.at(TN_(clamp)) = 1.0;
+    }
+    T.at(TN_(Fx0)) = Fx0; T.at(TN_(Fy0)) = Fy0;
+    const double sx = -vsx / vta;
+    double sy;
+    if (kSteered) {
+        const double N = vsy * c - vta * s, D = vta * c + vsy * s;
+        T.at(TN_(N)) = N;
+        T.at(TN_(D)) = D;
+        sy = -N / D;
+    } else {
+        sy = -vsy / vta;
+    }
+    T.at(TN_(sx)) = sx; T.at(TN_(sy)) = sy;
+    const double fzc = fmin(fz, K(K_PNMAX));
+    T.at(TN_(fzc)) = fzc;
+    T.at(TN_(fzcl)) = fz > K(K_PNMAX) ? 1.0 : 0.0;
+    const double fzn = fzc * K(K_INVPN);
+    T.at(TN_(fzn)) = fzn;
+    const double dfx0 = fzn * fma(-K(K_Q2DFX0), fzn, K(K_Q1DFX0));
+    const double dfy0 = fzn * fma(-K(K_Q2DFY0), fzn, K(K_Q1DFY0));
+    const double fxm = fzn * fma(-K(K_Q2FXM), fzn, K(K_Q1FXM));
+    const double fym = fzn * fma(-K(K_Q2FYM), fzn, K(K_Q1FYM));
+    const double fxs = fzn * fma(-K(K_Q2FXS), fzn, K(K_Q1FXS));
+    const double fys = fzn * fma(-K(K_Q2FYS), fzn, K(K_Q1FYS));
+    const double fzn1 = fzn - 1.0;
+    const double sxm = fma(K(K_DSXM), fzn1, K(K_LSXM));
+    const double sym = fma(K(K_DSYM), fzn1, K(K_LSYM));
+    const double sxs = fma(K(K_DSXS), fzn1, K(K_LSXS));
+    const double sys = fma(K(K_DSYS), fzn1, K(K_LSYS));
+    T.at(TN_(dfx0)) = dfx0; T.at(TN_(dfy0)) = dfy0; T.at(TN_(fxm)) = fxm; T.at(TN_(fym)) = fym; T.at(TN_(fxs)) = fxs; T.at(TN_(fys)) = fys;
+    T.at(TN_(sxm)) = sxm; T.at(TN_(sym)) = sym; T.at(TN_(sxs)) = sxs; T.at(TN_(sys)) = sys;
+    double w, dw;
+    sine_step01(fabs(ta.vsx), K(K_FRB0), K(K_FRB1), w, dw);
+    T.at(TN_(w)) = w; T.at(TN_(dw)) = dw;
+    const double q = fma(sx, sx, sy * sy);
+    double sc, calpha, salpha, isc = 0;
+    if (q > 0) {
+        isc = rsqrt(q);
+        sc = q * isc;
+        calpha = sx * isc;
+        salpha = sy * isc;
+        T.at(TN_(qpos)) = 1.0;
+    } else {
+        sc = 0;
+        calpha = kSqrt2Over2;
+        salpha = kSqrt2Over2;
+        T.at(TN_(qpos)) = 0.0;
+    }
+    T.at(TN_(q)) = q; T.at(TN_(isc)) = isc; T.at(TN_(sc)) = sc; T.at(TN_(calpha)) = calpha; T.at(TN_(salpha)) = salpha;
+    auto hyp = [](double a, double b) { return sqrt(fma(a, a, b * b)); };
+    const double df0 = hyp(dfx0 * calpha, dfy0 * salpha);
+    const double hfm = hyp(fxm * calpha, fym * salpha), hsm = hyp(sxm * calpha, sym * salpha);
+    const double hfs = hyp(fxs * calpha, fys * salpha), hss = hyp(sxs * calpha, sys * salpha);
+    const double fm = mu * hfm, sm = mu * hsm, fs = mu * hfs, ss = mu * hss;
+    T.at(TN_(df0)) = df0; T.at(TN_(hfm)) = hfm; T.at(TN_(hsm)) = hsm; T.at(TN_(hfs)) = hfs; T.at(TN_(hss)) = hss;
+    T.at(TN_(fm)) = fm; T.at(TN_(sm)) = sm; T.at(TN_(fs)) = fs; T.at(TN_(ss)) = ss;
+    double f, fos;
+    tmxy(f, fos, sc, df0, sm, fm, ss, fs);
+    T.at(TN_(f)) = f; T.at(TN_(fos)) = fos;
+    double Fx = 0., Fy = 0.;
+    if (sc > 0.) {
+        Fx = f * sx * isc;
+        Fy = f * sy * isc;
+    }
+    T.at(TN_(Fx)) = Fx; T.at(TN_(Fy)) = Fy;
+    ta.fx = fma(1.0 - w, Fx0, w * Fx);
+    ta.fy = fma(1.0 - w, Fy0, w * Fy);
+    const double th = tanh(omega);
+    T.at(TN_(th)) = th;
+    ta.My = -K(K_RR) * fzc * ta.rStat * th;
+    T.at(TT_(fx)) = ta.fx;
+    T.at(TT_(fy)) = ta.fy;
+    T.at(TT_(My)) = ta.My;
+}
+
+// One step18<kNr> with its tape; v/va/ts/ta as in step18.
+template <bool kNr = false>
 __device__ __forceinline__ void fwd18_tape(VehC& v, VehAux& va, TireC* ts, TireAux* ta, const TapeRef& T, const KView& K,
                                            const ClassDev18& C, double steering, double throttle, double braking,
                                            double dt) {
@@ -371,10 +542,17 @@ __device__ __forceinline__ void fwd18_tape(VehC& v, VehAux& va, TireC* ts, TireA
         ta[2].vsx = v.u - wcr;
         ta[3].vsx = v.u + wcr;
     }
-    tire_fwd_tape<true>(ts[0], ta[0], tire_ref(T, 0), K, cd, sd);
-    tire_fwd_tape<true>(ts[1], ta[1], tire_ref(T, 1), K, cd, sd);
-    tire_fwd_tape<false>(ts[2], ta[2], tire_ref(T, 2), K, 1.0, 0.0);
-    tire_fwd_tape<false>(ts[3], ta[3], tire_ref(T, 3), K, 1.0, 0.0);
+    if (kNr) {
+        tire_fwd_tape_nr<true>(ts[0], ta[0], tire_ref(T, 0), K, cd, sd);
+        tire_fwd_tape_nr<true>(ts[1], ta[1], tire_ref(T, 1), K, cd, sd);
+        tire_fwd_tape_nr<false>(ts[2], ta[2], tire_ref(T, 2), K, 1.0, 0.0);
+        tire_fwd_tape_nr<false>(ts[3], ta[3], tire_ref(T, 3), K, 1.0, 0.0);
+    } else {
+        tire_fwd_tape<true>(ts[0], ta[0], tire_ref(T, 0), K, cd, sd);
+        tire_fwd_tape<true>(ts[1], ta[1], tire_ref(T, 1), K, cd, sd);
+        tire_fwd_tape<false>(ts[2], ta[2], tire_ref(T, 2), K, 1.0, 0.0);
+        tire_fwd_tape<false>(ts[3], ta[3], tire_ref(T, 3), K, 1.0, 0.0);
+    }
     // powertrain (powertrain_rhs<false>) with its tape
     {
         double torque_t;
@@ -530,8 +708,10 @@ __device__ __forceinline__ void fwd18_tape(VehC& v, VehAux& va, TireC* ts, TireA
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        ts[k].xe = fma(ts[k].xedot, dt, ts[k].xe);
-        ts[k].ye = fma(ts[k].yedot, dt, ts[k].ye);
+        if (!kNr) {  // the TMeasyNr tire has no deflection states
+            ts[k].xe = fma(ts[k].xedot, dt, ts[k].xe);
+            ts[k].ye = fma(ts[k].yedot, dt, ts[k].ye);
+        }
         ts[k].omega = fma(ta[k].dOmega, dt, ts[k].omega);
     }
     if (C.tcbool) v.crank = fma(va.dOmega_crank, dt, v.crank);
@@ -851,6 +1031,139 @@ __device__ __forceinline__ void tire_rev(const TapeRef& T, const KView& K, const
     kb.at(KB_INVKT) = fma(T.at(TT_(fz)), xtb, kb.at(KB_INVKT));
 }
 
+// TMeasyNr tire adjoint (on-ground tire): from the adjoints of fx, fy, My (before any frame rotation)
+// and of rStat to those of omega, vsx before the slip correction, vsy, fz and cos/sin of the wheel
+// angle; branches (Coulomb clamp, blend band, curve regime, load clamp) as the forward took them.
+template <bool kSteered>
+__device__ __forceinline__ void tire_rev_nr(const TapeRef& T, const KView& K, const KBar& kb, double fxb, double fyb,
+                                            double Myb, double rStatb, double& omb, double& vsxinb, double& vsyb,
+                                            double& fzb, double& cb, double& sb_, double c, double s) {
+    const double mu = K(K_MU);
+    // rolling resistance My = -rr fzc rStat tanh(omega)
+    const double th = T.at(TN_(th)), fzc = T.at(TN_(fzc)), rStat = T.at(TN_(rStat));
+    double fzcb = -K(K_RR) * rStat * th * Myb;
+    rStatb = fma(-K(K_RR) * fzc * th, Myb, rStatb);
+    omb = fma(-K(K_RR) * fzc * rStat * fma(-th, th, 1.0), Myb, omb);
+    // blend of the Coulomb and the slip forces
+    const double w = T.at(TN_(w));
+    const double Fx0b = (1.0 - w) * fxb, Fy0b = (1.0 - w) * fyb;
+    const double Fxb = w * fxb, Fyb = w * fyb;
+    const double wb = fma(T.at(TN_(Fx)) - T.at(TN_(Fx0)), fxb, (T.at(TN_(Fy)) - T.at(TN_(Fy0))) * fyb);
+    vsxinb = fma(T.at(TN_(dw)) * (T.at(TN_(vsxin)) >= 0 ? 1.0 : -1.0), wb, vsxinb);
+    // Fx = f sx isc, Fy = f sy isc
+    const double sx = T.at(TN_(sx)), sy = T.at(TN_(sy));
+    double fb = 0, sxb = 0, syb = 0, iscb = 0;
+    if (T.at(TN_(sc)) > 0.0) {
+        const double f = T.at(TN_(f)), isc = T.at(TN_(isc));
+        const double pr = fma(sx, Fxb, sy * Fyb);
+        fb = isc * pr;
+        sxb = f * isc * Fxb;
+        syb = f * isc * Fyb;
+        iscb = f * pr;
+    }
+    // f = fos s on every regime of tmxy_combined
+    double scb = T.at(TN_(fos)) * fb, df0b = 0, smb = 0, fmb = 0, ssb = 0, fsb = 0;
+    tmxy_rev(T.at(TN_(sc)), T.at(TN_(df0)), T.at(TN_(sm)), T.at(TN_(fm)), T.at(TN_(ss)), T.at(TN_(fs)),
+             T.at(TN_(sc)) * fb, scb, df0b, smb, fmb, ssb, fsb);
+    // curve magnitudes: df0 = |(dfx0 ca, dfy0 sa)|, fm = mu |(fxm ca, fym sa)|, ...
+    const double ca = T.at(TN_(calpha)), sa = T.at(TN_(salpha));
+    double cab = 0, sab = 0;
+    double dfx0b = 0, dfy0b = 0, fxmb = 0, fymb = 0, fxsb = 0, fysb = 0, sxmb = 0, symb = 0, sxsb = 0, sysb = 0;
+    auto hyp_rev = [&](double p, double q, double h, double hb, double& pb_, double& qb_, double& cab_,
+                       double& sab_) {
+        if (h > 0 && hb != 0.0) {  // h = |(p ca, q sa)|
+            const double t = hb / h;
+            pb_ = fma(ca * (p * ca), t, pb_);
+            qb_ = fma(sa * (q * sa), t, qb_);
+            cab_ = fma(p * (p * ca), t, cab_);
+            sab_ = fma(q * (q * sa), t, sab_);
+        }
+    };
+    hyp_rev(T.at(TN_(dfx0)), T.at(TN_(dfy0)), T.at(TN_(df0)), df0b, dfx0b, dfy0b, cab, sab);
+    hyp_rev(T.at(TN_(fxm)), T.at(TN_(fym)), T.at(TN_(hfm)), mu * fmb, fxmb, fymb, cab, sab);
+    hyp_rev(T.at(TN_(sxm)), T.at(TN_(sym)), T.at(TN_(hsm)), mu * smb, sxmb, symb, cab, sab);
+    hyp_rev(T.at(TN_(fxs)), T.at(TN_(fys)), T.at(TN_(hfs)), mu * fsb, fxsb, fysb, cab, sab);
+    hyp_rev(T.at(TN_(sxs)), T.at(TN_(sys)), T.at(TN_(hss)), mu * ssb, sxsb, sysb, cab, sab);
+    // ca = sx isc, sa = sy isc, sc = q isc, isc = q^-1/2, q = sx^2 + sy^2
+    if (T.at(TN_(qpos)) != 0.0) {
+        const double isc = T.at(TN_(isc)), q = T.at(TN_(q));
+        sxb = fma(isc, cab, sxb);
+        syb = fma(isc, sab, syb);
+        iscb = fma(sx, cab, fma(sy, sab, iscb));
+        iscb = fma(q, scb, iscb);
+        const double qb = fma(isc, scb, -0.5 * isc * isc * isc * iscb);
+        sxb = fma(2.0 * sx, qb, sxb);
+        syb = fma(2.0 * sy, qb, syb);
+    }
+    // curve parameters from the normalised load
+    const double fzn = T.at(TN_(fzn));
+    double fznb = 0;
+    fznb = fma(fma(-2.0 * K(K_Q2DFX0), fzn, K(K_Q1DFX0)), dfx0b, fznb);
+    fznb = fma(fma(-2.0 * K(K_Q2DFY0), fzn, K(K_Q1DFY0)), dfy0b, fznb);
+    fznb = fma(fma(-2.0 * K(K_Q2FXM), fzn, K(K_Q1FXM)), fxmb, fznb);
+    fznb = fma(fma(-2.0 * K(K_Q2FYM), fzn, K(K_Q1FYM)), fymb, fznb);
+    fznb = fma(fma(-2.0 * K(K_Q2FXS), fzn, K(K_Q1FXS)), fxsb, fznb);
+    fznb = fma(fma(-2.0 * K(K_Q2FYS), fzn, K(K_Q1FYS)), fysb, fznb);
+    kb.at(KB_Q1FXM) = fma(fzn, fxmb, kb.at(KB_Q1FXM));
+    kb.at(KB_Q2FXM) = fma(-fzn * fzn, fxmb, kb.at(KB_Q2FXM));
+    kb.at(KB_Q1FYM) = fma(fzn, fymb, kb.at(KB_Q1FYM));
+    kb.at(KB_Q2FYM) = fma(-fzn * fzn, fymb, kb.at(KB_Q2FYM));
+    kb.at(KB_Q1FXS) = fma(fzn, fxsb, kb.at(KB_Q1FXS));
+    kb.at(KB_Q2FXS) = fma(-fzn * fzn, fxsb, kb.at(KB_Q2FXS));
+    kb.at(KB_Q1FYS) = fma(fzn, fysb, kb.at(KB_Q1FYS));
+    kb.at(KB_Q2FYS) = fma(-fzn * fzn, fysb, kb.at(KB_Q2FYS));
+    fznb = fma(K(K_DSXM), sxmb, fma(K(K_DSYM), symb, fma(K(K_DSXS), sxsb, fma(K(K_DSYS), sysb, fznb))));
+    fzcb = fma(K(K_INVPN), fznb, fzcb);
+    if (T.at(TN_(fzcl)) == 0.0) fzb += fzcb;
+    // slips
+    const double vta = T.at(TN_(vta)), ivta = 1.0 / vta;
+    double vsxb = -ivta * sxb;
+    double vtab = T.at(TN_(vsx)) * ivta * ivta * sxb;
+    if (kSteered) {
+        const double iD = 1.0 / T.at(TN_(D));
+        const double Nb = -syb * iD, Db = T.at(TN_(N)) * (iD * iD) * syb;
+        vsyb = fma(c, Nb, fma(s, Db, vsyb));
+        vtab = fma(-s, Nb, fma(c, Db, vtab));
+        cb = fma(T.at(TN_(vsy)), Nb, fma(vta, Db, cb));
+        sb_ = fma(-vta, Nb, fma(T.at(TN_(vsy)), Db, sb_));
+    } else {
+        vsyb = fma(-ivta, syb, vsyb);
+        vtab = fma(T.at(TN_(vsy)) * ivta * ivta, syb, vtab);
+    }
+    // Coulomb force: (a, b) = (tx, ty) fz mu, clamped to the circle of radius fz mu
+    {
+        const double fz = T.at(TN_(fz));
+        double ab = Fx0b, bb = Fy0b;
+        if (T.at(TN_(clamp)) != 0.0) {
+            const double a0 = T.at(TN_(a0)), b0 = T.at(TN_(b0)), h0 = T.at(TN_(h0));
+            const double ih = 1.0 / h0, g = fz * mu * ih;
+            const double dot = fma(a0, Fx0b, b0 * Fy0b);
+            ab = g * fma(-a0 * ih * ih, dot, Fx0b);
+            bb = g * fma(-b0 * ih * ih, dot, Fy0b);
+            fzb = fma(mu * ih, dot, fzb);
+        }
+        const double tx = T.at(TN_(tx)), ty = T.at(TN_(ty));
+        fzb = fma(mu, fma(tx, ab, ty * bb), fzb);
+        const double k2 = -2.0 / K(K_VCOUL);
+        vsxb = fma(fma(-tx, tx, 1.0) * k2, fz * mu * ab, vsxb);
+        vsyb = fma(fma(-ty, ty, 1.0) * k2, fz * mu * bb, vsyb);
+    }
+    // vsx = vsxin - omega r_eff, vta = r_eff |omega| + 0.01
+    const double om = T.at(TN_(om)), r_eff = T.at(TN_(r_eff));
+    double reffb = fabs(om) * vtab;
+    omb = fma(r_eff * (om > 0 ? 1.0 : (om < 0 ? -1.0 : 0.0)), vtab, omb);
+    vsxinb += vsxb;
+    omb = fma(-r_eff, vsxb, omb);
+    reffb = fma(-om, vsxb, reffb);
+    // r_eff = rdynco xt + rStat, rStat = r0 - xt, xt = fz / kt
+    double xtb = T.at(TN_(rdynco)) * reffb;
+    rStatb += reffb;
+    if (T.at(TN_(fzrd)) != 0.0) fzb += K(K_DRD) * K(K_INVPN) * (T.at(TN_(xt)) * reffb);
+    xtb += -rStatb;
+    fzb = fma(K(K_INVKT), xtb, fzb);
+    kb.at(KB_INVKT) = fma(T.at(TN_(fz)), xtb, kb.at(KB_INVKT));
+}
+
 // Reverse of one right-hand-side evaluation (rhsFun): from the adjoints of its outputs (udotb,
 // vdotb, wxdotb, wzdotb: chassis accelerations; dOcb: crank acceleration with a torque converter;
 // crank_outb: the crank speed the powertrain computes from the wheel speeds without one; dOmb,
@@ -859,6 +1172,7 @@ __device__ __forceinline__ void tire_rev(const TapeRef& T, const KView& K, const
 // carries for the deflections and receive (with L.om, L.xedot, L.yedot, L.udot, L.vdot) the
 // totals. The adjoints of the controls are added to steerb/thrb/brkb, those of the parameter
 // constants to kb.
+template <bool kNr = false>
 __device__ __forceinline__ void rev18_rhs(const TapeRef& T, const KView& K, const ClassDev18& C, const KBar& kb,
                                           const double udotb, const double vdotb, const double wxdotb,
                                           const double wzdotb, const double dOcb, double crank_outb,
@@ -1009,7 +1323,17 @@ __device__ __forceinline__ void rev18_rhs(const TapeRef& T, const KView& K, cons
         vsxinb[k] = vsyb[k] = fzb[k] = 0;
         if (tire_ref(T, k).at(TT_(on)) != 0.0) {
             double xeb = L.xe[k], yeb = L.ye[k], omb = om_midb[k];
-            if (k < 2)
+            if (kNr) {
+                xeb = yeb = 0;
+                if (k < 2)
+                    tire_rev_nr<true>(tire_ref(T, k), K, kb, fxb[k], fyb[k], Myb[k], rStatb[k], omb, vsxinb[k], vsyb[k],
+                                      fzb[k], cdb, sdb, T.at(TS_(cd)), T.at(TS_(sd)));
+                else {
+                    double cdum = 0, sdum = 0;
+                    tire_rev_nr<false>(tire_ref(T, k), K, kb, fxb[k], fyb[k], Myb[k], rStatb[k], omb, vsxinb[k],
+                                       vsyb[k], fzb[k], cdum, sdum, 1.0, 0.0);
+                }
+            } else if (k < 2)
                 tire_rev<true>(tire_ref(T, k), K, kb, xedotnb[k], yedotnb[k], fxb[k], fyb[k], Myb[k], rStatb[k], xeb, yeb,
                                omb, vsxinb[k], vsyb[k], fzb[k], cdb, sdb, T.at(TS_(cd)), T.at(TS_(sd)));
             else {

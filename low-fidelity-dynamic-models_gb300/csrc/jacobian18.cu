@@ -8,10 +8,11 @@
 // row; the four kinematic rows (dx, dy, dpsi = wz, dphi = wx) are written from their closed forms.
 //
 // Packed order (packY / packYDOT, 18dof/dof18_halfImplicit.cpp:879-1018): states
-// {xe, ye} of LF, RF, LR, RR; omega of LF, RF, LR, RR; crank speed (torque converter only); x, y, u,
-// v, psi, wz, phi, wx. Right-hand side in the same order: {xedot, yedot} x 4, domega x 4, dcrank,
-// dx, dy, udot, vdot, wz, wzdot, wx, wxdot. Controls: steering, throttle (braking enters the
-// right-hand side additively through the brake torque, so no derivative depends on it).
+// {xe, ye} of LF, RF, LR, RR (TMeasy tires only); omega of LF, RF, LR, RR; crank speed (torque
+// converter only); x, y, u, v, psi, wz, phi, wx. Right-hand side in the same order: {xedot, yedot}
+// x 4, domega x 4, dcrank, dx, dy, udot, vdot, wz, wzdot, wx, wxdot. Controls: steering, throttle
+// (braking enters the right-hand side additively through the brake torque, so no derivative
+// depends on it). The TMeasyNr tire is reversed by tire_rev_nr (dof18_adjoint.cuh).
 //
 // Evaluation point: PerturbRhsFun unpacks the packed states into a freshly constructed vehicle
 // state, so the reference differentiates with the previous accelerations (read by the load
@@ -33,6 +34,7 @@ size_t jac18_smem(int threads, int nclasses, bool* cls_smem) {
     return base + (in ? cls : 0);
 }
 
+template <bool kNr>
 __global__ void __launch_bounds__(128) rhs_jacobian18_kernel(const JacLaunch A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
@@ -76,10 +78,12 @@ __global__ void __launch_bounds__(128) rhs_jacobian18_kernel(const JacLaunch A) 
     const double psi = v.psi, u = v.u, vv = v.v;
     const double steer = __ldg(A.ctl + vid), thr = __ldg(A.ctl + nu + vid), brk = __ldg(A.ctl + 2 * nu + vid);
     const TapeRef T{A.tape + vid, np};
-    fwd18_tape(v, va, ts, ta, T, K, C, steer, thr, brk, 1e-3);
+    fwd18_tape<kNr>(v, va, ts, ta, T, K, C, steer, thr, brk, 1e-3);
 
     const bool tc = C.tcbool != 0;
-    const int ny = tc ? 21 : 20, o = tc ? 13 : 12;  // o: index of x in the packed vector
+    // TMeasy: {xe, ye} x 4, omega x 4, crank, x...; TMeasyNr: omega x 4, crank, x...
+    const int nt = kNr ? 0 : 8;                     // deflection states before the wheel speeds
+    const int ny = nt + (tc ? 13 : 12), o = nt + (tc ? 5 : 4);  // o: index of x in the packed vector
     auto J = [&](int r, int c) -> double& { return A.jac_state[((size_t)r * ny + c) * nu + vid]; };
     auto Ju = [&](int r, int c) -> double& { return A.jac_ctl[((size_t)r * 2 + c) * nu + vid]; };
     for (int r = 0; r < ny; ++r) {
@@ -108,9 +112,9 @@ __global__ void __launch_bounds__(128) rhs_jacobian18_kernel(const JacLaunch A) 
         // seed the adjoint of right-hand-side output r
         double udotb = 0, vdotb = 0, wxdotb = 0, wzdotb = 0, dOcb = 0;
         double dOmb[4] = {0, 0, 0, 0}, xedotb[4] = {0, 0, 0, 0}, yedotb[4] = {0, 0, 0, 0};
-        if (r < 8) (r & 1 ? yedotb : xedotb)[r >> 1] = 1.0;
-        else if (r < 12) dOmb[r - 8] = 1.0;
-        else if (tc && r == 12) dOcb = 1.0;
+        if (r < nt) (r & 1 ? yedotb : xedotb)[r >> 1] = 1.0;
+        else if (r < nt + 4) dOmb[r - nt] = 1.0;
+        else if (tc && r == nt + 4) dOcb = 1.0;
         else if (r == o + 2) udotb = 1.0;
         else if (r == o + 3) vdotb = 1.0;
         else if (r == o + 5) wzdotb = 1.0;
@@ -118,15 +122,17 @@ __global__ void __launch_bounds__(128) rhs_jacobian18_kernel(const JacLaunch A) 
         double ub = 0, vb = 0, wxb = 0, wzb = 0, phib = 0, crankb = 0, om_midb[4] = {0, 0, 0, 0};
         double steerb = 0, thrb = 0, brkb = 0;
         Adj18 L = {};
-        rev18_rhs(T, K, C, kb, udotb, vdotb, wxdotb, wzdotb, dOcb, 0.0, dOmb, xedotb, yedotb, ub, vb, wxb, wzb, phib,
-                  crankb, om_midb, L, steerb, thrb, brkb);
+        rev18_rhs<kNr>(T, K, C, kb, udotb, vdotb, wxdotb, wzdotb, dOcb, 0.0, dOmb, xedotb, yedotb, ub, vb, wxb, wzb,
+                       phib, crankb, om_midb, L, steerb, thrb, brkb);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            J(r, 2 * k) = L.xe[k];
-            J(r, 2 * k + 1) = L.ye[k];
-            J(r, 8 + k) = L.om[k];
+            if (!kNr) {
+                J(r, 2 * k) = L.xe[k];
+                J(r, 2 * k + 1) = L.ye[k];
+            }
+            J(r, nt + k) = L.om[k];
         }
-        if (tc) J(r, 12) = crankb;
+        if (tc) J(r, nt + 4) = crankb;
         J(r, o) = 0.0;      // x
         J(r, o + 1) = 0.0;  // y
         J(r, o + 2) = ub;
@@ -145,9 +151,10 @@ cudaError_t launch_rhs_jacobian18(const JacLaunch& A, cudaStream_t stream) {
     constexpr int threads = 128;
     JacLaunch L = A;
     const size_t smem = jac18_smem(threads, A.nclasses, &L.cls_smem);
-    cudaError_t e = cudaFuncSetAttribute(rhs_jacobian18_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    auto kern = A.tire_nr ? rhs_jacobian18_kernel<true> : rhs_jacobian18_kernel<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    rhs_jacobian18_kernel<<<(A.n + threads - 1) / threads, threads, smem, stream>>>(L);
+    kern<<<(A.n + threads - 1) / threads, threads, smem, stream>>>(L);
     return cudaGetLastError();
 }
 

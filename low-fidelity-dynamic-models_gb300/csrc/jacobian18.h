@@ -20,6 +20,7 @@ struct JacLaunch {
     const double* S = nullptr;             // [LFDM_S_COUNT][npad] states (SoA)
     const double* ctl = nullptr;           // [3][n] steering, throttle, braking
     int reference_point = 1;               // 1: PerturbRhsFun's fresh state; 0: the full current state
+    int tire_nr = 0;                       // 1: TMeasyNr tires
     double* tape = nullptr;                // [tape doubles][npad] scratch
     double* jac_state = nullptr;           // [ny][ny][n]
     double* jac_ctl = nullptr;             // [ny][2][n]

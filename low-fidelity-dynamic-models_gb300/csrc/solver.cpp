@@ -1021,7 +1021,6 @@ int lfdm_rhs_jacobian18(lfdm_solver* h, const double* ctl, int reference_point, 
     if (!h) return LFDM_ERR_ARG;
     if (!ctl || !jac_state || !jac_ctl) return h->fail(LFDM_ERR_ARG, "null array");
     if (h->model != LFDM_MODEL_18) return h->fail(LFDM_ERR_ARG, "the right-hand-side Jacobian is the 18-DOF model's");
-    if (h->tire_type == LFDM_TIRE_TMEASY_NR) return h->fail(LFDM_ERR_ARG, "the right-hand-side Jacobian needs TMeasy");
     if (h->precision != LFDM_PREC_FP64) return h->fail(LFDM_ERR_ARG, "the right-hand-side Jacobian is FP64");
     if (h->classes.empty()) return h->fail(LFDM_ERR_STATE, "no vehicles constructed");
     const int tc = h->classes[0].tcbool != 0;
@@ -1045,12 +1044,13 @@ int lfdm_rhs_jacobian18(lfdm_solver* h, const double* ctl, int reference_point, 
     A.S = h->d_S.p;
     A.ctl = ctl;
     A.reference_point = reference_point ? 1 : 0;
+    A.tire_nr = h->tire_type == LFDM_TIRE_TMEASY_NR ? 1 : 0;
     A.tape = h->d_adj_tape.p;
     A.jac_state = jac_state;
     A.jac_ctl = jac_ctl;
     CK(launch_rhs_jacobian18(A, h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    if (ny) *ny = tc ? 21 : 20;
+    if (ny) *ny = (A.tire_nr ? 12 : 20) + (tc ? 1 : 0);
     return LFDM_OK;
 }
 

@@ -1,4 +1,5 @@
-"""Exact right-hand-side Jacobians of the 18-DOF model on the GPU (lfdm_rhs_jacobian18) against
+"""Exact right-hand-side Jacobians of the 18-DOF model on the GPU (lfdm_rhs_jacobian18, TMeasy and
+TMeasyNr tires) against
 central differences of the reference algorithm's own right-hand side (the oracle's restatement of
 PerturbRhsFun, 18dof/dof18_halfImplicit.cpp:679-745), in the reference's packed order, at the point
 the reference differentiates at (fresh vehicle state) and at the full current state.
@@ -32,7 +33,10 @@ def _fleet(lfdm, n=48, seed=11):
     return f, sol, sol.get_states(), ctl
 
 
-def _fd(cls, p, y, ctl, full_state, steps):
+def _fd(cls, p, y, ctl, full_state, steps, tire_type=0):
+    def f(yy, cc):
+        return O.rhs(18, tire_type, cls, p, yy, cc, full_state)
+
     m = len(y)
     J = np.zeros((m, m))
     for c in range(m):
@@ -40,14 +44,14 @@ def _fd(cls, p, y, ctl, full_state, steps):
         yp, ym = y.copy(), y.copy()
         yp[c] += h
         ym[c] -= h
-        J[:, c] = (O.rhs18(cls, p, yp, ctl, full_state) - O.rhs18(cls, p, ym, ctl, full_state)) / (2 * h)
+        J[:, c] = (f(yp, ctl) - f(ym, ctl)) / (2 * h)
     Ju = np.zeros((m, 2))
     for c in range(2):
         h = 1e-7
         cp, cm = np.array(ctl, dtype=float), np.array(ctl, dtype=float)
         cp[c] += h
         cm[c] -= h
-        Ju[:, c] = (O.rhs18(cls, p, y, cp, full_state) - O.rhs18(cls, p, y, cm, full_state)) / (2 * h)
+        Ju[:, c] = (f(y, cp) - f(y, cm)) / (2 * h)
     return J, Ju
 
 
@@ -100,6 +104,87 @@ def test_jacobian_agrees_with_the_reference_scheme(built_lib):
         errs.append(_rel(js[i], J))
     e = np.concatenate(errs)
     print(f"vs the reference's 1e-3 differences ({e.size} nonzero entries): median {np.median(e):.1e}")
+    assert np.median(e) <= 1e-4
+
+
+def _nr_states(n, seed):
+    """The Sedan TMeasyNr golden case's final state, spread: velocities and wheel speeds scaled by
+    U[0.6, 1.4], and a third of the vehicles at 0.3-4 m/s with lateral slip (the Coulomb force, its
+    clamp to the friction circle and the blend into the slip forces)."""
+    import json
+    import os
+
+    from conftest import TESTS, case_inputs
+    with open(os.path.join(TESTS, "golden", "golden18.json")) as fh:
+        case = [c for c in json.load(fh)["cases"] if c["tire_type"] == 1][0]
+    cls, p, _, _ = case_inputs(case)
+    abi = pkg_mod("_abi")
+    rng = np.random.default_rng(seed)
+    s0 = np.array(case["expected_final"])
+    states = np.repeat(s0[None], n, axis=0)
+    om = [abi.S_TIRE0 + k * abi.C["LFDM_S_TIRE_STRIDE"] + abi.T["omega"] for k in range(4)]
+    fields = [abi.S[k] for k in ("u", "v", "wz", "wx")] + om
+    states[:, fields] *= rng.uniform(0.6, 1.4, (n, len(fields)))
+    r0 = float(p[abi.P["r0"]])
+    for i in range(0, n, 3):
+        u = rng.uniform(0.3, 4.0)
+        states[i, abi.S["u"]] = u
+        states[i, abi.S["v"]] = rng.uniform(-1.0, 1.0)
+        states[i, om] = u / r0 * rng.uniform(0.7, 1.3, 4)
+    ctl = np.stack([rng.uniform(-0.3, 0.3, n), rng.uniform(0.0, 1.0, n), rng.uniform(0.0, 0.3, n)])
+    return cls, p, states, ctl
+
+
+def _pack_nr(state, tc):
+    abi = pkg_mod("_abi")
+    y = [state[abi.S_TIRE0 + k * abi.C["LFDM_S_TIRE_STRIDE"] + abi.T["omega"]] for k in range(4)]
+    y += [state[abi.S["crankomega"]]] if tc else []
+    y += [state[abi.S[k]] for k in ("x", "y", "u", "v", "psi", "wz", "phi", "wx")]
+    return np.array(y)
+
+
+@pytest.mark.parametrize("reference_point", [True, False])
+def test_tmeasy_nr_jacobian_matches_central_differences(built_lib, reference_point):
+    """The exact Jacobian of the 18-DOF model with TMeasyNr tires (packed order without deflection
+    states: omega x 4, crank, x, y, u, v, psi, wz, phi, wx) against central differences of the
+    reference algorithm's TMeasyNr right-hand side, with the TMeasy test's tolerance."""
+    n = 48
+    cls, p, states, ctl = _nr_states(n, seed=17)
+    sol = built_lib.d18SolverHalfImplicitGPU(n)
+    sol.construct_class(cls, np.repeat(p[None], n, axis=0), 1)
+    sol.set_states(states)
+    js, ju = sol.rhs_jacobian(ctl[0], ctl[1], ctl[2], reference_point=reference_point)
+    sol.close()
+    tc = bool(cls.tcbool)
+    assert js.shape[1:] == (13 if tc else 12,) * 2 and ju.shape[2] == 2
+    errs, errs_u = [], []
+    for i in range(n):
+        y = _pack_nr(states[i], tc)
+        full = None if reference_point else states[i]
+        steps = 1e-6 * np.maximum(np.abs(y), 1e-2)
+        J, Ju = _fd(cls, p, y, ctl[:, i], full, steps, tire_type=1)
+        errs.append(_rel(js[i], J))
+        errs_u.append(_rel(ju[i], Ju))
+    e, eu = np.concatenate(errs), np.concatenate(errs_u)
+    print(f"TMeasyNr state Jacobian ({e.size} nonzero entries): median {np.median(e):.1e}, "
+          f"95% {np.quantile(e, 0.95):.1e}; controls: median {np.median(eu):.1e}, 95% {np.quantile(eu, 0.95):.1e}")
+    assert np.median(e) <= 1e-6 and (e <= 1e-5).mean() >= 0.95
+    assert np.median(eu) <= 1e-6 and (eu <= 1e-5).mean() >= 0.95
+
+
+def test_tmeasy_nr_exact_against_the_reference_scheme(built_lib):
+    """Exact and difference-scheme TMeasyNr Jacobians of the same vehicles agree to the scheme's
+    truncation error."""
+    n = 32
+    cls, p, states, ctl = _nr_states(n, seed=4)
+    sol = built_lib.d18SolverHalfImplicitGPU(n)
+    sol.construct_class(cls, np.repeat(p[None], n, axis=0), 1)
+    sol.set_states(states)
+    ex, _ = sol.rhs_jacobian(ctl[0], ctl[1], 0.0)
+    fd, _ = sol.rhs_jacobian_fd(ctl[0], ctl[1], 0.0)
+    sol.close()
+    e = np.concatenate([_rel(fd[i], ex[i]) for i in range(n)])
+    print(f"TMeasyNr difference scheme vs exact ({e.size} entries): median {np.median(e):.1e}")
     assert np.median(e) <= 1e-4
 
 
