@@ -46,7 +46,7 @@ typedef enum { LFDM_MODEL_11 = 11, LFDM_MODEL_18 = 18, LFDM_MODEL_24 = 24 } lfdm
 typedef enum { LFDM_TIRE_TMEASY = 0, LFDM_TIRE_TMEASY_NR = 1 } lfdm_tire_type;
 
 /* Arithmetic of the stepper. FP64 reproduces the reference; MIXED runs the RHS and tire math in  */
-/* FP32 and keeps FP64 in the X/Y/yaw accumulation and the low-speed slip normalisation.          */
+/* FP32 and keeps FP64 in the X/Y/yaw accumulation and the tire slip and transport velocities.   */
 typedef enum { LFDM_PREC_FP64 = 0, LFDM_PREC_MIXED = 1 } lfdm_precision;
 
 /* ------------------------------------------------------------------------------------------ */

@@ -4,8 +4,9 @@
 //     tire deflections) — increments of ~1e-3 relative would otherwise drift in FP32;
 //   * the global X/Y/yaw accumulation, with the yaw angle reduced to [-pi, pi] in FP64 before
 //     its FP32 sine/cosine;
-//   * the TMeasy low-speed slip normalisation: vsx - omega*r_eff (a cancellation of two large
-//     numbers at speed) and its division by vta = r_eff*|omega| + 0.01 (dof18_gpu.cu:424-431).
+//   * the TMeasy slip velocity vsx - omega*r_eff (a cancellation of two large numbers at speed) and
+//     the transport velocity vta = r_eff*|omega| + 0.01 (dof18_gpu.cu:424-431), rounded to FP32
+//     before the slips are formed.
 // Same algorithm and branch structure as dof18_device.cuh (the FP64 form), which is its oracle.
 #pragma once
 
@@ -131,7 +132,7 @@ struct TireAuxF {
     float dOmega, xt, rStat, fx, fy, fz, vsx, vsy, My, engTor;
 };
 
-// computeTireRHS, TMeasy (dof18_gpu.cu:379-530): FP32 except the slip normalisation.
+// computeTireRHS, TMeasy (dof18_gpu.cu:379-530): FP32 except the slip and transport velocities.
 template <bool kSteered>
 __device__ __forceinline__ void tire_rhs_tm_mixed(TireM& ts, TireAuxF& ta, const KViewF& K, float c, float s) {
     float fz = ta.fz;
@@ -157,17 +158,25 @@ __device__ __forceinline__ void tire_rhs_tm_mixed(TireM& ts, TireAuxF& ta, const
     } else {
         r_eff = fmaf(K(K_RDCRIT), ta.xt, ta.rStat);
     }
-    // FP64 island: slip velocity and its normalisation by the transport velocity
+    // FP64 island: the slip velocity (a difference of nearly equal terms near rolling without slip)
+    // and the transport velocity
     const double r_d = (double)r_eff;
     const double vsx_d = fma(-omega, r_d, (double)ta.vsx);
     const double vta_d = fma(r_d, fabs(omega), 0.01);
-    const float sx = (float)(-vsx_d / vta_d);
     const float vsx = (float)vsx_d;
     const float vta = (float)vta_d;
+    const float sx = -vsx / vta;
     const float rw = vta - 0.01f;
     float sy;
-    if (kSteered) sy = -(vsy * c - vta * s) / (vta * c + vsy * s);
-    else sy = -vsy / vta;
+    if (kSteered) {
+        // -tan(atan2(vsy, vta) - delta): infinite where the steered wheel's slip angle passes 90 degrees
+        // (vta c + vsy s = 0), a denominator FP32 can round to exactly 0; the slip is held to +-1e6,
+        // where the force curve is saturated and the force direction is the FP64 one to FP32 rounding.
+        sy = -(vsy * c - vta * s) / (vta * c + vsy * s);
+        sy = fminf(fmaxf(sy, -1e6f), 1e6f);
+    } else {
+        sy = -vsy / vta;
+    }
     fz = fminf(fz, K(K_PNMAX));
     const float fzn = fz * K(K_INVPN);
     const float dfx0 = fzn * fmaf(-K(K_Q2DFX0), fzn, K(K_Q1DFX0));
