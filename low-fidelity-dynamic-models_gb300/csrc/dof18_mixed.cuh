@@ -71,6 +71,12 @@ __device__ __forceinline__ float sine_stepf(float x, float x1, float y1, float x
 }
 
 __device__ __forceinline__ float sgnf_(float v) { return (float)((0.f < v) - (v < 0.f)); }
+// Sign of a double as a float (-1, 0, +1) from its bit pattern: integer-pipe instructions in place of
+// two FP64 comparisons.
+__device__ __forceinline__ float sgnf_of_d(double v) {
+    const long long b = __double_as_longlong(v);
+    return (b << 1) == 0 ? 0.f : (b < 0 ? -1.f : 1.f);
+}
 
 // FP32 view of the derived constants: KF(i).
 struct KViewF {
@@ -217,7 +223,7 @@ __device__ __forceinline__ void tire_rhs_tm_mixed(TireM& ts, TireAuxF& ta, const
     const float ss = hyp(sxs * cax, sys * say);
     float f, fos;
     tmxyf(f, fos, sc, df0, sm, fm, ss, fs);
-    ta.My = -K(K_RR) * fz * ta.rStat * (float)((0. < omega) - (omega < 0.));
+    ta.My = -K(K_RR) * fz * ta.rStat * sgnf_of_d(omega);
     const float vtxs = fmaf(rw, hsxn, 0.01f);
     const float vtys = fmaf(rw, hsyn, 0.01f);
     const float cx = K(K_CX), cy = K(K_CY), dx = K(K_DX), dy = K(K_DY);
