@@ -331,6 +331,14 @@ int lfdm_rhs_jacobian18(lfdm_solver* h, const double* ctl, int reference_point, 
 int lfdm_rhs_jacobian_fd(lfdm_solver* h, const double* ctl, int reference_point, double* jac_state, double* jac_ctl,
                          int* ny);
 
+/* Either Jacobian with HOST buffers, laid out per vehicle as the reference's CPU solvers return     */
+/* them (GetJacobianState / GetJacobianControls): ctl [3][N] = {steering, throttle, braking},       */
+/* jac_state [N][ny][ny], jac_ctl [N][ny][2]. exact = 1 selects lfdm_rhs_jacobian18 (18-DOF), 0 the */
+/* reference's difference scheme (lfdm_rhs_jacobian_fd). With jac_state and jac_ctl both NULL only  */
+/* *ny is set (ny <= 36 for every model).                                                           */
+int lfdm_rhs_jacobian_host(lfdm_solver* h, int exact, const double* ctl, int reference_point, double* jac_state,
+                           double* jac_ctl, int* ny);
+
 /* ------------------------------------------------------------------------------------------ */
 /* Mixed-DOF fleets (no counterpart class in the reference, whose solvers hold one model and one */
 /* end time each: d18SolverHalfImplicitGPU, d24SolverHalfImplicitGPU). A fleet holds 18-DOF and   */

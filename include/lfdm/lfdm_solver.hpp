@@ -69,6 +69,15 @@ inline void check(int rc, const lfdm_solver* h, const char* what) {
 #endif
 }
 
+// An argument error found by the wrapper itself, reported like the library's.
+inline void check_message(const char* what, const char* msg) {
+#ifdef LFDM_CPP_THROW
+    throw std::runtime_error(std::string(what) + ": " + msg);
+#else
+    std::fprintf(stderr, "lfdm: %s: %s\n", what, msg);
+#endif
+}
+
 inline int tire_code(TireType t) { return t == TireType::TMeasyNr ? LFDM_TIRE_TMEASY_NR : LFDM_TIRE_TMEASY; }
 
 // Copy between a struct's double fields (listed as member pointers, in the struct's field order)
@@ -145,6 +154,49 @@ class SolverBase {
         int t = LFDM_TIRE_TMEASY;
         check(lfdm_get_tire_type(h_, &t), h_, "GetTireType");
         return t == LFDM_TIRE_TMEASY_NR ? TireType::TMeasyNr : TireType::TMeasy;
+    }
+    // Extension: right-hand-side Jacobians of every vehicle at its current state, each as the
+    // reference's CPU solver returns one (GetJacobianState / GetJacobianControls after
+    // IntegrateStepWithJacobian): jac_state[i] is vehicle i's ny x ny matrix, jac_controls[i] its ny x 2
+    // one, in the packed order. exact: the exact Jacobian (18-DOF model) instead of the reference's
+    // central differences; reference_point: the packed states in a fresh state, as PerturbRhsFun.
+    // Controls hold one value per vehicle. Returns ny (0 on error).
+    int GetRhsJacobians(const std::vector<double>& steering, const std::vector<double>& throttle,
+                        const std::vector<double>& braking,
+                        std::vector<std::vector<std::vector<double>>>& jac_state,
+                        std::vector<std::vector<std::vector<double>>>& jac_controls, bool exact = false,
+                        bool reference_point = true) {
+        unsigned int total = 0, constructed = 0, initialized = 0;
+        int rc = lfdm_get_num_vehicles(h_, &total, &constructed, &initialized);
+        check(rc, h_, "GetRhsJacobians");
+        const std::size_t n = total;
+        if (rc != LFDM_OK || steering.size() != n || throttle.size() != n || braking.size() != n) {
+            if (rc == LFDM_OK) check_message("GetRhsJacobians", "one control value per vehicle is needed");
+            return 0;
+        }
+        int ny = 0;
+        rc = lfdm_rhs_jacobian_host(h_, exact ? 1 : 0, nullptr, 0, nullptr, nullptr, &ny);
+        check(rc, h_, "GetRhsJacobians");
+        if (rc != LFDM_OK) return 0;
+        std::vector<double> ctl;
+        ctl.reserve(3 * n);
+        ctl.insert(ctl.end(), steering.begin(), steering.end());
+        ctl.insert(ctl.end(), throttle.begin(), throttle.end());
+        ctl.insert(ctl.end(), braking.begin(), braking.end());
+        const std::size_t m = static_cast<std::size_t>(ny);
+        std::vector<double> js(n * m * m), ju(n * m * 2);
+        rc = lfdm_rhs_jacobian_host(h_, exact ? 1 : 0, ctl.data(), reference_point ? 1 : 0, js.data(), ju.data(), &ny);
+        check(rc, h_, "GetRhsJacobians");
+        if (rc != LFDM_OK) return 0;
+        jac_state.assign(n, std::vector<std::vector<double>>(m, std::vector<double>(m)));
+        jac_controls.assign(n, std::vector<std::vector<double>>(m, std::vector<double>(2)));
+        for (std::size_t i = 0; i < n; ++i)
+            for (std::size_t r = 0; r < m; ++r) {
+                for (std::size_t c = 0; c < m; ++c) jac_state[i][r][c] = js[(i * m + r) * m + c];
+                jac_controls[i][r][0] = ju[(i * m + r) * 2];
+                jac_controls[i][r][1] = ju[(i * m + r) * 2 + 1];
+            }
+        return ny;
     }
     // Extension: the C-ABI handle, for the lfdm_* calls that have no method here (per-vehicle
     // parameters, states and controls, response buffers, precision, timing).

@@ -98,6 +98,7 @@ def _sig(lib):
         "lfdm_traj18_last_ms": ([vp, _c_dp, _c_dp], i),
         "lfdm_rhs_jacobian18": ([vp, vp, i, vp, vp, ctypes.POINTER(i)], i),
         "lfdm_rhs_jacobian_fd": ([vp, vp, i, vp, vp, ctypes.POINTER(i)], i),
+        "lfdm_rhs_jacobian_host": ([vp, i, vp, i, vp, vp, ctypes.POINTER(i)], i),
         "lfdm_fleet_create": ([i, ctypes.POINTER(vp)], i),
         "lfdm_fleet_destroy": ([vp], i),
         "lfdm_fleet_last_error": ([vp], cp),

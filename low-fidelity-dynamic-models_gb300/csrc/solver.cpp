@@ -115,6 +115,8 @@ struct lfdm_solver {
     DevBuf<unsigned> d_bad;
     // differentiable rollout (lfdm_traj18_*)
     DevBuf<double> d_adj_ckpt, d_adj_tape;
+    // right-hand-side Jacobians with host buffers (lfdm_rhs_jacobian_host)
+    DevBuf<double> d_jac_in, d_jac_s, d_jac_u;
     unsigned adj_nsteps = 0, adj_ckpt = 0;
     bool adj_valid = false;
     double adj_fwd_ms = 0, adj_bwd_ms = 0;
@@ -1085,6 +1087,37 @@ int lfdm_rhs_jacobian_fd(lfdm_solver* h, const double* ctl, int reference_point,
     CK(launch_rhs_jacobian_fd(A, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     if (ny) *ny = jac_fd_ny(A.model, A.tire_nr != 0, tc != 0);
+    return LFDM_OK;
+}
+
+int lfdm_rhs_jacobian_host(lfdm_solver* h, int exact, const double* ctl, int reference_point, double* jac_state,
+                           double* jac_ctl, int* ny) {
+    if (!h) return LFDM_ERR_ARG;
+    if (h->classes.empty()) return h->fail(LFDM_ERR_STATE, "no vehicles constructed");
+    const bool nr = h->tire_type == LFDM_TIRE_TMEASY_NR;
+    const int m = jac_fd_ny((int)h->model, nr, h->classes[0].tcbool != 0);
+    if (ny) *ny = m;
+    if (!jac_state && !jac_ctl) return LFDM_OK;  // size query
+    if (!ctl || !jac_state || !jac_ctl) return h->fail(LFDM_ERR_ARG, "null array");
+    const size_t n = h->N, mm = (size_t)m * m;
+    CK(h->d_jac_in.ensure(3 * n));
+    CK(h->d_jac_s.ensure(mm * n));
+    CK(h->d_jac_u.ensure((size_t)m * 2 * n));
+    CK(cudaMemcpyAsync(h->d_jac_in.p, ctl, 3 * n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    int got = 0;
+    const int rc = exact ? lfdm_rhs_jacobian18(h, h->d_jac_in.p, reference_point, h->d_jac_s.p, h->d_jac_u.p, &got)
+                         : lfdm_rhs_jacobian_fd(h, h->d_jac_in.p, reference_point, h->d_jac_s.p, h->d_jac_u.p, &got);
+    if (rc) return rc;
+    if (got != m) return h->fail(LFDM_ERR_STATE, "unexpected Jacobian size");
+    // device [r][c][vehicle] -> host [vehicle][r][c]
+    std::vector<double> s_host(mm * n), u_host((size_t)m * 2 * n);
+    CK(cudaMemcpyAsync(s_host.data(), h->d_jac_s.p, s_host.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(u_host.data(), h->d_jac_u.p, u_host.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (size_t rc2 = 0; rc2 < mm; ++rc2)
+        for (size_t i = 0; i < n; ++i) jac_state[i * mm + rc2] = s_host[rc2 * n + i];
+    for (size_t rc2 = 0; rc2 < (size_t)m * 2; ++rc2)
+        for (size_t i = 0; i < n; ++i) jac_ctl[i * m * 2 + rc2] = u_host[rc2 * n + i];
     return LFDM_OK;
 }
 

@@ -8,9 +8,11 @@
 //   dropin_demo solve 11 <veh> <tire> - <driver> <n> <tend>
 //   dropin_demo solve 24 <veh> <tire> <sus> <driver> <n> <tend>
 //   dropin_demo step <veh> <tire> <n>
+//   dropin_demo jac <veh> <tire> <n>
 #include <cstdio>
 #include <cstdlib>
 #include <string>
+#include <vector>
 
 #include "dof11_halfImplicit_gpu.cuh"
 #include "dof18_halfImplicit_gpu.cuh"
@@ -141,6 +143,41 @@ static int step18(const char* veh, const char* tire, unsigned n) {
     return 0;
 }
 
+// The extension GetRhsJacobians after one SolveStep window: every entry of the last vehicle's
+// matrices, by the reference's difference scheme and exactly.
+static int jac18(const char* veh, const char* tire, unsigned n) {
+    d18SolverHalfImplicitGPU solver(n);
+    solver.Construct(veh, tire, n);
+    solver.SetTimeStep(1e-3);
+    solver.SetKernelSimTime(0.2);
+    d18GPU::VehicleState veh_st;
+    veh_st._u = 8.0;
+    d18GPU::TMeasyState tirelf_st, tirerf_st, tirelr_st, tirerr_st;
+    tirelf_st._omega = tirerf_st._omega = tirelr_st._omega = tirerr_st._omega = 8.0 / 0.47;
+    solver.Initialize(veh_st, tirelf_st, tirerf_st, tirelr_st, tirerr_st, n);
+    solver.SolveStep(0.0, 0.1, 0.5, 0.0);
+    std::vector<double> st(n), th(n), br(n, 0.0);
+    for (unsigned i = 0; i < n; ++i) {
+        st[i] = 0.05 * i;
+        th[i] = 0.3;
+    }
+    std::vector<std::vector<std::vector<double>>> js, ju;
+    for (int exact = 0; exact < 2; ++exact) {
+        const int ny = solver.GetRhsJacobians(st, th, br, js, ju, exact != 0);
+        const char* tag = exact ? "exact" : "fd";
+        out((std::string(tag) + ".ny").c_str(), ny);
+        for (int r = 0; r < ny; ++r) {
+            for (int c = 0; c < ny; ++c)
+                out((std::string(tag) + ".s." + std::to_string(r) + "." + std::to_string(c)).c_str(), js[n - 1][r][c]);
+            out((std::string(tag) + ".u." + std::to_string(r) + ".0").c_str(), ju[n - 1][r][0]);
+            out((std::string(tag) + ".u." + std::to_string(r) + ".1").c_str(), ju[n - 1][r][1]);
+        }
+    }
+    // a control vector of the wrong length is reported and nothing is computed
+    out("bad_size", solver.GetRhsJacobians(std::vector<double>(1), th, br, js, ju));
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc >= 9 && std::string(argv[1]) == "solve") {
         const int model = std::atoi(argv[2]);
@@ -151,6 +188,7 @@ int main(int argc, char** argv) {
         if (model == 24) return solve24(argv[3], argv[4], argv[5], argv[6], n, tend);
     }
     if (argc >= 5 && std::string(argv[1]) == "step") return step18(argv[2], argv[3], (unsigned)std::atoi(argv[4]));
+    if (argc >= 5 && std::string(argv[1]) == "jac") return jac18(argv[2], argv[3], (unsigned)std::atoi(argv[4]));
     std::fprintf(stderr, "usage: see the header of dropin_demo.cpp\n");
     return 2;
 }

@@ -182,3 +182,38 @@ def test_dropin_solve_step_scalar_and_functor(built_lib, golden18, demo, tmp_pat
         assert got[f"last.{k}"] == s[A.S[k]], k
     assert "lfdm: Initialize:" in err and got["after_error"] == 1.0
     sol.close()
+
+
+@pytest.mark.gpu
+def test_dropin_rhs_jacobians_match_binding(built_lib, golden18, demo, tmp_path):
+    """GetRhsJacobians (the C++ method over lfdm_rhs_jacobian_host, per-vehicle matrices as the
+    reference's GetJacobianState / GetJacobianControls) returns the binding's device Jacobians bit
+    for bit, for the difference scheme and the exact Jacobian; a control vector of the wrong length
+    is refused."""
+    case = _case(golden18, "hmmwv_acc3_gpu")
+    vj, tj = _write(tmp_path, "v.json", case["vehicle"]), _write(tmp_path, "t.json", case["tire"])
+    n = 6
+    got, err = _run(demo, "jac", vj, tj, n)
+    sol = built_lib.d18SolverHalfImplicitGPU(n)
+    sol.Construct(vj, tj, n)
+    sol.SetTimeStep(1e-3)
+    sol.SetKernelSimTime(0.2)
+    s0 = np.zeros(built_lib.S_COUNT)
+    A = pkg_mod("_abi")
+    s0[A.S["u"]] = 8.0
+    for k in range(4):
+        s0[A.S_TIRE0 + k * A.S_TIRE_STRIDE + A.T["omega"]] = 8.0 / 0.47
+    sol.Initialize(s0, n)
+    sol.SolveStep(0.0, 0.1, 0.5, 0.0)
+    st = 0.05 * np.arange(n)
+    for tag, fn in (("fd", sol.rhs_jacobian_fd), ("exact", sol.rhs_jacobian)):
+        js, ju = fn(st, np.full(n, 0.3), np.zeros(n))
+        ny = js.shape[1]
+        assert got[f"{tag}.ny"] == ny
+        for r in range(ny):
+            for c in range(ny):
+                assert got[f"{tag}.s.{r}.{c}"] == js[n - 1, r, c], (tag, r, c)
+            assert got[f"{tag}.u.{r}.0"] == ju[n - 1, r, 0] and got[f"{tag}.u.{r}.1"] == ju[n - 1, r, 1]
+    assert got["bad_size"] == 0 and "one control value per vehicle" in err
+    sol.close()
+
