@@ -135,3 +135,22 @@ def test_threaded_batch_equals_the_single_vehicle_jacobians(model):
     for i in range(n):
         a, b = O.jacobian_fd(model, 0, f["cls"][0], f["params"][i], f["states"][i], ctl[:, i], full_point=True)
         assert np.array_equal(js[i], a) and np.array_equal(jc[i], b)
+
+
+@pytest.mark.parametrize("model", [11, 18, 24])
+def test_threaded_batch_tmeasy_nr(model):
+    """The batch entry with TMeasyNr tires (golden Sedan state, spread controls) equals the single-
+    vehicle restatement, at the fresh and the full evaluation point."""
+    case = [c for c in _cases(model) if c["tire_type"] == 1][0]
+    cls, p, _, _ = INPUTS[model](case)
+    n = 8
+    states = np.repeat(np.array(case["expected_final"])[None], n, axis=0)
+    rng = np.random.default_rng(model + 100)
+    ctl = np.stack([rng.uniform(-0.3, 0.3, n), rng.uniform(0.0, 1.0, n), rng.uniform(0.0, 0.2, n)])
+    params = np.repeat(p[None], n, axis=0)
+    for full in (False, True):
+        js, jc = O.jacobian_fd_batch(model, 1, cls, params, states, ctl, full_point=full, nthreads=3)
+        for i in range(n):
+            a, b = O.jacobian_fd(model, 1, cls, p, states[i], ctl[:, i], full_point=full)
+            assert np.array_equal(js[i], a) and np.array_equal(jc[i], b)
+
