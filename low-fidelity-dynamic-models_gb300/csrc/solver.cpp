@@ -24,6 +24,7 @@
 #include <random>
 #include <sstream>
 #include <string>
+#include <new>
 #include <vector>
 
 #include "../../include/lfdm.h"
@@ -1110,7 +1111,13 @@ int lfdm_rhs_jacobian_host(lfdm_solver* h, int exact, const double* ctl, int ref
     if (rc) return rc;
     if (got != m) return h->fail(LFDM_ERR_STATE, "unexpected Jacobian size");
     // device [r][c][vehicle] -> host [vehicle][r][c]
-    std::vector<double> s_host(mm * n), u_host((size_t)m * 2 * n);
+    std::vector<double> s_host, u_host;
+    try {
+        s_host.resize(mm * n);
+        u_host.resize((size_t)m * 2 * n);
+    } catch (const std::bad_alloc&) {
+        return h->fail(LFDM_ERR_CAPACITY, "no host memory to stage the Jacobians");
+    }
     CK(cudaMemcpyAsync(s_host.data(), h->d_jac_s.p, s_host.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaMemcpyAsync(u_host.data(), h->d_jac_u.p, u_host.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
