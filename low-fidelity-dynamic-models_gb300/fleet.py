@@ -109,12 +109,13 @@ def jitter_params(base: np.ndarray, n: int, rng: np.random.Generator, frac: floa
 
 def driver_tables(n: int, rng: np.random.Generator, horizon: float, table_dt: float = 0.01,
                   max_steer: np.ndarray | float = 0.6, brake_pulse: bool = True,
-                  dtype=np.float64) -> np.ndarray:
-    """[n][rows][4] tables {t, steering, throttle, braking}, rows = horizon/table_dt + 1."""
+                  dtype=np.float64, amplitude: float = 0.5) -> np.ndarray:
+    """[n][rows][4] tables {t, steering, throttle, braking}, rows = horizon/table_dt + 1; the steering
+    wheel-angle amplitude is drawn from U[0, amplitude] rad."""
     rows = int(round(horizon / table_dt)) + 1
     t = (np.arange(rows, dtype=np.float64) / round(1.0 / table_dt)) if abs(1.0 / table_dt - round(1.0 / table_dt)) < 1e-9 \
         else np.arange(rows, dtype=np.float64) * table_dt
-    A = rng.uniform(0.0, 0.5, size=n)
+    A = rng.uniform(0.0, amplitude, size=n)
     f = rng.uniform(0.2, 1.0, size=n)
     thr = rng.uniform(0.3, 1.0, size=n)
     out = np.empty((n, rows, 4), dtype=dtype)
@@ -191,6 +192,38 @@ def fleet18(n: int, seed: int = 20261203, horizon: float = 10.0, table_dt: float
     return {"cls": [cls], "class_of": np.zeros(n, dtype=np.int32), "params": params, "tables": tables,
             "states": states, "seed": seed, "horizon": horizon}
 
+
+# Wheel inertia and brake of the calm companion fleet: an HMMWV-class wheel (the reference's HMMWV
+# tire files give jw = 6.5 kg m^2) and a 2,000 N m brake, which the 0.6 brake pulse cannot lock.
+CALM_JW = 6.5
+CALM_MAX_BRAKE_TORQUE = 2000.0
+CALM_STEER_AMPLITUDE = 0.1
+
+
+def fleet18_calm(n: int, seed: int = 20261204, horizon: float = 10.0, table_dt: float = 0.01) -> dict:
+    """A seeded 18-DOF SUV fleet whose whole trajectories are insensitive to rounding.
+
+    The parameter jitter (mass, Jz, CG position, tire stiffness, peak friction within +/-10 %), the
+    driver families (sine steering, throttle ramp, 1 s brake pulse of 0.6 at U[4, 8] s) and the
+    initial speeds U[0, 20] m/s are those of fleet18. Three things differ: the wheel inertia is
+    CALM_JW instead of 1.5 kg m^2 (a light wheel chatters in the explicit wheel-speed update at
+    dt = 1e-3), the brake torque is CALM_MAX_BRAKE_TORQUE (the brake pulse no longer locks the
+    wheels, whose sgn(omega) brake torque then chatters around zero speed) and the steering
+    amplitude is U[0, CALM_STEER_AMPLITUDE] rad (no vehicle spins out). On 4,096 such vehicles the
+    reference algorithm compiled with and without fused multiply-add contraction agrees to 5.3e-12
+    per state after 10 s, so any FP64 implementation must agree with it to rounding level over
+    the whole horizon."""
+    rng = np.random.default_rng(seed)
+    cls, base = suv18()
+    base = base.copy()
+    base[P["jw"]] = CALM_JW
+    base[P["maxbraketorque"]] = CALM_MAX_BRAKE_TORQUE
+    params = jitter_params(base, n, rng)
+    tables = driver_tables(n, rng, horizon, table_dt, params[:, P["maxsteer"]], True,
+                           amplitude=CALM_STEER_AMPLITUDE)
+    states = initial_states(cls, params, rng, (0.0, 20.0))
+    return {"cls": [cls], "class_of": np.zeros(n, dtype=np.int32), "params": params, "tables": tables,
+            "states": states, "seed": seed, "horizon": horizon}
 
 # The same SUV for the 24-DOF model: its JSON holds the 24-DOF keys (pitch inertia instead of the
 # roll-stiffness terms) and a suspension with ks = 4e4 N/m and bs = 4e3 N s/m at every corner.

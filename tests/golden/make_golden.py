@@ -84,6 +84,64 @@ def final_to_state(final: list[float]) -> list[float]:
     return s
 
 
+def _steer_map_for(max_steer: float) -> list:
+    """The ART vehicle's steering map (18dof-gpu/data/json/ART/vehicle.json) rescaled so that full
+    input gives the vehicle's own maximum wheel angle: a non-linear map for vehicles that ship
+    without one. The angles are rounded to 9 significant digits: the reference's JSON reader
+    (rapidjson without its full-precision flag) can round a 17-digit decimal to a neighbouring
+    double, which the reference data files, written with few digits, never meet."""
+    art = [(-1, -0.383972), (-0.8, -0.301942), (-0.6, -0.2199115), (-0.4, -0.151844), (-0.2, -0.0314159), (0, 0),
+           (0.2, 0.0314159), (0.4, 0.151844), (0.6, 0.2199115), (0.8, 0.301942), (1, 0.383972)]
+    return [[x, float(f"{y * max_steer / 0.383972:.9g}")] for x, y in art]
+
+
+def fixture_cases(data: str, model: int) -> list:
+    """Branch fixtures of one model from the reference's data files under `data` (<model>dof-gpu/data):
+    (name, vehicle, tire, tire type, driver file, ksim, tend, source). They cover the steering map
+    (vehToTireTransform's getMapY branch), throttleMod (driveTorque's scaled map), the 2WD torque split
+    to the rear or the front axle in computePowertrainRHS, and vehicles without a torque converter."""
+    j = lambda *p: json.load(open(os.path.join(data, "json", *p)))  # noqa: E731
+    out = []
+    pre = {18: "", 11: "11", 24: "24"}[model]
+    if model in (18, 11):
+        art_v, art_t = j("ART", "vehicle.json"), j("ART", "tmeasy.json")
+        out += [(f"art{pre}_ls5_gpu", art_v, art_t, 0, "long_sine5", 2.0, 20.0, "ART vehicle.json + tmeasy.json"),
+                (f"art{pre}_dl4_cpu", art_v, art_t, 0, "double_lane4", 0.0, None, "ART vehicle.json + tmeasy.json")]
+        audi_v, audi_rwd, audi_t = j("audi", "vehicle.json"), j("audi", "vehicle_RWD.json"), j("audi", "tmeasy.json")
+        audi_fwd = dict(audi_rwd, rearWheels=False)
+        out += [(f"audi{pre}_dl4_gpu", audi_v, audi_t, 0, "double_lane4", 2.0, 22.0, "audi vehicle.json + tmeasy.json"),
+                (f"audi{pre}_rwd_ls5_gpu", audi_rwd, audi_t, 0, "long_sine5", 1.0, 20.0,
+                 "audi vehicle_RWD.json + tmeasy.json"),
+                (f"audi{pre}_rwd_st3_cpu", audi_rwd, audi_t, 0, "st3_right", 0.0, None,
+                 "audi vehicle_RWD.json + tmeasy.json"),
+                (f"audi{pre}_fwd_ls5_gpu", audi_fwd, audi_t, 0, "long_sine5", 2.0, 20.0,
+                 "audi vehicle_RWD.json with rearWheels false (front-wheel drive) + tmeasy.json")]
+    sedan_v = j("Sedan", "vehicle.json")
+    # 24dof-gpu/data/json/Sedan/vehicle_RWD.json is an 18-DOF file (no "jy"; the reference's 24-DOF
+    # loader reads d["jy"] unconditionally, 24dof-gpu/dof24_gpu.cu:2237), so the 24-DOF rear-wheel-drive
+    # Sedan is the 24-DOF vehicle.json with "4wd" false
+    sedan_rwd = j("Sedan", "vehicle_RWD.json") if model != 24 else dict(sedan_v, **{"4wd": False})
+    sedan_t, sedan_nr = j("Sedan", "tmeasy.json"), j("Sedan", "tmeasyNr.json")
+    out += [(f"sedan{pre}_rwd_ls5_gpu", sedan_rwd, sedan_t, 0, "long_sine5", 2.0, 20.0,
+             "Sedan vehicle_RWD.json + tmeasy.json"),
+            (f"sedan{pre}_rwd_nr_acc05_gpu", sedan_rwd, sedan_nr, 1, "acc05", 2.0, 10.0,
+             "Sedan vehicle_RWD.json + tmeasyNr.json")]
+    hm = j("HMMWV", "vehicle.json")
+    hm_mod = dict(hm, throttleMod=True, nonLinearSteer=True, steerMap=_steer_map_for(hm["maxSteer"]))
+    out += [(f"hmmwv{pre}_tmod_nls_ls5_gpu", hm_mod, j("HMMWV", "tmeasy.json"), 0, "long_sine5", 2.0, 20.0,
+             "HMMWV vehicle.json with throttleMod and a steering map + tmeasy.json")]
+    sedan_mod = dict(sedan_v, throttleMod=True, nonLinearSteer=True, steerMap=_steer_map_for(sedan_v["maxSteer"]))
+    out += [(f"sedan{pre}_tmod_nls_nr_dl4_gpu", sedan_mod, sedan_nr, 1, "double_lane4", 2.0, 22.0,
+             "Sedan vehicle.json with throttleMod and a steering map + tmeasyNr.json")]
+    if model == 24:
+        out += [("sedan24_tm_dl4_gpu", sedan_v, sedan_t, 0, "double_lane4", 2.0, 22.0, "Sedan vehicle.json + tmeasy.json"),
+                ("sedan24_rwd_st3_cpu", sedan_rwd, sedan_t, 0, "st3_right", 0.0, None,
+                 "Sedan vehicle.json with 4wd false + tmeasy.json"),
+                ("sedan24_fwd_ls5_gpu", dict(sedan_rwd, rearWheels=False), sedan_t, 0, "long_sine5", 2.0, 20.0,
+                 "Sedan vehicle.json with 4wd and rearWheels false (front-wheel drive) + tmeasy.json")]
+    return out
+
+
 def main(ref: str) -> None:
     d18 = os.path.join(ref, "18dof-gpu", "data")
     veh_hmmwv = json.load(open(os.path.join(d18, "json", "HMMWV", "vehicle.json")))
@@ -134,16 +192,52 @@ def main(ref: str) -> None:
             meta.append({"name": name, "vehicle": veh_sedan, "tire": tire_sedan, "tire_type": 1, "driver": rows,
                          "dt": 0.001, "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
                          "state": [0.0] * abi.S_COUNT, "source": "Sedan vehicle.json + tmeasyNr.json, acc05.txt"})
-        # seeded synthetic SUV fleet (GPU schedule, 1 s windows)
-        n_syn = 12
-        fl = fleet.fleet18(n_syn, seed=SEED, horizon=10.0)
-        sj, stj = write_json("suv_vehicle.json", fleet.SUV18_VEHICLE), write_json("suv_tire.json", fleet.SUV_TIRE)
-        _, base = fleet.suv18()
         P = abi.P
         vfields = ["m", "jz", "a", "b"]
         tfields = ["kt"] + list(fleet.FRICTION_FIELDS)
         key = {"fxmpn": "fxmPn", "fxmp2n": "fxmP2n", "fxspn": "fxsPn", "fxsp2n": "fxsP2n", "fympn": "fymPn",
                "fymp2n": "fymP2n", "fyspn": "fysPn", "fysp2n": "fysP2n", "kt": "kt"}
+        # Branch fixtures: the reference's ART (steering map, throttleMod, no converter, one gear),
+        # Sedan and audi rear-wheel-drive files (2WD torque split) and audi 4WD files, plus the HMMWV
+        # with throttleMod and a steering map switched on (the branches with a torque converter).
+        for name, veh, tire, tt, drv, ksim, tend, src in fixture_cases(d18, 18):
+            rows = lfdm.params.load_driver_table(os.path.join(d18, "input", drv + ".txt")).tolist()
+            tp = write_table(f"{name}.txt", rows)
+            vjx, tjx = write_json(f"{name}_v.json", veh), write_json(f"{name}_t.json", tire)
+            tend_v = tend if tend is not None else rows[-1][0]
+            jobs += [f"veh {vjx}", f"tire {tjx}", f"tiretype {tt}", f"driver {tp}", "dt 0.001",
+                     f"tend {_fmt(tend_v)}", f"ksim {_fmt(ksim)}", "sample 100", "jac 0", "run"]
+            meta.append({"name": name, "vehicle": veh, "tire": tire, "tire_type": tt, "driver": rows, "dt": 0.001,
+                         "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
+                         "state": [0.0] * abi.S_COUNT, "source": src + f", {drv}.txt"})
+        # the calm companion fleet (rounding-insensitive over the whole horizon)
+        n_calm = 6
+        fc = fleet.fleet18_calm(n_calm, horizon=10.0)
+        cvj = write_json("calm_vehicle.json", fleet.SUV18_VEHICLE)
+        calm_tire = dict(fleet.SUV_TIRE, jw=fleet.CALM_JW)
+        ctj = write_json("calm_tire.json", calm_tire)
+        for i in range(n_calm):
+            rows = fc["tables"][i].tolist()
+            tp = write_table(f"calm_{i}.txt", rows)
+            vp = {k: float(fc["params"][i, P[k]]) for k in vfields}
+            vp["maxBrakeTorque"] = float(fc["params"][i, P["maxbraketorque"]])
+            tpv = {key[k]: float(fc["params"][i, P[k]]) for k in tfields}
+            st = fc["states"][i]
+            lines = [f"veh {cvj}", f"tire {ctj}", "tiretype 0", f"driver {tp}", "dt 0.001", "tend 10",
+                     "ksim 1", "sample 250"]
+            lines += [f"vp {k} {_fmt(v)}" for k, v in vp.items()] + [f"tp {k} {_fmt(v)}" for k, v in tpv.items()]
+            lines += [f"vs u {_fmt(st[abi.S['u']])}", f"vs crankOmega {_fmt(st[abi.S['crankomega']])}",
+                      f"gear {int(st[abi.S['current_gr']])}"]
+            lines += [f"ts {k} omega {_fmt(st[abi.S_TIRE0 + abi.T['omega']])}" for k in range(4)] + ["jac 0", "run"]
+            jobs += lines
+            meta.append({"name": f"calm_fleet_{i}", "vehicle": fleet.SUV18_VEHICLE, "tire": calm_tire,
+                         "tire_type": 0, "driver": rows, "dt": 0.001, "tend": 10.0, "ksim": 1.0, "sample": 250,
+                         "vp": vp, "tp": tpv, "state": st.tolist(),
+                         "source": f"calm synthetic SUV fleet seed {fc['seed']} vehicle {i}"})
+        # seeded synthetic SUV fleet (GPU schedule, 1 s windows)
+        n_syn = 12
+        fl = fleet.fleet18(n_syn, seed=SEED, horizon=10.0)
+        sj, stj = write_json("suv_vehicle.json", fleet.SUV18_VEHICLE), write_json("suv_tire.json", fleet.SUV_TIRE)
         for i in range(n_syn):
             rows = fl["tables"][i].tolist()
             tp = write_table(f"suv_{i}.txt", rows)
@@ -219,6 +313,16 @@ def main11(ref: str) -> None:
             cases.append({"name": name, "vehicle": veh_s, "tire": tire_s, "tire_type": 1, "driver": rows, "dt": 0.001,
                           "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
                           "state": [0.0] * abi.C["LFDM11_S_COUNT"], "source": "Sedan 11-DOF json, tmeasyNr, acc05.txt"})
+        for name, v, t, tt, drv, ksim, tend, src in fixture_cases(d11, 11):
+            rows = lfdm.params.load_driver_table(os.path.join(d11, "input", drv + ".txt")).tolist()
+            tp = write(f"{name}.txt", "".join(" ".join(_fmt(x) for x in r) + "\n" for r in rows))
+            vjx, tjx = write(f"{name}_v.json", json.dumps(v)), write(f"{name}_t.json", json.dumps(t))
+            tend_v = tend if tend is not None else rows[-1][0]
+            jobs += [f"veh {vjx}", f"tire {tjx}", f"tiretype {tt}", f"driver {tp}", "dt 0.001", f"tend {_fmt(tend_v)}",
+                     f"ksim {_fmt(ksim)}", "sample 100", "jac 0", "run"]
+            cases.append({"name": name, "vehicle": v, "tire": t, "tire_type": tt, "driver": rows, "dt": 0.001,
+                          "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
+                          "state": [0.0] * abi.C["LFDM11_S_COUNT"], "source": f"{src} (11-DOF files), {drv}.txt"})
         fl = fleet.fleet11(8, seed=SEED, horizon=10.0)
         sj, stj = write("sv.json", json.dumps(fleet.SUV11_VEHICLE)), write("st.json", json.dumps(fleet.SUV_TIRE))
         for i in range(8):
@@ -291,6 +395,22 @@ def main24(ref: str) -> None:
             cases.append({"name": name, "vehicle": veh_s, "tire": tire_s, "sus": sus, "tire_type": 1, "driver": rows,
                           "dt": 0.001, "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
                           "state": s_s.tolist(), "source": "Sedan 24-DOF json, tmeasyNr, HMMWV suspension, acc05.txt"})
+        sus_sedan = json.load(open(os.path.join(d24, "json", "Sedan", "suspension.json")))
+        ssj_sedan = write("s_sedan.json", json.dumps(sus_sedan))
+        for name, v, t, tt, drv, ksim, tend, src in fixture_cases(d24, 24):
+            su, suj = (sus, sj) if name.startswith("hmmwv") else (sus_sedan, ssj_sedan)
+            rows = lfdm.params.load_driver_table(os.path.join(d24, "input", drv + ".txt")).tolist()
+            tp = write(f"{name}.txt", "".join(" ".join(_fmt(x) for x in r) + "\n" for r in rows))
+            vjx, tjx = write(f"{name}_v.json", json.dumps(v)), write(f"{name}_t.json", json.dumps(t))
+            _, p_c = lfdm.params.vehicle_from_json(v, t, tt, model=24, sus=su)
+            s_c = fleet.init_tire_sus24(p_c[None], np.zeros((1, C["LFDM24_S_COUNT"])))[0]
+            tend_v = tend if tend is not None else rows[-1][0]
+            jobs += [f"veh {vjx}", f"tire {tjx}", f"sus {suj}", f"tiretype {tt}", f"driver {tp}", "dt 0.001",
+                     f"tend {_fmt(tend_v)}", f"ksim {_fmt(ksim)}", "sample 100", "jac 0", "run"]
+            cases.append({"name": name, "vehicle": v, "tire": t, "sus": su, "tire_type": tt, "driver": rows,
+                          "dt": 0.001, "tend": tend_v, "ksim": ksim, "sample": 100, "vp": {}, "tp": {},
+                          "state": s_c.tolist(),
+                          "source": f"{src} (24-DOF files), {'HMMWV' if su is sus else 'Sedan'} suspension.json, {drv}.txt"})
         fl = fleet.fleet24(8, seed=SEED, horizon=10.0)
         svj, stj, ssj = (write("sv.json", json.dumps(fleet.SUV24_VEHICLE)), write("st.json", json.dumps(fleet.SUV_TIRE)),
                          write("ss.json", json.dumps(fleet.SUV24_SUS)))
@@ -328,7 +448,10 @@ def main24(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/wheeled_vehicle_models"
+    # the reference checkout's wheeled_vehicle_models directory: argument, else $LFDM_REFERENCE, else
+    # the default checkout location
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LFDM_REFERENCE",
+                                                                "/root/reference/wheeled_vehicle_models")
     main(ref)
     main11(ref)
     main24(ref)

@@ -6,7 +6,7 @@ the floors of conftest.state_floors11(); a single window from many diverse state
 Trajectories that are rounding-chaotic (wheel chatter of the light SUV wheels) are held to
 max(1e-9, 100 x the reference algorithm's sensitivity envelope): the largest deviation, sample by
 sample, among the reference algorithm built with FMA contraction and the reference algorithm
-started from the initial state with u scaled by 1 +- 1e-15. An envelope of several perturbations
+started from the initial state with u moved by +-1e-15 max(|u|, 1 m/s). An envelope of several perturbations
 is needed because the host's libm and contraction differ between machines, so a single perturbed
 run can by chance stay close where the others (and the GPU) do not.
 """
@@ -69,7 +69,7 @@ def _perturbed_runs(cls, class_of, params, states, tables, **kw):
     out = [O.run18(cls, class_of, params, states, tables, fma=True, model=11, **kw)]
     for eps in (1e-15, -1e-15):
         s2 = np.array(states, dtype=np.float64, copy=True)
-        s2[:, U] *= 1.0 + eps
+        s2[:, U] += eps * np.maximum(np.abs(s2[:, U]), 1.0)  # relative, floored at 1 m/s (u0 may be 0)
         out.append(O.run18(cls, class_of, params, s2, tables, model=11, **kw))
     return out
 

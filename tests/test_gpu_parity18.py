@@ -13,7 +13,7 @@ no-contraction build. Those trajectories are checked three ways:
   * one window of 10 steps from many diverse states (no time for amplification): <= 1e-12;
   * full trajectories: the GPU's deviation from the reference is at most 100x the reference
     algorithm's own sensitivity (or 1e-9, whichever is larger), sample by sample: the largest
-    deviation among its FMA-contracted build and runs from u scaled by 1 +- 1e-15 (golden
+    deviation among its FMA-contracted build and runs from u moved by +-1e-15 max(|u|, 1 m/s) (golden
     trajectories), or its FMA-contracted build (seeded fleets);
   * the fraction of vehicles beyond 1e-9 is no larger than the reference's own fraction + 5%.
 """
@@ -63,7 +63,7 @@ def _run_golden_group(lfdm, cases, ksim, tend, tire_type, freq):
 
 def _envelope_responses(case, dtout):
     """The reference algorithm's responses under the perturbations of the sensitivity envelope: its
-    FMA-contracted build, and its plain build started from u scaled by 1 +- 1e-15 (a single
+    FMA-contracted build, and its plain build started from u moved by +-1e-15 max(|u|, 1 m/s) (a single
     perturbation can stay close by chance where others, and the GPU, do not)."""
     cls, p, s, tab = case_inputs(case)
     kw = dict(tire_type=case["tire_type"], dt=case["dt"], tend=case["tend"], ksim=case["ksim"], schedule=1,
@@ -72,7 +72,7 @@ def _envelope_responses(case, dtout):
     U = pkg_mod("_abi").S["u"]
     for eps in (1e-15, -1e-15):
         s2 = s.copy()
-        s2[U] *= 1.0 + eps
+        s2[U] += eps * max(abs(s2[U]), 1.0)  # relative, floored at 1 m/s (u0 may be 0)
         out.append(O.run18([cls], [0], p[None], s2[None], [tab], **kw)[1][:, :, 0])
     return out
 

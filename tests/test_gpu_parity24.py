@@ -6,7 +6,7 @@ Per state |gpu - ref| <= 1e-9 * max(|ref|, s_k) with the floors of conftest.stat
 kernel writes from a window's last step only). Rounding-chaotic trajectories (wheel chatter of the
 light SUV wheels) are held to max(1e-9, 100 x the reference algorithm's sensitivity envelope): the
 largest deviation, sample by sample, among the reference algorithm built with FMA contraction and
-started from u scaled by 1 +- 1e-15. A single window from many diverse states is held to 1e-12.
+started from u moved by +-1e-15 max(|u|, 1 m/s). A single window from many diverse states is held to 1e-12.
 
 The seeded 24-DOF SUV fleet is strongly chaotic: over 10 s about 330 of 512 vehicles of the
 reference algorithm itself move beyond 1e-9 under a 1e-15 perturbation of u, and about 40 saturate
@@ -72,7 +72,7 @@ def _perturbed_runs(cls, class_of, params, states, tables, **kw):
     out = [O.run18(cls, class_of, params, states, tables, fma=True, model=24, **kw)]
     for eps in (1e-15, -1e-15):
         s2 = np.array(states, dtype=np.float64, copy=True)
-        s2[:, U] *= 1.0 + eps
+        s2[:, U] += eps * np.maximum(np.abs(s2[:, U]), 1.0)  # relative, floored at 1 m/s (u0 may be 0)
         out.append(O.run18(cls, class_of, params, s2, tables, model=24, **kw))
     return out
 
