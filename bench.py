@@ -547,8 +547,8 @@ def run_ours(a, dist: Dist):
     # window's table rows, the response written)
     alg_bytes = n * (2 * 75 * 8 + 70 * 8 + (rows_w := int(round(ksim / 0.01)) + 1) * 32 + spw * 13 * 8)
     # DRAM bytes of one window launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu
-    # capture of this default configuration (300,000 vehicles, 1 s windows, 100 Hz outputs; the
-    # summary is profiles/window18_fp64.md); other configurations have no capture and report null
+    # capture of this default configuration (300,000 vehicles, 1 s windows, 100 Hz outputs); other
+    # configurations have no capture and report null
     traffic = 1687990272 + 3257568768 if (n == 300_000 and ksim == 1.0 and spw == 100) else None
     peaks = {}
     try:

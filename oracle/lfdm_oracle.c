@@ -753,10 +753,8 @@ static void vehToTireTransform11(Tire* t, const Veh11* v, const double* loads, c
     t[1].vsx = v->u;
 }
 
-/* tireToVehTransform: 11dof/dof11.cpp:100-124 — both front forces rotated by the wheel angle. (The  */
-/* GPU twin, 11dof-gpu/dof11_gpu.cu:98-123, computes the rotated lateral force but never stores it; */
-/* the reference's GPU test pin 104.805 m on double_lane4, tests/11dof_gpu.cu:77, holds only with    */
-/* the CPU behaviour, which is the one restated here.)                                              */
+/* tireToVehTransform: 11dof/dof11.cpp:100-124 — both front forces rotated by the wheel angle and  */
+/* stored back, as the GPU twin does too (11dof-gpu/dof11_gpu.cu:98-123, stores at :117-121).       */
 static void tireToVehTransform11(Tire* t, const Par* pp, double steering) {
     double delta = wheel_angle(pp, steering);
     double fx = t[0].fx * cos(delta) - t[0].fy * sin(delta);
