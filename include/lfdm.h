@@ -335,7 +335,9 @@ int lfdm_rhs_jacobian_fd(lfdm_solver* h, const double* ctl, int reference_point,
 /* them (GetJacobianState / GetJacobianControls): ctl [3][N] = {steering, throttle, braking},       */
 /* jac_state [N][ny][ny], jac_ctl [N][ny][2]. exact = 1 selects lfdm_rhs_jacobian18 (18-DOF), 0 the */
 /* reference's difference scheme (lfdm_rhs_jacobian_fd). With jac_state and jac_ctl both NULL only  */
-/* *ny is set (ny <= 36 for every model).                                                           */
+/* *ny is set (ny <= 36 for every model). The solver's configuration is checked first, so the size  */
+/* query fails (LFDM_ERR_ARG) for a configuration the chosen Jacobian does not support, before any   */
+/* buffer is allocated.                                                                              */
 int lfdm_rhs_jacobian_host(lfdm_solver* h, int exact, const double* ctl, int reference_point, double* jac_state,
                            double* jac_ctl, int* ny);
 
@@ -382,16 +384,22 @@ int lfdm_fleet_set_states(lfdm_fleet* f, int model, unsigned first, unsigned cou
 int lfdm_fleet_get_response(lfdm_fleet* f, int model, double* out, size_t capacity, unsigned* nsamples);
 int lfdm_fleet_get_status_words(lfdm_fleet* f, int model, uint32_t* out);
 
-/* No counterpart in the reference (its solver owns and allocates all of its memory). One 18-DOF   */
-/* FP64 window of nsteps steps of dt from t0 over n <= LFDM_NOALLOC_MAX_VEHICLES device-resident    */
-/* vehicles of one class, with per-vehicle constant controls, that allocates nothing: its scratch  */
-/* (derived constants, SoA state and controls, class table; about 20 MB) is one fixed static device */
-/* array. params [n][LFDM_P_COUNT], states [n][LFDM_S_COUNT] (in/out) and steering/throttle/braking */
+/* No counterpart in the reference (its solver owns and allocates all of its memory). For callers   */
+/* that cannot allocate device memory on their call path (a real-time control loop, a host that    */
+/* hands the GPU over with a fixed memory budget): one 18-DOF FP64 window of nsteps steps of dt     */
+/* from t0 over n <= LFDM_NOALLOC_MAX_VEHICLES device-resident vehicles of one class, with           */
+/* per-vehicle constant controls, that allocates nothing. Its scratch (derived constants, SoA state */
+/* and controls, class index and status words, class table) is one static device array of exactly   */
+/* LFDM_NOALLOC_SCRATCH_BYTES bytes (18.8 MiB), reserved on every device where the library is        */
+/* loaded. params [n][LFDM_P_COUNT], states [n][LFDM_S_COUNT] (in/out) and steering/throttle/braking */
 /* [n] are DEVICE pointers; the work is enqueued on `stream` (a cudaStream_t, NULL = legacy default */
-/* stream) and the call returns without synchronising. Larger n fails with LFDM_ERR_CAPACITY.       */
-/* Every call on a device shares that scratch, so calls that overlap on the GPU race: serialise     */
-/* them. err (err_len bytes, may be NULL) receives a message on failure.                            */
+/* stream), and the call waits for that stream at the end to read one status word: it returns       */
+/* LFDM_ERR_NUMERIC when a vehicle's state became non-finite (the states are still written back).   */
+/* Larger n fails with LFDM_ERR_CAPACITY. Every call on a device shares that scratch, so calls that  */
+/* overlap on the GPU race: serialise them. err (err_len bytes, may be NULL) receives a message on   */
+/* failure.                                                                                          */
 #define LFDM_NOALLOC_MAX_VEHICLES 16384
+#define LFDM_NOALLOC_SCRATCH_BYTES 19669504
 int lfdm_step18_noalloc(const lfdm_class18* cls, int tire_type, const double* params, double* states,
                         const double* steering, const double* throttle, const double* braking, unsigned n, double t0,
                         double dt, unsigned nsteps, void* stream, char* err, size_t err_len);

@@ -693,14 +693,18 @@ def _rollout_fn():
 
 
 NOALLOC_MAX_VEHICLES = _abi.C["LFDM_NOALLOC_MAX_VEHICLES"]
+NOALLOC_SCRATCH_BYTES = _abi.C["LFDM_NOALLOC_SCRATCH_BYTES"]
 
 
 def step18_noalloc(cls: Class18, params: int, states: int, steering: int, throttle: int, braking: int, n: int,
                    t0: float, dt: float, nsteps: int, stream: int = 0, tire_type: int = TireType.TMeasy) -> None:
     """lfdm_step18_noalloc: one FP64 18-DOF window over device-resident vehicles (device pointers,
     e.g. torch CUDA tensors' data_ptr(): params [n][P_COUNT], states [n][S_COUNT] in/out, controls
-    [n] each), enqueued on `stream` without allocating; n <= NOALLOC_MAX_VEHICLES. Calls share one
-    static scratch array per device, so calls that overlap on the GPU race."""
+    [n] each), enqueued on `stream` without allocating device memory; n <= NOALLOC_MAX_VEHICLES. For
+    callers that cannot allocate on their call path. The call waits for `stream` at the end to read
+    one status word and raises LfdmError (LFDM_ERR_NUMERIC) when a state became non-finite. Calls
+    share one static scratch array per device (NOALLOC_SCRATCH_BYTES), so calls that overlap on
+    the GPU race."""
     err = ctypes.create_string_buffer(512)
     rc = lib().lfdm_step18_noalloc(ctypes.byref(cls), int(tire_type), ctypes.c_void_p(params), ctypes.c_void_p(states),
                                    ctypes.c_void_p(steering), ctypes.c_void_p(throttle), ctypes.c_void_p(braking),

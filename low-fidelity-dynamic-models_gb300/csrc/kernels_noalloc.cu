@@ -5,20 +5,25 @@
 //
 // The window kernel needs memory beyond its inputs and outputs: the derived per-vehicle constants
 // K [K18_COUNT][npad], the SoA state [LFDM_S_COUNT][npad] it steps in place, the SoA controls
-// [3][npad], the class index per vehicle and the class table. All of that lives in ONE file-scope
-// `static __device__` array, `g_noalloc_scratch`, of a fixed size that holds kNoAllocMaxVehicles
-// vehicles; larger calls are rejected. Every call on a device shares that device's array, so
-// calls that overlap on the GPU (different streams, or host threads racing) race on it: the
-// caller serialises them. Nothing in it has to start at zero: each call writes every element it
-// later reads (the class-index words are cleared by a memset on the call's stream).
+// [3][npad], the class index and status word per vehicle, one summary status word and the class
+// table. All of that lives in ONE file-scope `static __device__` array, `g_noalloc_scratch`, of
+// exactly LFDM_NOALLOC_SCRATCH_BYTES bytes, which holds LFDM_NOALLOC_MAX_VEHICLES vehicles; larger
+// calls are rejected. The array is reserved on every device where the library's module is loaded,
+// whether or not this entry point is called. Every call on a device shares that device's array,
+// so calls that overlap on the GPU (different streams, or host threads racing) race on it: the
+// caller serialises them. The class-index, status and summary words are cleared by memsets on the
+// call's stream; every other element is written before it is read.
 //
-// Per device, at the first call with that device current, cudaGetSymbolAddress gives the array's
-// address, which is then passed to the kernels. No cudaMalloc, cudaFree, cudaMallocAsync or
-// allocating library routine is called; copies and memsets are enqueued on the caller's stream.
+// At every call, with the call's device current, cudaGetSymbolAddress gives the array's device
+// address (cheap, allocates nothing, and stays right if the device's context was torn down and
+// recreated in between), which is then passed to the kernels. No cudaMalloc, cudaFree,
+// cudaMallocAsync or allocating library routine is called; copies, memsets and kernels are
+// enqueued on the caller's stream, and the call waits for that stream at the end to read the
+// summary status word (LFDM_ERR_NUMERIC if any vehicle's state became non-finite, as in the
+// solver).
 
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 
 #include "dof18_device.cuh"
 #include "kernels.h"
@@ -36,14 +41,24 @@ constexpr size_t kOffK = 0;
 constexpr size_t kOffS = align_up(kOffK + sizeof(double) * (size_t)K18_COUNT * kNoAllocMaxVehicles);
 constexpr size_t kOffCtl = align_up(kOffS + sizeof(double) * (size_t)LFDM_S_COUNT * kNoAllocMaxVehicles);
 constexpr size_t kOffClassOf = align_up(kOffCtl + sizeof(double) * 3 * (size_t)kNoAllocMaxVehicles);
-constexpr size_t kOffClass = align_up(kOffClassOf + sizeof(int32_t) * (size_t)kNoAllocMaxVehicles);
+constexpr size_t kOffStatus = align_up(kOffClassOf + sizeof(int32_t) * (size_t)kNoAllocMaxVehicles);
+constexpr size_t kOffAny = align_up(kOffStatus + sizeof(uint32_t) * (size_t)kNoAllocMaxVehicles);
+constexpr size_t kOffClass = align_up(kOffAny + sizeof(uint32_t));
 constexpr size_t kScratchBytes = align_up(kOffClass + sizeof(ClassDev18));
+static_assert(kScratchBytes == LFDM_NOALLOC_SCRATCH_BYTES,
+              "LFDM_NOALLOC_SCRATCH_BYTES in include/lfdm.h states the scratch array's exact size");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-unsigned char* g_scratch_ptr[kMaxDevices] = {};
+constexpr int kAnyThreads = 256;
+
+// OR of the n per-vehicle status words into one summary word (one block).
+__global__ void __launch_bounds__(kAnyThreads) status_any_kernel(const uint32_t* status, int n, uint32_t* any) {
+    uint32_t bits = 0;
+    for (int i = threadIdx.x; i < n; i += kAnyThreads) bits |= status[i];
+    bits = __reduce_or_sync(0xffffffffu, bits);
+    if ((threadIdx.x & 31) == 0 && bits) atomicOr(any, bits);
+}
 
 void set_err(char* err, size_t err_len, const char* msg) {
     if (err && err_len) {
@@ -104,21 +119,11 @@ extern "C" int lfdm_step18_noalloc(const lfdm_class18* cls, int tire_type, const
         return LFDM_ERR_ARG;
     }
 
-    int dev = 0;
-    NA_CK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) {
-        set_err(err, err_len, "lfdm_step18_noalloc: device ordinal out of range");
-        return LFDM_ERR_ARG;
-    }
     unsigned char* base = nullptr;
     {
-        std::lock_guard<std::mutex> lock(g_mu);
-        if (!g_scratch_ptr[dev]) {
-            void* p = nullptr;
-            NA_CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-            g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
-        }
-        base = g_scratch_ptr[dev];
+        void* p = nullptr;
+        NA_CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        base = static_cast<unsigned char*>(p);
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int ni = (int)n;
@@ -127,6 +132,8 @@ extern "C" int lfdm_step18_noalloc(const lfdm_class18* cls, int tire_type, const
     double* S = reinterpret_cast<double*>(base + kOffS);
     double* ctl = reinterpret_cast<double*>(base + kOffCtl);
     int32_t* class_of = reinterpret_cast<int32_t*>(base + kOffClassOf);
+    uint32_t* status = reinterpret_cast<uint32_t*>(base + kOffStatus);
+    uint32_t* any = reinterpret_cast<uint32_t*>(base + kOffAny);
     ClassDev18* cdev = reinterpret_cast<ClassDev18*>(base + kOffClass);
 
     ClassDev18 host_cls;
@@ -134,6 +141,8 @@ extern "C" int lfdm_step18_noalloc(const lfdm_class18* cls, int tire_type, const
     // Pageable source: the copy has taken the bytes when cudaMemcpyAsync returns.
     NA_CK(cudaMemcpyAsync(cdev, &host_cls, sizeof(ClassDev18), cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemsetAsync(class_of, 0, sizeof(int32_t) * n, st));
+    NA_CK(cudaMemsetAsync(status, 0, sizeof(uint32_t) * n, st));
+    NA_CK(cudaMemsetAsync(any, 0, sizeof(uint32_t), st));
     NA_CK(launch_prepare18(params, ni, npad, K, st));
     NA_CK(launch_states_to_soa(states, ni, LFDM_S_COUNT, npad, S, st));
     NA_CK(cudaMemcpyAsync(ctl, steering, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
@@ -155,8 +164,18 @@ extern "C" int lfdm_step18_noalloc(const lfdm_class18* cls, int tire_type, const
     w.S = S;
     w.ctl_mode = CTL_ARRAY;
     w.ctl = ctl;
+    w.status = status;
     w.threads = 128;
     NA_CK(launch_window18(w, st));
     NA_CK(launch_states_to_aos(S, ni, LFDM_S_COUNT, npad, states, st));
+    status_any_kernel<<<1, kAnyThreads, 0, st>>>(status, ni, any);
+    NA_CK(cudaGetLastError());
+    uint32_t any_host = 0;
+    NA_CK(cudaMemcpyAsync(&any_host, any, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    NA_CK(cudaStreamSynchronize(st));
+    if (any_host & 1u) {
+        set_err(err, err_len, "lfdm_step18_noalloc: a vehicle's state became non-finite");
+        return LFDM_ERR_NUMERIC;
+    }
     return LFDM_OK;
 }
