@@ -1019,20 +1019,30 @@ int lfdm_traj18_backward(lfdm_solver* h, const double* ctl, const double* ref, u
     return LFDM_OK;
 }
 
-int lfdm_rhs_jacobian18(lfdm_solver* h, const double* ctl, int reference_point, double* jac_state, double* jac_ctl,
-                        int* ny) {
-    if (!h) return LFDM_ERR_ARG;
-    if (!ctl || !jac_state || !jac_ctl) return h->fail(LFDM_ERR_ARG, "null array");
-    if (h->model != LFDM_MODEL_18) return h->fail(LFDM_ERR_ARG, "the right-hand-side Jacobian is the 18-DOF model's");
+// The solver configurations a right-hand-side Jacobian can be formed for (exact: the 18-DOF model
+// without throttleMod; either: FP64, all vehicles with or without a torque converter).
+static int jacobian_supported(lfdm_solver* h, bool exact) {
+    if (exact && h->model != LFDM_MODEL_18)
+        return h->fail(LFDM_ERR_ARG, "the right-hand-side Jacobian is the 18-DOF model's");
     if (h->precision != LFDM_PREC_FP64) return h->fail(LFDM_ERR_ARG, "the right-hand-side Jacobian is FP64");
     if (h->classes.empty()) return h->fail(LFDM_ERR_STATE, "no vehicles constructed");
     const int tc = h->classes[0].tcbool != 0;
     for (const lfdm_class18& c : h->classes) {
-        if (c.throttleMod) return h->fail(LFDM_ERR_ARG, "throttleMod is not differentiated");
+        if (exact && c.throttleMod) return h->fail(LFDM_ERR_ARG, "throttleMod is not differentiated");
         if ((c.tcbool != 0) != (tc != 0))
             return h->fail(LFDM_ERR_ARG, "all vehicles must agree on the torque converter (it sets the state count)");
     }
-    int rc = check_ready(h, false);
+    return LFDM_OK;
+}
+
+int lfdm_rhs_jacobian18(lfdm_solver* h, const double* ctl, int reference_point, double* jac_state, double* jac_ctl,
+                        int* ny) {
+    if (!h) return LFDM_ERR_ARG;
+    if (!ctl || !jac_state || !jac_ctl) return h->fail(LFDM_ERR_ARG, "null array");
+    int rc = jacobian_supported(h, true);
+    if (rc) return rc;
+    const int tc = h->classes[0].tcbool != 0;
+    rc = check_ready(h, false);
     if (rc) return rc;
     rc = sync_device(h);
     if (rc) return rc;
@@ -1061,13 +1071,10 @@ int lfdm_rhs_jacobian_fd(lfdm_solver* h, const double* ctl, int reference_point,
                          int* ny) {
     if (!h) return LFDM_ERR_ARG;
     if (!ctl || !jac_state || !jac_ctl) return h->fail(LFDM_ERR_ARG, "null array");
-    if (h->precision != LFDM_PREC_FP64) return h->fail(LFDM_ERR_ARG, "the right-hand-side Jacobian is FP64");
-    if (h->classes.empty()) return h->fail(LFDM_ERR_STATE, "no vehicles constructed");
+    int rc = jacobian_supported(h, false);
+    if (rc) return rc;
     const int tc = h->classes[0].tcbool != 0;
-    for (const lfdm_class18& c : h->classes)
-        if ((c.tcbool != 0) != (tc != 0))
-            return h->fail(LFDM_ERR_ARG, "all vehicles must agree on the torque converter (it sets the state count)");
-    int rc = check_ready(h, false);
+    rc = check_ready(h, false);
     if (rc) return rc;
     rc = sync_device(h);
     if (rc) return rc;
@@ -1094,7 +1101,10 @@ int lfdm_rhs_jacobian_fd(lfdm_solver* h, const double* ctl, int reference_point,
 int lfdm_rhs_jacobian_host(lfdm_solver* h, int exact, const double* ctl, int reference_point, double* jac_state,
                            double* jac_ctl, int* ny) {
     if (!h) return LFDM_ERR_ARG;
-    if (h->classes.empty()) return h->fail(LFDM_ERR_STATE, "no vehicles constructed");
+    // every check the Jacobian call makes on the configuration runs before the size query and
+    // before any buffer is grown
+    const int sup = jacobian_supported(h, exact != 0);
+    if (sup) return sup;
     const bool nr = h->tire_type == LFDM_TIRE_TMEASY_NR;
     const int m = jac_fd_ny((int)h->model, nr, h->classes[0].tcbool != 0);
     if (ny) *ny = m;

@@ -202,3 +202,31 @@ def test_kinematic_rows_and_errors(built_lib):
     with pytest.raises(built_lib.LfdmError):
         jac(0.0, 0.0)
     s11.close()
+
+
+def test_host_jacobian_rejects_unsupported_configurations_before_sizing(built_lib):
+    """lfdm_rhs_jacobian_host checks the configuration first: the size query of the exact Jacobian on
+    an 11-DOF solver, or on an 18-DOF solver whose vehicle has throttleMod, fails like the call."""
+    import ctypes
+
+    fleet = pkg_mod("fleet")
+    L = built_lib.lib()
+    ny = ctypes.c_int(-1)
+    f11 = fleet.fleet11(8, seed=2, horizon=1.0)
+    s11 = built_lib.d11SolverHalfImplicitGPU(8)
+    s11.construct_class(f11["cls"][0], f11["params"])
+    s11.set_states(f11["states"])
+    assert L.lfdm_rhs_jacobian_host(s11._h, 1, None, 1, None, None, ctypes.byref(ny)) == \
+        built_lib._abi.C["LFDM_ERR_ARG"]
+    assert L.lfdm_rhs_jacobian_host(s11._h, 0, None, 1, None, None, ctypes.byref(ny)) == 0 and ny.value == 13
+    s11.close()
+    cls, p = fleet.suv18()
+    cls.throttleMod = 1
+    s18 = built_lib.d18SolverHalfImplicitGPU(4)
+    s18.construct_class(cls, np.repeat(p[None], 4, axis=0))
+    ny.value = -1
+    assert L.lfdm_rhs_jacobian_host(s18._h, 1, None, 1, None, None, ctypes.byref(ny)) == \
+        built_lib._abi.C["LFDM_ERR_ARG"]
+    assert ny.value == -1
+    assert L.lfdm_rhs_jacobian_host(s18._h, 0, None, 1, None, None, ctypes.byref(ny)) == 0 and ny.value == 21
+    s18.close()
