@@ -34,6 +34,9 @@ PKG = "low-fidelity-dynamic-models_gb300"
 SEED = 20261203
 W_ALG_18 = 1391  # FP64 source-level operations per 18-DOF vehicle-step of the reference algorithm
 W_ALG = {11: 675, 18: 1391, 24: 1941}  # the same count for the three models
+# FP64 thread-instructions the 18-DOF window kernel executes per vehicle-step (ncu instruction
+# counters of one capture, DFMA + DMUL + DADD + the divide and square-root sequences)
+FP64_INST_PER_VSTEP_18 = 1029
 METRIC = "18-DOF vehicle-steps/s on 1 GB300: FP64 plain vs mixed at stated error; adjoint/fwd"
 
 
@@ -50,6 +53,7 @@ def _args():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-models", action="store_true", help="skip the 11/24-DOF throughput lines")
     ap.add_argument("--no-fleet", action="store_true", help="skip the mixed-DOF fleet line")
+    ap.add_argument("--no-reference-gpu", action="store_true", help="skip timing the reference's own GPU solver")
     ap.add_argument("--fleet-vehicles", type=int, default=250_000)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-rollout line")
     ap.add_argument("--adjoint-vehicles", type=int, default=65_536)
@@ -146,18 +150,30 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def _oracle_rate(f, nveh: int, ksim: float, threads: int) -> tuple[float, float]:
-    """Vehicle-steps/s of the CPU restatement over nveh vehicles for one window."""
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle_lib
-    sl = slice(0, nveh)
-    tabs = f["tables"][sl]
-    t0 = time.perf_counter()
-    oracle_lib.run18(f["cls"], f["class_of"][sl], f["params"][sl], f["states"][sl], tabs, tend=ksim, ksim=ksim,
-                     schedule=1, nthreads=threads)
-    dt = time.perf_counter() - t0
-    steps = int(round(ksim / 1e-3))
-    return nveh * steps / dt, dt
+class CpuTrajectory:
+    """The reference's CPU algorithm (the oracle restatement, oracle/lfdm_oracle.c, built with the
+    reference's Release flags -O3) on the host cores over the first `nveh` vehicles of a fleet:
+    window() advances their trajectories by one stepping window of ksim seconds (the GPU solver's
+    schedule), continuing from where the previous call ended, and returns its wall time."""
+
+    def __init__(self, f, nveh: int, ksim: float, threads: int, model: int = 18):
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib
+        self.O = oracle_lib
+        sl = slice(0, nveh)
+        self.cls, self.class_of, self.params = f["cls"], f["class_of"][sl], f["params"][sl]
+        self.tables = f["tables"][sl]
+        self.states = np.array(f["states"][sl], copy=True)
+        self.nveh, self.ksim, self.threads, self.model = nveh, ksim, threads, model
+        self.k = 0
+
+    def window(self) -> float:
+        t0 = time.perf_counter()
+        self.states, _ = self.O.run18(self.cls, self.class_of, self.params, self.states, self.tables,
+                                      t0=self.k * self.ksim, tend=(self.k + 1) * self.ksim, ksim=self.ksim, schedule=1,
+                                      nthreads=self.threads, model=self.model, timing=True)
+        self.k += 1
+        return time.perf_counter() - t0
 
 
 def run_reference(a, dist: Dist):
@@ -167,12 +183,10 @@ def run_reference(a, dist: Dist):
     cores = os.cpu_count() or 1
     n = a.cpu_sample
     f = fleet.fleet18(n, seed=SEED, horizon=(a.warmup + a.steps) * a.ksim)
+    cpu = CpuTrajectory(f, n, a.ksim, cores)
     for _ in range(a.warmup):
-        _oracle_rate(f, n, a.ksim, cores)
-    times = []
-    for _ in range(a.steps):
-        _, dt = _oracle_rate(f, n, a.ksim, cores)
-        times.append(dt)
+        cpu.window()
+    times = [cpu.window() for _ in range(a.steps)]
     steps = int(round(a.ksim / 1e-3))
     v = n * steps * a.steps / sum(times)
     line = {
@@ -181,9 +195,11 @@ def run_reference(a, dist: Dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SUV fleet)",
         "config": _config(a, n_override=n),
         "cpu_baseline": {"value": v, "unit": "vehicle-steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{n} vehicles x {steps} steps per step (bounded sample of the fleet), "
+                         "sample": f"{n} vehicles x {steps} steps per step (bounded sample of the fleet), the "
+                                   "trajectories continued window after window, "
                                    f"{cores} host threads; the reference's CPU algorithm as restated in "
-                                   "oracle/lfdm_oracle.c (the reference checkout is not on this host)"},
+                                   "oracle/lfdm_oracle.c, built with the reference's Release flags (-O3); "
+                                   "the reference checkout is not on this host"},
         "e2e": {"value": v, "unit": "vehicle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -442,6 +458,33 @@ def _jacobian_bench(lfdm, fleet, dev, n: int, cpu_sample: int, torch) -> dict:
     return out
 
 
+def _reference_gpu_bench(fleet, model: int, n: int, windows: int, ksim: float, ours: float) -> dict:
+    """The reference's OWN GPU solver (its Integrate kernel compiled from the reference sources into
+    oracle/_ref/ref<model>.cubin, driven window by window as its Solve() does, with its managed AoS
+    records) on the seeded SUV fleet of the model with outputs every 10 ms: windows 2..windows timed
+    with CUDA events, at 16 and 32 threads per block (its best counts). ratio = ours / best."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import refgpu_lib
+    if not refgpu_lib.available(model):
+        return {"unavailable": f"oracle/_ref/ref{model}.cubin was not built (it is built where the reference "
+                               "checkout exists)"}
+    refgpu_lib.build_launcher()
+    gen = {11: fleet.fleet11, 18: fleet.fleet18, 24: fleet.fleet24}[model]
+    f = gen(n, seed=SEED + model, horizon=windows * ksim)
+    out = {"vehicles": n, "windows_timed": windows - 1, "window_s": ksim, "output_hz": 100}
+    best = 0.0
+    for tpb in (16, 32):
+        _, ms = refgpu_lib.run(f["cls"][0], f["params"], f["tables"], f["states"], model=model, ksim=ksim,
+                               tend=windows * ksim, dtout=0.01, tpb=tpb)
+        rate = n * int(round(ksim / 1e-3)) * (windows - 1) / (sum(ms[1:]) * 1e-3)
+        out[f"tpb{tpb}"] = {"value": rate, "unit": "vehicle-steps/s", "ms_per_window": sum(ms[1:]) / (windows - 1)}
+        best = max(best, rate)
+    out["best"] = best
+    out["ours"] = ours
+    out["ratio"] = ours / best
+    return out
+
+
 def run_ours(a, dist: Dist):
     import torch
 
@@ -538,7 +581,11 @@ def run_ours(a, dist: Dist):
         mixed = {"value": mvalue, "unit": "vehicle-steps/s", "speedup_vs_fp64": mvalue / value,
                  "ms_per_step": mms / K, "gpu_launches": mlaunch, "dtype": "f32 RHS + f64 states/X/Y/yaw/slip"}
         mixed["error_vs_fp64"] = _mixed_error(lfdm, fleet, dev, a.error_vehicles, a.error_horizon)
-    peak_dfma = lfdm.measure_fp64_peak(dev)
+    peak_dfma, probe_ghz = lfdm.measure_fp64_peak_clock(dev)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    max_ghz = (clocks.get("sm_max_mhz") or 2070.0) / 1e3
+    # nominal FP64 rate: one warp-wide DFMA per 64 cycles per SM sub-partition = 2 DFMA/clock/SM
+    peak_nominal = 2 * 2.0 * sms * max_ghz * 1e9 / 1e12
     launch_ms = kms / launches
     alg_flop = W_ALG_18 * n * steps_per_window
     achieved = alg_flop / (launch_ms * 1e-3) / 1e12
@@ -567,6 +614,14 @@ def run_ours(a, dist: Dist):
                   "11dof_scale": _model_rate(lfdm, fleet, dev, 11, n, 2, ksim, peak),
                   "24dof_scale": _model_rate(lfdm, fleet, dev, 24, n, 2, ksim, peak)}
         models["24dof_scale"]["config"] = "24-DOF SUV fleet (ks 4e4 N/m, bs 4e3 N s/m), jittered as the 18-DOF fleet"
+    # the reference's own GPU solver on this GPU: 18-DOF on the bench fleet's size, and the 11-DOF
+    # small config and the 24-DOF model at scale beside this library's lines above
+    ref_gpu = None
+    if not a.no_reference_gpu and dist.rank == 0:
+        ref_gpu = {"18dof": _reference_gpu_bench(fleet, 18, n, 3, ksim, value)}
+        if models:
+            ref_gpu["11dof_1024"] = _reference_gpu_bench(fleet, 11, 1024, 10, 1.0, models["11dof_1024"]["value"])
+            ref_gpu["24dof_scale"] = _reference_gpu_bench(fleet, 24, n, 3, ksim, models["24dof_scale"]["value"])
     fleet_line = None
     if not a.no_fleet:
         fleet_line = _fleet_bench(lfdm, fleet, dev, a.fleet_vehicles, torch)
@@ -580,10 +635,24 @@ def run_ours(a, dist: Dist):
     cpu = None
     if dist.rank == 0:
         cores = os.cpu_count() or 1
-        rate, secs = _oracle_rate(f, min(a.cpu_sample, n), ksim, cores)
+        m = min(a.cpu_sample, n)
+        traj = CpuTrajectory(f, m, ksim, cores)
+        traj.window()  # warm-up: window 0
+        secs = sum(traj.window() for _ in range(3))
+        rate = m * steps_per_window * 3 / secs
         cpu = {"value": rate, "unit": "vehicle-steps/s", "cores": cores, "kind": "port",
-               "sample": f"{min(a.cpu_sample, n)} vehicles x {steps_per_window} steps ({secs:.1f} s wall), "
-                         "oracle/lfdm_oracle.c (the reference's CPU algorithm restated) on all host cores"}
+               "sample": f"{m} vehicles of the fleet x windows 1-3 ({3 * steps_per_window} steps, {secs:.1f} s "
+                         "wall) after window 0, trajectories continued; oracle/lfdm_oracle.c (the reference's CPU "
+                         "algorithm restated) built with the reference's Release flags (-O3), all host cores"}
+        if models:
+            f11 = fleet.fleet11(1024, seed=SEED + 11, horizon=10.0)
+            t11 = CpuTrajectory(f11, 1024, 1.0, cores, model=11)
+            secs11 = sum(t11.window() for _ in range(10))
+            models["11dof_1024"]["cpu_baseline"] = {
+                "value": 1024 * 10000 / secs11, "unit": "vehicle-steps/s", "cores": cores, "kind": "port",
+                "sample": f"the whole config: 1,024 vehicles x 10 s ({secs11:.2f} s wall), the 11-DOF oracle "
+                          "restatement (-O3), all host cores"}
+            models["11dof_1024"]["speedup_vs_cpu"] = models["11dof_1024"]["value"] / models["11dof_1024"]["cpu_baseline"]["value"]
     if dist.rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "vehicle-steps/s", "n_gpus": dist.world, "steps": K,
@@ -593,8 +662,20 @@ def run_ours(a, dist: Dist):
             "rtf": (kms_max * 1e-3) / (K * ksim),
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "peak_source": "measured live: DFMA throughput kernel (lfdm_measure_fp64_peak), "
+                         "traffic_source": "constant: one ncu capture of this configuration (dram__bytes_read.sum "
+                                           "+ dram__bytes_write.sum of one window launch), not measured in this run",
+                         "peak_source": "measured live: DFMA throughput kernel (lfdm_measure_fp64_peak_clock), "
                                         "x2 flop/FMA; MEASURED_PEAKS.json has no FP64 figure",
+                         "probe_sm_ghz": probe_ghz,
+                         "probe_dfma_per_clk_per_sm": peak_dfma / (sms * probe_ghz * 1e9) if probe_ghz else None,
+                         "peak_nominal": peak_nominal, "frac_nominal": achieved / peak_nominal,
+                         "peak_nominal_source": f"2 DFMA/clock/SM x {sms} SMs x {max_ghz:.3f} GHz (max SM clock) x 2",
+                         "issue_view": {
+                             "fp64_inst_per_vehicle_step": FP64_INST_PER_VSTEP_18,
+                             "source": "ncu sm__sass_thread_inst_executed_op_dfma/dmul/dadd_pred_on (+ divide and "
+                                       "square-root sequences) per vehicle-step of the window kernel, one capture",
+                             "frac": FP64_INST_PER_VSTEP_18 * value / peak_dfma,
+                             "frac_nominal": FP64_INST_PER_VSTEP_18 * value / (peak_nominal * 1e12 / 2)},
                          "algorithmic": f"{W_ALG_18} FP64 ops per vehicle-step (reference op count) x "
                                         f"{n * steps_per_window} vehicle-steps per launch"},
             "roofline_hbm": {"bound": "hbm", "achieved": alg_bytes / (launch_ms * 1e-3) / 1e9, "peak": hbm_peak,
@@ -605,6 +686,7 @@ def run_ours(a, dist: Dist):
             "e2e": e2e,
             "mixed": mixed,
             "models": models,
+            "reference_gpu": ref_gpu,
             "fleet": fleet_line,
             "adjoint": adjoint_line,
             "jacobian": jacobian_line,

@@ -258,6 +258,9 @@ const char* lfdm_version(void);
 /* Measurement helper (no counterpart in the reference): FP64 fused-multiply-add instruction rate of */
 /* a device, measured with a throughput kernel (the FP64 issue roofline of the stepping kernel).     */
 int lfdm_measure_fp64_peak(int device, double* dfma_per_s);
+/* The same probe with the SM clock it ran at (GHz, from the SM clock counter over the global       */
+/* nanosecond timer), which normalises the rate to DFMA per clock per SM.                          */
+int lfdm_measure_fp64_peak_clock(int device, double* dfma_per_s, double* sm_ghz);
 
 /* Host-only utilities (no device needed). setVehParamsJSON + setTireParamsJSON + tireInit        */
 /* (dof18_gpu.cu:1075-1330, :227-241) into a class record and a flat parameter vector, and        */
@@ -301,6 +304,13 @@ int lfdm_traj18_backward(lfdm_solver* h, const double* ctl, const double* ref, u
                          unsigned ckpt_every, double* grad_ctl, double* grad_params, double* grad_state0);
 /* CUDA-event times of the last forward and backward kernels. */
 int lfdm_traj18_last_ms(lfdm_solver* h, double* forward_ms, double* backward_ms);
+/* Branch signature of the rollout lfdm_traj18_forward runs with the same controls: per vehicle a   */
+/* 64-bit hash of every discrete decision of every step (tire lift-off, tmxy_combined regime, clamps, */
+/* sineStep bands, wheel-speed sign, map segments, converter mode and flow direction, gear,          */
+/* differential bias bands). Two rollouts whose signatures are equal took the same branches, so a    */
+/* central difference between them does not straddle a kink of the loss. ctl [nsteps][3][N] and     */
+/* sig [N] are DEVICE arrays. (Extension: test instrumentation for the adjoint's derivative checks.) */
+int lfdm_traj18_branch_signature(lfdm_solver* h, const double* ctl, unsigned nsteps, uint64_t* sig);
 
 /* Exact Jacobians of the 18-DOF right-hand side for every vehicle (extension; the reference's GPU  */
 /* solver has none, its CPU solver takes central differences: IntegrateStepWithJacobian,           */
@@ -383,6 +393,32 @@ int lfdm_fleet_set_states(lfdm_fleet* f, int model, unsigned first, unsigned cou
 /* Response of one model, [nsamples][channels][n] in add order (out NULL: only *nsamples). */
 int lfdm_fleet_get_response(lfdm_fleet* f, int model, double* out, size_t capacity, unsigned* nsamples);
 int lfdm_fleet_get_status_words(lfdm_fleet* f, int model, uint32_t* out);
+
+/* Extension: the 11-DOF model's split-warp window kernel, which runs each vehicle's two tires on two */
+/* warps (for fleets too small to fill the GPU, whose time is set by one vehicle's FP64 instruction  */
+/* chain; results are bit for bit those of the one-warp kernel). mode -1 (default): used when the    */
+/* fleet needs at most 2 blocks of 64 threads per SM; 0: never; 1: always. Other models ignore it.  */
+int lfdm_set_split_warps(lfdm_solver* h, int mode);
+
+/* One stepping window run by a kernel the CALLER compiles: the C++ drop-in's SolveStep(t, func)     */
+/* with a __device__ functor (18dof-gpu/dof18_halfImplicit_gpu.cuh:234-287, the functor kernels at  */
+/* :455-640 and rhsFun at :646-694; include/lfdm/device/functor_window.cuh). begin uploads what has  */
+/* changed, clears the status words and describes the device data of the window that starts at t;   */
+/* the caller enqueues its kernel on view->stream, then end waits for that stream, marks the device  */
+/* states as the current ones and checks the status words (LFDM_ERR_NUMERIC on a non-finite state).  */
+/* FP64 only; refused with CSV output set, as SolveStep is. No responses are written.               */
+typedef struct {
+    int32_t model, tire_type, n, npad, nclasses, nsteps, kcount, pad_;
+    double t0, dt;              /* window start and step                                          */
+    const double* K;            /* [kcount][npad] derived per-vehicle constants                   */
+    const void* classes;        /* [nclasses] device class records (lfdm::ClassDev18)              */
+    const int32_t* class_of;    /* [n] class of each vehicle                                       */
+    double* S;                  /* [state count][npad] states (SoA), stepped in place              */
+    uint32_t* status;           /* [n] status words; bit 0 = the state became non-finite           */
+    void* stream;               /* cudaStream_t to enqueue the window on                           */
+} lfdm_device_window;
+int lfdm_device_window_begin(lfdm_solver* h, double t, lfdm_device_window* view);
+int lfdm_device_window_end(lfdm_solver* h, double t, double* t_out);
 
 /* No counterpart in the reference (its solver owns and allocates all of its memory). For callers   */
 /* that cannot allocate device memory on their call path (a real-time control loop, a host that    */

@@ -17,7 +17,7 @@
 
 #include <cstdint>
 
-#include "../../include/lfdm.h"
+#include "../../lfdm.h"
 #include "fp_order.cuh"
 
 namespace lfdm {

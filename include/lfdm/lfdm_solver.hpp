@@ -8,7 +8,8 @@
 // compiles against these headers (add include/lfdm to the include path) and links with
 // -llfdm; every method forwards to one or two lfdm_* calls.
 //
-// Header-only, plain C++17: nvcc is not needed to compile a caller.
+// Header-only, plain C++17: a caller compiles with a host compiler, or with nvcc for the device
+// functor SolveStep below.
 //
 // Errors. The reference prints CUDA errors and carries on (utils/utils_gpu.cuh CHECK_CUDA_ERROR),
 // asserts (compiled out in Release) or calls exit() (SolveStep with CSV output set). Here every
@@ -16,12 +17,17 @@
 // program behaves as it did against the reference; define LFDM_CPP_THROW before including to get a
 // std::runtime_error instead.
 //
+// SolveStep(t, func) with a functor (18dof-gpu/dof18_halfImplicit_gpu.cuh:234-287):
+//  - compiled with nvcc, the reference's way: a kernel instantiated for the functor's type (in
+//    device/functor_window.cuh, over the library's device headers in device/) calls the __device__
+//    functor at every step of the window and runs the library's step with those controls, on the
+//    solver's stream, over its device states (lfdm_device_window_begin/_end of lfdm.h). Compile
+//    with --fmad=false to get the states of the library's own kernels bit for bit.
+//  - compiled with a host compiler (or with LFDM_HOST_FUNCTOR defined), the functor is called on
+//    the host once per step of the window at the step's start time, and the window runs with that
+//    control schedule; its operator() must then be callable on the host.
+//
 // Differences a caller can see:
-//  - SolveStep(t, func): the reference launches a kernel that calls a __device__ functor at every
-//    step. A C ABI cannot carry a device functor, so the functor is called on the host, once per
-//    step of the window, at the step's start time (the times the reference's kernel passes it),
-//    and the window runs with that control schedule. The functor therefore has to be callable on
-//    the host: mark its operator() __host__ __device__ when compiling with nvcc.
 //  - The public m_sim_data / m_sim_states arrays are not exposed; parameters and states of
 //    individual vehicles are read and written through handle() and the lfdm_get/set_params and
 //    lfdm_get/set_states extensions of lfdm.h.
@@ -35,6 +41,15 @@
 
 #include "../lfdm.h"
 
+#if defined(__CUDACC__) && !defined(LFDM_HOST_FUNCTOR)
+#define LFDM_DEVICE_FUNCTOR 1
+#endif
+#if defined(__CUDACC__)
+#define LFDM_HD __host__ __device__
+#else
+#define LFDM_HD
+#endif
+
 #ifndef LFDM_TIRE_TYPE_DEFINED
 #define LFDM_TIRE_TYPE_DEFINED
 // 18dof-gpu/dof18_gpu.cuh:12 (the 11- and 24-DOF headers declare the same enum; here it is
@@ -46,14 +61,18 @@ enum class TireType { TMeasy, TMeasyNr };
 #define LFDM_DRIVER_INPUT_DEFINED
 // utils/utils_gpu.cuh:29-40: one row of a driver table, and what a SolveStep functor fills in.
 struct DriverInput {
-    DriverInput() : m_time(0), m_steering(0), m_throttle(0), m_braking(0) {}
-    DriverInput(double time, double steering, double throttle, double braking)
+    LFDM_HD DriverInput() : m_time(0), m_steering(0), m_throttle(0), m_braking(0) {}
+    LFDM_HD DriverInput(double time, double steering, double throttle, double braking)
         : m_time(time), m_steering(steering), m_throttle(throttle), m_braking(braking) {}
     double m_time;
     double m_steering;
     double m_throttle;
     double m_braking;
 };
+#endif
+
+#ifdef LFDM_DEVICE_FUNCTOR
+#include "device/functor_window.cuh"
 #endif
 
 namespace lfdm_cpp {
@@ -131,10 +150,22 @@ class SolverBase {
         check(lfdm_solve_step(h_, t, steering, throttle, braking, &t_out), h_, "SolveStep");
         return t_out;
     }
-    // Functor form (18dof-gpu/dof18_halfImplicit_gpu.cuh:234-287): func(t, DriverInput*) is called on
-    // the host at each step start time of the window [t, t + kernel_sim_time).
+    // Functor form (18dof-gpu/dof18_halfImplicit_gpu.cuh:234-287): func(t, DriverInput*) gives the
+    // controls at each step start time of the window [t, t + kernel_sim_time); on the device when
+    // compiled with nvcc, else on the host (see the top of this file).
     template <typename Func>
     double SolveStep(double t, Func func) {
+#ifdef LFDM_DEVICE_FUNCTOR
+        lfdm_device_window view;
+        int rc = lfdm_device_window_begin(h_, t, &view);
+        check(rc, h_, "SolveStep");
+        if (rc != LFDM_OK) return t;
+        const cudaError_t e = lfdm::launch_functor_window<Model>(view, func);
+        if (e != cudaSuccess) check_message("SolveStep", cudaGetErrorString(e));
+        double t_out = t;
+        check(lfdm_device_window_end(h_, t, &t_out), h_, "SolveStep");
+        return t_out;
+#else
         unsigned int n = 0;
         check(lfdm_window_steps(h_, t, &n, nullptr, 0), h_, "SolveStep");
         std::vector<double> times(n), ctl(3 * static_cast<std::size_t>(n));
@@ -149,6 +180,7 @@ class SolverBase {
         double t_out = t;
         check(lfdm_solve_step_schedule(h_, t, ctl.data(), n, 0, &t_out), h_, "SolveStep");
         return t_out;
+#endif
     }
     TireType GetTireType() const {
         int t = LFDM_TIRE_TMEASY;

@@ -89,6 +89,8 @@ def _sig(lib):
         "lfdm_set_response_device": ([vp, vp, sz, d], i),
         "lfdm_solve_range": ([vp, d, d], i),
         "lfdm_measure_fp64_peak": ([i, _c_dp], i),
+        "lfdm_set_split_warps": ([vp, i], i),
+        "lfdm_measure_fp64_peak_clock": ([i, _c_dp, _c_dp], i),
         "lfdm_parse_vehicle18": ([cp, cp, i, vp, dp, ctypes.c_char_p, sz], i),
         "lfdm_parse_vehicle": ([i, cp, cp, cp, i, vp, dp, ctypes.c_char_p, sz], i),
         "lfdm_load_driver_file": ([cp, dp, u, ctypes.POINTER(u), ctypes.c_char_p, sz], i),
@@ -96,6 +98,7 @@ def _sig(lib):
         "lfdm_traj18_forward": ([vp, vp, vp, u, d, u, vp], i),
         "lfdm_traj18_backward": ([vp, vp, vp, u, d, u, vp, vp, vp], i),
         "lfdm_traj18_last_ms": ([vp, _c_dp, _c_dp], i),
+        "lfdm_traj18_branch_signature": ([vp, vp, u, vp], i),
         "lfdm_rhs_jacobian18": ([vp, vp, i, vp, vp, ctypes.POINTER(i)], i),
         "lfdm_rhs_jacobian_fd": ([vp, vp, i, vp, vp, ctypes.POINTER(i)], i),
         "lfdm_rhs_jacobian_host": ([vp, i, vp, i, vp, vp, ctypes.POINTER(i)], i),
@@ -336,6 +339,10 @@ class _SolverGPU:
     def set_precision(self, precision: int):
         self._ck(self._L.lfdm_set_precision(self._h, int(precision)))
 
+    def set_split_warps(self, mode: int):
+        """11-DOF split-warp window kernel: -1 for small fleets (default), 0 never, 1 always."""
+        self._ck(self._L.lfdm_set_split_warps(self._h, int(mode)))
+
     def set_response_buffer(self, buf: np.ndarray | None, output_freq: float = 100.0):
         """Stream Solve's SoA response [sample][RESP_CHANNELS][N] into `buf` (float64, C-contiguous); samples
         beyond its capacity wrap around."""
@@ -460,11 +467,16 @@ class d24SolverHalfImplicitGPU(_SolverGPU):
 
 def measure_fp64_peak(device: int = 0) -> float:
     """Measured FP64 FMA instruction rate (DFMA/s) of a device."""
-    v = ctypes.c_double()
-    rc = lib().lfdm_measure_fp64_peak(int(device), ctypes.byref(v))
+    return measure_fp64_peak_clock(device)[0]
+
+
+def measure_fp64_peak_clock(device: int = 0) -> tuple[float, float]:
+    """(measured DFMA/s, SM clock in GHz the probe ran at) of a device."""
+    v, g = ctypes.c_double(), ctypes.c_double()
+    rc = lib().lfdm_measure_fp64_peak_clock(int(device), ctypes.byref(v), ctypes.byref(g))
     if rc:
         raise LfdmError(rc, "FP64 peak probe failed")
-    return v.value
+    return v.value, g.value
 
 
 class Fleet:
@@ -629,6 +641,12 @@ class Rollout18:
             self.solver._h, ctypes.c_void_p(controls.data_ptr()), ctypes.c_void_p(ref.data_ptr()), self.nsteps,
             self.weight_u, self.ckpt, ctypes.c_void_p(grad_ctl.data_ptr()), ctypes.c_void_p(grad_params.data_ptr()),
             ctypes.c_void_p(grad_state0.data_ptr()) if grad_state0 is not None else None))
+
+    def branch_signature(self, controls, out):
+        """lfdm_traj18_branch_signature: per-vehicle hash (int64 CUDA tensor `out` [N]) of the branches
+        the rollout with `controls` takes (at the solver's current parameters)."""
+        self.solver._ck(self.solver._L.lfdm_traj18_branch_signature(
+            self.solver._h, ctypes.c_void_p(controls.data_ptr()), self.nsteps, ctypes.c_void_p(out.data_ptr())))
 
     def last_ms(self) -> tuple[float, float]:
         f, b = ctypes.c_double(), ctypes.c_double()

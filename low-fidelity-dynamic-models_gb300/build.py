@@ -35,7 +35,8 @@ def _sources():
     cu = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     cpp = sorted(glob.glob(os.path.join(CSRC, "*.cpp")))
     hdr = sorted(glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) +
-                 glob.glob(os.path.join(ROOT_INCLUDE, "*.h")))
+                 glob.glob(os.path.join(ROOT_INCLUDE, "*.h")) +
+                 glob.glob(os.path.join(ROOT_INCLUDE, "lfdm", "device", "*.cuh")))
     return cu, cpp, hdr
 
 

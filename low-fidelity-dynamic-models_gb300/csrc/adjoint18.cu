@@ -292,6 +292,102 @@ static cudaError_t launch_rollout(void (*kern)(const AdjLaunch), const AdjLaunch
     kern<<<(A.n + threads - 1) / threads, threads, smem, stream>>>(L);
     return cudaGetLastError();
 }
+// ---------------------------------------------------------------------------------------------
+// Branch signature of a rollout: a 64-bit hash of every discrete decision the steps take (per tire:
+// wheel on the ground, dynamic-radius band, load clamp, zero combined slip, tmxy_combined regime,
+// structural-force clamps, sineStep bands of the force blend, sign of the wheel speed; per vehicle:
+// the segments of the steering, engine and loss maps, converter speed-ratio mode, flow direction
+// and map segments, drive-torque clip, gear, differential bias bands and slower wheels). Two rollouts
+// with equal signatures took the same branch at every step, so the loss is smooth between them.
+
+__device__ __forceinline__ uint64_t sig_mix(uint64_t h, uint64_t w) {
+    // FNV-1a over the 8 bytes of w
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        h ^= (w >> (8 * b)) & 0xffu;
+        h *= 0x100000001b3ull;
+    }
+    return h;
+}
+__device__ __forceinline__ uint64_t sig_d(uint64_t h, double x) { return sig_mix(h, (uint64_t)__double_as_longlong(x)); }
+// 0 below the sineStep band, 1 inside, 2 above (weight 1, between, 0)
+__device__ __forceinline__ double band(double w, double dw) {
+    return (dw != 0.0) ? 1.0 : (w == 1.0 ? 0.0 : (w == 0.0 ? 2.0 : 1.0));
+}
+__device__ __forceinline__ double seg(const MapDev& m, double x) {
+    if (x <= m.x[0]) return -1.0;
+    if (x >= m.x[m.n - 1]) return (double)m.n;
+    return (double)lower_bound_x(m.x, m.n, x);
+}
+
+__device__ uint64_t step_signature(uint64_t h, const TapeRef& T, const ClassDev18& C) {
+    h = sig_d(h, T.at(TS_(gear)));
+    h = sig_d(h, C.nonLinearSteer ? seg(C.steer, T.at(TS_(steer))) : 0.0);
+    const double crank_used = C.tcbool ? T.at(TS_(crank)) : T.at(TS_(omega_in));
+    h = sig_d(h, seg(C.pt, crank_used));
+    h = sig_d(h, seg(C.loss, crank_used));
+    if (C.tcbool) {
+        h = sig_d(h, T.at(TS_(srmode)));
+        h = sig_d(h, T.at(TS_(rev)));
+        h = sig_d(h, seg(C.cf, T.at(TS_(sr))));
+        h = sig_d(h, seg(C.tr, T.at(TS_(sr))));
+    }
+    h = sig_d(h, T.at(TS_(tclip)));
+    // bias band of each axle's differential; which wheel gets the larger share matters only with a bias
+    const double bf = T.at(TS_(dalf)) != 0.0 ? 1.0 : (T.at(TS_(alf)) == 0.5 ? 0.0 : 2.0);
+    const double br = T.at(TS_(dalr)) != 0.0 ? 1.0 : (T.at(TS_(alr)) == 0.5 ? 0.0 : 2.0);
+    h = sig_d(h, bf);
+    h = sig_d(h, br);
+    if (bf != 0.0) h = sig_d(h, T.at(TS_(slowf)));
+    if (br != 0.0) h = sig_d(h, T.at(TS_(slowr)));
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const TapeRef R = tire_ref(T, k);
+        const double on = R.at(TT_(on));
+        h = sig_d(h, on);
+        if (on == 0.0) continue;
+        h = sig_d(h, R.at(TT_(fzrd)));
+        h = sig_d(h, R.at(TT_(fzcl)));
+        h = sig_d(h, R.at(TT_(qpos)));
+        h = sig_d(h, R.at(TT_(reg)));
+        h = sig_d(h, R.at(TT_(clx)));
+        h = sig_d(h, R.at(TT_(cly)));
+        h = sig_d(h, band(R.at(TT_(wxw)), R.at(TT_(dwx))));
+        h = sig_d(h, band(R.at(TT_(wyw)), R.at(TT_(dwy))));
+        h = sig_d(h, R.at(TT_(sgn)));
+    }
+    return h;
+}
+
+// The rollout of traj18_forward_kernel (the same arithmetic: fwd18_tape rounds as step18) with a
+// one-step tape per vehicle, hashing each step's decisions.
+__global__ void __launch_bounds__(128) traj18_signature_kernel(const AdjLaunch A, uint64_t* sig) {
+    const int vid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (vid >= A.n) return;
+    const size_t np = (size_t)A.npad;
+    const KView K{A.K + vid, A.npad};
+    const ClassDev18& C = A.classes[__ldg(A.class_of + vid)];
+    VehC v;
+    VehAux va;
+    TireC ts[4];
+    TireAux ta[4];
+    load_state18(A.S0 + vid, np, v, va, ts, ta);
+    const size_t nu = (size_t)A.n;
+    const TapeRef T{A.tape + vid, np};
+    uint64_t h = 0xcbf29ce484222325ull;
+    for (int k = 0; k < A.nsteps; ++k) {
+        const double* U = A.ctl + (size_t)k * 3 * nu + vid;
+        fwd18_tape(v, va, ts, ta, T, K, C, __ldg(U), __ldg(U + nu), __ldg(U + 2 * nu), A.dt);
+        h = step_signature(h, T, C);
+    }
+    sig[vid] = h;
+}
+
+cudaError_t launch_traj18_signature(const AdjLaunch& A, uint64_t* sig, cudaStream_t stream) {
+    traj18_signature_kernel<<<(A.n + 127) / 128, 128, 0, stream>>>(A, sig);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_traj18_forward(const AdjLaunch& A, cudaStream_t stream) {
     return launch_rollout(traj18_forward_kernel, A, false, stream);
 }

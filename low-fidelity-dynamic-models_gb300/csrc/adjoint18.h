@@ -36,6 +36,8 @@ struct AdjLaunch {
 
 cudaError_t launch_traj18_forward(const AdjLaunch& A, cudaStream_t stream);
 cudaError_t launch_traj18_backward(const AdjLaunch& A, cudaStream_t stream);
+// Branch signature of the rollout per vehicle (sig [n], device); A.tape holds one step's tape.
+cudaError_t launch_traj18_signature(const AdjLaunch& A, uint64_t* sig, cudaStream_t stream);
 size_t traj18_tape_doubles_per_step();
 size_t traj18_smem(int threads, int nclasses, bool backward, bool* cls_smem);
 int traj18_ckpt_fields();

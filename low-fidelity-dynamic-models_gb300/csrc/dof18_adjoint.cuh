@@ -22,7 +22,7 @@
 
 #include <cstddef>
 
-#include "dof18_device.cuh"
+#include "../../include/lfdm/device/dof18_device.cuh"
 
 namespace lfdm {
 
@@ -98,6 +98,7 @@ struct TireTape {
     double vtxs, vtys, numx, numy, denx, deny, xedot, yedot, idenx, ideny, issum, ifsum, ivta;
     double Fx, Fy, fxstr, fystr, clx, cly, wxw, wyw, dwx, dwy;  // clx/cly: -1/0/+1 clamp side
     double fx, fy, My, sgn;
+    double reg;  // tmxy_combined regime (0 no force, 1 sliding, 2 adhesion, 3/4 the two parabolas, 5 cubic)
 };
 // Per-tire tape of a TMeasyNr tire, in the slots of TireTape: the fields the vehicle-level sweep
 // reads (on, om, rStat, fx, fy, My) sit at the same offsets as in TireTape, the rest of the head in
@@ -186,6 +187,23 @@ __device__ __forceinline__ void sine_step_w(double x, double& y, double& dy) {
 
 // ---------------------------------------------------------------------------------------------
 // forward with tape (the arithmetic of tire_rhs_tm / tire_core_tm / powertrain_rhs / step18)
+
+// The regime tmxy_frac takes for these arguments, by its own comparisons (the quantities they
+// compare are computed by the same expressions, so they round alike): 0 no force, 1 full sliding,
+// 2 adhesion, 3 and 4 the two parabolas, 5 the cubic fallback.
+__device__ __forceinline__ double tmxy_regime(double s, double df0, double sm, double ism, double fm, double ss,
+                                              double fs) {
+    double df0loc = 0.0;
+    if (gt0(sm)) df0loc = max_nn(2.0 * fm * ism, df0);
+    if (!(gt0(s) && gt0(df0loc))) return 0.0;
+    if (gt_nn(s, ss)) return 1.0;
+    if (gt_nn(sm, s)) return 2.0;
+    const double q = fm * ism;
+    const double a = q * q / (df0loc * sm);
+    const double sstar = sm + (fm - fs) / (a * (ss - sm));
+    if (sstar <= ss) return s <= sstar ? 3.0 : 4.0;
+    return 5.0;
+}
 
 template <bool kSteered>
 __device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, const TapeRef& T, const KView& K, double c, double s) {
@@ -309,6 +327,7 @@ __device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, const Tape
     double fn, fd;
     tmxy_frac(fn, fd, sc, isc, df0, sm, ism, fm, ifm, ss, fs);
     T.at(TT_(fos)) = fn / fd;  // the ratio itself, for the reverse
+    T.at(TT_(reg)) = tmxy_regime(sc, df0, sm, ism, fm, ss, fs);
     T.at(TT_(sgn)) = sgnd(omega);
     ta.My = -K(K_RR) * fzc * ta.rStat * T.at(TT_(sgn));
     const double vtxs = fma(rw, hsxn, 0.01);

@@ -10,7 +10,7 @@
 // Same algorithm and branch structure as dof18_device.cuh (the FP64 form), which is its oracle.
 #pragma once
 
-#include "dof18_device.cuh"
+#include "../../include/lfdm/device/dof18_device.cuh"
 
 namespace lfdm {
 

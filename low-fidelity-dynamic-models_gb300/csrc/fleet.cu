@@ -19,7 +19,7 @@
 // the tile's derived constants; class tables are read through L1.
 #include <cuda_runtime.h>
 
-#include "dof24_device.cuh"
+#include "../../include/lfdm/device/dof24_device.cuh"
 #include "fleet.h"
 #include "window_common.cuh"
 

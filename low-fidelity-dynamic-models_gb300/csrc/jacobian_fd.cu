@@ -21,8 +21,8 @@
 // (its state Jacobian is zero); here every model and tire unpacks.
 #include <cuda_runtime.h>
 
-#include "dof11_device.cuh"
-#include "dof24_device.cuh"
+#include "../../include/lfdm/device/dof11_device.cuh"
+#include "../../include/lfdm/device/dof24_device.cuh"
 #include "jacobian_fd.h"
 #include "window_common.cuh"
 

@@ -41,6 +41,7 @@ struct Window18 {
     const int32_t* sample_steps = nullptr;  // [nsamples] 1-based step index after which sample k is taken
     uint32_t* status = nullptr;          // [n] OR-ed status bits
     int threads = 128;
+    int split = -1;                      // 11-DOF split-warp kernel: -1 small fleets, 0 never, 1 always
 };
 
 // Launch one stepping window on `stream`. Returns cudaSuccess or the launch error.
@@ -69,9 +70,10 @@ int k24_count();
 cudaError_t launch_check_tables(const double* rows, long long ntables, int nrows, unsigned* bad_dev,
                                 cudaStream_t stream);
 
-// Measured FP64 fused-multiply-add throughput of the current device, in DFMA instructions per second
-// (a dependent-chain-free kernel timed with CUDA events).
-cudaError_t measure_dfma_rate(double* dfma_per_s);
+// Measured FP64 fused-multiply-add throughput of the current device, in DFMA lane operations per
+// second (a kernel of independent chains timed with CUDA events), and the SM clock it ran at in GHz
+// (clock counter over the global timer; sm_ghz may be null).
+cudaError_t measure_dfma_rate(double* dfma_per_s, double* sm_ghz);
 
 // Host-side conversion of a class record into the device table (computes segment reciprocals).
 void build_class_dev18(const lfdm_class18& c, ClassDev18* out);

@@ -12,10 +12,12 @@
 // memory.
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include <cmath>
 #include <cstring>
 
-#include "dof18_device.cuh"
+#include "../../include/lfdm/device/dof18_device.cuh"
 #include "dof18_mixed.cuh"
 #include "kernels.h"
 #include "window_common.cuh"
@@ -140,9 +142,19 @@ cudaError_t launch_check_tables(const double* rows, long long ntables, int nrows
     return cudaGetLastError();
 }
 
+// FP64 pipe probe: every thread runs 8 independent DFMA chains (enough to keep a sub-partition's
+// FP64 unit busy: on GB300 it accepts one warp-wide DFMA every 64 cycles whatever the number of
+// active lanes, so the rate is set by warp instructions, not by latency), 8 warps per sub-partition.
+// Thread 0 of every block reads the SM clock counter and the global nanosecond timer at its start
+// and end, which gives the SM clock the probe ran at.
 constexpr int kProbeIter = 4096;
-__global__ void dfma_probe_kernel(double* out, double seed) {
+__global__ void __launch_bounds__(1024) dfma_probe_kernel(double* out, long long* clk, double seed) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    long long c0 = 0, t0 = 0;
+    if (threadIdx.x == 0) {
+        c0 = clock64();
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    }
     double a[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) a[k] = seed + tid * 1e-9 + k * 0.1;
@@ -156,35 +168,61 @@ __global__ void dfma_probe_kernel(double* out, double seed) {
 #pragma unroll
     for (int k = 0; k < 8; ++k) s += a[k];
     out[tid] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long t1 = 0;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+        clk[2 * blockIdx.x] = clock64() - c0;
+        clk[2 * blockIdx.x + 1] = t1 - t0;
+    }
 }
 
-cudaError_t measure_dfma_rate(double* rate) {
+cudaError_t measure_dfma_rate(double* rate, double* sm_ghz) {
     int dev = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    const int threads = 256, blocks = sms * 8;
+    const int threads = 1024, blocks = sms;  // 32 warps per SM, 8 per sub-partition
     double* out = nullptr;
+    long long* clk = nullptr;
     if ((e = cudaMalloc(&out, sizeof(double) * threads * blocks)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&clk, sizeof(long long) * 2 * blocks)) != cudaSuccess) {
+        cudaFree(out);
+        return e;
+    }
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
-    dfma_probe_kernel<<<blocks, threads>>>(out, 0.5);
+    dfma_probe_kernel<<<blocks, threads>>>(out, clk, 0.5);
     float best = 1e30f;
-    for (int r = 0; r < 3; ++r) {
+    double ghz = 0;
+    std::vector<long long> h(2 * (size_t)blocks);
+    for (int r = 0; r < 5; ++r) {
         cudaEventRecord(a);
-        dfma_probe_kernel<<<blocks, threads>>>(out, 0.5);
+        dfma_probe_kernel<<<blocks, threads>>>(out, clk, 0.5);
         cudaEventRecord(b);
         cudaEventSynchronize(b);
         float ms = 0;
         cudaEventElapsedTime(&ms, a, b);
-        best = ms < best ? ms : best;
+        if (ms < best) {
+            best = ms;
+            if (cudaMemcpy(h.data(), clk, h.size() * sizeof(long long), cudaMemcpyDeviceToHost) == cudaSuccess) {
+                double cyc = 0, ns = 0;
+                for (int k = 0; k < blocks; ++k) {
+                    cyc += (double)h[2 * k];
+                    ns += (double)h[2 * k + 1];
+                }
+                ghz = ns > 0 ? cyc / ns : 0;
+            }
+        }
     }
     e = cudaGetLastError();
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     cudaFree(out);
+    cudaFree(clk);
     *rate = (double)threads * blocks * kProbeIter * 8 / (best * 1e-3);
+    if (sm_ghz) *sm_ghz = ghz;
     return e;
 }
 

@@ -25,7 +25,7 @@
 #include <cstdio>
 #include <cstring>
 
-#include "dof18_device.cuh"
+#include "../../include/lfdm/device/dof18_device.cuh"
 #include "kernels.h"
 
 namespace lfdm {

@@ -88,6 +88,7 @@ struct lfdm_solver {
     unsigned tpb_hint = 32;
     int threads = 128;
     int precision = LFDM_PREC_FP64;
+    int split = -1;  // 11-DOF split-warp kernel: -1 for small fleets, 0 never, 1 always
 
     // CSV output (SetOutput)
     bool output = false;
@@ -399,6 +400,7 @@ int run_windows(lfdm_solver* h, double t0, double t_end, bool solve_all, int ctl
     w.sched = sched_dev;
     w.status = h->d_status.p;
     w.threads = h->threads;
+    w.split = h->split;
 
     std::vector<int32_t> samp;
     double current = solve_all ? 0.0 : t0;
@@ -549,9 +551,13 @@ extern "C" {
 const char* lfdm_version(void) { return "lfdm-gb300 0.1 (sm_103a, FP64 + mixed)"; }
 
 int lfdm_measure_fp64_peak(int device, double* dfma_per_s) {
+    return lfdm_measure_fp64_peak_clock(device, dfma_per_s, nullptr);
+}
+
+int lfdm_measure_fp64_peak_clock(int device, double* dfma_per_s, double* sm_ghz) {
     if (!dfma_per_s) return LFDM_ERR_ARG;
     if (cudaSetDevice(device) != cudaSuccess) return LFDM_ERR_NODEVICE;
-    return measure_dfma_rate(dfma_per_s) == cudaSuccess ? LFDM_OK : LFDM_ERR_CUDA;
+    return measure_dfma_rate(dfma_per_s, sm_ghz) == cudaSuccess ? LFDM_OK : LFDM_ERR_CUDA;
 }
 
 int lfdm_create_on_device(int model, unsigned total_num_vehicles, int device, lfdm_solver** out) {
@@ -996,6 +1002,18 @@ int lfdm_traj18_forward(lfdm_solver* h, const double* ctl, const double* ref, un
     return LFDM_OK;
 }
 
+int lfdm_traj18_branch_signature(lfdm_solver* h, const double* ctl, unsigned nsteps, uint64_t* sig) {
+    if (!h) return LFDM_ERR_ARG;
+    if (!sig) return h->fail(LFDM_ERR_ARG, "null signature array");
+    int rc = traj_guard(h, ctl, ctl, nsteps, 1);
+    if (rc) return rc;
+    CK(h->d_adj_tape.ensure(traj18_tape_doubles_per_step() * h->npad));
+    AdjLaunch A = traj_launch(h, ctl, ctl, nsteps, 0.0, 1);
+    CK(launch_traj18_signature(A, sig, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return LFDM_OK;
+}
+
 int lfdm_traj18_backward(lfdm_solver* h, const double* ctl, const double* ref, unsigned nsteps, double weight_u,
                          unsigned ckpt_every, double* grad_ctl, double* grad_params, double* grad_state0) {
     if (!h) return LFDM_ERR_ARG;
@@ -1219,6 +1237,60 @@ int lfdm_solve_step_schedule(lfdm_solver* h, double t, const double* ctl, unsign
     rc = run_windows(h, t, t, false, CTL_SCHEDULE, 0, 0, 0, nullptr, sched, nsteps, false);
     if (rc) return rc;
     if (t_out) *t_out = t + h->ksim;
+    return LFDM_OK;
+}
+
+int lfdm_device_window_begin(lfdm_solver* h, double t, lfdm_device_window* view) {
+    if (!h || !view) return h ? h->fail(LFDM_ERR_ARG, "null view") : LFDM_ERR_ARG;
+    int rc = step_guard(h);
+    if (rc) return rc;
+    if (h->precision != LFDM_PREC_FP64) return h->fail(LFDM_ERR_ARG, "a device-functor window steps in FP64");
+    rc = sync_device(h);
+    if (rc) return rc;
+    std::vector<int32_t> samp;
+    int nsteps = 0;
+    window_schedule(t, h->ksim, h->step, 0.0, 0, nsteps, samp);
+    CK(cudaMemsetAsync(h->d_status.p, 0, h->N * sizeof(uint32_t), h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    std::memset(view, 0, sizeof(*view));
+    view->model = h->model;
+    view->tire_type = h->tire_type;
+    view->n = (int32_t)h->N;
+    view->npad = h->npad;
+    view->nclasses = (int32_t)h->classes.size();
+    view->nsteps = nsteps;
+    view->kcount = h->model == LFDM_MODEL_24 ? k24_count() : k18_count();
+    view->t0 = t;
+    view->dt = h->step;
+    view->K = h->d_K.p;
+    view->classes = h->d_classes.p;
+    view->class_of = h->d_class_of.p;
+    view->S = h->d_S.p;
+    view->status = h->d_status.p;
+    view->stream = h->stream;
+    h->device_newer = true;  // the caller's kernel steps the device states
+    return LFDM_OK;
+}
+
+int lfdm_device_window_end(lfdm_solver* h, double t, double* t_out) {
+    if (!h) return LFDM_ERR_ARG;
+    int rc = set_device(h);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->stream));
+    h->device_newer = true;
+    h->last_launches = 1;
+    std::vector<uint32_t> st_words(h->N);
+    CK(cudaMemcpy(st_words.data(), h->d_status.p, h->N * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (t_out) *t_out = t + h->ksim;
+    for (size_t i = 0; i < h->N; ++i)
+        if (st_words[i] & 1u) return h->fail(LFDM_ERR_NUMERIC, "vehicle %zu reached a non-finite state", i);
+    return LFDM_OK;
+}
+
+int lfdm_set_split_warps(lfdm_solver* h, int mode) {
+    if (!h) return LFDM_ERR_ARG;
+    if (mode < -1 || mode > 1) return h->fail(LFDM_ERR_ARG, "split-warp mode must be -1, 0 or 1");
+    h->split = mode;
     return LFDM_OK;
 }
 

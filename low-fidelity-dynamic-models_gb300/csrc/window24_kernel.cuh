@@ -4,7 +4,7 @@
 
 #include <cuda_runtime.h>
 
-#include "dof24_device.cuh"
+#include "../../include/lfdm/device/dof24_device.cuh"
 #include "kernels.h"
 #include "window_common.cuh"
 

@@ -3,7 +3,7 @@
 
 #include <cuda_runtime.h>
 
-#include "fp_order.cuh"
+#include "../../include/lfdm/device/fp_order.cuh"
 
 namespace lfdm {
 

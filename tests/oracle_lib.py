@@ -23,12 +23,14 @@ def build() -> str:
 
 
 LIB_FMA = os.path.join(ORACLE_DIR, "_build", "liboracle_fma.so")
+LIB_O3 = os.path.join(ORACLE_DIR, "_build", "liboracle_o3.so")
 _libs = {}
 
 
-def lib(fma: bool = False):
-    """The oracle; fma=True loads the same restatement compiled with FMA contraction."""
-    path = LIB_FMA if fma else LIB
+def lib(fma: bool = False, timing: bool = False):
+    """The oracle; fma=True loads the same restatement compiled with FMA contraction, timing=True the
+    build with the reference's Release flags (-O3) that the CPU baseline times."""
+    path = LIB_O3 if timing else (LIB_FMA if fma else LIB)
     if path not in _libs:
         if not os.path.exists(path):
             build()
@@ -78,7 +80,7 @@ def _ptr(a):
 
 
 def run18(classes, class_of, params, states, tables=None, ctl=None, *, tire_type=0, dt=1e-3, t0=0.0,
-          tend=10.0, ksim=2.0, schedule=1, dtout=0.0, nthreads=1, fma=False, model=18):
+          tend=10.0, ksim=2.0, schedule=1, dtout=0.0, nthreads=1, fma=False, model=18, timing=False):
     """Advance `states` ([n][75] for 18-DOF, [n][42] for 11-DOF; copied) with the oracle. `tables` is
     a list of per-vehicle [rows][4] arrays or one [n][rows][4] array. schedule 0 = CPU solver,
     1 = GPU Solve, 2 = one SolveStep window. Returns (states, resp or None)."""
@@ -117,7 +119,8 @@ def run18(classes, class_of, params, states, tables=None, ctl=None, *, tire_type
               params=_ptr(params), states=_ptr(st), drv_rows=_ptr(rows), drv_off=_ptr(off), drv_len=_ptr(ln),
               ctl=_ptr(ctl_arr), dt=dt, t0=t0, tend=tend, ksim=ksim, schedule=schedule, dtout=dtout,
               resp=_ptr(resp), resp_samples=nsamp, samples_per_window=spw, nthreads=nthreads)
-    fn = {18: lib(fma).oracle18_run, 11: lib(fma).oracle11_run, 24: lib(fma).oracle24_run}[model]
+    L = lib(fma, timing)
+    fn = {18: L.oracle18_run, 11: L.oracle11_run, 24: L.oracle24_run}[model]
     rc = fn(ctypes.byref(a))
     if rc != 0:
         raise RuntimeError(f"oracle18_run failed rc={rc}")

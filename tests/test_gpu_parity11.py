@@ -210,3 +210,41 @@ def test_model11_rejects_mixed_and_mixed_tire_types(built_lib):
     with pytest.raises(built_lib.LfdmError):  # one tire type per solver
         sol.construct_class(cls, p[None, :], built_lib.TireType.TMeasy)
     sol.close()
+
+
+@pytest.mark.parametrize("n,tire", [(1000, 0), (33, 0), (70, 1)])
+def test_split_warp_kernel_bit_exact(built_lib, golden11, n, tire):
+    """The split-warp window kernel (two warps per 32 vehicles, used for small fleets) steps every
+    vehicle bit for bit as the one-warp kernel: final states and every response sample, for the
+    seeded SUV fleet (TMeasy) and the Sedan with TMeasyNr tires, with vehicle counts that leave a
+    block partly empty."""
+    fleet = pkg_mod("fleet")
+    if tire == 0:
+        f = fleet.fleet11(n, seed=n, horizon=3.0)
+        cls, params, tables, states = f["cls"][0], f["params"], f["tables"], f["states"]
+    else:
+        c = {x["name"]: x for x in golden11["cases"]}["sedan11_nr_acc05_gpu"]
+        cls, p, s, tab = case_inputs11(c)
+        params = np.repeat(p[None], n, axis=0)
+        rng = np.random.default_rng(3)
+        states = np.repeat(s[None], n, axis=0)
+        S11 = pkg_mod("_abi").S11
+        states[:, S11["u"]] = rng.uniform(0.0, 25.0, n)
+        tables = np.repeat(tab[None, :301], n, axis=0)
+    out = []
+    for mode in (0, 1):
+        sol = built_lib.d11SolverHalfImplicitGPU(n)
+        sol.construct_class(cls, params, tire)
+        sol.set_driver_tables(tables)
+        sol.set_states(states)
+        sol.SetKernelSimTime(1.0)
+        sol.SetEndTime(3.0)
+        sol.set_split_warps(mode)
+        resp = np.full((304, built_lib.RESP11, n), np.nan)
+        sol.set_response_buffer(resp, 100.0)
+        sol.Solve()
+        out.append((sol.get_states(), resp))
+        sol.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1][:300], out[1][1][:300])
+    assert np.isfinite(out[1][0][:, :6]).all()
