@@ -1,12 +1,16 @@
 """Hand-written adjoint of the 18-DOF half-implicit step (Rollout18, lfdm_traj18_*): gradients of
 the rollout loss with respect to per-step controls and to five parameters, checked against central
 finite differences (h = 1e-6) of the GPU rollout and of the reference algorithm on the CPU (the
-oracle restatement stepped with the same controls), through torch.autograd.
+oracle restatement stepped with the same controls), through torch.autograd, over the
+differentiation config's 2 s horizon (2,000 steps, a checkpoint every 100).
 
-Tolerance: median relative error of directional derivatives <= 1e-6 and >= 90% of vehicles
-<= 1e-5. The rest are vehicles where the +-h perturbation crosses a branch of the tire model or the
-drivetrain (regime boundary of tmxy_combined, sineStep band, clamp, gear shift), which a finite
-difference straddles and the adjoint, differentiating the branch taken, does not.
+A central difference straddles a kink of the loss where the +h and -h rollouts take different
+branches somewhere along the 2,000 steps (a tmxy_combined regime boundary, a sineStep band, a clamp,
+a map segment, a gear shift); the adjoint differentiates the branch taken. Such rollouts are
+detected, not assumed: lfdm_traj18_branch_signature hashes every discrete decision of every step,
+and a direction is excluded exactly when its +h and -h rollouts have different signatures. Every
+other directional derivative must match to 1e-6 relative; the excluded count is printed and capped
+at 5 %.
 """
 import numpy as np
 import pytest
@@ -19,28 +23,52 @@ pytestmark = pytest.mark.gpu
 DT = 1e-3
 
 
-def _setup(lfdm, n=64, T=300, seed=3, ckpt=100):
+def _setup(lfdm, n=64, T=2000, seed=3, ckpt=100, copies=1, chaotic=False):
+    """n seeded SUV vehicles on clothoid reference paths with sine steering and constant throttle
+    U[0.5, 0.9]; each vehicle appears `copies` times in a row (so that one rollout carries several
+    perturbation directions per vehicle).
+
+    Two choices keep the rollouts where a derivative exists, unless `chaotic` is set:
+      * the wheel inertia is HMMWV-class (fleet.CALM_JW): with the configured SUV's 1.5 kg m^2 the
+        explicit wheel-speed update chatters at dt = 1e-3 and the 2 s rollouts are rounding-chaotic
+        (the reference algorithm built with fused multiply-adds moves the loss of 14 of 64 such
+        vehicles by up to 3e-4), so a central difference at h = 1e-6 measures no derivative;
+      * the crank starts 20 % above the speed the wheels drive it at, so the torque converter runs
+        in forward flow: started exactly at lock-up (speed ratio 1) it flips between forward and
+        reverse flow every few steps, and the reference's converter torque jumps by 2 (omega_in /
+        cf)^2 at each flip (computePowertrainRHS, 18dof-gpu/dof18_gpu.cu:683-716)."""
     torch = pytest.importorskip("torch")
     fleet = pkg_mod("fleet")
+    abi = pkg_mod("_abi")
     rng = np.random.default_rng(seed)
     cls, base = fleet.suv18()
+    if not chaotic:
+        base = base.copy()
+        base[abi.P["jw"]] = fleet.CALM_JW
     params = fleet.jitter_params(base, n, rng)
     ref, v = fleet.clothoid_refs(n, T, DT, rng, speed=(8.0, 18.0))
     states = fleet.states_at_speed(cls, params, v)
-    sol = lfdm.d18SolverHalfImplicitGPU(n)
-    sol.construct_class(cls, params)
-    sol.set_states(states)
-    sol.SetTimeStep(DT)
+    states[:, abi.S["crankomega"]] *= 1.2
     t = np.arange(T) * DT
     A = rng.uniform(-0.08, 0.08, n)
     f = rng.uniform(0.5, 2.0, n)
     ctl = np.zeros((T, 3, n))
     ctl[:, 0, :] = A[None, :] * np.sin(2 * np.pi * f[None, :] * t[:, None])
-    ctl[:, 1, :] = rng.uniform(0.2, 0.5, n)[None, :]
+    ctl[:, 1, :] = rng.uniform(0.5, 0.9, n)[None, :]
+    if copies > 1:
+        params = np.repeat(params, copies, axis=0)
+        states = np.repeat(states, copies, axis=0)
+        ctl = np.repeat(ctl, copies, axis=2)
+        ref = np.repeat(ref, copies, axis=2)
+    N = n * copies
+    sol = lfdm.d18SolverHalfImplicitGPU(N)
+    sol.construct_class(cls, params)
+    sol.set_states(states)
+    sol.SetTimeStep(DT)
     dev = torch.device("cuda", 0)
     return {"sol": sol, "cls": cls, "params": params, "states": states, "ctl": ctl, "ref": ref,
             "ctl_t": torch.tensor(ctl, dtype=torch.float64, device=dev),
-            "ref_t": torch.tensor(ref, dtype=torch.float64, device=dev), "T": T, "n": n,
+            "ref_t": torch.tensor(ref, dtype=torch.float64, device=dev), "T": T, "n": N,
             "ro": lfdm.Rollout18(sol, T, ckpt_every=ckpt)}
 
 
@@ -48,9 +76,30 @@ def _rel(a, b, floor):
     return np.abs(a - b) / np.maximum(np.abs(b), floor)
 
 
-def test_control_gradient_matches_finite_differences(built_lib):
+def _signature(S, ctl_t):
     torch = pytest.importorskip("torch")
-    S = _setup(built_lib)
+    sig = torch.empty(S["n"], dtype=torch.int64, device=ctl_t.device)
+    S["ro"].branch_signature(ctl_t.contiguous(), sig)
+    return sig.cpu().numpy()
+
+
+def _check(name, ad, fd, same, floor, cap=0.05):
+    e = _rel(ad, fd, floor)
+    ex = ~same
+    kept = e[same]
+    print(f"{name}: {int(ex.sum())}/{len(e)} directions excluded (branches differ between +h and -h); kept: "
+          f"median {np.median(kept) if kept.size else 0:.2e}, max {kept.max() if kept.size else 0:.2e}; "
+          f"excluded max {e[ex].max() if ex.any() else 0:.2e}")
+    assert ex.mean() <= cap, (name, int(ex.sum()))
+    assert (kept <= 1e-6).all(), (name, float(kept.max()), int(np.argmax(np.where(same, e, 0))))
+
+
+def test_control_gradient_matches_finite_differences(built_lib):
+    """64 vehicles x 16 random directions of the 2,000 x 3 control sequence (steering and throttle),
+    each vehicle's 16 directions carried by 16 copies of it in one rollout."""
+    torch = pytest.importorskip("torch")
+    nd = 16
+    S = _setup(built_lib, n=64, copies=nd)
     ro, n, T = S["ro"], S["n"], S["T"]
     c = S["ctl_t"].clone().requires_grad_(True)
     loss = ro.loss(c, S["ref_t"])
@@ -64,17 +113,19 @@ def test_control_gradient_matches_finite_differences(built_lib):
     dt_ = torch.tensor(d, dtype=torch.float64, device=c.device)
     lp = torch.empty(n, dtype=torch.float64, device=c.device)
     lm = torch.empty_like(lp)
-    ro.forward_raw((S["ctl_t"] + h * dt_).contiguous(), S["ref_t"], lp)
-    ro.forward_raw((S["ctl_t"] - h * dt_).contiguous(), S["ref_t"], lm)
+    cp = (S["ctl_t"] + h * dt_).contiguous()
+    cm = (S["ctl_t"] - h * dt_).contiguous()
+    ro.forward_raw(cp, S["ref_t"], lp)
+    ro.forward_raw(cm, S["ref_t"], lm)
+    same = _signature(S, cp) == _signature(S, cm)
     fd = (lp - lm).cpu().numpy() / (2 * h)
     ad = np.einsum("tcn,tcn->n", g, d)
-    e = _rel(ad, fd, 1e-8 * np.abs(loss.detach().cpu().numpy()).max())
-    print(f"control gradient: median rel err {np.median(e):.2e}, p90 {np.quantile(e, 0.9):.2e}, max {e.max():.2e}")
-    assert np.median(e) <= 1e-6
-    assert (e <= 1e-5).mean() >= 0.9
+    _check("control gradient", ad, fd, same, 1e-8 * np.abs(loss.detach().cpu().numpy()).max())
 
 
 def test_parameter_gradients_match_finite_differences(built_lib):
+    """64 vehicles x the 5 parameters (mass, Jz, CG-to-front distance, tire friction scale, tire
+    vertical stiffness), central differences with steps of 1e-6 of each parameter's scale."""
     torch = pytest.importorskip("torch")
     S = _setup(built_lib, seed=4)
     ro, n = S["ro"], S["n"]
@@ -87,30 +138,29 @@ def test_parameter_gradients_match_finite_differences(built_lib):
     scales = [base[:, P["m"]], base[:, P["jz"]], base[:, P["a"]], np.ones(n), base[:, P["kt"]]]
     for j, name in enumerate(built_lib.ROLLOUT_PARAMS):
         h = 1e-6 * scales[j]
-        out = []
+        out, sigs = [], []
         for sgn in (1.0, -1.0):
             th = torch.zeros(5, n, dtype=torch.float64, device="cuda")
             th[j] = torch.tensor(sgn * h, dtype=torch.float64, device="cuda")
             with torch.no_grad():
                 out.append(ro.loss(S["ctl_t"], S["ref_t"], th).cpu().numpy())
+            sigs.append(_signature(S, S["ctl_t"]))  # at the parameters the loss call applied
         fd = (out[0] - out[1]) / (2 * h)
-        e = _rel(g[j], fd, 1e-8 * np.abs(fd).max())
-        print(f"{name}: median rel err {np.median(e):.2e}, max {e.max():.2e}")
-        assert np.median(e) <= 1e-6, name
-        assert (e <= 1e-5).mean() >= 0.9, name
+        _check(name, g[j], fd, sigs[0] == sigs[1], 1e-8 * np.abs(fd).max())
 
 
-def _oracle_loss(S, ctl, idx):
+def _oracle_loss(S, ctl, idx, fma=False):
     """The rollout loss of vehicles idx with the reference algorithm on the CPU (the oracle stepped
-    one step at a time with the step's controls)."""
+    one step at a time with the step's controls; fma: its build with fused multiply-adds)."""
     st = S["states"][idx].copy()
     cls = S["cls"]
     P = S["params"][idx]
     L = np.zeros(len(idx))
+    Sx = pkg_mod("_abi").S
     for k in range(S["T"]):
         u = ctl[k][:, idx].T.copy()
-        st, _ = O.run18([cls], np.zeros(len(idx), np.int32), P, st, ctl=u, t0=k * DT, dt=DT, ksim=DT, schedule=2)
-        Sx = pkg_mod("_abi").S
+        st, _ = O.run18([cls], np.zeros(len(idx), np.int32), P, st, ctl=u, t0=k * DT, dt=DT, ksim=DT, schedule=2,
+                        fma=fma)
         xr, yr, pr = S["ref"][k][:, idx]
         el = -(st[:, Sx["x"]] - xr) * np.sin(pr) + (st[:, Sx["y"]] - yr) * np.cos(pr)
         eh = st[:, Sx["psi"]] - pr
@@ -119,27 +169,34 @@ def _oracle_loss(S, ctl, idx):
 
 
 def test_gradient_against_reference_algorithm_on_cpu(built_lib):
-    """The adjoint's directional derivative against a central difference of the reference
-    algorithm itself (oracle), and the GPU loss against the oracle's loss."""
+    """64 vehicles over the 2,000 steps: the GPU loss against the loss of the reference algorithm
+    (oracle), and the adjoint's directional derivative against a central difference of the
+    reference algorithm itself where the GPU's +h and -h rollouts take the same branches."""
     torch = pytest.importorskip("torch")
-    S = _setup(built_lib, n=16, T=200, seed=5)
-    ro = S["ro"]
+    S = _setup(built_lib, n=64, seed=5)
+    ro, n = S["ro"], S["n"]
     c = S["ctl_t"].clone().requires_grad_(True)
     loss = ro.loss(c, S["ref_t"])
     loss.sum().backward()
     g = c.grad.detach().cpu().numpy()
-    idx = np.arange(4)
+    idx = np.arange(n)
     lo = _oracle_loss(S, S["ctl"], idx)
-    assert np.allclose(loss.detach().cpu().numpy()[idx], lo, rtol=1e-10, atol=0)
+    # the reference algorithm's own rounding sensitivity: its build with fused multiply-adds (a gear
+    # shift that a rounding difference moves by one step changes the loss by more than 1e-9)
+    env = _rel(_oracle_loss(S, S["ctl"], idx, fma=True), lo, 0.0)
+    el = _rel(loss.detach().cpu().numpy(), lo, 0.0)
+    print(f"GPU loss vs oracle: max rel {el.max():.2e} (oracle FMA build {env.max():.2e}); "
+          f"{int((el > 1e-9).sum())} vehicles beyond 1e-9")
+    assert (el <= np.maximum(1e-9, 100 * env)).all(), (float(el.max()), int(el.argmax()))
     rng = np.random.default_rng(2)
     d = np.zeros_like(S["ctl"])
     d[:, 0, :] = rng.standard_normal(d[:, 0, :].shape) * 0.05
     h = 1e-6
     fd = (_oracle_loss(S, S["ctl"] + h * d, idx) - _oracle_loss(S, S["ctl"] - h * d, idx)) / (2 * h)
-    ad = np.einsum("tcn,tcn->n", g[:, :, idx], d[:, :, idx])
-    e = _rel(ad, fd, 1e-8 * np.abs(lo).max())
-    print("adjoint vs oracle central difference:", e)
-    assert np.median(e) <= 1e-6
+    dt_ = torch.tensor(d, dtype=torch.float64, device=c.device)
+    same = _signature(S, (S["ctl_t"] + h * dt_).contiguous()) == _signature(S, (S["ctl_t"] - h * dt_).contiguous())
+    ad = np.einsum("tcn,tcn->n", g, d)
+    _check("adjoint vs oracle central difference", ad, fd, same, 1e-8 * np.abs(lo).max())
 
 
 def test_checkpoint_interval_does_not_change_gradients(built_lib):
@@ -155,12 +212,16 @@ def test_checkpoint_interval_does_not_change_gradients(built_lib):
 
 
 def test_backward_forward_time_ratio(built_lib):
+    """The differentiation config: the configured SUV (1.5 kg m^2 wheels), 65,536 vehicles x 2,000
+    steps, a checkpoint every 100 steps. Target: the gradient costs at most 3x the forward rollout."""
     torch = pytest.importorskip("torch")
-    S = _setup(built_lib, n=8192, T=500, seed=7)
+    S = _setup(built_lib, n=65536, T=2000, seed=7, chaotic=True)
     ro = S["ro"]
     c = S["ctl_t"].clone().requires_grad_(True)
-    loss = ro.loss(c, S["ref_t"])
-    loss.sum().backward()
+    for _ in range(2):  # the first pass allocates the checkpoints and the tape
+        c.grad = None
+        loss = ro.loss(c, S["ref_t"])
+        loss.sum().backward()
     fwd, bwd = ro.last_ms()
     print(f"forward {fwd:.2f} ms, backward {bwd:.2f} ms, ratio {bwd / fwd:.2f}")
-    assert bwd / fwd < 6.0
+    assert bwd / fwd < 3.0
