@@ -37,6 +37,13 @@ W_ALG = {11: 675, 18: 1391, 24: 1941}  # the same count for the three models
 # FP64 thread-instructions the 18-DOF window kernel executes per vehicle-step (ncu instruction
 # counters of one capture, DFMA + DMUL + DADD + the divide and square-root sequences)
 FP64_INST_PER_VSTEP_18 = 1029
+# The mixed-precision forms of the 18-DOF stepper: (precision enum, key, arithmetic)
+MIXED_FORMS = ((1, "mixed", "f32 RHS and tire math; f64 states, X/Y/yaw accumulation, slip and transport velocities"),
+               (2, "mixed_tire", "f32 TMeasy tire core; f64 everything else"))
+# Thread-level instructions per vehicle-step of the mixed window kernels, (FP32, FP64): ncu
+# sm__sass_thread_inst_executed_op_{ffma,fmul,fadd}_pred_on.sum and _{dfma,dmul,dadd}_pred_on.sum
+# of one window launch on 32,768 vehicles of the seeded fleet, divided by its vehicle-steps
+MIXED_INST_PER_VSTEP = {1: None, 2: None}
 METRIC = "18-DOF vehicle-steps/s on 1 GB300: FP64 plain vs mixed at stated error; adjoint/fwd"
 
 
@@ -59,8 +66,11 @@ def _args():
     ap.add_argument("--adjoint-vehicles", type=int, default=65_536)
     ap.add_argument("--no-jacobian", action="store_true", help="skip the right-hand-side Jacobian line")
     ap.add_argument("--jacobian-vehicles", type=int, default=65_536)
-    ap.add_argument("--error-vehicles", type=int, default=65536)
+    ap.add_argument("--error-vehicles", type=int, default=1_000_000,
+                    help="vehicles of the mixed-precision error run (the precision config's 1,000,000)")
     ap.add_argument("--error-horizon", type=float, default=20.0)
+    ap.add_argument("--ceiling-vehicles", type=int, default=65536,
+                    help="vehicles of the FP64-sensitivity runs that bound what any FP32-based form can hold")
     ap.add_argument("--cpu-sample", type=int, default=32768, help="vehicles in the CPU-baseline sample")
     return ap.parse_args()
 
@@ -213,19 +223,13 @@ def _config(a, n_override=None):
             "l2": "inputs larger than L2 (driver tables ~32 KB/vehicle, state 600 B, constants 560 B)"}
 
 
-def _mixed_error(lfdm, fleet, dev, n, horizon):
-    """End-of-horizon error of the mixed form against the FP64 form: the seeded fleet with initial
-    speeds U[0.5, 30] m/s (near-standstill starts stress the low-speed slip path). Also the FP64
-    form's own sensitivity: the same FP64 run from initial speeds u (1 + eps) for eps = 1e-15 (FP64
-    rounding level) and 1e-7 (FP32 rounding level). Vehicles the 1e-15 run moves by more than 1 cm are
-    rounding-chaotic (no FP64 implementation with other rounding holds them to 1 cm either); those
-    the 1e-7 run moves that far are beyond what any FP32-based arithmetic can hold. The mixed error
-    is also reported over the vehicles each run leaves within 1 cm."""
-    f = fleet.fleet18(n, seed=SEED + 7, horizon=horizon, u0_range=(0.5, 30.0))
+def _error_runs(lfdm, dev, f, horizon, runs):
+    """Final states of the seeded fleet `f` after `horizon` seconds for each (key, precision, eps):
+    the initial speeds scaled by (1 + eps)."""
     S = lfdm.S
     out = {}
-    for key, prec, eps in (("fp64", 0, 0.0), ("mixed", 1, 0.0), ("fp64_1e-15", 0, 1e-15), ("fp64_1e-7", 0, 1e-7)):
-        s = lfdm.d18SolverHalfImplicitGPU(n, device=dev)
+    for key, prec, eps in runs:
+        s = lfdm.d18SolverHalfImplicitGPU(f["params"].shape[0], device=dev)
         s.construct_class(f["cls"][0], f["params"])
         s.set_driver_tables(f["tables"])
         st0 = np.array(f["states"], copy=True)
@@ -237,29 +241,62 @@ def _mixed_error(lfdm, fleet, dev, n, horizon):
         s.Solve()
         out[key] = s.get_states()
         s.close()
-    a, b = out["fp64"], out["mixed"]
+    return out
 
-    def dpos(x, y):
-        return np.hypot(y[:, S["x"]] - x[:, S["x"]], y[:, S["y"]] - x[:, S["y"]])
 
-    pos = dpos(a, b)
-    yaw = np.abs(b[:, S["psi"]] - a[:, S["psi"]])
-    spd = np.abs(np.hypot(b[:, S["u"]], b[:, S["v"]]) - np.hypot(a[:, S["u"]], a[:, S["v"]]))
+def _dpos(S, x, y):
+    return np.hypot(y[:, S["x"]] - x[:, S["x"]], y[:, S["y"]] - x[:, S["y"]])
 
-    def st(e):
-        return {"max": float(e.max()), "p99": float(np.quantile(e, 0.99)), "p50": float(np.median(e))}
 
-    sens = {}
-    for eps in ("1e-15", "1e-7"):
-        d = dpos(a, out["fp64_" + eps])
-        stable = d <= 0.01
-        sens["u0_x(1+" + eps + ")"] = {
-            "position_m": st(d), "frac_within_1cm": float(stable.mean()),
-            "mixed_frac_within_1cm_on_these_stable": float((pos[stable] <= 0.01).mean()) if stable.any() else None}
+def _stats(e):
+    return {"max": float(e.max()), "p99": float(np.quantile(e, 0.99)), "p50": float(np.median(e))}
 
-    return {"vehicles": n, "horizon_s": horizon, "u0_range": [0.5, 30.0], "position_m": st(pos), "yaw_rad": st(yaw),
-            "fp64_sensitivity": sens,
-            "speed_mps": st(spd), "frac_position_within_1cm": float((pos <= 0.01).mean())}
+
+def _mixed_error(lfdm, fleet, dev, n, horizon):
+    """End-of-horizon position, yaw and speed error of each mixed form against the FP64 form (max,
+    p99, p50 over vehicles, and the fraction within 1 cm): the seeded fleet at n vehicles with
+    initial speeds U[0.5, 30] m/s (near-standstill starts stress the low-speed slip path) and driver
+    tables sampled every 50 ms (the 10 ms tables of 1,000,000 vehicles over 20 s would take 64 GB)."""
+    f = fleet.fleet18(n, seed=SEED + 7, horizon=horizon, table_dt=0.05, u0_range=(0.5, 30.0))
+    runs = [("fp64", 0, 0.0)] + [(key, prec, 0.0) for prec, key, _ in MIXED_FORMS]
+    out = _error_runs(lfdm, dev, f, horizon, runs)
+    del f
+    S = lfdm.S
+    a = out["fp64"]
+    res = {"vehicles": n, "horizon_s": horizon, "u0_range": [0.5, 30.0], "table_dt_s": 0.05}
+    for _, key, _ in MIXED_FORMS:
+        b = out[key]
+        pos = _dpos(S, a, b)
+        yaw = np.abs(b[:, S["psi"]] - a[:, S["psi"]])
+        spd = np.abs(np.hypot(b[:, S["u"]], b[:, S["v"]]) - np.hypot(a[:, S["u"]], a[:, S["v"]]))
+        res[key] = {"position_m": _stats(pos), "yaw_rad": _stats(yaw), "speed_mps": _stats(spd),
+                    "frac_position_within_1cm": float((pos <= 0.01).mean()),
+                    "finite": bool(np.isfinite(b[:, :15]).all())}
+    return res
+
+
+def _mixed_retention(lfdm, fleet, dev, n, horizon):
+    """What FP32-level rounding costs beyond the fleet's own sensitivity. The FP64 form is rerun from
+    initial speeds u (1 + 1e-15) (FP64 rounding level) and u (1 + 1e-7) (FP32 rounding level, applied
+    once). Vehicles the 1e-7 run leaves within 1 cm of FP64 are insensitive at FP32 level; the
+    retention of a form is the fraction of those that it also ends within 1 cm of FP64. The 1e-15
+    run's own retention is the ceiling: vehicles that even an FP64-level perturbation moves past
+    1 cm are lost to rounding-level chaos whatever the arithmetic."""
+    f = fleet.fleet18(n, seed=SEED + 7, horizon=horizon, table_dt=0.05, u0_range=(0.5, 30.0))
+    runs = [("fp64", 0, 0.0), ("fp64_1e-15", 0, 1e-15), ("fp64_1e-7", 0, 1e-7)]
+    runs += [(key, prec, 0.0) for prec, key, _ in MIXED_FORMS]
+    out = _error_runs(lfdm, dev, f, horizon, runs)
+    S = lfdm.S
+    a = out["fp64"]
+    d = {k: _dpos(S, a, v) for k, v in out.items() if k != "fp64"}
+    stable = d["fp64_1e-7"] <= 0.01
+    res = {"vehicles": n, "horizon_s": horizon, "insensitive_at_1e-7": float(stable.mean()),
+           "fp64_1e-15_within_1cm": float((d["fp64_1e-15"] <= 0.01).mean()),
+           "ceiling_fp64_1e-15_retention": float((d["fp64_1e-15"][stable] <= 0.01).mean())}
+    for _, key, _ in MIXED_FORMS:
+        res[key + "_retention"] = float((d[key][stable] <= 0.01).mean())
+        res[key + "_within_1cm"] = float((d[key] <= 0.01).mean())
+    return res
 
 
 def _model_rate(lfdm, fleet, dev, model: int, n: int, windows: int, ksim: float, peak_tflops: float) -> dict:
@@ -310,6 +347,13 @@ def _fleet_bench(lfdm, fleet, dev, n: int, torch) -> dict:
     f.solve()
     ms, launches = f.last_ms()
     finite = {m: bool(np.isfinite(f.get_states(m)[:, :8]).all()) for m in (18, 24)}
+    # the same solve from the same states without model affinity (every SM starts on the 18-DOF tiles)
+    for m in (18, 24):
+        f.set_states(m, np.concatenate([g["states"] for g in mf["groups"] if g["model"] == m]))
+    frac18 = f.get_affinity()[1]
+    f.set_affinity(False)
+    f.solve()
+    ms_noaff, _ = f.last_ms()
     f.close()
     vs = info["vehicle_steps"]
     # baseline: per-group solvers, kernel time summed over the groups
@@ -352,7 +396,11 @@ def _fleet_bench(lfdm, fleet, dev, n: int, torch) -> dict:
                                    "solver_runs": groups, "gpu_launches": base_launches,
                                    "what": "one window-kernel solver per (model, class, window count), "
                                            "kernel time summed"},
-            "speedup_vs_per_group": value / base_value, "finite_states": finite}
+            "speedup_vs_per_group": value / base_value, "finite_states": finite,
+            "model_affinity": {"frac18_of_work": frac18, "ms_with": ms, "ms_without": ms_noaff,
+                               "speedup": ms_noaff / ms,
+                               "what": "SMs split between the 18-DOF and 24-DOF tile lists in proportion to their "
+                                       "estimated work, against all SMs taking the 18-DOF tiles first"}}
 
 
 def _adjoint_bench(lfdm, fleet, dev, n: int, nsteps: int, torch) -> dict:
@@ -559,29 +607,56 @@ def run_ours(a, dist: Dist):
                "h2d_bytes_per_step": int(win_tabs[0].nbytes), "d2h_bytes_per_step": int(per_window * 8),
                "ms_per_step": 1e3 * e2e_wall / K}
 
-    # mixed precision: throughput on the same fleet and windows, accuracy against the FP64 path
+    # mixed precision: throughput of both forms on the same fleet and windows, accuracy against the
+    # FP64 path (the precision config at 1,000,000 vehicles) and against the fleet's own sensitivity
     mixed = None
+    peak_ffma, probe32_ghz = (lfdm.measure_fp32_peak_clock(dev) if not a.no_mixed else (None, None))
     if not a.no_mixed:
-        solm = lfdm.d18SolverHalfImplicitGPU(n, device=dev)
-        solm.construct_class(f["cls"][0], f["params"])
-        solm.set_driver_tables(f["tables"])
-        solm.set_states(f["states"])
-        solm.SetKernelSimTime(ksim)
-        solm.SetEndTime(horizon)
-        solm.set_precision(1)
-        if a.threads:
-            solm.SetThreadsPerBlock(a.threads)
-        solm.set_response_device(dresp.data_ptr(), dresp.numel(), 100.0)
-        solm.solve_range(-0.5 * ksim, (W - 0.5) * ksim)
-        torch.cuda.synchronize()
-        solm.solve_range((W - 0.5) * ksim, (W + K - 0.5) * ksim)
-        mms, mlaunch = solm.last_kernel_ms()
-        solm.close()
-        mvalue = dist.sum(vsteps_rank) / (dist.max(mms) * 1e-3)
-        mixed = {"value": mvalue, "unit": "vehicle-steps/s", "speedup_vs_fp64": mvalue / value,
-                 "ms_per_step": mms / K, "gpu_launches": mlaunch, "dtype": "f32 RHS + f64 states/X/Y/yaw/slip"}
+        mixed = {}
+        for prec, key, arith in MIXED_FORMS:
+            solm = lfdm.d18SolverHalfImplicitGPU(n, device=dev)
+            solm.construct_class(f["cls"][0], f["params"])
+            solm.set_driver_tables(f["tables"])
+            solm.set_states(f["states"])
+            solm.SetKernelSimTime(ksim)
+            solm.SetEndTime(horizon)
+            solm.set_precision(prec)
+            if a.threads:
+                solm.SetThreadsPerBlock(a.threads)
+            solm.set_response_device(dresp.data_ptr(), dresp.numel(), 100.0)
+            solm.solve_range(-0.5 * ksim, (W - 0.5) * ksim)
+            torch.cuda.synchronize()
+            solm.solve_range((W - 0.5) * ksim, (W + K - 0.5) * ksim)
+            mms, mlaunch = solm.last_kernel_ms()
+            solm.close()
+            mvalue = dist.sum(vsteps_rank) / (dist.max(mms) * 1e-3)
+            mixed[key] = {"precision": prec, "value": mvalue, "unit": "vehicle-steps/s",
+                          "speedup_vs_fp64": mvalue / value, "ms_per_step": mms / K, "gpu_launches": mlaunch,
+                          "dtype": arith}
         mixed["error_vs_fp64"] = _mixed_error(lfdm, fleet, dev, a.error_vehicles, a.error_horizon)
+        mixed["retention"] = _mixed_retention(lfdm, fleet, dev, a.ceiling_vehicles, a.error_horizon)
     peak_dfma, probe_ghz = lfdm.measure_fp64_peak_clock(dev)
+    if mixed:
+        # issue roofline of each mixed form: its FP32 and FP64 thread-instructions per second against
+        # the FFMA and DFMA probes (separate pipes, so the larger fraction is the bound)
+        for prec, key, _ in MIXED_FORMS:
+            m, inst = mixed[key], MIXED_INST_PER_VSTEP.get(prec)
+            if inst is None:
+                m["roofline"] = None
+                continue
+            f32, f64 = inst[0] * m["value"] / peak_ffma, inst[1] * m["value"] / peak_dfma
+            fp32_bound = f32 >= f64
+            m["roofline"] = {
+                "bound": "fp32 issue" if fp32_bound else "fp64 issue",
+                "achieved": (inst[0] if fp32_bound else inst[1]) * m["value"],
+                "peak": peak_ffma if fp32_bound else peak_dfma, "unit": "thread-instructions/s",
+                "frac": max(f32, f64), "fp32_frac": f32, "fp64_frac": f64,
+                "inst_per_vehicle_step": {"fp32": inst[0], "fp64": inst[1]},
+                "peak_source": "measured live: FFMA and DFMA throughput kernels (lfdm_measure_fp32_peak_clock, "
+                               "lfdm_measure_fp64_peak_clock)",
+                "probe_fp32_sm_ghz": probe32_ghz, "probe_fp64_sm_ghz": probe_ghz,
+                "inst_source": "ncu sm__sass_thread_inst_executed_op_{ffma,fmul,fadd,dfma,dmul,dadd}_pred_on.sum of "
+                               "one window launch on 32,768 vehicles, per vehicle-step"}
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     max_ghz = (clocks.get("sm_max_mhz") or 2070.0) / 1e3
     # nominal FP64 rate: one warp-wide DFMA per 64 cycles per SM sub-partition = 2 DFMA/clock/SM

@@ -45,9 +45,11 @@ typedef enum { LFDM_MODEL_11 = 11, LFDM_MODEL_18 = 18, LFDM_MODEL_24 = 24 } lfdm
 /* TireType (18dof-gpu/dof18_gpu.cuh:12) */
 typedef enum { LFDM_TIRE_TMEASY = 0, LFDM_TIRE_TMEASY_NR = 1 } lfdm_tire_type;
 
-/* Arithmetic of the stepper. FP64 reproduces the reference; MIXED runs the RHS and tire math in  */
-/* FP32 and keeps FP64 in the X/Y/yaw accumulation and the tire slip and transport velocities.   */
-typedef enum { LFDM_PREC_FP64 = 0, LFDM_PREC_MIXED = 1 } lfdm_precision;
+/* Arithmetic of the stepper. FP64 reproduces the reference; MIXED (18-DOF, TMeasy) runs the RHS  */
+/* and tire math in FP32 and keeps FP64 in the X/Y/yaw accumulation and the tire slip and         */
+/* transport velocities; MIXED_TIRE (11/18/24-DOF, TMeasy) runs only the TMeasy tire core (load    */
+/* interpolation, combined slip, force curve, relaxation) in FP32 and everything else in FP64.    */
+typedef enum { LFDM_PREC_FP64 = 0, LFDM_PREC_MIXED = 1, LFDM_PREC_MIXED_TIRE = 2 } lfdm_precision;
 
 /* ------------------------------------------------------------------------------------------ */
 /* Flat per-vehicle parameter vector (doubles). Vehicle part follows VehicleParam               */
@@ -261,6 +263,9 @@ int lfdm_measure_fp64_peak(int device, double* dfma_per_s);
 /* The same probe with the SM clock it ran at (GHz, from the SM clock counter over the global       */
 /* nanosecond timer), which normalises the rate to DFMA per clock per SM.                          */
 int lfdm_measure_fp64_peak_clock(int device, double* dfma_per_s, double* sm_ghz);
+/* The same probe on FP32 FMA chains: lane FFMA per second and the SM clock it ran at (the FP32     */
+/* issue roofline of the mixed-precision steppers).                                                */
+int lfdm_measure_fp32_peak_clock(int device, double* ffma_per_s, double* sm_ghz);
 
 /* Host-only utilities (no device needed). setVehParamsJSON + setTireParamsJSON + tireInit        */
 /* (dof18_gpu.cu:1075-1330, :227-241) into a class record and a flat parameter vector, and        */
@@ -379,6 +384,12 @@ int lfdm_fleet_set_output(lfdm_fleet* f, double dtout);
 /* and steps per launch (0: the whole horizon in one launch).                                      */
 int lfdm_fleet_set_launch(lfdm_fleet* f, unsigned threads, unsigned blocks_per_sm, unsigned steps_per_launch);
 int lfdm_fleet_get_launch(lfdm_fleet* f, unsigned* threads, unsigned* blocks_per_sm, unsigned* steps_per_launch);
+/* Model affinity (default on): the SMs are split between the 18-DOF and the 24-DOF tiles in      */
+/* proportion to their estimated work (steps x per-step cost); each warp drains its SM's home list */
+/* before it helps with the other. Off: all warps take the 18-DOF tiles first. *frac18 receives   */
+/* the 18-DOF share of the work of the prepared fleet (1 before the first solve or tune).          */
+int lfdm_fleet_set_affinity(lfdm_fleet* f, int on);
+int lfdm_fleet_get_affinity(lfdm_fleet* f, int* on, double* frac18);
 /* Autotuner: times the candidate configurations on the first pilot_steps steps (states restored) */
 /* and keeps the fastest; *best_ms receives its pilot time.                                        */
 int lfdm_fleet_tune(lfdm_fleet* f, unsigned pilot_steps, double* best_ms);

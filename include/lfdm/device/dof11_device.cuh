@@ -75,10 +75,10 @@ __device__ __forceinline__ void rear_kinematics11(const Veh11& v, TireAux& ta, c
     ta.vsy = fma(-v.wz, K(K_B), v.v);
     ta.vsx = v.u;
 }
-template <bool kNr, bool kSteered>
+template <bool kNr, bool kSteered, bool kF32 = false>
 __device__ __forceinline__ void tire11(TireC& ts, TireAux& ta, const KView& K, double cd, double sd) {
     if (kNr) tire_rhs_nr<kSteered>(ts, ta, K, cd, sd);  // computeTireRHS, TMeasyNr (dof11_gpu.cu:470-599)
-    else tire_rhs_tm<kSteered>(ts, ta, K, cd, sd);
+    else tire_rhs_tm<kSteered, kF32>(ts, ta, K, cd, sd);
 }
 // computePowertrainRHS (dof11_gpu.cu:601-745) up to the wheel torques: converter, engine, gear,
 // differential. w0, w1: the front and rear wheel speeds after the tires.
@@ -144,15 +144,15 @@ __device__ __forceinline__ void chassis11(Veh11& v, Veh11Aux& va, const TireC* t
 }
 
 // One right-hand-side evaluation (rhsFun, 11dof-gpu/dof11_halfImplicit_gpu.cu:663-700).
-template <bool kNr>
+template <bool kNr, bool kF32 = false>
 __device__ __forceinline__ void rhs11(Veh11& v, Veh11Aux& va, TireC* ts, TireAux* ta, const KView& K,
                                       const ClassDev18& C, double steering, double throttle, double braking) {
     loads11(v, ta, K);
     double cd, sd;
     front_kinematics11(v, ta[0], K, C, steering, cd, sd);
     rear_kinematics11(v, ta[1], K);
-    tire11<kNr, true>(ts[0], ta[0], K, cd, sd);
-    tire11<kNr, false>(ts[1], ta[1], K, 1.0, 0.0);
+    tire11<kNr, true, kF32>(ts[0], ta[0], K, cd, sd);
+    tire11<kNr, false, kF32>(ts[1], ta[1], K, 1.0, 0.0);
     powertrain11(v, va, ts[0].omega, ts[1].omega, ta[0].engTor, ta[1].engTor, K, C, throttle);
     chassis11(v, va, ts, ta, K, braking, cd, sd);
 }
@@ -187,11 +187,11 @@ __device__ __forceinline__ void update11(Veh11& v, const Veh11Aux& va, TireC* ts
 }
 
 // One step: rhs11 followed by update11.
-template <bool kNr>
+template <bool kNr, bool kF32 = false>
 __device__ __forceinline__ void step11(Veh11& v, Veh11Aux& va, TireC* ts, TireAux* ta, const KView& K,
                                        const ClassDev18& C, double steering, double throttle, double braking,
                                        double dt) {
-    rhs11<kNr>(v, va, ts, ta, K, C, steering, throttle, braking);
+    rhs11<kNr, kF32>(v, va, ts, ta, K, C, steering, throttle, braking);
     update11<kNr>(v, va, ts, ta, C, dt);
 }
 

@@ -306,7 +306,9 @@ __device__ __forceinline__ bool state18_finite(const VehC& v, const TireC* ts) {
 struct KView {
     const double* base;  // base + i*stride
     int stride;
+    const float* fbase = nullptr;  // FP32 copies of the same constants (kernels with an FP32 tire core)
     __device__ __forceinline__ double operator()(int i) const { return base[i * stride]; }
+    __device__ __forceinline__ float f(int i) const { return fbase[i * stride]; }
 };
 
 // tmxy_combined (dof18_gpu.cu:243-285) given the reciprocals of s, sm and fm (is, ism, ifm; the
@@ -507,10 +509,158 @@ __device__ __forceinline__ void tire_core_tm(TireC& ts, TireAux& ta, const KView
     ta.fy = is_zero(wy) ? fydyn : fma(wy, fystr, (1. - wy) * fydyn);
 }
 
+// ---------------------------------------------------------------------------------------------
+// FP32 tire core (precision LFDM_PREC_MIXED_TIRE): the part of computeTireRHS, TMeasy, that dominates
+// a step's FP64 instructions — load interpolation of the curve parameters, slips, combined-slip
+// normalisation, the tmxy_combined curve, the relaxation rates and the structural/dynamic blend —
+// in FP32, on FP32 copies of the derived constants (K.f). Kept in FP64: the slip velocity
+// vsx - omega r_eff and the transport velocity r_eff |omega| + 0.01 (a cancellation of nearly equal
+// terms at rolling without slip), rounded to FP32 before the slips are formed, and the rolling
+// resistance; the wheel speed and the deflections stay FP64 states. The branch structure is that of
+// tire_core_tm.
+
+__device__ __forceinline__ float sine_stepf(float x, float x1, float y1, float x2, float y2) {
+    if (x <= x1) return y1;
+    if (x >= x2) return y2;
+    const float dx = x2 - x1, dy = y2 - y1;
+    const float u = (x - x1) / dx;
+    return y1 + dy * u - (dy * (1.0f / 6.2831853071795865f)) * __sinf(6.2831853071795865f * u);
+}
+
+// tmxy_combined (dof18_gpu.cu:243-285) in FP32: the combined force f and f / s
+__device__ __forceinline__ void tmxyf(float& f, float& fos, float s, float df0, float sm, float fm, float ss,
+                                      float fs) {
+    float df0loc = 0.0f;
+    if (sm > 0.0f) df0loc = fmaxf(2.0f * fm / sm, df0);
+    if (s > 0.0f && df0loc > 0.0f) {
+        if (s > ss) {
+            f = fs;
+            fos = fs / s;
+        } else if (s < sm) {
+            const float p = df0loc * sm / fm - 2.0f;
+            const float sn = s / sm;
+            const float dn = fmaf(sn + p, sn, 1.0f);
+            const float idn = 1.0f / dn;
+            f = df0loc * sm * sn * idn;
+            fos = df0loc * idn;
+        } else {
+            const float q = fm / sm;
+            const float a = q * q / (df0loc * sm);
+            const float sstar = sm + (fm - fs) / (a * (ss - sm));
+            if (sstar <= ss) {
+                if (s <= sstar) {
+                    f = fm - a * (s - sm) * (s - sm);
+                } else {
+                    const float b = a * (sstar - sm) / (ss - sstar);
+                    f = fs + b * (ss - s) * (ss - s);
+                }
+            } else {
+                const float sn = (s - sm) / (ss - sm);
+                f = fm - (fm - fs) * sn * sn * (3.0f - 2.0f * sn);
+            }
+            fos = f / s;
+        }
+    } else {
+        f = 0.0f;
+        fos = 0.0f;
+    }
+}
+
+template <bool kSteered>
+__device__ __forceinline__ void tire_core_tm_f32(TireC& ts, TireAux& ta, const KView& K, double c_d, double s_d,
+                                                 double fz_d, double r_eff_d) {
+    const double omega = ts.omega;
+    const double vsx_d = fma(-omega, r_eff_d, ta.vsx);
+    const double rw_d = r_eff_d * fabs(omega);
+    const float vsx = (float)vsx_d;
+    const float vta = (float)(rw_d + 0.01);
+    const float rw = (float)rw_d;
+    const float vsy = (float)ta.vsy;
+    const float sx = -vsx / vta;
+    float sy;
+    if (kSteered) {
+        const float c = (float)c_d, s = (float)s_d;
+        // -tan(atan2(vsy, vta) - delta) is infinite where the steered wheel's slip angle passes 90
+        // degrees (vta c + vsy s = 0), a denominator FP32 can round to exactly 0: held to +-1e6,
+        // where the force curve is saturated and the direction is the FP64 one to FP32 rounding
+        sy = -(vsy * c - vta * s) / (vta * c + vsy * s);
+        sy = fminf(fmaxf(sy, -1e6f), 1e6f);
+    } else {
+        sy = -vsy / vta;
+    }
+    const float fz = fminf((float)fz_d, K.f(K_PNMAX));
+    const float fzn = fz * K.f(K_INVPN);
+    const float dfx0 = fzn * fmaf(-K.f(K_Q2DFX0), fzn, K.f(K_Q1DFX0));
+    const float dfy0 = fzn * fmaf(-K.f(K_Q2DFY0), fzn, K.f(K_Q1DFY0));
+    const float fxm = fzn * fmaf(-K.f(K_Q2FXM), fzn, K.f(K_Q1FXM));
+    const float fym = fzn * fmaf(-K.f(K_Q2FYM), fzn, K.f(K_Q1FYM));
+    const float fxs = fzn * fmaf(-K.f(K_Q2FXS), fzn, K.f(K_Q1FXS));
+    const float fys = fzn * fmaf(-K.f(K_Q2FYS), fzn, K.f(K_Q1FYS));
+    const float fzn1 = fzn - 1.0f;
+    const float sxm = fmaf(K.f(K_DSXM), fzn1, K.f(K_LSXM));
+    const float sym = fmaf(K.f(K_DSYM), fzn1, K.f(K_LSYM));
+    const float sxs = fmaf(K.f(K_DSXS), fzn1, K.f(K_LSXS));
+    const float sys = fmaf(K.f(K_DSYS), fzn1, K.f(K_LSYS));
+    const float fxd = fxm * dfy0, fyd = fym * dfx0;
+    const float issum = 1.0f / (sxm + sym), ifsum = 1.0f / (fxd + fyd);
+    const float hsxn = fmaf(sxm, issum, fxd * ifsum);
+    const float hsyn = fmaf(sym, issum, fyd * ifsum);
+    const float ihx = 1.0f / hsxn, ihy = 1.0f / hsyn;
+    const float sxn = sx * ihx, syn = sy * ihy;
+    const float q = fmaf(sxn, sxn, syn * syn);
+    float sc, calpha, salpha;
+    if (q > 0.f) {
+        const float isc = rsqrtf(q);
+        sc = q * isc;
+        calpha = sxn * isc;
+        salpha = syn * isc;
+    } else {
+        sc = 0.f;
+        calpha = 0.70710678f;
+        salpha = 0.70710678f;
+    }
+    auto hyp = [](float a, float b) { return sqrtf(fmaf(a, a, b * b)); };
+    const float df0 = hyp(dfx0 * calpha * hsxn, dfy0 * salpha * hsyn);
+    const float fm = hyp(fxm * calpha, fym * salpha);
+    const float cax = calpha * ihx, say = salpha * ihy;
+    const float sm = hyp(sxm * cax, sym * say);
+    const float fs = hyp(fxs * calpha, fys * salpha);
+    const float ss = hyp(sxs * cax, sys * say);
+    float f, fos;
+    tmxyf(f, fos, sc, df0, sm, fm, ss, fs);
+    ta.My = -K(K_RR) * min_nn(fz_d, K(K_PNMAX)) * ta.rStat * sgnd(omega);
+    const float vtxs = fmaf(rw, hsxn, 0.01f);
+    const float vtys = fmaf(rw, hsyn, 0.01f);
+    const float cx = K.f(K_CX), cy = K.f(K_CY), dx = K.f(K_DX), dy = K.f(K_DY);
+    const float xe = (float)ts.xe, ye = (float)ts.ye;
+    const float numx = fmaf(-vtxs * cx, xe, -fos * vsx);
+    const float numy = fmaf(-vtys * cy, ye, fos * (sy * vta));
+    const float xedot = numx / fmaf(vtxs, dx, fos);
+    const float yedot = numy / fmaf(vtys, dy, fos);
+    ts.xedot = xedot;
+    ts.yedot = yedot;
+    const float fxdyn = fmaf(dx, xedot, cx * xe);
+    const float fydyn = fmaf(dy, yedot, cy * ye);
+    const float fxstr = fminf(fmaxf(fmaf(xe, cx, xedot * dx), -K.f(K_FXMP2N)), K.f(K_FXMP2N));
+    const float fystr = fminf(fmaxf(fmaf(ye, cy, yedot * dy), -K.f(K_FYMP2N)), K.f(K_FYMP2N));
+    const float wx = sine_stepf(fabsf(vsx), 1.f, 1.f, 1.5f, 0.f);
+    const float wy = sine_stepf(fabsf(sy * vta), 1.f, 1.f, 1.5f, 0.f);
+    ta.fx = (wx == 0.f) ? fxdyn : fmaf(wx, fxstr, (1.f - wx) * fxdyn);
+    ta.fy = (wy == 0.f) ? fydyn : fmaf(wy, fystr, (1.f - wy) * fydyn);
+}
+
+// The TMeasy tire core in the arithmetic a kernel runs: FP64 (tire_core_tm) or FP32 (kF32).
+template <bool kSteered, bool kF32>
+__device__ __forceinline__ void tire_core_tm_p(TireC& ts, TireAux& ta, const KView& K, double c, double s, double fz,
+                                               double r_eff) {
+    if constexpr (kF32) tire_core_tm_f32<kSteered>(ts, ta, K, c, s, fz, r_eff);
+    else tire_core_tm<kSteered>(ts, ta, K, c, s, fz, r_eff);
+}
+
 // computeTireRHS, TMeasy (dof18_gpu.cu:379-530). (c, s) = (cos, sin) of this tire's wheel angle;
 // steered says whether the angle may be nonzero. Writes xedot/yedot (left stale when the wheel is
 // off the ground, as in the reference) and the aux values.
-template <bool kSteered>
+template <bool kSteered, bool kF32 = false>
 __device__ __forceinline__ void tire_rhs_tm(TireC& ts, TireAux& ta, const KView& K, double c, double s) {
     const double fz = ta.fz;
     if (!gt0(fz)) {
@@ -533,7 +683,7 @@ __device__ __forceinline__ void tire_rhs_tm(TireC& ts, TireAux& ta, const KView&
     } else {
         r_eff = fma(K(K_RDCRIT), ta.xt, ta.rStat);
     }
-    tire_core_tm<kSteered>(ts, ta, K, c, s, fz, r_eff);
+    tire_core_tm_p<kSteered, kF32>(ts, ta, K, c, s, fz, r_eff);
 }
 
 // computeCombinedCoulombForce (dof18_gpu.cu:287-303)
@@ -735,7 +885,7 @@ __device__ __forceinline__ void powertrain_rhs(VehC& v, VehAux& va, TireC* ts, T
 // One right-hand-side evaluation (rhsFun, dof18_halfImplicit_gpu.cu:685-729): tire loads, tire
 // forces and deflection rates, powertrain (wheel and crank accelerations, gear), chassis
 // accelerations. steering/throttle/braking are the driver inputs.
-template <bool kNr>
+template <bool kNr, bool kF32 = false>
 __device__ __forceinline__ void rhs18(VehC& v, VehAux& va, TireC* ts, TireAux* ta, const KView& K,
                                       const ClassDev18& C, double steering, double throttle, double braking) {
     // computeTireLoads (dof18_gpu.cu:305-340); udot/vdot are the previous step's accelerations.
@@ -779,10 +929,10 @@ __device__ __forceinline__ void rhs18(VehC& v, VehAux& va, TireC* ts, TireAux* t
         tire_rhs_nr<false>(ts[2], ta[2], K, 1.0, 0.0);
         tire_rhs_nr<false>(ts[3], ta[3], K, 1.0, 0.0);
     } else {
-        tire_rhs_tm<true>(ts[0], ta[0], K, cd, sd);
-        tire_rhs_tm<true>(ts[1], ta[1], K, cd, sd);
-        tire_rhs_tm<false>(ts[2], ta[2], K, 1.0, 0.0);
-        tire_rhs_tm<false>(ts[3], ta[3], K, 1.0, 0.0);
+        tire_rhs_tm<true, kF32>(ts[0], ta[0], K, cd, sd);
+        tire_rhs_tm<true, kF32>(ts[1], ta[1], K, cd, sd);
+        tire_rhs_tm<false, kF32>(ts[2], ta[2], K, 1.0, 0.0);
+        tire_rhs_tm<false, kF32>(ts[3], ta[3], K, 1.0, 0.0);
     }
     powertrain_rhs<kNr>(v, va, ts, ta, K, C, throttle, braking);
     // tireToVehTransform (dof18_gpu.cu:152-185): front forces into the vehicle frame
@@ -835,12 +985,12 @@ __device__ __forceinline__ void update18(VehC& v, const VehAux& va, TireC* ts, c
     v.phi = fma(v.wx, dt, v.phi);
 }
 
-// One step: rhs18 followed by update18.
-template <bool kNr>
+// One step: rhs18 followed by update18 (kF32: the FP32 tire core).
+template <bool kNr, bool kF32 = false>
 __device__ __forceinline__ void step18(VehC& v, VehAux& va, TireC* ts, TireAux* ta, const KView& K,
                                        const ClassDev18& C, double steering, double throttle, double braking,
                                        double dt) {
-    rhs18<kNr>(v, va, ts, ta, K, C, steering, throttle, braking);
+    rhs18<kNr, kF32>(v, va, ts, ta, K, C, steering, throttle, braking);
     update18<kNr>(v, va, ts, ta, C, dt);
 }
 

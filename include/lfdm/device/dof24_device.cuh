@@ -76,7 +76,7 @@ struct Rhs24 {
 // write the step's non-carried values to S. The flag is a run-time value on purpose: every step runs
 // the same compiled arithmetic (a separate instantiation for storing steps could fuse multiplies
 // and adds differently and round differently).
-template <bool kNr>
+template <bool kNr, bool kF32 = false>
 __device__ __forceinline__ void rhs24(VehC& v, Veh24X& vx, VehAux& va, TireC* ts, TireAux* ta, Sus24C* su,
                                       const Corner24K* ck, const KView& K, const ClassDev18& C, double steering,
                                       double throttle, double braking, Rhs24& R, double* S, size_t np, bool sink) {
@@ -160,8 +160,8 @@ __device__ __forceinline__ void rhs24(VehC& v, Veh24X& vx, VehAux& va, TireC* ts
                 if (c < 2) tire_core_nr<true>(ts[c], ta[c], K, cd, sd, fz, r_eff);
                 else tire_core_nr<false>(ts[c], ta[c], K, 1.0, 0.0, fz, r_eff);
             } else {
-                if (c < 2) tire_core_tm<true>(ts[c], ta[c], K, cd, sd, fz, r_eff);
-                else tire_core_tm<false>(ts[c], ta[c], K, 1.0, 0.0, fz, r_eff);
+                if (c < 2) tire_core_tm_p<true, kF32>(ts[c], ta[c], K, cd, sd, fz, r_eff);
+                else tire_core_tm_p<false, kF32>(ts[c], ta[c], K, 1.0, 0.0, fz, r_eff);
             }
         }
     }
@@ -309,13 +309,13 @@ __device__ __forceinline__ void update24(VehC& v, Veh24X& vx, const VehAux& va, 
 }
 #undef SINK
 
-// One step: rhs24 followed by update24.
-template <bool kNr>
+// One step: rhs24 followed by update24 (kF32: the FP32 tire core).
+template <bool kNr, bool kF32 = false>
 __device__ __forceinline__ void step24(VehC& v, Veh24X& vx, VehAux& va, TireC* ts, TireAux* ta, Sus24C* su,
                                        const Corner24K* ck, const KView& K, const ClassDev18& C, double steering,
                                        double throttle, double braking, double dt, double* S, size_t np, bool sink) {
     Rhs24 R;
-    rhs24<kNr>(v, vx, va, ts, ta, su, ck, K, C, steering, throttle, braking, R, S, np, sink);
+    rhs24<kNr, kF32>(v, vx, va, ts, ta, su, ck, K, C, steering, throttle, braking, R, S, np, sink);
     update24<kNr>(v, vx, va, ts, ta, su, C, R, dt, S, np, sink);
 }
 

@@ -91,6 +91,7 @@ def _sig(lib):
         "lfdm_measure_fp64_peak": ([i, _c_dp], i),
         "lfdm_set_split_warps": ([vp, i], i),
         "lfdm_measure_fp64_peak_clock": ([i, _c_dp, _c_dp], i),
+        "lfdm_measure_fp32_peak_clock": ([i, _c_dp, _c_dp], i),
         "lfdm_parse_vehicle18": ([cp, cp, i, vp, dp, ctypes.c_char_p, sz], i),
         "lfdm_parse_vehicle": ([i, cp, cp, cp, i, vp, dp, ctypes.c_char_p, sz], i),
         "lfdm_load_driver_file": ([cp, dp, u, ctypes.POINTER(u), ctypes.c_char_p, sz], i),
@@ -112,6 +113,8 @@ def _sig(lib):
         "lfdm_fleet_set_output": ([vp, d], i),
         "lfdm_fleet_set_launch": ([vp, u, u, u], i),
         "lfdm_fleet_get_launch": ([vp, ctypes.POINTER(u), ctypes.POINTER(u), ctypes.POINTER(u)], i),
+        "lfdm_fleet_set_affinity": ([vp, i], i),
+        "lfdm_fleet_get_affinity": ([vp, ctypes.POINTER(i), _c_dp], i),
         "lfdm_fleet_tune": ([vp, u, _c_dp], i),
         "lfdm_fleet_solve": ([vp], i),
         "lfdm_fleet_last_ms": ([vp, _c_dp, ctypes.POINTER(u)], i),
@@ -479,6 +482,15 @@ def measure_fp64_peak_clock(device: int = 0) -> tuple[float, float]:
     return v.value, g.value
 
 
+def measure_fp32_peak_clock(device: int = 0) -> tuple[float, float]:
+    """(measured lane FFMA/s, SM clock in GHz the probe ran at) of a device."""
+    v, g = ctypes.c_double(), ctypes.c_double()
+    rc = lib().lfdm_measure_fp32_peak_clock(int(device), ctypes.byref(v), ctypes.byref(g))
+    if rc:
+        raise LfdmError(rc, "FP32 peak probe failed")
+    return v.value, g.value
+
+
 class Fleet:
     """Mixed 18/24-DOF fleet with per-vehicle end times, stepped in one persistent launch captured in
     a CUDA graph (lfdm_fleet_* in include/lfdm.h). Vehicles are added per (model, class) group with
@@ -546,6 +558,16 @@ class Fleet:
         a, b, c = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint()
         self._ck(self._L.lfdm_fleet_get_launch(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
         return a.value, b.value, c.value
+
+    def set_affinity(self, on: bool = True):
+        """Split the SMs between the 18-DOF and 24-DOF tile lists (default on)."""
+        self._ck(self._L.lfdm_fleet_set_affinity(self._h, int(bool(on))))
+
+    def get_affinity(self) -> tuple[bool, float]:
+        """(affinity on, 18-DOF share of the prepared fleet's estimated work)."""
+        on, fr = ctypes.c_int(), ctypes.c_double()
+        self._ck(self._L.lfdm_fleet_get_affinity(self._h, ctypes.byref(on), ctypes.byref(fr)))
+        return bool(on.value), fr.value
 
     def tune(self, pilot_steps: int = 500) -> float:
         ms = ctypes.c_double()

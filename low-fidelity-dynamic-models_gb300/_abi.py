@@ -65,6 +65,7 @@ TIRE_TMEASY = C["LFDM_TIRE_TMEASY"]
 TIRE_TMEASY_NR = C["LFDM_TIRE_TMEASY_NR"]
 PREC_FP64 = C["LFDM_PREC_FP64"]
 PREC_MIXED = C["LFDM_PREC_MIXED"]
+PREC_MIXED_TIRE = C["LFDM_PREC_MIXED_TIRE"]
 
 STATUS = {v: k for k, v in C.items() if k.startswith("LFDM_OK") or k.startswith("LFDM_ERR_")}
 

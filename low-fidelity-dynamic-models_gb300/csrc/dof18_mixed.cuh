@@ -62,14 +62,6 @@ __device__ __forceinline__ float map_yf_scaled(const MapF& m, float x, float s) 
     return fmaf(mbar, m.y[l] * s - m.y[lf] * s, m.y[lf] * s);
 }
 
-__device__ __forceinline__ float sine_stepf(float x, float x1, float y1, float x2, float y2) {
-    if (x <= x1) return y1;
-    if (x >= x2) return y2;
-    const float dx = x2 - x1, dy = y2 - y1;
-    const float u = (x - x1) / dx;
-    return y1 + dy * u - (dy * (1.0f / 6.2831853071795865f)) * __sinf(6.2831853071795865f * u);
-}
-
 __device__ __forceinline__ float sgnf_(float v) { return (float)((0.f < v) - (v < 0.f)); }
 // Sign of a double as a float (-1, 0, +1) from its bit pattern: integer-pipe instructions in place of
 // two FP64 comparisons.
@@ -84,44 +76,6 @@ struct KViewF {
     int stride;
     __device__ __forceinline__ float operator()(int i) const { return base[i * stride]; }
 };
-
-__device__ __forceinline__ void tmxyf(float& f, float& fos, float s, float df0, float sm, float fm, float ss,
-                                      float fs) {
-    float df0loc = 0.0f;
-    if (sm > 0.0f) df0loc = fmaxf(2.0f * fm / sm, df0);
-    if (s > 0.0f && df0loc > 0.0f) {
-        if (s > ss) {
-            f = fs;
-            fos = fs / s;
-        } else if (s < sm) {
-            const float p = df0loc * sm / fm - 2.0f;
-            const float sn = s / sm;
-            const float dn = fmaf(sn + p, sn, 1.0f);
-            const float idn = 1.0f / dn;
-            f = df0loc * sm * sn * idn;
-            fos = df0loc * idn;
-        } else {
-            const float q = fm / sm;
-            const float a = q * q / (df0loc * sm);
-            const float sstar = sm + (fm - fs) / (a * (ss - sm));
-            if (sstar <= ss) {
-                if (s <= sstar) {
-                    f = fm - a * (s - sm) * (s - sm);
-                } else {
-                    const float b = a * (sstar - sm) / (ss - sstar);
-                    f = fs + b * (ss - s) * (ss - s);
-                }
-            } else {
-                const float sn = (s - sm) / (ss - sm);
-                f = fm - (fm - fs) * sn * sn * (3.0f - 2.0f * sn);
-            }
-            fos = f / s;
-        }
-    } else {
-        f = 0.0f;
-        fos = 0.0f;
-    }
-}
 
 // Mixed-precision carried state: FP64 for the accumulated kinematic states, FP32 for the tire
 // deflections (a contractive first-order relaxation: rounding errors decay instead of drifting).

@@ -4,11 +4,14 @@
 // The reference solves one model, one end time and (per Construct) one parameter set per solver
 // (d18SolverHalfImplicitGPU / d24SolverHalfImplicitGPU, m_tend global), so an uneven fleet needs one
 // solver run per model and horizon group. Here the vehicles of each model are sorted by their step
-// count (longest first) and cut into tiles of 32 (one warp). The tiles of both models form one work
-// list ordered by estimated cost (steps x per-step cost of the model), largest first. A persistent
-// grid (SMs x resident blocks) pulls tiles from that list with one atomic per tile and runs each
-// tile's vehicles over the steps of this launch, keeping their state in registers, so long-horizon
-// vehicles start first and short ones fill the tail (longest-processing-time-first scheduling).
+// count (longest first) and cut into tiles of 32 (one warp). Each model's tiles form a work list
+// ordered by estimated cost (steps x vehicles), largest first. A persistent grid (SMs x resident
+// blocks) pulls tiles with one atomic per tile and runs each tile's vehicles over the steps of this
+// launch, keeping their state in registers, so long-horizon vehicles start first and short ones
+// fill the tail (longest-processing-time-first scheduling). Model affinity: the SMs are split in
+// proportion to the two models' estimated work; a warp first drains its SM's home list and then
+// helps with the other one. An SM then runs one model's code for most of the launch instead of
+// interleaving the two step functions (together larger than the instruction cache).
 //
 // Each vehicle follows exactly the reference's per-vehicle schedule: the step start times are the
 // ones the reference's Solve loop produces (windows of kernel_sim_time from t = 0, t restarting at
@@ -138,17 +141,29 @@ __global__ void __launch_bounds__(128) fleet_kernel(const FleetLaunch L) {
     extern __shared__ __align__(16) double fleet_smem[];
     const int lane = threadIdx.x & 31;
     double* ks = fleet_smem + (size_t)(threadIdx.x >> 5) * kFleetKMax * 32;
-    for (;;) {
-        int tile = 0;
-        if (lane == 0) tile = atomicAdd(L.queue, 1);
-        tile = __shfl_sync(0xffffffffu, tile, 0);
-        if (tile >= L.ntiles) break;
-        const FleetTile T = L.tiles[tile];
-        if (T.nsteps_max > L.s_begin) {
-            if (T.model == LFDM_MODEL_24) run_tile24(L, T, ks, lane);
-            else run_tile18(L, T, ks, lane);
+    unsigned smid, nsmid;
+    asm("mov.u32 %0, %%smid;" : "=r"(smid));
+    asm("mov.u32 %0, %%nsmid;" : "=r"(nsmid));
+    const int home = (float)smid < L.home18 * (float)nsmid ? 0 : 1;  // 0: 18-DOF list, 1: 24-DOF list
+    const int base[2] = {0, L.ntiles18};
+    const int count[2] = {L.ntiles18, L.ntiles - L.ntiles18};
+    // each list is taken until its counter passes its length (a counter already past it is seen
+    // with a plain read, saving the atomic); then the other list; then the warp is done
+    for (int pass = 0; pass < 2; ++pass) {
+        const int q = pass == 0 ? home : 1 - home;
+        if (count[q] == 0) continue;
+        for (;;) {
+            int tile = count[q];
+            if (lane == 0 && *(volatile int*)(L.queue + q) < count[q]) tile = atomicAdd(L.queue + q, 1);
+            tile = __shfl_sync(0xffffffffu, tile, 0);
+            if (tile >= count[q]) break;
+            const FleetTile T = L.tiles[base[q] + tile];
+            if (T.nsteps_max > L.s_begin) {
+                if (T.model == LFDM_MODEL_24) run_tile24(L, T, ks, lane);
+                else run_tile18(L, T, ks, lane);
+            }
+            __syncwarp();
         }
-        __syncwarp();
     }
 }
 

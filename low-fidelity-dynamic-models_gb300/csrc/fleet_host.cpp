@@ -86,7 +86,10 @@ struct lfdm_fleet {
     std::vector<int32_t> step_sample;
     std::vector<int32_t> window_end;  // cumulative steps at the end of each window
     int spw = 0, nsamples = 0, total_steps = 0;
-    std::vector<FleetTile> tiles;
+    std::vector<FleetTile> tiles;  // the 18-DOF tiles [0, ntiles18), then the 24-DOF tiles
+    int ntiles18 = 0;
+    double frac18 = 1.0;           // 18-DOF share of the estimated work (steps x per-step cost)
+    bool affinity = true;          // split the SMs between the two models' tile lists
     DBuf<double> d_rows, d_step_t;
     DBuf<int32_t> d_step_sample;
     DBuf<FleetTile> d_tiles;
@@ -268,10 +271,14 @@ int prepare(lfdm_fleet* f) {
         int rc = prepare_group(f, *g);
         if (rc) return rc;
     }
-    // tiles of 32 vehicles in step-count order, both models, largest estimated cost first
+    // tiles of 32 vehicles in step-count order: the 18-DOF list, then the 24-DOF list, each largest
+    // estimated cost first; the share of the estimated work that is 18-DOF sets the SM split
     f->tiles.clear();
+    double work[2] = {0, 0};
     for (ModelGroup* g : {&f->g18, &f->g24}) {
+        const size_t start = f->tiles.size();
         const unsigned n = g->n();
+        const bool m24 = g->model == LFDM_MODEL_24;
         for (unsigned first = 0; first < n; first += 32) {
             FleetTile t;
             t.model = g->model;
@@ -280,12 +287,13 @@ int prepare(lfdm_fleet* f) {
             t.nsteps_max = g->nsteps[g->perm[first]];
             if (t.nsteps_max > 0) f->tiles.push_back(t);
         }
+        for (unsigned k = 0; k < n; ++k) work[m24] += (double)g->nsteps[k] * (m24 ? kCost24 : kCost18);
+        std::stable_sort(f->tiles.begin() + start, f->tiles.end(), [](const FleetTile& a, const FleetTile& b) {
+            return (double)a.nsteps_max * a.count > (double)b.nsteps_max * b.count;
+        });
+        if (!m24) f->ntiles18 = (int)f->tiles.size();
     }
-    std::stable_sort(f->tiles.begin(), f->tiles.end(), [](const FleetTile& a, const FleetTile& b) {
-        const double ca = a.nsteps_max * (a.model == LFDM_MODEL_24 ? kCost24 : kCost18) * a.count;
-        const double cb = b.nsteps_max * (b.model == LFDM_MODEL_24 ? kCost24 : kCost18) * b.count;
-        return ca > cb;
-    });
+    f->frac18 = work[0] + work[1] > 0 ? work[0] / (work[0] + work[1]) : 1.0;
     FCK(f->d_rows.ensure(std::max<size_t>(4, f->rows.size())));
     FCK(cudaMemcpyAsync(f->d_rows.p, f->rows.data(), f->rows.size() * sizeof(double), cudaMemcpyHostToDevice,
                         f->stream));
@@ -340,13 +348,13 @@ int plan(lfdm_fleet* f, int steps, unsigned threads, unsigned bps, unsigned spl,
     p->chunk = spl ? (int)std::min<unsigned>(spl, (unsigned)steps) : steps;
     p->nl = (steps + p->chunk - 1) / p->chunk;
     p->threads = threads;
-    FCK(f->d_queue.ensure(std::max(1, p->nl)));
+    FCK(f->d_queue.ensure(2 * std::max(1, p->nl)));
     return LFDM_OK;
 }
 
 // Enqueue (or record into a capture) the launches of a plan.
 int enqueue(lfdm_fleet* f, int steps, const Plan& p) {
-    FCK(cudaMemsetAsync(f->d_queue.p, 0, p.nl * sizeof(int), f->stream));
+    FCK(cudaMemsetAsync(f->d_queue.p, 0, 2 * p.nl * sizeof(int), f->stream));
     for (int c = 0; c < p.nl; ++c) {
         FleetLaunch L;
         L.m18 = model_dev(f, f->g18);
@@ -354,7 +362,10 @@ int enqueue(lfdm_fleet* f, int steps, const Plan& p) {
         L.rows = f->d_rows.p;
         L.tiles = f->d_tiles.p;
         L.ntiles = (int)f->tiles.size();
-        L.queue = f->d_queue.p + c;
+        L.ntiles18 = f->ntiles18;
+        L.queue = f->d_queue.p + 2 * c;
+        // without affinity every SM starts on the 18-DOF list, and the 24-DOF list follows
+        L.home18 = f->affinity ? (float)f->frac18 : 1.0f;
         L.step_t = f->d_step_t.p;
         L.step_sample = f->d_step_sample.p;
         L.s_begin = c * p.chunk;
@@ -530,6 +541,20 @@ int lfdm_fleet_set_launch(lfdm_fleet* f, unsigned threads, unsigned blocks_per_s
     f->blocks_per_sm = blocks_per_sm;
     f->steps_per_launch = steps_per_launch;
     f->drop_graph();
+    return LFDM_OK;
+}
+
+int lfdm_fleet_set_affinity(lfdm_fleet* f, int on) {
+    if (!f) return LFDM_ERR_ARG;
+    f->affinity = on != 0;
+    f->drop_graph();
+    return LFDM_OK;
+}
+
+int lfdm_fleet_get_affinity(lfdm_fleet* f, int* on, double* frac18) {
+    if (!f) return LFDM_ERR_ARG;
+    if (on) *on = f->affinity ? 1 : 0;
+    if (frac18) *frac18 = f->frac18;
     return LFDM_OK;
 }
 

@@ -48,7 +48,7 @@ struct Window18 {
 cudaError_t launch_window18(const Window18& w, cudaStream_t stream);
 
 // Dynamic shared memory one block of `threads` needs for `nclasses` classes; 0 if it cannot fit.
-size_t window18_smem(int threads, int nclasses);
+size_t window18_smem(int threads, int nclasses, bool f32 = false);
 
 // Derived per-vehicle constants: params AoS [n][LFDM_P_COUNT] (device) -> K SoA [K18_COUNT][npad].
 cudaError_t launch_prepare18(const double* params_dev, int n, int npad, double* K_dev, cudaStream_t stream);
@@ -74,6 +74,7 @@ cudaError_t launch_check_tables(const double* rows, long long ntables, int nrows
 // second (a kernel of independent chains timed with CUDA events), and the SM clock it ran at in GHz
 // (clock counter over the global timer; sm_ghz may be null).
 cudaError_t measure_dfma_rate(double* dfma_per_s, double* sm_ghz);
+cudaError_t measure_ffma_rate(double* ffma_per_s, double* sm_ghz);
 
 // Host-side conversion of a class record into the device table (computes segment reciprocals).
 void build_class_dev18(const lfdm_class18& c, ClassDev18* out);

@@ -8,13 +8,16 @@
 
 namespace lfdm {
 
-template <bool kNr, int kCtl, bool kOut>
+// kF32: the TMeasy tire core in FP32 (precision LFDM_PREC_MIXED_TIRE), on FP32 copies of the
+// derived constants staged beside the FP64 ones.
+template <bool kNr, int kCtl, bool kOut, bool kF32>
 __global__ void __launch_bounds__(128) window11_kernel(const Window18 w) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
     const bool cls_smem = w.nclasses <= kMaxSmemClasses;
     ClassDev18* cls = reinterpret_cast<ClassDev18*>(smem);
     double* ks = reinterpret_cast<double*>(smem + (cls_smem ? (size_t)w.nclasses * sizeof(ClassDev18) : 0));
+    float* fks = reinterpret_cast<float*>(ks + (size_t)K18_COUNT * blockDim.x);
     if (cls_smem) {
         const int4* src = reinterpret_cast<const int4*>(w.classes);
         int4* dst = reinterpret_cast<int4*>(smem);
@@ -25,11 +28,15 @@ __global__ void __launch_bounds__(128) window11_kernel(const Window18 w) {
     const bool active = vid < w.n;
     if (active) {
 #pragma unroll 4
-        for (int k = 0; k < K18_COUNT; ++k) ks[k * blockDim.x + tid] = __ldg(w.K + (size_t)k * w.npad + vid);
+        for (int k = 0; k < K18_COUNT; ++k) {
+            const double x = __ldg(w.K + (size_t)k * w.npad + vid);
+            ks[k * blockDim.x + tid] = x;
+            if (kF32) fks[k * blockDim.x + tid] = (float)x;
+        }
     }
     __syncthreads();
     if (!active) return;
-    const KView K{ks + tid, (int)blockDim.x};
+    const KView K{ks + tid, (int)blockDim.x, kF32 ? fks + tid : nullptr};
     const int ci = __ldg(w.class_of + vid);
     const ClassDev18& C = cls_smem ? cls[ci] : w.classes[ci];
     const size_t np = (size_t)w.npad;
@@ -61,7 +68,7 @@ __global__ void __launch_bounds__(128) window11_kernel(const Window18 w) {
             thr = __ldg(w.sched + 3 * s + 1);
             brk = __ldg(w.sched + 3 * s + 2);
         }
-        step11<kNr>(v, va, ts, ta, K, C, steer, thr, brk, dt);
+        step11<kNr, kF32>(v, va, ts, ta, K, C, steer, thr, brk, dt);
         t += dt;
         if (kOut && s + 1 == next_step) {
             double* r = w.resp + (size_t)next_k * LFDM11_RESP_CHANNELS * w.n + vid;
@@ -83,28 +90,29 @@ __global__ void __launch_bounds__(128) window11_kernel(const Window18 w) {
     if (w.status && !state11_finite(v, ts)) w.status[vid] |= 1u;
 }
 
-template <bool kNr, int kCtl, bool kOut>
+template <bool kNr, int kCtl, bool kOut, bool kF32>
 static cudaError_t launch11_t(const Window18& w, cudaStream_t stream) {
     const int threads = w.threads;
-    const size_t smem = window18_smem(threads, w.nclasses);
-    auto kern = window11_kernel<kNr, kCtl, kOut>;
+    const size_t smem = window18_smem(threads, w.nclasses, kF32);
+    auto kern = window11_kernel<kNr, kCtl, kOut, kF32>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<(w.n + threads - 1) / threads, threads, smem, stream>>>(w);
     return cudaGetLastError();
 }
 
-template <bool kNr, int kCtl>
+template <bool kNr, int kCtl, bool kF32>
 static cudaError_t launch11_o(const Window18& w, cudaStream_t s) {
-    return (w.resp && w.nsamples > 0) ? launch11_t<kNr, kCtl, true>(w, s) : launch11_t<kNr, kCtl, false>(w, s);
+    return (w.resp && w.nsamples > 0) ? launch11_t<kNr, kCtl, true, kF32>(w, s)
+                                      : launch11_t<kNr, kCtl, false, kF32>(w, s);
 }
-template <bool kNr>
+template <bool kNr, bool kF32 = false>
 static cudaError_t launch11_c(const Window18& w, cudaStream_t stream) {
     switch (w.ctl_mode) {
-        case CTL_TABLE: return launch11_o<kNr, CTL_TABLE>(w, stream);
-        case CTL_SCALAR: return launch11_o<kNr, CTL_SCALAR>(w, stream);
-        case CTL_SCHEDULE: return launch11_o<kNr, CTL_SCHEDULE>(w, stream);
-        default: return launch11_o<kNr, CTL_ARRAY>(w, stream);
+        case CTL_TABLE: return launch11_o<kNr, CTL_TABLE, kF32>(w, stream);
+        case CTL_SCALAR: return launch11_o<kNr, CTL_SCALAR, kF32>(w, stream);
+        case CTL_SCHEDULE: return launch11_o<kNr, CTL_SCHEDULE, kF32>(w, stream);
+        default: return launch11_o<kNr, CTL_ARRAY, kF32>(w, stream);
     }
 }
 
@@ -121,12 +129,13 @@ static cudaError_t launch11_c(const Window18& w, cudaStream_t stream) {
 // update11 are composed of, so every vehicle steps bit for bit as in window11_kernel.
 constexpr int kSplit11Fields = 33;  // exchanged doubles per vehicle and step: 16 from warp 0, 17 from warp 1
 
-size_t window11_split_smem(int nclasses) {
+size_t window11_split_smem(int nclasses, bool f32) {
     const size_t cls = nclasses <= kMaxSmemClasses ? (size_t)nclasses * sizeof(ClassDev18) : 0;
-    return cls + (size_t)K18_COUNT * 32 * sizeof(double) + 2 * (size_t)kSplit11Fields * 32 * sizeof(double);
+    return cls + (size_t)K18_COUNT * 32 * sizeof(double) + 2 * (size_t)kSplit11Fields * 32 * sizeof(double) +
+           (f32 ? (size_t)K18_COUNT * 32 * sizeof(float) : 0);
 }
 
-template <bool kNr, int kCtl, bool kOut>
+template <bool kNr, int kCtl, bool kOut, bool kF32>
 __global__ void __launch_bounds__(64) window11_split_kernel(const Window18 w) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x, lane = tid & 31, role = tid >> 5;
@@ -134,6 +143,7 @@ __global__ void __launch_bounds__(64) window11_split_kernel(const Window18 w) {
     ClassDev18* cls = reinterpret_cast<ClassDev18*>(smem);
     double* ks = reinterpret_cast<double*>(smem + (cls_smem ? (size_t)w.nclasses * sizeof(ClassDev18) : 0));
     double* xbuf = ks + (size_t)K18_COUNT * 32;
+    float* fks = reinterpret_cast<float*>(xbuf + 2 * (size_t)kSplit11Fields * 32);
     if (cls_smem) {
         const int4* src = reinterpret_cast<const int4*>(w.classes);
         int4* dst = reinterpret_cast<int4*>(smem);
@@ -145,9 +155,13 @@ __global__ void __launch_bounds__(64) window11_split_kernel(const Window18 w) {
     // lanes past the fleet run a copy of the last vehicle (so that both warps reach every barrier)
     // and store nothing
     const int vid = active ? vid_raw : w.n - 1;
-    for (int k = role; k < K18_COUNT; k += 2) ks[k * 32 + lane] = __ldg(w.K + (size_t)k * w.npad + vid);
+    for (int k = role; k < K18_COUNT; k += 2) {
+        const double x = __ldg(w.K + (size_t)k * w.npad + vid);
+        ks[k * 32 + lane] = x;
+        if (kF32) fks[k * 32 + lane] = (float)x;
+    }
     __syncthreads();
-    const KView K{ks + lane, 32};
+    const KView K{ks + lane, 32, kF32 ? fks + lane : nullptr};
     const int ci = __ldg(w.class_of + vid);
     const ClassDev18& C = cls_smem ? cls[ci] : w.classes[ci];
     const size_t np = (size_t)w.npad;
@@ -184,7 +198,7 @@ __global__ void __launch_bounds__(64) window11_split_kernel(const Window18 w) {
         double cd, sd, sp, cp;
         if (role == 0) {
             front_kinematics11(v, ta[0], K, C, steer, cd, sd);
-            tire11<kNr, true>(ts[0], ta[0], K, cd, sd);
+            tire11<kNr, true, kF32>(ts[0], ta[0], K, cd, sd);
             sincos(v.psi, &sp, &cp);
             const double out[16] = {ts[0].xe, ts[0].ye, ts[0].xedot, ts[0].yedot, ts[0].omega, ta[0].xt, ta[0].rStat,
                                     ta[0].fx, ta[0].fy, ta[0].My, ta[0].vsx, ta[0].vsy, cd, sd, sp, cp};
@@ -192,7 +206,7 @@ __global__ void __launch_bounds__(64) window11_split_kernel(const Window18 w) {
             for (int f = 0; f < 16; ++f) X[f * 32] = out[f];
         } else {
             rear_kinematics11(v, ta[1], K);
-            tire11<kNr, false>(ts[1], ta[1], K, 1.0, 0.0);
+            tire11<kNr, false, kF32>(ts[1], ta[1], K, 1.0, 0.0);
             const double w0 = gt0(ta[0].fz) ? ts[0].omega : 0.0;  // the front tire zeroes it off the ground
             powertrain11(v, va, w0, ts[1].omega, ta[0].engTor, ta[1].engTor, K, C, thr);
             const double out[17] = {ts[1].xe, ts[1].ye, ts[1].xedot, ts[1].yedot, ts[1].omega, ta[1].xt, ta[1].rStat,
@@ -265,27 +279,27 @@ __global__ void __launch_bounds__(64) window11_split_kernel(const Window18 w) {
     }
 }
 
-template <bool kNr, int kCtl, bool kOut>
+template <bool kNr, int kCtl, bool kOut, bool kF32>
 static cudaError_t launch11_split_t(const Window18& w, cudaStream_t stream) {
-    const size_t smem = window11_split_smem(w.nclasses);
-    auto kern = window11_split_kernel<kNr, kCtl, kOut>;
+    const size_t smem = window11_split_smem(w.nclasses, kF32);
+    auto kern = window11_split_kernel<kNr, kCtl, kOut, kF32>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<(w.n + 31) / 32, 64, smem, stream>>>(w);
     return cudaGetLastError();
 }
-template <bool kNr, int kCtl>
+template <bool kNr, int kCtl, bool kF32>
 static cudaError_t launch11_split_o(const Window18& w, cudaStream_t s) {
-    return (w.resp && w.nsamples > 0) ? launch11_split_t<kNr, kCtl, true>(w, s)
-                                      : launch11_split_t<kNr, kCtl, false>(w, s);
+    return (w.resp && w.nsamples > 0) ? launch11_split_t<kNr, kCtl, true, kF32>(w, s)
+                                      : launch11_split_t<kNr, kCtl, false, kF32>(w, s);
 }
-template <bool kNr>
+template <bool kNr, bool kF32 = false>
 static cudaError_t launch11_split_c(const Window18& w, cudaStream_t stream) {
     switch (w.ctl_mode) {
-        case CTL_TABLE: return launch11_split_o<kNr, CTL_TABLE>(w, stream);
-        case CTL_SCALAR: return launch11_split_o<kNr, CTL_SCALAR>(w, stream);
-        case CTL_SCHEDULE: return launch11_split_o<kNr, CTL_SCHEDULE>(w, stream);
-        default: return launch11_split_o<kNr, CTL_ARRAY>(w, stream);
+        case CTL_TABLE: return launch11_split_o<kNr, CTL_TABLE, kF32>(w, stream);
+        case CTL_SCALAR: return launch11_split_o<kNr, CTL_SCALAR, kF32>(w, stream);
+        case CTL_SCHEDULE: return launch11_split_o<kNr, CTL_SCHEDULE, kF32>(w, stream);
+        default: return launch11_split_o<kNr, CTL_ARRAY, kF32>(w, stream);
     }
 }
 
@@ -304,6 +318,10 @@ static bool use_split11(const Window18& w) {
 cudaError_t launch_window11(const Window18& w, cudaStream_t stream) {
     if (w.n <= 0 || w.nsteps <= 0) return cudaSuccess;
     if (w.threads <= 0 || w.threads > 128 || (w.threads & 31)) return cudaErrorInvalidValue;
+    if (w.precision == LFDM_PREC_MIXED_TIRE) {
+        if (w.tire_nr) return cudaErrorInvalidValue;
+        return use_split11(w) ? launch11_split_c<false, true>(w, stream) : launch11_c<false, true>(w, stream);
+    }
     if (w.precision != LFDM_PREC_FP64) return cudaErrorInvalidValue;
     if (use_split11(w)) return w.tire_nr ? launch11_split_c<true>(w, stream) : launch11_split_c<false>(w, stream);
     return w.tire_nr ? launch11_c<true>(w, stream) : launch11_c<false>(w, stream);

@@ -142,29 +142,32 @@ cudaError_t launch_check_tables(const double* rows, long long ntables, int nrows
     return cudaGetLastError();
 }
 
-// FP64 pipe probe: every thread runs 8 independent DFMA chains (enough to keep a sub-partition's
-// FP64 unit busy: on GB300 it accepts one warp-wide DFMA every 64 cycles whatever the number of
-// active lanes, so the rate is set by warp instructions, not by latency), 8 warps per sub-partition.
-// Thread 0 of every block reads the SM clock counter and the global nanosecond timer at its start
-// and end, which gives the SM clock the probe ran at.
+// FMA pipe probes. FP64: every thread runs 8 independent DFMA chains (enough to keep a
+// sub-partition's FP64 unit busy: on GB300 it accepts one warp-wide DFMA every 64 cycles whatever
+// the number of active lanes, so the rate is set by warp instructions, not by latency), 8 warps per
+// sub-partition. FP32: the same kernel on FFMA chains, 64 times as many iterations (the FP32 pipes
+// retire 64 times as many lane operations per clock). Thread 0 of every block reads the SM clock
+// counter and the global nanosecond timer at its start and end, which gives the SM clock the probe
+// ran at.
 constexpr int kProbeIter = 4096;
-__global__ void __launch_bounds__(1024) dfma_probe_kernel(double* out, long long* clk, double seed) {
+template <typename T>
+__global__ void __launch_bounds__(1024) fma_probe_kernel(T* out, long long* clk, T seed, int iters) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     long long c0 = 0, t0 = 0;
     if (threadIdx.x == 0) {
         c0 = clock64();
         asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
     }
-    double a[8];
+    T a[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) a[k] = seed + tid * 1e-9 + k * 0.1;
-    const double m = 0.999999, c = 1e-7;
+    for (int k = 0; k < 8; ++k) a[k] = seed + (T)(tid * 1e-9) + (T)(k * 0.1);
+    const T m = (T)0.999999, c = (T)1e-7;
 #pragma unroll 4
-    for (int i = 0; i < kProbeIter; ++i) {
+    for (int i = 0; i < iters; ++i) {
 #pragma unroll
         for (int k = 0; k < 8; ++k) a[k] = fma(a[k], m, c);
     }
-    double s = 0;
+    T s = 0;
 #pragma unroll
     for (int k = 0; k < 8; ++k) s += a[k];
     out[tid] = s;
@@ -177,15 +180,18 @@ __global__ void __launch_bounds__(1024) dfma_probe_kernel(double* out, long long
     }
 }
 
-cudaError_t measure_dfma_rate(double* rate, double* sm_ghz) {
+// Best of 5 timed launches (after one warm-up) of the probe on every SM: lane FMA per second and the
+// SM clock (GHz) of the fastest launch.
+template <typename T>
+static cudaError_t measure_fma_rate(double* rate, double* sm_ghz, int iters) {
     int dev = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
     const int threads = 1024, blocks = sms;  // 32 warps per SM, 8 per sub-partition
-    double* out = nullptr;
+    T* out = nullptr;
     long long* clk = nullptr;
-    if ((e = cudaMalloc(&out, sizeof(double) * threads * blocks)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&out, sizeof(T) * threads * blocks)) != cudaSuccess) return e;
     if ((e = cudaMalloc(&clk, sizeof(long long) * 2 * blocks)) != cudaSuccess) {
         cudaFree(out);
         return e;
@@ -193,13 +199,13 @@ cudaError_t measure_dfma_rate(double* rate, double* sm_ghz) {
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
-    dfma_probe_kernel<<<blocks, threads>>>(out, clk, 0.5);
+    fma_probe_kernel<T><<<blocks, threads>>>(out, clk, (T)0.5, iters);
     float best = 1e30f;
     double ghz = 0;
     std::vector<long long> h(2 * (size_t)blocks);
     for (int r = 0; r < 5; ++r) {
         cudaEventRecord(a);
-        dfma_probe_kernel<<<blocks, threads>>>(out, clk, 0.5);
+        fma_probe_kernel<T><<<blocks, threads>>>(out, clk, (T)0.5, iters);
         cudaEventRecord(b);
         cudaEventSynchronize(b);
         float ms = 0;
@@ -221,9 +227,14 @@ cudaError_t measure_dfma_rate(double* rate, double* sm_ghz) {
     cudaEventDestroy(b);
     cudaFree(out);
     cudaFree(clk);
-    *rate = (double)threads * blocks * kProbeIter * 8 / (best * 1e-3);
+    *rate = (double)threads * blocks * iters * 8 / (best * 1e-3);
     if (sm_ghz) *sm_ghz = ghz;
     return e;
+}
+
+cudaError_t measure_dfma_rate(double* rate, double* sm_ghz) { return measure_fma_rate<double>(rate, sm_ghz, kProbeIter); }
+cudaError_t measure_ffma_rate(double* rate, double* sm_ghz) {
+    return measure_fma_rate<float>(rate, sm_ghz, 64 * kProbeIter);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -276,18 +287,21 @@ void build_class_dev18(const lfdm_class18& c, ClassDev18* out) {
 // window kernel
 
 
-size_t window18_smem(int threads, int nclasses) {
+size_t window18_smem(int threads, int nclasses, bool f32) {
     const size_t cls = nclasses <= kMaxSmemClasses ? (size_t)nclasses * sizeof(ClassDev18) : 0;
-    return cls + (size_t)K18_COUNT * threads * sizeof(double);
+    return cls + (size_t)K18_COUNT * threads * (sizeof(double) + (f32 ? sizeof(float) : 0));
 }
 
-template <bool kNr, int kCtl, bool kOut>
+// kF32: the TMeasy tire core in FP32 (precision LFDM_PREC_MIXED_TIRE), on FP32 copies of the
+// derived constants staged beside the FP64 ones.
+template <bool kNr, int kCtl, bool kOut, bool kF32>
 __global__ void __launch_bounds__(128) window18_kernel(const Window18 w) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
     const bool cls_smem = w.nclasses <= kMaxSmemClasses;
     ClassDev18* cls = reinterpret_cast<ClassDev18*>(smem);
     double* ks = reinterpret_cast<double*>(smem + (cls_smem ? (size_t)w.nclasses * sizeof(ClassDev18) : 0));
+    float* fks = reinterpret_cast<float*>(ks + (size_t)K18_COUNT * blockDim.x);
     if (cls_smem) {
         const int4* src = reinterpret_cast<const int4*>(w.classes);
         int4* dst = reinterpret_cast<int4*>(smem);
@@ -298,12 +312,16 @@ __global__ void __launch_bounds__(128) window18_kernel(const Window18 w) {
     const bool active = vid < w.n;
     if (active) {
 #pragma unroll 4
-        for (int k = 0; k < K18_COUNT; ++k) ks[k * blockDim.x + tid] = __ldg(w.K + (size_t)k * w.npad + vid);
+        for (int k = 0; k < K18_COUNT; ++k) {
+            const double x = __ldg(w.K + (size_t)k * w.npad + vid);
+            ks[k * blockDim.x + tid] = x;
+            if (kF32) fks[k * blockDim.x + tid] = (float)x;
+        }
     }
     __syncthreads();
     if (!active) return;
 
-    const KView K{ks + tid, (int)blockDim.x};
+    const KView K{ks + tid, (int)blockDim.x, kF32 ? fks + tid : nullptr};
     const int ci = __ldg(w.class_of + vid);
     const ClassDev18& C = cls_smem ? cls[ci] : w.classes[ci];
     const size_t np = (size_t)w.npad;
@@ -337,7 +355,7 @@ __global__ void __launch_bounds__(128) window18_kernel(const Window18 w) {
             thr = __ldg(w.sched + 3 * s + 1);
             brk = __ldg(w.sched + 3 * s + 2);
         }
-        step18<kNr>(v, va, ts, ta, K, C, steer, thr, brk, dt);
+        step18<kNr, kF32>(v, va, ts, ta, K, C, steer, thr, brk, dt);
         t += dt;
         if (kOut && s + 1 == next_step) {
             double* r = w.resp + (size_t)next_k * LFDM18_RESP_CHANNELS * w.n + vid;
@@ -626,11 +644,11 @@ void build_class_dev18f(const lfdm_class18& c, ClassDev18F* out) {
 }
 size_t class_dev18f_size() { return sizeof(ClassDev18F); }
 
-template <bool kNr, int kCtl, bool kOut>
+template <bool kNr, int kCtl, bool kOut, bool kF32>
 static cudaError_t launch_t(const Window18& w, cudaStream_t stream) {
     const int threads = w.threads;
-    const size_t smem = window18_smem(threads, w.nclasses);
-    auto kern = window18_kernel<kNr, kCtl, kOut>;
+    const size_t smem = window18_smem(threads, w.nclasses, kF32);
+    auto kern = window18_kernel<kNr, kCtl, kOut, kF32>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int blocks = (w.n + threads - 1) / threads;
@@ -638,17 +656,17 @@ static cudaError_t launch_t(const Window18& w, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
-template <bool kNr, int kCtl>
+template <bool kNr, int kCtl, bool kF32>
 static cudaError_t launch_o(const Window18& w, cudaStream_t s) {
-    return (w.resp && w.nsamples > 0) ? launch_t<kNr, kCtl, true>(w, s) : launch_t<kNr, kCtl, false>(w, s);
+    return (w.resp && w.nsamples > 0) ? launch_t<kNr, kCtl, true, kF32>(w, s) : launch_t<kNr, kCtl, false, kF32>(w, s);
 }
-template <bool kNr>
+template <bool kNr, bool kF32 = false>
 static cudaError_t launch_c(const Window18& w, cudaStream_t s) {
     switch (w.ctl_mode) {
-        case CTL_TABLE: return launch_o<kNr, CTL_TABLE>(w, s);
-        case CTL_SCALAR: return launch_o<kNr, CTL_SCALAR>(w, s);
-        case CTL_SCHEDULE: return launch_o<kNr, CTL_SCHEDULE>(w, s);
-        default: return launch_o<kNr, CTL_ARRAY>(w, s);
+        case CTL_TABLE: return launch_o<kNr, CTL_TABLE, kF32>(w, s);
+        case CTL_SCALAR: return launch_o<kNr, CTL_SCALAR, kF32>(w, s);
+        case CTL_SCHEDULE: return launch_o<kNr, CTL_SCHEDULE, kF32>(w, s);
+        default: return launch_o<kNr, CTL_ARRAY, kF32>(w, s);
     }
 }
 
@@ -659,6 +677,11 @@ cudaError_t launch_window18(const Window18& w, cudaStream_t stream) {
         if (w.tire_nr || !w.classes_f) return cudaErrorInvalidValue;
         return launch_mixed(w, stream);
     }
+    if (w.precision == LFDM_PREC_MIXED_TIRE) {
+        if (w.tire_nr) return cudaErrorInvalidValue;
+        return launch_c<false, true>(w, stream);
+    }
+    if (w.precision != LFDM_PREC_FP64) return cudaErrorInvalidValue;
     return w.tire_nr ? launch_c<true>(w, stream) : launch_c<false>(w, stream);
 }
 

@@ -43,14 +43,15 @@ cudaError_t launch_prepare24(const double* params_dev, int n, int npad, double* 
 }
 
 
-size_t window24_smem(int threads, int nclasses) {
+size_t window24_smem(int threads, int nclasses, bool f32) {
     const size_t cls = nclasses <= kMaxSmemClasses ? (size_t)nclasses * sizeof(ClassDev18) : 0;
-    return cls + (size_t)K24_COUNT * threads * sizeof(double);
+    return cls + (size_t)K24_COUNT * threads * (sizeof(double) + (f32 ? sizeof(float) : 0));
 }
 
 cudaError_t launch_window24(const Window18& w, cudaStream_t stream) {
     if (w.n <= 0 || w.nsteps <= 0) return cudaSuccess;
     if (w.threads <= 0 || w.threads > 128 || (w.threads & 31)) return cudaErrorInvalidValue;
+    if (w.precision == LFDM_PREC_MIXED_TIRE) return w.tire_nr ? cudaErrorInvalidValue : launch_window24_f32(w, stream);
     if (w.precision != LFDM_PREC_FP64) return cudaErrorInvalidValue;
     return w.tire_nr ? launch_window24_nr(w, stream) : launch24_tire<false>(w, stream);
 }

@@ -384,8 +384,8 @@ int run_windows(lfdm_solver* h, double t0, double t_end, bool solve_all, int ctl
     w.K = h->d_K.p;
     w.classes = reinterpret_cast<const ClassDev18*>(h->d_classes.p);
     w.classes_f = reinterpret_cast<const ClassDev18F*>(h->d_classes_f.p);
-    if (h->precision == LFDM_PREC_MIXED && w.tire_nr)
-        return h->fail(LFDM_ERR_ARG, "the mixed-precision stepper supports TMeasy tires only");
+    if (h->precision != LFDM_PREC_FP64 && w.tire_nr)
+        return h->fail(LFDM_ERR_ARG, "the mixed-precision steppers support TMeasy tires only");
     w.nclasses = (int)h->classes.size();
     w.class_of = h->d_class_of.p;
     w.S = h->d_S.p;
@@ -558,6 +558,12 @@ int lfdm_measure_fp64_peak_clock(int device, double* dfma_per_s, double* sm_ghz)
     if (!dfma_per_s) return LFDM_ERR_ARG;
     if (cudaSetDevice(device) != cudaSuccess) return LFDM_ERR_NODEVICE;
     return measure_dfma_rate(dfma_per_s, sm_ghz) == cudaSuccess ? LFDM_OK : LFDM_ERR_CUDA;
+}
+
+int lfdm_measure_fp32_peak_clock(int device, double* ffma_per_s, double* sm_ghz) {
+    if (!ffma_per_s) return LFDM_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return LFDM_ERR_NODEVICE;
+    return measure_ffma_rate(ffma_per_s, sm_ghz) == cudaSuccess ? LFDM_OK : LFDM_ERR_CUDA;
 }
 
 int lfdm_create_on_device(int model, unsigned total_num_vehicles, int device, lfdm_solver** out) {
@@ -850,7 +856,7 @@ int lfdm_get_num_vehicles(lfdm_solver* h, unsigned* total, unsigned* constructed
 }
 int lfdm_set_precision(lfdm_solver* h, int precision) {
     if (!h) return LFDM_ERR_ARG;
-    if (precision != LFDM_PREC_FP64 && precision != LFDM_PREC_MIXED)
+    if (precision != LFDM_PREC_FP64 && precision != LFDM_PREC_MIXED && precision != LFDM_PREC_MIXED_TIRE)
         return h->fail(LFDM_ERR_ARG, "unknown precision %d", precision);
     if (precision == LFDM_PREC_MIXED && h->model != LFDM_MODEL_18)
         return h->fail(LFDM_ERR_ARG, "mixed precision is built for the 18-DOF model only");

@@ -1,5 +1,6 @@
-// The 24-DOF window kernel and its launch templates, instantiated for TMeasy tires in kernels24.cu
-// and for TMeasyNr tires in kernels24nr.cu (two translation units that compile in parallel).
+// The 24-DOF window kernel and its launch templates, instantiated for TMeasy tires in kernels24.cu,
+// for TMeasyNr tires in kernels24nr.cu and for TMeasy tires with the FP32 tire core in
+// kernels24tf.cu (three translation units that compile in parallel).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -10,16 +11,20 @@
 
 namespace lfdm {
 
-size_t window24_smem(int threads, int nclasses);
+size_t window24_smem(int threads, int nclasses, bool f32);
 cudaError_t launch_window24_nr(const Window18& w, cudaStream_t stream);
+cudaError_t launch_window24_f32(const Window18& w, cudaStream_t stream);
 
-template <bool kNr, int kCtl, bool kOut>
+// kF32: the TMeasy tire core in FP32 (precision LFDM_PREC_MIXED_TIRE), on FP32 copies of the
+// derived constants staged beside the FP64 ones.
+template <bool kNr, int kCtl, bool kOut, bool kF32>
 __global__ void __launch_bounds__(128) window24_kernel(const Window18 w) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
     const bool cls_smem = w.nclasses <= kMaxSmemClasses;
     ClassDev18* cls = reinterpret_cast<ClassDev18*>(smem);
     double* ks = reinterpret_cast<double*>(smem + (cls_smem ? (size_t)w.nclasses * sizeof(ClassDev18) : 0));
+    float* fks = reinterpret_cast<float*>(ks + (size_t)K24_COUNT * blockDim.x);
     if (cls_smem) {
         const int4* src = reinterpret_cast<const int4*>(w.classes);
         int4* dst = reinterpret_cast<int4*>(smem);
@@ -30,11 +35,15 @@ __global__ void __launch_bounds__(128) window24_kernel(const Window18 w) {
     const bool active = vid < w.n;
     if (active) {
 #pragma unroll 4
-        for (int k = 0; k < K24_COUNT; ++k) ks[k * blockDim.x + tid] = __ldg(w.K + (size_t)k * w.npad + vid);
+        for (int k = 0; k < K24_COUNT; ++k) {
+            const double x = __ldg(w.K + (size_t)k * w.npad + vid);
+            ks[k * blockDim.x + tid] = x;
+            if (kF32) fks[k * blockDim.x + tid] = (float)x;
+        }
     }
     __syncthreads();
     if (!active) return;
-    const KView K{ks + tid, (int)blockDim.x};
+    const KView K{ks + tid, (int)blockDim.x, kF32 ? fks + tid : nullptr};
     const int ci = __ldg(w.class_of + vid);
     const ClassDev18& C = cls_smem ? cls[ci] : w.classes[ci];
     const size_t np = (size_t)w.npad;
@@ -97,7 +106,7 @@ __global__ void __launch_bounds__(128) window24_kernel(const Window18 w) {
     for (int s = 0; s <= last; ++s) {
         controls(s);
         // the last step also writes the values the reference leaves in its state structs
-        step24<kNr>(v, vx, va, ts, ta, su, ck, K, C, steer, thr, brk, dt, S, np, s == last);
+        step24<kNr, kF32>(v, vx, va, ts, ta, su, ck, K, C, steer, thr, brk, dt, S, np, s == last);
         t += dt;
         sample(s);
     }
@@ -106,30 +115,31 @@ __global__ void __launch_bounds__(128) window24_kernel(const Window18 w) {
     if (w.status && !state24_finite(v, vx, ts)) w.status[vid] |= 1u;
 }
 
-template <bool kNr, int kCtl, bool kOut>
+template <bool kNr, int kCtl, bool kOut, bool kF32>
 static cudaError_t launch24_t(const Window18& w, cudaStream_t stream) {
     const int threads = w.threads;
-    const size_t smem = window24_smem(threads, w.nclasses);
-    auto kern = window24_kernel<kNr, kCtl, kOut>;
+    const size_t smem = window24_smem(threads, w.nclasses, kF32);
+    auto kern = window24_kernel<kNr, kCtl, kOut, kF32>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<(w.n + threads - 1) / threads, threads, smem, stream>>>(w);
     return cudaGetLastError();
 }
 
-template <bool kNr, int kCtl>
+template <bool kNr, int kCtl, bool kF32>
 static cudaError_t launch24_o(const Window18& w, cudaStream_t s) {
-    return (w.resp && w.nsamples > 0) ? launch24_t<kNr, kCtl, true>(w, s) : launch24_t<kNr, kCtl, false>(w, s);
+    return (w.resp && w.nsamples > 0) ? launch24_t<kNr, kCtl, true, kF32>(w, s)
+                                      : launch24_t<kNr, kCtl, false, kF32>(w, s);
 }
 
-// All control modes and output settings of one tire model.
-template <bool kNr>
+// All control modes and output settings of one tire model and tire-core arithmetic.
+template <bool kNr, bool kF32 = false>
 static cudaError_t launch24_tire(const Window18& w, cudaStream_t stream) {
     switch (w.ctl_mode) {
-        case CTL_TABLE: return launch24_o<kNr, CTL_TABLE>(w, stream);
-        case CTL_SCALAR: return launch24_o<kNr, CTL_SCALAR>(w, stream);
-        case CTL_SCHEDULE: return launch24_o<kNr, CTL_SCHEDULE>(w, stream);
-        default: return launch24_o<kNr, CTL_ARRAY>(w, stream);
+        case CTL_TABLE: return launch24_o<kNr, CTL_TABLE, kF32>(w, stream);
+        case CTL_SCALAR: return launch24_o<kNr, CTL_SCALAR, kF32>(w, stream);
+        case CTL_SCHEDULE: return launch24_o<kNr, CTL_SCHEDULE, kF32>(w, stream);
+        default: return launch24_o<kNr, CTL_ARRAY, kF32>(w, stream);
     }
 }
 

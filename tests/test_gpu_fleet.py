@@ -114,6 +114,39 @@ def test_fleet_launch_configurations_agree(built_lib, reference_runs, launch):
     f.close()
 
 
+@pytest.mark.parametrize("on", [False, True])
+def test_fleet_model_affinity_changes_nothing(built_lib, reference_runs, on):
+    """Splitting the SMs between the 18-DOF and 24-DOF tile lists (or not) changes no result; the
+    18-DOF share of the estimated work is reported after the solve."""
+    mf, ref = reference_runs
+    f = _make(built_lib, mf, (64, 0, 0))
+    f.set_affinity(on)
+    f.solve()
+    got_on, frac18 = f.get_affinity()
+    assert got_on == on and 0.0 < frac18 < 1.0
+    _check(built_lib, f, mf, ref)
+    f.close()
+
+
+@pytest.mark.parametrize("model", [18, 24])
+def test_fleet_of_one_model(built_lib, reference_runs, model):
+    """A fleet of one model only (the other tile list empty, the SMs all on one list)."""
+    mf, (states, resp) = reference_runs
+    f = built_lib.Fleet(dt=1e-3, kernel_sim_time=KSIM, output_dt=DTOUT)
+    base = f.add_rows(mf["rows"])
+    for g in mf["groups"]:
+        if g["model"] == model:
+            f.add(g["model"], g["cls"], g["params"], g["states"], g["horizons"], None, base + g["row_off"],
+                  g["row_len"])
+    f.solve()
+    assert f.get_affinity()[1] == (1.0 if model == 18 else 0.0)
+    assert np.array_equal(f.get_states(model), states[model])
+    fr = f.get_response(model)
+    for i, r in enumerate(resp[model]):
+        assert np.array_equal(fr[: r.shape[0], :, i], r), i
+    f.close()
+
+
 def test_fleet_autotune_then_solve(built_lib, reference_runs):
     mf, ref = reference_runs
     f = _make(built_lib, mf)
