@@ -34,16 +34,21 @@ PKG = "low-fidelity-dynamic-models_gb300"
 SEED = 20261203
 W_ALG_18 = 1391  # FP64 source-level operations per 18-DOF vehicle-step of the reference algorithm
 W_ALG = {11: 675, 18: 1391, 24: 1941}  # the same count for the three models
-# FP64 thread-instructions the 18-DOF window kernel executes per vehicle-step (ncu instruction
-# counters of one capture, DFMA + DMUL + DADD + the divide and square-root sequences)
-FP64_INST_PER_VSTEP_18 = 1029
+# FP64 instructions the 18-DOF window kernel executes per vehicle-step (ncu, one window launch on
+# 32,768 vehicles of the seeded fleet, the fourth 1 s window): DFMA + DMUL + DADD of active lanes
+# (sm__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on.sum), and everything the FP64 pipe
+# issued in lanes (sm__inst_executed_pipe_fp64.sum x 32: also compares, min/max and conversions, and
+# the inactive lanes of divergent warps, which occupy the pipe alike)
+FP64_INST_PER_VSTEP_18 = 1046
+FP64_PIPE_PER_VSTEP_18 = 1402
 # The mixed-precision forms of the 18-DOF stepper: (precision enum, key, arithmetic)
 MIXED_FORMS = ((1, "mixed", "f32 RHS and tire math; f64 states, X/Y/yaw accumulation, slip and transport velocities"),
                (2, "mixed_tire", "f32 TMeasy tire core; f64 everything else"))
-# Thread-level instructions per vehicle-step of the mixed window kernels, (FP32, FP64): ncu
-# sm__sass_thread_inst_executed_op_{ffma,fmul,fadd}_pred_on.sum and _{dfma,dmul,dadd}_pred_on.sum
-# of one window launch on 32,768 vehicles of the seeded fleet, divided by its vehicle-steps
-MIXED_INST_PER_VSTEP = {1: None, 2: None}
+# Lane instructions per vehicle-step the two pipes of the mixed window kernels issue, (FMA pipe,
+# FP64 pipe): ncu sm__inst_executed_pipe_fma.sum and sm__inst_executed_pipe_fp64.sum x 32 of one
+# window launch on 32,768 vehicles of the seeded fleet (the fourth 1 s window), per vehicle-step.
+# Of the FP64 pipe's 83 (MIXED) and 384 (MIXED_TIRE), 52 are float/double conversions.
+MIXED_INST_PER_VSTEP = {1: (1187, 83), 2: (1002, 384)}
 METRIC = "18-DOF vehicle-steps/s on 1 GB300: FP64 plain vs mixed at stated error; adjoint/fwd"
 
 
@@ -301,30 +306,43 @@ def _mixed_retention(lfdm, fleet, dev, n, horizon):
 
 def _model_rate(lfdm, fleet, dev, model: int, n: int, windows: int, ksim: float, peak_tflops: float) -> dict:
     """FP64 vehicle-steps/s of one model's window kernel on its seeded SUV fleet: `windows` timed
-    windows of ksim seconds after one warm-up window (device time, CUDA events)."""
+    windows of ksim seconds after one warm-up window (device time, CUDA events); then the same with
+    the FP32 tire core (LFDM_PREC_MIXED_TIRE) and its end-of-horizon error against FP64."""
     gen = {11: fleet.fleet11, 18: fleet.fleet18, 24: fleet.fleet24}[model]
     cls_ = {11: lfdm.d11SolverHalfImplicitGPU, 18: lfdm.d18SolverHalfImplicitGPU, 24: lfdm.d24SolverHalfImplicitGPU}
+    lay = {11: lfdm.S11, 18: lfdm.S, 24: lfdm.S24}[model]
     horizon = (windows + 1) * ksim
     f = gen(n, seed=SEED + model, horizon=horizon)
-    sol = cls_[model](n, device=dev)
-    sol.construct_class(f["cls"][0], f["params"])
-    sol.set_driver_tables(f["tables"])
-    sol.set_states(f["states"])
-    sol.SetKernelSimTime(ksim)
-    sol.SetEndTime(horizon)
-    sol.solve_range(-0.5 * ksim, 0.5 * ksim)
-    sol.solve_range(0.5 * ksim, (windows + 0.5) * ksim)
-    ms, launches = sol.last_kernel_ms()
-    finite = bool(np.isfinite(sol.get_states()[:, :8]).all())
-    sol.close()
+    out = {}
+    for prec in (0, 2):
+        sol = cls_[model](n, device=dev)
+        sol.construct_class(f["cls"][0], f["params"])
+        sol.set_driver_tables(f["tables"])
+        sol.set_states(f["states"])
+        sol.SetKernelSimTime(ksim)
+        sol.SetEndTime(horizon)
+        sol.set_precision(prec)
+        sol.solve_range(-0.5 * ksim, 0.5 * ksim)
+        sol.solve_range(0.5 * ksim, (windows + 0.5) * ksim)
+        ms, launches = sol.last_kernel_ms()
+        out[prec] = (ms, launches, sol.get_states())
+        sol.close()
+    ms, launches, st = out[0]
+    finite = bool(np.isfinite(st[:, :8]).all())
     vsteps = n * int(round(ksim / 1e-3)) * windows
     rate = vsteps / (ms * 1e-3)
     achieved = W_ALG[model] * rate / 1e12
+    tf_ms, _, tf_st = out[2]
+    d = _dpos(lay, st, tf_st)
     return {"model": f"{model}dof-tmeasy", "vehicles": n, "value": rate, "unit": "vehicle-steps/s",
             "ms_per_window": ms / windows, "gpu_launches": launches, "finite_states": finite,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",
                          "frac": achieved / peak_tflops,
-                         "algorithmic": f"{W_ALG[model]} FP64 ops per vehicle-step (reference op count)"}}
+                         "algorithmic": f"{W_ALG[model]} FP64 ops per vehicle-step (reference op count)"},
+            "mixed_tire": {"value": vsteps / (tf_ms * 1e-3), "speedup_vs_fp64": ms / tf_ms,
+                           "dtype": "f32 TMeasy tire core; f64 everything else",
+                           "error_vs_fp64": {"horizon_s": horizon, "position_m": _stats(d),
+                                             "frac_position_within_1cm": float((d <= 0.01).mean())}}}
 
 
 def _fleet_bench(lfdm, fleet, dev, n: int, torch) -> dict:
@@ -346,7 +364,8 @@ def _fleet_bench(lfdm, fleet, dev, n: int, torch) -> dict:
     threads, bps, spl = f.get_launch()
     f.solve()
     ms, launches = f.last_ms()
-    finite = {m: bool(np.isfinite(f.get_states(m)[:, :8]).all()) for m in (18, 24)}
+    fp64_states = {m: f.get_states(m) for m in (18, 24)}
+    finite = {m: bool(np.isfinite(fp64_states[m][:, :8]).all()) for m in (18, 24)}
     # the same solve from the same states without model affinity (every SM starts on the 18-DOF tiles)
     for m in (18, 24):
         f.set_states(m, np.concatenate([g["states"] for g in mf["groups"] if g["model"] == m]))
@@ -354,6 +373,31 @@ def _fleet_bench(lfdm, fleet, dev, n: int, torch) -> dict:
     f.set_affinity(False)
     f.solve()
     ms_noaff, _ = f.last_ms()
+    f.close()
+    # the same fleet without response outputs: what the 0.1 s output schedule costs the launch
+    f = lfdm.Fleet(device=dev, dt=1e-3, kernel_sim_time=ksim, output_dt=0.0)
+    base = f.add_rows(mf["rows"])
+    for g in mf["groups"]:
+        f.add(g["model"], g["cls"], g["params"], g["states"], g["horizons"], None, base + g["row_off"], g["row_len"])
+    f.set_launch(threads, bps, spl)
+    f.solve()
+    ms_noout, _ = f.last_ms()
+    f.close()
+    # the same fleet and launch configuration with the FP32 tire core, against the FP64 solve
+    f = lfdm.Fleet(device=dev, dt=1e-3, kernel_sim_time=ksim, output_dt=dtout)
+    base = f.add_rows(mf["rows"])
+    for g in mf["groups"]:
+        f.add(g["model"], g["cls"], g["params"], g["states"], g["horizons"], None, base + g["row_off"], g["row_len"])
+    f.set_launch(threads, bps, spl)
+    f.set_precision(2)
+    f.solve()
+    ms_tf, _ = f.last_ms()
+    tf_err = {}
+    for m in (18, 24):
+        lay = lfdm.S if m == 18 else lfdm.S24
+        d = _dpos(lay, fp64_states[m], f.get_states(m))
+        tf_err[f"{m}dof_position_m"] = _stats(d)
+        tf_err[f"{m}dof_frac_within_1cm"] = float((d <= 0.01).mean())
     f.close()
     vs = info["vehicle_steps"]
     # baseline: per-group solvers, kernel time summed over the groups
@@ -400,7 +444,12 @@ def _fleet_bench(lfdm, fleet, dev, n: int, torch) -> dict:
             "model_affinity": {"frac18_of_work": frac18, "ms_with": ms, "ms_without": ms_noaff,
                                "speedup": ms_noaff / ms,
                                "what": "SMs split between the 18-DOF and 24-DOF tile lists in proportion to their "
-                                       "estimated work, against all SMs taking the 18-DOF tiles first"}}
+                                       "estimated work, against all SMs taking the 18-DOF tiles first"},
+            "mixed_tire": {"value": vs / (ms_tf * 1e-3), "unit": "vehicle-steps/s", "ms": ms_tf,
+                           "speedup_vs_fp64": ms / ms_tf, "error_vs_fp64_end_of_horizon": tf_err,
+                           "dtype": "f32 TMeasy tire core; f64 everything else"},
+            "outputs": {"ms_with_0.1s_outputs": ms, "ms_without_outputs": ms_noout, "cost_frac": ms / ms_noout - 1.0,
+                        "what": "the same fleet and launch configuration with no response buffer"}}
 
 
 def _adjoint_bench(lfdm, fleet, dev, n: int, nsteps: int, torch) -> dict:
@@ -633,9 +682,13 @@ def run_ours(a, dist: Dist):
             mixed[key] = {"precision": prec, "value": mvalue, "unit": "vehicle-steps/s",
                           "speedup_vs_fp64": mvalue / value, "ms_per_step": mms / K, "gpu_launches": mlaunch,
                           "dtype": arith}
-        mixed["error_vs_fp64"] = _mixed_error(lfdm, fleet, dev, a.error_vehicles, a.error_horizon)
-        mixed["retention"] = _mixed_retention(lfdm, fleet, dev, a.ceiling_vehicles, a.error_horizon)
+        if a.error_vehicles > 0:
+            mixed["error_vs_fp64"] = _mixed_error(lfdm, fleet, dev, a.error_vehicles, a.error_horizon)
+        if a.ceiling_vehicles > 0:
+            mixed["retention"] = _mixed_retention(lfdm, fleet, dev, a.ceiling_vehicles, a.error_horizon)
     peak_dfma, probe_ghz = lfdm.measure_fp64_peak_clock(dev)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    max_ghz = (clocks.get("sm_max_mhz") or 2070.0) / 1e3
     if mixed:
         # issue roofline of each mixed form: its FP32 and FP64 thread-instructions per second against
         # the FFMA and DFMA probes (separate pipes, so the larger fraction is the bound)
@@ -655,10 +708,10 @@ def run_ours(a, dist: Dist):
                 "peak_source": "measured live: FFMA and DFMA throughput kernels (lfdm_measure_fp32_peak_clock, "
                                "lfdm_measure_fp64_peak_clock)",
                 "probe_fp32_sm_ghz": probe32_ghz, "probe_fp64_sm_ghz": probe_ghz,
-                "inst_source": "ncu sm__sass_thread_inst_executed_op_{ffma,fmul,fadd,dfma,dmul,dadd}_pred_on.sum of "
-                               "one window launch on 32,768 vehicles, per vehicle-step"}
-    sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    max_ghz = (clocks.get("sm_max_mhz") or 2070.0) / 1e3
+                "inst_source": "ncu sm__inst_executed_pipe_fma.sum and sm__inst_executed_pipe_fp64.sum x 32 of "
+                               "one window launch on 32,768 vehicles, per vehicle-step",
+                "peak_nominal_fp64_per_s": 2 * sms * max_ghz * 1e9,
+                "fp64_frac_nominal": inst[1] * m["value"] / (2 * sms * max_ghz * 1e9)}
     # nominal FP64 rate: one warp-wide DFMA per 64 cycles per SM sub-partition = 2 DFMA/clock/SM
     peak_nominal = 2 * 2.0 * sms * max_ghz * 1e9 / 1e12
     launch_ms = kms / launches
@@ -708,7 +761,7 @@ def run_ours(a, dist: Dist):
         jacobian_line = _jacobian_bench(lfdm, fleet, dev, a.jacobian_vehicles, a.jacobian_vehicles, torch)
 
     cpu = None
-    if dist.rank == 0:
+    if dist.rank == 0 and a.cpu_sample > 0:
         cores = os.cpu_count() or 1
         m = min(a.cpu_sample, n)
         traj = CpuTrajectory(f, m, ksim, cores)
@@ -746,11 +799,14 @@ def run_ours(a, dist: Dist):
                          "peak_nominal": peak_nominal, "frac_nominal": achieved / peak_nominal,
                          "peak_nominal_source": f"2 DFMA/clock/SM x {sms} SMs x {max_ghz:.3f} GHz (max SM clock) x 2",
                          "issue_view": {
-                             "fp64_inst_per_vehicle_step": FP64_INST_PER_VSTEP_18,
-                             "source": "ncu sm__sass_thread_inst_executed_op_dfma/dmul/dadd_pred_on (+ divide and "
-                                       "square-root sequences) per vehicle-step of the window kernel, one capture",
-                             "frac": FP64_INST_PER_VSTEP_18 * value / peak_dfma,
-                             "frac_nominal": FP64_INST_PER_VSTEP_18 * value / (peak_nominal * 1e12 / 2)},
+                             "fp64_arith_inst_per_vehicle_step": FP64_INST_PER_VSTEP_18,
+                             "fp64_pipe_inst_per_vehicle_step": FP64_PIPE_PER_VSTEP_18,
+                             "source": "ncu sm__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on.sum and "
+                                       "sm__inst_executed_pipe_fp64.sum x 32 per vehicle-step of one window launch "
+                                       "(32,768 vehicles), one capture",
+                             "frac": FP64_PIPE_PER_VSTEP_18 * value / peak_dfma,
+                             "frac_nominal": FP64_PIPE_PER_VSTEP_18 * value / (peak_nominal * 1e12 / 2),
+                             "arith_frac_nominal": FP64_INST_PER_VSTEP_18 * value / (peak_nominal * 1e12 / 2)},
                          "algorithmic": f"{W_ALG_18} FP64 ops per vehicle-step (reference op count) x "
                                         f"{n * steps_per_window} vehicle-steps per launch"},
             "roofline_hbm": {"bound": "hbm", "achieved": alg_bytes / (launch_ms * 1e-3) / 1e9, "peak": hbm_peak,

@@ -389,6 +389,8 @@ int lfdm_fleet_get_launch(lfdm_fleet* f, unsigned* threads, unsigned* blocks_per
 /* before it helps with the other. Off: all warps take the 18-DOF tiles first. *frac18 receives   */
 /* the 18-DOF share of the work of the prepared fleet (1 before the first solve or tune).          */
 int lfdm_fleet_set_affinity(lfdm_fleet* f, int on);
+/* Arithmetic of the fleet kernel: LFDM_PREC_FP64 (default) or LFDM_PREC_MIXED_TIRE.               */
+int lfdm_fleet_set_precision(lfdm_fleet* f, int precision);
 int lfdm_fleet_get_affinity(lfdm_fleet* f, int* on, double* frac18);
 /* Autotuner: times the candidate configurations on the first pilot_steps steps (states restored) */
 /* and keeps the fastest; *best_ms receives its pilot time.                                        */

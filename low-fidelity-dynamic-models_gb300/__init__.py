@@ -114,6 +114,7 @@ def _sig(lib):
         "lfdm_fleet_set_launch": ([vp, u, u, u], i),
         "lfdm_fleet_get_launch": ([vp, ctypes.POINTER(u), ctypes.POINTER(u), ctypes.POINTER(u)], i),
         "lfdm_fleet_set_affinity": ([vp, i], i),
+        "lfdm_fleet_set_precision": ([vp, i], i),
         "lfdm_fleet_get_affinity": ([vp, ctypes.POINTER(i), _c_dp], i),
         "lfdm_fleet_tune": ([vp, u, _c_dp], i),
         "lfdm_fleet_solve": ([vp], i),
@@ -558,6 +559,10 @@ class Fleet:
         a, b, c = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint()
         self._ck(self._L.lfdm_fleet_get_launch(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
         return a.value, b.value, c.value
+
+    def set_precision(self, precision: int):
+        """LFDM_PREC_FP64 (0, default) or LFDM_PREC_MIXED_TIRE (2)."""
+        self._ck(self._L.lfdm_fleet_set_precision(self._h, int(precision)))
 
     def set_affinity(self, on: bool = True):
         """Split the SMs between the 18-DOF and 24-DOF tile lists (default on)."""

@@ -30,9 +30,13 @@ namespace lfdm {
 
 constexpr int kFleetKMax = (int)K18_COUNT > (int)K24_COUNT ? (int)K18_COUNT : (int)K24_COUNT;
 
-size_t fleet_smem_per_warp() { return (size_t)kFleetKMax * 32 * sizeof(double); }
+// per warp: the tile's derived constants in FP64, and their FP32 copies for the FP32 tire core
+size_t fleet_smem_per_warp(bool f32) {
+    return (size_t)kFleetKMax * 32 * (sizeof(double) + (f32 ? sizeof(float) : 0));
+}
 
-__device__ __forceinline__ void run_tile18(const FleetLaunch& L, const FleetTile& T, double* ks, int lane) {
+template <bool kF32>
+__device__ __forceinline__ void run_tile18(const FleetLaunch& L, const FleetTile& T, double* ks, float* fks, int lane) {
     const FleetModelDev& M = L.m18;
     if (lane >= T.count) return;
     const int i = T.first + lane;
@@ -40,8 +44,12 @@ __device__ __forceinline__ void run_tile18(const FleetLaunch& L, const FleetTile
     if (nst <= L.s_begin) return;
     const size_t np = (size_t)M.npad;
 #pragma unroll 4
-    for (int k = 0; k < K18_COUNT; ++k) ks[k * 32 + lane] = __ldg(M.K + (size_t)k * np + i);
-    const KView K{ks + lane, 32};
+    for (int k = 0; k < K18_COUNT; ++k) {
+        const double x = __ldg(M.K + (size_t)k * np + i);
+        ks[k * 32 + lane] = x;
+        if (kF32) fks[k * 32 + lane] = (float)x;
+    }
+    const KView K{ks + lane, 32, kF32 ? fks + lane : nullptr};
     const ClassDev18& C = M.classes[__ldg(M.class_of + i)];
     double* S = M.S + i;
     VehC v;
@@ -55,7 +63,7 @@ __device__ __forceinline__ void run_tile18(const FleetLaunch& L, const FleetTile
     for (int s = L.s_begin; s < nst; ++s) {
         const double t = __ldg(L.step_t + s);
         driver_at(cur, t, steer, thr, brk);
-        step18<false>(v, va, ts, ta, K, C, steer, thr, brk, L.dt);
+        step18<false, kF32>(v, va, ts, ta, K, C, steer, thr, brk, L.dt);
         const int k = __ldg(L.step_sample + s);
         if (M.resp && k >= 0 && k < L.nsamples) {
             double* r = M.resp + (size_t)k * LFDM18_RESP_CHANNELS * M.n + i;
@@ -79,7 +87,8 @@ __device__ __forceinline__ void run_tile18(const FleetLaunch& L, const FleetTile
     if (!state18_finite(v, ts)) M.status[i] |= 1u;
 }
 
-__device__ __forceinline__ void run_tile24(const FleetLaunch& L, const FleetTile& T, double* ks, int lane) {
+template <bool kF32>
+__device__ __forceinline__ void run_tile24(const FleetLaunch& L, const FleetTile& T, double* ks, float* fks, int lane) {
     const FleetModelDev& M = L.m24;
     if (lane >= T.count) return;
     const int i = T.first + lane;
@@ -87,8 +96,12 @@ __device__ __forceinline__ void run_tile24(const FleetLaunch& L, const FleetTile
     if (nst <= L.s_begin) return;
     const size_t np = (size_t)M.npad;
 #pragma unroll 4
-    for (int k = 0; k < K24_COUNT; ++k) ks[k * 32 + lane] = __ldg(M.K + (size_t)k * np + i);
-    const KView K{ks + lane, 32};
+    for (int k = 0; k < K24_COUNT; ++k) {
+        const double x = __ldg(M.K + (size_t)k * np + i);
+        ks[k * 32 + lane] = x;
+        if (kF32) fks[k * 32 + lane] = (float)x;
+    }
+    const KView K{ks + lane, 32, kF32 ? fks + lane : nullptr};
     const ClassDev18& C = M.classes[__ldg(M.class_of + i)];
     double* S = M.S + i;
     VehC v;
@@ -130,17 +143,21 @@ __device__ __forceinline__ void run_tile24(const FleetLaunch& L, const FleetTile
         driver_at(cur, t, steer, thr, brk);
         // the step that ends this launch's range for the vehicle also writes the values the
         // reference leaves in its state structs (as the window kernel does for a window's last step)
-        step24<false>(v, vx, va, ts, ta, su, ck, K, C, steer, thr, brk, L.dt, S, np, s == last);
+        step24<false, kF32>(v, vx, va, ts, ta, su, ck, K, C, steer, thr, brk, L.dt, S, np, s == last);
         sample(s, t);
     }
     store_state24(S, np, v, vx, va, ts, ta, su, C.tcbool);
     if (!state24_finite(v, vx, ts)) M.status[i] |= 1u;
 }
 
+// kF32: the TMeasy tire core in FP32 (precision LFDM_PREC_MIXED_TIRE)
+template <bool kF32>
 __global__ void __launch_bounds__(128) fleet_kernel(const FleetLaunch L) {
     extern __shared__ __align__(16) double fleet_smem[];
-    const int lane = threadIdx.x & 31;
-    double* ks = fleet_smem + (size_t)(threadIdx.x >> 5) * kFleetKMax * 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double* ks = fleet_smem + (size_t)warp * kFleetKMax * 32;
+    float* fks = reinterpret_cast<float*>(fleet_smem + (size_t)(blockDim.x >> 5) * kFleetKMax * 32) +
+                 (size_t)warp * kFleetKMax * 32;
     unsigned smid, nsmid;
     asm("mov.u32 %0, %%smid;" : "=r"(smid));
     asm("mov.u32 %0, %%nsmid;" : "=r"(nsmid));
@@ -159,30 +176,35 @@ __global__ void __launch_bounds__(128) fleet_kernel(const FleetLaunch L) {
             if (tile >= count[q]) break;
             const FleetTile T = L.tiles[base[q] + tile];
             if (T.nsteps_max > L.s_begin) {
-                if (T.model == LFDM_MODEL_24) run_tile24(L, T, ks, lane);
-                else run_tile18(L, T, ks, lane);
+                if (T.model == LFDM_MODEL_24) run_tile24<kF32>(L, T, ks, fks, lane);
+                else run_tile18<kF32>(L, T, ks, fks, lane);
             }
             __syncwarp();
         }
     }
 }
 
-// Raises the kernel's dynamic shared-memory limit to what 4 warps per block need (every
+// Raises the kernels' dynamic shared-memory limits to what 4 warps per block need (every
 // configuration uses at most that); called before any launch or occupancy query, outside capture.
 cudaError_t fleet_kernel_setup() {
-    return cudaFuncSetAttribute(fleet_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(fleet_smem_per_warp() * 4));
+    cudaError_t e = cudaFuncSetAttribute(fleet_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(fleet_smem_per_warp(false) * 4));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(fleet_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(fleet_smem_per_warp(true) * 4));
 }
 
-cudaError_t fleet_occupancy(int threads, int* blocks_per_sm) {
-    const size_t smem = fleet_smem_per_warp() * (threads / 32);
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fleet_kernel, threads, smem);
+cudaError_t fleet_occupancy(int threads, bool f32, int* blocks_per_sm) {
+    const size_t smem = fleet_smem_per_warp(f32) * (threads / 32);
+    return f32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fleet_kernel<true>, threads, smem)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fleet_kernel<false>, threads, smem);
 }
 
-cudaError_t launch_fleet(const FleetLaunch& L, int blocks, int threads, cudaStream_t stream) {
+cudaError_t launch_fleet(const FleetLaunch& L, int blocks, int threads, bool f32, cudaStream_t stream) {
     if (threads <= 0 || threads > 128 || (threads & 31) || blocks <= 0) return cudaErrorInvalidValue;
-    const size_t smem = fleet_smem_per_warp() * (threads / 32);
-    fleet_kernel<<<blocks, threads, smem, stream>>>(L);
+    const size_t smem = fleet_smem_per_warp(f32) * (threads / 32);
+    if (f32) fleet_kernel<true><<<blocks, threads, smem, stream>>>(L);
+    else fleet_kernel<false><<<blocks, threads, smem, stream>>>(L);
     return cudaGetLastError();
 }
 

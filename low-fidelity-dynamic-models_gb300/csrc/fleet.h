@@ -50,9 +50,10 @@ struct FleetLaunch {
     int nsamples = 0;                      // samples the response buffers hold
 };
 
-size_t fleet_smem_per_warp();
+// f32: the kernel with the FP32 TMeasy tire core (precision LFDM_PREC_MIXED_TIRE)
+size_t fleet_smem_per_warp(bool f32);
 cudaError_t fleet_kernel_setup();
-cudaError_t fleet_occupancy(int threads, int* blocks_per_sm);
-cudaError_t launch_fleet(const FleetLaunch& L, int blocks, int threads, cudaStream_t stream);
+cudaError_t fleet_occupancy(int threads, bool f32, int* blocks_per_sm);
+cudaError_t launch_fleet(const FleetLaunch& L, int blocks, int threads, bool f32, cudaStream_t stream);
 
 }  // namespace lfdm

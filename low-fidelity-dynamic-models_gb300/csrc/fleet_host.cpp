@@ -90,6 +90,8 @@ struct lfdm_fleet {
     int ntiles18 = 0;
     double frac18 = 1.0;           // 18-DOF share of the estimated work (steps x per-step cost)
     bool affinity = true;          // split the SMs between the two models' tile lists
+    int precision = LFDM_PREC_FP64;  // or LFDM_PREC_MIXED_TIRE
+    bool f32() const { return precision == LFDM_PREC_MIXED_TIRE; }
     DBuf<double> d_rows, d_step_t;
     DBuf<int32_t> d_step_sample;
     DBuf<FleetTile> d_tiles;
@@ -341,7 +343,7 @@ int plan(lfdm_fleet* f, int steps, unsigned threads, unsigned bps, unsigned spl,
     FCK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, f->device));
     FCK(fleet_kernel_setup());
     int occ = 0;
-    FCK(fleet_occupancy((int)threads, &occ));
+    FCK(fleet_occupancy((int)threads, f->f32(), &occ));
     if (occ < 1) return f->fail(LFDM_ERR_CUDA, "the fleet kernel does not fit with %u threads per block", threads);
     const int per_sm = bps ? std::min<int>((int)bps, occ) : occ;
     p->blocks = dev_sms * per_sm;
@@ -372,7 +374,7 @@ int enqueue(lfdm_fleet* f, int steps, const Plan& p) {
         L.s_end = std::min(steps, (c + 1) * p.chunk);
         L.dt = f->dt;
         L.nsamples = f->nsamples;
-        FCK(launch_fleet(L, p.blocks, (int)p.threads, f->stream));
+        FCK(launch_fleet(L, p.blocks, (int)p.threads, f->f32(), f->stream));
     }
     return LFDM_OK;
 }
@@ -544,6 +546,15 @@ int lfdm_fleet_set_launch(lfdm_fleet* f, unsigned threads, unsigned blocks_per_s
     return LFDM_OK;
 }
 
+int lfdm_fleet_set_precision(lfdm_fleet* f, int precision) {
+    if (!f) return LFDM_ERR_ARG;
+    if (precision != LFDM_PREC_FP64 && precision != LFDM_PREC_MIXED_TIRE)
+        return f->fail(LFDM_ERR_ARG, "the fleet steps in FP64 or with the FP32 tire core (precision %d)", precision);
+    f->precision = precision;
+    f->drop_graph();
+    return LFDM_OK;
+}
+
 int lfdm_fleet_set_affinity(lfdm_fleet* f, int on) {
     if (!f) return LFDM_ERR_ARG;
     f->affinity = on != 0;
@@ -638,7 +649,7 @@ int lfdm_fleet_tune(lfdm_fleet* f, unsigned pilot_steps, double* best_ms) {
     FCK(fleet_kernel_setup());
     for (unsigned th : {32u, 64u, 128u}) {
         int occ = 0;
-        FCK(fleet_occupancy((int)th, &occ));
+        FCK(fleet_occupancy((int)th, f->f32(), &occ));
         if (occ < 1) continue;
         std::vector<unsigned> bl = {0u};
         if (occ >= 2) bl.push_back((unsigned)occ / 2);

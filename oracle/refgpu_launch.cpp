@@ -240,7 +240,7 @@ int main(int argc, char** argv) {
     r.ksim = dh[1];
     r.tend = dh[2];
     r.dtout = dh[3];
-    const int ns = model == 11 ? LFDM11_S_COUNT : model == 24 ? LFDM24_S_COUNT : LFDM_S_COUNT;
+    const int ns = model == 11 ? (int)LFDM11_S_COUNT : model == 24 ? (int)LFDM24_S_COUNT : (int)LFDM_S_COUNT;
     if ((model != 11 && model != 18 && model != 24) || r.n <= 0 || r.nrows <= 0 || r.tpb <= 0) return 2;
     r.P.resize((size_t)r.n * LFDM_P_COUNT);
     r.T.resize((size_t)r.n * r.nrows * 4);

@@ -37,7 +37,7 @@ def _windows(h):
     return w
 
 
-def _per_group(lfdm, mf):
+def _per_group(lfdm, mf, precision=0):
     """Each (model, class, window count) group through the regular solver: states and responses in
     the fleet's add order per model."""
     out = {18: [], 24: []}
@@ -53,6 +53,7 @@ def _per_group(lfdm, mf):
             idx = np.nonzero(wins == w)[0]
             sol = cls_(len(idx))
             sol.construct_class(g["cls"], g["params"][idx])
+            sol.set_precision(precision)
             tabs = np.stack([mf["rows"][g["row_off"][i]: g["row_off"][i] + g["row_len"][i]] for i in idx])
             sol.set_driver_tables(tabs)
             sol.set_states(g["states"][idx])
@@ -144,6 +145,26 @@ def test_fleet_of_one_model(built_lib, reference_runs, model):
     fr = f.get_response(model)
     for i, r in enumerate(resp[model]):
         assert np.array_equal(fr[: r.shape[0], :, i], r), i
+    f.close()
+
+
+def test_fleet_mixed_tire_precision_matches_per_group_solves(built_lib):
+    """With the FP32 tire core (LFDM_PREC_MIXED_TIRE) the fleet kernel gives every vehicle what the
+    window kernels of that precision give it, bit for bit, with and without model affinity."""
+    mf = _small_fleet(n=300, seed=12)
+    ref = _per_group(built_lib, mf, precision=2)
+    for on in (True, False):
+        f = _make(built_lib, mf, (64, 0, 0))
+        f.set_precision(2)
+        f.set_affinity(on)
+        f.solve()
+        _check(built_lib, f, mf, ref)
+        f.close()
+    fp64 = _per_group(built_lib, mf)[0]
+    assert not np.array_equal(fp64[18], ref[0][18])  # the FP32 core does round differently
+    f = _make(built_lib, mf)
+    with pytest.raises(built_lib.LfdmError):
+        f.set_precision(1)  # the FP32 right-hand side form is built for the window kernels only
     f.close()
 
 
