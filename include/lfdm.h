@@ -332,6 +332,13 @@ int lfdm_traj18_branch_signature(lfdm_solver* h, const double* ctl, unsigned nst
 int lfdm_rhs_jacobian18(lfdm_solver* h, const double* ctl, int reference_point, double* jac_state, double* jac_ctl,
                         int* ny);
 
+/* Exact Jacobians of the 11-DOF right-hand side as well (replaces the Jacobian block of            */
+/* 11dof/dof11_halfImplicit.cpp:335-429): the same call for an 11- or 18-DOF solver, each in its     */
+/* model's packed order; 11-DOF y = {xe, ye} front, rear (TMeasy only), omega front, rear, crank     */
+/* speed (torque converter only), x, y, u, v, psi, wz: ny = 13 / 12 (TMeasy), 9 / 8 (TMeasyNr).       */
+int lfdm_rhs_jacobian_exact(lfdm_solver* h, const double* ctl, int reference_point, double* jac_state,
+                            double* jac_ctl, int* ny);
+
 /* The reference's own Jacobian scheme for every model and tire type, batched over vehicles        */
 /* (replaces IntegrateStepWithJacobian's Jacobian block: 11dof/dof11_halfImplicit.cpp:335-429,     */
 /* 18dof/dof18_halfImplicit.cpp:356-449, 24dof/dof24_halfImplicit.cpp:402-494): every packed state   */
@@ -348,11 +355,11 @@ int lfdm_rhs_jacobian_fd(lfdm_solver* h, const double* ctl, int reference_point,
 
 /* Either Jacobian with HOST buffers, laid out per vehicle as the reference's CPU solvers return     */
 /* them (GetJacobianState / GetJacobianControls): ctl [3][N] = {steering, throttle, braking},       */
-/* jac_state [N][ny][ny], jac_ctl [N][ny][2]. exact = 1 selects lfdm_rhs_jacobian18 (18-DOF), 0 the */
-/* reference's difference scheme (lfdm_rhs_jacobian_fd). With jac_state and jac_ctl both NULL only  */
-/* *ny is set (ny <= 36 for every model). The solver's configuration is checked first, so the size  */
-/* query fails (LFDM_ERR_ARG) for a configuration the chosen Jacobian does not support, before any   */
-/* buffer is allocated.                                                                              */
+/* jac_state [N][ny][ny], jac_ctl [N][ny][2]. exact = 1 selects lfdm_rhs_jacobian_exact (11- and  */
+/* 18-DOF), 0 the reference's difference scheme (lfdm_rhs_jacobian_fd). With jac_state and jac_ctl  */
+/* both NULL only *ny is set (ny <= 36 for every model). The solver's configuration is checked      */
+/* first, so the size query fails (LFDM_ERR_ARG) for a configuration the chosen Jacobian does not  */
+/* support, before any buffer is allocated.                                                         */
 int lfdm_rhs_jacobian_host(lfdm_solver* h, int exact, const double* ctl, int reference_point, double* jac_state,
                            double* jac_ctl, int* ny);
 
@@ -384,10 +391,11 @@ int lfdm_fleet_set_output(lfdm_fleet* f, double dtout);
 /* and steps per launch (0: the whole horizon in one launch).                                      */
 int lfdm_fleet_set_launch(lfdm_fleet* f, unsigned threads, unsigned blocks_per_sm, unsigned steps_per_launch);
 int lfdm_fleet_get_launch(lfdm_fleet* f, unsigned* threads, unsigned* blocks_per_sm, unsigned* steps_per_launch);
-/* Model affinity (default on): the SMs are split between the 18-DOF and the 24-DOF tiles in      */
-/* proportion to their estimated work (steps x per-step cost); each warp drains its SM's home list */
-/* before it helps with the other. Off: all warps take the 18-DOF tiles first. *frac18 receives   */
-/* the 18-DOF share of the work of the prepared fleet (1 before the first solve or tune).          */
+/* Model affinity (default off; lfdm_fleet_tune tries both): the SMs are split between the 18-DOF */
+/* and 24-DOF tiles in proportion to their estimated work (steps x per-step cost) and each warp    */
+/* drains its SM's home list before it helps with the other. Off: one list of both models' tiles  */
+/* by estimated cost. *frac18 receives the 18-DOF share of the work of the prepared fleet (1 before */
+/* the first solve or tune).                                                                        */
 int lfdm_fleet_set_affinity(lfdm_fleet* f, int on);
 /* Arithmetic of the fleet kernel: LFDM_PREC_FP64 (default) or LFDM_PREC_MIXED_TIRE.               */
 int lfdm_fleet_set_precision(lfdm_fleet* f, int precision);

@@ -101,6 +101,7 @@ def _sig(lib):
         "lfdm_traj18_last_ms": ([vp, _c_dp, _c_dp], i),
         "lfdm_traj18_branch_signature": ([vp, vp, u, vp], i),
         "lfdm_rhs_jacobian18": ([vp, vp, i, vp, vp, ctypes.POINTER(i)], i),
+        "lfdm_rhs_jacobian_exact": ([vp, vp, i, vp, vp, ctypes.POINTER(i)], i),
         "lfdm_rhs_jacobian_fd": ([vp, vp, i, vp, vp, ctypes.POINTER(i)], i),
         "lfdm_rhs_jacobian_host": ([vp, i, vp, i, vp, vp, ctypes.POINTER(i)], i),
         "lfdm_fleet_create": ([i, ctypes.POINTER(vp)], i),
@@ -443,11 +444,19 @@ class d11SolverHalfImplicitGPU(_SolverGPU):
     """11-DOF batched half-implicit stepper on one GPU (reference: 11dof-gpu/dof11_halfImplicit_gpu.cuh).
 
     States use the LFDM11_S_* layout (S11): chassis X, Y, u, v, psi, wz, their rates, crank speed,
-    crank acceleration, current gear, then the front and rear TMeasy tire blocks; FP64 only."""
+    crank acceleration, current gear, then the front and rear TMeasy tire blocks."""
 
     MODEL = 11
     STATE_COUNT = S11_COUNT
     RESP_CHANNELS = RESP11
+
+    def rhs_jacobian(self, steering, throttle, braking=0.0, reference_point: bool = True):
+        """Exact Jacobians of the 11-DOF right-hand side at every vehicle's current state
+        (lfdm_rhs_jacobian_exact; the reference CPU solver's GetJacobianState / GetJacobianControls
+        by central differences, 11dof/dof11_halfImplicit.cpp:335-429). Returns (jac_state [N, ny, ny],
+        jac_controls [N, ny, 2]) in the reference's packed order: ny = 13 with a torque converter and
+        12 without (9 and 8 with TMeasyNr tires)."""
+        return self._jacobian(self._L.lfdm_rhs_jacobian_exact, steering, throttle, braking, reference_point)
 
 
 class d24SolverHalfImplicitGPU(_SolverGPU):

@@ -4,13 +4,14 @@
 // The reference solves one model, one end time and (per Construct) one parameter set per solver
 // (d18SolverHalfImplicitGPU / d24SolverHalfImplicitGPU, m_tend global), so an uneven fleet needs one
 // solver run per model and horizon group. Here the vehicles of each model are sorted by their step
-// count (longest first) and cut into tiles of 32 (one warp). Each model's tiles form a work list
-// ordered by estimated cost (steps x vehicles), largest first. A persistent grid (SMs x resident
-// blocks) pulls tiles with one atomic per tile and runs each tile's vehicles over the steps of this
-// launch, keeping their state in registers, so long-horizon vehicles start first and short ones
-// fill the tail (longest-processing-time-first scheduling). Model affinity: the SMs are split in
+// count (longest first) and cut into tiles of 32 (one warp). The tiles of both models form one work
+// list ordered by estimated cost (steps x vehicles x per-step cost of the model), largest first. A
+// persistent grid (SMs x resident blocks) pulls tiles with one atomic per tile and runs each tile's
+// vehicles over the steps of this launch, keeping their state in registers, so long-horizon
+// vehicles start first and short ones fill the tail (longest-processing-time-first scheduling).
+// Model affinity (an autotuner choice): each model's tiles in a list of its own, and the SMs split in
 // proportion to the two models' estimated work; a warp first drains its SM's home list and then
-// helps with the other one. An SM then runs one model's code for most of the launch instead of
+// helps with the other one, so that an SM runs one model's code for most of the launch instead of
 // interleaving the two step functions (together larger than the instruction cache).
 //
 // Each vehicle follows exactly the reference's per-vehicle schedule: the step start times are the
@@ -158,6 +159,21 @@ __global__ void __launch_bounds__(128) fleet_kernel(const FleetLaunch L) {
     double* ks = fleet_smem + (size_t)warp * kFleetKMax * 32;
     float* fks = reinterpret_cast<float*>(fleet_smem + (size_t)(blockDim.x >> 5) * kFleetKMax * 32) +
                  (size_t)warp * kFleetKMax * 32;
+    if (!L.affinity) {
+        for (;;) {
+            int tile = 0;
+            if (lane == 0) tile = atomicAdd(L.queue, 1);
+            tile = __shfl_sync(0xffffffffu, tile, 0);
+            if (tile >= L.ntiles) break;
+            const FleetTile T = L.merged[tile];
+            if (T.nsteps_max > L.s_begin) {
+                if (T.model == LFDM_MODEL_24) run_tile24<kF32>(L, T, ks, fks, lane);
+                else run_tile18<kF32>(L, T, ks, fks, lane);
+            }
+            __syncwarp();
+        }
+        return;
+    }
     unsigned smid, nsmid;
     asm("mov.u32 %0, %%smid;" : "=r"(smid));
     asm("mov.u32 %0, %%nsmid;" : "=r"(nsmid));

@@ -38,11 +38,13 @@ struct FleetLaunch {
     FleetModelDev m18, m24;
     const double* rows = nullptr;          // driver rows {t, steering, throttle, braking}
     const FleetTile* tiles = nullptr;      // the 18-DOF tiles [0, ntiles18), then the 24-DOF ones
+    const FleetTile* merged = nullptr;     // the same tiles in one list by estimated cost (both models)
     int ntiles = 0;
     int ntiles18 = 0;
-    int* queue = nullptr;                  // this launch's two tile counters (18-DOF, 24-DOF), zero at its start
-    float home18 = 0.0f;                   // SMs with smid < home18 * nsmid start on the 18-DOF tiles, the
-                                           // others on the 24-DOF tiles; 0 or 1 without model affinity
+    int* queue = nullptr;                  // this launch's two tile counters, zero at its start
+    int affinity = 0;                      // 0: one list by cost (merged, counter 0); 1: model affinity
+    float home18 = 0.0f;                   // with affinity: SMs with smid < home18 * nsmid start on the
+                                           // 18-DOF tiles, the others on the 24-DOF tiles
     const double* step_t = nullptr;        // [total steps] start time of each global step
     const int32_t* step_sample = nullptr;  // [total steps] sample index taken after the step, or -1
     int s_begin = 0, s_end = 0;            // global steps [s_begin, s_end) of this launch

@@ -86,10 +86,11 @@ struct lfdm_fleet {
     std::vector<int32_t> step_sample;
     std::vector<int32_t> window_end;  // cumulative steps at the end of each window
     int spw = 0, nsamples = 0, total_steps = 0;
-    std::vector<FleetTile> tiles;  // the 18-DOF tiles [0, ntiles18), then the 24-DOF tiles
+    std::vector<FleetTile> tiles;   // the 18-DOF tiles [0, ntiles18), then the 24-DOF tiles
+    std::vector<FleetTile> merged;  // all tiles in one list by estimated cost
     int ntiles18 = 0;
-    double frac18 = 1.0;           // 18-DOF share of the estimated work (steps x per-step cost)
-    bool affinity = true;          // split the SMs between the two models' tile lists
+    double frac18 = 1.0;            // 18-DOF share of the estimated work (steps x per-step cost)
+    bool affinity = false;          // split the SMs between the two models' tile lists
     int precision = LFDM_PREC_FP64;  // or LFDM_PREC_MIXED_TIRE
     bool f32() const { return precision == LFDM_PREC_MIXED_TIRE; }
     DBuf<double> d_rows, d_step_t;
@@ -296,6 +297,12 @@ int prepare(lfdm_fleet* f) {
         if (!m24) f->ntiles18 = (int)f->tiles.size();
     }
     f->frac18 = work[0] + work[1] > 0 ? work[0] / (work[0] + work[1]) : 1.0;
+    f->merged = f->tiles;
+    std::stable_sort(f->merged.begin(), f->merged.end(), [](const FleetTile& a, const FleetTile& b) {
+        const double ca = (double)a.nsteps_max * (a.model == LFDM_MODEL_24 ? kCost24 : kCost18) * a.count;
+        const double cb = (double)b.nsteps_max * (b.model == LFDM_MODEL_24 ? kCost24 : kCost18) * b.count;
+        return ca > cb;
+    });
     FCK(f->d_rows.ensure(std::max<size_t>(4, f->rows.size())));
     FCK(cudaMemcpyAsync(f->d_rows.p, f->rows.data(), f->rows.size() * sizeof(double), cudaMemcpyHostToDevice,
                         f->stream));
@@ -305,9 +312,11 @@ int prepare(lfdm_fleet* f) {
                         f->stream));
     FCK(cudaMemcpyAsync(f->d_step_sample.p, f->step_sample.data(), f->total_steps * sizeof(int32_t),
                         cudaMemcpyHostToDevice, f->stream));
-    FCK(f->d_tiles.ensure(std::max<size_t>(1, f->tiles.size())));
+    FCK(f->d_tiles.ensure(std::max<size_t>(2, 2 * f->tiles.size())));
     FCK(cudaMemcpyAsync(f->d_tiles.p, f->tiles.data(), f->tiles.size() * sizeof(FleetTile), cudaMemcpyHostToDevice,
                         f->stream));
+    FCK(cudaMemcpyAsync(f->d_tiles.p + f->tiles.size(), f->merged.data(), f->merged.size() * sizeof(FleetTile),
+                        cudaMemcpyHostToDevice, f->stream));
     FCK(cudaStreamSynchronize(f->stream));
     f->drop_graph();
     f->dirty = false;
@@ -364,10 +373,11 @@ int enqueue(lfdm_fleet* f, int steps, const Plan& p) {
         L.rows = f->d_rows.p;
         L.tiles = f->d_tiles.p;
         L.ntiles = (int)f->tiles.size();
+        L.merged = f->d_tiles.p + f->tiles.size();
         L.ntiles18 = f->ntiles18;
         L.queue = f->d_queue.p + 2 * c;
-        // without affinity every SM starts on the 18-DOF list, and the 24-DOF list follows
-        L.home18 = f->affinity ? (float)f->frac18 : 1.0f;
+        L.affinity = f->affinity ? 1 : 0;
+        L.home18 = (float)f->frac18;
         L.step_t = f->d_step_t.p;
         L.step_sample = f->d_step_sample.p;
         L.s_begin = c * p.chunk;
@@ -644,6 +654,7 @@ int lfdm_fleet_tune(lfdm_fleet* f, unsigned pilot_steps, double* best_ms) {
     }
     struct Cand {
         unsigned threads, bps, spl;
+        bool aff;
     };
     std::vector<Cand> cands;
     FCK(fleet_kernel_setup());
@@ -654,11 +665,15 @@ int lfdm_fleet_tune(lfdm_fleet* f, unsigned pilot_steps, double* best_ms) {
         std::vector<unsigned> bl = {0u};
         if (occ >= 2) bl.push_back((unsigned)occ / 2);
         for (unsigned b : bl)
-            for (unsigned spl : {0u, (unsigned)std::max(1, steps / 4)}) cands.push_back({th, b, spl});
+            for (unsigned spl : {0u, (unsigned)std::max(1, steps / 4)})
+                for (bool aff : {false, true}) cands.push_back({th, b, spl, aff});
     }
     double best = 1e300;
-    Cand best_c = {f->threads, f->blocks_per_sm, f->steps_per_launch};
+    Cand best_c = {f->threads, f->blocks_per_sm, f->steps_per_launch, f->affinity};
+    const bool both_models = f->g18.n() > 0 && f->g24.n() > 0;
     for (const Cand& c : cands) {
+        if (c.aff && !both_models) continue;  // one model: the lists coincide
+        f->affinity = c.aff;
         for (ModelGroup* g : {&f->g18, &f->g24})
             if (g->n())
                 FCK(cudaMemcpyAsync(g->d_S.p, g->d_S_backup.p, g->d_S.n * sizeof(double), cudaMemcpyDeviceToDevice,
@@ -687,6 +702,7 @@ int lfdm_fleet_tune(lfdm_fleet* f, unsigned pilot_steps, double* best_ms) {
     FCK(cudaStreamSynchronize(f->stream));
     f->threads = best_c.threads;
     f->blocks_per_sm = best_c.bps;
+    f->affinity = best_c.aff;
     // the pilot's chunking, scaled to the whole horizon (0 = one launch)
     f->steps_per_launch = best_c.spl ? (unsigned)std::max<long long>(1, (long long)f->total_steps / 4) : 0;
     f->tune_ms = best;

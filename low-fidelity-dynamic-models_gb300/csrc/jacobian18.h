@@ -1,4 +1,4 @@
-// Batched exact Jacobians of the 18-DOF right-hand side (jacobian18.cu).
+// Batched exact Jacobians of the 18- and 11-DOF right-hand sides (jacobian18.cu, jacobian11.cu).
 #pragma once
 
 #include <cstddef>
@@ -27,5 +27,10 @@ struct JacLaunch {
 };
 
 cudaError_t launch_rhs_jacobian18(const JacLaunch& A, cudaStream_t stream);
+// The same for the 11-DOF model (jacobian11.cu); S holds [LFDM11_S_COUNT][npad] states.
+cudaError_t launch_rhs_jacobian11(const JacLaunch& A, cudaStream_t stream);
+// Dynamic shared memory of a Jacobian block (derived constants, their adjoint scratch and, when
+// they fit, the class tables; *cls_smem says whether they do).
+size_t jac18_smem(int threads, int nclasses, bool* cls_smem);
 
 }  // namespace lfdm

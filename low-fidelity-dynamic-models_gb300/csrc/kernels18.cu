@@ -294,8 +294,18 @@ size_t window18_smem(int threads, int nclasses, bool f32) {
 
 // kF32: the TMeasy tire core in FP32 (precision LFDM_PREC_MIXED_TIRE), on FP32 copies of the
 // derived constants staged beside the FP64 ones.
+// Resident 128-thread blocks per SM the compiler budgets registers for (1: up to 255 registers, 8
+// warps per SM): the FP64 kernels are FP64-pipe bound and fastest with every register; the FP32-core
+// kernels issue mostly short-latency FP32 work and are tuned separately.
+#ifndef LFDM_TF_MIN_BLOCKS
+#define LFDM_TF_MIN_BLOCKS 1
+#endif
+#ifndef LFDM_MIXED_MIN_BLOCKS
+#define LFDM_MIXED_MIN_BLOCKS 1
+#endif
+
 template <bool kNr, int kCtl, bool kOut, bool kF32>
-__global__ void __launch_bounds__(128) window18_kernel(const Window18 w) {
+__global__ void __launch_bounds__(128, kF32 ? LFDM_TF_MIN_BLOCKS : 1) window18_kernel(const Window18 w) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
     const bool cls_smem = w.nclasses <= kMaxSmemClasses;
@@ -437,7 +447,7 @@ __device__ __forceinline__ void driver_at_f(DriverCursorF& d, double t, float& s
 }
 
 template <int kCtl, bool kOut>
-__global__ void __launch_bounds__(128) window18_mixed_kernel(const Window18 w) {
+__global__ void __launch_bounds__(128, LFDM_MIXED_MIN_BLOCKS) window18_mixed_kernel(const Window18 w) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int tid = threadIdx.x;
     const bool cls_smem = w.nclasses <= kMaxSmemClasses;

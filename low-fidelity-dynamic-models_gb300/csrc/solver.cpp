@@ -1043,11 +1043,11 @@ int lfdm_traj18_backward(lfdm_solver* h, const double* ctl, const double* ref, u
     return LFDM_OK;
 }
 
-// The solver configurations a right-hand-side Jacobian can be formed for (exact: the 18-DOF model
-// without throttleMod; either: FP64, all vehicles with or without a torque converter).
+// The solver configurations a right-hand-side Jacobian can be formed for (exact: the 11- and 18-DOF
+// models without throttleMod; either: FP64, all vehicles with or without a torque converter).
 static int jacobian_supported(lfdm_solver* h, bool exact) {
-    if (exact && h->model != LFDM_MODEL_18)
-        return h->fail(LFDM_ERR_ARG, "the right-hand-side Jacobian is the 18-DOF model's");
+    if (exact && h->model == LFDM_MODEL_24)
+        return h->fail(LFDM_ERR_ARG, "the exact right-hand-side Jacobian is built for the 11- and 18-DOF models");
     if (h->precision != LFDM_PREC_FP64) return h->fail(LFDM_ERR_ARG, "the right-hand-side Jacobian is FP64");
     if (h->classes.empty()) return h->fail(LFDM_ERR_STATE, "no vehicles constructed");
     const int tc = h->classes[0].tcbool != 0;
@@ -1061,6 +1061,13 @@ static int jacobian_supported(lfdm_solver* h, bool exact) {
 
 int lfdm_rhs_jacobian18(lfdm_solver* h, const double* ctl, int reference_point, double* jac_state, double* jac_ctl,
                         int* ny) {
+    if (!h) return LFDM_ERR_ARG;
+    if (h->model != LFDM_MODEL_18) return h->fail(LFDM_ERR_ARG, "lfdm_rhs_jacobian18 needs an 18-DOF solver");
+    return lfdm_rhs_jacobian_exact(h, ctl, reference_point, jac_state, jac_ctl, ny);
+}
+
+int lfdm_rhs_jacobian_exact(lfdm_solver* h, const double* ctl, int reference_point, double* jac_state,
+                            double* jac_ctl, int* ny) {
     if (!h) return LFDM_ERR_ARG;
     if (!ctl || !jac_state || !jac_ctl) return h->fail(LFDM_ERR_ARG, "null array");
     int rc = jacobian_supported(h, true);
@@ -1085,9 +1092,9 @@ int lfdm_rhs_jacobian18(lfdm_solver* h, const double* ctl, int reference_point, 
     A.tape = h->d_adj_tape.p;
     A.jac_state = jac_state;
     A.jac_ctl = jac_ctl;
-    CK(launch_rhs_jacobian18(A, h->stream));
+    CK(h->model == LFDM_MODEL_11 ? launch_rhs_jacobian11(A, h->stream) : launch_rhs_jacobian18(A, h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    if (ny) *ny = (A.tire_nr ? 12 : 20) + (tc ? 1 : 0);
+    if (ny) *ny = jac_fd_ny((int)h->model, A.tire_nr != 0, tc != 0);
     return LFDM_OK;
 }
 
@@ -1140,7 +1147,7 @@ int lfdm_rhs_jacobian_host(lfdm_solver* h, int exact, const double* ctl, int ref
     CK(h->d_jac_u.ensure((size_t)m * 2 * n));
     CK(cudaMemcpyAsync(h->d_jac_in.p, ctl, 3 * n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     int got = 0;
-    const int rc = exact ? lfdm_rhs_jacobian18(h, h->d_jac_in.p, reference_point, h->d_jac_s.p, h->d_jac_u.p, &got)
+    const int rc = exact ? lfdm_rhs_jacobian_exact(h, h->d_jac_in.p, reference_point, h->d_jac_s.p, h->d_jac_u.p, &got)
                          : lfdm_rhs_jacobian_fd(h, h->d_jac_in.p, reference_point, h->d_jac_s.p, h->d_jac_u.p, &got);
     if (rc) return rc;
     if (got != m) return h->fail(LFDM_ERR_STATE, "unexpected Jacobian size");
