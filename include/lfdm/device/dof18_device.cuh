@@ -156,6 +156,45 @@ __device__ __forceinline__ double sine_step_nn(double x, double x1, double y1, d
     return y1 + dy * u - (dy / k2Pi) * sin(k2Pi * u);
 }
 
+// The structural/dynamic blend weights of one tire, sineStep(a, 1, 1, 1.5, 0) of its longitudinal
+// and lateral slip speeds (computeTireRHS, 18dof-gpu/dof18_gpu.cu:509-529), for the lanes of a warp
+// together. Outside the band 1 < a < 1.5 the weight is 1 or 0; inside it takes a division by a
+// constant and a sine. Evaluated lane by lane, a warp runs the band code once for the x blend and
+// once for the y blend whenever any of its lanes is in that band, so it pays two band evaluations
+// on nearly every step. Here the warp's in-band arguments (x blends first, then y blends) are dealt
+// to its lanes, each lane evaluates one (with sine_step_nn itself, so each weight is the value it
+// had lane by lane, bit for bit) and the weights are returned to their lanes: one band evaluation
+// per 32 in-band arguments. The lanes that reach this point together (__activemask) take part, so
+// lanes that left earlier (a lifted wheel, a finished vehicle) are not waited for.
+__device__ __forceinline__ void blend_weights(double ax, double ay, double& wx, double& wy) {
+    const bool bx = gt_nn(ax, 1.0) && gt_nn(1.5, ax);
+    const bool by = gt_nn(ay, 1.0) && gt_nn(1.5, ay);
+    wx = gt_nn(ax, 1.0) ? 0.0 : 1.0;  // the band's lanes are filled in below
+    wy = gt_nn(ay, 1.0) ? 0.0 : 1.0;
+    const unsigned act = __activemask();
+    const unsigned mx = __ballot_sync(act, bx), my = __ballot_sync(act, by);
+    const int nx = __popc(mx), total = nx + __popc(my);
+    if (total == 0) return;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned below = (1u << lane) - 1u;
+    const int nact = __popc(act), rank = __popc(act & below);
+    const int ex = __popc(mx & below), ey = nx + __popc(my & below);  // this lane's entries
+    for (int base = 0; base < total; base += nact) {
+        const int e = base + rank;  // the entry this lane evaluates
+        const bool isx = e < nx;
+        const unsigned src = e < total ? __fns(isx ? mx : my, 0, (isx ? e : e - nx) + 1) : lane;
+        const double vx = __shfl_sync(act, ax, src), vy = __shfl_sync(act, ay, src);
+        const double a = e < total ? (isx ? vx : vy) : 1.25;  // idle lanes evaluate an in-band dummy
+        const double w = sine_step_nn(a, 1., 1., 1.5, 0.);
+        const int ox = ex - base, oy = ey - base;
+        const bool gx = bx && ox >= 0 && ox < nact, gy = by && oy >= 0 && oy < nact;
+        const double rx = __shfl_sync(act, w, gx ? __fns(act, 0, ox + 1) : lane);
+        const double ry = __shfl_sync(act, w, gy ? __fns(act, 0, oy + 1) : lane);
+        if (gx) wx = rx;
+        if (gy) wy = ry;
+    }
+}
+
 // The shared prefix [0, KT_COUNT) of the derived constants from one flat parameter vector p:
 // tire curve coefficients (InterpQ(fz,w1,w2,pn) = fzn*(Q1 - Q2*fzn), InterpL(fz,w1,w2,pn) =
 // w1 + (w2-w1)*(fzn-1) with fzn = fz/pn, utils_gpu.cuh:86-93), powertrain and steering constants.
@@ -503,8 +542,8 @@ __device__ __forceinline__ void tire_core_tm(TireC& ts, TireAux& ta, const KView
     const double fydyn = fma(dy, ts.yedot, cy * ts.ye);
     const double fxstr = clamp_sym(fma(ts.xe, cx, ts.xedot * dx), K(K_FXMP2N));
     const double fystr = clamp_sym(fma(ts.ye, cy, ts.yedot * dy), K(K_FYMP2N));
-    const double wx = sine_step_nn(fabs(vsx), 1., 1., 1.5, 0.);
-    const double wy = sine_step_nn(fabs(sy * vta), 1., 1., 1.5, 0.);
+    double wx, wy;
+    blend_weights(fabs(vsx), fabs(sy * vta), wx, wy);
     ta.fx = is_zero(wx) ? fxdyn : fma(wx, fxstr, (1. - wx) * fxdyn);
     ta.fy = is_zero(wy) ? fydyn : fma(wy, fystr, (1. - wy) * fydyn);
 }

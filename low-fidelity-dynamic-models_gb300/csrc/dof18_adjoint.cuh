@@ -190,19 +190,24 @@ __device__ __forceinline__ void sine_step_w(double x, double& y, double& dy) {
 
 // The regime tmxy_frac takes for these arguments, by its own comparisons (the quantities they
 // compare are computed by the same expressions, so they round alike): 0 no force, 1 full sliding,
-// 2 adhesion, 3 and 4 the two parabolas, 5 the cubic fallback.
+// 2 adhesion, 3 and 4 the two parabolas, 5 the cubic fallback; plus 8 where the initial slope is
+// 2 fm / sm rather than df0 (the max of the two is a kink of the curve in every regime that reads it).
 __device__ __forceinline__ double tmxy_regime(double s, double df0, double sm, double ism, double fm, double ss,
                                               double fs) {
-    double df0loc = 0.0;
-    if (gt0(sm)) df0loc = max_nn(2.0 * fm * ism, df0);
+    double df0loc = 0.0, side = 0.0;
+    if (gt0(sm)) {
+        const double c2 = 2.0 * fm * ism;
+        df0loc = max_nn(c2, df0);
+        side = gt_nn(c2, df0) ? 8.0 : 0.0;
+    }
     if (!(gt0(s) && gt0(df0loc))) return 0.0;
     if (gt_nn(s, ss)) return 1.0;
-    if (gt_nn(sm, s)) return 2.0;
+    if (gt_nn(sm, s)) return 2.0 + side;
     const double q = fm * ism;
     const double a = q * q / (df0loc * sm);
     const double sstar = sm + (fm - fs) / (a * (ss - sm));
-    if (sstar <= ss) return s <= sstar ? 3.0 : 4.0;
-    return 5.0;
+    if (sstar <= ss) return (s <= sstar ? 3.0 : 4.0) + side;
+    return 5.0 + side;
 }
 
 template <bool kSteered>

@@ -294,14 +294,17 @@ size_t window18_smem(int threads, int nclasses, bool f32) {
 
 // kF32: the TMeasy tire core in FP32 (precision LFDM_PREC_MIXED_TIRE), on FP32 copies of the
 // derived constants staged beside the FP64 ones.
-// Resident 128-thread blocks per SM the compiler budgets registers for (1: up to 255 registers, 8
-// warps per SM): the FP64 kernels are FP64-pipe bound and fastest with every register; the FP32-core
-// kernels issue mostly short-latency FP32 work and are tuned separately.
+// Resident 128-thread blocks per SM the compiler budgets registers for. 1 (up to 255 registers, 8
+// warps per SM) for the FP64 kernels, which are FP64-pipe bound and fastest with every register, and
+// for the FP32-tire-core kernels (measured: 2 and 3 blocks were 3 % and 8 % slower). 4 (128
+// registers, 16 warps per SM) for the FP32 right-hand-side kernel, whose mostly short-latency FP32
+// chains need more warps in flight: 4.50e9 against 3.58e9 vehicle-steps/s at 1 block, 3.97e9 at 5
+// and 3.88e9 at 6 (300,000 vehicles; bit-identical results).
 #ifndef LFDM_TF_MIN_BLOCKS
 #define LFDM_TF_MIN_BLOCKS 1
 #endif
 #ifndef LFDM_MIXED_MIN_BLOCKS
-#define LFDM_MIXED_MIN_BLOCKS 1
+#define LFDM_MIXED_MIN_BLOCKS 4
 #endif
 
 template <bool kNr, int kCtl, bool kOut, bool kF32>
