@@ -206,7 +206,8 @@ def test_kinematic_rows_and_errors(built_lib):
 
 def test_host_jacobian_rejects_unsupported_configurations_before_sizing(built_lib):
     """lfdm_rhs_jacobian_host checks the configuration first: the size query of the exact Jacobian on
-    an 11-DOF solver, or on an 18-DOF solver whose vehicle has throttleMod, fails like the call."""
+    a 24-DOF solver, or on an 18-DOF solver whose vehicle has throttleMod, fails like the call; on
+    an 11-DOF solver both Jacobians are sized."""
     import ctypes
 
     fleet = pkg_mod("fleet")
@@ -216,10 +217,19 @@ def test_host_jacobian_rejects_unsupported_configurations_before_sizing(built_li
     s11 = built_lib.d11SolverHalfImplicitGPU(8)
     s11.construct_class(f11["cls"][0], f11["params"])
     s11.set_states(f11["states"])
-    assert L.lfdm_rhs_jacobian_host(s11._h, 1, None, 1, None, None, ctypes.byref(ny)) == \
-        built_lib._abi.C["LFDM_ERR_ARG"]
-    assert L.lfdm_rhs_jacobian_host(s11._h, 0, None, 1, None, None, ctypes.byref(ny)) == 0 and ny.value == 13
+    for exact in (1, 0):
+        ny.value = -1
+        assert L.lfdm_rhs_jacobian_host(s11._h, exact, None, 1, None, None, ctypes.byref(ny)) == 0 and ny.value == 13
     s11.close()
+    f24 = fleet.fleet24(4, seed=2, horizon=1.0)
+    s24 = built_lib.d24SolverHalfImplicitGPU(4)
+    s24.construct_class(f24["cls"][0], f24["params"])
+    s24.set_states(f24["states"])
+    ny.value = -1
+    assert L.lfdm_rhs_jacobian_host(s24._h, 1, None, 1, None, None, ctypes.byref(ny)) == \
+        built_lib._abi.C["LFDM_ERR_ARG"]
+    assert ny.value == -1
+    s24.close()
     cls, p = fleet.suv18()
     cls.throttleMod = 1
     s18 = built_lib.d18SolverHalfImplicitGPU(4)
