@@ -47,8 +47,9 @@ typedef enum { LFDM_TIRE_TMEASY = 0, LFDM_TIRE_TMEASY_NR = 1 } lfdm_tire_type;
 
 /* Arithmetic of the stepper. FP64 reproduces the reference; MIXED (18-DOF, TMeasy) runs the RHS  */
 /* and tire math in FP32 and keeps FP64 in the X/Y/yaw accumulation and the tire slip and         */
-/* transport velocities; MIXED_TIRE (11/18/24-DOF, TMeasy) runs only the TMeasy tire core (load    */
-/* interpolation, combined slip, force curve, relaxation) in FP32 and everything else in FP64.    */
+/* transport velocities; MIXED_TIRE (11/18/24-DOF, TMeasy and TMeasyNr) runs only the tire core   */
+/* (load interpolation, combined slip, force curve, relaxation or Coulomb blend) in FP32 and       */
+/* everything else in FP64.                                                                        */
 typedef enum { LFDM_PREC_FP64 = 0, LFDM_PREC_MIXED = 1, LFDM_PREC_MIXED_TIRE = 2 } lfdm_precision;
 
 /* ------------------------------------------------------------------------------------------ */

@@ -77,7 +77,7 @@ __device__ __forceinline__ void rear_kinematics11(const Veh11& v, TireAux& ta, c
 }
 template <bool kNr, bool kSteered, bool kF32 = false>
 __device__ __forceinline__ void tire11(TireC& ts, TireAux& ta, const KView& K, double cd, double sd) {
-    if (kNr) tire_rhs_nr<kSteered>(ts, ta, K, cd, sd);  // computeTireRHS, TMeasyNr (dof11_gpu.cu:470-599)
+    if (kNr) tire_rhs_nr<kSteered, kF32>(ts, ta, K, cd, sd);  // computeTireRHS, TMeasyNr (dof11_gpu.cu:470-599)
     else tire_rhs_tm<kSteered, kF32>(ts, ta, K, cd, sd);
 }
 // computePowertrainRHS (dof11_gpu.cu:601-745) up to the wheel torques: converter, engine, gear,

@@ -799,8 +799,94 @@ __device__ __forceinline__ void tire_core_nr(TireC& ts, TireAux& ta, const KView
     ta.My = -K(K_RR) * fz * ta.rStat * tanh(omega);
 }
 
-// computeTireRHS, TMeasyNr (dof18_gpu.cu:532-662)
+// tire_core_nr with its Coulomb force, slips, curve parameters, combined force and blend in FP32 (on
+// the FP32 copies of the derived constants, precision LFDM_PREC_MIXED_TIRE). As in tire_core_tm_f32,
+// the slip velocity vsx - omega r_eff and the transport velocity r_eff |omega| + 0.01 are formed in
+// FP64 and rounded once, the steered lateral slip is held to +-1e6 and the rolling resistance stays
+// FP64.
 template <bool kSteered>
+__device__ __forceinline__ void tire_core_nr_f32(TireC& ts, TireAux& ta, const KView& K, double c_d, double s_d,
+                                                 double fz_d, double r_eff_d) {
+    const double omega = ts.omega;
+    const float vsx = (float)fma(-omega, r_eff_d, ta.vsx);
+    const float vta = (float)(r_eff_d * fabs(omega) + 0.01);
+    const float vsy = (float)ta.vsy;
+    const float mu = K.f(K_MU);
+    const float fzf = (float)fz_d;
+    // computeCombinedCoulombForce
+    float Fx0 = tanhf(-2.0f * vsx / K.f(K_VCOUL)) * fzf * mu;
+    float Fy0 = tanhf(-2.0f * vsy / K.f(K_VCOUL)) * fzf * mu;
+    {
+        const float h = sqrtf(fmaf(Fx0, Fx0, Fy0 * Fy0));
+        if (h > fzf * mu) {
+            const float r = fzf * mu / h;
+            Fx0 *= r;
+            Fy0 *= r;
+        }
+    }
+    const float sx = -vsx / vta;
+    float sy;
+    if (kSteered) {
+        const float c = (float)c_d, s = (float)s_d;
+        sy = -(vsy * c - vta * s) / (vta * c + vsy * s);
+        sy = fminf(fmaxf(sy, -1e6f), 1e6f);
+    } else {
+        sy = -vsy / vta;
+    }
+    const float fz = fminf(fzf, K.f(K_PNMAX));
+    const float fzn = fz * K.f(K_INVPN);
+    const float dfx0 = fzn * fmaf(-K.f(K_Q2DFX0), fzn, K.f(K_Q1DFX0));
+    const float dfy0 = fzn * fmaf(-K.f(K_Q2DFY0), fzn, K.f(K_Q1DFY0));
+    const float fxm = fzn * fmaf(-K.f(K_Q2FXM), fzn, K.f(K_Q1FXM));
+    const float fym = fzn * fmaf(-K.f(K_Q2FYM), fzn, K.f(K_Q1FYM));
+    const float fxs = fzn * fmaf(-K.f(K_Q2FXS), fzn, K.f(K_Q1FXS));
+    const float fys = fzn * fmaf(-K.f(K_Q2FYS), fzn, K.f(K_Q1FYS));
+    const float fzn1 = fzn - 1.0f;
+    const float sxm = fmaf(K.f(K_DSXM), fzn1, K.f(K_LSXM));
+    const float sym = fmaf(K.f(K_DSYM), fzn1, K.f(K_LSYM));
+    const float sxs = fmaf(K.f(K_DSXS), fzn1, K.f(K_LSXS));
+    const float sys = fmaf(K.f(K_DSYS), fzn1, K.f(K_LSYS));
+    const float frblend = sine_stepf(fabsf((float)ta.vsx), K.f(K_FRB0), 0.f, K.f(K_FRB1), 1.f);
+    const float q = fmaf(sx, sx, sy * sy);
+    float sc, calpha, salpha, isc = 0.f;
+    if (q > 0.f) {
+        isc = rsqrtf(q);
+        sc = q * isc;
+        calpha = sx * isc;
+        salpha = sy * isc;
+    } else {
+        sc = 0.f;
+        calpha = 0.70710678f;
+        salpha = 0.70710678f;
+    }
+    auto hyp = [](float a, float b) { return sqrtf(fmaf(a, a, b * b)); };
+    const float df0 = hyp(dfx0 * calpha, dfy0 * salpha);
+    const float fm = mu * hyp(fxm * calpha, fym * salpha);
+    const float sm = mu * hyp(sxm * calpha, sym * salpha);
+    const float fs = mu * hyp(fxs * calpha, fys * salpha);
+    const float ss = mu * hyp(sxs * calpha, sys * salpha);
+    float f, fos;
+    tmxyf(f, fos, sc, df0, sm, fm, ss, fs);
+    float Fx = 0.f, Fy = 0.f;
+    if (sc > 0.f) {
+        Fx = f * sx * isc;
+        Fy = f * sy * isc;
+    }
+    ta.fx = fmaf(1.0f - frblend, Fx0, frblend * Fx);
+    ta.fy = fmaf(1.0f - frblend, Fy0, frblend * Fy);
+    ta.My = -K(K_RR) * fmin(fz_d, K(K_PNMAX)) * ta.rStat * tanh(omega);
+}
+
+// The TMeasyNr tire core in the arithmetic a kernel runs: FP64 (tire_core_nr) or FP32 (kF32).
+template <bool kSteered, bool kF32>
+__device__ __forceinline__ void tire_core_nr_p(TireC& ts, TireAux& ta, const KView& K, double c, double s, double fz,
+                                               double r_eff) {
+    if constexpr (kF32) tire_core_nr_f32<kSteered>(ts, ta, K, c, s, fz, r_eff);
+    else tire_core_nr<kSteered>(ts, ta, K, c, s, fz, r_eff);
+}
+
+// computeTireRHS, TMeasyNr (dof18_gpu.cu:532-662)
+template <bool kSteered, bool kF32 = false>
 __device__ __forceinline__ void tire_rhs_nr(TireC& ts, TireAux& ta, const KView& K, double c, double s) {
     const double fz = ta.fz;
     if (!gt0(fz)) {
@@ -821,7 +907,7 @@ __device__ __forceinline__ void tire_rhs_nr(TireC& ts, TireAux& ta, const KView&
     } else {
         r_eff = fma(K(K_RDCRIT), ta.xt, ta.rStat);
     }
-    tire_core_nr<kSteered>(ts, ta, K, c, s, fz, r_eff);
+    tire_core_nr_p<kSteered, kF32>(ts, ta, K, c, s, fz, r_eff);
 }
 
 // differentialSplit (dof18_gpu.cu:42-69) with max_bias = 2.
@@ -963,10 +1049,10 @@ __device__ __forceinline__ void rhs18(VehC& v, VehAux& va, TireC* ts, TireAux* t
         ta[3].vsx = v.u + wcr;
     }
     if (kNr) {
-        tire_rhs_nr<true>(ts[0], ta[0], K, cd, sd);
-        tire_rhs_nr<true>(ts[1], ta[1], K, cd, sd);
-        tire_rhs_nr<false>(ts[2], ta[2], K, 1.0, 0.0);
-        tire_rhs_nr<false>(ts[3], ta[3], K, 1.0, 0.0);
+        tire_rhs_nr<true, kF32>(ts[0], ta[0], K, cd, sd);
+        tire_rhs_nr<true, kF32>(ts[1], ta[1], K, cd, sd);
+        tire_rhs_nr<false, kF32>(ts[2], ta[2], K, 1.0, 0.0);
+        tire_rhs_nr<false, kF32>(ts[3], ta[3], K, 1.0, 0.0);
     } else {
         tire_rhs_tm<true, kF32>(ts[0], ta[0], K, cd, sd);
         tire_rhs_tm<true, kF32>(ts[1], ta[1], K, cd, sd);

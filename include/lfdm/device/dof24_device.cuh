@@ -157,8 +157,8 @@ __device__ __forceinline__ void rhs24(VehC& v, Veh24X& vx, VehAux& va, TireC* ts
                 !gt_nn(fz, K(K_FZRD)) ? fma(K(K_DRD), fma(fz, K(K_INVPN), -1.0), K(K_RDPN)) : K(K_RDCRIT);
             const double r_eff = fma(rdynco, r0 - rs, rs);
             if (kNr) {  // computeTireRHS, TMeasyNr (24dof-gpu/dof24_gpu.cu:990-1119)
-                if (c < 2) tire_core_nr<true>(ts[c], ta[c], K, cd, sd, fz, r_eff);
-                else tire_core_nr<false>(ts[c], ta[c], K, 1.0, 0.0, fz, r_eff);
+                if (c < 2) tire_core_nr_p<true, kF32>(ts[c], ta[c], K, cd, sd, fz, r_eff);
+                else tire_core_nr_p<false, kF32>(ts[c], ta[c], K, 1.0, 0.0, fz, r_eff);
             } else {
                 if (c < 2) tire_core_tm_p<true, kF32>(ts[c], ta[c], K, cd, sd, fz, r_eff);
                 else tire_core_tm_p<false, kF32>(ts[c], ta[c], K, 1.0, 0.0, fz, r_eff);

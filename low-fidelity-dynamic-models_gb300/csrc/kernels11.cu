@@ -319,8 +319,9 @@ cudaError_t launch_window11(const Window18& w, cudaStream_t stream) {
     if (w.n <= 0 || w.nsteps <= 0) return cudaSuccess;
     if (w.threads <= 0 || w.threads > 128 || (w.threads & 31)) return cudaErrorInvalidValue;
     if (w.precision == LFDM_PREC_MIXED_TIRE) {
-        if (w.tire_nr) return cudaErrorInvalidValue;
-        return use_split11(w) ? launch11_split_c<false, true>(w, stream) : launch11_c<false, true>(w, stream);
+        if (use_split11(w))
+            return w.tire_nr ? launch11_split_c<true, true>(w, stream) : launch11_split_c<false, true>(w, stream);
+        return w.tire_nr ? launch11_c<true, true>(w, stream) : launch11_c<false, true>(w, stream);
     }
     if (w.precision != LFDM_PREC_FP64) return cudaErrorInvalidValue;
     if (use_split11(w)) return w.tire_nr ? launch11_split_c<true>(w, stream) : launch11_split_c<false>(w, stream);

@@ -690,10 +690,8 @@ cudaError_t launch_window18(const Window18& w, cudaStream_t stream) {
         if (w.tire_nr || !w.classes_f) return cudaErrorInvalidValue;
         return launch_mixed(w, stream);
     }
-    if (w.precision == LFDM_PREC_MIXED_TIRE) {
-        if (w.tire_nr) return cudaErrorInvalidValue;
-        return launch_c<false, true>(w, stream);
-    }
+    if (w.precision == LFDM_PREC_MIXED_TIRE)
+        return w.tire_nr ? launch_c<true, true>(w, stream) : launch_c<false, true>(w, stream);
     if (w.precision != LFDM_PREC_FP64) return cudaErrorInvalidValue;
     return w.tire_nr ? launch_c<true>(w, stream) : launch_c<false>(w, stream);
 }

@@ -51,7 +51,8 @@ size_t window24_smem(int threads, int nclasses, bool f32) {
 cudaError_t launch_window24(const Window18& w, cudaStream_t stream) {
     if (w.n <= 0 || w.nsteps <= 0) return cudaSuccess;
     if (w.threads <= 0 || w.threads > 128 || (w.threads & 31)) return cudaErrorInvalidValue;
-    if (w.precision == LFDM_PREC_MIXED_TIRE) return w.tire_nr ? cudaErrorInvalidValue : launch_window24_f32(w, stream);
+    if (w.precision == LFDM_PREC_MIXED_TIRE)
+        return w.tire_nr ? launch_window24_nr_f32(w, stream) : launch_window24_f32(w, stream);
     if (w.precision != LFDM_PREC_FP64) return cudaErrorInvalidValue;
     return w.tire_nr ? launch_window24_nr(w, stream) : launch24_tire<false>(w, stream);
 }

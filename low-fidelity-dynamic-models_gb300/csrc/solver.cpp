@@ -384,8 +384,8 @@ int run_windows(lfdm_solver* h, double t0, double t_end, bool solve_all, int ctl
     w.K = h->d_K.p;
     w.classes = reinterpret_cast<const ClassDev18*>(h->d_classes.p);
     w.classes_f = reinterpret_cast<const ClassDev18F*>(h->d_classes_f.p);
-    if (h->precision != LFDM_PREC_FP64 && w.tire_nr)
-        return h->fail(LFDM_ERR_ARG, "the mixed-precision steppers support TMeasy tires only");
+    if (h->precision == LFDM_PREC_MIXED && w.tire_nr)
+        return h->fail(LFDM_ERR_ARG, "the FP32 right-hand-side stepper supports TMeasy tires only");
     w.nclasses = (int)h->classes.size();
     w.class_of = h->d_class_of.p;
     w.S = h->d_S.p;

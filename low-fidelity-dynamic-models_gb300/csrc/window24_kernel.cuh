@@ -1,6 +1,6 @@
 // The 24-DOF window kernel and its launch templates, instantiated for TMeasy tires in kernels24.cu,
-// for TMeasyNr tires in kernels24nr.cu and for TMeasy tires with the FP32 tire core in
-// kernels24tf.cu (three translation units that compile in parallel).
+// for TMeasyNr tires in kernels24nr.cu, and for either tire with the FP32 tire core in kernels24tf.cu
+// and kernels24nrtf.cu (four translation units that compile in parallel).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -14,6 +14,7 @@ namespace lfdm {
 size_t window24_smem(int threads, int nclasses, bool f32);
 cudaError_t launch_window24_nr(const Window18& w, cudaStream_t stream);
 cudaError_t launch_window24_f32(const Window18& w, cudaStream_t stream);
+cudaError_t launch_window24_nr_f32(const Window18& w, cudaStream_t stream);
 
 // kF32: the TMeasy tire core in FP32 (precision LFDM_PREC_MIXED_TIRE), on FP32 copies of the
 // derived constants staged beside the FP64 ones.

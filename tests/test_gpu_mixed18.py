@@ -162,26 +162,51 @@ def test_fp32_probe_rate(built_lib):
     assert 0.5 < g32 < 3.0
 
 
-@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("model", [18, 11, 24])
-def test_mixed_rejects_tmeasy_nr(built_lib, prec, model):
+def test_mixed_rejects_tmeasy_nr(built_lib, model):
+    """The FP32 right-hand-side form is built for the 18-DOF model with TMeasy tires only."""
     lfdm = built_lib
-    if prec == 1 and model != 18:
+    if model != 18:
         s = _solver(lfdm, model, 2)
         with pytest.raises(lfdm.LfdmError):
-            s.set_precision(prec)
+            s.set_precision(1)
         s.close()
         return
     fleet = pkg_mod("fleet")
-    cls, p = {18: fleet.suv18, 11: fleet.suv11, 24: fleet.suv24}[model]()
-    count = {18: lfdm.S_COUNT, 11: pkg_mod("_abi").S11_COUNT, 24: lfdm.S24_COUNT}[model]
+    cls, p = fleet.suv18()
     s = _solver(lfdm, model, 2)
     s.construct_class(cls, np.repeat(p[None], 2, 0), tire_type=1)
-    s.set_states(np.zeros((2, count)))
+    s.set_states(np.zeros((2, lfdm.S_COUNT)))
     s.set_driver_tables(np.array([[0.0, 0, 0, 0], [1.0, 0, 0, 0]]))
     s.SetEndTime(0.1)
     s.SetKernelSimTime(0.1)
-    s.set_precision(prec)
+    s.set_precision(1)
     with pytest.raises(lfdm.LfdmError):
         s.Solve()
     s.close()
+
+
+@pytest.mark.parametrize("model,case", [(18, "sedan_rwd_nr_acc05_gpu"), (11, "sedan11_rwd_nr_acc05_gpu"),
+                                        (24, "sedan24_rwd_nr_acc05_gpu"), (18, "sedan_tmod_nls_nr_dl4_gpu")])
+def test_mixed_tire_with_tmeasy_nr(built_lib, golden18, golden11_cases, golden24_cases, model, case):
+    """The FP32 tire core with TMeasyNr tires (Coulomb force, slips, curve, blend in FP32) on the
+    Sedan TMeasyNr fixtures (trajectories insensitive to rounding): the end position within 1 cm of
+    the reference's FP64 result."""
+    from conftest import case_inputs11, case_inputs24
+    golden = {18: golden18, 11: golden11_cases, 24: golden24_cases}[model]
+    inputs = {18: case_inputs, 11: case_inputs11, 24: case_inputs24}[model]
+    c = {x["name"]: x for x in golden["cases"]}[case]
+    cls, p, st, tab = inputs(c)
+    sol = _solver(built_lib, model, 1)
+    sol.construct_class(cls, p[None], 1)
+    sol.set_driver_tables(tab[None])
+    sol.set_states(st[None])
+    sol.SetKernelSimTime(c["ksim"])
+    sol.SetEndTime(c["tend"])
+    sol.set_precision(2)
+    sol.Solve()
+    got = sol.get_states()
+    sol.close()
+    e = _pos_err(got, np.array(c["expected_final"])[None], model)[0]
+    print(f"{case}: FP32 Nr tire core end-position error {e:.2e} m")
+    assert e <= 0.01
