@@ -382,6 +382,7 @@ def _fleet_bench(lfdm, fleet, dev, n: int, torch) -> dict:
     for g in mf["groups"]:
         f.add(g["model"], g["cls"], g["params"], g["states"], g["horizons"], None, base + g["row_off"], g["row_len"])
     f.set_launch(threads, bps, spl)
+    f.set_affinity(tuned_aff)
     f.solve()
     ms_noout, _ = f.last_ms()
     f.close()
@@ -391,6 +392,7 @@ def _fleet_bench(lfdm, fleet, dev, n: int, torch) -> dict:
     for g in mf["groups"]:
         f.add(g["model"], g["cls"], g["params"], g["states"], g["horizons"], None, base + g["row_off"], g["row_len"])
     f.set_launch(threads, bps, spl)
+    f.set_affinity(tuned_aff)
     f.set_precision(2)
     f.solve()
     ms_tf, _ = f.last_ms()
