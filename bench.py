@@ -39,16 +39,16 @@ W_ALG = {11: 675, 18: 1391, 24: 1941}  # the same count for the three models
 # (sm__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on.sum), and everything the FP64 pipe
 # issued in lanes (sm__inst_executed_pipe_fp64.sum x 32: also compares, min/max and conversions, and
 # the inactive lanes of divergent warps, which occupy the pipe alike)
-FP64_INST_PER_VSTEP_18 = 1046
-FP64_PIPE_PER_VSTEP_18 = 1402
+FP64_INST_PER_VSTEP_18 = 1113
+FP64_PIPE_PER_VSTEP_18 = 1320
 # The mixed-precision forms of the 18-DOF stepper: (precision enum, key, arithmetic)
 MIXED_FORMS = ((1, "mixed", "f32 RHS and tire math; f64 states, X/Y/yaw accumulation, slip and transport velocities"),
                (2, "mixed_tire", "f32 TMeasy tire core; f64 everything else"))
 # Lane instructions per vehicle-step the two pipes of the mixed window kernels issue, (FMA pipe,
 # FP64 pipe): ncu sm__inst_executed_pipe_fma.sum and sm__inst_executed_pipe_fp64.sum x 32 of one
 # window launch on 32,768 vehicles of the seeded fleet (the fourth 1 s window), per vehicle-step.
-# Of the FP64 pipe's 83 (MIXED) and 384 (MIXED_TIRE), 52 are float/double conversions.
-MIXED_INST_PER_VSTEP = {1: (1187, 83), 2: (1002, 384)}
+# Of the FP64 pipe's 101 (MIXED) and 384 (MIXED_TIRE), 69 and 52 are float/double conversions.
+MIXED_INST_PER_VSTEP = {1: (1320, 101), 2: (1005, 384)}
 METRIC = "18-DOF vehicle-steps/s on 1 GB300: FP64 plain vs mixed at stated error; adjoint/fwd"
 
 
