@@ -471,6 +471,14 @@ class d24SolverHalfImplicitGPU(_SolverGPU):
     STATE_COUNT = S24_COUNT
     RESP_CHANNELS = RESP24
 
+    def rhs_jacobian(self, steering, throttle, braking=0.0, reference_point: bool = True):
+        """Exact Jacobians of the 24-DOF right-hand side (TMeasy tires) at every vehicle's current
+        state (lfdm_rhs_jacobian_exact; the reference CPU solver's GetJacobianState /
+        GetJacobianControls by central differences, 24dof/dof24_halfImplicit.cpp:402-494). Returns
+        (jac_state [N, ny, ny], jac_controls [N, ny, 2]) in the reference's packed order: ny = 36 with
+        a torque converter and 35 without."""
+        return self._jacobian(self._L.lfdm_rhs_jacobian_exact, steering, throttle, braking, reference_point)
+
     def Construct(self, vehicle_params_file: str, tire_params_file: str, sus_params_file: str,  # noqa: N802
                   num_vehicles: int, driver_inputs_file: str | None = None, type: int = TireType.TMeasy):  # noqa: A002
         self._ck(self._L.lfdm_construct(self._h, vehicle_params_file.encode(), tire_params_file.encode(),

@@ -211,6 +211,10 @@ __device__ __forceinline__ double tmxy_regime(double s, double df0, double sm, d
 }
 
 template <bool kSteered>
+__device__ __forceinline__ void tire_fwd_tape_core(TireC& ts, TireAux& ta, const TapeRef& T, const KView& K, double c,
+                                                   double s, double fz, double r_eff);
+
+template <bool kSteered>
 __device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, const TapeRef& T, const KView& K, double c, double s) {
     const double fz = ta.fz;
     T.at(TT_(fz)) = fz;
@@ -244,6 +248,15 @@ __device__ __forceinline__ void tire_fwd_tape(TireC& ts, TireAux& ta, const Tape
         T.at(TT_(rdynco)) = K(K_RDCRIT);
     }
     const double r_eff = fma(T.at(TT_(rdynco)), ta.xt, ta.rStat);
+    tire_fwd_tape_core<kSteered>(ts, ta, T, K, c, s, fz, r_eff);
+}
+
+// The part of tire_fwd_tape that follows the load and the radii (tire_core_tm's arithmetic): the
+// caller has set ta.vsx, ta.vsy, ta.rStat, the tape's fz, om, xe, ye, vsy and on fields, and
+// passes the load fz > 0 and the effective radius r_eff.
+template <bool kSteered>
+__device__ __forceinline__ void tire_fwd_tape_core(TireC& ts, TireAux& ta, const TapeRef& T, const KView& K, double c,
+                                                   double s, double fz, double r_eff) {
     T.at(TT_(r_eff)) = r_eff;
     const double omega = ts.omega;
     const double vsy = ta.vsy;
@@ -872,11 +885,14 @@ __device__ __forceinline__ void tmxy_rev(double s, double df0, double sm, double
 // Tire adjoint (on-ground tire): from the adjoints of the core outputs (xedot, yedot, fx, fy, My as
 // the tire model returns them, before any frame rotation) and of rStat, to those of the inputs
 // (xe, ye, omega, vsx before the slip correction, vsy, fz, cos/sin of the wheel angle).
+// tire_rev_core is the part that ends at the effective radius: its adjoint is returned in reffb,
+// the load's (through the curve parameters) is added to fzb and rStatb is taken as it comes (the
+// rolling resistance adds to it inside); the caller maps r_eff and rStat to its own states.
 template <bool kSteered>
-__device__ __forceinline__ void tire_rev(const TapeRef& T, const KView& K, const KBar& kb, double xedotb,
-                                         double yedotb, double fxb, double fyb, double Myb, double rStatb, double& xeb,
-                                         double& yeb, double& omb, double& vsxinb, double& vsyb, double& fzb,
-                                         double& cb, double& sb_, double c, double s) {
+__device__ __forceinline__ void tire_rev_core(const TapeRef& T, const KView& K, const KBar& kb, double xedotb,
+                                              double yedotb, double fxb, double fyb, double Myb, double& rStatb,
+                                              double& xeb, double& yeb, double& omb, double& vsxinb, double& vsyb,
+                                              double& fzb, double& reffb, double& cb, double& sb_, double c, double s) {
     const double cx = K(K_CX), cy = K(K_CY), dx = K(K_DX), dy = K(K_DY);
     double vsxb = 0, syb = 0, vtab = 0, fosb = 0, rwb = 0, hsxnb = 0, hsynb = 0, fzcb = 0, sxb = 0;
     // blend of structural and dynamic forces
@@ -1041,11 +1057,21 @@ __device__ __forceinline__ void tire_rev(const TapeRef& T, const KView& K, const
         vtab = fma(T.at(TT_(vsy)) * ivta * ivta, syb, vtab);
     }
     rwb += vtab;
-    double reffb = fabs(T.at(TT_(om))) * rwb;
+    reffb = fabs(T.at(TT_(om))) * rwb;
     omb = fma(T.at(TT_(r_eff)) * T.at(TT_(sgn)), rwb, omb);
     vsxinb += vsxb;
     omb = fma(-T.at(TT_(r_eff)), vsxb, omb);
     reffb = fma(-T.at(TT_(om)), vsxb, reffb);
+}
+
+template <bool kSteered>
+__device__ __forceinline__ void tire_rev(const TapeRef& T, const KView& K, const KBar& kb, double xedotb,
+                                         double yedotb, double fxb, double fyb, double Myb, double rStatb, double& xeb,
+                                         double& yeb, double& omb, double& vsxinb, double& vsyb, double& fzb,
+                                         double& cb, double& sb_, double c, double s) {
+    double reffb = 0.0;
+    tire_rev_core<kSteered>(T, K, kb, xedotb, yedotb, fxb, fyb, Myb, rStatb, xeb, yeb, omb, vsxinb, vsyb, fzb, reffb,
+                            cb, sb_, c, s);
     // r_eff = rdynco xt + rStat, rStat = r0 - xt, xt = fz / kt
     double xtb = T.at(TT_(rdynco)) * reffb;
     rStatb += reffb;

@@ -1,4 +1,5 @@
-// Batched exact Jacobians of the 18- and 11-DOF right-hand sides (jacobian18.cu, jacobian11.cu).
+// Batched exact Jacobians of the 18-, 11- and 24-DOF right-hand sides (jacobian18.cu, jacobian11.cu,
+// jacobian24.cu).
 #pragma once
 
 #include <cstddef>
@@ -29,6 +30,10 @@ struct JacLaunch {
 cudaError_t launch_rhs_jacobian18(const JacLaunch& A, cudaStream_t stream);
 // The same for the 11-DOF model (jacobian11.cu); S holds [LFDM11_S_COUNT][npad] states.
 cudaError_t launch_rhs_jacobian11(const JacLaunch& A, cudaStream_t stream);
+// The same for the 24-DOF model with TMeasy tires (jacobian24.cu); S holds [LFDM24_S_COUNT][npad]
+// states and the tape needs jac24_tape_doubles() doubles per vehicle.
+cudaError_t launch_rhs_jacobian24(const JacLaunch& A, cudaStream_t stream);
+size_t jac24_tape_doubles();
 // Dynamic shared memory of a Jacobian block (derived constants, their adjoint scratch and, when
 // they fit, the class tables; *cls_smem says whether they do).
 size_t jac18_smem(int threads, int nclasses, bool* cls_smem);

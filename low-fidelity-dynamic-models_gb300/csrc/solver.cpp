@@ -1043,11 +1043,12 @@ int lfdm_traj18_backward(lfdm_solver* h, const double* ctl, const double* ref, u
     return LFDM_OK;
 }
 
-// The solver configurations a right-hand-side Jacobian can be formed for (exact: the 11- and 18-DOF
-// models without throttleMod; either: FP64, all vehicles with or without a torque converter).
+// The solver configurations a right-hand-side Jacobian can be formed for (exact: every model without
+// throttleMod, the 24-DOF model with TMeasy tires; either: FP64, all vehicles with or without a
+// torque converter).
 static int jacobian_supported(lfdm_solver* h, bool exact) {
-    if (exact && h->model == LFDM_MODEL_24)
-        return h->fail(LFDM_ERR_ARG, "the exact right-hand-side Jacobian is built for the 11- and 18-DOF models");
+    if (exact && h->model == LFDM_MODEL_24 && h->tire_type == LFDM_TIRE_TMEASY_NR)
+        return h->fail(LFDM_ERR_ARG, "the exact 24-DOF right-hand-side Jacobian is built for TMeasy tires");
     if (h->precision != LFDM_PREC_FP64) return h->fail(LFDM_ERR_ARG, "the right-hand-side Jacobian is FP64");
     if (h->classes.empty()) return h->fail(LFDM_ERR_STATE, "no vehicles constructed");
     const int tc = h->classes[0].tcbool != 0;
@@ -1077,7 +1078,7 @@ int lfdm_rhs_jacobian_exact(lfdm_solver* h, const double* ctl, int reference_poi
     if (rc) return rc;
     rc = sync_device(h);
     if (rc) return rc;
-    CK(h->d_adj_tape.ensure(traj18_tape_doubles_per_step() * h->npad));
+    CK(h->d_adj_tape.ensure(std::max(traj18_tape_doubles_per_step(), jac24_tape_doubles()) * h->npad));
     JacLaunch A;
     A.n = (int)h->N;
     A.npad = h->npad;
@@ -1092,7 +1093,9 @@ int lfdm_rhs_jacobian_exact(lfdm_solver* h, const double* ctl, int reference_poi
     A.tape = h->d_adj_tape.p;
     A.jac_state = jac_state;
     A.jac_ctl = jac_ctl;
-    CK(h->model == LFDM_MODEL_11 ? launch_rhs_jacobian11(A, h->stream) : launch_rhs_jacobian18(A, h->stream));
+    CK(h->model == LFDM_MODEL_11   ? launch_rhs_jacobian11(A, h->stream)
+       : h->model == LFDM_MODEL_24 ? launch_rhs_jacobian24(A, h->stream)
+                                   : launch_rhs_jacobian18(A, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     if (ny) *ny = jac_fd_ny((int)h->model, A.tire_nr != 0, tc != 0);
     return LFDM_OK;

@@ -166,13 +166,3 @@ def test_jacobian11_exact_against_the_difference_scheme_and_host_form(built_lib)
     sol.close()
     assert rc == 0 and got.value == ny
     assert np.array_equal(hs, js) and np.array_equal(hu, ju)
-
-
-def test_exact_jacobian_rejects_24dof(built_lib):
-    cls, p = pkg_mod("fleet").suv24()
-    sol = built_lib.d24SolverHalfImplicitGPU(1)
-    sol.construct_class(cls, p[None])
-    sol.set_states(np.zeros((1, built_lib.S24_COUNT)))
-    with pytest.raises(built_lib.LfdmError):
-        sol._jacobian(sol._L.lfdm_rhs_jacobian_exact, [0.0], [0.0], 0.0, True)
-    sol.close()

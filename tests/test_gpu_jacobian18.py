@@ -206,8 +206,8 @@ def test_kinematic_rows_and_errors(built_lib):
 
 def test_host_jacobian_rejects_unsupported_configurations_before_sizing(built_lib):
     """lfdm_rhs_jacobian_host checks the configuration first: the size query of the exact Jacobian on
-    a 24-DOF solver, or on an 18-DOF solver whose vehicle has throttleMod, fails like the call; on
-    an 11-DOF solver both Jacobians are sized."""
+    a 24-DOF solver with TMeasyNr tires, or on an 18-DOF solver whose vehicle has throttleMod, fails
+    like the call; on 11-DOF and 24-DOF TMeasy solvers both Jacobians are sized."""
     import ctypes
 
     fleet = pkg_mod("fleet")
@@ -222,14 +222,14 @@ def test_host_jacobian_rejects_unsupported_configurations_before_sizing(built_li
         assert L.lfdm_rhs_jacobian_host(s11._h, exact, None, 1, None, None, ctypes.byref(ny)) == 0 and ny.value == 13
     s11.close()
     f24 = fleet.fleet24(4, seed=2, horizon=1.0)
-    s24 = built_lib.d24SolverHalfImplicitGPU(4)
-    s24.construct_class(f24["cls"][0], f24["params"])
-    s24.set_states(f24["states"])
-    ny.value = -1
-    assert L.lfdm_rhs_jacobian_host(s24._h, 1, None, 1, None, None, ctypes.byref(ny)) == \
-        built_lib._abi.C["LFDM_ERR_ARG"]
-    assert ny.value == -1
-    s24.close()
+    for tire, want in ((0, 0), (1, built_lib._abi.C["LFDM_ERR_ARG"])):
+        s24 = built_lib.d24SolverHalfImplicitGPU(4)
+        s24.construct_class(f24["cls"][0], f24["params"], tire)
+        s24.set_states(f24["states"])
+        ny.value = -1
+        assert L.lfdm_rhs_jacobian_host(s24._h, 1, None, 1, None, None, ctypes.byref(ny)) == want
+        assert ny.value == (36 if want == 0 else -1)
+        s24.close()
     cls, p = fleet.suv18()
     cls.throttleMod = 1
     s18 = built_lib.d18SolverHalfImplicitGPU(4)
