@@ -502,8 +502,8 @@ def _adjoint_bench(lfdm, fleet, dev, n: int, nsteps: int, torch) -> dict:
 def _jacobian_bench(lfdm, fleet, dev, n: int, cpu_sample: int, torch) -> dict:
     """Right-hand-side Jacobians of every vehicle of the seeded 11/18/24-DOF SUV fleets after 1 s of
     their drivers (TMeasy, torque converter): the reference's difference scheme
-    (lfdm_rhs_jacobian_fd; 2 ny + 4 right-hand sides per vehicle) and, for the 11- and 18-DOF
-    models, the exact Jacobian (lfdm_rhs_jacobian_exact). Each figure is the host wall time of the C-ABI call (it
+    (lfdm_rhs_jacobian_fd; 2 ny + 4 right-hand sides per vehicle) and the exact Jacobian
+    (lfdm_rhs_jacobian_exact). Each figure is the host wall time of the C-ABI call (it
     returns after its stream synchronizes), best of 3 after one untimed call. Beside them, the same
     scheme on all host cores over the same vehicles: the oracle's restatement of
     IntegrateStepWithJacobian's Jacobian block, pinned bit for bit to the reference's CPU solvers."""
@@ -531,7 +531,7 @@ def _jacobian_bench(lfdm, fleet, dev, n: int, cpu_sample: int, torch) -> dict:
         js = torch.empty(36 * 36 * n, dtype=torch.float64, device=gdev)
         ju = torch.empty(36 * 2 * n, dtype=torch.float64, device=gdev)
         ny = ctypes.c_int()
-        fns = [("fd", sol._L.lfdm_rhs_jacobian_fd)] + ([("exact", sol._L.lfdm_rhs_jacobian_exact)] if model != 24 else [])
+        fns = [("fd", sol._L.lfdm_rhs_jacobian_fd), ("exact", sol._L.lfdm_rhs_jacobian_exact)]
         for name, fn in fns:
             def call():
                 t0 = time.perf_counter()

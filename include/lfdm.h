@@ -333,10 +333,10 @@ int lfdm_traj18_branch_signature(lfdm_solver* h, const double* ctl, unsigned nst
 int lfdm_rhs_jacobian18(lfdm_solver* h, const double* ctl, int reference_point, double* jac_state, double* jac_ctl,
                         int* ny);
 
-/* Exact Jacobians of the 11-DOF right-hand side as well (replaces the Jacobian block of            */
-/* 11dof/dof11_halfImplicit.cpp:335-429): the same call for an 11- or 18-DOF solver, each in its     */
-/* model's packed order; 11-DOF y = {xe, ye} front, rear (TMeasy only), omega front, rear, crank     */
-/* speed (torque converter only), x, y, u, v, psi, wz: ny = 13 / 12 (TMeasy), 9 / 8 (TMeasyNr).       */
+/* Exact Jacobians of every model (replaces the Jacobian blocks of 11dof/dof11_halfImplicit.cpp:     */
+/* 335-429 and 24dof/dof24_halfImplicit.cpp:402-494 as well): the same call for an 11-, 18- or      */
+/* 24-DOF solver, each in its model's packed order (the difference scheme's, below); 11-DOF ny = 13 */
+/* / 12 (TMeasy), 9 / 8 (TMeasyNr); 24-DOF TMeasy tires only, ny = 36 / 35.                         */
 int lfdm_rhs_jacobian_exact(lfdm_solver* h, const double* ctl, int reference_point, double* jac_state,
                             double* jac_ctl, int* ny);
 

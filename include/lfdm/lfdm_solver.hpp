@@ -190,7 +190,7 @@ class SolverBase {
     // Extension: right-hand-side Jacobians of every vehicle at its current state, each as the
     // reference's CPU solver returns one (GetJacobianState / GetJacobianControls after
     // IntegrateStepWithJacobian): jac_state[i] is vehicle i's ny x ny matrix, jac_controls[i] its ny x 2
-    // one, in the packed order. exact: the exact Jacobian (11- and 18-DOF models) instead of the reference's
+    // one, in the packed order. exact: the exact Jacobian (24-DOF: TMeasy tires) instead of the reference's
     // central differences; reference_point: the packed states in a fresh state, as PerturbRhsFun.
     // Controls hold one value per vehicle. Returns ny (0 on error).
     int GetRhsJacobians(const std::vector<double>& steering, const std::vector<double>& throttle,
