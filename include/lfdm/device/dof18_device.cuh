@@ -350,6 +350,22 @@ struct KView {
     __device__ __forceinline__ float f(int i) const { return fbase[i * stride]; }
 };
 
+// The joint of tmxy_combined's two parabolas: a = (fm / sm)^2 / (df0loc sm) and
+// sstar = sm + (fm - fs) / (a (ss - sm)) (dof18_gpu.cu:262-266), from one reciprocal instead of two
+// divisions: with D = df0loc sm and E = (fm / sm)^2 (ss - sm), R = 1 / (D E) gives 1 / D = E R and
+// (fm - fs) / (a (ss - sm)) = (fm - fs) D / E = (fm - fs) D (D R). Both round within a few ulps of
+// the two quotients; the regime this selects is recorded for the adjoint from the same values.
+__device__ __forceinline__ void tmxy_knee(double fm, double ism, double df0loc, double sm, double ss, double fs,
+                                          double& a, double& sstar) {
+    const double q = fm * ism;
+    const double q2 = q * q;
+    const double D = df0loc * sm;
+    const double E = q2 * (ss - sm);
+    const double R = 1.0 / (D * E);
+    a = q2 * (E * R);
+    sstar = fma(fm - fs, D * (D * R), sm);
+}
+
 // tmxy_combined (dof18_gpu.cu:243-285) given the reciprocals of s, sm and fm (is, ism, ifm; the
 // TMeasy tire has them from the rsqrt of the squared norms it takes anyway). Returns the ratio of
 // the combined force to the combined slip, fos = f / s, as a fraction fn / fd: in the adhesion
@@ -370,9 +386,8 @@ __device__ __forceinline__ void tmxy_frac(double& fn, double& fd, double s, doub
             fd = fma(sn + p, sn, 1.0);
             fn = df0loc;
         } else {
-            const double q = fm * ism;
-            const double a = q * q / (df0loc * sm);
-            const double sstar = sm + (fm - fs) / (a * (ss - sm));
+            double a, sstar;
+            tmxy_knee(fm, ism, df0loc, sm, ss, fs, a, sstar);
             double f;
             if (sstar <= ss) {
                 if (s <= sstar) {

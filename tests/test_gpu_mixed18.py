@@ -71,6 +71,17 @@ def test_mixed_on_reference_fixtures(built_lib, golden18, prec):
         assert abs(m[0, 2] - e[2]) <= 1e-4, c["name"]
 
 
+def _within_floor(noise, gap, n):
+    """The least fraction of n vehicles within 1 cm of FP64 a form may reach: the reference build's
+    noise floor less the form's allowed gap, less two binomial standard deviations of the fraction
+    at n vehicles. On a rounding-chaotic fleet each vehicle's end point flips in or out of 1 cm
+    under an ulp-level change of either run (a change of FP64 rounding in one tire-curve regime
+    moved the 24-DOF fraction by 0.003 at 2,048 vehicles with the FP32 code untouched), so the
+    fraction carries that sampling noise."""
+    p = min(max(noise - gap, 0.0), 1.0)
+    return noise - gap - 2.0 * np.sqrt(p * (1.0 - p) / n)
+
+
 def _noise_within(model, f, horizon, tol=0.01):
     args = (f["cls"], f["class_of"], f["params"], f["states"], f["tables"])
     ref, _ = O.run18(*args, tend=horizon, ksim=1.0, nthreads=NT, model=model)
@@ -82,7 +93,8 @@ def _noise_within(model, f, horizon, tol=0.01):
 def test_mixed_error_distribution_on_seeded_fleet(built_lib, prec):
     """The rounding-chaotic SUV fleet (10 s): median end-position error within 1 cm, and the
     fraction of vehicles within 1 cm no more than 0.15 (MIXED) or 0.08 (MIXED_TIRE) below that of
-    the reference's own FMA-contracted FP64 build (its rounding-noise floor)."""
+    the reference's own FMA-contracted FP64 build (its rounding-noise floor), to the fraction's
+    sampling noise at 2,048 vehicles."""
     fleet = pkg_mod("fleet")
     n, H = 2048, 10.0
     f = fleet.fleet18(n, seed=5, horizon=H)
@@ -93,7 +105,7 @@ def test_mixed_error_distribution_on_seeded_fleet(built_lib, prec):
     print(f"prec {prec} vs fp64: p50 {np.median(e_mix):.2e} m, within 1 cm {np.mean(e_mix <= 0.01):.3f}; "
           f"reference FMA-build noise within 1 cm {noise:.3f}")
     assert np.median(e_mix) <= 0.01
-    assert np.mean(e_mix <= 0.01) >= noise - (0.15 if prec == 1 else 0.08)
+    assert np.mean(e_mix <= 0.01) >= _within_floor(noise, 0.15 if prec == 1 else 0.08, n)
 
 
 def test_mixed_on_calm_fleet(built_lib):
@@ -132,7 +144,8 @@ def test_mixed_is_faster(built_lib, prec, factor):
 def test_mixed_tire_11_and_24dof(built_lib, model):
     """The FP32 tire core in the single-track and 24-DOF steppers: on the seeded SUV fleets (10 s)
     median end-position error within 1 cm of FP64 and the fraction within 1 cm no more than 0.08
-    below the reference's FMA-build noise floor; at 65,536 vehicles at least 1.3 times as fast."""
+    below the reference's FMA-build noise floor (to its sampling noise); at 65,536 vehicles at least
+    1.3 times as fast."""
     fleet = pkg_mod("fleet")
     gen = {11: fleet.fleet11, 24: fleet.fleet24}[model]
     n, H = 2048, 10.0
@@ -144,7 +157,7 @@ def test_mixed_tire_11_and_24dof(built_lib, model):
     print(f"{model}-DOF tire core FP32 vs fp64: p50 {np.median(e):.2e} m, within 1 cm {np.mean(e <= 0.01):.3f}; "
           f"reference FMA-build noise within 1 cm {noise:.3f}")
     assert np.median(e) <= 0.01
-    assert np.mean(e <= 0.01) >= noise - 0.08
+    assert np.mean(e <= 0.01) >= _within_floor(noise, 0.08, n)
     g = gen(65536, seed=9, horizon=1.0)
     _, ms64 = _solve(built_lib, g["cls"][0], g["params"], g["tables"], g["states"], 1.0, 0, model=model)
     _, ms32 = _solve(built_lib, g["cls"][0], g["params"], g["tables"], g["states"], 1.0, 2, model=model)
