@@ -39,8 +39,8 @@ W_ALG = {11: 675, 18: 1391, 24: 1941}  # the same count for the three models
 # (sm__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on.sum), and everything the FP64 pipe
 # issued in lanes (sm__inst_executed_pipe_fp64.sum x 32: also compares, min/max and conversions, and
 # the inactive lanes of divergent warps, which occupy the pipe alike)
-FP64_INST_PER_VSTEP_18 = 1107
-FP64_PIPE_PER_VSTEP_18 = 1297
+FP64_INST_PER_VSTEP_18 = 1092
+FP64_PIPE_PER_VSTEP_18 = 1232
 # The mixed-precision forms of the 18-DOF stepper: (precision enum, key, arithmetic)
 MIXED_FORMS = ((1, "mixed", "f32 RHS and tire math; f64 states, X/Y/yaw accumulation, slip and transport velocities"),
                (2, "mixed_tire", "f32 TMeasy tire core; f64 everything else"))

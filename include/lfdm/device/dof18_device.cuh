@@ -350,20 +350,20 @@ struct KView {
     __device__ __forceinline__ float f(int i) const { return fbase[i * stride]; }
 };
 
-// The joint of tmxy_combined's two parabolas: a = (fm / sm)^2 / (df0loc sm) and
-// sstar = sm + (fm - fs) / (a (ss - sm)) (dof18_gpu.cu:262-266), from one reciprocal instead of two
-// divisions: with D = df0loc sm and E = (fm / sm)^2 (ss - sm), R = 1 / (D E) gives 1 / D = E R and
-// (fm - fs) / (a (ss - sm)) = (fm - fs) D / E = (fm - fs) D (D R). Both round within a few ulps of
-// the two quotients; the regime this selects is recorded for the adjoint from the same values.
-__device__ __forceinline__ void tmxy_knee(double fm, double ism, double df0loc, double sm, double ss, double fs,
-                                          double& a, double& sstar) {
+// The transition regime of tmxy_combined (sm <= s <= ss; dof18_gpu.cu:262-276) without a division.
+// With q = fm / sm, D = df0loc sm, dss = ss - sm, E = q^2 dss and H = (fm - fs) D, the first
+// parabola's coefficient is a = q^2 / D and the parabolas' joint is sstar = sm + H / E; as D and E
+// are positive here, sstar <= ss reads H <= dss E and s <= sstar reads (s - sm) E <= H. Returns 0
+// (first parabola), 1 (second parabola) or 2 (the cubic, where the joint lies beyond ss).
+__device__ __forceinline__ int tmxy_joint(double s, double fm, double ism, double df0loc, double sm, double ss,
+                                          double fs, double& q2, double& D, double& E, double& H) {
     const double q = fm * ism;
-    const double q2 = q * q;
-    const double D = df0loc * sm;
-    const double E = q2 * (ss - sm);
-    const double R = 1.0 / (D * E);
-    a = q2 * (E * R);
-    sstar = fma(fm - fs, D * (D * R), sm);
+    q2 = q * q;
+    D = df0loc * sm;
+    E = q2 * (ss - sm);
+    H = (fm - fs) * D;
+    if (H <= (ss - sm) * E) return (s - sm) * E <= H ? 0 : 1;
+    return 2;
 }
 
 // tmxy_combined (dof18_gpu.cu:243-285) given the reciprocals of s, sm and fm (is, ism, ifm; the
@@ -385,22 +385,23 @@ __device__ __forceinline__ void tmxy_frac(double& fn, double& fd, double s, doub
             const double sn = s * ism;
             fd = fma(sn + p, sn, 1.0);
             fn = df0loc;
-        } else {
-            double a, sstar;
-            tmxy_knee(fm, ism, df0loc, sm, ss, fs, a, sstar);
-            double f;
-            if (sstar <= ss) {
-                if (s <= sstar) {
-                    f = fm - a * (s - sm) * (s - sm);
-                } else {
-                    const double b = a * (sstar - sm) / (ss - sstar);
-                    f = fs + b * (ss - s) * (ss - s);
-                }
-            } else {
-                const double sn = (s - sm) / (ss - sm);
-                f = fm - (fm - fs) * sn * sn * (3.0 - 2.0 * sn);
+        } else {  // transition: f = fn s / fd over the denominator of its piece
+            double q2, D, E, H;
+            const int piece = tmxy_joint(s, fm, ism, df0loc, sm, ss, fs, q2, D, E, H);
+            const double ds = s - sm, dss = ss - sm;
+            if (piece == 0) {  // f = fm - a ds^2, a = q^2 / D
+                fn = fma(-q2 * ds, ds, fm * D) * is;
+                fd = D;
+            } else if (piece == 1) {  // f = fs + b (ss - s)^2, b = a (sstar - sm) / (ss - sstar) = q^2 (fm - fs) / G
+                const double G = fma(dss, E, -H);
+                const double r = ss - s;
+                fn = fma(q2 * (fm - fs) * r, r, fs * G) * is;
+                fd = G;
+            } else {  // f = fm - (fm - fs) sn^2 (3 - 2 sn), sn = ds / dss
+                const double d3 = dss * dss * dss;
+                fn = fma(-(fm - fs) * ds * ds, fma(-2.0, ds, 3.0 * dss), fm * d3) * is;
+                fd = d3;
             }
-            fn = f * is;
         }
     } else {
         fn = 0.0;

@@ -203,10 +203,8 @@ __device__ __forceinline__ double tmxy_regime(double s, double df0, double sm, d
     if (!(gt0(s) && gt0(df0loc))) return 0.0;
     if (gt_nn(s, ss)) return 1.0;
     if (gt_nn(sm, s)) return 2.0 + side;
-    double a, sstar;
-    tmxy_knee(fm, ism, df0loc, sm, ss, fs, a, sstar);
-    if (sstar <= ss) return (s <= sstar ? 3.0 : 4.0) + side;
-    return 5.0 + side;
+    double q2, D, E, H;
+    return 3.0 + tmxy_joint(s, fm, ism, df0loc, sm, ss, fs, q2, D, E, H) + side;
 }
 
 template <bool kSteered>
@@ -809,16 +807,17 @@ __device__ __forceinline__ void tmxy_rev(double s, double df0, double sm, double
         sb = fma(snb, ism, sb);
         smb = fma(-s * ism * ism, snb, smb);
     } else {
-        // a and sstar as the forward step computed them, so both take the same branch
-        double a, sstar;
-        tmxy_knee(fm, ism, df0loc, sm, ss, fs, a, sstar);
+        double q2, D, E, H;  // the piece the forward step took, by its comparisons
+        const int piece = tmxy_joint(s, fm, ism, df0loc, sm, ss, fs, q2, D, E, H);
         const double q = fm * ism;
         const double idsm = 1.0 / (df0loc * sm);
+        const double a = q * q * idsm;
         const double ida = 1.0 / (a * (ss - sm));
+        const double sstar = fma((fm - fs), ida, sm);
         double f, ab = 0.0, sstarb = 0.0;
         double b = 0.0, sn3 = 0.0;
-        if (sstar <= ss) {
-            if (s <= sstar) {
+        if (piece != 2) {
+            if (piece == 0) {
                 f = fm - a * (s - sm) * (s - sm);
             } else {
                 b = a * (sstar - sm) / (ss - sstar);
@@ -830,8 +829,8 @@ __device__ __forceinline__ void tmxy_rev(double s, double df0, double sm, double
         }
         const double fb = fosb * is;  // fos = f / s
         sb = fma(-f * is * is, fosb, sb);
-        if (sstar <= ss) {
-            if (s <= sstar) {
+        if (piece != 2) {
+            if (piece == 0) {
                 fmb += fb;
                 ab = fma(-(s - sm) * (s - sm), fb, ab);
                 sb = fma(-2.0 * a * (s - sm), fb, sb);
