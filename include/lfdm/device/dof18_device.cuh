@@ -366,12 +366,33 @@ __device__ __forceinline__ int tmxy_joint(double s, double fm, double ism, doubl
     return 2;
 }
 
+// The force of the transition regime as f = num / den over the denominator of its piece.
+__device__ __forceinline__ void tmxy_transition(double& num, double& den, double s, double df0loc, double sm,
+                                                double ism, double fm, double ss, double fs) {
+    double q2, D, E, H;
+    const int piece = tmxy_joint(s, fm, ism, df0loc, sm, ss, fs, q2, D, E, H);
+    const double ds = s - sm, dss = ss - sm;
+    if (piece == 0) {  // f = fm - a ds^2, a = q^2 / D
+        num = fma(-q2 * ds, ds, fm * D);
+        den = D;
+    } else if (piece == 1) {  // f = fs + b (ss - s)^2, b = a (sstar - sm) / (ss - sstar) = q^2 (fm - fs) / G
+        const double G = fma(dss, E, -H);
+        const double r = ss - s;
+        num = fma(q2 * (fm - fs) * r, r, fs * G);
+        den = G;
+    } else {  // f = fm - (fm - fs) sn^2 (3 - 2 sn), sn = ds / dss
+        const double d3 = dss * dss * dss;
+        num = fma(-(fm - fs) * ds * ds, fma(-2.0, ds, 3.0 * dss), fm * d3);
+        den = d3;
+    }
+}
+
 // tmxy_combined (dof18_gpu.cu:243-285) given the reciprocals of s, sm and fm (is, ism, ifm; the
 // TMeasy tire has them from the rsqrt of the squared norms it takes anyway). Returns the ratio of
-// the combined force to the combined slip, fos = f / s, as a fraction fn / fd: in the adhesion
-// regime, which nearly every step is in, fos = df0 / dn and the caller folds 1/dn into its own
-// division; elsewhere fd = 1 and no division is taken (the full-sliding and transition regimes use
-// is = 1/s).
+// the combined force to the combined slip, fos = f / s, as a fraction fn / fd that the caller folds
+// into its own division: in the adhesion regime, which nearly every step is in, fos = df0 / dn; in
+// the transition regime fd is the denominator of its piece (tmxy_transition); in full sliding
+// fd = 1. No regime divides (is = 1/s).
 __device__ __forceinline__ void tmxy_frac(double& fn, double& fd, double s, double is, double df0, double sm,
                                           double ism, double fm, double ifm, double ss, double fs) {
     fd = 1.0;
@@ -385,23 +406,9 @@ __device__ __forceinline__ void tmxy_frac(double& fn, double& fd, double s, doub
             const double sn = s * ism;
             fd = fma(sn + p, sn, 1.0);
             fn = df0loc;
-        } else {  // transition: f = fn s / fd over the denominator of its piece
-            double q2, D, E, H;
-            const int piece = tmxy_joint(s, fm, ism, df0loc, sm, ss, fs, q2, D, E, H);
-            const double ds = s - sm, dss = ss - sm;
-            if (piece == 0) {  // f = fm - a ds^2, a = q^2 / D
-                fn = fma(-q2 * ds, ds, fm * D) * is;
-                fd = D;
-            } else if (piece == 1) {  // f = fs + b (ss - s)^2, b = a (sstar - sm) / (ss - sstar) = q^2 (fm - fs) / G
-                const double G = fma(dss, E, -H);
-                const double r = ss - s;
-                fn = fma(q2 * (fm - fs) * r, r, fs * G) * is;
-                fd = G;
-            } else {  // f = fm - (fm - fs) sn^2 (3 - 2 sn), sn = ds / dss
-                const double d3 = dss * dss * dss;
-                fn = fma(-(fm - fs) * ds * ds, fma(-2.0, ds, 3.0 * dss), fm * d3) * is;
-                fd = d3;
-            }
+        } else {  // transition: fos = num / (den s)
+            tmxy_transition(fn, fd, s, df0loc, sm, ism, fm, ss, fs);
+            fn *= is;
         }
     } else {
         fn = 0.0;
@@ -440,21 +447,10 @@ __device__ __forceinline__ void tmxy(double& f, double& fos, double s, double df
             double idn = 1.0 / dn;
             f = df0loc * sm * sn * idn;
             fos = df0loc * idn;
-        } else {
-            double q = fm * ism;
-            double a = q * q / (df0loc * sm);
-            double sstar = sm + (fm - fs) / (a * (ss - sm));
-            if (sstar <= ss) {
-                if (s <= sstar) {
-                    f = fm - a * (s - sm) * (s - sm);
-                } else {
-                    double b = a * (sstar - sm) / (ss - sstar);
-                    f = fs + b * (ss - s) * (ss - s);
-                }
-            } else {
-                double sn = (s - sm) / (ss - sm);
-                f = fm - (fm - fs) * sn * sn * (3.0 - 2.0 * sn);
-            }
+        } else {  // the piece and its force as tmxy_frac takes them, with one division
+            double num, den;
+            tmxy_transition(num, den, s, df0loc, sm, ism, fm, ss, fs);
+            f = num / den;
             fos = f / s;
         }
     } else {
