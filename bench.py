@@ -40,7 +40,7 @@ W_ALG = {11: 675, 18: 1391, 24: 1941}  # the same count for the three models
 # issued in lanes (sm__inst_executed_pipe_fp64.sum x 32: also compares, min/max and conversions, and
 # the inactive lanes of divergent warps, which occupy the pipe alike)
 FP64_INST_PER_VSTEP_18 = 1092
-FP64_PIPE_PER_VSTEP_18 = 1232
+FP64_PIPE_PER_VSTEP_18 = 1227
 # The mixed-precision forms of the 18-DOF stepper: (precision enum, key, arithmetic)
 MIXED_FORMS = ((1, "mixed", "f32 RHS and tire math; f64 states, X/Y/yaw accumulation, slip and transport velocities"),
                (2, "mixed_tire", "f32 TMeasy tire core; f64 everything else"))

@@ -130,14 +130,15 @@ __device__ __forceinline__ double map_y_scaled(const MapDev& m, double x, double
     return yl + mbar * (yr - yl);
 }
 
-// sineStep (utils/utils_gpu.cu:78-88)
+// sineStep (utils/utils_gpu.cu:78-88). sin(2 pi u) for u in (0, 1) is taken as sinpi(2 u): the same
+// function, with an exact argument reduction instead of the reduction of the rounded 2 pi u.
 __device__ __forceinline__ double sine_step(double x, double x1, double y1, double x2, double y2) {
     if (x <= x1) return y1;
     if (x >= x2) return y2;
     double dx = x2 - x1;
     double dy = y2 - y1;
     double u = (x - x1) / dx;
-    return y1 + dy * u - (dy / k2Pi) * sin(k2Pi * u);
+    return y1 + dy * u - (dy / k2Pi) * sinpi(2.0 * u);
 }
 
 // sgn (utils/utils_gpu.cuh): -1, 0 or 1 (0 for both zeros)
@@ -153,7 +154,7 @@ __device__ __forceinline__ double sine_step_nn(double x, double x1, double y1, d
     const double dx = x2 - x1;
     const double dy = y2 - y1;
     const double u = (x - x1) / dx;
-    return y1 + dy * u - (dy / k2Pi) * sin(k2Pi * u);
+    return y1 + dy * u - (dy / k2Pi) * sinpi(2.0 * u);
 }
 
 // The structural/dynamic blend weights of one tire, sineStep(a, 1, 1, 1.5, 0) of its longitudinal

@@ -182,7 +182,7 @@ __device__ __forceinline__ void sine_step_w(double x, double& y, double& dy) {
     }
     y = sine_step(x, 1., 1., 1.5, 0.);
     const double u = (x - 1.0) / 0.5;
-    dy = -2.0 + 2.0 * cos(k2Pi * u);
+    dy = -2.0 + 2.0 * cospi(2.0 * u);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -386,7 +386,7 @@ __device__ __forceinline__ void sine_step01(double x, double x1, double x2, doub
         return;
     }
     const double u = (x - x1) / (x2 - x1);
-    dy = (1.0 - cos(k2Pi * u)) / (x2 - x1);
+    dy = (1.0 - cospi(2.0 * u)) / (x2 - x1);
 }
 
 // The arithmetic of tire_rhs_nr / tire_core_nr (dof18_device.cuh) with its tape.
