@@ -570,7 +570,7 @@ int lfdm_create_on_device(int model, unsigned total_num_vehicles, int device, lf
     if (!out) return LFDM_ERR_ARG;
     *out = nullptr;
     if (model != LFDM_MODEL_18 && model != LFDM_MODEL_11 && model != LFDM_MODEL_24) {
-        g_create_error = "model " + std::to_string(model) + " is not available in this build";
+        g_create_error = "model " + std::to_string(model) + " is not one of the library's models (11, 18, 24)";
         return LFDM_ERR_ARG;
     }
     if (total_num_vehicles == 0 || total_num_vehicles > (1u << 30)) {

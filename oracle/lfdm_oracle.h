@@ -2,8 +2,8 @@
  * ORACLE — test infrastructure only. Nothing in the product links, loads or calls this.
  *
  * CPU restatement (plain C, FP64, no FMA contraction) of the reference's batched half-implicit
- * stepper for the 18-, 11- and 24-DOF models with TMeasy and TMeasyNr tires. It is the checker the CUDA path is compared against in tests/, smoke() and bench.py's
- * CPU-baseline leg. It is pinned against the reference's own CPU solvers (oracle/refrun{11,18,24}.cpp,
+ * stepper for the 18-, 11- and 24-DOF models with TMeasy and TMeasyNr tires. The CUDA path is
+ * compared against it in tests/ and smoke(); bench.py's CPU-baseline leg times it. It is pinned against the reference's own CPU solvers (oracle/refrun{11,18,24}.cpp,
  * built by `make ref`) through the golden fixtures in tests/golden/.
  */
 #ifndef LFDM_ORACLE_H

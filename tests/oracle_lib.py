@@ -1,7 +1,7 @@
 """ctypes access to the oracle (oracle/_build/liboracle.so) — test infrastructure only.
 
-The oracle is the CPU restatement of the reference stepper (oracle/lfdm_oracle.c); tests and
-bench.py's CPU-baseline leg use it as the checker. It is built with `make -C oracle oracle`.
+The oracle is the CPU restatement of the reference stepper (oracle/lfdm_oracle.c); tests compare
+the CUDA path against it and bench.py's CPU-baseline leg times it. It is built with `make -C oracle oracle`.
 """
 from __future__ import annotations
 

@@ -112,8 +112,8 @@ def _ours_rate(built_lib, model, f, n, ksim, windows, output_hz):
                                                            (24, 100_000, 1.0, 3, 100.0, 1.5)])
 def test_throughput_vs_reference_gpu_kernel(launcher, built_lib, model, n, ksim, windows, hz, factor):
     """The seeded SUV fleets with outputs every 10 ms, 1 s windows; windows 2 and 3 timed for both
-    (the reference at 16 and 32 threads per block, its best counts). Spec target for the
-    18-DOF model at 300,000 vehicles: at least 2x the reference's GPU solver."""
+    (the reference at 16 and 32 threads per block, its best counts). The 18-DOF model at 300,000
+    vehicles must run at least 2x as fast as the reference's GPU solver."""
     fleet = pkg_mod("fleet")
     gen = {11: fleet.fleet11, 18: fleet.fleet18, 24: fleet.fleet24}[model]
     f = gen(n, seed=20261203, horizon=windows * ksim)
